@@ -1,0 +1,429 @@
+"""Benchmark: AMG-preconditioned CG to 1e-8 relative residual on the 256^3
+27-point lognormal diffusion system (16.7M rows, 449M non-zeros, CSR, FP64
+values, int32 columns), plain FP64 and mixed precision, plus the CSR SpMV
+bandwidth on the same matrix.
+
+One step = one full AMG-PCG solve from x0 = 0 (hierarchy set up once,
+outside the timed region; its setup time is reported separately).  The
+matrix (5.7 GB) is far larger than the 129 MB L2, so no flush is needed
+between steps.  Inputs are seeded synthetic data: conductivity
+k = exp(1.5 N(0,1)) (numpy PCG64, seed 1), b ~ U[-1, 1] (seed 0).
+
+--impl reference times the CPU restatement of lineal's shared-memory path
+(oracle/, the reference itself cannot be built: its thesauros/grex
+dependencies are not vendored) on the host cores, on a bounded sample of the
+same workload, extrapolated to the full size.
+
+Multi-GPU: the solve path has no exchange step on one box; N > 1 runs N
+independent replicas (one system per rank, weak scaling) and reports the
+slowest rank.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "AMG-PCG ms to 1e-8 rel. residual & SpMV HBM GB/s at 256^3: mixed vs plain FP64"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def parity_colours(dims):
+    i, j, k = np.meshgrid(*[np.arange(d, dtype=np.int32) for d in dims], indexing="ij")
+    return ((i % 2) * 4 + (j % 2) * 2 + (k % 2)).ravel().astype(np.int32)
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def make_problem(n_edge, seed_k=1, seed_b=0, sigma=1.5):
+    dims = (n_edge, n_edge, n_edge)
+    n = n_edge ** 3
+    k = np.exp(sigma * np.random.default_rng(seed_k).standard_normal(n))
+    b = np.random.default_rng(seed_b).uniform(-1.0, 1.0, n)
+    return dims, k, b
+
+
+def csr_bytes(n, nnz, val_bytes=8, vec_bytes=8):
+    # values + int32 columns + int64 row offsets + x once + y once
+    return nnz * (val_bytes + 4) + 8 * (n + 1) + vec_bytes * n + vec_bytes * n
+
+
+# ---------------------------------------------------------------------------
+# CPU restatement (reference arm and cpu_baseline)
+# ---------------------------------------------------------------------------
+def cpu_amg_pcg_sample(n_edge_sample, threads):
+    """Oracle AMG-PCG on a smaller grid with the reference's shared-memory
+    semantics (aggregation partitions clamp(n/8, 1, threads), thread-hybrid
+    SOR with one part per thread).  Returns (setup_s, solve_s, iterations,
+    nnz)."""
+    import oracle as lo
+
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    dims, k, b = make_problem(n_edge_sample)
+    a = lo.gen_27pt(dims, k)
+    t0 = time.perf_counter()
+    amg = lo.Amg(a, min_coarsen_size=2000, partition_size=8, max_partitions=threads,
+                 smoother_parts=threads)
+    t1 = time.perf_counter()
+    x, it, hist = lo.pcg(a, b, precon=lo.PRECON_AMG, amg=amg, rtol=1e-8, maxit=500)
+    t2 = time.perf_counter()
+    return t1 - t0, t2 - t1, it, a.nnz
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        if rank != 0:
+            dist.barrier()
+            dist.destroy_process_group()
+            return
+    import oracle as lo
+
+    lo.build()
+    threads = os.cpu_count() or 1
+    full_nnz = (3 * args.grid - 2) ** 3
+    sample_edge = args.cpu_sample_edge
+    vals = []
+    iters_full = args.reference_iterations
+    for step in range(args.warmup + args.steps):
+        setup_s, solve_s, it, nnz = cpu_amg_pcg_sample(sample_edge, threads)
+        per_iter = solve_s / max(it, 1)
+        est_ms = per_iter * (full_nnz / nnz) * (iters_full or it) * 1e3
+        if step >= args.warmup:
+            vals.append(est_ms)
+        log(f"[reference] sample {sample_edge}^3: setup {setup_s:.2f}s solve {solve_s:.2f}s "
+            f"{it} it -> {est_ms:.0f} ms at {args.grid}^3")
+    value = float(np.mean(vals))
+    sample = (f"oracle AMG-PCG on {sample_edge}^3 27-pt (same generator), {threads} threads; "
+              f"ms/iteration scaled by nnz to {args.grid}^3 and multiplied by the "
+              f"{iters_full or it} iterations of the full-size solve")
+    out = {
+        "metric": METRIC, "value": value, "unit": "ms", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": f"{args.grid}^3 27-point lognormal(sigma=1.5) CSR AMG-PCG to 1e-8",
+                   "parallelism": f"replicas x{world}"},
+        "cpu_baseline": {"value": value, "unit": "ms", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# GB300 arm
+# ---------------------------------------------------------------------------
+def run_gb300(args):
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import lineal_gb300 as g
+
+    g.build.build()
+    stream = torch.cuda.current_stream()
+    peak, peak_kind = measured_peaks()
+
+    dims, k, b_host = make_problem(args.grid)
+    n = int(np.prod(dims))
+    t0 = time.perf_counter()
+    a = g.gen_27pt(dims, k)
+    nnz = a.non_zero_num()
+    colours = parity_colours(dims)
+    col = g.Colouring.from_array(a, colours, 8)
+    torch.cuda.synchronize()
+    log(f"[gb300] generated {dims} nnz={nnz} in {time.perf_counter() - t0:.2f}s")
+
+    wright = g.HierarchyWright(min_coarsen_size=2000, partition_size=args.partition_size)
+    t0 = time.perf_counter()
+    h64 = wright.instantiate(a, finest_colouring=col)
+    torch.cuda.synchronize()
+    setup64 = time.perf_counter() - t0
+    rows, nnzs = h64.sizes()
+    log(f"[gb300] FP64 hierarchy {rows} in {setup64:.2f}s")
+
+    b = torch.as_tensor(b_host, device="cuda")
+
+    def solve(h):
+        return g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=1e-8, maxit=500)
+
+    # ---- plain FP64: warm-up then K timed solves --------------------------
+    for _ in range(args.warmup):
+        res = solve(h64)
+    iters64 = res.iterations
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    launches0 = g.kernel_launches()
+    e0.record(stream)
+    for _ in range(args.steps):
+        res = solve(h64)
+    e1.record(stream)
+    e1.synchronize()
+    launches = g.kernel_launches() - launches0
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms64 = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms64], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms64 = float(t.item())
+    x = res.x
+    r, rn = g.residual(a, b, x)
+    rel64 = float(np.sqrt(rn)) / float(torch.linalg.norm(b).item())
+    log(f"[gb300] FP64 AMG-PCG {ms64:.1f} ms, {res.iterations} it, rel {rel64:.2e}")
+
+    # ---- mixed precision: float cycle under the FP64 CG ---------------------
+    wright32 = g.HierarchyWright(min_coarsen_size=2000, partition_size=args.partition_size,
+                                 cycle_f32=True)
+    t0 = time.perf_counter()
+    h32 = wright32.instantiate(a, finest_colouring=col)
+    torch.cuda.synchronize()
+    setup32 = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        res32 = solve(h32)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        res32 = solve(h32)
+    e1.record(stream)
+    e1.synchronize()
+    ms32 = e0.elapsed_time(e1) / args.steps
+    _, rn32 = g.residual(a, b, res32.x)
+    rel32 = float(np.sqrt(rn32)) / float(torch.linalg.norm(b).item())
+    err = float(torch.linalg.norm(res32.x - x).item() / torch.linalg.norm(x).item())
+    log(f"[gb300] mixed AMG-PCG {ms32:.1f} ms, {res32.iterations} it, rel {rel32:.2e}")
+
+    # ---- SpMV bandwidth (FP64 values, and float values) ---------------------
+    xs = torch.randn(n, dtype=torch.float64, device="cuda")
+    ys = torch.empty_like(xs)
+    spmv_reps = 20
+
+    def time_spmv(m, x_, y_, fn):
+        for _ in range(3):
+            fn(m, x_, y_)
+        torch.cuda.synchronize()
+        s0 = torch.cuda.Event(enable_timing=True)
+        s1 = torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        for _ in range(spmv_reps):
+            fn(m, x_, y_)
+        s1.record(stream)
+        s1.synchronize()
+        return s0.elapsed_time(s1) / spmv_reps
+
+    t_spmv64 = time_spmv(a, xs, ys, lambda m, x_, y_: g.spmv(m, x_, out=y_))
+    bytes64 = csr_bytes(n, nnz, 8, 8)
+    gbs64 = bytes64 / (t_spmv64 * 1e-3) / 1e9
+    del h64
+    a32 = g.gen_27pt(dims, k, storage=g.F32)
+    xs32 = xs.float()
+    ys32 = torch.empty_like(xs32)
+    t_spmv32 = time_spmv(a32, xs32, ys32, lambda m, x_, y_: g.spmv_f32(m, x_, out=y_))
+    bytes32 = csr_bytes(n, nnz, 4, 4)
+    gbs32 = bytes32 / (t_spmv32 * 1e-3) / 1e9
+    del a32
+    log(f"[gb300] SpMV fp64 {t_spmv64:.3f} ms {gbs64:.0f} GB/s; fp32 {t_spmv32:.3f} ms "
+        f"{gbs32:.0f} GB/s")
+
+    # ---- end to end through the C ABI with host buffers -----------------------
+    e2e = None
+    if args.e2e:
+        rowptr, colidx, val = a.download()
+        h_rowptr = torch.from_numpy(rowptr).pin_memory()
+        h_col = torch.from_numpy(colidx).pin_memory()
+        h_val = torch.from_numpy(val).pin_memory()
+        h_b = torch.from_numpy(b_host).pin_memory()
+        h_col_colours = torch.from_numpy(colours).pin_memory()
+        del h32
+        e2e_ms = []
+        for step in range(args.e2e_steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            d_rowptr = h_rowptr.to("cuda", non_blocking=True)
+            d_col = h_col.to("cuda", non_blocking=True)
+            d_val = h_val.to("cuda", non_blocking=True)
+            d_b = h_b.to("cuda", non_blocking=True)
+            d_colours = h_col_colours.to("cuda", non_blocking=True)
+            m = g.CsrMatrix.from_device(d_rowptr, d_col, d_val, symmetric=True)
+            del d_rowptr, d_col, d_val
+            c = g.Colouring.from_array(m, d_colours, 8)
+            hh = g.HierarchyWright(min_coarsen_size=2000, partition_size=args.partition_size,
+                                   cycle_f32=True).instantiate(m, finest_colouring=c)
+            rr = g.pcg(m, d_b, precon=g.PRECON_AMG, amg=hh, rtol=1e-8, maxit=500)
+            xh = rr.x.cpu()
+            torch.cuda.synchronize()
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+            del m, c, hh, rr
+        h2d = (rowptr.nbytes + colidx.nbytes + val.nbytes + b_host.nbytes + colours.nbytes)
+        e2e = {"value": float(np.median(e2e_ms)), "unit": "ms", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(n * 8),
+               "what": "host CSR + b (pinned) -> device, AMG setup (mixed), PCG, x -> host"}
+        log(f"[gb300] e2e {e2e['value']:.0f} ms")
+
+    # ---- CPU baseline (bounded sample) -----------------------------------------
+    cpu = None
+    if rank == 0 and args.cpu_baseline:
+        threads = os.cpu_count() or 1
+        setup_s, solve_s, it, snnz = cpu_amg_pcg_sample(args.cpu_sample_edge, threads)
+        full_nnz = nnz
+        est = solve_s / max(it, 1) * (full_nnz / snnz) * iters64 * 1e3
+        cpu = {"value": est, "unit": "ms", "cores": threads, "kind": "port",
+               "sample": f"oracle AMG-PCG on {args.cpu_sample_edge}^3 27-pt, {threads} threads, "
+                         f"{it} iterations in {solve_s:.2f}s (setup {setup_s:.2f}s); ms/iteration "
+                         f"scaled by nnz to {args.grid}^3 times the {iters64} GPU iterations"}
+
+    out = {
+        "metric": METRIC, "value": ms64, "unit": "ms", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms64, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {
+            "workload": f"{args.grid}^3 27-point lognormal(sigma=1.5) CSR, AMG-PCG to 1e-8",
+            "rows": n, "nnz": nnz, "parallelism": f"replicas x{world}",
+            "l2": "inputs (5.7 GB matrix) larger than L2; no flush",
+            "amg": {"levels": rows, "level_nnz": nnzs, "partition_size": args.partition_size,
+                    "finest_colouring": "grid parity, 8 colours"},
+        },
+        "iterations": iters64, "final_rel_residual": rel64, "setup_ms": setup64 * 1e3,
+        "mixed": {"ms": ms32, "iterations": res32.iterations, "rel_residual_fp64": rel32,
+                  "setup_ms": setup32 * 1e3, "speedup_vs_fp64": ms64 / ms32,
+                  "rel_error_vs_fp64_solution": err},
+        "spmv": {"fp64_ms": t_spmv64, "fp64_gbs": gbs64, "fp64_frac": gbs64 / peak,
+                 "fp32_ms": t_spmv32, "fp32_gbs": gbs32, "fp32_frac": gbs32 / peak,
+                 "bytes_fp64": bytes64, "bytes_fp32": bytes32},
+        "roofline": {"bound": "hbm", "kernel": "k_csr_spmv<double,double>",
+                     "achieved": gbs64, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                     "frac": gbs64 / peak, "traffic": args.spmv_traffic},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--grid", type=int, default=256)
+    ap.add_argument("--partition-size", type=int, default=4096)
+    ap.add_argument("--cpu-sample-edge", type=int, default=64)
+    ap.add_argument("--reference-iterations", type=int, default=0,
+                    help="iterations of the full-size solve used to extrapolate the CPU sample")
+    ap.add_argument("--no-e2e", dest="e2e", action="store_false")
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--spmv-traffic", type=float, default=None,
+                    help="DRAM bytes per SpMV launch from an ncu capture")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be at least 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,302 @@
+/*
+ * lineal_gb300 C ABI: GB300 (sm_103a) implementation of lineal's solve path.
+ *
+ * lineal (KurtBoehm/lineal) is a header-only C++23 library whose operator
+ * interface is a set of concepts (include/lineal/base/concept/range.hpp:17-40,
+ * include/lineal/base/concept/solver.hpp:16-37).  This ABI is the device-side
+ * boundary below the C++ wrappers in include/lineal_gb300/lineal.hpp, which
+ * restate those concepts; every entry point names the reference interface it
+ * replaces.
+ *
+ * Conventions
+ *  - Every call returns lgx_status; lgx_last_error() holds a message for the
+ *    calling thread.  No call throws and none traps on the device: breakdown
+ *    and non-finite values are reported as statuses.
+ *  - Pointers named d_* are device pointers; h_* are host pointers.  Vectors
+ *    are plain arrays of double (or float where the name says f32).
+ *  - Every call that launches work takes a cudaStream_t (0 = legacy default)
+ *    and only enqueues on that stream, except where a host result is
+ *    returned (documented per call).
+ *  - Matrices are opaque handles owning device memory.  CSR input is
+ *    row-major with sorted column indices per row and a stored diagonal
+ *    (the invariants of include/lineal/tensor/dynamic/csr/shared.hpp:258-262).
+ */
+#ifndef LINEAL_GB300_H
+#define LINEAL_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *lgx_stream; /* == cudaStream_t */
+
+typedef enum {
+  LGX_OK = 0,
+  LGX_ERR_INVALID = 1,     /* bad argument, size or handle */
+  LGX_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+  LGX_ERR_NOMEM = 3,       /* device allocation failed */
+  LGX_ERR_BREAKDOWN = 4,   /* Krylov breakdown (zero denominator) */
+  LGX_ERR_NONFINITE = 5,   /* NaN/Inf detected in a reduction */
+  LGX_ERR_NOT_SPD = 6,     /* coarse Cholesky met a non-positive pivot */
+  LGX_ERR_UNSUPPORTED = 7, /* operation not available for this matrix kind */
+  LGX_ERR_NOT_CONVERGED = 8
+} lgx_status;
+
+const char *lgx_status_string(lgx_status s);
+/* Message describing the last failure on the calling host thread. */
+const char *lgx_last_error(void);
+/* Library version string. */
+const char *lgx_version(void);
+/* Number of kernels this library has launched since it was loaded (every
+ * launch site counts; used to report launches inside a timed region). */
+uint64_t lgx_kernel_launches(void);
+
+/* ------------------------------------------------------------------------
+ * Matrices.  One handle type covers every matrix kind of the reference that
+ * the solve path uses:
+ *   LGX_MATRIX_CSR             CsrMatrix (tensor/dynamic/csr/shared.hpp:1114-1116)
+ *   LGX_MATRIX_STENCIL_LOOKUP  AdjacentStencilMatrix<StationaryDiffusionLookupValuator>
+ *   LGX_MATRIX_STENCIL_VALUE   AdjacentStencilMatrix<StationaryDiffusionValueValuator>
+ *                              (tensor/dynamic/stencil/matrix/shared.hpp:34-358)
+ * ---------------------------------------------------------------------- */
+typedef struct lgx_matrix lgx_matrix;
+
+typedef enum {
+  LGX_MATRIX_CSR = 0,
+  LGX_MATRIX_STENCIL_LOOKUP = 1,
+  LGX_MATRIX_STENCIL_VALUE = 2
+} lgx_matrix_kind;
+
+typedef enum { LGX_F64 = 0, LGX_F32 = 1 } lgx_dtype;
+
+/* Builds a CSR matrix from device arrays (copied).  values are stored in
+ * `storage` precision (LGX_F32 rounds each value to float).  Replaces
+ * CsrMatrix's RowWiseBuilder / MultithreadBuilder (csr/shared.hpp:424-903). */
+lgx_status lgx_csr_create(int64_t n, int64_t nnz, const int64_t *d_rowptr, const int32_t *d_col,
+                          const double *d_val, int symmetric, lgx_dtype storage, lgx_stream stream,
+                          lgx_matrix **out);
+/* Same from host arrays (uploaded with synchronous copies). */
+lgx_status lgx_csr_create_host(int64_t n, int64_t nnz, const int64_t *h_rowptr,
+                               const int32_t *h_col, const double *h_val, int symmetric,
+                               lgx_dtype storage, lgx_matrix **out);
+/* Copies the CSR arrays back to the host (sizes from lgx_matrix_info).
+ * Synchronises `stream`. */
+lgx_status lgx_csr_download(const lgx_matrix *a, int64_t *h_rowptr, int32_t *h_col,
+                            double *h_val, lgx_stream stream);
+
+/* Matrix-free 7-point diffusion stencil with Dirichlet values on both faces
+ * of axis 0 and zero-flux elsewhere (valuator semantics of
+ * stencil/valuator/stationary-diffusion-lookup.hpp:28-201 and
+ * stationary-diffusion-value.hpp:31-204).  dims are cell counts (axis 2
+ * fastest), q the axis quotients of BoxInfo (discretization/box-equidistant
+ * .hpp:67-79).  Lookup: d_mat holds one material index (< 4) per cell and
+ * coeffs the material conductivities.  Value: d_k holds one conductivity per
+ * cell.  zero_to_one selects ZeroToOneTag (a zero diagonal becomes 1). */
+lgx_status lgx_stencil_create_lookup(const int64_t dims[3], const double q[3],
+                                     const double coeffs[4], const uint8_t *d_mat,
+                                     double sol_start, double sol_end, int zero_to_one,
+                                     lgx_stream stream, lgx_matrix **out);
+lgx_status lgx_stencil_create_value(const int64_t dims[3], const double q[3], const double *d_k,
+                                    double sol_start, double sol_end, int zero_to_one,
+                                    lgx_stream stream, lgx_matrix **out);
+
+lgx_status lgx_matrix_destroy(lgx_matrix *a);
+/* kind, rows, stored non-zeros (stencils: the non-zeros of the assembled
+ * matrix), symmetric flag (IsSymmetric, base/type-safe.hpp:11). */
+lgx_status lgx_matrix_info(const lgx_matrix *a, int *kind, int64_t *n, int64_t *nnz,
+                           int *symmetric);
+
+/* y = A x (MatrixVectorProductExpr, component-wise/matrix-vector-product.hpp:
+ * 34-140).  CSR rows accumulate fma(a_ij, x_j, sum) in ascending column order,
+ * stencil rows in the scalar unordered order of stencil/matrix/algorithm.hpp
+ * :178-225, so results equal the reference's scalar path bit for bit. */
+lgx_status lgx_spmv(const lgx_matrix *a, const double *d_x, double *d_y, lgx_stream stream);
+/* y = A x with float vectors (float-stored CSR; products accumulated in
+ * float). */
+lgx_status lgx_spmv_f32(const lgx_matrix *a, const float *d_x, float *d_y, lgx_stream stream);
+/* r = b - A x, optionally d_norm2sq[0] = ||r||^2 (assign_expr +
+ * euclidean_squared, conjugate-gradients/solver.hpp:59-61). */
+lgx_status lgx_residual(const lgx_matrix *a, const double *d_b, const double *d_x, double *d_r,
+                        double *d_norm2sq, lgx_stream stream);
+/* diagonal of A (AdjacentStencilMatrix::diagonal_at, stencil/matrix/shared.hpp
+ * :242-244; CsrMatrix row diagonal()). */
+lgx_status lgx_diagonal(const lgx_matrix *a, double *d_diag, lgx_stream stream);
+/* Right-hand side of a stencil system (AdjacentStencilVector,
+ * stencil/vector/shared.hpp:181-205). */
+lgx_status lgx_stencil_rhs(const lgx_matrix *a, double *d_b, lgx_stream stream);
+/* Assembles a stencil matrix as CSR (csr_from_adjacent_stencil,
+ * csr/create-from.hpp:37-246); zero off-diagonals are dropped.  With
+ * zero_to_one == 0, rows with a zero diagonal are removed and d_compress_map
+ * (cells entries, may be NULL) receives the compressed row or -1. */
+lgx_status lgx_stencil_to_csr(const lgx_matrix *a, int64_t *d_compress_map, lgx_stream stream,
+                              lgx_matrix **out);
+
+/* Synthetic operators (no reference counterpart; the reference stencil is
+ * 7-point).  d_k holds one conductivity per cell on a unit-spaced grid.
+ * Off-diagonal to a neighbour at offset o: -hm(k_i, k_j) * w with w = 1
+ * (face), 1/2 (edge), 1/4 (corner) and hm the harmonic mean of
+ * math/harmonic-mean.hpp:13-25; the diagonal adds 2 k_i on both faces of
+ * axis 0 and then the off-diagonal weights in ascending column order; a zero
+ * diagonal becomes 1.  The 7-point variant keeps the faces only. */
+lgx_status lgx_gen_27pt(const int64_t dims[3], const double *d_k, lgx_dtype storage,
+                        lgx_stream stream, lgx_matrix **out);
+lgx_status lgx_gen_7pt(const int64_t dims[3], const double *d_k, lgx_dtype storage,
+                       lgx_stream stream, lgx_matrix **out);
+
+/* ------------------------------------------------------------------------
+ * Vector reductions and updates (component-wise/sink/accumulator.hpp:151-218,
+ * vector-expression.hpp:67-92).  Reductions are deterministic: fixed block
+ * partition, fixed-order second stage.  Results land in device memory.
+ * ---------------------------------------------------------------------- */
+lgx_status lgx_dot(int64_t n, const double *d_a, const double *d_b, double *d_out,
+                   lgx_stream stream);
+lgx_status lgx_norm2sq(int64_t n, const double *d_a, double *d_out, lgx_stream stream);
+lgx_status lgx_max_norm(int64_t n, const double *d_a, double *d_out, lgx_stream stream);
+/* y = y + alpha * x */
+lgx_status lgx_axpy(int64_t n, double alpha, const double *d_x, double *d_y, lgx_stream stream);
+
+/* ------------------------------------------------------------------------
+ * Smoothers (linear-solver/iterative-stationary/).
+ * ---------------------------------------------------------------------- */
+/* One Jacobi sweep (jacobi/sweep.hpp:66-87); d_x_in == NULL means zero. */
+lgx_status lgx_jacobi_sweep(const lgx_matrix *a, double relax, const double *d_x_in,
+                            double *d_x_out, const double *d_b, lgx_stream stream);
+
+/* A colouring of the matrix graph.  The GPU replaces the reference's
+ * thread-block-hybrid SOR (gauss-seidel-variant/sweep.hpp:134-200) by a
+ * multicolour sweep: colours are visited in ascending order (forward) or
+ * descending order (backward); a row reads the values of already visited
+ * colours from the output and all others from the input.  The result equals
+ * the reference SOR applied in the order "rows sorted by (colour, index)". */
+typedef struct lgx_colouring lgx_colouring;
+/* Jones-Plassmann colouring with splitmix64 priorities (deterministic). */
+lgx_status lgx_colouring_create_jp(const lgx_matrix *a, uint64_t seed, lgx_stream stream,
+                                   lgx_colouring **out);
+/* User colouring (device array, one colour in [0, ncolours) per row; e.g.
+ * the parity colouring of a structured grid).  Validated on the device. */
+lgx_status lgx_colouring_create(const lgx_matrix *a, const int32_t *d_colour, int32_t ncolours,
+                                lgx_stream stream, lgx_colouring **out);
+lgx_status lgx_colouring_destroy(lgx_colouring *c);
+/* Copies the colour of every row to d_colour; *ncolours receives the count.
+ * Synchronises `stream`. */
+lgx_status lgx_colouring_export(const lgx_colouring *c, int32_t *d_colour, int32_t *ncolours,
+                                lgx_stream stream);
+
+/* One multicolour SOR sweep (SorSolver/SorBroom, gauss-seidel-variant/
+ * solver.hpp:22-41, regular or ultra variant).  d_x_in == NULL means zero;
+ * d_x_in may equal d_x_out (in situ). */
+lgx_status lgx_sor_sweep(const lgx_matrix *a, const lgx_colouring *c, double relax, int forward,
+                         int ultra, const double *d_x_in, double *d_x_out, const double *d_b,
+                         lgx_stream stream);
+
+/* ------------------------------------------------------------------------
+ * Aggregation AMG (linear-solver/multigrid/).
+ * ---------------------------------------------------------------------- */
+typedef struct {
+  int32_t min_aggregate_size;  /* AggregationParams (aggregation/params.hpp:13-20) */
+  int32_t max_aggregate_size;
+  int64_t partition_size;      /* vertices per sequential aggregation partition */
+  int64_t max_partitions;      /* clamp on the partition count */
+  double strong_threshold;     /* DuneDependencyCriterion (dependency/criterion.hpp:103-118) */
+  double aggressive_threshold;
+  int64_t max_level_num;       /* HierarchyWrightParams (hierarchy/wright.hpp:46-55) */
+  int64_t min_coarsen_size;
+  double min_coarsen_factor;
+  int coarse_f32;              /* coarse matrices stored as float, cycle arithmetic in
+                                  double (the reference tests' CsrMatrix<f32> levels) */
+  int cycle_f32;               /* precision form: every level stored as float and the
+                                  whole cycle (smoothers, residuals, transfers) computed
+                                  in float; the coarsest solve stays FP64 */
+  double relax;                /* MultiGridSolver relax: correction scaled by 1/relax */
+  double smoother_relax;       /* SOR relax */
+  int smoother_ultra;          /* SorVariant::ultra */
+  uint64_t colour_seed;        /* JP colouring seed of the coarse levels */
+} lgx_amg_params;
+
+void lgx_amg_default_params(lgx_amg_params *p);
+
+typedef struct lgx_amg lgx_amg;
+/* HierarchyWrightInstance::create (hierarchy/wright.hpp:146-309): strength
+ * (DuneDependencyCriterion), greedy aggregation per partition
+ * (IndependentAggregationSink + BaseAggregator), Galerkin coarse matrices
+ * (coarsen_matrix), multicolour SOR smoothers and a dense FP64 coarsest
+ * solver.  finest_colouring may be NULL (JP colouring is computed).  The
+ * finest matrix must stay alive while the hierarchy is used.  Synchronises
+ * `stream` (level sizes decide the loop). */
+lgx_status lgx_amg_setup(const lgx_matrix *a, const lgx_amg_params *p,
+                         const lgx_colouring *finest_colouring, lgx_stream stream,
+                         lgx_amg **out);
+lgx_status lgx_amg_destroy(lgx_amg *h);
+/* Number of levels, and per level (up to max_levels entries) rows and
+ * stored non-zeros. */
+lgx_status lgx_amg_info(const lgx_amg *h, int64_t *nlevels, int64_t *rows, int64_t *nnz,
+                        int64_t max_levels);
+/* Level matrix (natural ordering) and fine->coarse aggregate map of `level`
+ * to host arrays (NULL pointers skip an array).  Synchronises `stream`. */
+lgx_status lgx_amg_level_download(const lgx_amg *h, int64_t level, int64_t *h_rowptr,
+                                  int32_t *h_col, double *h_val, uint32_t *h_agg,
+                                  lgx_stream stream);
+/* One V-cycle from a zero initial guess: x = M^-1 b (MultiGridSolver::
+ * Instance::apply, multigrid/solver.hpp:41-176, REGULAR cycle, 1 iteration). */
+lgx_status lgx_amg_vcycle(lgx_amg *h, const double *d_b, double *d_x, lgx_stream stream);
+
+/* The individual setup steps, for parity checks.
+ * Strength of connection (dependency/criterion.hpp:35-78): per stored entry
+ * depends/influences bytes, per row the isolated byte. */
+lgx_status lgx_amg_strength(const lgx_matrix *a, double theta, uint8_t *d_depends,
+                            uint8_t *d_influences, uint8_t *d_isolated, lgx_stream stream);
+/* Greedy aggregation in nparts contiguous partitions (aggregation/base.hpp:
+ * 532-677, independent.hpp:47-216) followed by the aggregate-map merge
+ * (aggregate-map/multithread.hpp:107-143).  d_agg receives global aggregate
+ * ids, 0xFFFFFFFE for isolated vertices.  *ncoarse is written to host memory
+ * (synchronises `stream`). */
+lgx_status lgx_amg_aggregate(const lgx_matrix *a, const uint8_t *d_depends,
+                             const uint8_t *d_influences, const uint8_t *d_isolated,
+                             int32_t min_size, int32_t max_size, int64_t nparts, int aggressive,
+                             uint32_t *d_agg, int64_t *ncoarse, lgx_stream stream);
+
+/* ------------------------------------------------------------------------
+ * Krylov solvers (linear-solver/conjugate-gradients/solver.hpp:24-225,
+ * linear-solver/bicgstab/solver.hpp:25-263) driven as in run_iterative_solver
+ * (linear-solver/runner.hpp:17-84): iterate until ||r|| <= rtol * ||r0|| or
+ * maxit iterations.  The true residual is recomputed when iteration > 0 and
+ * iteration % rere_period == 0 (the rere_controller of
+ * test/aux/iterative.hpp:97-99).  Scalars stay on the device; the host
+ * reads ||r||^2 once per iteration to decide termination.
+ * ---------------------------------------------------------------------- */
+typedef enum {
+  LGX_PRECON_NONE = 0,
+  LGX_PRECON_JACOBI = 1, /* one Jacobi sweep from zero */
+  LGX_PRECON_SSOR = 2,   /* one multicolour SSOR sweep pair from zero */
+  LGX_PRECON_AMG = 3     /* one V-cycle */
+} lgx_precon_kind;
+
+typedef struct {
+  int precon;                   /* lgx_precon_kind */
+  double relax;                 /* Jacobi / SSOR relax */
+  int ultra;                    /* SSOR variant */
+  const lgx_colouring *colouring; /* SSOR colouring (NULL: computed) */
+  lgx_amg *amg;                 /* LGX_PRECON_AMG */
+  double rtol;
+  int64_t maxit;
+  int64_t rere_period;          /* 0 disables true-residual recomputation */
+} lgx_solve_params;
+
+void lgx_solve_default_params(lgx_solve_params *p);
+
+/* Solve A x = b; x holds the initial guess on entry.  *iterations and
+ * *final_rel_residual are host outputs; h_history (optional, maxit + 1
+ * entries) receives ||r|| after each iteration.  Synchronises `stream`. */
+lgx_status lgx_pcg(const lgx_matrix *a, const double *d_b, double *d_x,
+                   const lgx_solve_params *p, lgx_stream stream, int64_t *iterations,
+                   double *final_rel_residual, double *h_history);
+lgx_status lgx_pbicgstab(const lgx_matrix *a, const double *d_b, double *d_x,
+                         const lgx_solve_params *p, lgx_stream stream, int64_t *iterations,
+                         double *final_rel_residual, double *h_history);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,617 @@
+"""Python front end of lineal_gb300 (ctypes over the C ABI in include/lineal_gb300.h).
+
+The names follow lineal's C++ API (KurtBoehm/lineal): ``CsrMatrix`` and the
+stencil matrices (``AdjacentStencilMatrix`` with lookup/value valuators),
+``ConjugateGradientsSolver`` / ``BiCgStabSolver`` (linear-solver/
+conjugate-gradients/solver.hpp, linear-solver/bicgstab/solver.hpp),
+``JacobiSolver`` / ``SorSolver`` / ``SsorSolver`` (linear-solver/
+iterative-stationary/) and ``MultiGridSolver`` over a ``HierarchyWright``
+(linear-solver/multigrid/).  Vectors are CUDA tensors from PyTorch, which is
+used only for device memory and streams; every computation runs in the
+library's own sm_103a kernels.
+
+There is no CPU fallback: importing this module without the compiled library
+raises ``LinealLibraryMissing``.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import build as _build
+
+__all__ = [
+    "LinealError", "LinealLibraryMissing", "lib", "CsrMatrix", "StencilMatrix", "Colouring",
+    "HierarchyWright", "Hierarchy", "pcg", "pbicgstab", "spmv", "residual", "jacobi_sweep",
+    "sor_sweep", "gen_27pt", "gen_7pt", "amg_strength", "amg_aggregate", "dot", "norm2sq",
+    "max_norm", "PRECON_NONE", "PRECON_JACOBI", "PRECON_SSOR", "PRECON_AMG",
+]
+
+PRECON_NONE, PRECON_JACOBI, PRECON_SSOR, PRECON_AMG = 0, 1, 2, 3
+KIND_CSR, KIND_STENCIL_LOOKUP, KIND_STENCIL_VALUE = 0, 1, 2
+F64, F32 = 0, 1
+ISOLATED = 0xFFFFFFFE
+
+
+class LinealError(RuntimeError):
+    """A lineal_gb300 call returned a non-OK status."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"lineal_gb300 status {status}: {message}")
+        self.status = status
+
+
+class LinealLibraryMissing(ImportError):
+    pass
+
+
+_lib = None
+
+
+class _AmgParams(C.Structure):
+    _fields_ = [
+        ("min_aggregate_size", C.c_int32),
+        ("max_aggregate_size", C.c_int32),
+        ("partition_size", C.c_int64),
+        ("max_partitions", C.c_int64),
+        ("strong_threshold", C.c_double),
+        ("aggressive_threshold", C.c_double),
+        ("max_level_num", C.c_int64),
+        ("min_coarsen_size", C.c_int64),
+        ("min_coarsen_factor", C.c_double),
+        ("coarse_f32", C.c_int),
+        ("cycle_f32", C.c_int),
+        ("relax", C.c_double),
+        ("smoother_relax", C.c_double),
+        ("smoother_ultra", C.c_int),
+        ("colour_seed", C.c_uint64),
+    ]
+
+
+class _SolveParams(C.Structure):
+    _fields_ = [
+        ("precon", C.c_int),
+        ("relax", C.c_double),
+        ("ultra", C.c_int),
+        ("colouring", C.c_void_p),
+        ("amg", C.c_void_p),
+        ("rtol", C.c_double),
+        ("maxit", C.c_int64),
+        ("rere_period", C.c_int64),
+    ]
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def lib():
+    """Loads liblineal_gb300.so (building it first when sources are newer)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        raise LinealLibraryMissing(
+            f"{path} is missing: run lineal_gb300.build.build() (nvcc, sm_103a) first")
+    L = C.CDLL(path)
+    _signatures(L)
+    _lib = L
+    return L
+
+
+def _signatures(L):
+    V, P, I64, I32, D = C.c_void_p, C.POINTER, C.c_int64, C.c_int32, C.c_double
+    L.lgx_status_string.restype = C.c_char_p
+    L.lgx_status_string.argtypes = [C.c_int]
+    L.lgx_last_error.restype = C.c_char_p
+    L.lgx_version.restype = C.c_char_p
+    L.lgx_kernel_launches.restype = C.c_uint64
+    L.lgx_kernel_launches.argtypes = []
+    sigs = {
+        "lgx_csr_create": [I64, I64, V, V, V, C.c_int, C.c_int, V, P(V)],
+        "lgx_csr_create_host": [I64, I64, V, V, V, C.c_int, C.c_int, P(V)],
+        "lgx_csr_download": [V, V, V, V, V],
+        "lgx_stencil_create_lookup": [V, V, V, V, D, D, C.c_int, V, P(V)],
+        "lgx_stencil_create_value": [V, V, V, D, D, C.c_int, V, P(V)],
+        "lgx_matrix_destroy": [V],
+        "lgx_matrix_info": [V, P(C.c_int), P(I64), P(I64), P(C.c_int)],
+        "lgx_spmv": [V, V, V, V],
+        "lgx_spmv_f32": [V, V, V, V],
+        "lgx_residual": [V, V, V, V, V, V],
+        "lgx_diagonal": [V, V, V],
+        "lgx_stencil_rhs": [V, V, V],
+        "lgx_stencil_to_csr": [V, V, V, P(V)],
+        "lgx_gen_27pt": [V, V, C.c_int, V, P(V)],
+        "lgx_gen_7pt": [V, V, C.c_int, V, P(V)],
+        "lgx_dot": [I64, V, V, V, V],
+        "lgx_norm2sq": [I64, V, V, V],
+        "lgx_max_norm": [I64, V, V, V],
+        "lgx_axpy": [I64, D, V, V, V],
+        "lgx_jacobi_sweep": [V, D, V, V, V, V],
+        "lgx_colouring_create_jp": [V, C.c_uint64, V, P(V)],
+        "lgx_colouring_create": [V, V, I32, V, P(V)],
+        "lgx_colouring_destroy": [V],
+        "lgx_colouring_export": [V, V, P(I32), V],
+        "lgx_sor_sweep": [V, V, D, C.c_int, C.c_int, V, V, V, V],
+        "lgx_amg_setup": [V, P(_AmgParams), V, V, P(V)],
+        "lgx_amg_destroy": [V],
+        "lgx_amg_info": [V, P(I64), V, V, I64],
+        "lgx_amg_level_download": [V, I64, V, V, V, V, V],
+        "lgx_amg_vcycle": [V, V, V, V],
+        "lgx_amg_strength": [V, D, V, V, V, V],
+        "lgx_amg_aggregate": [V, V, V, V, I32, I32, I64, C.c_int, V, P(I64), V],
+        "lgx_pcg": [V, V, V, P(_SolveParams), V, P(I64), P(D), V],
+        "lgx_pbicgstab": [V, V, V, P(_SolveParams), V, P(I64), P(D), V],
+    }
+    for name, args in sigs.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = C.c_int
+    L.lgx_amg_default_params.argtypes = [P(_AmgParams)]
+    L.lgx_amg_default_params.restype = None
+    L.lgx_solve_default_params.argtypes = [P(_SolveParams)]
+    L.lgx_solve_default_params.restype = None
+
+
+def _check(status: int):
+    if status != 0:
+        raise LinealError(status, lib().lgx_last_error().decode())
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _stream():
+    torch = _torch()
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t) -> C.c_void_p:
+    if t is None:
+        return C.c_void_p(0)
+    if isinstance(t, np.ndarray):
+        return t.ctypes.data_as(C.c_void_p)
+    return C.c_void_p(t.data_ptr())
+
+
+def _dvec(t, dtype=None):
+    """Contiguous CUDA tensor of the requested dtype."""
+    torch = _torch()
+    dtype = dtype or torch.float64
+    if not isinstance(t, torch.Tensor):
+        t = torch.as_tensor(np.ascontiguousarray(t))
+    return t.to(device="cuda", dtype=dtype).contiguous()
+
+
+def _empty(n: int, dtype=None):
+    torch = _torch()
+    return torch.empty(max(int(n), 0), dtype=dtype or torch.float64, device="cuda")
+
+
+# ---------------------------------------------------------------------------
+# Matrices
+# ---------------------------------------------------------------------------
+class _Matrix:
+    def __init__(self, handle: C.c_void_p):
+        self._h = handle
+
+    @property
+    def handle(self):
+        return self._h
+
+    def info(self):
+        kind, n, nnz, sym = C.c_int(), C.c_int64(), C.c_int64(), C.c_int()
+        _check(lib().lgx_matrix_info(self._h, C.byref(kind), C.byref(n), C.byref(nnz),
+                                     C.byref(sym)))
+        return kind.value, n.value, nnz.value, bool(sym.value)
+
+    @property
+    def kind(self) -> int:
+        return self.info()[0]
+
+    def row_num(self) -> int:
+        return self.info()[1]
+
+    def column_num(self) -> int:
+        return self.info()[1]
+
+    def non_zero_num(self) -> int:
+        return self.info()[2]
+
+    def is_symmetric(self) -> bool:
+        return self.info()[3]
+
+    def __mul__(self, x):
+        return spmv(self, x)
+
+    def spmv(self, x, out=None):
+        return spmv(self, x, out)
+
+    def diagonal(self):
+        d = _empty(self.row_num())
+        _check(lib().lgx_diagonal(self._h, _ptr(d), _stream()))
+        return d
+
+    def close(self):
+        if self._h:
+            lib().lgx_matrix_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class CsrMatrix(_Matrix):
+    """CsrMatrix (tensor/dynamic/csr/shared.hpp): sorted columns, stored diagonal."""
+
+    @classmethod
+    def from_host(cls, rowptr, col, val, symmetric=True, storage=F64) -> "CsrMatrix":
+        rowptr = np.ascontiguousarray(rowptr, dtype=np.int64)
+        col = np.ascontiguousarray(col, dtype=np.int32)
+        val = np.ascontiguousarray(val, dtype=np.float64)
+        n = len(rowptr) - 1
+        h = C.c_void_p()
+        _check(lib().lgx_csr_create_host(n, int(rowptr[-1]), _ptr(rowptr), _ptr(col), _ptr(val),
+                                         int(symmetric), storage, C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_device(cls, rowptr, col, val, symmetric=True, storage=F64) -> "CsrMatrix":
+        torch = _torch()
+        rowptr = _dvec(rowptr, torch.int64)
+        col = _dvec(col, torch.int32)
+        val = _dvec(val, torch.float64)
+        h = C.c_void_p()
+        _check(lib().lgx_csr_create(rowptr.numel() - 1, col.numel(), _ptr(rowptr), _ptr(col),
+                                    _ptr(val), int(symmetric), storage, _stream(), C.byref(h)))
+        return cls(h)
+
+    def download(self):
+        _, n, nnz, _ = self.info()
+        rowptr = np.empty(n + 1, dtype=np.int64)
+        col = np.empty(nnz, dtype=np.int32)
+        val = np.empty(nnz, dtype=np.float64)
+        _check(lib().lgx_csr_download(self._h, _ptr(rowptr), _ptr(col), _ptr(val), _stream()))
+        return rowptr, col, val
+
+
+class StencilMatrix(_Matrix):
+    """AdjacentStencilMatrix over a stationary-diffusion valuator (7-point,
+    Dirichlet on the faces of axis 0)."""
+
+    @classmethod
+    def lookup(cls, dims, q, coeffs, materials, sol_start=1.0, sol_end=0.0,
+               zero_to_one=True) -> "StencilMatrix":
+        torch = _torch()
+        d = np.ascontiguousarray(dims, dtype=np.int64)
+        qq = np.ascontiguousarray(q, dtype=np.float64)
+        cc = np.ascontiguousarray(coeffs, dtype=np.float64)
+        mat = _dvec(materials, torch.uint8)
+        h = C.c_void_p()
+        _check(lib().lgx_stencil_create_lookup(_ptr(d), _ptr(qq), _ptr(cc), _ptr(mat), sol_start,
+                                               sol_end, int(zero_to_one), _stream(), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def value(cls, dims, q, k, sol_start=1.0, sol_end=0.0, zero_to_one=True) -> "StencilMatrix":
+        d = np.ascontiguousarray(dims, dtype=np.int64)
+        qq = np.ascontiguousarray(q, dtype=np.float64)
+        kk = _dvec(k)
+        h = C.c_void_p()
+        _check(lib().lgx_stencil_create_value(_ptr(d), _ptr(qq), _ptr(kk), sol_start, sol_end,
+                                              int(zero_to_one), _stream(), C.byref(h)))
+        return cls(h)
+
+    def rhs(self):
+        b = _empty(self.row_num())
+        _check(lib().lgx_stencil_rhs(self._h, _ptr(b), _stream()))
+        return b
+
+    def to_csr(self, with_compress_map=False):
+        torch = _torch()
+        cmap = _empty(self.row_num(), torch.int64) if with_compress_map else None
+        h = C.c_void_p()
+        _check(lib().lgx_stencil_to_csr(self._h, _ptr(cmap), _stream(), C.byref(h)))
+        m = CsrMatrix(h)
+        return (m, cmap) if with_compress_map else m
+
+
+def gen_27pt(dims, k, storage=F64) -> CsrMatrix:
+    d = np.ascontiguousarray(dims, dtype=np.int64)
+    kk = _dvec(k)
+    h = C.c_void_p()
+    _check(lib().lgx_gen_27pt(_ptr(d), _ptr(kk), storage, _stream(), C.byref(h)))
+    return CsrMatrix(h)
+
+
+def gen_7pt(dims, k, storage=F64) -> CsrMatrix:
+    d = np.ascontiguousarray(dims, dtype=np.int64)
+    kk = _dvec(k)
+    h = C.c_void_p()
+    _check(lib().lgx_gen_7pt(_ptr(d), _ptr(kk), storage, _stream(), C.byref(h)))
+    return CsrMatrix(h)
+
+
+# ---------------------------------------------------------------------------
+# Kernels
+# ---------------------------------------------------------------------------
+def spmv(a: _Matrix, x, out=None):
+    x = _dvec(x)
+    y = out if out is not None else _empty(a.row_num())
+    _check(lib().lgx_spmv(a.handle, _ptr(x), _ptr(y), _stream()))
+    return y
+
+
+def spmv_f32(a: _Matrix, x, out=None):
+    torch = _torch()
+    x = _dvec(x, torch.float32)
+    y = out if out is not None else _empty(a.row_num(), torch.float32)
+    _check(lib().lgx_spmv_f32(a.handle, _ptr(x), _ptr(y), _stream()))
+    return y
+
+
+def residual(a: _Matrix, b, x, with_norm=True):
+    b, x = _dvec(b), _dvec(x)
+    r = _empty(a.row_num())
+    nrm = _empty(1) if with_norm else None
+    _check(lib().lgx_residual(a.handle, _ptr(b), _ptr(x), _ptr(r), _ptr(nrm), _stream()))
+    return (r, float(nrm.item())) if with_norm else r
+
+
+def dot(a, b) -> float:
+    a, b = _dvec(a), _dvec(b)
+    out = _empty(1)
+    _check(lib().lgx_dot(a.numel(), _ptr(a), _ptr(b), _ptr(out), _stream()))
+    return float(out.item())
+
+
+def norm2sq(a) -> float:
+    a = _dvec(a)
+    out = _empty(1)
+    _check(lib().lgx_norm2sq(a.numel(), _ptr(a), _ptr(out), _stream()))
+    return float(out.item())
+
+
+def max_norm(a) -> float:
+    a = _dvec(a)
+    out = _empty(1)
+    _check(lib().lgx_max_norm(a.numel(), _ptr(a), _ptr(out), _stream()))
+    return float(out.item())
+
+
+def jacobi_sweep(a: _Matrix, b, x_in=None, relax=1.0):
+    b = _dvec(b)
+    xi = None if x_in is None else _dvec(x_in)
+    out = _empty(a.row_num())
+    _check(lib().lgx_jacobi_sweep(a.handle, relax, _ptr(xi), _ptr(out), _ptr(b), _stream()))
+    return out
+
+
+class Colouring:
+    """Graph colouring driving the multicolour SOR sweeps."""
+
+    def __init__(self, handle: C.c_void_p, n: int):
+        self._h = handle
+        self.n = n
+
+    @classmethod
+    def jp(cls, a: CsrMatrix, seed: int = 0x5EED) -> "Colouring":
+        h = C.c_void_p()
+        _check(lib().lgx_colouring_create_jp(a.handle, seed, _stream(), C.byref(h)))
+        return cls(h, a.row_num())
+
+    @classmethod
+    def from_array(cls, a: CsrMatrix, colours, ncolours: int | None = None) -> "Colouring":
+        torch = _torch()
+        c = _dvec(colours, torch.int32)
+        nc = int(c.max().item()) + 1 if ncolours is None else ncolours
+        h = C.c_void_p()
+        _check(lib().lgx_colouring_create(a.handle, _ptr(c), nc, _stream(), C.byref(h)))
+        return cls(h, a.row_num())
+
+    def export(self):
+        torch = _torch()
+        out = _empty(self.n, torch.int32)
+        nc = C.c_int32()
+        _check(lib().lgx_colouring_export(self._h, _ptr(out), C.byref(nc), _stream()))
+        return out, nc.value
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            lib().lgx_colouring_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def sor_sweep(a: CsrMatrix, colouring: Colouring, b, x_in=None, relax=1.0, forward=True,
+              ultra=False, out=None):
+    b = _dvec(b)
+    xi = None if x_in is None else _dvec(x_in)
+    y = out if out is not None else _empty(a.row_num())
+    _check(lib().lgx_sor_sweep(a.handle, colouring.handle, relax, int(forward), int(ultra),
+                               _ptr(xi), _ptr(y), _ptr(b), _stream()))
+    return y
+
+
+# ---------------------------------------------------------------------------
+# AMG
+# ---------------------------------------------------------------------------
+@dataclass
+class HierarchyWright:
+    """HierarchyWrightParams + AggregationParams + DuneDependencyCriterion
+    (hierarchy/wright.hpp:46-55, aggregation/params.hpp:13-20,
+    dependency/criterion.hpp:103-118)."""
+
+    max_level_num: int = 16
+    min_coarsen_size: int = 2000
+    min_coarsen_factor: float = 1.2
+    strong_threshold: float = 1.0 / 3.0
+    aggressive_threshold: float = 1.0 / 3.0
+    min_aggregate_size: int = 6
+    max_aggregate_size: int = 9
+    partition_size: int = 4096
+    max_partitions: int = 1 << 30
+    coarse_f32: bool = False
+    cycle_f32: bool = False
+    relax: float = 1.0
+    smoother_relax: float = 1.0
+    smoother_ultra: bool = False
+    colour_seed: int = 0x5EED
+
+    def params(self) -> _AmgParams:
+        p = _AmgParams()
+        lib().lgx_amg_default_params(C.byref(p))
+        for f in self.__dataclass_fields__:
+            v = getattr(self, f)
+            setattr(p, f, int(v) if isinstance(v, bool) else v)
+        return p
+
+    def instantiate(self, a: CsrMatrix, finest_colouring: Colouring | None = None) -> "Hierarchy":
+        p = self.params()
+        h = C.c_void_p()
+        _check(lib().lgx_amg_setup(a.handle, C.byref(p),
+                                   finest_colouring.handle if finest_colouring else None,
+                                   _stream(), C.byref(h)))
+        return Hierarchy(h, a)
+
+
+class Hierarchy:
+    def __init__(self, handle, matrix):
+        self._h = handle
+        self._a = matrix  # the finest matrix must outlive the hierarchy
+
+    @property
+    def handle(self):
+        return self._h
+
+    def level_num(self) -> int:
+        return len(self.sizes()[0])
+
+    def sizes(self):
+        L = C.c_int64()
+        rows = np.zeros(32, dtype=np.int64)
+        nnz = np.zeros(32, dtype=np.int64)
+        _check(lib().lgx_amg_info(self._h, C.byref(L), _ptr(rows), _ptr(nnz), 32))
+        return rows[: L.value].tolist(), nnz[: L.value].tolist()
+
+    def level(self, l: int, with_agg: bool = True):
+        rows, nnz = self.sizes()
+        n, m = rows[l], nnz[l]
+        rowptr = np.empty(n + 1, dtype=np.int64)
+        col = np.empty(m, dtype=np.int32)
+        val = np.empty(m, dtype=np.float64)
+        agg = np.empty(n, dtype=np.uint32) if with_agg and l + 1 < len(rows) else None
+        _check(lib().lgx_amg_level_download(self._h, l, _ptr(rowptr), _ptr(col), _ptr(val),
+                                            _ptr(agg), _stream()))
+        return rowptr, col, val, agg
+
+    def vcycle(self, b, out=None):
+        b = _dvec(b)
+        x = out if out is not None else _empty(b.numel())
+        _check(lib().lgx_amg_vcycle(self._h, _ptr(b), _ptr(x), _stream()))
+        return x
+
+    def close(self):
+        if self._h:
+            lib().lgx_amg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def amg_strength(a: CsrMatrix, theta: float = 1.0 / 3.0):
+    torch = _torch()
+    _, n, nnz, _ = a.info()
+    dep = _empty(nnz, torch.uint8)
+    inf = _empty(nnz, torch.uint8)
+    iso = _empty(n, torch.uint8)
+    _check(lib().lgx_amg_strength(a.handle, theta, _ptr(dep), _ptr(inf), _ptr(iso), _stream()))
+    return dep, inf, iso
+
+
+def amg_aggregate(a: CsrMatrix, dep, inf, iso, min_size=6, max_size=9, nparts=1,
+                  aggressive=False):
+    torch = _torch()
+    agg = _empty(a.row_num(), torch.int32)
+    nc = C.c_int64()
+    _check(lib().lgx_amg_aggregate(a.handle, _ptr(dep), _ptr(inf), _ptr(iso), min_size, max_size,
+                                   nparts, int(aggressive), _ptr(agg), C.byref(nc), _stream()))
+    return nc.value, agg.cpu().numpy().view(np.uint32)
+
+
+# ---------------------------------------------------------------------------
+# Krylov solvers
+# ---------------------------------------------------------------------------
+@dataclass
+class SolveResult:
+    x: object
+    iterations: int
+    rel_residual: float
+    history: np.ndarray = field(repr=False)
+
+
+def _solve(fn, a: _Matrix, b, x0=None, precon=PRECON_NONE, relax=1.0, ultra=False,
+           colouring: Colouring | None = None, amg: Hierarchy | None = None, rtol=1e-8,
+           maxit=1000, rere_period=8) -> SolveResult:
+    b = _dvec(b)
+    x = _dvec(x0) if x0 is not None else _empty(b.numel()).zero_()
+    if x0 is not None:
+        x = x.clone()
+    p = _SolveParams()
+    lib().lgx_solve_default_params(C.byref(p))
+    p.precon = precon
+    p.relax = relax
+    p.ultra = int(ultra)
+    p.colouring = colouring.handle if colouring else None
+    p.amg = amg.handle if amg else None
+    p.rtol = rtol
+    p.maxit = maxit
+    p.rere_period = rere_period
+    it = C.c_int64()
+    rel = C.c_double()
+    hist = np.zeros(maxit + 1)
+    _check(fn(a.handle, _ptr(b), _ptr(x), C.byref(p), _stream(), C.byref(it), C.byref(rel),
+              _ptr(hist)))
+    return SolveResult(x, it.value, rel.value, hist[: it.value + 1])
+
+
+def pcg(a: _Matrix, b, **kw) -> SolveResult:
+    """Preconditioned CG (ConjugateGradientsSolver)."""
+    return _solve(lib().lgx_pcg, a, b, **kw)
+
+
+def pbicgstab(a: _Matrix, b, **kw) -> SolveResult:
+    """Preconditioned BiCGStab (BiCgStabSolver)."""
+    return _solve(lib().lgx_pbicgstab, a, b, **kw)
+
+
+def kernel_launches() -> int:
+    """Kernels launched by the library since it was loaded."""
+    return int(lib().lgx_kernel_launches())
+
+
+def version() -> str:
+    return lib().lgx_version().decode()

@@ -1,0 +1,1165 @@
+// Aggregation AMG on the device: strength of connection, greedy aggregation
+// per partition, aggregate-map merge, Galerkin coarse matrices, the level
+// hierarchy, a dense FP64 coarsest solver and the V-cycle.
+//
+// Reference: include/lineal/linear-solver/multigrid/ (dependency/criterion.hpp,
+// aggregation/base.hpp, aggregation/independent.hpp,
+// aggregate-map/multithread.hpp, transport/matrix-shared.hpp,
+// transport/vector-shared.hpp, hierarchy/wright.hpp, solver.hpp).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <memory>
+#include <vector>
+
+#include "lgx_internal.cuh"
+
+namespace lgx {
+
+// ===========================================================================
+// Strength of connection (dependency/criterion.hpp:35-78) with the
+// NegativeOffdiagonalTransform (graph/weight-transform.hpp:28-38): edge
+// weight w_ij = -a_ij, vertex weight a_jj.  strength = max(w_ij,0) * w' /
+// a_jj with w' = max(w_ij,0) for value-symmetric matrices, else the reverse
+// edge's max(w_ji,0) (0 if absent); an edge is strong iff strength >
+// theta * max strength of the row.  The arithmetic runs in the matrix value
+// type (GraphWeight = matrix Value).  depends is written for the row's own
+// edges, influences for their reverse edges (each slot has one writer).
+// ===========================================================================
+__device__ __forceinline__ int64_t find_col(const int64_t *rowptr, const int32_t *col,
+                                            int64_t row, int32_t c) {
+  int64_t lo = rowptr[row], hi = rowptr[row + 1];
+  const int64_t end = hi;
+  while (lo < hi) {
+    const int64_t mid = lo + (hi - lo) / 2;
+    if (col[mid] < c) lo = mid + 1; else hi = mid;
+  }
+  return (lo < end && col[lo] == c) ? lo : -1;
+}
+
+template <typename VT>
+__global__ void k_row_diag(int64_t n, const int64_t *rowptr, const int32_t *col, const VT *val,
+                           VT *diag) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = find_col(rowptr, col, i, (int32_t)i);
+    diag[i] = k >= 0 ? val[k] : VT(0);
+  }
+}
+
+template <typename VT>
+__device__ __forceinline__ VT edge_strength(int64_t i, int64_t e, const int64_t *rowptr,
+                                            const int32_t *col, const VT *val, const VT *diag,
+                                            int symmetric) {
+  const int32_t j = col[e];
+  const VT w = -val[e];
+  const VT nn = w > VT(0) ? w : VT(0);
+  VT opp;
+  if (symmetric) {
+    opp = nn;
+  } else {
+    const int64_t r = find_col(rowptr, col, j, (int32_t)i);
+    const VT wr = r >= 0 ? -val[r] : VT(0);
+    opp = r >= 0 ? (wr > VT(0) ? wr : VT(0)) : VT(0);
+  }
+  return nn * opp / diag[j];
+}
+
+template <typename VT>
+__global__ void k_strength(int64_t n, const int64_t *rowptr, const int32_t *col, const VT *val,
+                           const VT *diag, int symmetric, VT theta, uint8_t *dep, uint8_t *inf,
+                           uint8_t *iso) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = rowptr[i], e = rowptr[i + 1];
+    VT maxs = VT(0);
+    for (int64_t k = b; k < e; ++k) {
+      if (col[k] == i) continue;
+      const VT s = edge_strength(i, k, rowptr, col, val, diag, symmetric);
+      if (s > maxs) maxs = s;
+    }
+    const VT lb = theta * maxs;
+    bool any = false;
+    for (int64_t k = b; k < e; ++k) {
+      const int32_t j = col[k];
+      if (j == i) {
+        dep[k] = 0;
+        continue;
+      }
+      const VT s = edge_strength(i, k, rowptr, col, val, diag, symmetric);
+      const bool cond = s > lb;
+      any = any || cond;
+      dep[k] = cond;
+      const int64_t r = find_col(rowptr, col, j, (int32_t)i);
+      if (r >= 0) inf[r] = cond;
+    }
+    iso[i] = !any;
+  }
+}
+
+__global__ void k_fill_u8(int64_t n, uint8_t *p, uint8_t v) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = v;
+}
+
+lgx_status strength(const Csr &a, double theta, uint8_t *dep, uint8_t *inf, uint8_t *iso,
+                    cudaStream_t s) {
+  const int64_t n = a.n;
+  if (n == 0) return LGX_OK;
+  const unsigned g = (unsigned)std::min<int64_t>(grid_for(n, 128), 65535);
+  // diagonal entries of the diagonal itself carry no influence flag
+  k_fill_u8<<<std::min<int64_t>(grid_for(a.nnz, 256), 16384), 256, 0, s>>>(a.nnz, inf, 0);
+  LGX_LAUNCH_CHECK();
+  if (a.storage == LGX_F64) {
+    DBuf<double> d;
+    LGX_CHECK(d.alloc(n));
+    k_row_diag<double><<<g, 128, 0, s>>>(n, a.rowptr.p, a.col.p, a.v64.p, d.p);
+    LGX_LAUNCH_CHECK();
+    k_strength<double><<<g, 128, 0, s>>>(n, a.rowptr.p, a.col.p, a.v64.p, d.p, a.symmetric, theta,
+                                         dep, inf, iso);
+    LGX_LAUNCH_CHECK();
+    LGX_CUDA(cudaStreamSynchronize(s));
+  } else {
+    DBuf<float> d;
+    LGX_CHECK(d.alloc(n));
+    k_row_diag<float><<<g, 128, 0, s>>>(n, a.rowptr.p, a.col.p, a.v32.p, d.p);
+    LGX_LAUNCH_CHECK();
+    k_strength<float><<<g, 128, 0, s>>>(n, a.rowptr.p, a.col.p, a.v32.p, d.p, a.symmetric,
+                                        (float)theta, dep, inf, iso);
+    LGX_LAUNCH_CHECK();
+    LGX_CUDA(cudaStreamSynchronize(s));
+  }
+  return LGX_OK;
+}
+
+// ===========================================================================
+// Greedy aggregation, one thread per contiguous partition
+// (aggregation/base.hpp:28-711 via independent.hpp:47-216).  The subgraph of
+// a partition keeps only edges whose head lies inside it.  All scratch lives
+// in n-sized arrays indexed by vertex, so partition p owns the slots
+// [pb, pe) (and [pb*max, pe*max) of the aggregate blocks).
+// ===========================================================================
+struct AggDev {
+  const int64_t *rowptr;
+  const int32_t *col;
+  const uint8_t *dep, *inf, *iso;
+  uint32_t *agg;
+  int64_t n, nparts;
+  int32_t min_size, max_size;
+  int aggressive;
+  int32_t *front;       // sorted front, slots [pb, pe)
+  uint8_t *front_mark;  // by vertex
+  int32_t *conn;        // connected local aggregate ids, slots [pb, pe)
+  int32_t *cand;        // candidates, slots [pb, pe)
+  int32_t *blocks;      // aggregate k of partition p: [(pb + k) * max, ...)
+  int32_t *block_len;   // aggregate k of partition p: slot pb + k
+  int64_t *pcount;      // aggregates per partition
+  int64_t *stats;       // 5 counters (atomic adds)
+};
+
+__device__ __forceinline__ int64_t part_begin(int64_t n, int64_t p, int64_t k) {
+  const int64_t base = n / p, rem = n % p;
+  return k * base + (k < rem ? k : rem);
+}
+
+struct AggThread {
+  const AggDev &D;
+  int64_t pb, pe;
+  int64_t front_len = 0, conn_len = 0, cand_len = 0, counter = 0;
+  int64_t st[5] = {0, 0, 0, 0, 0};
+
+  __device__ AggThread(const AggDev &d, int64_t b, int64_t e) : D(d), pb(b), pe(e) {}
+
+  __device__ bool in_range(int64_t v) const { return v >= pb && v < pe; }
+  __device__ bool front_contains(int64_t v) const { return D.front_mark[v]; }
+  __device__ void front_insert(int64_t v) {
+    int32_t *f = D.front + pb;
+    int64_t lo = 0, hi = front_len;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) / 2;
+      if (f[mid] < v) lo = mid + 1; else hi = mid;
+    }
+    if (lo < front_len && f[lo] == v) return;
+    for (int64_t k = front_len; k > lo; --k) f[k] = f[k - 1];
+    f[lo] = (int32_t)v;
+    ++front_len;
+    D.front_mark[v] = 1;
+  }
+  __device__ void front_erase(int64_t v) {
+    int32_t *f = D.front + pb;
+    int64_t lo = 0, hi = front_len;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) / 2;
+      if (f[mid] < v) lo = mid + 1; else hi = mid;
+    }
+    if (lo < front_len && f[lo] == v) {
+      for (int64_t k = lo; k + 1 < front_len; ++k) f[k] = f[k + 1];
+      --front_len;
+    }
+    D.front_mark[v] = 0;
+  }
+  __device__ void helpers_clear() {
+    const int32_t *f = D.front + pb;
+    for (int64_t k = 0; k < front_len; ++k) D.front_mark[f[k]] = 0;
+    front_len = 0;
+    conn_len = 0;
+  }
+  __device__ bool is_connected(uint32_t ag) const {
+    const int32_t *c = D.conn + pb;
+    for (int64_t k = 0; k < conn_len; ++k)
+      if ((uint32_t)c[k] == ag) return true;
+    return false;
+  }
+  __device__ int32_t &blen(uint32_t ag) const { return D.block_len[pb + ag]; }
+  __device__ int32_t *block(uint32_t ag) const {
+    return D.blocks + (pb + (int64_t)ag) * D.max_size;
+  }
+
+  // AggregateManager::add_help (base.hpp:263-287)
+  __device__ void add_help(int64_t v, uint32_t ag, int64_t &size) {
+    ++size;
+    D.agg[v] = ag;
+    block(ag)[blen(ag)++] = (int32_t)v;
+    for (int64_t e = D.rowptr[v]; e < D.rowptr[v + 1]; ++e) {
+      const int64_t t = D.col[e];
+      if (t == v || !in_range(t)) continue;
+      const uint32_t ta = D.agg[t];
+      if (ta < kIsolated && !is_connected(ta)) D.conn[pb + conn_len++] = (int32_t)ta;
+      if (ta == kUnaggregated && !front_contains(t)) front_insert(t);
+    }
+  }
+  __device__ void add_candidates(uint32_t ag, int64_t &size) {
+    for (int64_t k = 0; k < cand_len; ++k) {
+      const int64_t v = D.cand[pb + k];
+      front_erase(v);
+      add_help(v, ag, size);
+    }
+  }
+
+  // grow_aggregate (base.hpp:532-585)
+  __device__ void grow(uint32_t ag, int64_t &size) {
+    while (size < D.min_size) {
+      int64_t m0 = 0, m2 = 0;
+      double m1 = 0.0;
+      bool has_cons2 = false;
+      cand_len = 0;
+      const int32_t *f = D.front + pb;
+      for (int64_t fi = 0; fi < front_len; ++fi) {
+        const int64_t vtx = f[fi];
+        if (D.iso[vtx]) continue;
+        int64_t con = 0, nbs = 0, cons2 = 0, cons1 = 0;
+        for (int64_t e = D.rowptr[vtx]; e < D.rowptr[vtx + 1]; ++e) {
+          const int64_t t = D.col[e];
+          if (t == vtx || !in_range(t)) continue;
+          const uint32_t ha = D.agg[t];
+          const bool dep = D.dep[e], inf = D.inf[e];
+          con += (ha < kIsolated) && is_connected(ha);
+          nbs += front_contains(t);
+          cons2 += (ha == ag) && (inf && dep);
+          cons1 += (ha == ag) && (!inf && dep);
+        }
+        const int64_t adj = (D.rowptr[vtx + 1] - D.rowptr[vtx]) - 1;
+        const double cond = (double)con / (double)adj;
+        if (cons2 > 0 && !has_cons2) {
+          has_cons2 = true;
+          m0 = cons2;
+          m1 = cond;
+          m2 = nbs;
+          cand_len = 0;
+          D.cand[pb + cand_len++] = (int32_t)vtx;
+        } else {
+          const int64_t t0 = has_cons2 ? cons2 : cons1;
+          if (t0 > 0) {
+            int cmp;
+            if (t0 != m0) cmp = t0 > m0 ? 1 : -1;
+            else if (cond != m1) cmp = cond > m1 ? 1 : (cond < m1 ? -1 : 2);
+            else if (nbs != m2) cmp = nbs > m2 ? 1 : -1;
+            else cmp = 0;
+            if (cmp == 1) {
+              m0 = t0;
+              m1 = cond;
+              m2 = nbs;
+              cand_len = 0;
+              D.cand[pb + cand_len++] = (int32_t)vtx;
+            } else if (cmp == 0) {
+              D.cand[pb + cand_len++] = (int32_t)vtx;
+            }
+          }
+        }
+      }
+      if (cand_len == 0) break;
+      const int64_t room = D.max_size - size;
+      if (cand_len > room) cand_len = room;
+      add_candidates(ag, size);
+    }
+  }
+
+  // round_aggregate (base.hpp:601-636)
+  __device__ void round(uint32_t ag, int64_t &size) {
+    while (size < D.max_size) {
+      cand_len = 0;
+      const int32_t *f = D.front + pb;
+      for (int64_t fi = 0; fi < front_len; ++fi) {
+        const int64_t vtx = f[fi];
+        if (D.iso[vtx]) continue;
+        int64_t cons = 0, unagg = 0, inagg = 0;
+        for (int64_t e = D.rowptr[vtx]; e < D.rowptr[vtx + 1]; ++e) {
+          const int64_t t = D.col[e];
+          if (t == vtx || !in_range(t)) continue;
+          const uint32_t ha = D.agg[t];
+          cons += (ha == ag) && D.dep[e];
+          unagg += ha == kUnaggregated;
+          inagg += ha == ag;
+        }
+        if (cons == 0 || unagg >= inagg) continue;
+        D.cand[pb + cand_len++] = (int32_t)vtx;
+        break;
+      }
+      if (cand_len == 0) break;
+      const int64_t room = D.max_size - size;
+      if (cand_len > room) cand_len = room;
+      add_candidates(ag, size);
+    }
+  }
+
+  // handle_vertex (base.hpp:638-677)
+  __device__ void handle(int64_t seed) {
+    if (D.agg[seed] != kUnaggregated) return;
+    if (D.iso[seed]) {
+      D.agg[seed] = kIsolated;
+      ++st[4];
+      return;
+    }
+    const uint32_t ag = (uint32_t)counter;
+    int64_t size = 0;
+    add_help(seed, ag, size);
+    grow(ag, size);
+    round(ag, size);
+    if (size == 1 && D.max_size > 1) {
+      uint32_t target = kUnaggregated;
+      for (int64_t e = D.rowptr[seed]; e < D.rowptr[seed + 1]; ++e) {
+        const int64_t t = D.col[e];
+        if (t == seed || !in_range(t)) continue;
+        if (!(D.dep[e] || D.inf[e])) continue;
+        const uint32_t ta = D.agg[t];
+        if (ta < kIsolated && blen(ta) < D.max_size) {
+          target = ta;
+          break;
+        }
+      }
+      if (target != kUnaggregated) {
+        blen(ag) = 0;
+        D.agg[seed] = target;
+        block(target)[blen(target)++] = (int32_t)seed;
+        ++st[3];
+        helpers_clear();
+        return;
+      }
+      if (D.aggressive) {
+        blen(ag) = 0;
+        D.agg[seed] = kIsolated;
+        ++st[4];
+        helpers_clear();
+        return;
+      }
+      ++st[2];
+    } else {
+      ++st[1];
+    }
+    ++counter;
+    helpers_clear();
+  }
+};
+
+__global__ void k_aggregate(AggDev D) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < D.nparts;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t pb = part_begin(D.n, D.nparts, p), pe = part_begin(D.n, D.nparts, p + 1);
+    for (int64_t v = pb; v < pe; ++v) D.block_len[v] = 0;
+    AggThread T(D, pb, pe);
+    for (int64_t v = pb; v < pe; ++v) T.handle(v);
+    D.pcount[p] = T.counter;
+    T.st[0] = T.counter;
+    for (int k = 0; k < 5; ++k)
+      if (T.st[k]) atomicAdd((unsigned long long *)&D.stats[k], (unsigned long long)T.st[k]);
+  }
+}
+
+// merge (aggregate-map/multithread.hpp:107-143): global ids and the list
+// lengths of every aggregate in global order
+__global__ void k_agg_merge(AggDev D, const int64_t *poff, int64_t *glen) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < D.nparts;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t pb = part_begin(D.n, D.nparts, p), pe = part_begin(D.n, D.nparts, p + 1);
+    const uint32_t off = (uint32_t)poff[p];
+    for (int64_t v = pb; v < pe; ++v)
+      if (D.agg[v] < kIsolated) D.agg[v] += off;
+    for (int64_t k = 0; k < D.pcount[p]; ++k) glen[off + k] = D.block_len[pb + k];
+  }
+}
+
+__global__ void k_agg_lists(AggDev D, const int64_t *poff, const int64_t *list_ptr,
+                            int32_t *list) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < D.nparts;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t pb = part_begin(D.n, D.nparts, p);
+    const int64_t off = poff[p];
+    for (int64_t k = 0; k < D.pcount[p]; ++k) {
+      const int32_t *blk = D.blocks + (pb + k) * D.max_size;
+      int64_t o = list_ptr[off + k];
+      for (int32_t m = 0; m < D.block_len[pb + k]; ++m) list[o++] = blk[m];
+    }
+  }
+}
+
+struct AggResult {
+  int64_t ncoarse = 0;
+  DBuf<uint32_t> agg;
+  DBuf<int64_t> list_ptr;
+  DBuf<int32_t> list;
+  int64_t stats[5] = {0, 0, 0, 0, 0};
+};
+
+lgx_status aggregate(const Csr &a, const uint8_t *dep, const uint8_t *inf, const uint8_t *iso,
+                     int32_t min_size, int32_t max_size, int64_t nparts, int aggressive,
+                     cudaStream_t s, AggResult &out, uint32_t *agg_out = nullptr) {
+  const int64_t n = a.n;
+  if (nparts < 1) nparts = 1;
+  if (nparts > n && n > 0) nparts = n;
+  if (max_size < 1 || min_size < 1) return fail(LGX_ERR_INVALID, "invalid aggregate sizes");
+  uint32_t *agg = agg_out;
+  if (!agg) {
+    LGX_CHECK(out.agg.alloc(n));
+    agg = out.agg.p;
+  }
+  DBuf<int32_t> front, conn, cand, blocks, blen;
+  DBuf<uint8_t> mark;
+  DBuf<int64_t> pcount, poff, stats, glen;
+  LGX_CHECK(front.alloc(n));
+  LGX_CHECK(conn.alloc(n));
+  LGX_CHECK(cand.alloc(n));
+  LGX_CHECK(blocks.alloc(n * max_size));
+  LGX_CHECK(blen.alloc(n));
+  LGX_CHECK(mark.alloc(n));
+  LGX_CHECK(pcount.alloc(nparts));
+  LGX_CHECK(poff.alloc(nparts + 1));
+  LGX_CHECK(stats.alloc(5));
+  LGX_CUDA(cudaMemsetAsync(agg, 0xFF, sizeof(uint32_t) * std::max<int64_t>(n, 1), s));
+  LGX_CUDA(cudaMemsetAsync(mark.p, 0, std::max<int64_t>(n, 1), s));
+  LGX_CUDA(cudaMemsetAsync(stats.p, 0, sizeof(int64_t) * 5, s));
+  AggDev D{a.rowptr.p, a.col.p, dep,      inf,    iso,      agg,      n,         nparts,
+           min_size,   max_size, aggressive, front.p, mark.p, conn.p, cand.p, blocks.p,
+           blen.p,     pcount.p, stats.p};
+  if (n > 0) {
+    k_aggregate<<<grid_for(nparts, 64), 64, 0, s>>>(D);
+    LGX_LAUNCH_CHECK();
+  }
+  LGX_CHECK(inclusive_offsets(nparts, pcount.p, poff.p, s));
+  int64_t nc = 0;
+  LGX_CUDA(cudaMemcpyAsync(&nc, poff.p + nparts, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  LGX_CUDA(cudaMemcpyAsync(out.stats, stats.p, sizeof(int64_t) * 5, cudaMemcpyDeviceToHost, s));
+  LGX_CUDA(cudaStreamSynchronize(s));
+  out.ncoarse = nc;
+  LGX_CHECK(glen.alloc(nc));
+  LGX_CHECK(out.list_ptr.alloc(nc + 1));
+  if (n > 0) {
+    k_agg_merge<<<grid_for(nparts, 64), 64, 0, s>>>(D, poff.p, glen.p);
+    LGX_LAUNCH_CHECK();
+  }
+  LGX_CHECK(inclusive_offsets(nc, glen.p, out.list_ptr.p, s));
+  int64_t total = 0;
+  LGX_CUDA(cudaMemcpyAsync(&total, out.list_ptr.p + nc, sizeof(int64_t), cudaMemcpyDeviceToHost,
+                           s));
+  LGX_CUDA(cudaStreamSynchronize(s));
+  LGX_CHECK(out.list.alloc(total));
+  if (n > 0 && nc > 0) {
+    k_agg_lists<<<grid_for(nparts, 64), 64, 0, s>>>(D, poff.p, out.list_ptr.p, out.list.p);
+    LGX_LAUNCH_CHECK();
+  }
+  LGX_CUDA(cudaStreamSynchronize(s));
+  return LGX_OK;
+}
+
+// ===========================================================================
+// Galerkin coarse matrix (transport/matrix-shared.hpp:85-183, non-unique
+// builder csr/shared.hpp:730-764): coarse row I gathers the fine rows of
+// aggregate I in list order, columns ascending; each value is first cast to
+// the coarse value type, then accumulated in double per coarse column in
+// first-encounter order; the row is sorted by column; entries in isolated
+// columns are dropped.  One thread per coarse row, scratch slots at the
+// offsets of the row's fine entries.
+// ===========================================================================
+template <typename VT>
+__global__ void k_galerkin_upper(int64_t nc, const int64_t *rowptr, const int64_t *list_ptr,
+                                 const int32_t *list, int64_t *upper) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nc;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    int64_t u = 0;
+    for (int64_t k = list_ptr[c]; k < list_ptr[c + 1]; ++k)
+      u += rowptr[list[k] + 1] - rowptr[list[k]];
+    upper[c] = u;
+  }
+}
+
+template <typename VT>
+__global__ void k_galerkin_accumulate(int64_t nc, const int64_t *rowptr, const int32_t *col,
+                                      const VT *val, const uint32_t *agg, const int64_t *list_ptr,
+                                      const int32_t *list, int coarse_f32, const int64_t *soff,
+                                      int32_t *scol, double *sval, int64_t *count) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nc;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    int32_t *cc = scol + soff[c];
+    double *vv = sval + soff[c];
+    int64_t m = 0;
+    for (int64_t k = list_ptr[c]; k < list_ptr[c + 1]; ++k) {
+      const int64_t i = list[k];
+      for (int64_t e = rowptr[i]; e < rowptr[i + 1]; ++e) {
+        const uint32_t J = agg[col[e]];
+        if (J >= kIsolated) continue;
+        const double v = coarse_f32 ? (double)(float)val[e] : (double)val[e];
+        int64_t f = 0;
+        while (f < m && cc[f] != (int32_t)J) ++f;
+        if (f == m) {
+          cc[m] = (int32_t)J;
+          vv[m] = v;
+          ++m;
+        } else {
+          vv[f] = __dadd_rn(vv[f], v);
+        }
+      }
+    }
+    // insertion sort by column
+    for (int64_t x = 1; x < m; ++x) {
+      const int32_t c0 = cc[x];
+      const double v0 = vv[x];
+      int64_t y = x - 1;
+      while (y >= 0 && cc[y] > c0) {
+        cc[y + 1] = cc[y];
+        vv[y + 1] = vv[y];
+        --y;
+      }
+      cc[y + 1] = c0;
+      vv[y + 1] = v0;
+    }
+    count[c] = m;
+  }
+}
+
+__global__ void k_galerkin_emit(int64_t nc, const int64_t *soff, const int32_t *scol,
+                                const double *sval, const int64_t *rowptr_c, int32_t *col_c,
+                                double *val_c, int coarse_f32) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nc;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t o = rowptr_c[c], m = rowptr_c[c + 1] - o;
+    for (int64_t k = 0; k < m; ++k) {
+      col_c[o + k] = scol[soff[c] + k];
+      const double v = sval[soff[c] + k];
+      val_c[o + k] = coarse_f32 ? (double)(float)v : v;
+    }
+  }
+}
+
+lgx_status galerkin(const Csr &a, const AggResult &ag, int coarse_f32, cudaStream_t s, Csr &out) {
+  const int64_t nc = ag.ncoarse;
+  DBuf<int64_t> upper, soff, count, rowptr_c;
+  LGX_CHECK(upper.alloc(nc));
+  LGX_CHECK(soff.alloc(nc + 1));
+  LGX_CHECK(count.alloc(nc));
+  LGX_CHECK(rowptr_c.alloc(nc + 1));
+  const unsigned g = (unsigned)std::min<int64_t>(grid_for(nc, 128), 65535);
+  if (nc > 0) {
+    k_galerkin_upper<double><<<g, 128, 0, s>>>(nc, a.rowptr.p, ag.list_ptr.p, ag.list.p, upper.p);
+    LGX_LAUNCH_CHECK();
+  }
+  LGX_CHECK(inclusive_offsets(nc, upper.p, soff.p, s));
+  int64_t total = 0;
+  LGX_CUDA(cudaMemcpyAsync(&total, soff.p + nc, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  LGX_CUDA(cudaStreamSynchronize(s));
+  DBuf<int32_t> scol;
+  DBuf<double> sval;
+  LGX_CHECK(scol.alloc(total));
+  LGX_CHECK(sval.alloc(total));
+  if (nc > 0) {
+    if (a.storage == LGX_F64)
+      k_galerkin_accumulate<double><<<g, 128, 0, s>>>(nc, a.rowptr.p, a.col.p, a.v64.p, ag.agg.p,
+                                                      ag.list_ptr.p, ag.list.p, coarse_f32, soff.p,
+                                                      scol.p, sval.p, count.p);
+    else
+      k_galerkin_accumulate<float><<<g, 128, 0, s>>>(nc, a.rowptr.p, a.col.p, a.v32.p, ag.agg.p,
+                                                     ag.list_ptr.p, ag.list.p, coarse_f32, soff.p,
+                                                     scol.p, sval.p, count.p);
+    LGX_LAUNCH_CHECK();
+  }
+  LGX_CHECK(inclusive_offsets(nc, count.p, rowptr_c.p, s));
+  int64_t nnz_c = 0;
+  LGX_CUDA(cudaMemcpyAsync(&nnz_c, rowptr_c.p + nc, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  LGX_CUDA(cudaStreamSynchronize(s));
+  DBuf<int32_t> col_c;
+  DBuf<double> val_c;
+  LGX_CHECK(col_c.alloc(nnz_c));
+  LGX_CHECK(val_c.alloc(nnz_c));
+  if (nc > 0) {
+    k_galerkin_emit<<<g, 128, 0, s>>>(nc, soff.p, scol.p, sval.p, rowptr_c.p, col_c.p, val_c.p,
+                                      coarse_f32);
+    LGX_LAUNCH_CHECK();
+  }
+  return csr_from_device(nc, nnz_c, rowptr_c.p, col_c.p, val_c.p, a.symmetric,
+                         coarse_f32 ? LGX_F32 : a.storage, s, out);
+}
+
+// ===========================================================================
+// Dense FP64 coarsest solver.  The coarsest matrix (at most a few thousand
+// rows) is inverted once by Gauss-Jordan elimination without pivoting (SPD);
+// each cycle then applies the inverse with one dense matrix-vector product,
+// which replaces the sequential forward/backward substitution of
+// cholesky/solver.hpp:42-50 by a fully parallel kernel.
+// ===========================================================================
+__global__ void k_dense_from_csr(int64_t n, const int64_t *rowptr, const int32_t *col,
+                                 const double *v64, const float *v32, double *d) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double *row = d + i * n;
+    for (int64_t j = 0; j < n; ++j) row[j] = 0.0;
+    for (int64_t e = rowptr[i]; e < rowptr[i + 1]; ++e)
+      row[col[e]] = v64 ? v64[e] : (double)v32[e];
+  }
+}
+
+// step k, part 1: pivot row scaled into prow, column factors into pcol
+__global__ void k_gj_pivot(int64_t n, int64_t k, double *a, double *prow, double *pcol,
+                           int *bad) {
+  const double p = a[k * n + k];
+  if (!(p > 0.0)) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(bad, 1);
+    return;
+  }
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n;
+       j += (int64_t)gridDim.x * blockDim.x) {
+    prow[j] = j == k ? 1.0 / p : a[k * n + j] / p;
+    pcol[j] = a[j * n + k];
+  }
+}
+
+// step k, part 2: rank-one update of all rows
+__global__ void k_gj_update(int64_t n, int64_t k, double *a, const double *prow,
+                            const double *pcol, const int *bad) {
+  if (*bad) return;
+  const int64_t total = n * n;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t / n, j = t % n;
+    if (i == k) {
+      a[t] = prow[j];
+    } else {
+      const double f = pcol[i];
+      a[t] = j == k ? -f * prow[k] : fma(-f, prow[j], a[t]);
+    }
+  }
+}
+
+// x = A^-1 b, one warp per row
+template <typename XT>
+__global__ void k_dense_apply(int64_t n, const double *ainv, const XT *b, XT *x) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = warp; i < n; i += nwarps) {
+    double s = 0.0;
+    const double *row = ainv + i * n;
+    for (int64_t j = lane; j < n; j += 32) s = fma(row[j], (double)b[j], s);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) x[i] = (XT)s;
+  }
+}
+
+lgx_status dense_inverse(const Csr &a, cudaStream_t s, DBuf<double> &inv) {
+  const int64_t n = a.n;
+  LGX_CHECK(inv.alloc(n * n));
+  DBuf<double> prow, pcol;
+  DBuf<int> bad;
+  LGX_CHECK(prow.alloc(n));
+  LGX_CHECK(pcol.alloc(n));
+  LGX_CHECK(bad.alloc(1));
+  LGX_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), s));
+  if (n == 0) return LGX_OK;
+  k_dense_from_csr<<<grid_for(n, 128), 128, 0, s>>>(n, a.rowptr.p, a.col.p,
+                                                   a.storage == LGX_F64 ? a.v64.p : nullptr,
+                                                   a.storage == LGX_F32 ? a.v32.p : nullptr,
+                                                   inv.p);
+  LGX_LAUNCH_CHECK();
+  const unsigned g1 = (unsigned)std::min<int64_t>(grid_for(n, 256), 1024);
+  const unsigned g2 = (unsigned)std::min<int64_t>(grid_for(n * n, 256), 4096);
+  for (int64_t k = 0; k < n; ++k) {
+    k_gj_pivot<<<g1, 256, 0, s>>>(n, k, inv.p, prow.p, pcol.p, bad.p);
+    k_gj_update<<<g2, 256, 0, s>>>(n, k, inv.p, prow.p, pcol.p, bad.p);
+  }
+  LGX_LAUNCH_CHECK();
+  int h_bad = 0;
+  LGX_CUDA(cudaMemcpyAsync(&h_bad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  LGX_CUDA(cudaStreamSynchronize(s));
+  if (h_bad) return fail(LGX_ERR_NOT_SPD, "coarsest matrix has a non-positive pivot");
+  return LGX_OK;
+}
+
+// ===========================================================================
+// Transfers in the colour-permuted spaces of two consecutive levels
+// ===========================================================================
+// agg_p[i'] = permuted coarse id of the aggregate of fine row perm_f[i']
+__global__ void k_agg_permute(int64_t n, const int32_t *perm_f, const uint32_t *agg,
+                              const int32_t *iperm_c, uint32_t *agg_p) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = perm_f ? perm_f[r] : r;
+    const uint32_t a = agg[i];
+    agg_p[r] = a < kIsolated ? (iperm_c ? (uint32_t)iperm_c[a] : a) : kIsolated;
+  }
+}
+
+__global__ void k_rlist_len(int64_t nc, const int32_t *perm_c, const int64_t *list_ptr,
+                            int64_t *len) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nc;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = perm_c ? perm_c[r] : r;
+    len[r] = list_ptr[c + 1] - list_ptr[c];
+  }
+}
+
+__global__ void k_rlist_fill(int64_t nc, const int32_t *perm_c, const int64_t *list_ptr,
+                             const int32_t *list, const int32_t *iperm_f, const int64_t *rptr,
+                             int32_t *rlist) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nc;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = perm_c ? perm_c[r] : r;
+    int64_t o = rptr[r];
+    for (int64_t k = list_ptr[c]; k < list_ptr[c + 1]; ++k, ++o)
+      rlist[o] = iperm_f ? iperm_f[list[k]] : list[k];
+  }
+}
+
+// coarse b[I'] = sum over the aggregate's fine rows (list order) of r
+// (vector-shared.hpp:49-56)
+template <typename XT>
+__global__ void k_restrict(int64_t nc, const int64_t *rptr, const int32_t *rlist,
+                           const XT *__restrict__ r, XT *__restrict__ bc) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nc;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    XT s = XT(0);
+    for (int64_t k = rptr[c]; k < rptr[c + 1]; ++k) s = s + r[rlist[k]];
+    bc[c] = s;
+  }
+}
+
+// x_f += inv_relax * refine(x_c) (vector-shared.hpp:121-134, solver.hpp:129-136)
+template <typename XT>
+__global__ void k_prolong(int64_t n, const uint32_t *__restrict__ agg_p, const XT *__restrict__ xc,
+                          XT inv_relax, XT *__restrict__ x) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t a = agg_p[i];
+    const XT ref = a < kIsolated ? xc[a] : XT(0);
+    x[i] = x[i] + ref * inv_relax;
+  }
+}
+
+template <typename T, typename U>
+__global__ void k_convert(int64_t n, const T *src, U *dst) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = (U)src[i];
+}
+
+}  // namespace lgx
+
+// ===========================================================================
+// Hierarchy
+// ===========================================================================
+struct lgx_amg_level {
+  lgx::Csr own;                      // natural-order matrix (levels >= 1)
+  const lgx::Csr *a = nullptr;       // natural-order matrix of this level
+  lgx::AggResult agg;                // this level -> next (non-coarsest levels)
+  std::unique_ptr<lgx_colouring> col;  // smoother colouring and permuted matrix
+  lgx::DBuf<uint32_t> agg_p;         // permuted fine -> permuted coarse
+  lgx::DBuf<int64_t> rptr;           // permuted coarse row -> fine rows (permuted)
+  lgx::DBuf<int32_t> rlist;
+  lgx::DBuf<double> b64, x64, r64;   // cycle vectors (permuted order)
+  lgx::DBuf<float> b32, x32, r32;
+};
+
+struct lgx_amg {
+  lgx_amg_params p{};
+  std::vector<std::unique_ptr<lgx_amg_level>> lv;
+  lgx::DBuf<double> inv;             // dense inverse of the coarsest matrix
+  int64_t stats[32][5] = {};
+  lgx::DBuf<double> nat_b, nat_x;    // natural-order staging for lgx_amg_vcycle
+  bool f32 = false;
+};
+
+namespace lgx {
+
+int64_t amg_partitions(int64_t n, const lgx_amg_params &p) {
+  int64_t parts = p.partition_size > 0 ? n / p.partition_size : 1;
+  if (parts < 1) parts = 1;
+  if (parts > p.max_partitions) parts = p.max_partitions;
+  return parts;
+}
+
+static lgx_status amg_build(const lgx_matrix *m, const lgx_amg_params &p,
+                            const lgx_colouring *finest_colouring, cudaStream_t s, lgx_amg &h) {
+  h.p = p;
+  h.f32 = p.cycle_f32 != 0;
+  auto l0 = std::make_unique<lgx_amg_level>();
+  l0->a = &m->csr;
+  h.lv.push_back(std::move(l0));
+  bool aggressive = false;
+  for (int64_t level = 0;; ++level) {
+    lgx_amg_level &fine = *h.lv[level];
+    const Csr &a = *fine.a;
+    DBuf<uint8_t> dep, inf, iso;
+    LGX_CHECK(dep.alloc(a.nnz));
+    LGX_CHECK(inf.alloc(a.nnz));
+    LGX_CHECK(iso.alloc(a.n));
+    LGX_CHECK(strength(a, aggressive ? p.aggressive_threshold : p.strong_threshold, dep.p, inf.p,
+                       iso.p, s));
+    LGX_CHECK(aggregate(a, dep.p, inf.p, iso.p, p.min_aggregate_size, p.max_aggregate_size,
+                        amg_partitions(a.n, p), aggressive, s, fine.agg));
+    if (level < 32)
+      for (int k = 0; k < 5; ++k) h.stats[level][k] = fine.agg.stats[k];
+    if (fine.agg.ncoarse == 0 && a.n > 0)
+      return fail(LGX_ERR_INVALID, "aggregation produced no aggregates (all rows isolated)");
+    auto coarse = std::make_unique<lgx_amg_level>();
+    LGX_CHECK(galerkin(a, fine.agg, p.coarse_f32, s, coarse->own));
+    coarse->a = &coarse->own;
+    const int64_t fsize = a.n, csize = coarse->own.n;
+    h.lv.push_back(std::move(coarse));
+    // level_action (hierarchy/wright.hpp:120-143)
+    bool stop = false;
+    if (csize < p.min_coarsen_size) {
+      stop = true;
+    } else if (level + 1 >= p.max_level_num) {
+      stop = true;
+    } else if (p.min_coarsen_factor * (double)csize > (double)fsize) {
+      if (aggressive) stop = true; else aggressive = true;
+    }
+    if (stop || level + 2 >= 32) break;
+  }
+  const int64_t L = (int64_t)h.lv.size();
+  // smoother colourings (all but the coarsest level)
+  for (int64_t l = 0; l + 1 < L; ++l) {
+    lgx_amg_level &lv = *h.lv[l];
+    lv.col = std::make_unique<lgx_colouring>();
+    if (l == 0 && finest_colouring) {
+      LGX_CHECK(colouring_build(*lv.a, finest_colouring->colour.p, finest_colouring->ncolours, s,
+                                *lv.col));
+    } else {
+      int32_t nc = 0;
+      LGX_CHECK(colouring_jp(*lv.a, p.colour_seed + (uint64_t)l, s, lv.col->colour, nc));
+      LGX_CHECK(colouring_build(*lv.a, lv.col->colour.p, nc, s, *lv.col));
+    }
+    if (h.f32) LGX_CHECK(colouring_make_f32(*lv.col, s));
+  }
+  // transfers in permuted spaces
+  for (int64_t l = 0; l + 1 < L; ++l) {
+    lgx_amg_level &f = *h.lv[l];
+    lgx_amg_level &c = *h.lv[l + 1];
+    const int32_t *perm_c = c.col ? c.col->perm.p : nullptr;
+    const int32_t *iperm_c = c.col ? c.col->iperm.p : nullptr;
+    const int64_t nf = f.a->n, nc = c.a->n;
+    LGX_CHECK(f.agg_p.alloc(nf));
+    k_agg_permute<<<std::min<int64_t>(grid_for(nf, 256), 16384), 256, 0, s>>>(
+      nf, f.col->perm.p, f.agg.agg.p, iperm_c, f.agg_p.p);
+    LGX_LAUNCH_CHECK();
+    DBuf<int64_t> len;
+    LGX_CHECK(len.alloc(nc));
+    LGX_CHECK(f.rptr.alloc(nc + 1));
+    if (nc) {
+      k_rlist_len<<<std::min<int64_t>(grid_for(nc, 256), 16384), 256, 0, s>>>(
+        nc, perm_c, f.agg.list_ptr.p, len.p);
+      LGX_LAUNCH_CHECK();
+    }
+    LGX_CHECK(inclusive_offsets(nc, len.p, f.rptr.p, s));
+    const int64_t total = f.agg.list.n;
+    LGX_CHECK(f.rlist.alloc(total));
+    if (nc) {
+      k_rlist_fill<<<std::min<int64_t>(grid_for(nc, 256), 16384), 256, 0, s>>>(
+        nc, perm_c, f.agg.list_ptr.p, f.agg.list.p, f.col->iperm.p, f.rptr.p, f.rlist.p);
+      LGX_LAUNCH_CHECK();
+    }
+    LGX_CUDA(cudaStreamSynchronize(s));
+  }
+  // cycle vectors
+  for (int64_t l = 0; l < L; ++l) {
+    lgx_amg_level &lv = *h.lv[l];
+    const int64_t n = lv.a->n;
+    if (h.f32) {
+      LGX_CHECK(lv.b32.alloc(n));
+      LGX_CHECK(lv.x32.alloc(n));
+      LGX_CHECK(lv.r32.alloc(n));
+    } else {
+      LGX_CHECK(lv.b64.alloc(n));
+      LGX_CHECK(lv.x64.alloc(n));
+      LGX_CHECK(lv.r64.alloc(n));
+    }
+  }
+  return dense_inverse(*h.lv[L - 1]->a, s, h.inv);
+}
+
+// Smoother sweep / residual on one level with the level's value storage:
+// double cycles read the stored values (double or float), float cycles read
+// float values (the stored floats or the float copy of a double level).
+template <typename XT>
+static lgx_status level_sor(lgx_amg_level &lv, const lgx_amg &h, int forward, const XT *b, XT *x,
+                            cudaStream_t s) {
+  const lgx_colouring &c = *lv.col;
+  const double relax = h.p.smoother_relax;
+  const int ultra = h.p.smoother_ultra;
+  if constexpr (sizeof(XT) == 8) {
+    if (c.pcsr.storage == LGX_F64)
+      return mc_sor_sweep<double, double>(c, c.pcsr.v64.p, relax, forward, ultra, b, x, s);
+    return mc_sor_sweep<float, double>(c, c.pcsr.v32.p, relax, forward, ultra, b, x, s);
+  } else {
+    const float *v = c.pcsr.storage == LGX_F32 ? c.pcsr.v32.p : c.pv32.p;
+    return mc_sor_sweep<float, float>(c, v, relax, forward, ultra, b, x, s);
+  }
+}
+
+template <typename XT>
+static lgx_status level_residual(lgx_amg_level &lv, const XT *b, const XT *x, XT *r,
+                                 cudaStream_t s) {
+  const lgx_colouring &c = *lv.col;
+  if constexpr (sizeof(XT) == 8) {
+    if (c.pcsr.storage == LGX_F64)
+      return csr_residual<double, double>(c.pcsr, c.pcsr.v64.p, b, x, r, nullptr, nullptr,
+                                          nullptr, s);
+    return csr_residual<float, double>(c.pcsr, c.pcsr.v32.p, b, x, r, nullptr, nullptr, nullptr,
+                                       s);
+  } else {
+    const float *v = c.pcsr.storage == LGX_F32 ? c.pcsr.v32.p : c.pv32.p;
+    return csr_residual<float, float>(c.pcsr, v, b, x, r, nullptr, nullptr, nullptr, s);
+  }
+}
+
+template <typename XT>
+static XT *level_vec(lgx_amg_level &lv, int which) {
+  if constexpr (sizeof(XT) == 8) {
+    return which == 0 ? (XT *)lv.b64.p : which == 1 ? (XT *)lv.x64.p : (XT *)lv.r64.p;
+  } else {
+    return which == 0 ? (XT *)lv.b32.p : which == 1 ? (XT *)lv.x32.p : (XT *)lv.r32.p;
+  }
+}
+
+// V-cycle in permuted space (multigrid/solver.hpp:56-176, REGULAR cycle with
+// one iteration): forward SOR from zero, residual restricted by aggregate
+// sums, dense coarsest solve, correction injected with 1/relax, backward SOR
+// in place.  b0/x0 are the finest-level vectors (permuted order).
+template <typename XT>
+static lgx_status vcycle_impl(lgx_amg &h, const XT *b0, XT *x0, cudaStream_t s) {
+  const int64_t L = (int64_t)h.lv.size();
+  for (int64_t l = 0; l + 1 < L; ++l) {
+    lgx_amg_level &lv = *h.lv[l];
+    const XT *b = l == 0 ? b0 : level_vec<XT>(lv, 0);
+    XT *x = l == 0 ? x0 : level_vec<XT>(lv, 1);
+    const int64_t n = lv.a->n;
+    if (n == 0) continue;
+    LGX_CUDA(cudaMemsetAsync(x, 0, sizeof(XT) * n, s));
+    LGX_CHECK(level_sor<XT>(lv, h, 1, b, x, s));
+    LGX_CHECK(level_residual<XT>(lv, b, x, level_vec<XT>(lv, 2), s));
+    lgx_amg_level &cv = *h.lv[l + 1];
+    const int64_t nc = cv.a->n;
+    if (nc) {
+      k_restrict<XT><<<std::min<int64_t>(grid_for(nc, 128), 65535), 128, 0, s>>>(
+        nc, lv.rptr.p, lv.rlist.p, level_vec<XT>(lv, 2), level_vec<XT>(cv, 0));
+      LGX_LAUNCH_CHECK();
+    }
+  }
+  {
+    lgx_amg_level &last = *h.lv[L - 1];
+    const int64_t nc = last.a->n;
+    if (nc) {
+      XT *bl = L == 1 ? const_cast<XT *>(b0) : level_vec<XT>(last, 0);
+      XT *xl = L == 1 ? x0 : level_vec<XT>(last, 1);
+      k_dense_apply<XT><<<(unsigned)std::min<int64_t>(grid_for(nc * 32, 256), 4096), 256, 0, s>>>(
+        nc, h.inv.p, bl, xl);
+      LGX_LAUNCH_CHECK();
+    }
+  }
+  const XT inv_relax = (XT)(1.0 / h.p.relax);
+  for (int64_t l = L - 2; l >= 0; --l) {
+    lgx_amg_level &lv = *h.lv[l];
+    const XT *b = l == 0 ? b0 : level_vec<XT>(lv, 0);
+    XT *x = l == 0 ? x0 : level_vec<XT>(lv, 1);
+    const int64_t n = lv.a->n;
+    if (n == 0) continue;
+    k_prolong<XT><<<std::min<int64_t>(grid_for(n, 256), 65535), 256, 0, s>>>(
+      n, lv.agg_p.p, level_vec<XT>(*h.lv[l + 1], 1), inv_relax, x);
+    LGX_LAUNCH_CHECK();
+    LGX_CHECK(level_sor<XT>(lv, h, 0, b, x, s));
+  }
+  return LGX_OK;
+}
+
+const Csr &amg_finest_permuted(const lgx_amg &h) { return h.lv[0]->col->pcsr; }
+lgx_colouring *amg_finest_colouring(lgx_amg &h) { return h.lv[0]->col.get(); }
+
+// Applies the preconditioner in the finest level's permuted space with
+// double vectors (the outer Krylov vectors).
+lgx_status amg_apply_permuted(lgx_amg &h, const double *b, double *x, cudaStream_t s) {
+  lgx_amg_level &l0 = *h.lv[0];
+  const int64_t n = l0.a->n;
+  if (!h.f32) return vcycle_impl<double>(h, b, x, s);
+  k_convert<double, float><<<std::min<int64_t>(grid_for(n, 256), 16384), 256, 0, s>>>(
+    n, b, l0.b32.p);
+  LGX_LAUNCH_CHECK();
+  LGX_CHECK(vcycle_impl<float>(h, l0.b32.p, l0.x32.p, s));
+  k_convert<float, double><<<std::min<int64_t>(grid_for(n, 256), 16384), 256, 0, s>>>(
+    n, l0.x32.p, x);
+  LGX_LAUNCH_CHECK();
+  return LGX_OK;
+}
+
+}  // namespace lgx
+
+using namespace lgx;
+
+extern "C" {
+
+void lgx_amg_default_params(lgx_amg_params *p) {
+  if (!p) return;
+  p->min_aggregate_size = 6;
+  p->max_aggregate_size = 9;
+  p->partition_size = 4096;
+  p->max_partitions = 1 << 30;
+  p->strong_threshold = 1.0 / 3.0;
+  p->aggressive_threshold = 1.0 / 3.0;
+  p->max_level_num = 16;
+  p->min_coarsen_size = 2000;
+  p->min_coarsen_factor = 1.2;
+  p->coarse_f32 = 0;
+  p->cycle_f32 = 0;
+  p->relax = 1.0;
+  p->smoother_relax = 1.0;
+  p->smoother_ultra = 0;
+  p->colour_seed = 0x5eed;
+}
+
+lgx_status lgx_amg_setup(const lgx_matrix *a, const lgx_amg_params *p,
+                         const lgx_colouring *finest_colouring, lgx_stream stream,
+                         lgx_amg **out) {
+  if (!a || !p || !out) return fail(LGX_ERR_INVALID, "null argument");
+  if (a->kind != LGX_MATRIX_CSR)
+    return fail(LGX_ERR_UNSUPPORTED, "AMG setup needs a CSR matrix (assemble stencils first)");
+  if (finest_colouring && finest_colouring->n != a->n)
+    return fail(LGX_ERR_INVALID, "finest colouring does not match the matrix");
+  if (p->max_aggregate_size > 64 || p->min_aggregate_size < 1 ||
+      p->min_aggregate_size > p->max_aggregate_size)
+    return fail(LGX_ERR_INVALID, "aggregate sizes must satisfy 1 <= min <= max <= 64");
+  if (!(p->relax != 0.0)) return fail(LGX_ERR_INVALID, "relax must be non-zero");
+  auto *h = new lgx_amg();
+  lgx_status st = amg_build(a, *p, finest_colouring, stream, *h);
+  if (st != LGX_OK) {
+    delete h;
+    return st;
+  }
+  *out = h;
+  return LGX_OK;
+}
+
+lgx_status lgx_amg_destroy(lgx_amg *h) {
+  delete h;
+  return LGX_OK;
+}
+
+lgx_status lgx_amg_info(const lgx_amg *h, int64_t *nlevels, int64_t *rows, int64_t *nnz,
+                        int64_t max_levels) {
+  if (!h) return fail(LGX_ERR_INVALID, "null hierarchy");
+  const int64_t L = (int64_t)h->lv.size();
+  if (nlevels) *nlevels = L;
+  for (int64_t l = 0; l < L && l < max_levels; ++l) {
+    if (rows) rows[l] = h->lv[l]->a->n;
+    if (nnz) nnz[l] = h->lv[l]->a->nnz;
+  }
+  return LGX_OK;
+}
+
+lgx_status lgx_amg_level_download(const lgx_amg *h, int64_t level, int64_t *h_rowptr,
+                                  int32_t *h_col, double *h_val, uint32_t *h_agg,
+                                  lgx_stream stream) {
+  if (!h || level < 0 || level >= (int64_t)h->lv.size())
+    return fail(LGX_ERR_INVALID, "bad level");
+  const lgx_amg_level &lv = *h->lv[level];
+  const Csr &c = *lv.a;
+  if (h_rowptr)
+    LGX_CUDA(cudaMemcpyAsync(h_rowptr, c.rowptr.p, sizeof(int64_t) * (c.n + 1),
+                             cudaMemcpyDeviceToHost, stream));
+  if (h_col && c.nnz)
+    LGX_CUDA(cudaMemcpyAsync(h_col, c.col.p, sizeof(int32_t) * c.nnz, cudaMemcpyDeviceToHost,
+                             stream));
+  if (h_val && c.nnz) {
+    if (c.storage == LGX_F64) {
+      LGX_CUDA(cudaMemcpyAsync(h_val, c.v64.p, sizeof(double) * c.nnz, cudaMemcpyDeviceToHost,
+                               stream));
+    } else {
+      DBuf<double> tmp;
+      LGX_CHECK(tmp.alloc(c.nnz));
+      k_convert<float, double><<<std::min<int64_t>(grid_for(c.nnz, 256), 16384), 256, 0,
+                                 stream>>>(c.nnz, c.v32.p, tmp.p);
+      LGX_LAUNCH_CHECK();
+      LGX_CUDA(cudaMemcpyAsync(h_val, tmp.p, sizeof(double) * c.nnz, cudaMemcpyDeviceToHost,
+                               stream));
+      LGX_CUDA(cudaStreamSynchronize(stream));
+    }
+  }
+  if (h_agg) {
+    if (level + 1 >= (int64_t)h->lv.size())
+      return fail(LGX_ERR_INVALID, "the coarsest level has no aggregate map");
+    LGX_CUDA(cudaMemcpyAsync(h_agg, lv.agg.agg.p, sizeof(uint32_t) * c.n, cudaMemcpyDeviceToHost,
+                             stream));
+  }
+  LGX_CUDA(cudaStreamSynchronize(stream));
+  return LGX_OK;
+}
+
+lgx_status lgx_amg_vcycle(lgx_amg *h, const double *d_b, double *d_x, lgx_stream stream) {
+  if (!h || !d_b || !d_x) return fail(LGX_ERR_INVALID, "null argument");
+  lgx_amg_level &l0 = *h->lv[0];
+  const int64_t n = l0.a->n;
+  if (!h->nat_b.p) {
+    LGX_CHECK(h->nat_b.alloc(n));
+    LGX_CHECK(h->nat_x.alloc(n));
+  }
+  const int32_t *perm = h->lv.size() > 1 ? l0.col->perm.p : nullptr;
+  if (perm) {
+    LGX_CHECK(gather<double, double>(n, perm, d_b, h->nat_b.p, stream));
+    LGX_CHECK(amg_apply_permuted(*h, h->nat_b.p, h->nat_x.p, stream));
+    return scatter<double, double>(n, perm, h->nat_x.p, d_x, stream);
+  }
+  return amg_apply_permuted(*h, d_b, d_x, stream);
+}
+
+lgx_status lgx_amg_strength(const lgx_matrix *a, double theta, uint8_t *d_depends,
+                            uint8_t *d_influences, uint8_t *d_isolated, lgx_stream stream) {
+  if (!a || !d_depends || !d_influences || !d_isolated)
+    return fail(LGX_ERR_INVALID, "null argument");
+  if (a->kind != LGX_MATRIX_CSR) return fail(LGX_ERR_UNSUPPORTED, "strength needs a CSR matrix");
+  return strength(a->csr, theta, d_depends, d_influences, d_isolated, stream);
+}
+
+lgx_status lgx_amg_aggregate(const lgx_matrix *a, const uint8_t *d_depends,
+                             const uint8_t *d_influences, const uint8_t *d_isolated,
+                             int32_t min_size, int32_t max_size, int64_t nparts, int aggressive,
+                             uint32_t *d_agg, int64_t *ncoarse, lgx_stream stream) {
+  if (!a || !d_depends || !d_influences || !d_isolated || !d_agg)
+    return fail(LGX_ERR_INVALID, "null argument");
+  if (a->kind != LGX_MATRIX_CSR)
+    return fail(LGX_ERR_UNSUPPORTED, "aggregation needs a CSR matrix");
+  if (max_size > 64 || min_size < 1 || min_size > max_size)
+    return fail(LGX_ERR_INVALID, "aggregate sizes must satisfy 1 <= min <= max <= 64");
+  AggResult r;
+  LGX_CHECK(aggregate(a->csr, d_depends, d_influences, d_isolated, min_size, max_size, nparts,
+                      aggressive, stream, r, d_agg));
+  if (ncoarse) *ncoarse = r.ncoarse;
+  return LGX_OK;
+}
+
+}  // extern "C"

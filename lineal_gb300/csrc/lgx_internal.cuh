@@ -1,0 +1,247 @@
+// Internal definitions shared by the lineal_gb300 CUDA sources.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "lineal_gb300.h"
+
+namespace lgx {
+
+// ---- error handling -----------------------------------------------------
+void set_error(const std::string &msg);
+lgx_status fail(lgx_status s, const std::string &msg);
+lgx_status cuda_fail(cudaError_t e, const char *what);
+
+#define LGX_CUDA(...)                                                          \
+  do {                                                                         \
+    cudaError_t lgx_e_ = (__VA_ARGS__);                                        \
+    if (lgx_e_ != cudaSuccess) return ::lgx::cuda_fail(lgx_e_, #__VA_ARGS__); \
+  } while (0)
+#define LGX_CHECK(...)                           \
+  do {                                           \
+    lgx_status lgx_s_ = (__VA_ARGS__);           \
+    if (lgx_s_ != LGX_OK) return lgx_s_;         \
+  } while (0)
+void count_launch();
+// Every kernel launch site is followed by this check, which also counts the
+// launch (lgx_kernel_launches).
+#define LGX_LAUNCH_CHECK()     \
+  do {                         \
+    ::lgx::count_launch();     \
+    LGX_CUDA(cudaGetLastError()); \
+  } while (0)
+
+// ---- device buffers -----------------------------------------------------
+template <typename T>
+struct DBuf {
+  T *p = nullptr;
+  int64_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  DBuf(DBuf &&o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DBuf &operator=(DBuf &&o) noexcept {
+    if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+    return *this;
+  }
+  ~DBuf() { release(); }
+  lgx_status alloc(int64_t count) {
+    release();
+    if (count <= 0) count = 1;
+    cudaError_t e = cudaMalloc(&p, sizeof(T) * (size_t)count);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      cudaGetLastError();
+      return fail(LGX_ERR_NOMEM, "device allocation of " + std::to_string(sizeof(T) * count) +
+                                     " bytes failed: " + cudaGetErrorString(e));
+    }
+    n = count;
+    return LGX_OK;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+constexpr uint32_t kUnaggregated = 0xFFFFFFFFu;
+constexpr uint32_t kIsolated = 0xFFFFFFFEu;
+
+// ---- matrices -------------------------------------------------------------
+struct Csr {
+  int64_t n = 0, nnz = 0;
+  int64_t max_row = 0;
+  int symmetric = 0;
+  lgx_dtype storage = LGX_F64;
+  DBuf<int64_t> rowptr;
+  DBuf<int32_t> col;
+  DBuf<double> v64;
+  DBuf<float> v32;
+};
+
+struct StencilDesc {
+  int64_t dims[3];
+  double q[3];
+  double coeffs[4];
+  double conn[48];
+  double sol_start, sol_end;
+  int zero_to_one;
+  int lookup;
+  const uint8_t *mat;
+  const double *k;
+};
+
+}  // namespace lgx
+
+struct lgx_matrix {
+  int kind = LGX_MATRIX_CSR;
+  int64_t n = 0;
+  int64_t nnz = 0;
+  int symmetric = 1;
+  lgx::Csr csr;                 // CSR kinds
+  lgx::StencilDesc st{};        // stencil kinds
+  lgx::DBuf<uint8_t> mat;       // stencil lookup materials (owned copy)
+  lgx::DBuf<double> k;          // stencil value conductivities (owned copy)
+  lgx::DBuf<double> diag;       // cached diagonal (lazily computed)
+};
+
+// Colour-permuted copy of a CSR matrix used by the multicolour smoothers.
+// Row r' of the permuted matrix is row perm[r'] of the original; its entries
+// keep the original column order (columns mapped through iperm) so that the
+// row sums are formed in exactly the order of the original row.
+struct lgx_colouring {
+  int64_t n = 0;
+  int32_t ncolours = 0;
+  std::vector<int64_t> offsets;  // host: colour c occupies rows [offsets[c], offsets[c+1])
+  lgx::DBuf<int32_t> colour;     // natural order
+  lgx::DBuf<int32_t> perm;       // permuted -> natural
+  lgx::DBuf<int32_t> iperm;      // natural -> permuted
+  lgx::Csr pcsr;                 // permuted matrix (values in the source storage type)
+  lgx::DBuf<float> pv32;         // float copy of the permuted values (float cycles)
+  lgx::DBuf<double> work_b, work_x;  // natural<->permuted staging for the public sweep API
+};
+
+namespace lgx {
+
+// ---- kernels exposed across translation units --------------------------
+// Deterministic two-stage reductions.  `partials` needs reduce_blocks(n)
+// doubles; `counter` one zero-initialised unsigned int.
+constexpr int kReduceThreads = 256;
+int reduce_blocks(int64_t n);
+
+lgx_status csr_from_device(int64_t n, int64_t nnz, const int64_t *rowptr, const int32_t *col,
+                           const double *val, int symmetric, lgx_dtype storage,
+                           cudaStream_t s, Csr &out);
+lgx_status csr_compute_max_row(Csr &a, cudaStream_t s);
+
+// y = A x for CSR with value type VT and vector type XT (accumulation in XT)
+template <typename VT, typename XT>
+lgx_status csr_spmv(const Csr &a, const VT *val, const XT *x, XT *y, cudaStream_t s);
+// r = b - A x; if norm != nullptr, norm[0] = ||r||^2 (double, deterministic)
+template <typename VT, typename XT>
+lgx_status csr_residual(const Csr &a, const VT *val, const XT *b, const XT *x, XT *r,
+                        double *norm, double *partials, unsigned *counter, cudaStream_t s);
+
+lgx_status stencil_spmv(const StencilDesc &st, const double *x, double *y, cudaStream_t s);
+lgx_status stencil_residual(const StencilDesc &st, const double *b, const double *x, double *r,
+                            double *norm, double *partials, unsigned *counter, cudaStream_t s);
+lgx_status stencil_diagonal(const StencilDesc &st, double *d, cudaStream_t s);
+lgx_status matrix_diagonal(lgx_matrix *a, cudaStream_t s, const double **out);
+
+// Generic matrix application for the Krylov drivers (CSR or stencil).
+lgx_status matrix_spmv(const lgx_matrix *a, const double *x, double *y, cudaStream_t s);
+lgx_status matrix_residual(const lgx_matrix *a, const double *b, const double *x, double *r,
+                           double *norm, double *partials, unsigned *counter, cudaStream_t s);
+
+lgx_status dot(int64_t n, const double *a, const double *b, double *out, double *partials,
+               unsigned *counter, cudaStream_t s);
+
+// colouring helpers
+lgx_status colouring_build(const Csr &a, const int32_t *d_colour, int32_t ncolours,
+                           cudaStream_t s, lgx_colouring &out);
+lgx_status colouring_jp(const Csr &a, uint64_t seed, cudaStream_t s, DBuf<int32_t> &colour,
+                        int32_t &ncolours);
+// One multicolour sweep on the permuted matrix (vectors in permuted order,
+// in place).  VT value type, XT vector/arithmetic type.
+template <typename VT, typename XT>
+lgx_status mc_sor_sweep(const lgx_colouring &c, const VT *val, double relax, int forward,
+                        int ultra, const XT *b, XT *x, cudaStream_t s);
+
+lgx_status jacobi_csr(const Csr &a, double relax, const double *x_in, double *x_out,
+                      const double *b, cudaStream_t s);
+lgx_status jacobi_diag_zero(int64_t n, const double *d, double relax, const double *b, double *x,
+                            cudaStream_t s);
+lgx_status colouring_make_f32(lgx_colouring &c, cudaStream_t s);
+lgx_status colouring_sweep_natural(lgx_colouring &c, double relax, int forward, int ultra,
+                                   const double *x_in, double *x_out, const double *b,
+                                   cudaStream_t s);
+
+// permutation gathers
+template <typename T, typename U>
+lgx_status gather(int64_t n, const int32_t *idx, const T *src, U *dst, cudaStream_t s);
+template <typename T, typename U>
+lgx_status scatter(int64_t n, const int32_t *idx, const T *src, U *dst, cudaStream_t s);
+
+inline unsigned grid_for(int64_t n, int threads) {
+  return (unsigned)((n + threads - 1) / threads);
+}
+
+lgx_status inclusive_offsets(int64_t n, const int64_t *in, int64_t *out, cudaStream_t s);
+// partial-sum slots needed by the fused reductions of the row-block kernels
+int64_t csr_partials(int64_t n);
+int64_t matrix_partials(const lgx_matrix *a);
+lgx_status stencil_ensure(lgx_matrix *a, cudaStream_t s);
+
+// ---- device helpers ------------------------------------------------------
+template <int T>
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+  sh[threadIdx.x] = v;
+  __syncthreads();
+#pragma unroll
+  for (int s = T / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  const double r = sh[0];
+  __syncthreads();
+  return r;
+}
+
+// Deterministic grid reduction.  Every block calls it with its threads'
+// values; block `bid` of `nblocks` stores its (fixed-shape tree) sum in
+// partials[bid]; the last block to arrive sums the partials in index order
+// (fixed strided split + tree), stores the total in *total (thread 0) and
+// re-arms the counter.  Returns true in that last block only.  Requires
+// blockDim.x == T (a power of two).
+template <int T>
+__device__ __forceinline__ bool grid_reduce(double v, unsigned bid, unsigned nblocks,
+                                            double *partials, unsigned *counter, double *total) {
+  __shared__ double sh[T];
+  __shared__ bool last;
+  const double bs = block_sum<T>(v, sh);
+  if (threadIdx.x == 0) {
+    partials[bid] = bs;
+    __threadfence();
+    const unsigned done = atomicAdd(counter, 1u);
+    last = (done == nblocks - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  double acc = 0.0;
+  for (unsigned b = threadIdx.x; b < nblocks; b += T) acc += ((volatile double *)partials)[b];
+  const double t = block_sum<T>(acc, sh);
+  if (threadIdx.x == 0) {
+    *total = t;
+    *counter = 0;
+  }
+  return true;
+}
+
+}  // namespace lgx

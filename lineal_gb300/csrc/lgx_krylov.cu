@@ -1,0 +1,530 @@
+// Krylov drivers: preconditioned CG (conjugate-gradients/solver.hpp:24-225)
+// and BiCGStab (bicgstab/solver.hpp:25-263), run as run_iterative_solver does
+// (runner.hpp:17-84).  Solver scalars (rho, alpha, beta, omega, ||r||^2) live
+// in device memory and are produced by the last block of each deterministic
+// reduction, so no scalar makes a host round trip; the host reads ||r||^2 once
+// per iteration to decide termination.
+//
+// With an SSOR or AMG preconditioner on a CSR matrix the whole iteration runs
+// in the colour-permuted ordering of the finest level (the smoother's native
+// layout); b and x are permuted on entry and exit.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <memory>
+#include <vector>
+
+#include "lgx_internal.cuh"
+
+namespace lgx {
+lgx_status amg_apply_permuted(lgx_amg &h, const double *b, double *x, cudaStream_t s);
+const Csr &amg_finest_permuted(const lgx_amg &h);
+lgx_colouring *amg_finest_colouring(lgx_amg &h);
+}  // namespace lgx
+
+namespace lgx {
+
+struct KScalars {
+  double rho, rho_old, alpha, beta, omega, res2, den, tmp;
+  int flag;  // bit 0: breakdown, bit 1: non-finite
+};
+
+constexpr int kKT = 256;
+
+__device__ __forceinline__ void set_flags(KScalars *ks, double num, double den) {
+  if (!isfinite(num) || !isfinite(den)) ks->flag |= 2;
+  if (den == 0.0) ks->flag |= 1;
+}
+
+enum Post { POST_ALPHA = 0, POST_RHO_BETA = 1, POST_OMEGA = 2 };
+
+// dot(a, b) with a post operation in the last block
+__global__ void __launch_bounds__(kKT)
+  k_dot_post(int64_t n, const double *__restrict__ a, const double *__restrict__ b, int post,
+             KScalars *ks, double *partials, unsigned *counter) {
+  double s = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    s = fma(a[i], b[i], s);
+  double t;
+  if (grid_reduce<kKT>(s, blockIdx.x, gridDim.x, partials, counter, &t) && threadIdx.x == 0) {
+    if (post == POST_ALPHA) {  // alpha = rho / t
+      set_flags(ks, ks->rho, t);
+      ks->den = t;
+      ks->alpha = ks->rho / t;
+    } else if (post == POST_RHO_BETA) {  // rho_old = rho; rho = t; beta = rho / rho_old
+      ks->rho_old = ks->rho;
+      ks->rho = t;
+      set_flags(ks, t, ks->rho_old);
+      ks->beta = t / ks->rho_old;
+    }
+  }
+}
+
+// two dots in one pass: t1 = a.b, t2 = c.d
+__global__ void __launch_bounds__(kKT)
+  k_dot2_post(int64_t n, const double *__restrict__ a, const double *__restrict__ b,
+              const double *__restrict__ c, const double *__restrict__ d, int post, KScalars *ks,
+              double *partials, double *partials2, unsigned *counter, unsigned *counter2) {
+  double s1 = 0.0, s2 = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    s1 = fma(a[i], b[i], s1);
+    s2 = fma(c[i], d[i], s2);
+  }
+  double t1, t2;
+  const bool l1 = grid_reduce<kKT>(s1, blockIdx.x, gridDim.x, partials, counter, &t1);
+  if (l1 && threadIdx.x == 0) ks->tmp = t1;
+  const bool l2 = grid_reduce<kKT>(s2, blockIdx.x, gridDim.x, partials2, counter2, &t2);
+  if (l2 && threadIdx.x == 0) {
+    __threadfence();
+    const double u1 = ((volatile KScalars *)ks)->tmp;
+    if (post == POST_OMEGA) {  // omega = (t.r) / (t.t)
+      set_flags(ks, u1, t2);
+      ks->omega = u1 / t2;
+    }
+  }
+}
+
+// x += alpha p ; r -= alpha q ; res2 = ||r||^2 (CG, solver.hpp:87, 93-94)
+// plain: also rho_old = rho, rho = res2, beta = rho / rho_old (solver.hpp:105-107)
+__global__ void __launch_bounds__(kKT)
+  k_cg_update(int64_t n, KScalars *ks, const double *__restrict__ p, const double *__restrict__ q,
+              double *__restrict__ x, double *__restrict__ r, int update_r, int plain,
+              double *partials, unsigned *counter) {
+  const double alpha = ks->alpha;
+  double s = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] = fma(p[i], alpha, x[i]);
+    if (update_r) {
+      const double rv = fma(-alpha, q[i], r[i]);
+      r[i] = rv;
+      s = fma(rv, rv, s);
+    }
+  }
+  if (!update_r) return;
+  double t;
+  if (grid_reduce<kKT>(s, blockIdx.x, gridDim.x, partials, counter, &t) && threadIdx.x == 0) {
+    ks->res2 = t;
+    if (!isfinite(t)) ks->flag |= 2;
+    if (plain) {
+      ks->rho_old = ks->rho;
+      ks->rho = t;
+      ks->beta = t / ks->rho_old;
+    }
+  }
+}
+
+// after a true-residual recomputation into ks->res2 (plain CG bookkeeping)
+__global__ void k_cg_plain_rho(KScalars *ks) {
+  ks->rho_old = ks->rho;
+  ks->rho = ks->res2;
+  ks->beta = ks->res2 / ks->rho_old;
+}
+
+// p = z + beta p
+__global__ void k_xpby(int64_t n, const KScalars *ks, const double *__restrict__ z,
+                       double *__restrict__ p) {
+  const double beta = ks->beta;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = fma(p[i], beta, z[i]);
+}
+
+// x += s y with s = ks->alpha (which == 0) or ks->omega (which == 1)
+__global__ void k_axpy_ks(int64_t n, const KScalars *ks, int which, const double *__restrict__ y,
+                          double *__restrict__ x) {
+  const double s = which == 0 ? ks->alpha : ks->omega;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = fma(y[i], s, x[i]);
+}
+
+// BiCGStab: r -= omega t (unless recomputed); rho_new = r.r0, res2 = r.r;
+// beta = (rho_new / rho) * (alpha / omega); p = r + beta (p - omega v)
+__global__ void __launch_bounds__(kKT)
+  k_bicg_r(int64_t n, KScalars *ks, int update_r, const double *__restrict__ t,
+           double *__restrict__ r, const double *__restrict__ r0, double *partials,
+           double *partials2, unsigned *counter, unsigned *counter2) {
+  const double omega = ks->omega;
+  double s1 = 0.0, s2 = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double rv = r[i];
+    if (update_r) {
+      rv = fma(-omega, t[i], rv);
+      r[i] = rv;
+    }
+    s1 = fma(rv, r0[i], s1);
+    s2 = fma(rv, rv, s2);
+  }
+  double t1, t2;
+  const bool l1 = grid_reduce<kKT>(s1, blockIdx.x, gridDim.x, partials, counter, &t1);
+  if (l1 && threadIdx.x == 0) ks->tmp = t1;
+  const bool l2 = grid_reduce<kKT>(s2, blockIdx.x, gridDim.x, partials2, counter2, &t2);
+  if (l2 && threadIdx.x == 0) {
+    __threadfence();
+    const double rho_new = ((volatile KScalars *)ks)->tmp;
+    ks->rho_old = ks->rho;
+    ks->rho = rho_new;
+    ks->res2 = t2;
+    set_flags(ks, rho_new, ks->omega);
+    if (ks->rho_old == 0.0) ks->flag |= 1;
+    ks->beta = (rho_new / ks->rho_old) * (ks->alpha / ks->omega);
+  }
+}
+
+__global__ void k_bicg_p(int64_t n, const KScalars *ks, const double *__restrict__ r,
+                         const double *__restrict__ v, double *__restrict__ p) {
+  const double beta = ks->beta, omega = ks->omega;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = fma(fma(-omega, v[i], p[i]), beta, r[i]);
+}
+
+// r = b - A x already computed with its norm: rho = res2 (BiCGStab init)
+__global__ void k_bicg_init(KScalars *ks) {
+  ks->rho = ks->res2;
+  ks->flag = 0;
+}
+
+// ---------------------------------------------------------------------------
+// Operator / preconditioner plumbing
+// ---------------------------------------------------------------------------
+struct Solver {
+  const lgx_matrix *m = nullptr;  // natural-order operator (when pcsr == nullptr)
+  const Csr *pcsr = nullptr;      // permuted CSR operator
+  const int32_t *perm = nullptr;  // permuted -> natural (when pcsr)
+  int precon = LGX_PRECON_NONE;
+  double relax = 1.0;
+  int ultra = 0;
+  lgx_colouring *col = nullptr;   // SSOR colouring (permuted space)
+  lgx_amg *amg = nullptr;
+  const double *diag = nullptr;   // Jacobi
+  int64_t n = 0;
+  cudaStream_t s = nullptr;
+  DBuf<double> partials, partials2;
+  DBuf<unsigned> counters;
+  DBuf<KScalars> ks;
+
+  lgx_status init() {
+    const int64_t slots = std::max<int64_t>(
+      {(int64_t)reduce_blocks(n), pcsr ? csr_partials(n) : matrix_partials(m), (int64_t)1});
+    LGX_CHECK(partials.alloc(slots));
+    LGX_CHECK(partials2.alloc(slots));
+    LGX_CHECK(counters.alloc(2));
+    LGX_CHECK(ks.alloc(1));
+    LGX_CUDA(cudaMemsetAsync(counters.p, 0, 2 * sizeof(unsigned), s));
+    LGX_CUDA(cudaMemsetAsync(ks.p, 0, sizeof(KScalars), s));
+    return LGX_OK;
+  }
+  lgx_status apply(const double *x, double *y) {
+    if (pcsr) {
+      if (pcsr->storage == LGX_F64) return csr_spmv<double, double>(*pcsr, pcsr->v64.p, x, y, s);
+      return csr_spmv<float, double>(*pcsr, pcsr->v32.p, x, y, s);
+    }
+    return matrix_spmv(m, x, y, s);
+  }
+  lgx_status residual(const double *b, const double *x, double *r, double *norm) {
+    if (pcsr) {
+      if (pcsr->storage == LGX_F64)
+        return csr_residual<double, double>(*pcsr, pcsr->v64.p, b, x, r, norm, partials.p,
+                                            counters.p, s);
+      return csr_residual<float, double>(*pcsr, pcsr->v32.p, b, x, r, norm, partials.p,
+                                         counters.p, s);
+    }
+    return matrix_residual(m, b, x, r, norm, partials.p, counters.p, s);
+  }
+  lgx_status precondition(const double *r, double *z) {
+    switch (precon) {
+      case LGX_PRECON_JACOBI: return jacobi_diag_zero(n, diag, relax, r, z, s);
+      case LGX_PRECON_SSOR: {
+        LGX_CUDA(cudaMemsetAsync(z, 0, sizeof(double) * n, s));
+        const Csr &p = col->pcsr;
+        if (p.storage == LGX_F64) {
+          LGX_CHECK(mc_sor_sweep<double, double>(*col, p.v64.p, relax, 1, ultra, r, z, s));
+          return mc_sor_sweep<double, double>(*col, p.v64.p, relax, 0, ultra, r, z, s);
+        }
+        LGX_CHECK(mc_sor_sweep<float, double>(*col, p.v32.p, relax, 1, ultra, r, z, s));
+        return mc_sor_sweep<float, double>(*col, p.v32.p, relax, 0, ultra, r, z, s);
+      }
+      case LGX_PRECON_AMG: return amg_apply_permuted(*amg, r, z, s);
+      default:
+        LGX_CUDA(cudaMemcpyAsync(z, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+        return LGX_OK;
+    }
+  }
+  unsigned vgrid() const { return (unsigned)std::min<int64_t>(grid_for(n, 256), 16384); }
+  lgx_status read(KScalars &h) {
+    LGX_CUDA(cudaMemcpyAsync(&h, ks.p, sizeof(KScalars), cudaMemcpyDeviceToHost, s));
+    LGX_CUDA(cudaStreamSynchronize(s));
+    return LGX_OK;
+  }
+};
+
+static lgx_status setup_solver(const lgx_matrix *a, const lgx_solve_params *p, cudaStream_t s,
+                               Solver &S, std::unique_ptr<lgx_colouring> &own_col) {
+  S.n = a->n;
+  S.s = s;
+  S.precon = p->precon;
+  S.relax = p->relax;
+  S.ultra = p->ultra;
+  S.m = a;
+  switch (p->precon) {
+    case LGX_PRECON_NONE: break;
+    case LGX_PRECON_JACOBI:
+      LGX_CHECK(matrix_diagonal(const_cast<lgx_matrix *>(a), s, &S.diag));
+      break;
+    case LGX_PRECON_SSOR: {
+      if (a->kind != LGX_MATRIX_CSR)
+        return fail(LGX_ERR_UNSUPPORTED, "SSOR preconditioning needs a CSR matrix");
+      lgx_colouring *c = const_cast<lgx_colouring *>(p->colouring);
+      if (!c) {
+        own_col = std::make_unique<lgx_colouring>();
+        int32_t nc = 0;
+        LGX_CHECK(colouring_jp(a->csr, 0x5eed, s, own_col->colour, nc));
+        LGX_CHECK(colouring_build(a->csr, own_col->colour.p, nc, s, *own_col));
+        c = own_col.get();
+      }
+      if (c->n != a->n) return fail(LGX_ERR_INVALID, "colouring does not match the matrix");
+      S.col = c;
+      S.pcsr = &c->pcsr;
+      S.perm = c->perm.p;
+      break;
+    }
+    case LGX_PRECON_AMG: {
+      if (!p->amg) return fail(LGX_ERR_INVALID, "AMG preconditioner without a hierarchy");
+      S.amg = p->amg;
+      lgx_colouring *c = amg_finest_colouring(*p->amg);
+      if (c) {
+        if (c->n != a->n) return fail(LGX_ERR_INVALID, "hierarchy does not match the matrix");
+        S.pcsr = &c->pcsr;
+        S.perm = c->perm.p;
+      }
+      break;
+    }
+    default: return fail(LGX_ERR_INVALID, "unknown preconditioner");
+  }
+  return S.init();
+}
+
+struct Vecs {
+  std::vector<DBuf<double>> v;
+  lgx_status alloc(int count, int64_t n) {
+    v.resize(count);
+    for (auto &b : v) LGX_CHECK(b.alloc(n));
+    return LGX_OK;
+  }
+  double *operator[](int i) { return v[i].p; }
+};
+
+static lgx_status check_flags(const KScalars &h, int64_t it) {
+  if (h.flag & 2)
+    return fail(LGX_ERR_NONFINITE, "non-finite value in iteration " + std::to_string(it));
+  if (h.flag & 1)
+    return fail(LGX_ERR_BREAKDOWN, "zero denominator in iteration " + std::to_string(it));
+  return LGX_OK;
+}
+
+static lgx_status run_pcg(const lgx_matrix *a, const double *d_b, double *d_x,
+                          const lgx_solve_params *p, cudaStream_t s, int64_t *iterations,
+                          double *final_rel, double *history) {
+  Solver S;
+  std::unique_ptr<lgx_colouring> own_col;
+  LGX_CHECK(setup_solver(a, p, s, S, own_col));
+  const int64_t n = S.n;
+  Vecs V;
+  // 0 b, 1 x, 2 r, 3 p, 4 q/z
+  LGX_CHECK(V.alloc(5, n));
+  double *b = V[0], *x = V[1], *r = V[2], *pd = V[3], *q = V[4];
+  if (S.perm) {
+    LGX_CHECK(gather<double, double>(n, S.perm, d_b, b, s));
+    LGX_CHECK(gather<double, double>(n, S.perm, d_x, x, s));
+  } else {
+    LGX_CUDA(cudaMemcpyAsync(b, d_b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    LGX_CUDA(cudaMemcpyAsync(x, d_x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  }
+  KScalars *ks = S.ks.p;
+  const unsigned rg = (unsigned)reduce_blocks(n);
+  const bool precon = S.precon != LGX_PRECON_NONE;
+  // initialisation (solver.hpp:50-73)
+  LGX_CHECK(S.residual(b, x, r, &ks->res2));
+  if (precon) {
+    LGX_CHECK(S.precondition(r, pd));
+    k_dot_post<<<rg, kKT, 0, s>>>(n, pd, r, POST_RHO_BETA, ks, S.partials.p, S.counters.p);
+    LGX_LAUNCH_CHECK();
+  } else {
+    LGX_CUDA(cudaMemcpyAsync(pd, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    k_cg_plain_rho<<<1, 1, 0, s>>>(ks);
+    LGX_LAUNCH_CHECK();
+  }
+  KScalars h{};
+  LGX_CHECK(S.read(h));
+  if (!std::isfinite(h.res2) || !std::isfinite(h.rho))
+    return fail(LGX_ERR_NONFINITE, "non-finite initial residual or preconditioned residual");
+  const double r0 = std::sqrt(h.res2);
+  if (history) history[0] = r0;
+  int64_t it = 0;
+  double res = r0;
+  lgx_status st = LGX_OK;
+  while (it < p->maxit && res > p->rtol * r0 && h.rho != 0.0) {
+    LGX_CHECK(S.apply(pd, q));
+    k_dot_post<<<rg, kKT, 0, s>>>(n, pd, q, POST_ALPHA, ks, S.partials.p, S.counters.p);
+    LGX_LAUNCH_CHECK();
+    const bool rere = p->rere_period > 0 && it > 0 && it % p->rere_period == 0;
+    k_cg_update<<<rg, kKT, 0, s>>>(n, ks, pd, q, x, r, rere ? 0 : 1, precon ? 0 : 1,
+                                   S.partials.p, S.counters.p);
+    LGX_LAUNCH_CHECK();
+    if (rere) {
+      LGX_CHECK(S.residual(b, x, r, &ks->res2));
+      if (!precon) {
+        k_cg_plain_rho<<<1, 1, 0, s>>>(ks);
+        LGX_LAUNCH_CHECK();
+      }
+    }
+    if (precon) {
+      LGX_CHECK(S.precondition(r, q));
+      k_dot_post<<<rg, kKT, 0, s>>>(n, r, q, POST_RHO_BETA, ks, S.partials.p, S.counters.p);
+      LGX_LAUNCH_CHECK();
+      k_xpby<<<S.vgrid(), 256, 0, s>>>(n, ks, q, pd);
+    } else {
+      k_xpby<<<S.vgrid(), 256, 0, s>>>(n, ks, r, pd);
+    }
+    LGX_LAUNCH_CHECK();
+    ++it;
+    LGX_CHECK(S.read(h));
+    res = std::sqrt(h.res2);
+    if (history) history[it] = res;
+    if ((st = check_flags(h, it)) != LGX_OK) break;
+  }
+  if (S.perm) {
+    LGX_CHECK(scatter<double, double>(n, S.perm, x, d_x, s));
+  } else {
+    LGX_CUDA(cudaMemcpyAsync(d_x, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  }
+  LGX_CUDA(cudaStreamSynchronize(s));
+  if (iterations) *iterations = it;
+  if (final_rel) *final_rel = r0 > 0 ? res / r0 : 0.0;
+  return st;
+}
+
+static lgx_status run_pbicgstab(const lgx_matrix *a, const double *d_b, double *d_x,
+                                const lgx_solve_params *p, cudaStream_t s, int64_t *iterations,
+                                double *final_rel, double *history) {
+  Solver S;
+  std::unique_ptr<lgx_colouring> own_col;
+  LGX_CHECK(setup_solver(a, p, s, S, own_col));
+  const int64_t n = S.n;
+  Vecs V;
+  // 0 b, 1 x, 2 r, 3 r0, 4 p, 5 v, 6 t, 7 px
+  LGX_CHECK(V.alloc(8, n));
+  double *b = V[0], *x = V[1], *r = V[2], *r0 = V[3], *pd = V[4], *v = V[5], *t = V[6],
+         *px = V[7];
+  if (S.perm) {
+    LGX_CHECK(gather<double, double>(n, S.perm, d_b, b, s));
+    LGX_CHECK(gather<double, double>(n, S.perm, d_x, x, s));
+  } else {
+    LGX_CUDA(cudaMemcpyAsync(b, d_b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    LGX_CUDA(cudaMemcpyAsync(x, d_x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  }
+  KScalars *ks = S.ks.p;
+  const unsigned rg = (unsigned)reduce_blocks(n);
+  const bool precon = S.precon != LGX_PRECON_NONE;
+  // initialisation (bicgstab/solver.hpp:51-71)
+  LGX_CHECK(S.residual(b, x, r, &ks->res2));
+  LGX_CUDA(cudaMemcpyAsync(r0, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  LGX_CUDA(cudaMemcpyAsync(pd, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  k_bicg_init<<<1, 1, 0, s>>>(ks);
+  LGX_LAUNCH_CHECK();
+  KScalars h{};
+  LGX_CHECK(S.read(h));
+  if (!std::isfinite(h.res2))
+    return fail(LGX_ERR_NONFINITE, "non-finite initial residual");
+  const double rn0 = std::sqrt(h.res2);
+  if (history) history[0] = rn0;
+  int64_t it = 0;
+  double res = rn0;
+  lgx_status st = LGX_OK;
+  double *partials2 = S.partials2.p;
+  unsigned *c1 = S.counters.p, *c2 = S.counters.p + 1;
+  while (it < p->maxit && res > p->rtol * rn0 && h.rho != 0.0) {
+    const double *y = pd;
+    if (precon) {
+      LGX_CHECK(S.precondition(pd, px));
+      y = px;
+    }
+    LGX_CHECK(S.apply(y, v));
+    k_dot_post<<<rg, kKT, 0, s>>>(n, r0, v, POST_ALPHA, ks, S.partials.p, c1);
+    LGX_LAUNCH_CHECK();
+    // x += alpha y ; r -= alpha v ; res2 = ||r||^2
+    k_cg_update<<<rg, kKT, 0, s>>>(n, ks, y, v, x, r, 1, 0, S.partials.p, c1);
+    LGX_LAUNCH_CHECK();
+    const double *z = r;
+    if (precon) {
+      LGX_CHECK(S.precondition(r, px));
+      z = px;
+    }
+    LGX_CHECK(S.apply(z, t));
+    k_dot2_post<<<rg, kKT, 0, s>>>(n, t, r, t, t, POST_OMEGA, ks, S.partials.p, partials2, c1,
+                                    c2);
+    LGX_LAUNCH_CHECK();
+    k_axpy_ks<<<S.vgrid(), 256, 0, s>>>(n, ks, 1, z, x);
+    LGX_LAUNCH_CHECK();
+    const bool rere = p->rere_period > 0 && it > 0 && it % p->rere_period == 0;
+    if (rere) LGX_CHECK(S.residual(b, x, r, nullptr));
+    k_bicg_r<<<rg, kKT, 0, s>>>(n, ks, rere ? 0 : 1, t, r, r0, S.partials.p, partials2, c1, c2);
+    LGX_LAUNCH_CHECK();
+    k_bicg_p<<<S.vgrid(), 256, 0, s>>>(n, ks, r, v, pd);
+    LGX_LAUNCH_CHECK();
+    ++it;
+    LGX_CHECK(S.read(h));
+    res = std::sqrt(h.res2);
+    if (history) history[it] = res;
+    if ((st = check_flags(h, it)) != LGX_OK) break;
+  }
+  if (S.perm) {
+    LGX_CHECK(scatter<double, double>(n, S.perm, x, d_x, s));
+  } else {
+    LGX_CUDA(cudaMemcpyAsync(d_x, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  }
+  LGX_CUDA(cudaStreamSynchronize(s));
+  if (iterations) *iterations = it;
+  if (final_rel) *final_rel = rn0 > 0 ? res / rn0 : 0.0;
+  return st;
+}
+
+}  // namespace lgx
+
+using namespace lgx;
+
+extern "C" {
+
+void lgx_solve_default_params(lgx_solve_params *p) {
+  if (!p) return;
+  p->precon = LGX_PRECON_NONE;
+  p->relax = 1.0;
+  p->ultra = 0;
+  p->colouring = nullptr;
+  p->amg = nullptr;
+  p->rtol = 1e-8;
+  p->maxit = 1000;
+  p->rere_period = 8;
+}
+
+lgx_status lgx_pcg(const lgx_matrix *a, const double *d_b, double *d_x,
+                   const lgx_solve_params *p, lgx_stream stream, int64_t *iterations,
+                   double *final_rel_residual, double *h_history) {
+  if (!a || !p || (a->n > 0 && (!d_b || !d_x))) return fail(LGX_ERR_INVALID, "null argument");
+  return run_pcg(a, d_b, d_x, p, stream, iterations, final_rel_residual, h_history);
+}
+
+lgx_status lgx_pbicgstab(const lgx_matrix *a, const double *d_b, double *d_x,
+                         const lgx_solve_params *p, lgx_stream stream, int64_t *iterations,
+                         double *final_rel_residual, double *h_history) {
+  if (!a || !p || (a->n > 0 && (!d_b || !d_x))) return fail(LGX_ERR_INVALID, "null argument");
+  return run_pbicgstab(a, d_b, d_x, p, stream, iterations, final_rel_residual, h_history);
+}
+
+}  // extern "C"

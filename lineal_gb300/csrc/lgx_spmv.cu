@@ -1,0 +1,779 @@
+// Sparse matrix-vector products: CSR (row blocks staged through shared
+// memory, one thread per row) and matrix-free 7-point diffusion stencils.
+//
+// GB300 note: FP64 runs at ~1.2 TFLOP/s on this part (58x below FP32), so
+// every FP64 kernel is co-limited by the FP64 pipe.  The CSR kernels use one
+// thread per row (27 FMAs for a 27-point row, no shuffle reductions whose
+// FP64 adds would multiply the pipe load) and stage each block's contiguous
+// CSR segment in shared memory so the global reads stay fully coalesced.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "lgx_internal.cuh"
+
+namespace lgx {
+
+// ---------------------------------------------------------------------------
+// CSR row-block engine
+// ---------------------------------------------------------------------------
+constexpr int kRows = 128;  // rows (= threads) per block
+
+template <typename VT>
+struct SegCap {
+  static constexpr int value = 48 * 1024 / (int)(sizeof(int32_t) + sizeof(VT));
+};
+
+// Loads the CSR segment of rows [r0, r1) into shared memory when it fits and
+// returns pointers to the calling thread's row (shared or global).
+template <typename VT>
+struct RowSlice {
+  const int32_t *c;
+  const VT *v;
+  int len;
+};
+
+template <typename VT>
+__device__ __forceinline__ bool stage_segment(const int64_t *__restrict__ rowptr,
+                                              const int32_t *__restrict__ col,
+                                              const VT *__restrict__ val, int64_t r0, int64_t r1,
+                                              int32_t *s_col, VT *s_val, int64_t &e0) {
+  constexpr int CAP = SegCap<VT>::value;
+  e0 = rowptr[r0];
+  const int64_t e1 = rowptr[r1];
+  if (e1 - e0 > CAP) return false;
+  const int cnt = (int)(e1 - e0);
+  for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
+    s_col[k] = __ldg(col + e0 + k);
+    s_val[k] = __ldg(val + e0 + k);
+  }
+  __syncthreads();
+  return true;
+}
+
+// sum_k fma(a_k, x[c_k], sum) in storage order, starting from `init`
+template <typename VT, typename XT>
+__device__ __forceinline__ XT row_dot(const int32_t *c, const VT *v, int len,
+                                      const XT *__restrict__ x, XT init) {
+  XT sum = init;
+  int k = 0;
+  for (; k + 4 <= len; k += 4) {
+    const int32_t c0 = c[k], c1 = c[k + 1], c2 = c[k + 2], c3 = c[k + 3];
+    const XT a0 = (XT)v[k], a1 = (XT)v[k + 1], a2 = (XT)v[k + 2], a3 = (XT)v[k + 3];
+    const XT x0 = __ldg(x + c0), x1 = __ldg(x + c1), x2 = __ldg(x + c2), x3 = __ldg(x + c3);
+    sum = fma(a0, x0, sum);
+    sum = fma(a1, x1, sum);
+    sum = fma(a2, x2, sum);
+    sum = fma(a3, x3, sum);
+  }
+  for (; k < len; ++k) sum = fma((XT)v[k], __ldg(x + c[k]), sum);
+  return sum;
+}
+
+template <typename VT, typename XT>
+__global__ void __launch_bounds__(kRows)
+  k_csr_spmv(int64_t n, const int64_t *__restrict__ rowptr, const int32_t *__restrict__ col,
+             const VT *__restrict__ val, const XT *__restrict__ x, XT *__restrict__ y) {
+  constexpr int CAP = SegCap<VT>::value;
+  __shared__ int32_t s_col[CAP];
+  __shared__ VT s_val[CAP];
+  const int64_t r0 = (int64_t)blockIdx.x * kRows;
+  const int64_t r1 = min(r0 + kRows, n);
+  const int64_t row = r0 + threadIdx.x;
+  int64_t e0;
+  if (stage_segment(rowptr, col, val, r0, r1, s_col, s_val, e0)) {
+    if (row < r1) {
+      const int64_t b = rowptr[row], e = rowptr[row + 1];
+      y[row] = row_dot(s_col + (b - e0), s_val + (b - e0), (int)(e - b), x, XT(0));
+    }
+  } else if (row < r1) {
+    const int64_t b = rowptr[row], e = rowptr[row + 1];
+    y[row] = row_dot(col + b, val + b, (int)(e - b), x, XT(0));
+  }
+}
+
+// r = b - A x, optionally reducing ||r||^2 deterministically
+template <typename VT, typename XT, bool NORM>
+__global__ void __launch_bounds__(kRows)
+  k_csr_residual(int64_t n, const int64_t *__restrict__ rowptr, const int32_t *__restrict__ col,
+                 const VT *__restrict__ val, const XT *__restrict__ b, const XT *__restrict__ x,
+                 XT *__restrict__ r, double *norm, double *partials, unsigned *counter) {
+  constexpr int CAP = SegCap<VT>::value;
+  __shared__ int32_t s_col[CAP];
+  __shared__ VT s_val[CAP];
+  const int64_t r0 = (int64_t)blockIdx.x * kRows;
+  const int64_t r1 = min(r0 + kRows, n);
+  const int64_t row = r0 + threadIdx.x;
+  int64_t e0;
+  double contrib = 0.0;
+  if (stage_segment(rowptr, col, val, r0, r1, s_col, s_val, e0)) {
+    if (row < r1) {
+      const int64_t bb = rowptr[row], e = rowptr[row + 1];
+      const XT ax = row_dot(s_col + (bb - e0), s_val + (bb - e0), (int)(e - bb), x, XT(0));
+      const XT rv = b[row] - ax;
+      r[row] = rv;
+      contrib = (double)rv * (double)rv;
+    }
+  } else if (row < r1) {
+    const int64_t bb = rowptr[row], e = rowptr[row + 1];
+    const XT ax = row_dot(col + bb, val + bb, (int)(e - bb), x, XT(0));
+    const XT rv = b[row] - ax;
+    r[row] = rv;
+    contrib = (double)rv * (double)rv;
+  }
+  if constexpr (NORM) {
+    double t;
+    if (grid_reduce<kRows>(contrib, blockIdx.x, gridDim.x, partials, counter, &t) &&
+        threadIdx.x == 0)
+      norm[0] = t;
+  }
+}
+
+template <typename VT, typename XT>
+lgx_status csr_spmv(const Csr &a, const VT *val, const XT *x, XT *y, cudaStream_t s) {
+  if (a.n == 0) return LGX_OK;
+  k_csr_spmv<VT, XT><<<grid_for(a.n, kRows), kRows, 0, s>>>(a.n, a.rowptr.p, a.col.p, val, x, y);
+  LGX_LAUNCH_CHECK();
+  return LGX_OK;
+}
+
+template <typename VT, typename XT>
+lgx_status csr_residual(const Csr &a, const VT *val, const XT *b, const XT *x, XT *r,
+                        double *norm, double *partials, unsigned *counter, cudaStream_t s) {
+  if (a.n == 0) {
+    if (norm) LGX_CUDA(cudaMemsetAsync(norm, 0, sizeof(double), s));
+    return LGX_OK;
+  }
+  if (norm) {
+    k_csr_residual<VT, XT, true><<<grid_for(a.n, kRows), kRows, 0, s>>>(
+      a.n, a.rowptr.p, a.col.p, val, b, x, r, norm, partials, counter);
+  } else {
+    k_csr_residual<VT, XT, false><<<grid_for(a.n, kRows), kRows, 0, s>>>(
+      a.n, a.rowptr.p, a.col.p, val, b, x, r, nullptr, nullptr, nullptr);
+  }
+  LGX_LAUNCH_CHECK();
+  return LGX_OK;
+}
+
+int64_t csr_partials(int64_t n) { return std::max<int64_t>(1, grid_for(n, kRows)); }
+
+template lgx_status csr_spmv<double, double>(const Csr &, const double *, const double *,
+                                             double *, cudaStream_t);
+template lgx_status csr_spmv<float, double>(const Csr &, const float *, const double *, double *,
+                                            cudaStream_t);
+template lgx_status csr_spmv<float, float>(const Csr &, const float *, const float *, float *,
+                                           cudaStream_t);
+template lgx_status csr_residual<double, double>(const Csr &, const double *, const double *,
+                                                 const double *, double *, double *, double *,
+                                                 unsigned *, cudaStream_t);
+template lgx_status csr_residual<float, double>(const Csr &, const float *, const double *,
+                                                const double *, double *, double *, double *,
+                                                unsigned *, cudaStream_t);
+template lgx_status csr_residual<float, float>(const Csr &, const float *, const float *,
+                                               const float *, float *, double *, double *,
+                                               unsigned *, cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// Matrix-free 7-point diffusion stencil
+//
+// Row semantics (stencil/matrix/algorithm.hpp:93-227, scalar valued
+// unordered iteration): off-diagonal to the neighbour on side s of axis d is
+// -conn_d(i, j); the diagonal is the Dirichlet border terms of axis 0
+// (2 q_0 c_i per boundary face) followed by the six connection values in the
+// visiting order before(d = 0,1,2), after(d = 2,1,0); zero_to_one maps a zero
+// diagonal to 1.  The product accumulates fma(-conn, x_j, sum) in the same
+// visiting order and finishes with fma(diag, x_i, sum).
+//
+// The diagonal is computed once per matrix and cached (8 B/cell): on GB300
+// the six FP64 additions per cell would otherwise nearly double the FP64
+// pipe load of every product.  For the value valuator the harmonic means
+// (one FP64 division per face) are likewise computed once into three face
+// arrays; FP64 division runs at ~59 G/s on this part, so recomputing them
+// would make the product ~10x slower than streaming the cached faces.
+// ---------------------------------------------------------------------------
+struct StencilDev {
+  int n0, n1, n2;
+  int lookup;
+  double conn[48];  // lookup tables, staged into shared memory by each block
+  const uint8_t *mat;
+  const double *face0, *face1, *face2;  // value valuator: face d of cell i joins i and i+stride_d
+  const double *diag;
+};
+
+// Copies the lookup tables of S into shared memory (all threads of the block
+// must call it).
+__device__ __forceinline__ const double *stage_conn(const StencilDev &S, double *sh) {
+  const unsigned t = threadIdx.x + blockDim.x * threadIdx.y;
+  if (S.lookup && t < 48) sh[t] = S.conn[t];
+  __syncthreads();
+  return sh;
+}
+
+__device__ __forceinline__ double st_conn_lookup(const double *conn, const uint8_t *mat, int d,
+                                                 int64_t i, int64_t j) {
+  return conn[d * 16 + mat[i] * 4 + mat[j]];
+}
+
+// off-diagonal connection values of cell (p0,p1,p2) = i, in visiting order
+template <bool LOOKUP>
+__device__ __forceinline__ void st_row(const StencilDev &S, const double *conn, int p0, int p1,
+                                       int p2, int64_t i, double cv[6], int64_t cj[6],
+                                       bool has[6]) {
+  const int64_t s0 = (int64_t)S.n1 * S.n2, s1 = S.n2;
+  // before: d = 0, 1, 2 ; after: d = 2, 1, 0
+  has[0] = p0 > 0;
+  has[1] = p1 > 0;
+  has[2] = p2 > 0;
+  has[3] = p2 + 1 < S.n2;
+  has[4] = p1 + 1 < S.n1;
+  has[5] = p0 + 1 < S.n0;
+  cj[0] = i - s0;
+  cj[1] = i - s1;
+  cj[2] = i - 1;
+  cj[3] = i + 1;
+  cj[4] = i + s1;
+  cj[5] = i + s0;
+  if constexpr (LOOKUP) {
+    cv[0] = has[0] ? st_conn_lookup(conn, S.mat, 0, i, cj[0]) : 0.0;
+    cv[1] = has[1] ? st_conn_lookup(conn, S.mat, 1, i, cj[1]) : 0.0;
+    cv[2] = has[2] ? st_conn_lookup(conn, S.mat, 2, i, cj[2]) : 0.0;
+    cv[3] = has[3] ? st_conn_lookup(conn, S.mat, 2, i, cj[3]) : 0.0;
+    cv[4] = has[4] ? st_conn_lookup(conn, S.mat, 1, i, cj[4]) : 0.0;
+    cv[5] = has[5] ? st_conn_lookup(conn, S.mat, 0, i, cj[5]) : 0.0;
+  } else {
+    cv[0] = has[0] ? S.face0[cj[0]] : 0.0;
+    cv[1] = has[1] ? S.face1[cj[1]] : 0.0;
+    cv[2] = has[2] ? S.face2[cj[2]] : 0.0;
+    cv[3] = has[3] ? S.face2[i] : 0.0;
+    cv[4] = has[4] ? S.face1[i] : 0.0;
+    cv[5] = has[5] ? S.face0[i] : 0.0;
+  }
+}
+
+__device__ __forceinline__ double hm_dev(double a, double b) {
+  const double p = __dmul_rn(a, b);
+  return p != 0.0 ? __ddiv_rn(__dadd_rn(p, p), __dadd_rn(a, b)) : 0.0;
+}
+
+// value valuator faces: face_d[i] = hm(k_i, k_{i+stride_d}) * q_d
+__global__ void k_st_faces(int n0, int n1, int n2, const double *k, double q0, double q1, double q2,
+                           double *f0, double *f1, double *f2) {
+  const int p2 = blockIdx.x * blockDim.x + threadIdx.x;
+  const int p1 = blockIdx.y * blockDim.y + threadIdx.y;
+  const int p0 = blockIdx.z;
+  if (p2 >= n2 || p1 >= n1) return;
+  const int64_t s0 = (int64_t)n1 * n2;
+  const int64_t i = (int64_t)p0 * s0 + (int64_t)p1 * n2 + p2;
+  const double ki = k[i];
+  f0[i] = p0 + 1 < n0 ? __dmul_rn(hm_dev(ki, k[i + s0]), q0) : 0.0;
+  f1[i] = p1 + 1 < n1 ? __dmul_rn(hm_dev(ki, k[i + n2]), q1) : 0.0;
+  f2[i] = p2 + 1 < n2 ? __dmul_rn(hm_dev(ki, k[i + 1]), q2) : 0.0;
+}
+
+template <bool LOOKUP>
+__global__ void k_st_diag(StencilDev S, const double *cell_value, double border_q0,
+                          int zero_to_one, double *diag) {
+  __shared__ double sh_conn[48];
+  const double *conn = stage_conn(S, sh_conn);
+  const int p2 = blockIdx.x * blockDim.x + threadIdx.x;
+  const int p1 = blockIdx.y * blockDim.y + threadIdx.y;
+  const int p0 = blockIdx.z;
+  if (p2 >= S.n2 || p1 >= S.n1) return;
+  const int64_t i = ((int64_t)p0 * S.n1 + p1) * S.n2 + p2;
+  double cv[6];
+  int64_t cj[6];
+  bool has[6];
+  st_row<LOOKUP>(S, conn, p0, p1, p2, i, cv, cj, has);
+  const double c = cell_value[i];
+  double d = 0.0;
+  const double bt = __dmul_rn(border_q0, c);
+  if (p0 == 0) d = __dadd_rn(d, bt);
+  if (p0 + 1 == S.n0) d = __dadd_rn(d, bt);
+#pragma unroll
+  for (int e = 0; e < 6; ++e)
+    if (has[e]) d = __dadd_rn(d, cv[e]);
+  if (zero_to_one && d == 0.0) d = 1.0;
+  diag[i] = d;
+}
+
+// cell values of the lookup valuator: coeffs[mat[i]]
+__global__ void k_st_cellvalue(int64_t n, const uint8_t *mat, double c0, double c1, double c2,
+                               double c3, double *out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const uint8_t m = mat[i];
+    out[i] = m == 0 ? c0 : m == 1 ? c1 : m == 2 ? c2 : c3;
+  }
+}
+
+template <bool LOOKUP, bool RESID, bool NORM>
+__global__ void __launch_bounds__(256)
+  k_st_apply(StencilDev S, const double *__restrict__ x, const double *__restrict__ b,
+             double *__restrict__ y, double *norm, double *partials, unsigned *counter) {
+  __shared__ double sh_conn[48];
+  const double *conn = stage_conn(S, sh_conn);
+  const int p2 = blockIdx.x * blockDim.x + threadIdx.x;
+  const int p1 = blockIdx.y * blockDim.y + threadIdx.y;
+  const int p0 = blockIdx.z;
+  double contrib = 0.0;
+  if (p2 < S.n2 && p1 < S.n1) {
+    const int64_t i = ((int64_t)p0 * S.n1 + p1) * S.n2 + p2;
+    double cv[6];
+    int64_t cj[6];
+    bool has[6];
+    st_row<LOOKUP>(S, conn, p0, p1, p2, i, cv, cj, has);
+    double sum = 0.0;
+#pragma unroll
+    for (int e = 0; e < 6; ++e)
+      if (has[e]) sum = fma(-cv[e], __ldg(x + cj[e]), sum);
+    sum = fma(S.diag[i], x[i], sum);
+    if constexpr (RESID) {
+      const double rv = b[i] - sum;
+      y[i] = rv;
+      contrib = rv * rv;
+    } else {
+      y[i] = sum;
+    }
+  }
+  if constexpr (NORM) {
+    const unsigned bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    const unsigned nb = gridDim.x * gridDim.y * gridDim.z;
+    __shared__ double sh[256];
+    __shared__ bool last;
+    // flatten (x, y) thread index for the block reduction
+    const unsigned t = threadIdx.x + blockDim.x * threadIdx.y;
+    sh[t] = contrib;
+    __syncthreads();
+    for (unsigned s = 128; s > 0; s >>= 1) {
+      if (t < s) sh[t] += sh[t + s];
+      __syncthreads();
+    }
+    if (t == 0) {
+      partials[bid] = sh[0];
+      __threadfence();
+      last = atomicAdd(counter, 1u) == nb - 1;
+    }
+    __syncthreads();
+    if (last) {
+      __threadfence();
+      double acc = 0.0;
+      for (unsigned k = t; k < nb; k += 256) acc += ((volatile double *)partials)[k];
+      sh[t] = acc;
+      __syncthreads();
+      for (unsigned s = 128; s > 0; s >>= 1) {
+        if (t < s) sh[t] += sh[t + s];
+        __syncthreads();
+      }
+      if (t == 0) {
+        norm[0] = sh[0];
+        *counter = 0;
+      }
+    }
+  }
+}
+
+__global__ void k_st_rhs(int n0, int n1, int n2, const double *cell_value, double border_q0,
+                         double us, double ue, double *b) {
+  const int p2 = blockIdx.x * blockDim.x + threadIdx.x;
+  const int p1 = blockIdx.y * blockDim.y + threadIdx.y;
+  const int p0 = blockIdx.z;
+  if (p2 >= n2 || p1 >= n1) return;
+  const int64_t i = ((int64_t)p0 * n1 + p1) * n2 + p2;
+  const double bt = __dmul_rn(border_q0, cell_value[i]);
+  double sum = 0.0;
+  if (p0 == 0) sum = __dadd_rn(sum, __dmul_rn(bt, us));
+  if (p0 + 1 == n0) sum = __dadd_rn(sum, __dmul_rn(bt, ue));
+  b[i] = sum;
+}
+
+static dim3 st_grid(const StencilDesc &st) {
+  return dim3((unsigned)((st.dims[2] + 31) / 32), (unsigned)((st.dims[1] + 7) / 8),
+              (unsigned)st.dims[0]);
+}
+static const dim3 kStBlock(32, 8, 1);
+
+int64_t stencil_partials(const StencilDesc &st) {
+  const dim3 g = st_grid(st);
+  return (int64_t)g.x * g.y * g.z;
+}
+
+}  // namespace lgx
+
+// Device view of a stencil matrix.  The value valuator keeps its face arrays
+// behind the conductivities in one buffer: k (n) | face0 (n) | face1 (n) |
+// face2 (n).
+namespace lgx {
+
+static StencilDev dev_of(const lgx_matrix *a) {
+  StencilDev S;
+  S.n0 = (int)a->st.dims[0];
+  S.n1 = (int)a->st.dims[1];
+  S.n2 = (int)a->st.dims[2];
+  S.lookup = a->st.lookup;
+  S.mat = a->mat.p;
+  S.face0 = S.face1 = S.face2 = nullptr;
+  S.diag = a->diag.p;
+  for (int t = 0; t < 48; ++t) S.conn[t] = a->st.conn[t];
+  if (!a->st.lookup) {
+    const double *base = a->k.p;
+    S.face0 = base + a->n;
+    S.face1 = base + 2 * a->n;
+    S.face2 = base + 3 * a->n;
+  }
+  return S;
+}
+
+lgx_status stencil_ensure(lgx_matrix *a, cudaStream_t s) {
+  if (a->diag.p) return LGX_OK;
+  const StencilDesc &st = a->st;
+  const int64_t n = a->n;
+  if (!st.lookup) {
+    // faces into k buffer slots 1..3
+    double *base = a->k.p;
+    k_st_faces<<<st_grid(st), kStBlock, 0, s>>>((int)st.dims[0], (int)st.dims[1],
+                                                (int)st.dims[2], base, st.q[0], st.q[1], st.q[2],
+                                                base + n, base + 2 * n, base + 3 * n);
+    LGX_LAUNCH_CHECK();
+  }
+  DBuf<double> cellv;
+  const double *cell_value = a->k.p;
+  if (st.lookup) {
+    LGX_CHECK(cellv.alloc(n));
+    k_st_cellvalue<<<std::min<int64_t>(grid_for(n, 256), 8192), 256, 0, s>>>(
+      n, a->mat.p, st.coeffs[0], st.coeffs[1], st.coeffs[2], st.coeffs[3], cellv.p);
+    LGX_LAUNCH_CHECK();
+    cell_value = cellv.p;
+  }
+  LGX_CHECK(a->diag.alloc(n));
+  StencilDev S = dev_of(a);
+  const double bq0 = 2.0 * st.q[0];
+  if (st.lookup) {
+    k_st_diag<true><<<st_grid(st), kStBlock, 0, s>>>(S, cell_value, bq0, st.zero_to_one,
+                                                     a->diag.p);
+  } else {
+    k_st_diag<false><<<st_grid(st), kStBlock, 0, s>>>(S, cell_value, bq0, st.zero_to_one,
+                                                      a->diag.p);
+  }
+  LGX_LAUNCH_CHECK();
+  LGX_CUDA(cudaStreamSynchronize(s));  // cellv is released on return
+  return LGX_OK;
+}
+
+static lgx_status stencil_apply(const lgx_matrix *ac, const double *x, const double *b, double *y,
+                                double *norm, double *partials, unsigned *counter,
+                                cudaStream_t s) {
+  lgx_matrix *a = const_cast<lgx_matrix *>(ac);
+  LGX_CHECK(stencil_ensure(a, s));
+  StencilDev S = dev_of(a);
+  const dim3 g = st_grid(a->st);
+  const bool lk = a->st.lookup;
+  if (!b) {
+    if (lk) k_st_apply<true, false, false><<<g, kStBlock, 0, s>>>(S, x, nullptr, y, nullptr,
+                                                                  nullptr, nullptr);
+    else k_st_apply<false, false, false><<<g, kStBlock, 0, s>>>(S, x, nullptr, y, nullptr,
+                                                                nullptr, nullptr);
+  } else if (!norm) {
+    if (lk) k_st_apply<true, true, false><<<g, kStBlock, 0, s>>>(S, x, b, y, nullptr, nullptr,
+                                                                 nullptr);
+    else k_st_apply<false, true, false><<<g, kStBlock, 0, s>>>(S, x, b, y, nullptr, nullptr,
+                                                               nullptr);
+  } else {
+    if (lk) k_st_apply<true, true, true><<<g, kStBlock, 0, s>>>(S, x, b, y, norm, partials,
+                                                                counter);
+    else k_st_apply<false, true, true><<<g, kStBlock, 0, s>>>(S, x, b, y, norm, partials,
+                                                              counter);
+  }
+  LGX_LAUNCH_CHECK();
+  return LGX_OK;
+}
+
+lgx_status matrix_spmv(const lgx_matrix *a, const double *x, double *y, cudaStream_t s) {
+  if (a->kind == LGX_MATRIX_CSR) {
+    if (a->csr.storage == LGX_F64) return csr_spmv<double, double>(a->csr, a->csr.v64.p, x, y, s);
+    return csr_spmv<float, double>(a->csr, a->csr.v32.p, x, y, s);
+  }
+  return stencil_apply(a, x, nullptr, y, nullptr, nullptr, nullptr, s);
+}
+
+lgx_status matrix_residual(const lgx_matrix *a, const double *b, const double *x, double *r,
+                           double *norm, double *partials, unsigned *counter, cudaStream_t s) {
+  if (a->kind == LGX_MATRIX_CSR) {
+    if (a->csr.storage == LGX_F64)
+      return csr_residual<double, double>(a->csr, a->csr.v64.p, b, x, r, norm, partials, counter,
+                                          s);
+    return csr_residual<float, double>(a->csr, a->csr.v32.p, b, x, r, norm, partials, counter, s);
+  }
+  return stencil_apply(a, x, b, r, norm, partials, counter, s);
+}
+
+int64_t matrix_partials(const lgx_matrix *a) {
+  if (a->kind == LGX_MATRIX_CSR) return csr_partials(a->n);
+  return stencil_partials(a->st);
+}
+
+__global__ void k_csr_diag(int64_t n, const int64_t *rowptr, const int32_t *col,
+                           const double *v64, const float *v32, double *d) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double v = 0.0;
+    for (int64_t e = rowptr[i]; e < rowptr[i + 1]; ++e)
+      if (col[e] == i) v = v64 ? v64[e] : (double)v32[e];
+    d[i] = v;
+  }
+}
+
+lgx_status matrix_diagonal(lgx_matrix *a, cudaStream_t s, const double **out) {
+  if (a->kind != LGX_MATRIX_CSR) {
+    LGX_CHECK(stencil_ensure(a, s));
+    *out = a->diag.p;
+    return LGX_OK;
+  }
+  if (!a->diag.p) {
+    LGX_CHECK(a->diag.alloc(a->n));
+    const Csr &c = a->csr;
+    k_csr_diag<<<std::min<int64_t>(grid_for(a->n, 256), 8192), 256, 0, s>>>(
+      a->n, c.rowptr.p, c.col.p, c.storage == LGX_F64 ? c.v64.p : nullptr,
+      c.storage == LGX_F32 ? c.v32.p : nullptr, a->diag.p);
+    LGX_LAUNCH_CHECK();
+  }
+  *out = a->diag.p;
+  return LGX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Stencil -> CSR (csr/create-from.hpp:37-246)
+// ---------------------------------------------------------------------------
+__global__ void k_st_count(StencilDev S, int zero_to_one, const double *__restrict__ raw_diag,
+                           int64_t *keep, int64_t *rowlen, bool lookup) {
+  __shared__ double sh_conn[48];
+  const double *conn = stage_conn(S, sh_conn);
+  const int p2 = blockIdx.x * blockDim.x + threadIdx.x;
+  const int p1 = blockIdx.y * blockDim.y + threadIdx.y;
+  const int p0 = blockIdx.z;
+  if (p2 >= S.n2 || p1 >= S.n1) return;
+  const int64_t i = ((int64_t)p0 * S.n1 + p1) * S.n2 + p2;
+  double cv[6];
+  int64_t cj[6];
+  bool has[6];
+  if (lookup) st_row<true>(S, conn, p0, p1, p2, i, cv, cj, has);
+  else st_row<false>(S, conn, p0, p1, p2, i, cv, cj, has);
+  const bool kept = zero_to_one || S.diag[i] != 0.0;
+  keep[i] = kept;
+  int64_t c = 1;
+  for (int e = 0; e < 6; ++e) c += has[e] && cv[e] != 0.0;
+  rowlen[i] = kept ? c : 0;
+}
+
+__global__ void k_st_fill(StencilDev S, bool lookup, const int64_t *rowid_incl,
+                          const int64_t *rowptr_by_cell, int64_t *rowptr, int32_t *col,
+                          double *val, int64_t *cmap) {
+  __shared__ double sh_conn[48];
+  const double *conn = stage_conn(S, sh_conn);
+  const int p2 = blockIdx.x * blockDim.x + threadIdx.x;
+  const int p1 = blockIdx.y * blockDim.y + threadIdx.y;
+  const int p0 = blockIdx.z;
+  if (p2 >= S.n2 || p1 >= S.n1) return;
+  const int64_t i = ((int64_t)p0 * S.n1 + p1) * S.n2 + p2;
+  // rowid_incl: offsets array of the keep flags (rowid_incl[i] = rows before i)
+  const bool kept = rowid_incl[i + 1] != rowid_incl[i];
+  if (cmap) cmap[i] = kept ? rowid_incl[i] : -1;
+  if (!kept) return;
+  const int64_t r = rowid_incl[i];
+  int64_t pos = rowptr_by_cell[i];
+  rowptr[r] = pos;
+  double cv[6];
+  int64_t cj[6];
+  bool has[6];
+  if (lookup) st_row<true>(S, conn, p0, p1, p2, i, cv, cj, has);
+  else st_row<false>(S, conn, p0, p1, p2, i, cv, cj, has);
+  for (int e = 0; e < 3; ++e)
+    if (has[e] && cv[e] != 0.0) {
+      col[pos] = (int32_t)rowid_incl[cj[e]];
+      val[pos++] = -cv[e];
+    }
+  col[pos] = (int32_t)r;
+  val[pos++] = S.diag[i];
+  for (int e = 3; e < 6; ++e)
+    if (has[e] && cv[e] != 0.0) {
+      col[pos] = (int32_t)rowid_incl[cj[e]];
+      val[pos++] = -cv[e];
+    }
+}
+
+}  // namespace lgx
+
+using namespace lgx;
+
+extern "C" {
+
+static lgx_status stencil_create(const int64_t dims[3], const double q[3], const double coeffs[4],
+                                 const uint8_t *d_mat, const double *d_k, double sol_start,
+                                 double sol_end, int zero_to_one, lgx_stream stream,
+                                 lgx_matrix **out) {
+  if (!dims || !q || !out) return fail(LGX_ERR_INVALID, "null argument");
+  if (dims[0] < 1 || dims[1] < 1 || dims[2] < 1)
+    return fail(LGX_ERR_INVALID, "grid dimensions must be positive");
+  if (dims[0] > 65535) return fail(LGX_ERR_INVALID, "axis 0 is limited to 65535 cells");
+  const int64_t n = dims[0] * dims[1] * dims[2];
+  if (n > INT32_MAX) return fail(LGX_ERR_INVALID, "grid too large for 32-bit indices");
+  auto *m = new lgx_matrix();
+  m->kind = d_mat ? LGX_MATRIX_STENCIL_LOOKUP : LGX_MATRIX_STENCIL_VALUE;
+  m->n = n;
+  m->symmetric = 1;
+  StencilDesc &st = m->st;
+  for (int d = 0; d < 3; ++d) {
+    st.dims[d] = dims[d];
+    st.q[d] = q[d];
+  }
+  st.sol_start = sol_start;
+  st.sol_end = sol_end;
+  st.zero_to_one = zero_to_one;
+  st.lookup = d_mat != nullptr;
+  lgx_status s = LGX_OK;
+  if (d_mat) {
+    for (int c = 0; c < 4; ++c) st.coeffs[c] = coeffs[c];
+    // lookup-wright.hpp:73-85: conn[d][a*4+b] = hm(c_a, c_b) * q_d
+    for (int d = 0; d < 3; ++d)
+      for (int f = 0; f < 16; ++f) {
+        const double a = coeffs[f / 4], b = coeffs[f % 4];
+        const double p = a * b;
+        const double h = p != 0.0 ? (p + p) / (a + b) : 0.0;
+        st.conn[d * 16 + f] = h * q[d];
+      }
+    s = m->mat.alloc(n);
+    if (s == LGX_OK &&
+        cudaMemcpyAsync(m->mat.p, d_mat, n, cudaMemcpyDeviceToDevice, stream) != cudaSuccess)
+      s = fail(LGX_ERR_CUDA, "copying materials failed");
+  } else {
+    s = m->k.alloc(4 * n);  // k | face0 | face1 | face2
+    if (s == LGX_OK && cudaMemcpyAsync(m->k.p, d_k, sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                                       stream) != cudaSuccess)
+      s = fail(LGX_ERR_CUDA, "copying conductivities failed");
+  }
+  if (s == LGX_OK) s = stencil_ensure(m, stream);
+  if (s != LGX_OK) {
+    delete m;
+    return s;
+  }
+  // stored non-zeros of the assembled matrix (zero connections included)
+  int64_t nnz = n;
+  for (int d = 0; d < 3; ++d) nnz += 2 * (dims[d] - 1) * (n / dims[d]);
+  m->nnz = nnz;
+  *out = m;
+  return LGX_OK;
+}
+
+lgx_status lgx_stencil_create_lookup(const int64_t dims[3], const double q[3],
+                                     const double coeffs[4], const uint8_t *d_mat,
+                                     double sol_start, double sol_end, int zero_to_one,
+                                     lgx_stream stream, lgx_matrix **out) {
+  if (!d_mat || !coeffs) return fail(LGX_ERR_INVALID, "null materials");
+  return stencil_create(dims, q, coeffs, d_mat, nullptr, sol_start, sol_end, zero_to_one, stream,
+                        out);
+}
+
+lgx_status lgx_stencil_create_value(const int64_t dims[3], const double q[3], const double *d_k,
+                                    double sol_start, double sol_end, int zero_to_one,
+                                    lgx_stream stream, lgx_matrix **out) {
+  if (!d_k) return fail(LGX_ERR_INVALID, "null conductivities");
+  return stencil_create(dims, q, nullptr, nullptr, d_k, sol_start, sol_end, zero_to_one, stream,
+                        out);
+}
+
+lgx_status lgx_spmv(const lgx_matrix *a, const double *d_x, double *d_y, lgx_stream stream) {
+  if (!a || (a->n > 0 && (!d_x || !d_y))) return fail(LGX_ERR_INVALID, "null argument");
+  return matrix_spmv(a, d_x, d_y, stream);
+}
+
+lgx_status lgx_spmv_f32(const lgx_matrix *a, const float *d_x, float *d_y, lgx_stream stream) {
+  if (!a || (a->n > 0 && (!d_x || !d_y))) return fail(LGX_ERR_INVALID, "null argument");
+  if (a->kind != LGX_MATRIX_CSR || a->csr.storage != LGX_F32)
+    return fail(LGX_ERR_UNSUPPORTED, "lgx_spmv_f32 needs a float-stored CSR matrix");
+  return csr_spmv<float, float>(a->csr, a->csr.v32.p, d_x, d_y, stream);
+}
+
+lgx_status lgx_residual(const lgx_matrix *a, const double *d_b, const double *d_x, double *d_r,
+                        double *d_norm2sq, lgx_stream stream) {
+  if (!a || (a->n > 0 && (!d_b || !d_x || !d_r))) return fail(LGX_ERR_INVALID, "null argument");
+  DBuf<double> partials;
+  DBuf<unsigned> counter;
+  if (d_norm2sq) {
+    LGX_CHECK(partials.alloc(matrix_partials(a)));
+    LGX_CHECK(counter.alloc(1));
+    LGX_CUDA(cudaMemsetAsync(counter.p, 0, sizeof(unsigned), stream));
+  }
+  LGX_CHECK(matrix_residual(a, d_b, d_x, d_r, d_norm2sq, partials.p, counter.p, stream));
+  if (d_norm2sq) LGX_CUDA(cudaStreamSynchronize(stream));
+  return LGX_OK;
+}
+
+lgx_status lgx_diagonal(const lgx_matrix *a, double *d_diag, lgx_stream stream) {
+  if (!a || (a->n > 0 && !d_diag)) return fail(LGX_ERR_INVALID, "null argument");
+  const double *d = nullptr;
+  LGX_CHECK(matrix_diagonal(const_cast<lgx_matrix *>(a), stream, &d));
+  if (a->n)
+    LGX_CUDA(cudaMemcpyAsync(d_diag, d, sizeof(double) * a->n, cudaMemcpyDeviceToDevice, stream));
+  return LGX_OK;
+}
+
+lgx_status lgx_stencil_rhs(const lgx_matrix *a, double *d_b, lgx_stream stream) {
+  if (!a || !d_b) return fail(LGX_ERR_INVALID, "null argument");
+  if (a->kind == LGX_MATRIX_CSR) return fail(LGX_ERR_UNSUPPORTED, "not a stencil matrix");
+  const StencilDesc &st = a->st;
+  DBuf<double> cellv;
+  const double *cv = a->k.p;
+  if (st.lookup) {
+    LGX_CHECK(cellv.alloc(a->n));
+    k_st_cellvalue<<<std::min<int64_t>(grid_for(a->n, 256), 8192), 256, 0, stream>>>(
+      a->n, a->mat.p, st.coeffs[0], st.coeffs[1], st.coeffs[2], st.coeffs[3], cellv.p);
+    LGX_LAUNCH_CHECK();
+    cv = cellv.p;
+  }
+  k_st_rhs<<<st_grid(st), kStBlock, 0, stream>>>((int)st.dims[0], (int)st.dims[1],
+                                                 (int)st.dims[2], cv, 2.0 * st.q[0], st.sol_start,
+                                                 st.sol_end, d_b);
+  LGX_LAUNCH_CHECK();
+  LGX_CUDA(cudaStreamSynchronize(stream));
+  return LGX_OK;
+}
+
+lgx_status lgx_stencil_to_csr(const lgx_matrix *ac, int64_t *d_compress_map, lgx_stream stream,
+                              lgx_matrix **out) {
+  if (!ac || !out) return fail(LGX_ERR_INVALID, "null argument");
+  if (ac->kind == LGX_MATRIX_CSR) return fail(LGX_ERR_UNSUPPORTED, "not a stencil matrix");
+  lgx_matrix *a = const_cast<lgx_matrix *>(ac);
+  LGX_CHECK(stencil_ensure(a, stream));
+  const int64_t n = a->n;
+  DBuf<int64_t> keep, rowlen, rowid, rptr_cell;
+  LGX_CHECK(keep.alloc(n));
+  LGX_CHECK(rowlen.alloc(n));
+  LGX_CHECK(rowid.alloc(n + 1));
+  LGX_CHECK(rptr_cell.alloc(n + 1));
+  StencilDev S = dev_of(a);
+  const dim3 g = st_grid(a->st);
+  k_st_count<<<g, kStBlock, 0, stream>>>(S, a->st.zero_to_one, a->diag.p, keep.p, rowlen.p,
+                                         a->st.lookup != 0);
+  LGX_LAUNCH_CHECK();
+  LGX_CHECK(inclusive_offsets(n, keep.p, rowid.p, stream));
+  LGX_CHECK(inclusive_offsets(n, rowlen.p, rptr_cell.p, stream));
+  int64_t rows = 0, nnz = 0;
+  LGX_CUDA(cudaMemcpyAsync(&rows, rowid.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, stream));
+  LGX_CUDA(cudaMemcpyAsync(&nnz, rptr_cell.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost,
+                           stream));
+  LGX_CUDA(cudaStreamSynchronize(stream));
+  DBuf<int64_t> rowptr;
+  DBuf<int32_t> col;
+  DBuf<double> val;
+  LGX_CHECK(rowptr.alloc(rows + 1));
+  LGX_CHECK(col.alloc(nnz));
+  LGX_CHECK(val.alloc(nnz));
+  k_st_fill<<<g, kStBlock, 0, stream>>>(S, a->st.lookup != 0, rowid.p, rptr_cell.p, rowptr.p,
+                                        col.p, val.p, d_compress_map);
+  LGX_LAUNCH_CHECK();
+  LGX_CUDA(cudaMemcpyAsync(rowptr.p + rows, &nnz, sizeof(int64_t), cudaMemcpyHostToDevice,
+                           stream));
+  return lgx_csr_create(rows, nnz, rowptr.p, col.p, val.p, 1, LGX_F64, stream, out);
+}
+
+}  // extern "C"

@@ -1,0 +1,467 @@
+/*
+ * Oracle core: partitions, geometry, valuators, stencil rows, CSR assembly,
+ * generators, CSR kernels, reductions and colouring.
+ * TEST INFRASTRUCTURE ONLY (see lineal_oracle.h).
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "lineal_oracle.h"
+
+void lo_csr_free(lo_csr *a) {
+  free(a->rowptr);
+  free(a->col);
+  free(a->val);
+  a->rowptr = NULL;
+  a->col = NULL;
+  a->val = NULL;
+}
+
+int64_t lo_csr_nnz(const lo_csr *a) { return a->rowptr[a->n]; }
+
+int lo_csr_alloc(lo_csr *a, int64_t n, int64_t nnz) {
+  a->n = n;
+  a->ncols = n;
+  a->rowptr = (int64_t *)calloc((size_t)n + 1, sizeof(int64_t));
+  a->col = (int32_t *)malloc((size_t)(nnz > 0 ? nnz : 1) * sizeof(int32_t));
+  a->val = (double *)malloc((size_t)(nnz > 0 ? nnz : 1) * sizeof(double));
+  a->symmetric = 0;
+  a->is_f32 = 0;
+  return (a->rowptr && a->col && a->val) ? 0 : -1;
+}
+
+int64_t lo_part_begin(int64_t n, int64_t p, int64_t k) {
+  const int64_t base = n / p, rem = n % p;
+  return k * base + (k < rem ? k : rem);
+}
+
+/* box-equidistant.hpp:67-79: q_d = prod_{e != d} h_e / h_d with h = L / N */
+void lo_axis_quotients(const int64_t dims[3], const double lengths[3], double q[3]) {
+  double h[3];
+  for (int d = 0; d < 3; ++d) h[d] = lengths[d] / (double)dims[d];
+  for (int d = 0; d < 3; ++d) {
+    double area = 1.0;
+    for (int e = 0; e < 3; ++e)
+      if (e != d) area = area * h[e];
+    q[d] = area / h[d];
+  }
+}
+
+/* math/harmonic-mean.hpp:13-25: 2ab/(a+b) if ab != 0 else 0 */
+double lo_harmonic_mean(double a, double b) {
+  const double p = a * b;
+  return p != 0.0 ? (p + p) / (a + b) : 0.0;
+}
+
+/* test/aux/materials.hpp:217-233: (sum of coordinates except the flow axis)
+ * modulo the material count; index -> position is row-major, last axis
+ * fastest (python-reference/defs/defs.py:63-70). */
+void lo_material_diagonal_lines(const int64_t dims[3], int64_t max_material_num, uint8_t *mat) {
+  const int64_t n = dims[0] * dims[1] * dims[2];
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t z = i % dims[2], y = (i / dims[2]) % dims[1];
+    mat[i] = (uint8_t)((y + z) % max_material_num);
+  }
+}
+
+/* python-reference/defs/materials.py:22-38 (flow axis 0) */
+void lo_material_flow_cylinder_gap(const int64_t dims[3], double radius, uint8_t *mat) {
+  const int64_t n = dims[0] * dims[1] * dims[2];
+  const int64_t mid = dims[0] / 2;
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t z = i % dims[2], y = (i / dims[2]) % dims[1], x = i / (dims[1] * dims[2]);
+    const double fy = (double)y / (double)dims[1] - 0.5, fz = (double)z / (double)dims[2] - 0.5;
+    const double v = fy * fy + fz * fz;
+    mat[i] = (v <= radius && x != mid) ? 3 : 0;
+  }
+}
+
+/* lookup-wright.hpp:73-85 */
+void lo_lookup_tables(const double coeffs[4], const double q[3], double conn[48]) {
+  for (int d = 0; d < 3; ++d)
+    for (int f = 0; f < 16; ++f)
+      conn[d * 16 + f] = lo_harmonic_mean(coeffs[f / 4], coeffs[f % 4]) * q[d];
+}
+
+void lo_stencil_init(lo_stencil *s) {
+  if (!s->k) lo_lookup_tables(s->coeffs, s->q, s->conn);
+}
+
+static inline double st_cell_value(const lo_stencil *s, int64_t i) {
+  return s->k ? s->k[i] : s->coeffs[s->mat[i]];
+}
+/* connection_value (lookup: table gather; value: hm(k_from, k_to) * q_d) */
+static inline double st_conn(const lo_stencil *s, int d, int64_t from, int64_t to) {
+  if (s->k) return lo_harmonic_mean(s->k[from], s->k[to]) * s->q[d];
+  return s->conn[d * 16 + s->mat[from] * 4 + s->mat[to]];
+}
+
+typedef struct {
+  int64_t cols[7];
+  double vals[7];
+  int cnt;     /* off-diagonal entries in visiting order, then the diagonal */
+  double diag;
+} st_row;
+
+/* algorithm.hpp:93-227 (valued, unordered): diagonal starts at
+ * diagonal_base (0), border summands of the flow axis (start, end), then the
+ * "before" neighbours of dims 0,1,2 and the "after" neighbours of dims 2,1,0
+ * each adding their connection value; finally valuator.diagonal(). */
+static void st_make_row(const lo_stencil *s, int64_t idx, st_row *row) {
+  const int64_t n1 = s->dims[1], n2 = s->dims[2];
+  const int64_t stride[3] = {n1 * n2, n2, 1};
+  const int64_t pos[3] = {idx / (n1 * n2), (idx / n2) % n1, idx % n2};
+  const double cv = st_cell_value(s, idx);
+  double diag = 0.0;
+  if (pos[0] == 0) diag += (2.0 * s->q[0]) * cv;
+  if (pos[0] + 1 == s->dims[0]) diag += (2.0 * s->q[0]) * cv;
+  row->cnt = 0;
+  for (int d = 0; d < 3; ++d) {
+    if (pos[d] > 0) {
+      const int64_t j = idx - stride[d];
+      const double c = st_conn(s, d, idx, j);
+      row->cols[row->cnt] = j;
+      row->vals[row->cnt] = -c;
+      ++row->cnt;
+      diag += c;
+    }
+  }
+  for (int d = 2; d >= 0; --d) {
+    if (pos[d] + 1 < s->dims[d]) {
+      const int64_t j = idx + stride[d];
+      const double c = st_conn(s, d, idx, j);
+      row->cols[row->cnt] = j;
+      row->vals[row->cnt] = -c;
+      ++row->cnt;
+      diag += c;
+    }
+  }
+  if (s->zero_to_one && diag == 0.0) diag = 1.0;
+  row->diag = diag;
+}
+
+void lo_stencil_spmv(const lo_stencil *s, const double *x, double *y) {
+  const int64_t n = s->dims[0] * s->dims[1] * s->dims[2];
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    st_row row;
+    st_make_row(s, i, &row);
+    double sum = 0.0;
+    for (int e = 0; e < row.cnt; ++e) sum = fma(row.vals[e], x[row.cols[e]], sum);
+    y[i] = fma(row.diag, x[i], sum);
+  }
+}
+
+void lo_stencil_diagonal(const lo_stencil *s, double *d) {
+  const int64_t n = s->dims[0] * s->dims[1] * s->dims[2];
+  for (int64_t i = 0; i < n; ++i) {
+    st_row row;
+    st_make_row(s, i, &row);
+    d[i] = row.diag;
+  }
+}
+
+/* stencil/vector/shared.hpp:181-205: border_rhs_summand = 2 q_0 c * u_D */
+void lo_stencil_rhs(const lo_stencil *s, double *b) {
+  const int64_t n1 = s->dims[1], n2 = s->dims[2];
+  const int64_t n = s->dims[0] * n1 * n2;
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t p0 = i / (n1 * n2);
+    const double cv = st_cell_value(s, i);
+    double sum = 0.0;
+    if (p0 == 0) sum += ((2.0 * s->q[0]) * cv) * s->sol_start;
+    if (p0 + 1 == s->dims[0]) sum += ((2.0 * s->q[0]) * cv) * s->sol_end;
+    b[i] = sum;
+  }
+}
+
+/* csr/create-from.hpp:82-232: rows of the stencil matrix with zero
+ * off-diagonals dropped and sorted columns; with ZeroToZero valuators rows
+ * whose diagonal is 0 are removed (compress map). */
+int lo_stencil_to_csr(const lo_stencil *s, lo_csr *out, int64_t *compress_map) {
+  const int64_t n = s->dims[0] * s->dims[1] * s->dims[2];
+  int64_t *cmap = (int64_t *)malloc((size_t)n * sizeof(int64_t));
+  int64_t rows = 0, nnz = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    st_row row;
+    st_make_row(s, i, &row);
+    if (!s->zero_to_one && row.diag == 0.0) {
+      cmap[i] = -1;
+      continue;
+    }
+    cmap[i] = rows++;
+    nnz += 1;
+    for (int e = 0; e < row.cnt; ++e) nnz += row.vals[e] != 0.0;
+  }
+  if (lo_csr_alloc(out, rows, nnz)) {
+    free(cmap);
+    return -1;
+  }
+  int64_t pos = 0, r = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    if (cmap[i] < 0) continue;
+    st_row row;
+    st_make_row(s, i, &row);
+    out->rowptr[r] = pos;
+    /* sorted insertion: before entries are ascending, then diagonal, then after ascending */
+    int64_t cols[7];
+    double vals[7];
+    int cnt = 0;
+    for (int e = 0; e < row.cnt; ++e) {
+      if (row.vals[e] == 0.0) continue;
+      cols[cnt] = cmap[row.cols[e]];
+      vals[cnt] = row.vals[e];
+      ++cnt;
+    }
+    cols[cnt] = r;
+    vals[cnt] = row.diag;
+    ++cnt;
+    for (int a = 1; a < cnt; ++a) { /* insertion sort, tiny */
+      int64_t c = cols[a];
+      double v = vals[a];
+      int b = a - 1;
+      while (b >= 0 && cols[b] > c) {
+        cols[b + 1] = cols[b];
+        vals[b + 1] = vals[b];
+        --b;
+      }
+      cols[b + 1] = c;
+      vals[b + 1] = v;
+    }
+    for (int e = 0; e < cnt; ++e) {
+      out->col[pos] = (int32_t)cols[e];
+      out->val[pos] = vals[e];
+      ++pos;
+    }
+    ++r;
+  }
+  out->rowptr[rows] = pos;
+  out->symmetric = 1;
+  if (compress_map) memcpy(compress_map, cmap, (size_t)n * sizeof(int64_t));
+  free(cmap);
+  return 0;
+}
+
+/* Generic structured assembly used by the 27-point and 7-point generators. */
+static int gen_structured(const int64_t dims[3], const double *k, int npts, lo_csr *out) {
+  const int64_t n0 = dims[0], n1 = dims[1], n2 = dims[2];
+  const int64_t n = n0 * n1 * n2;
+  /* count */
+  int64_t nnz = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t p[3] = {i / (n1 * n2), (i / n2) % n1, i % n2};
+    int64_t c = 1;
+    for (int a = -1; a <= 1; ++a)
+      for (int b = -1; b <= 1; ++b)
+        for (int cc = -1; cc <= 1; ++cc) {
+          const int m = abs(a) + abs(b) + abs(cc);
+          if (m == 0 || (npts == 7 && m != 1)) continue;
+          if (p[0] + a < 0 || p[0] + a >= n0 || p[1] + b < 0 || p[1] + b >= n1 ||
+              p[2] + cc < 0 || p[2] + cc >= n2)
+            continue;
+          ++c;
+        }
+    nnz += c;
+  }
+  if (lo_csr_alloc(out, n, nnz)) return -1;
+  static const double w[4] = {0.0, 1.0, 0.5, 0.25};
+  int64_t pos = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t p[3] = {i / (n1 * n2), (i / n2) % n1, i % n2};
+    out->rowptr[i] = pos;
+    const double ki = k[i];
+    double diag = 0.0;
+    if (p[0] == 0) diag = diag + 2.0 * ki;
+    if (p[0] + 1 == n0) diag = diag + 2.0 * ki;
+    int64_t dpos = -1;
+    /* offsets in ascending column order: a (axis 0) outermost */
+    for (int a = -1; a <= 1; ++a)
+      for (int b = -1; b <= 1; ++b)
+        for (int cc = -1; cc <= 1; ++cc) {
+          const int m = abs(a) + abs(b) + abs(cc);
+          if (npts == 7 && m > 1) continue;
+          if (p[0] + a < 0 || p[0] + a >= n0 || p[1] + b < 0 || p[1] + b >= n1 ||
+              p[2] + cc < 0 || p[2] + cc >= n2)
+            continue;
+          const int64_t j = i + a * n1 * n2 + b * n2 + cc;
+          out->col[pos] = (int32_t)j;
+          if (m == 0) {
+            dpos = pos;
+            out->val[pos] = 0.0;
+          } else {
+            const double c = lo_harmonic_mean(ki, k[j]) * w[m];
+            out->val[pos] = -c;
+            diag = diag + c;
+          }
+          ++pos;
+        }
+    if (diag == 0.0) diag = 1.0;
+    out->val[dpos] = diag;
+  }
+  out->rowptr[n] = pos;
+  out->symmetric = 1;
+  return 0;
+}
+
+int lo_gen_27pt(const int64_t dims[3], const double *k, lo_csr *out) {
+  return gen_structured(dims, k, 27, out);
+}
+int lo_gen_7pt(const int64_t dims[3], const double *k, lo_csr *out) {
+  return gen_structured(dims, k, 7, out);
+}
+
+/* First-order upwind convection-diffusion, D = 1, unit spacing:
+ * a_ij = -(1 + max(-v_d*s, 0)) for the neighbour at side s (+1/-1) of axis d,
+ * a_ii = sum of |a_ij| over all six directions (missing neighbours act as
+ * zero Dirichlet values, so they still count). */
+int lo_gen_convdiff(const int64_t dims[3], const double v[3], lo_csr *out) {
+  const int64_t n0 = dims[0], n1 = dims[1], n2 = dims[2];
+  const int64_t n = n0 * n1 * n2;
+  const int64_t stride[3] = {n1 * n2, n2, 1};
+  int64_t nnz = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t p[3] = {i / (n1 * n2), (i / n2) % n1, i % n2};
+    nnz += 1;
+    for (int d = 0; d < 3; ++d) nnz += (p[d] > 0) + (p[d] + 1 < dims[d]);
+  }
+  if (lo_csr_alloc(out, n, nnz)) return -1;
+  int64_t pos = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t p[3] = {i / (n1 * n2), (i / n2) % n1, i % n2};
+    out->rowptr[i] = pos;
+    double off[6];
+    for (int d = 0; d < 3; ++d) {
+      const double up_minus = v[d] > 0.0 ? v[d] : 0.0;  /* inflow from the - side */
+      const double up_plus = v[d] < 0.0 ? -v[d] : 0.0;  /* inflow from the + side */
+      off[2 * d] = 1.0 + up_minus;
+      off[2 * d + 1] = 1.0 + up_plus;
+    }
+    double diag = 0.0;
+    for (int e = 0; e < 6; ++e) diag = diag + off[e];
+    /* ascending columns: -d0, -d1, -d2, diag, +d2, +d1, +d0 */
+    for (int d = 0; d < 3; ++d)
+      if (p[d] > 0) {
+        out->col[pos] = (int32_t)(i - stride[d]);
+        out->val[pos++] = -off[2 * d];
+      }
+    out->col[pos] = (int32_t)i;
+    out->val[pos++] = diag;
+    for (int d = 2; d >= 0; --d)
+      if (p[d] + 1 < dims[d]) {
+        out->col[pos] = (int32_t)(i + stride[d]);
+        out->val[pos++] = -off[2 * d + 1];
+      }
+  }
+  out->rowptr[n] = pos;
+  out->symmetric = 0;
+  return 0;
+}
+
+/* matrix-vector-product.hpp:71-82 */
+void lo_csr_spmv(const lo_csr *a, const double *x, double *y) {
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < a->n; ++i) {
+    double sum = 0.0;
+    for (int64_t e = a->rowptr[i]; e < a->rowptr[i + 1]; ++e) sum = fma(a->val[e], x[a->col[e]], sum);
+    y[i] = sum;
+  }
+}
+
+void lo_csr_residual(const lo_csr *a, const double *b, const double *x, double *r) {
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < a->n; ++i) {
+    double sum = 0.0;
+    for (int64_t e = a->rowptr[i]; e < a->rowptr[i + 1]; ++e) sum = fma(a->val[e], x[a->col[e]], sum);
+    r[i] = b[i] - sum;
+  }
+}
+
+double lo_dot(int64_t n, const double *a, const double *b) {
+  double s = 0.0;
+  for (int64_t i = 0; i < n; ++i) s += a[i] * b[i];
+  return s;
+}
+double lo_norm2sq(int64_t n, const double *a) { return lo_dot(n, a, a); }
+double lo_max_norm(int64_t n, const double *a) {
+  double m = 0.0;
+  for (int64_t i = 0; i < n; ++i) {
+    const double v = fabs(a[i]);
+    if (v > m) m = v;
+  }
+  return m;
+}
+
+/* splitmix64 finaliser: priority of vertex i for the colouring */
+static uint64_t lo_hash(uint64_t seed, uint64_t i) {
+  uint64_t z = seed * 0x9E3779B97F4A7C15ull + i + 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+/* Jones-Plassmann: in each round every uncoloured vertex whose (priority,
+ * index) exceeds that of all uncoloured neighbours takes the smallest colour
+ * not used by an already coloured neighbour (colours of the current round
+ * are not visible within the round, so the result is order independent). */
+int32_t lo_colour_jp(const lo_csr *a, uint64_t seed, int32_t *colour) {
+  const int64_t n = a->n;
+  uint64_t *prio = (uint64_t *)malloc((size_t)n * sizeof(uint64_t));
+  int32_t *next = (int32_t *)malloc((size_t)n * sizeof(int32_t));
+  for (int64_t i = 0; i < n; ++i) {
+    prio[i] = lo_hash(seed, (uint64_t)i);
+    colour[i] = -1;
+  }
+  int64_t left = n;
+  int32_t ncol = 0;
+  while (left > 0) {
+    for (int64_t i = 0; i < n; ++i) {
+      next[i] = -1;
+      if (colour[i] >= 0) continue;
+      int is_max = 1;
+      uint64_t used = 0; /* colours < 64 as a bitmask, larger ones by scan */
+      for (int64_t e = a->rowptr[i]; e < a->rowptr[i + 1]; ++e) {
+        const int64_t j = a->col[e];
+        if (j == i) continue;
+        if (colour[j] < 0) {
+          if (prio[j] > prio[i] || (prio[j] == prio[i] && j > i)) {
+            is_max = 0;
+            break;
+          }
+        } else if (colour[j] < 64) {
+          used |= 1ull << colour[j];
+        }
+      }
+      if (!is_max) continue;
+      int32_t c = 0;
+      for (;;) {
+        int taken = 0;
+        if (c < 64) {
+          taken = (int)((used >> c) & 1ull);
+        } else {
+          for (int64_t e = a->rowptr[i]; e < a->rowptr[i + 1]; ++e)
+            if (a->col[e] != i && colour[a->col[e]] == c) taken = 1;
+        }
+        if (!taken) break;
+        ++c;
+      }
+      next[i] = c;
+    }
+    for (int64_t i = 0; i < n; ++i)
+      if (next[i] >= 0) {
+        colour[i] = next[i];
+        --left;
+        if (next[i] + 1 > ncol) ncol = next[i] + 1;
+      }
+  }
+  free(prio);
+  free(next);
+  return ncol;
+}
+
+void lo_colour_order(int64_t n, const int32_t *colour, int32_t ncolours, int32_t *order) {
+  int64_t pos = 0;
+  for (int32_t c = 0; c < ncolours; ++c)
+    for (int64_t i = 0; i < n; ++i)
+      if (colour[i] == c) order[pos++] = (int32_t)i;
+}

@@ -1,0 +1,59 @@
+"""CPU-side checks of the C ABI: the library builds for sm_103a, loads, and
+exports every entry point that include/lineal_gb300.h declares.  No compute
+calls are made (there is no GPU here)."""
+
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "lineal_gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(lgx_\w+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope="module")
+def library():
+    from lineal_gb300 import build
+
+    return build.build()
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    assert "lgx_spmv" in names and "lgx_pcg" in names and "lgx_amg_setup" in names
+    assert len(names) >= 30
+
+
+def test_library_exports_every_declared_symbol(library):
+    out = subprocess.run(["nm", "-D", "--defined-only", library], capture_output=True, text=True,
+                         check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    missing = [n for n in declared_functions() if n not in exported]
+    assert not missing, f"declared but not exported: {missing}"
+
+
+def test_library_loads_without_gpu(library):
+    lib = ctypes.CDLL(library)
+    lib.lgx_version.restype = ctypes.c_char_p
+    assert b"sm_103a" in lib.lgx_version()
+    lib.lgx_status_string.restype = ctypes.c_char_p
+    assert lib.lgx_status_string(0) == b"ok"
+
+
+def test_invalid_arguments_are_statuses(library):
+    import lineal_gb300 as g
+
+    lib = g.lib()
+    # null handles are rejected on the host before any device work
+    assert lib.lgx_spmv(None, None, None, None) == 1
+    assert lib.lgx_matrix_info(None, None, None, None, None) == 1
+    assert b"null" in lib.lgx_last_error()

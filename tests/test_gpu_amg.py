@@ -1,0 +1,124 @@
+"""GPU parity of the AMG setup (bit-exact integer/bit data and level
+matrices) and of the V-cycle against the oracle."""
+
+import os
+
+import numpy as np
+import pytest
+
+import oracle as lo
+from lineal_gb300 import io as lio
+
+pytestmark = pytest.mark.gpu
+
+
+def _case(dims=(14, 15, 16), seed=1, sigma=1.5, npts=27):
+    n = int(np.prod(dims))
+    k = np.exp(sigma * np.random.default_rng(seed).standard_normal(n))
+    return (lo.gen_27pt if npts == 27 else lo.gen_7pt)(dims, k)
+
+
+def _dev(cuda, ref, storage=0):
+    return cuda.CsrMatrix.from_host(ref.rowptr, ref.col, ref.val, symmetric=ref.symmetric,
+                                    storage=storage)
+
+
+def _ufz(golden_dir):
+    rowptr, col, val, _ = lio.read_smf(os.path.join(golden_dir, "UFZ_CT_02_LHS.smf"))
+    return lo.Csr(rowptr, col, val, symmetric=False)
+
+
+@pytest.mark.parametrize("which", ["27pt", "7pt", "ufz"])
+def test_strength_bitexact(cuda, golden_dir, which):
+    ref = _ufz(golden_dir) if which == "ufz" else _case(npts=27 if which == "27pt" else 7)
+    m = _dev(cuda, ref)
+    dep, inf, iso = cuda.amg_strength(m)
+    rdep, rinf, riso = lo.amg_strength(ref)
+    np.testing.assert_array_equal(dep.cpu().numpy(), rdep)
+    np.testing.assert_array_equal(inf.cpu().numpy(), rinf)
+    np.testing.assert_array_equal(iso.cpu().numpy(), riso)
+
+
+@pytest.mark.parametrize("nparts", [1, 7, 64])
+@pytest.mark.parametrize("aggressive", [False, True])
+def test_aggregation_bitexact(cuda, nparts, aggressive):
+    ref = _case()
+    m = _dev(cuda, ref)
+    dep, inf, iso = cuda.amg_strength(m)
+    nc, agg = cuda.amg_aggregate(m, dep, inf, iso, 6, 9, nparts, aggressive)
+    rdep, rinf, riso = lo.amg_strength(ref)
+    rnc, ragg, _, _, _ = lo.amg_aggregate(ref, rdep, rinf, riso, 6, 9, nparts, aggressive)
+    assert nc == rnc
+    np.testing.assert_array_equal(agg, ragg)
+
+
+def test_aggregation_ufz_bitexact(cuda, golden_dir):
+    ref = _ufz(golden_dir)
+    m = _dev(cuda, ref)
+    dep, inf, iso = cuda.amg_strength(m)
+    nc, agg = cuda.amg_aggregate(m, dep, inf, iso, 6, 9, 4)
+    rdep, rinf, riso = lo.amg_strength(ref)
+    rnc, ragg, _, _, _ = lo.amg_aggregate(ref, rdep, rinf, riso, 6, 9, 4)
+    assert nc == rnc
+    np.testing.assert_array_equal(agg, ragg)
+
+
+PARAMS = dict(min_coarsen_size=64, partition_size=512, max_partitions=1 << 30)
+
+
+@pytest.mark.parametrize("coarse_f32", [False, True])
+def test_hierarchy_bitexact(cuda, coarse_f32):
+    ref = _case()
+    m = _dev(cuda, ref)
+    h = cuda.HierarchyWright(coarse_f32=coarse_f32, **PARAMS).instantiate(m)
+    oh = lo.Amg(ref, coarse_f32=int(coarse_f32), smoother_parts=0, **PARAMS)
+    rows, _ = h.sizes()
+    assert len(rows) == oh.nlevels >= 3
+    for l in range(oh.nlevels):
+        rowptr, col, val, agg = h.level(l)
+        rl = oh.level_csr(l)
+        np.testing.assert_array_equal(rowptr, rl.rowptr)
+        np.testing.assert_array_equal(col, rl.col)
+        np.testing.assert_array_equal(val, rl.val)
+        if agg is not None:
+            np.testing.assert_array_equal(agg, oh.level_agg(l))
+
+
+@pytest.mark.parametrize("coarse_f32", [False, True])
+def test_vcycle_matches_oracle(cuda, coarse_f32):
+    ref = _case()
+    m = _dev(cuda, ref)
+    h = cuda.HierarchyWright(coarse_f32=coarse_f32, **PARAMS).instantiate(m)
+    oh = lo.Amg(ref, coarse_f32=int(coarse_f32), smoother_parts=0, **PARAMS)
+    b = np.random.default_rng(3).uniform(-1, 1, ref.n)
+    got = h.vcycle(b).cpu().numpy()
+    want = oh.vcycle(b)
+    # same colour orders and level matrices; the coarsest solve is a dense
+    # inverse on the GPU and a Cholesky substitution in the oracle
+    assert np.abs(got - want).max() <= 1e-11 * np.abs(want).max()
+
+
+def test_vcycle_float_cycle(cuda):
+    ref = _case()
+    m = _dev(cuda, ref)
+    h = cuda.HierarchyWright(cycle_f32=True, **PARAMS).instantiate(m)
+    oh = lo.Amg(ref, smoother_parts=0, **PARAMS)
+    b = np.random.default_rng(3).uniform(-1, 1, ref.n)
+    got = h.vcycle(b).cpu().numpy()
+    want = oh.vcycle(b)
+    assert np.abs(got - want).max() <= 1e-4 * np.abs(want).max()
+
+
+def test_finest_parity_colouring(cuda):
+    dims = (12, 12, 12)
+    ref = _case(dims)
+    m = _dev(cuda, ref)
+    i, j, k = np.meshgrid(*[np.arange(d) for d in dims], indexing="ij")
+    colours = ((i % 2) * 4 + (j % 2) * 2 + (k % 2)).ravel().astype(np.int32)
+    col = cuda.Colouring.from_array(m, colours, 8)
+    h = cuda.HierarchyWright(**PARAMS).instantiate(m, finest_colouring=col)
+    b = np.random.default_rng(1).uniform(-1, 1, ref.n)
+    x = h.vcycle(b).cpu().numpy()
+    # one V-cycle reduces the residual of the error equation
+    r = b - lo.spmv(ref, x)
+    assert np.linalg.norm(r) < 0.5 * np.linalg.norm(b)

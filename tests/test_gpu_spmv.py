@@ -1,0 +1,137 @@
+"""GPU parity of the operators against the oracle (bit-exact where the
+summation order is the reference's scalar order)."""
+
+import os
+
+import numpy as np
+import pytest
+
+import oracle as lo
+from lineal_gb300 import io as lio
+
+pytestmark = pytest.mark.gpu
+
+
+def _ufz(golden_dir):
+    rowptr, col, val, _ = lio.read_smf(os.path.join(golden_dir, "UFZ_CT_02_LHS.smf"))
+    b = lio.read_dvf(os.path.join(golden_dir, "UFZ_CT_02_RHS.dvf"))
+    return lo.Csr(rowptr, col, val, symmetric=False), b
+
+
+def test_csr_spmv_ufz_bitexact(cuda, golden_dir):
+    a, b = _ufz(golden_dir)
+    m = cuda.CsrMatrix.from_host(a.rowptr, a.col, a.val, symmetric=False)
+    assert m.info()[1:3] == (a.n, a.nnz)
+    for seed in range(3):
+        x = np.random.default_rng(seed).uniform(-1, 1, a.n)
+        y = cuda.spmv(m, x).cpu().numpy()
+        np.testing.assert_array_equal(y, lo.spmv(a, x))
+    r, nrm = cuda.residual(m, b, x)
+    ref = lo.residual(a, b, x)
+    np.testing.assert_array_equal(r.cpu().numpy(), ref)
+    assert abs(nrm - ref @ ref) <= 1e-14 * (ref @ ref)
+
+
+@pytest.mark.parametrize("dims", [(5, 6, 7), (16, 9, 33), (1, 1, 1), (40, 3, 2)])
+@pytest.mark.parametrize("npts", [27, 7])
+def test_generator_bitexact(cuda, dims, npts):
+    n = int(np.prod(dims))
+    k = np.exp(1.5 * np.random.default_rng(1).standard_normal(n))
+    gen = cuda.gen_27pt if npts == 27 else cuda.gen_7pt
+    m = gen(dims, k)
+    ref = (lo.gen_27pt if npts == 27 else lo.gen_7pt)(dims, k)
+    rowptr, col, val = m.download()
+    np.testing.assert_array_equal(rowptr, ref.rowptr)
+    np.testing.assert_array_equal(col, ref.col)
+    np.testing.assert_array_equal(val, ref.val)
+    x = np.random.default_rng(5).uniform(-1, 1, n)
+    np.testing.assert_array_equal(cuda.spmv(m, x).cpu().numpy(), lo.spmv(ref, x))
+
+
+def test_generator_f32_storage(cuda):
+    dims = (12, 10, 9)
+    n = int(np.prod(dims))
+    k = np.exp(np.random.default_rng(3).standard_normal(n))
+    m32 = cuda.gen_27pt(dims, k, storage=cuda.F32)
+    ref = lo.gen_27pt(dims, k)
+    x = np.random.default_rng(4).uniform(-1, 1, n)
+    v32 = ref.val.astype(np.float32).astype(np.float64)
+    ref32 = lo.Csr(ref.rowptr, ref.col, v32)
+    # double accumulation over float-stored values
+    np.testing.assert_array_equal(cuda.spmv(m32, x).cpu().numpy(), lo.spmv(ref32, x))
+    y = cuda.spmv_f32(m32, x.astype(np.float32)).cpu().numpy().astype(np.float64)
+    exact = lo.spmv(ref32, x.astype(np.float32).astype(np.float64))
+    assert np.abs(y - exact).max() <= 1e-5 * np.abs(exact).max()
+
+
+def _lookup_case(dims, seed):
+    rng = np.random.default_rng(seed)
+    mat = rng.integers(0, 4, int(np.prod(dims))).astype(np.uint8)
+    return mat
+
+
+@pytest.mark.parametrize("dims", [(4, 9, 7), (17, 13, 19), (1, 5, 3), (33, 1, 40)])
+@pytest.mark.parametrize("zero_to_one", [True, False])
+def test_stencil_lookup_bitexact(cuda, dims, zero_to_one):
+    mat = _lookup_case(dims, 11)
+    q = lo.axis_quotients(dims, (1.3, 0.7, 2.1))
+    coeffs = (0.0, 1.0, 2.0, 3.0)
+    ref = lo.Stencil(dims, q=q, mat=mat, coeffs=coeffs, sol_start=1.0, sol_end=0.5,
+                     zero_to_one=zero_to_one)
+    m = cuda.StencilMatrix.lookup(dims, q, coeffs, mat, 1.0, 0.5, zero_to_one)
+    x = np.random.default_rng(2).uniform(-1, 1, ref.n)
+    np.testing.assert_array_equal(cuda.spmv(m, x).cpu().numpy(), ref.spmv(x))
+    np.testing.assert_array_equal(m.diagonal().cpu().numpy(), ref.diagonal())
+    np.testing.assert_array_equal(m.rhs().cpu().numpy(), ref.rhs())
+    csr, cmap = m.to_csr(with_compress_map=True)
+    rcsr, rcmap = ref.to_csr()
+    rowptr, col, val = csr.download()
+    np.testing.assert_array_equal(rowptr, rcsr.rowptr)
+    np.testing.assert_array_equal(col, rcsr.col)
+    np.testing.assert_array_equal(val, rcsr.val)
+    np.testing.assert_array_equal(cmap.cpu().numpy(), rcmap)
+
+
+@pytest.mark.parametrize("dims", [(4, 9, 7), (21, 8, 30)])
+def test_stencil_value_bitexact(cuda, dims):
+    n = int(np.prod(dims))
+    k = np.exp(np.random.default_rng(9).standard_normal(n))
+    k[::7] = 0.0  # zero conductivities exercise the harmonic-mean guard
+    q = lo.axis_quotients(dims, dims)
+    ref = lo.Stencil(dims, q=q, k=k, sol_start=1.0, sol_end=0.0)
+    m = cuda.StencilMatrix.value(dims, q, k, 1.0, 0.0)
+    x = np.random.default_rng(8).uniform(-1, 1, n)
+    np.testing.assert_array_equal(cuda.spmv(m, x).cpu().numpy(), ref.spmv(x))
+    np.testing.assert_array_equal(m.rhs().cpu().numpy(), ref.rhs())
+    b = ref.rhs()
+    r, nrm = cuda.residual(m, b, x)
+    rr = b - ref.spmv(x)
+    np.testing.assert_array_equal(r.cpu().numpy(), rr)
+    assert abs(nrm - rr @ rr) <= 1e-13 * (rr @ rr)
+
+
+def test_reductions(cuda):
+    rng = np.random.default_rng(0)
+    for n in (1, 255, 256 * 8 + 3, 1 << 20):
+        a = rng.uniform(-1, 1, n)
+        b = rng.uniform(-1, 1, n)
+        assert abs(cuda.dot(a, b) - np.dot(a, b)) <= 1e-12 * max(1.0, np.abs(a * b).sum())
+        assert cuda.max_norm(a) == np.abs(a).max()
+        d1 = cuda.dot(a, b)
+        assert cuda.dot(a, b) == d1  # deterministic
+
+
+def test_empty_and_tiny(cuda):
+    m = cuda.CsrMatrix.from_host(np.array([0, 1]), np.array([0]), np.array([4.0]))
+    np.testing.assert_array_equal(cuda.spmv(m, [2.0]).cpu().numpy(), [8.0])
+    e = cuda.CsrMatrix.from_host(np.array([0]), np.array([], dtype=np.int32), np.array([]))
+    assert e.row_num() == 0
+    assert cuda.spmv(e, np.zeros(0)).numel() == 0
+
+
+def test_invalid_csr_rejected(cuda):
+    # missing diagonal / unsorted columns are reported, not computed
+    with pytest.raises(cuda.LinealError):
+        cuda.CsrMatrix.from_host(np.array([0, 1, 2]), np.array([1, 0]), np.array([1.0, 1.0]))
+    with pytest.raises(cuda.LinealError):
+        cuda.CsrMatrix.from_host(np.array([0, 2]), np.array([0, 0]), np.array([1.0, 1.0]))

@@ -1,0 +1,228 @@
+"""Pins the CPU restatement (oracle/) against the reference's own golden data.
+
+* test/python-reference/sor.py: matrix and all 128 SOR iterates
+  (tests/golden/sor_python_reference.npz, generated by make_golden.py).
+* test/python-reference/cholesky.py: factor and solves.
+* test/data/UFZ_CT_02_{LHS.smf,RHS.dvf}: a real CSR system.
+* the residual/error bound tables of test/shared-stencil.hpp:157-180 and
+  201-224 (4x9x7 grid, diagonal_lines materials, coefficients 0..3).
+"""
+
+import os
+
+import numpy as np
+import pytest
+
+import oracle as lo
+from lineal_gb300 import io as lio
+
+
+@pytest.fixture(scope="module")
+def sor_golden(golden_dir):
+    return np.load(os.path.join(golden_dir, "sor_python_reference.npz"))
+
+
+def test_partition_blocks():
+    # contiguous parts covering [0, n), sizes differing by at most one
+    for n, p in [(10, 3), (252, 2), (7, 7), (1000, 64)]:
+        b = [lo.lib().lo_part_begin(n, p, k) for k in range(p + 1)]
+        sizes = np.diff(b)
+        assert b[0] == 0 and b[-1] == n
+        assert sizes.max() - sizes.min() <= 1
+
+
+def test_sor_python_reference_matrix(sor_golden):
+    g = sor_golden
+    q = lo.axis_quotients(g["dims"], g["lengths"])
+    mat = lo.material_flow_cylinder_gap(g["dims"], float(g["radius"]))
+    assert np.array_equal(mat, g["materials"])
+    s = lo.Stencil(g["dims"], q=q, mat=mat, coeffs=g["coeffs"], zero_to_one=True)
+    a, _ = s.to_csr()
+    # defs/diffusion_matrix.py sums the diagonal in another order: 1 ulp allowed
+    np.testing.assert_allclose(a.to_dense(), g["lhs"], rtol=1e-15, atol=0)
+    np.testing.assert_array_equal(s.spmv(g["x_true"]), g["lhs"] @ g["x_true"])
+
+
+def test_sor_python_reference_iterates(sor_golden):
+    g = sor_golden
+    s = lo.Stencil(g["dims"], q=(1, 1, 1), mat=g["materials"], coeffs=g["coeffs"])
+    a, _ = s.to_csr()
+    x = np.zeros(a.n)
+    for k in range(128):
+        x = lo.sor_sweep(a, g["rhs"], x_in=x, relax=float(g["relax"]), nparts=1)
+        ref = g["iterates"][k + 1]
+        # sor.py evaluates relax/diag * (...) instead of (...)/diag: rounding only
+        assert np.abs(x - ref).max() <= 1e-14 * np.abs(ref).max()
+
+
+def test_cholesky_python_reference(golden_dir):
+    c = np.load(os.path.join(golden_dir, "cholesky_python_reference.npz"))
+    lhs = c["lhs"]
+    n = lhs.shape[0]
+    rows, cols = np.nonzero(lhs)
+    rowptr = np.zeros(n + 1, dtype=np.int64)
+    np.add.at(rowptr, rows + 1, 1)
+    a = lo.Csr(np.cumsum(rowptr), cols.astype(np.int32), lhs[rows, cols])
+    l = lo.cholesky_factor(a)
+    np.testing.assert_allclose(l, c["chol"], rtol=0, atol=1e-14)
+    np.testing.assert_allclose(lo.cholesky_solve(l, c["rhs"]), c["sol"], rtol=0, atol=1e-13)
+
+
+def test_ufz_io_roundtrip(golden_dir, tmp_path):
+    lhs = os.path.join(golden_dir, "UFZ_CT_02_LHS.smf")
+    rhs = os.path.join(golden_dir, "UFZ_CT_02_RHS.dvf")
+    rowptr, col, val, ncols = lio.read_smf(lhs)
+    assert (len(rowptr) - 1, ncols, len(val)) == (0x21B, 0x21B, 0xD27)  # tensor-io test sizes
+    out = tmp_path / "m.smf"
+    lio.write_smf(str(out), rowptr, col, val, ncols)
+    assert out.read_bytes() == open(lhs, "rb").read()
+    b = lio.read_dvf(rhs)
+    assert len(b) == 539
+    out2 = tmp_path / "v.dvf"
+    lio.write_dvf(str(out2), b)
+    assert out2.read_bytes() == open(rhs, "rb").read()
+
+
+def _ufz(golden_dir):
+    rowptr, col, val, _ = lio.read_smf(os.path.join(golden_dir, "UFZ_CT_02_LHS.smf"))
+    b = lio.read_dvf(os.path.join(golden_dir, "UFZ_CT_02_RHS.dvf"))
+    return lo.Csr(rowptr, col, val, symmetric=False), b
+
+
+def test_ufz_spmv_and_solve(golden_dir):
+    a, b = _ufz(golden_dir)
+    x = np.linspace(-1, 1, a.n)
+    np.testing.assert_allclose(lo.spmv(a, x), a.to_dense() @ x, rtol=1e-13, atol=1e-13)
+    amg = lo.Amg(a, min_coarsen_size=32, partition_size=64, max_partitions=8,
+                 smoother_parts=0)
+    xs, it, hist = lo.pbicgstab(a, b, precon=lo.PRECON_AMG, amg=amg, rtol=1e-10, maxit=200)
+    assert hist[-1] <= 1e-10 * hist[0]
+    r = lo.residual(a, b, xs)
+    assert np.linalg.norm(r) <= 1e-9 * np.linalg.norm(b)
+
+
+def _stencil_system():
+    dims = (4, 9, 7)
+    mat = lo.material_diagonal_lines(dims, 4)
+    s = lo.Stencil(dims, q=(1, 1, 1), mat=mat, coeffs=(0, 1, 2, 3), sol_start=1, sol_end=0)
+    a, _ = s.to_csr()
+    return s, a
+
+
+def test_stencil_variants_agree():
+    # shared-stencil.hpp:124-131: A*2 through every representation
+    dims = (4, 9, 7)
+    s, a = _stencil_system()
+    mat = lo.material_diagonal_lines(dims, 4)
+    sv = lo.Stencil(dims, k=np.array([0, 1, 2, 3.0])[mat], sol_start=1, sol_end=0)
+    two = np.full(a.n, 2.0)
+    np.testing.assert_array_equal(s.spmv(two), sv.spmv(two))
+    np.testing.assert_allclose(s.spmv(two), lo.spmv(a, two), rtol=1e-14, atol=1e-14)
+    np.testing.assert_array_equal(s.rhs(), sv.rhs())
+
+
+# (name, iterations, kwargs, bound x=2, bound rhs); bounds from
+# test/shared-stencil.hpp:157-180 and 201-224 (regular variant)
+SUITE = [
+    ("cg", 129, dict(), 1e-12, 1e-13),
+    ("bicgstab", 129, dict(), 1e-12, 1e-13),
+    ("pcg_ssor1", 129, dict(precon=lo.PRECON_SSOR, nparts=2), 1e-13, 1e-13),
+    ("pbicgstab_ssor1", 129, dict(precon=lo.PRECON_SSOR, nparts=2), 1e-12, 1e-13),
+    ("pcg_amg", 33, dict(precon=lo.PRECON_AMG), 1e-13, 2e-14),
+    ("pbicgstab_amg", 33, dict(precon=lo.PRECON_AMG), 1e-13, 1e-13),
+]
+
+
+@pytest.mark.parametrize("name,iters,kw,bound_x2,bound_rhs", SUITE)
+def test_stencil_suite_bounds(name, iters, kw, bound_x2, bound_rhs):
+    s, a = _stencil_system()
+    amg = lo.Amg(a, min_coarsen_size=32, partition_size=8, max_partitions=2, coarse_f32=1,
+                 smoother_parts=2)
+    kw = dict(kw)
+    if kw.get("precon") == lo.PRECON_AMG:
+        kw["amg"] = amg
+    fn = lo.pcg if name.startswith(("cg", "pcg")) else lo.pbicgstab
+    b2 = lo.spmv(a, np.full(a.n, 2.0))
+    x, it, hist = fn(a, b2, rtol=0.0, maxit=iters, **kw)
+    assert hist[-1] <= bound_x2 and np.abs(x - 2).max() <= bound_x2
+    b = s.rhs()
+    x, it, hist = fn(a, b, rtol=0.0, maxit=iters, **kw)
+    assert hist[-1] <= bound_rhs and np.abs(lo.spmv(a, x) - b).max() <= bound_rhs
+
+
+def test_sor_smoother_bounds():
+    # "sor" entries: 129 in-situ sweeps, 2 thread partitions
+    s, a = _stencil_system()
+    for b, bound in ((lo.spmv(a, np.full(a.n, 2.0)), 1e-8), (s.rhs(), 1e-9)):
+        x = np.zeros(a.n)
+        for _ in range(129):
+            x = lo.sor_sweep(a, b, x_in=x, nparts=2)
+        assert np.linalg.norm(lo.spmv(a, x) - b) <= bound
+
+
+def test_colouring_valid_and_deterministic():
+    k = np.exp(np.random.default_rng(7).standard_normal(6 * 7 * 8))
+    a = lo.gen_27pt((6, 7, 8), k)
+    c1, n1 = lo.colour_jp(a, 11)
+    c2, n2 = lo.colour_jp(a, 11)
+    assert np.array_equal(c1, c2) and n1 == n2
+    for i in range(a.n):
+        for e in range(a.rowptr[i], a.rowptr[i + 1]):
+            j = a.col[e]
+            assert j == i or c1[j] != c1[i]
+    order = lo.colour_order(c1, n1)
+    assert sorted(order.tolist()) == list(range(a.n))
+
+
+def test_ordered_sor_identity_order_is_lexicographic():
+    s, a = _stencil_system()
+    b = s.rhs()
+    x0 = np.linspace(0, 1, a.n)
+    ident = np.arange(a.n, dtype=np.int32)
+    for fwd in (True, False):
+        np.testing.assert_array_equal(
+            lo.sor_sweep(a, b, x_in=x0, forward=fwd, order=ident),
+            lo.sor_sweep(a, b, x_in=x0, forward=fwd, nparts=1))
+
+
+def test_aggregation_invariants():
+    k = np.exp(1.5 * np.random.default_rng(1).standard_normal(12 * 12 * 12))
+    a = lo.gen_27pt((12, 12, 12), k)
+    dep, inf, iso = lo.amg_strength(a)
+    for nparts in (1, 3, 8):
+        nc, agg, lp, lst, stats = lo.amg_aggregate(a, dep, inf, iso, 6, 9, nparts)
+        assert stats[0] == nc
+        sizes = np.diff(lp)
+        assert sizes.min() >= 1 and sizes.max() <= 9
+        for c in range(nc):
+            assert np.all(agg[lst[lp[c]:lp[c + 1]]] == c)
+        assert np.all((agg < nc) | (agg == lo.ISOLATED))
+        # aggregates never cross partitions
+        bounds = [lo.lib().lo_part_begin(a.n, nparts, p) for p in range(nparts + 1)]
+        part = np.searchsorted(bounds, np.arange(a.n), side="right") - 1
+        for c in range(nc):
+            assert len(set(part[lst[lp[c]:lp[c + 1]]])) == 1
+
+
+def test_galerkin_matches_dense_product():
+    k = np.exp(np.random.default_rng(2).standard_normal(8 * 8 * 8))
+    a = lo.gen_27pt((8, 8, 8), k)
+    dep, inf, iso = lo.amg_strength(a)
+    nc, agg, lp, lst, _ = lo.amg_aggregate(a, dep, inf, iso, 6, 9, 2)
+    ac = lo.amg_galerkin(a, nc, agg, lp, lst)
+    p = np.zeros((a.n, nc))
+    for i in range(a.n):
+        if agg[i] < nc:
+            p[i, agg[i]] = 1.0
+    np.testing.assert_allclose(ac.to_dense(), p.T @ a.to_dense() @ p, rtol=1e-13, atol=1e-13)
+
+
+def test_amg_pcg_27pt_converges():
+    dims = (16, 16, 16)
+    k = np.exp(1.5 * np.random.default_rng(1).standard_normal(np.prod(dims)))
+    a = lo.gen_27pt(dims, k)
+    b = np.random.default_rng(0).uniform(-1, 1, a.n)
+    amg = lo.Amg(a, min_coarsen_size=100, partition_size=512, smoother_parts=0)
+    x, it, hist = lo.pcg(a, b, precon=lo.PRECON_AMG, amg=amg, rtol=1e-8, maxit=200)
+    assert hist[-1] <= 1e-8 * hist[0]
+    assert it < 60
