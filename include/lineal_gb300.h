@@ -296,6 +296,24 @@ lgx_status lgx_pbicgstab(const lgx_matrix *a, const double *d_b, double *d_x,
                          const lgx_solve_params *p, lgx_stream stream, int64_t *iterations,
                          double *final_rel_residual, double *h_history);
 
+/* Step-wise form of the same solvers: lgx_krylov_create performs the
+ * SystemInstance construction (initial residual, first preconditioner
+ * application), lgx_krylov_iterate one SystemInstance::iterate, and
+ * lgx_krylov_state returns the iteration count, residual_norm() and rho()
+ * (synchronised host copies).  lgx_krylov_solution writes the current
+ * iterate to d_x (natural ordering).  b and the initial guess are copied at
+ * creation, so d_b and d_x need not stay valid afterwards. */
+typedef struct lgx_krylov lgx_krylov;
+typedef enum { LGX_KRYLOV_CG = 0, LGX_KRYLOV_BICGSTAB = 1 } lgx_krylov_kind;
+lgx_status lgx_krylov_create(int kind, const lgx_matrix *a, const double *d_b,
+                             const double *d_x, const lgx_solve_params *p, lgx_stream stream,
+                             lgx_krylov **out);
+lgx_status lgx_krylov_iterate(lgx_krylov *k);
+lgx_status lgx_krylov_state(const lgx_krylov *k, int64_t *iteration, double *residual_norm,
+                            double *rho);
+lgx_status lgx_krylov_solution(lgx_krylov *k, double *d_x);
+lgx_status lgx_krylov_destroy(lgx_krylov *k);
+
 #ifdef __cplusplus
 }
 #endif

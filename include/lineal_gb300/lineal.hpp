@@ -1,0 +1,551 @@
+// lineal_gb300 C++ layer: GPU types that satisfy lineal's named requirements.
+//
+// lineal (KurtBoehm/lineal) is written against concepts, i.e. types are
+// recognised by deriving from empty tag bases (include/lineal/base/concept/
+// range.hpp:17-40, include/lineal/base/concept/solver.hpp:16-37) and by
+// providing a set of members.  This header restates those tag bases and
+// concepts and provides device-resident implementations whose bodies call the
+// C ABI of include/lineal_gb300.h, so that code written in lineal's style --
+// solver.instantiate(lhs, env), instance.instantiate(sol, rhs, env),
+// system.iterate(env), run_iterative_solver(...) -- runs on a GB300.
+//
+// Header-only, C++20, no exceptions across the ABI: failures raise
+// lineal::gb300::Error on the host side of this header.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <concepts>
+#include <cstddef>
+#include <cstdint>
+#include <optional>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <utility>
+#include <vector>
+
+#include "lineal_gb300.h"
+
+namespace lineal::gb300 {
+
+// ---- errors ------------------------------------------------------------------
+struct Error : std::runtime_error {
+  lgx_status status;
+  Error(lgx_status s, const std::string &what) : std::runtime_error(what), status(s) {}
+};
+
+inline void check(lgx_status s) {
+  if (s != LGX_OK)
+    throw Error(s, std::string("lineal_gb300: ") + lgx_status_string(s) + ": " +
+                     lgx_last_error());
+}
+inline void check_cuda(cudaError_t e) {
+  if (e != cudaSuccess) throw Error(LGX_ERR_CUDA, cudaGetErrorString(e));
+}
+
+// ---- tag bases and concepts (base/concept/range.hpp:17-40, solver.hpp:16-37)
+struct SharedVectorBase {};
+struct SharedMatrixBase {};
+struct SharedStationaryIterativeSolverBase {};
+struct SharedNonStationaryIterativeSolverBase {};
+struct SharedDirectSolverBase {};
+struct EnvBase {};
+
+template <typename T>
+concept SharedVector = std::is_base_of_v<SharedVectorBase, std::decay_t<T>>;
+template <typename T>
+concept AnyVector = SharedVector<T>;
+template <typename T>
+concept SharedMatrix = std::is_base_of_v<SharedMatrixBase, std::decay_t<T>>;
+template <typename T>
+concept AnyMatrix = SharedMatrix<T>;
+template <typename T>
+concept StationaryIterativeSolver =
+  std::is_base_of_v<SharedStationaryIterativeSolverBase, std::decay_t<T>>;
+template <typename T>
+concept NonStationaryIterativeSolver =
+  std::is_base_of_v<SharedNonStationaryIterativeSolverBase, std::decay_t<T>>;
+template <typename T>
+concept Env = std::is_base_of_v<EnvBase, std::decay_t<T>>;
+
+enum struct IsSymmetric : bool {};
+
+// ---- environment (environment/environment.hpp:17-69) -------------------------
+// The execution policy of a device environment is a CUDA stream.
+struct DevicePolicy {
+  cudaStream_t stream = nullptr;
+  [[nodiscard]] std::size_t thread_num() const { return 1; }
+};
+
+struct Environment : EnvBase {
+  explicit Environment(cudaStream_t s = nullptr) : policy_{s} {}
+  [[nodiscard]] const DevicePolicy &execution_policy() const { return policy_; }
+  [[nodiscard]] cudaStream_t stream() const { return policy_.stream; }
+  template <typename T>
+  void log(const char * /*name*/, const T & /*value*/) const {}
+  [[nodiscard]] const Environment &add_object(const char * /*name*/ = nullptr) const {
+    return *this;
+  }
+  [[nodiscard]] const Environment &dummy() const { return *this; }
+
+ private:
+  DevicePolicy policy_;
+};
+
+// ---- dense vectors (tensor/dynamic/dense/vector/shared.hpp:350-362) -----------
+template <typename TValue = double>
+class DenseVector : public SharedVectorBase {
+ public:
+  using Value = TValue;
+  using Size = std::size_t;
+
+  DenseVector() = default;
+  explicit DenseVector(Size n) : n_(n) { alloc(); }
+  DenseVector(Size n, const Environment & /*env*/) : DenseVector(n) {}
+  DenseVector(Size n, Value value, const Environment &env) : DenseVector(n) {
+    std::vector<Value> h(n, value);
+    check_cuda(cudaMemcpyAsync(p_, h.data(), n * sizeof(Value), cudaMemcpyHostToDevice,
+                               env.stream()));
+    check_cuda(cudaStreamSynchronize(env.stream()));
+  }
+  DenseVector(const DenseVector &) = delete;
+  DenseVector &operator=(const DenseVector &) = delete;
+  DenseVector(DenseVector &&o) noexcept : n_(o.n_), p_(std::exchange(o.p_, nullptr)) {}
+  DenseVector &operator=(DenseVector &&o) noexcept {
+    std::swap(n_, o.n_);
+    std::swap(p_, o.p_);
+    return *this;
+  }
+  ~DenseVector() {
+    if (p_) cudaFree(p_);
+  }
+
+  [[nodiscard]] Size size() const { return n_; }
+  [[nodiscard]] Value *data() { return p_; }
+  [[nodiscard]] const Value *data() const { return p_; }
+
+  void upload(const std::vector<Value> &h, const Environment &env) {
+    check_cuda(cudaMemcpyAsync(p_, h.data(), n_ * sizeof(Value), cudaMemcpyHostToDevice,
+                               env.stream()));
+    check_cuda(cudaStreamSynchronize(env.stream()));
+  }
+  [[nodiscard]] std::vector<Value> download(const Environment &env) const {
+    std::vector<Value> h(n_);
+    check_cuda(cudaMemcpyAsync(h.data(), p_, n_ * sizeof(Value), cudaMemcpyDeviceToHost,
+                               env.stream()));
+    check_cuda(cudaStreamSynchronize(env.stream()));
+    return h;
+  }
+
+ private:
+  void alloc() {
+    if (n_) check_cuda(cudaMalloc(&p_, n_ * sizeof(Value)));
+  }
+  Size n_ = 0;
+  Value *p_ = nullptr;
+};
+
+template <typename TVec>
+TVec create_numa_undef_like(const AnyMatrix auto &m, const Environment &env) {
+  return TVec(m.row_num(), env);
+}
+
+// ---- matrices ---------------------------------------------------------------------
+class MatrixHandle : public SharedMatrixBase {
+ public:
+  using Value = double;
+  using Size = std::size_t;
+
+  MatrixHandle() = default;
+  explicit MatrixHandle(lgx_matrix *h) : h_(h) {}
+  MatrixHandle(const MatrixHandle &) = delete;
+  MatrixHandle &operator=(const MatrixHandle &) = delete;
+  MatrixHandle(MatrixHandle &&o) noexcept : h_(std::exchange(o.h_, nullptr)) {}
+  MatrixHandle &operator=(MatrixHandle &&o) noexcept {
+    std::swap(h_, o.h_);
+    return *this;
+  }
+  ~MatrixHandle() {
+    if (h_) lgx_matrix_destroy(h_);
+  }
+
+  [[nodiscard]] lgx_matrix *handle() const { return h_; }
+  [[nodiscard]] Size row_num() const { return (Size)info().n; }
+  [[nodiscard]] Size column_num() const { return row_num(); }
+  [[nodiscard]] Size non_zero_num() const { return (Size)info().nnz; }
+  [[nodiscard]] IsSymmetric is_symmetric() const { return IsSymmetric{info().sym != 0}; }
+
+ private:
+  struct Info {
+    int kind;
+    int64_t n, nnz;
+    int sym;
+  };
+  [[nodiscard]] Info info() const {
+    Info i{};
+    check(lgx_matrix_info(h_, &i.kind, &i.n, &i.nnz, &i.sym));
+    return i;
+  }
+  lgx_matrix *h_ = nullptr;
+};
+
+// CsrMatrix (tensor/dynamic/csr/shared.hpp:1114-1116); built from host CSR
+// arrays (RowWiseBuilder-style input: sorted columns, stored diagonal).
+class CsrMatrix : public MatrixHandle {
+ public:
+  using MatrixHandle::MatrixHandle;
+  static CsrMatrix from_host(const std::vector<int64_t> &rowptr, const std::vector<int32_t> &col,
+                             const std::vector<double> &val, IsSymmetric sym,
+                             lgx_dtype storage = LGX_F64) {
+    lgx_matrix *h = nullptr;
+    check(lgx_csr_create_host((int64_t)rowptr.size() - 1, (int64_t)col.size(), rowptr.data(),
+                              col.data(), val.data(), sym == IsSymmetric{true}, storage, &h));
+    return CsrMatrix(h);
+  }
+  // the synthetic 27-point lognormal operator on a grid (device generator)
+  static CsrMatrix diffusion_27pt(const int64_t dims[3], const DenseVector<double> &k,
+                                  const Environment &env, lgx_dtype storage = LGX_F64) {
+    lgx_matrix *h = nullptr;
+    check(lgx_gen_27pt(dims, k.data(), storage, env.stream(), &h));
+    return CsrMatrix(h);
+  }
+};
+
+// AdjacentStencilMatrix with a StationaryDiffusionLookupValuator / ValueValuator
+class StencilMatrix : public MatrixHandle {
+ public:
+  using MatrixHandle::MatrixHandle;
+  static StencilMatrix lookup(const int64_t dims[3], const double q[3], const double coeffs[4],
+                              const DenseVector<uint8_t> &materials, double sol_start,
+                              double sol_end, bool zero_to_one, const Environment &env) {
+    lgx_matrix *h = nullptr;
+    check(lgx_stencil_create_lookup(dims, q, coeffs, materials.data(), sol_start, sol_end,
+                                    zero_to_one, env.stream(), &h));
+    return StencilMatrix(h);
+  }
+  static StencilMatrix value(const int64_t dims[3], const double q[3],
+                             const DenseVector<double> &k, double sol_start, double sol_end,
+                             bool zero_to_one, const Environment &env) {
+    lgx_matrix *h = nullptr;
+    check(lgx_stencil_create_value(dims, q, k.data(), sol_start, sol_end, zero_to_one,
+                                   env.stream(), &h));
+    return StencilMatrix(h);
+  }
+};
+
+// ---- component-wise operations (component-wise/*) ------------------------------
+template <typename TLhs, typename TRhs>
+struct MatrixVectorProductExpr {
+  const TLhs &lhs;
+  const TRhs &rhs;
+};
+
+template <AnyMatrix TLhs, AnyVector TRhs>
+MatrixVectorProductExpr<TLhs, TRhs> operator*(const TLhs &lhs, const TRhs &rhs) {
+  return {lhs, rhs};
+}
+
+// assign(y, A * x) (sink/assignment.hpp:114-117)
+template <typename TLhs, typename TRhs>
+void assign(DenseVector<double> &y, const MatrixVectorProductExpr<TLhs, TRhs> &e,
+            const DevicePolicy &pol) {
+  check(lgx_spmv(e.lhs.handle(), e.rhs.data(), y.data(), pol.stream));
+}
+
+inline double scalar_from_device(const double *d, cudaStream_t s) {
+  double h = 0.0;
+  check_cuda(cudaMemcpyAsync(&h, d, sizeof(double), cudaMemcpyDeviceToHost, s));
+  check_cuda(cudaStreamSynchronize(s));
+  return h;
+}
+
+// dot / euclidean_squared / euclidean_norm / max_norm (sink/accumulator.hpp:151-218)
+template <typename TReal = double>
+TReal dot(const DenseVector<double> &a, const DenseVector<double> &b, const DevicePolicy &pol) {
+  DenseVector<double> out(1);
+  check(lgx_dot((int64_t)a.size(), a.data(), b.data(), out.data(), pol.stream));
+  return scalar_from_device(out.data(), pol.stream);
+}
+template <typename TReal = double>
+TReal euclidean_squared(const DenseVector<double> &a, const DevicePolicy &pol) {
+  return dot<TReal>(a, a, pol);
+}
+template <typename TReal = double>
+TReal euclidean_norm(const DenseVector<double> &a, const DevicePolicy &pol) {
+  return std::sqrt(euclidean_squared<TReal>(a, pol));
+}
+template <typename TReal = double>
+TReal max_norm(const DenseVector<double> &a, const DevicePolicy &pol) {
+  DenseVector<double> out(1);
+  check(lgx_max_norm((int64_t)a.size(), a.data(), out.data(), pol.stream));
+  return scalar_from_device(out.data(), pol.stream);
+}
+
+// ---- stationary solvers (iterative-stationary/*) --------------------------------
+struct forward_tag_t {};
+struct backward_tag_t {};
+inline constexpr forward_tag_t forward_tag{};
+inline constexpr backward_tag_t backward_tag{};
+enum struct SorVariant : uint8_t { regular, ultra };
+
+// JacobiSolver (jacobi/solver.hpp:38-39), one sweep per apply
+struct JacobiSolver : SharedStationaryIterativeSolverBase {
+  double relax = 1.0;
+  explicit JacobiSolver(double r) : relax(r) {}
+  template <AnyMatrix TLhs>
+  struct Instance {
+    const TLhs &lhs;
+    double relax;
+    static constexpr std::size_t in_situ_aux_size = 1;
+    static constexpr std::size_t ex_situ_aux_size = 0;
+    // ex situ: out = sweep(in)
+    void apply(const DenseVector<double> *in, DenseVector<double> &out,
+               const DenseVector<double> &rhs, const Environment &env) const {
+      check(lgx_jacobi_sweep(lhs.handle(), relax, in ? in->data() : nullptr, out.data(),
+                             rhs.data(), env.stream()));
+    }
+  };
+  template <AnyMatrix TLhs>
+  Instance<TLhs> instantiate(const TLhs &lhs, const Environment & /*env*/) const {
+    return {lhs, relax};
+  }
+};
+
+// Multicolour SorSolver / SsorSolver (gauss-seidel-variant/solver.hpp:91-96)
+class Colouring {
+ public:
+  Colouring() = default;
+  Colouring(const CsrMatrix &a, uint64_t seed, const Environment &env) {
+    check(lgx_colouring_create_jp(a.handle(), seed, env.stream(), &h_));
+  }
+  Colouring(const Colouring &) = delete;
+  Colouring &operator=(const Colouring &) = delete;
+  Colouring(Colouring &&o) noexcept : h_(std::exchange(o.h_, nullptr)) {}
+  ~Colouring() {
+    if (h_) lgx_colouring_destroy(h_);
+  }
+  [[nodiscard]] lgx_colouring *handle() const { return h_; }
+
+ private:
+  lgx_colouring *h_ = nullptr;
+};
+
+template <typename TDir, SorVariant tVariant = SorVariant::regular>
+struct SorSolver : SharedStationaryIterativeSolverBase {
+  double relax = 1.0;
+  explicit SorSolver(double r) : relax(r) {}
+  struct Instance {
+    const CsrMatrix &lhs;
+    Colouring colouring;
+    double relax;
+    static constexpr std::size_t in_situ_aux_size = 1;
+    static constexpr std::size_t ex_situ_aux_size = 0;
+    void apply(const DenseVector<double> *in, DenseVector<double> &out,
+               const DenseVector<double> &rhs, const Environment &env) const {
+      check(lgx_sor_sweep(lhs.handle(), colouring.handle(), relax,
+                          std::is_same_v<TDir, forward_tag_t>, tVariant == SorVariant::ultra,
+                          in ? in->data() : nullptr, out.data(), rhs.data(), env.stream()));
+    }
+    // in situ (SingleSweepImpl, broom.hpp:43-51)
+    void apply(DenseVector<double> &sol, const DenseVector<double> &rhs,
+               const Environment &env) const {
+      apply(&sol, sol, rhs, env);
+    }
+  };
+  Instance instantiate(const CsrMatrix &lhs, const Environment &env) const {
+    return Instance{lhs, Colouring(lhs, 0x5eed, env), relax};
+  }
+};
+
+// ---- AMG (multigrid/*) -------------------------------------------------------------
+enum struct CycleKind : uint8_t { REGULAR, DECREASING };
+struct DefaultCycle {
+  CycleKind kind = CycleKind::REGULAR;
+  std::size_t iterations = 1;
+};
+
+struct HierarchyWrightParams {
+  std::size_t max_level_num = 16;
+  std::size_t min_coarsen_size = 2000;
+  double min_coarsen_factor = 1.2;
+};
+
+struct AggregationParams {
+  int32_t min_aggregate_size = 6;
+  int32_t max_aggregate_size = 9;
+  int64_t partition_size = 4096;
+};
+
+struct DuneDependencyCriterion {
+  double strong_threshold = 1.0 / 3.0;
+  double aggressive_strong_threshold = 1.0 / 3.0;
+};
+
+// MultiGridSolver{relax, DefaultCycle{REGULAR, 1}, wright} with lineal's
+// default component choice: DuneDependencyCriterion + homogeneous greedy
+// aggregation, SOR forward pre- and backward post-smoothing, direct coarsest
+// solve (test/aux/default.hpp:155-188).
+struct MultiGridSolver : SharedStationaryIterativeSolverBase {
+  double relax = 1.0;
+  DefaultCycle cycle{};
+  HierarchyWrightParams hierarchy{};
+  AggregationParams aggregation{};
+  DuneDependencyCriterion criterion{};
+  double smoother_relax = 1.0;
+  bool float_cycle = false;
+
+  class Instance {
+   public:
+    Instance(const CsrMatrix &lhs, const MultiGridSolver &s, const Environment &env) {
+      if (s.cycle.kind != CycleKind::REGULAR || s.cycle.iterations != 1)
+        throw Error(LGX_ERR_UNSUPPORTED, "only the REGULAR cycle with one iteration (V-cycle)");
+      lgx_amg_params p;
+      lgx_amg_default_params(&p);
+      p.max_level_num = (int64_t)s.hierarchy.max_level_num;
+      p.min_coarsen_size = (int64_t)s.hierarchy.min_coarsen_size;
+      p.min_coarsen_factor = s.hierarchy.min_coarsen_factor;
+      p.min_aggregate_size = s.aggregation.min_aggregate_size;
+      p.max_aggregate_size = s.aggregation.max_aggregate_size;
+      p.partition_size = s.aggregation.partition_size;
+      p.strong_threshold = s.criterion.strong_threshold;
+      p.aggressive_threshold = s.criterion.aggressive_strong_threshold;
+      p.relax = s.relax;
+      p.smoother_relax = s.smoother_relax;
+      p.cycle_f32 = s.float_cycle;
+      check(lgx_amg_setup(lhs.handle(), &p, nullptr, env.stream(), &h_));
+    }
+    Instance(const Instance &) = delete;
+    Instance(Instance &&o) noexcept : h_(std::exchange(o.h_, nullptr)) {}
+    ~Instance() {
+      if (h_) lgx_amg_destroy(h_);
+    }
+    static constexpr std::size_t in_situ_aux_size = 0;
+    static constexpr std::size_t ex_situ_aux_size = 0;
+    // apply(constant 0, out, rhs) -- the preconditioner application
+    void apply(DenseVector<double> &out, const DenseVector<double> &rhs,
+               const Environment &env) const {
+      check(lgx_amg_vcycle(h_, rhs.data(), out.data(), env.stream()));
+    }
+    [[nodiscard]] lgx_amg *handle() const { return h_; }
+    [[nodiscard]] std::size_t level_num() const {
+      int64_t l = 0;
+      check(lgx_amg_info(h_, &l, nullptr, nullptr, 0));
+      return (std::size_t)l;
+    }
+
+   private:
+    lgx_amg *h_ = nullptr;
+  };
+
+  Instance instantiate(const CsrMatrix &lhs, const Environment &env) const {
+    return Instance(lhs, *this, env);
+  }
+};
+
+// ---- non-stationary solvers ----------------------------------------------------------
+struct NoPrecon {};
+
+// ConjugateGradientsSolver / BiCgStabSolver (conjugate-gradients/solver.hpp:24-225,
+// bicgstab/solver.hpp:25-263).  TPrecon is void, JacobiSolver, MultiGridSolver.
+template <lgx_krylov_kind tKind, typename TPrecon>
+struct KrylovSolver : SharedNonStationaryIterativeSolverBase {
+  std::size_t rere_period = 8;  // rere_controller: iter > 0 && iter % 8 == 0
+  std::optional<TPrecon> precon;
+
+  KrylovSolver() = default;
+  explicit KrylovSolver(TPrecon p, std::size_t rere = 8) : rere_period(rere), precon(std::move(p)) {}
+
+  template <AnyMatrix TLhs>
+  struct Instance {
+    const TLhs &lhs;
+    const KrylovSolver &solver;
+    std::optional<MultiGridSolver::Instance> amg;
+
+    struct SystemInstance {
+      SystemInstance(const Instance &inst, DenseVector<double> &sol,
+                     const DenseVector<double> &rhs, const Environment &env)
+          : sol_(sol) {
+        lgx_solve_params p;
+        lgx_solve_default_params(&p);
+        p.rere_period = (int64_t)inst.solver.rere_period;
+        if constexpr (std::is_same_v<TPrecon, JacobiSolver>) {
+          p.precon = LGX_PRECON_JACOBI;
+          p.relax = inst.solver.precon->relax;
+        } else if constexpr (std::is_same_v<TPrecon, MultiGridSolver>) {
+          p.precon = LGX_PRECON_AMG;
+          p.amg = inst.amg->handle();
+        }
+        check(lgx_krylov_create(tKind, inst.lhs.handle(), rhs.data(), sol.data(), &p,
+                                env.stream(), &h_));
+      }
+      SystemInstance(const SystemInstance &) = delete;
+      ~SystemInstance() {
+        if (h_) lgx_krylov_destroy(h_);
+      }
+      void iterate(const Environment & /*env*/) { check(lgx_krylov_iterate(h_)); }
+      [[nodiscard]] double residual_norm() const { return state().res; }
+      [[nodiscard]] double rho() const { return state().rho; }
+      [[nodiscard]] const DenseVector<double> &solution() {
+        check(lgx_krylov_solution(h_, sol_.data()));
+        return sol_;
+      }
+
+     private:
+      struct St {
+        int64_t it;
+        double res, rho;
+      };
+      [[nodiscard]] St state() const {
+        St s{};
+        check(lgx_krylov_state(h_, &s.it, &s.res, &s.rho));
+        return s;
+      }
+      lgx_krylov *h_ = nullptr;
+      DenseVector<double> &sol_;
+    };
+
+    SystemInstance instantiate(DenseVector<double> &sol, const DenseVector<double> &rhs,
+                               const Environment &env) const {
+      return SystemInstance(*this, sol, rhs, env);
+    }
+  };
+
+  template <AnyMatrix TLhs>
+  Instance<TLhs> instantiate(const TLhs &lhs, const Environment &env) const {
+    Instance<TLhs> inst{lhs, *this, std::nullopt};
+    if constexpr (std::is_same_v<TPrecon, MultiGridSolver>) inst.amg.emplace(lhs, *precon, env);
+    return inst;
+  }
+};
+
+template <typename TPrecon = void>
+using ConjugateGradientsSolver =
+  KrylovSolver<LGX_KRYLOV_CG, std::conditional_t<std::is_void_v<TPrecon>, NoPrecon, TPrecon>>;
+template <typename TPrecon = void>
+using BiCgStabSolver =
+  KrylovSolver<LGX_KRYLOV_BICGSTAB, std::conditional_t<std::is_void_v<TPrecon>, NoPrecon, TPrecon>>;
+
+// run_iterative_solver (linear-solver/runner.hpp:17-84): the caller's iter_op
+// decides when to stop and returns the value to report.
+template <typename TSolver, AnyMatrix TLhs, typename TIterOp>
+auto run_iterative_solver(const TSolver &solver, const TLhs &lhs, DenseVector<double> &sol,
+                          const DenseVector<double> &rhs, const Environment &env,
+                          TIterOp iter_op) {
+  auto instance = solver.instantiate(lhs, env);
+  auto system = instance.instantiate(sol, rhs, env);
+  if (auto r = iter_op(std::size_t{0}, system, env); r.has_value()) {
+    (void)system.solution();
+    return *r;
+  }
+  for (std::size_t i = 1;; ++i) {
+    system.iterate(env);
+    if (auto r = iter_op(i, system, env); r.has_value()) {
+      (void)system.solution();
+      return *r;
+    }
+  }
+}
+
+}  // namespace lineal::gb300

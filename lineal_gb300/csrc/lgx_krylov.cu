@@ -37,7 +37,7 @@ __device__ __forceinline__ void set_flags(KScalars *ks, double num, double den) 
   if (den == 0.0) ks->flag |= 1;
 }
 
-enum Post { POST_ALPHA = 0, POST_RHO_BETA = 1, POST_OMEGA = 2 };
+enum Post { POST_ALPHA = 0, POST_RHO_BETA = 1, POST_OMEGA = 2, POST_RHO = 3 };
 
 // dot(a, b) with a post operation in the last block
 __global__ void __launch_bounds__(kKT)
@@ -58,6 +58,9 @@ __global__ void __launch_bounds__(kKT)
       ks->rho = t;
       set_flags(ks, t, ks->rho_old);
       ks->beta = t / ks->rho_old;
+    } else if (post == POST_RHO) {  // initial rho = z.r (solver.hpp:63-64)
+      ks->rho = t;
+      if (!isfinite(t)) ks->flag |= 2;
     }
   }
 }
@@ -328,17 +331,31 @@ static lgx_status check_flags(const KScalars &h, int64_t it) {
   return LGX_OK;
 }
 
-static lgx_status run_pcg(const lgx_matrix *a, const double *d_b, double *d_x,
-                          const lgx_solve_params *p, cudaStream_t s, int64_t *iterations,
-                          double *final_rel, double *history) {
-  Solver S;
+}  // namespace lgx
+
+// Krylov solver state: the SystemInstance of the reference solvers.
+struct lgx_krylov {
+  int kind = LGX_KRYLOV_CG;
+  lgx_solve_params p{};
+  lgx::Solver S;
   std::unique_ptr<lgx_colouring> own_col;
-  LGX_CHECK(setup_solver(a, p, s, S, own_col));
+  lgx::Vecs V;
+  lgx::KScalars h{};
+  int64_t it = 0;
+  double r0 = 0.0;
+};
+
+namespace lgx {
+
+// CG vectors: 0 b, 1 x, 2 r, 3 p, 4 q/z.  BiCGStab: 0 b, 1 x, 2 r, 3 r0, 4 p,
+// 5 v, 6 t, 7 px.
+static lgx_status krylov_init(lgx_krylov &K, const double *d_b, const double *d_x) {
+  Solver &S = K.S;
   const int64_t n = S.n;
-  Vecs V;
-  // 0 b, 1 x, 2 r, 3 p, 4 q/z
-  LGX_CHECK(V.alloc(5, n));
-  double *b = V[0], *x = V[1], *r = V[2], *pd = V[3], *q = V[4];
+  const bool cg = K.kind == LGX_KRYLOV_CG;
+  LGX_CHECK(K.V.alloc(cg ? 5 : 8, n));
+  double *b = K.V[0], *x = K.V[1], *r = K.V[2];
+  cudaStream_t s = S.s;
   if (S.perm) {
     LGX_CHECK(gather<double, double>(n, S.perm, d_b, b, s));
     LGX_CHECK(gather<double, double>(n, S.perm, d_x, x, s));
@@ -348,151 +365,159 @@ static lgx_status run_pcg(const lgx_matrix *a, const double *d_b, double *d_x,
   }
   KScalars *ks = S.ks.p;
   const unsigned rg = (unsigned)reduce_blocks(n);
-  const bool precon = S.precon != LGX_PRECON_NONE;
-  // initialisation (solver.hpp:50-73)
   LGX_CHECK(S.residual(b, x, r, &ks->res2));
-  if (precon) {
-    LGX_CHECK(S.precondition(r, pd));
-    k_dot_post<<<rg, kKT, 0, s>>>(n, pd, r, POST_RHO_BETA, ks, S.partials.p, S.counters.p);
-    LGX_LAUNCH_CHECK();
-  } else {
-    LGX_CUDA(cudaMemcpyAsync(pd, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-    k_cg_plain_rho<<<1, 1, 0, s>>>(ks);
-    LGX_LAUNCH_CHECK();
-  }
-  KScalars h{};
-  LGX_CHECK(S.read(h));
-  if (!std::isfinite(h.res2) || !std::isfinite(h.rho))
-    return fail(LGX_ERR_NONFINITE, "non-finite initial residual or preconditioned residual");
-  const double r0 = std::sqrt(h.res2);
-  if (history) history[0] = r0;
-  int64_t it = 0;
-  double res = r0;
-  lgx_status st = LGX_OK;
-  while (it < p->maxit && res > p->rtol * r0 && h.rho != 0.0) {
-    LGX_CHECK(S.apply(pd, q));
-    k_dot_post<<<rg, kKT, 0, s>>>(n, pd, q, POST_ALPHA, ks, S.partials.p, S.counters.p);
-    LGX_LAUNCH_CHECK();
-    const bool rere = p->rere_period > 0 && it > 0 && it % p->rere_period == 0;
-    k_cg_update<<<rg, kKT, 0, s>>>(n, ks, pd, q, x, r, rere ? 0 : 1, precon ? 0 : 1,
-                                   S.partials.p, S.counters.p);
-    LGX_LAUNCH_CHECK();
-    if (rere) {
-      LGX_CHECK(S.residual(b, x, r, &ks->res2));
-      if (!precon) {
-        k_cg_plain_rho<<<1, 1, 0, s>>>(ks);
-        LGX_LAUNCH_CHECK();
-      }
-    }
-    if (precon) {
-      LGX_CHECK(S.precondition(r, q));
-      k_dot_post<<<rg, kKT, 0, s>>>(n, r, q, POST_RHO_BETA, ks, S.partials.p, S.counters.p);
+  if (cg) {
+    // conjugate-gradients/solver.hpp:50-73
+    double *pd = K.V[3];
+    if (S.precon != LGX_PRECON_NONE) {
+      LGX_CHECK(S.precondition(r, pd));
+      k_dot_post<<<rg, kKT, 0, s>>>(n, pd, r, POST_RHO, ks, S.partials.p, S.counters.p);
       LGX_LAUNCH_CHECK();
-      k_xpby<<<S.vgrid(), 256, 0, s>>>(n, ks, q, pd);
     } else {
-      k_xpby<<<S.vgrid(), 256, 0, s>>>(n, ks, r, pd);
+      LGX_CUDA(cudaMemcpyAsync(pd, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+      k_cg_plain_rho<<<1, 1, 0, s>>>(ks);
+      LGX_LAUNCH_CHECK();
     }
-    LGX_LAUNCH_CHECK();
-    ++it;
-    LGX_CHECK(S.read(h));
-    res = std::sqrt(h.res2);
-    if (history) history[it] = res;
-    if ((st = check_flags(h, it)) != LGX_OK) break;
-  }
-  if (S.perm) {
-    LGX_CHECK(scatter<double, double>(n, S.perm, x, d_x, s));
   } else {
-    LGX_CUDA(cudaMemcpyAsync(d_x, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    // bicgstab/solver.hpp:51-71
+    LGX_CUDA(cudaMemcpyAsync(K.V[3], r, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    LGX_CUDA(cudaMemcpyAsync(K.V[4], r, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    k_bicg_init<<<1, 1, 0, s>>>(ks);
+    LGX_LAUNCH_CHECK();
   }
-  LGX_CUDA(cudaStreamSynchronize(s));
-  if (iterations) *iterations = it;
-  if (final_rel) *final_rel = r0 > 0 ? res / r0 : 0.0;
-  return st;
+  LGX_CHECK(S.read(K.h));
+  if (!std::isfinite(K.h.res2) || !std::isfinite(K.h.rho))
+    return fail(LGX_ERR_NONFINITE, "non-finite initial residual or preconditioned residual");
+  K.r0 = std::sqrt(K.h.res2);
+  K.it = 0;
+  return LGX_OK;
 }
 
-static lgx_status run_pbicgstab(const lgx_matrix *a, const double *d_b, double *d_x,
-                                const lgx_solve_params *p, cudaStream_t s, int64_t *iterations,
-                                double *final_rel, double *history) {
-  Solver S;
-  std::unique_ptr<lgx_colouring> own_col;
-  LGX_CHECK(setup_solver(a, p, s, S, own_col));
+// conjugate-gradients/solver.hpp:75-115
+static lgx_status cg_iterate(lgx_krylov &K) {
+  Solver &S = K.S;
   const int64_t n = S.n;
-  Vecs V;
-  // 0 b, 1 x, 2 r, 3 r0, 4 p, 5 v, 6 t, 7 px
-  LGX_CHECK(V.alloc(8, n));
-  double *b = V[0], *x = V[1], *r = V[2], *r0 = V[3], *pd = V[4], *v = V[5], *t = V[6],
-         *px = V[7];
-  if (S.perm) {
-    LGX_CHECK(gather<double, double>(n, S.perm, d_b, b, s));
-    LGX_CHECK(gather<double, double>(n, S.perm, d_x, x, s));
-  } else {
-    LGX_CUDA(cudaMemcpyAsync(b, d_b, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-    LGX_CUDA(cudaMemcpyAsync(x, d_x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-  }
+  cudaStream_t s = S.s;
+  double *b = K.V[0], *x = K.V[1], *r = K.V[2], *pd = K.V[3], *q = K.V[4];
   KScalars *ks = S.ks.p;
   const unsigned rg = (unsigned)reduce_blocks(n);
   const bool precon = S.precon != LGX_PRECON_NONE;
-  // initialisation (bicgstab/solver.hpp:51-71)
-  LGX_CHECK(S.residual(b, x, r, &ks->res2));
-  LGX_CUDA(cudaMemcpyAsync(r0, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-  LGX_CUDA(cudaMemcpyAsync(pd, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-  k_bicg_init<<<1, 1, 0, s>>>(ks);
+  LGX_CHECK(S.apply(pd, q));
+  k_dot_post<<<rg, kKT, 0, s>>>(n, pd, q, POST_ALPHA, ks, S.partials.p, S.counters.p);
   LGX_LAUNCH_CHECK();
-  KScalars h{};
-  LGX_CHECK(S.read(h));
-  if (!std::isfinite(h.res2))
-    return fail(LGX_ERR_NONFINITE, "non-finite initial residual");
-  const double rn0 = std::sqrt(h.res2);
-  if (history) history[0] = rn0;
-  int64_t it = 0;
-  double res = rn0;
-  lgx_status st = LGX_OK;
+  const bool rere = K.p.rere_period > 0 && K.it > 0 && K.it % K.p.rere_period == 0;
+  k_cg_update<<<rg, kKT, 0, s>>>(n, ks, pd, q, x, r, rere ? 0 : 1, precon ? 0 : 1, S.partials.p,
+                                 S.counters.p);
+  LGX_LAUNCH_CHECK();
+  if (rere) {
+    LGX_CHECK(S.residual(b, x, r, &ks->res2));
+    if (!precon) {
+      k_cg_plain_rho<<<1, 1, 0, s>>>(ks);
+      LGX_LAUNCH_CHECK();
+    }
+  }
+  if (precon) {
+    LGX_CHECK(S.precondition(r, q));
+    k_dot_post<<<rg, kKT, 0, s>>>(n, r, q, POST_RHO_BETA, ks, S.partials.p, S.counters.p);
+    LGX_LAUNCH_CHECK();
+    k_xpby<<<S.vgrid(), 256, 0, s>>>(n, ks, q, pd);
+  } else {
+    k_xpby<<<S.vgrid(), 256, 0, s>>>(n, ks, r, pd);
+  }
+  LGX_LAUNCH_CHECK();
+  return LGX_OK;
+}
+
+// bicgstab/solver.hpp:73-151
+static lgx_status bicgstab_iterate(lgx_krylov &K) {
+  Solver &S = K.S;
+  const int64_t n = S.n;
+  cudaStream_t s = S.s;
+  double *b = K.V[0], *x = K.V[1], *r = K.V[2], *r0 = K.V[3], *pd = K.V[4], *v = K.V[5],
+         *t = K.V[6], *px = K.V[7];
+  KScalars *ks = S.ks.p;
+  const unsigned rg = (unsigned)reduce_blocks(n);
+  const bool precon = S.precon != LGX_PRECON_NONE;
   double *partials2 = S.partials2.p;
   unsigned *c1 = S.counters.p, *c2 = S.counters.p + 1;
-  while (it < p->maxit && res > p->rtol * rn0 && h.rho != 0.0) {
-    const double *y = pd;
-    if (precon) {
-      LGX_CHECK(S.precondition(pd, px));
-      y = px;
-    }
-    LGX_CHECK(S.apply(y, v));
-    k_dot_post<<<rg, kKT, 0, s>>>(n, r0, v, POST_ALPHA, ks, S.partials.p, c1);
-    LGX_LAUNCH_CHECK();
-    // x += alpha y ; r -= alpha v ; res2 = ||r||^2
-    k_cg_update<<<rg, kKT, 0, s>>>(n, ks, y, v, x, r, 1, 0, S.partials.p, c1);
-    LGX_LAUNCH_CHECK();
-    const double *z = r;
-    if (precon) {
-      LGX_CHECK(S.precondition(r, px));
-      z = px;
-    }
-    LGX_CHECK(S.apply(z, t));
-    k_dot2_post<<<rg, kKT, 0, s>>>(n, t, r, t, t, POST_OMEGA, ks, S.partials.p, partials2, c1,
-                                    c2);
-    LGX_LAUNCH_CHECK();
-    k_axpy_ks<<<S.vgrid(), 256, 0, s>>>(n, ks, 1, z, x);
-    LGX_LAUNCH_CHECK();
-    const bool rere = p->rere_period > 0 && it > 0 && it % p->rere_period == 0;
-    if (rere) LGX_CHECK(S.residual(b, x, r, nullptr));
-    k_bicg_r<<<rg, kKT, 0, s>>>(n, ks, rere ? 0 : 1, t, r, r0, S.partials.p, partials2, c1, c2);
-    LGX_LAUNCH_CHECK();
-    k_bicg_p<<<S.vgrid(), 256, 0, s>>>(n, ks, r, v, pd);
-    LGX_LAUNCH_CHECK();
-    ++it;
-    LGX_CHECK(S.read(h));
-    res = std::sqrt(h.res2);
-    if (history) history[it] = res;
-    if ((st = check_flags(h, it)) != LGX_OK) break;
+  const double *y = pd;
+  if (precon) {
+    LGX_CHECK(S.precondition(pd, px));
+    y = px;
   }
-  if (S.perm) {
-    LGX_CHECK(scatter<double, double>(n, S.perm, x, d_x, s));
+  LGX_CHECK(S.apply(y, v));
+  k_dot_post<<<rg, kKT, 0, s>>>(n, r0, v, POST_ALPHA, ks, S.partials.p, c1);
+  LGX_LAUNCH_CHECK();
+  k_cg_update<<<rg, kKT, 0, s>>>(n, ks, y, v, x, r, 1, 0, S.partials.p, c1);
+  LGX_LAUNCH_CHECK();
+  const double *z = r;
+  if (precon) {
+    LGX_CHECK(S.precondition(r, px));
+    z = px;
+  }
+  LGX_CHECK(S.apply(z, t));
+  k_dot2_post<<<rg, kKT, 0, s>>>(n, t, r, t, t, POST_OMEGA, ks, S.partials.p, partials2, c1, c2);
+  LGX_LAUNCH_CHECK();
+  k_axpy_ks<<<S.vgrid(), 256, 0, s>>>(n, ks, 1, z, x);
+  LGX_LAUNCH_CHECK();
+  const bool rere = K.p.rere_period > 0 && K.it > 0 && K.it % K.p.rere_period == 0;
+  if (rere) LGX_CHECK(S.residual(b, x, r, nullptr));
+  k_bicg_r<<<rg, kKT, 0, s>>>(n, ks, rere ? 0 : 1, t, r, r0, S.partials.p, partials2, c1, c2);
+  LGX_LAUNCH_CHECK();
+  k_bicg_p<<<S.vgrid(), 256, 0, s>>>(n, ks, r, v, pd);
+  LGX_LAUNCH_CHECK();
+  return LGX_OK;
+}
+
+static lgx_status krylov_iterate(lgx_krylov &K) {
+  LGX_CHECK(K.kind == LGX_KRYLOV_CG ? cg_iterate(K) : bicgstab_iterate(K));
+  ++K.it;
+  LGX_CHECK(K.S.read(K.h));
+  return check_flags(K.h, K.it);
+}
+
+static lgx_status krylov_solution(lgx_krylov &K, double *d_x) {
+  const int64_t n = K.S.n;
+  if (K.S.perm) {
+    LGX_CHECK(scatter<double, double>(n, K.S.perm, K.V[1], d_x, K.S.s));
   } else {
-    LGX_CUDA(cudaMemcpyAsync(d_x, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    LGX_CUDA(cudaMemcpyAsync(d_x, K.V[1], sizeof(double) * n, cudaMemcpyDeviceToDevice, K.S.s));
   }
-  LGX_CUDA(cudaStreamSynchronize(s));
-  if (iterations) *iterations = it;
-  if (final_rel) *final_rel = rn0 > 0 ? res / rn0 : 0.0;
-  return st;
+  LGX_CUDA(cudaStreamSynchronize(K.S.s));
+  return LGX_OK;
+}
+
+static lgx_status krylov_create(int kind, const lgx_matrix *a, const double *d_b,
+                                const double *d_x, const lgx_solve_params *p, cudaStream_t s,
+                                std::unique_ptr<lgx_krylov> &out) {
+  auto K = std::make_unique<lgx_krylov>();
+  K->kind = kind;
+  K->p = *p;
+  LGX_CHECK(setup_solver(a, p, s, K->S, K->own_col));
+  LGX_CHECK(krylov_init(*K, d_b, d_x));
+  out = std::move(K);
+  return LGX_OK;
+}
+
+static lgx_status run_solve(int kind, const lgx_matrix *a, const double *d_b, double *d_x,
+                            const lgx_solve_params *p, cudaStream_t s, int64_t *iterations,
+                            double *final_rel, double *history) {
+  std::unique_ptr<lgx_krylov> K;
+  LGX_CHECK(krylov_create(kind, a, d_b, d_x, p, s, K));
+  if (history) history[0] = K->r0;
+  double res = K->r0;
+  lgx_status st = LGX_OK;
+  // run_iterative_solver with the stopping rule ||r|| <= rtol ||r0||, maxit, rho == 0
+  while (K->it < p->maxit && res > p->rtol * K->r0 && K->h.rho != 0.0) {
+    st = krylov_iterate(*K);
+    res = std::sqrt(K->h.res2);
+    if (history) history[K->it] = res;
+    if (st != LGX_OK) break;
+  }
+  const lgx_status st2 = krylov_solution(*K, d_x);
+  if (iterations) *iterations = K->it;
+  if (final_rel) *final_rel = K->r0 > 0 ? res / K->r0 : 0.0;
+  return st != LGX_OK ? st : st2;
 }
 
 }  // namespace lgx
@@ -517,14 +542,53 @@ lgx_status lgx_pcg(const lgx_matrix *a, const double *d_b, double *d_x,
                    const lgx_solve_params *p, lgx_stream stream, int64_t *iterations,
                    double *final_rel_residual, double *h_history) {
   if (!a || !p || (a->n > 0 && (!d_b || !d_x))) return fail(LGX_ERR_INVALID, "null argument");
-  return run_pcg(a, d_b, d_x, p, stream, iterations, final_rel_residual, h_history);
+  return run_solve(LGX_KRYLOV_CG, a, d_b, d_x, p, stream, iterations, final_rel_residual,
+                   h_history);
 }
 
 lgx_status lgx_pbicgstab(const lgx_matrix *a, const double *d_b, double *d_x,
                          const lgx_solve_params *p, lgx_stream stream, int64_t *iterations,
                          double *final_rel_residual, double *h_history) {
   if (!a || !p || (a->n > 0 && (!d_b || !d_x))) return fail(LGX_ERR_INVALID, "null argument");
-  return run_pbicgstab(a, d_b, d_x, p, stream, iterations, final_rel_residual, h_history);
+  return run_solve(LGX_KRYLOV_BICGSTAB, a, d_b, d_x, p, stream, iterations, final_rel_residual,
+                   h_history);
+}
+
+lgx_status lgx_krylov_create(int kind, const lgx_matrix *a, const double *d_b,
+                             const double *d_x, const lgx_solve_params *p, lgx_stream stream,
+                             lgx_krylov **out) {
+  if (!a || !p || !out || (a->n > 0 && (!d_b || !d_x)))
+    return fail(LGX_ERR_INVALID, "null argument");
+  if (kind != LGX_KRYLOV_CG && kind != LGX_KRYLOV_BICGSTAB)
+    return fail(LGX_ERR_INVALID, "unknown Krylov method");
+  std::unique_ptr<lgx_krylov> K;
+  LGX_CHECK(krylov_create(kind, a, d_b, d_x, p, stream, K));
+  *out = K.release();
+  return LGX_OK;
+}
+
+lgx_status lgx_krylov_iterate(lgx_krylov *k) {
+  if (!k) return fail(LGX_ERR_INVALID, "null solver");
+  return krylov_iterate(*k);
+}
+
+lgx_status lgx_krylov_state(const lgx_krylov *k, int64_t *iteration, double *residual_norm,
+                            double *rho) {
+  if (!k) return fail(LGX_ERR_INVALID, "null solver");
+  if (iteration) *iteration = k->it;
+  if (residual_norm) *residual_norm = std::sqrt(k->h.res2);
+  if (rho) *rho = k->h.rho;
+  return LGX_OK;
+}
+
+lgx_status lgx_krylov_solution(lgx_krylov *k, double *d_x) {
+  if (!k || !d_x) return fail(LGX_ERR_INVALID, "null argument");
+  return krylov_solution(*k, d_x);
+}
+
+lgx_status lgx_krylov_destroy(lgx_krylov *k) {
+  delete k;
+  return LGX_OK;
 }
 
 }  // extern "C"
