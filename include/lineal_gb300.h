@@ -282,6 +282,8 @@ typedef struct {
   double rtol;
   int64_t maxit;
   int64_t rere_period;          /* 0 disables true-residual recomputation */
+  int use_graphs;               /* capture each iteration (SpMV, reductions, updates and
+                                   the whole V-cycle) in a CUDA graph and replay it */
 } lgx_solve_params;
 
 void lgx_solve_default_params(lgx_solve_params *p);

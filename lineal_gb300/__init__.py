@@ -82,6 +82,7 @@ class _SolveParams(C.Structure):
         ("rtol", C.c_double),
         ("maxit", C.c_int64),
         ("rere_period", C.c_int64),
+        ("use_graphs", C.c_int),
     ]
 
 
@@ -575,7 +576,7 @@ class SolveResult:
 
 def _solve(fn, a: _Matrix, b, x0=None, precon=PRECON_NONE, relax=1.0, ultra=False,
            colouring: Colouring | None = None, amg: Hierarchy | None = None, rtol=1e-8,
-           maxit=1000, rere_period=8) -> SolveResult:
+           maxit=1000, rere_period=8, use_graphs=True) -> SolveResult:
     b = _dvec(b)
     x = _dvec(x0) if x0 is not None else _empty(b.numel()).zero_()
     if x0 is not None:
@@ -590,6 +591,7 @@ def _solve(fn, a: _Matrix, b, x0=None, precon=PRECON_NONE, relax=1.0, ultra=Fals
     p.rtol = rtol
     p.maxit = maxit
     p.rere_period = rere_period
+    p.use_graphs = int(use_graphs)
     it = C.c_int64()
     rel = C.c_double()
     hist = np.zeros(maxit + 1)

@@ -9,7 +9,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <memory>
 #include <vector>
 
@@ -805,8 +807,23 @@ int64_t amg_partitions(int64_t n, const lgx_amg_params &p) {
   return parts;
 }
 
+// Setup phase timer (LGX_VERBOSE=1 prints the phases to stderr).
+struct PhaseTimer {
+  bool on = std::getenv("LGX_VERBOSE") != nullptr;
+  std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+  void mark(cudaStream_t s, const char *what, int64_t level) {
+    if (!on) return;
+    cudaStreamSynchronize(s);
+    const auto now = std::chrono::steady_clock::now();
+    std::fprintf(stderr, "[lgx setup] level %lld %-12s %9.2f ms\n", (long long)level, what,
+                 std::chrono::duration<double, std::milli>(now - t).count());
+    t = now;
+  }
+};
+
 static lgx_status amg_build(const lgx_matrix *m, const lgx_amg_params &p,
                             const lgx_colouring *finest_colouring, cudaStream_t s, lgx_amg &h) {
+  PhaseTimer timer;
   h.p = p;
   h.f32 = p.cycle_f32 != 0;
   auto l0 = std::make_unique<lgx_amg_level>();
@@ -822,14 +839,17 @@ static lgx_status amg_build(const lgx_matrix *m, const lgx_amg_params &p,
     LGX_CHECK(iso.alloc(a.n));
     LGX_CHECK(strength(a, aggressive ? p.aggressive_threshold : p.strong_threshold, dep.p, inf.p,
                        iso.p, s));
+    timer.mark(s, "strength", level);
     LGX_CHECK(aggregate(a, dep.p, inf.p, iso.p, p.min_aggregate_size, p.max_aggregate_size,
                         amg_partitions(a.n, p), aggressive, s, fine.agg));
+    timer.mark(s, "aggregate", level);
     if (level < 32)
       for (int k = 0; k < 5; ++k) h.stats[level][k] = fine.agg.stats[k];
     if (fine.agg.ncoarse == 0 && a.n > 0)
       return fail(LGX_ERR_INVALID, "aggregation produced no aggregates (all rows isolated)");
     auto coarse = std::make_unique<lgx_amg_level>();
     LGX_CHECK(galerkin(a, fine.agg, p.coarse_f32, s, coarse->own));
+    timer.mark(s, "galerkin", level);
     coarse->a = &coarse->own;
     const int64_t fsize = a.n, csize = coarse->own.n;
     h.lv.push_back(std::move(coarse));
@@ -858,6 +878,7 @@ static lgx_status amg_build(const lgx_matrix *m, const lgx_amg_params &p,
       LGX_CHECK(colouring_build(*lv.a, lv.col->colour.p, nc, s, *lv.col));
     }
     if (h.f32) LGX_CHECK(colouring_make_f32(*lv.col, s));
+    timer.mark(s, "colouring", l);
   }
   // transfers in permuted spaces
   for (int64_t l = 0; l + 1 < L; ++l) {
@@ -902,7 +923,10 @@ static lgx_status amg_build(const lgx_matrix *m, const lgx_amg_params &p,
       LGX_CHECK(lv.r64.alloc(n));
     }
   }
-  return dense_inverse(*h.lv[L - 1]->a, s, h.inv);
+  timer.mark(s, "transfers", -1);
+  LGX_CHECK(dense_inverse(*h.lv[L - 1]->a, s, h.inv));
+  timer.mark(s, "coarse_inv", L - 1);
+  return LGX_OK;
 }
 
 // Smoother sweep / residual on one level with the level's value storage:

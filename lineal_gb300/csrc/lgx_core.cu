@@ -18,6 +18,40 @@ static std::atomic<uint64_t> g_launches{0};
 
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+int sm_count() {
+  static int n = [] {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v > 0 ? v : 1;
+  }();
+  return n;
+}
+
+int *device_error_flag() {
+  static int *p = [] {
+    int *q = nullptr;
+    if (cudaMalloc(&q, sizeof(int)) != cudaSuccess) return (int *)nullptr;
+    cudaMemset(q, 0, sizeof(int));
+    cudaDeviceSynchronize();
+    return q;
+  }();
+  return p;
+}
+
+lgx_status check_device_error(cudaStream_t s) {
+  int *p = device_error_flag();
+  if (!p) return fail(LGX_ERR_NOMEM, "device error flag not allocated");
+  int h = 0;
+  LGX_CUDA(cudaMemcpyAsync(&h, p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  LGX_CUDA(cudaStreamSynchronize(s));
+  if (h) {
+    LGX_CUDA(cudaMemsetAsync(p, 0, sizeof(int), s));
+    return fail(LGX_ERR_CUDA, "a device wait on a shared-memory copy timed out");
+  }
+  return LGX_OK;
+}
+
 void set_error(const std::string &msg) { g_last_error = msg; }
 
 lgx_status fail(lgx_status s, const std::string &msg) {
@@ -76,17 +110,15 @@ lgx_status csr_from_device(int64_t n, int64_t nnz, const int64_t *rowptr, const 
   out.symmetric = symmetric;
   out.storage = storage;
   LGX_CHECK(out.rowptr.alloc(n + 1));
-  LGX_CHECK(out.col.alloc(nnz));
+  LGX_CHECK(csr_alloc_arrays(out, nnz, storage));
   LGX_CUDA(cudaMemcpyAsync(out.rowptr.p, rowptr, sizeof(int64_t) * (n + 1),
                            cudaMemcpyDeviceToDevice, s));
   if (nnz) LGX_CUDA(cudaMemcpyAsync(out.col.p, col, sizeof(int32_t) * nnz,
                                     cudaMemcpyDeviceToDevice, s));
   if (storage == LGX_F64) {
-    LGX_CHECK(out.v64.alloc(nnz));
     if (nnz) LGX_CUDA(cudaMemcpyAsync(out.v64.p, val, sizeof(double) * nnz,
                                       cudaMemcpyDeviceToDevice, s));
   } else {
-    LGX_CHECK(out.v32.alloc(nnz));
     if (nnz) {
       k_f64_to_f32<<<std::min<int64_t>(grid_for(nnz, 256), 4096), 256, 0, s>>>(nnz, val,
                                                                                out.v32.p);
@@ -94,6 +126,16 @@ lgx_status csr_from_device(int64_t n, int64_t nnz, const int64_t *rowptr, const 
     }
   }
   return csr_compute_max_row(out, s);
+}
+
+lgx_status csr_alloc_arrays(Csr &a, int64_t nnz, lgx_dtype storage) {
+  LGX_CHECK(a.col.alloc(nnz + kCsrPad));
+  if (storage == LGX_F64) {
+    LGX_CHECK(a.v64.alloc(nnz + kCsrPad));
+  } else {
+    LGX_CHECK(a.v32.alloc(nnz + kCsrPad));
+  }
+  return LGX_OK;
 }
 
 lgx_status csr_compute_max_row(Csr &a, cudaStream_t s) {
@@ -377,9 +419,9 @@ static lgx_status gen_structured(const int64_t dims[3], const double *d_k, int n
   c.symmetric = 1;
   c.storage = storage;
   c.rowptr = std::move(rowptr);
-  lgx_status st = c.col.alloc(nnz);
+  lgx_status st = c.col.alloc(nnz + kCsrPad);
   DBuf<double> v64;
-  if (st == LGX_OK) st = v64.alloc(nnz);
+  if (st == LGX_OK) st = v64.alloc(nnz + kCsrPad);
   if (st != LGX_OK) {
     delete m;
     return st;
@@ -392,7 +434,7 @@ static lgx_status gen_structured(const int64_t dims[3], const double *d_k, int n
   if (storage == LGX_F64) {
     c.v64 = std::move(v64);
   } else {
-    st = c.v32.alloc(nnz);
+    st = c.v32.alloc(nnz + kCsrPad);
     if (st != LGX_OK) {
       delete m;
       return st;

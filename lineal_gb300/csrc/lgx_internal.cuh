@@ -71,6 +71,9 @@ struct DBuf {
 };
 
 constexpr uint32_t kUnaggregated = 0xFFFFFFFFu;
+// trailing elements of every CSR column/value buffer (the staged row kernels
+// copy 16-byte-aligned spans that may reach past the last entry)
+constexpr int kCsrPad = 16;
 constexpr uint32_t kIsolated = 0xFFFFFFFEu;
 
 // ---- matrices -------------------------------------------------------------
@@ -193,6 +196,10 @@ inline unsigned grid_for(int64_t n, int threads) {
 }
 
 lgx_status inclusive_offsets(int64_t n, const int64_t *in, int64_t *out, cudaStream_t s);
+lgx_status check_device_error(cudaStream_t s);
+// allocates the column/value arrays of a CSR with the trailing padding that
+// the staged row kernels rely on
+lgx_status csr_alloc_arrays(Csr &a, int64_t nnz, lgx_dtype storage);
 // partial-sum slots needed by the fused reductions of the row-block kernels
 int64_t csr_partials(int64_t n);
 int64_t matrix_partials(const lgx_matrix *a);

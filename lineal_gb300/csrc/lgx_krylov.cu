@@ -343,6 +343,15 @@ struct lgx_krylov {
   lgx::KScalars h{};
   int64_t it = 0;
   double r0 = 0.0;
+  // captured iterations: [0] regular, [1] with true-residual recomputation
+  cudaStream_t user_stream = nullptr;
+  cudaStream_t capture_stream = nullptr;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  ~lgx_krylov() {
+    for (auto &g : graph)
+      if (g) cudaGraphExecDestroy(g);
+    if (capture_stream) cudaStreamDestroy(capture_stream);
+  }
 };
 
 namespace lgx {
@@ -469,8 +478,47 @@ static lgx_status bicgstab_iterate(lgx_krylov &K) {
   return LGX_OK;
 }
 
+static lgx_status iterate_body(lgx_krylov &K) {
+  return K.kind == LGX_KRYLOV_CG ? cg_iterate(K) : bicgstab_iterate(K);
+}
+
+// Records one iteration (the variant selected by `rere`) into a CUDA graph.
+// Capture runs on a private stream (the legacy default stream cannot be
+// captured); the graph is then launched on the caller's stream.
+static lgx_status capture_iteration(lgx_krylov &K, int rere) {
+  if (!K.capture_stream)
+    LGX_CUDA(cudaStreamCreateWithFlags(&K.capture_stream, cudaStreamNonBlocking));
+  const int64_t saved_it = K.it;
+  // the rere decision inside the bodies depends on K.it: pick a representative
+  K.it = rere ? K.p.rere_period : 1;
+  K.S.s = K.capture_stream;
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(K.capture_stream, cudaStreamCaptureModeThreadLocal);
+  lgx_status st = e == cudaSuccess ? iterate_body(K) : cuda_fail(e, "cudaStreamBeginCapture");
+  cudaError_t e2 = cudaStreamEndCapture(K.capture_stream, &g);
+  K.S.s = K.user_stream;
+  K.it = saved_it;
+  if (st != LGX_OK) {
+    if (g) cudaGraphDestroy(g);
+    return st;
+  }
+  if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(&K.graph[rere], g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+  return LGX_OK;
+}
+
 static lgx_status krylov_iterate(lgx_krylov &K) {
-  LGX_CHECK(K.kind == LGX_KRYLOV_CG ? cg_iterate(K) : bicgstab_iterate(K));
+  const bool rere = K.p.rere_period > 0 && K.it > 0 && K.it % K.p.rere_period == 0;
+  if (K.p.use_graphs && K.it > 0) {
+    // the first iteration ran eagerly (it also initialises per-kernel
+    // attributes); later iterations replay captured graphs
+    if (!K.graph[rere]) LGX_CHECK(capture_iteration(K, rere ? 1 : 0));
+    LGX_CUDA(cudaGraphLaunch(K.graph[rere], K.user_stream));
+  } else {
+    LGX_CHECK(iterate_body(K));
+  }
   ++K.it;
   LGX_CHECK(K.S.read(K.h));
   return check_flags(K.h, K.it);
@@ -493,6 +541,7 @@ static lgx_status krylov_create(int kind, const lgx_matrix *a, const double *d_b
   auto K = std::make_unique<lgx_krylov>();
   K->kind = kind;
   K->p = *p;
+  K->user_stream = s;
   LGX_CHECK(setup_solver(a, p, s, K->S, K->own_col));
   LGX_CHECK(krylov_init(*K, d_b, d_x));
   out = std::move(K);
@@ -536,6 +585,7 @@ void lgx_solve_default_params(lgx_solve_params *p) {
   p->rtol = 1e-8;
   p->maxit = 1000;
   p->rere_period = 8;
+  p->use_graphs = 1;
 }
 
 lgx_status lgx_pcg(const lgx_matrix *a, const double *d_b, double *d_x,

@@ -15,79 +15,37 @@
 #include <vector>
 
 #include "lgx_internal.cuh"
+#include "lgx_rows.cuh"
 
 namespace lgx {
 
-constexpr int kSmRows = 128;
-
-template <typename VT>
-struct SmCap {
-  static constexpr int value = 48 * 1024 / (int)(sizeof(int32_t) + sizeof(VT));
-};
-
-template <typename VT>
-__device__ __forceinline__ bool sm_stage(const int64_t *__restrict__ rowptr,
-                                         const int32_t *__restrict__ col,
-                                         const VT *__restrict__ val, int64_t r0, int64_t r1,
-                                         int32_t *s_col, VT *s_val, int64_t &e0) {
-  constexpr int CAP = SmCap<VT>::value;
-  e0 = rowptr[r0];
-  const int64_t e1 = rowptr[r1];
-  if (e1 - e0 > CAP) return false;
-  const int cnt = (int)(e1 - e0);
-  for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
-    s_col[k] = __ldg(col + e0 + k);
-    s_val[k] = __ldg(val + e0 + k);
-  }
-  __syncthreads();
-  return true;
-}
-
 // ---- Jacobi ----------------------------------------------------------------
 template <typename VT>
-__device__ __forceinline__ double jacobi_row(int64_t i, const int32_t *c, const VT *v, int len,
-                                             const double *__restrict__ x_in, double bi,
-                                             double relax, double m1) {
-  double accum = bi, diag = 0.0;
-  for (int k = 0; k < len; ++k) {
-    const int32_t j = c[k];
-    const double a = (double)v[k];
-    if (j == i) {
-      diag = a;
-    } else if (x_in) {
-      accum = fma(-a, __ldg(x_in + j), accum);
-    } else {
-      accum = fma(-a, 0.0, accum);
+struct JacobiOp {
+  const double *x_in;  // nullptr: zero input vector
+  double *x_out;
+  const double *b;
+  double relax, m1;
+  static constexpr bool kReduce = false;
+  double *partials = nullptr;
+  unsigned *counter = nullptr;
+  __device__ __forceinline__ double row(int64_t i, const int32_t *c, const VT *v, int len) const {
+    double accum = b[i], diag = 0.0;
+    for (int k = 0; k < len; ++k) {
+      const int32_t j = c[k];
+      const double a = (double)v[k];
+      if (j == i) {
+        diag = a;
+      } else {
+        accum = fma(-a, x_in ? __ldg(x_in + j) : 0.0, accum);
+      }
     }
+    const double quot = accum / diag;
+    x_out[i] = fma(relax, quot, m1 * (x_in ? x_in[i] : 0.0));
+    return 0.0;
   }
-  const double quot = accum / diag;
-  return fma(relax, quot, m1 * (x_in ? x_in[i] : 0.0));
-}
-
-template <typename VT>
-__global__ void __launch_bounds__(kSmRows)
-  k_jacobi(int64_t n, const int64_t *__restrict__ rowptr, const int32_t *__restrict__ col,
-           const VT *__restrict__ val, double relax, const double *__restrict__ x_in,
-           double *__restrict__ x_out, const double *__restrict__ b) {
-  constexpr int CAP = SmCap<VT>::value;
-  __shared__ int32_t s_col[CAP];
-  __shared__ VT s_val[CAP];
-  const int64_t r0 = (int64_t)blockIdx.x * kSmRows;
-  const int64_t r1 = min(r0 + kSmRows, n);
-  const int64_t row = r0 + threadIdx.x;
-  int64_t e0;
-  const double m1 = 1.0 - relax;
-  if (sm_stage(rowptr, col, val, r0, r1, s_col, s_val, e0)) {
-    if (row < r1) {
-      const int64_t bb = rowptr[row], e = rowptr[row + 1];
-      x_out[row] = jacobi_row(row, s_col + (bb - e0), s_val + (bb - e0), (int)(e - bb), x_in,
-                              b[row], relax, m1);
-    }
-  } else if (row < r1) {
-    const int64_t bb = rowptr[row], e = rowptr[row + 1];
-    x_out[row] = jacobi_row(row, col + bb, val + bb, (int)(e - bb), x_in, b[row], relax, m1);
-  }
-}
+  __device__ __forceinline__ void finish(double) const {}
+};
 
 // Jacobi from a zero start with a cached diagonal (stencil matrices):
 // x = fma(relax, b / d, m1 * 0) -- the reference's arithmetic with x_in = 0.
@@ -312,16 +270,14 @@ lgx_status colouring_build(const Csr &a, const int32_t *d_colour, int32_t ncolou
   p.storage = a.storage;
   p.max_row = a.max_row;
   LGX_CHECK(p.rowptr.alloc(n + 1));
-  LGX_CHECK(p.col.alloc(a.nnz));
+  LGX_CHECK(csr_alloc_arrays(p, a.nnz, a.storage));
   k_perm_rowlen<<<g, 256, 0, s>>>(n, a.rowptr.p, out.perm.p, flag.p);
   LGX_LAUNCH_CHECK();
   LGX_CHECK(inclusive_offsets(n, flag.p, p.rowptr.p, s));
   if (a.storage == LGX_F64) {
-    LGX_CHECK(p.v64.alloc(a.nnz));
     k_perm_fill<double><<<g, 256, 0, s>>>(n, a.rowptr.p, a.col.p, a.v64.p, out.perm.p,
                                           out.iperm.p, p.rowptr.p, p.col.p, p.v64.p);
   } else {
-    LGX_CHECK(p.v32.alloc(a.nnz));
     k_perm_fill<float><<<g, 256, 0, s>>>(n, a.rowptr.p, a.col.p, a.v32.p, out.perm.p, out.iperm.p,
                                          p.rowptr.p, p.col.p, p.v32.p);
   }
@@ -332,7 +288,7 @@ lgx_status colouring_build(const Csr &a, const int32_t *d_colour, int32_t ncolou
 
 lgx_status colouring_make_f32(lgx_colouring &c, cudaStream_t s) {
   if (c.pcsr.storage == LGX_F32 || c.pv32.p) return LGX_OK;
-  LGX_CHECK(c.pv32.alloc(c.pcsr.nnz));
+  LGX_CHECK(c.pv32.alloc(c.pcsr.nnz + kCsrPad));
   k_to_f32<<<std::min<int64_t>(grid_for(c.pcsr.nnz, 256), 16384), 256, 0, s>>>(
     c.pcsr.nnz, c.pcsr.v64.p, c.pv32.p);
   LGX_LAUNCH_CHECK();
@@ -340,66 +296,70 @@ lgx_status colouring_make_f32(lgx_colouring &c, cudaStream_t s) {
 }
 
 // ---- multicolour SOR -------------------------------------------------------
+// One row of gauss-seidel-variant/sweep.hpp:134-200 in place: rows of other
+// colours already visited in this sweep hold their new values in x, the rest
+// their input values; rows of the same colour are never adjacent.
 template <typename VT, typename XT>
-__device__ __forceinline__ void sor_row(int64_t i, const int32_t *c, const VT *v, int len,
-                                        const XT *__restrict__ b, XT *x, XT relax, XT m1,
-                                        bool ultra) {
-  XT accum = b[i], diag = XT(0);
-  const XT xi = x[i];
-  for (int k = 0; k < len; ++k) {
-    const int32_t j = c[k];
-    const XT a = (XT)v[k];
-    if (j == i) {
-      diag = a;
-      if (ultra) accum = fma(-a, xi, accum);
+struct SorOp {
+  const XT *b;
+  XT *x;
+  XT relax, m1;
+  int ultra;
+  static constexpr bool kReduce = false;
+  double *partials = nullptr;
+  unsigned *counter = nullptr;
+  __device__ __forceinline__ double row(int64_t i, const int32_t *c, const VT *v, int len) const {
+    XT accum = b[i], diag = XT(0);
+    const XT xi = x[i];
+    int k = 0;
+    for (; k + 8 <= len; k += 8) {
+      int32_t cc[8];
+      XT xv[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) cc[u] = c[k + u];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) xv[u] = x[cc[u]];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const XT a = (XT)v[k + u];
+        if (cc[u] == i) {
+          diag = a;
+          if (ultra) accum = fma(-a, xi, accum);
+        } else {
+          accum = fma(-a, xv[u], accum);
+        }
+      }
+    }
+    for (; k < len; ++k) {
+      const int32_t j = c[k];
+      const XT a = (XT)v[k];
+      if (j == i) {
+        diag = a;
+        if (ultra) accum = fma(-a, xi, accum);
+      } else {
+        accum = fma(-a, x[j], accum);
+      }
+    }
+    if (ultra) {
+      x[i] = xi + relax * accum / fabs(diag);
     } else {
-      accum = fma(-a, x[j], accum);
+      const XT quot = accum / diag;
+      x[i] = fma(relax, quot, m1 * xi);
     }
+    return 0.0;
   }
-  if (ultra) {
-    x[i] = xi + relax * accum / fabs(diag);
-  } else {
-    const XT quot = accum / diag;
-    x[i] = fma(relax, quot, m1 * xi);
-  }
-}
-
-template <typename VT, typename XT>
-__global__ void __launch_bounds__(kSmRows)
-  k_mc_sor(int64_t rb, int64_t re, const int64_t *__restrict__ rowptr,
-           const int32_t *__restrict__ col, const VT *__restrict__ val, const XT *__restrict__ b,
-           XT *x, XT relax, int ultra) {
-  constexpr int CAP = SmCap<VT>::value;
-  __shared__ int32_t s_col[CAP];
-  __shared__ VT s_val[CAP];
-  const int64_t r0 = rb + (int64_t)blockIdx.x * kSmRows;
-  const int64_t r1 = min(r0 + kSmRows, re);
-  const int64_t row = r0 + threadIdx.x;
-  int64_t e0;
-  const XT m1 = XT(1) - relax;
-  if (sm_stage(rowptr, col, val, r0, r1, s_col, s_val, e0)) {
-    if (row < r1) {
-      const int64_t bb = rowptr[row], e = rowptr[row + 1];
-      sor_row<VT, XT>(row, s_col + (bb - e0), s_val + (bb - e0), (int)(e - bb), b, x, relax, m1,
-                      ultra != 0);
-    }
-  } else if (row < r1) {
-    const int64_t bb = rowptr[row], e = rowptr[row + 1];
-    sor_row<VT, XT>(row, col + bb, val + bb, (int)(e - bb), b, x, relax, m1, ultra != 0);
-  }
-}
+  __device__ __forceinline__ void finish(double) const {}
+};
 
 template <typename VT, typename XT>
 lgx_status mc_sor_sweep(const lgx_colouring &c, const VT *val, double relax, int forward,
                         int ultra, const XT *b, XT *x, cudaStream_t s) {
   const Csr &p = c.pcsr;
+  const SorOp<VT, XT> op{b, x, (XT)relax, XT(1) - (XT)relax, ultra};
   for (int32_t k = 0; k < c.ncolours; ++k) {
     const int32_t col_id = forward ? k : c.ncolours - 1 - k;
     const int64_t rb = c.offsets[col_id], re = c.offsets[col_id + 1];
-    if (re <= rb) continue;
-    k_mc_sor<VT, XT><<<grid_for(re - rb, kSmRows), kSmRows, 0, s>>>(
-      rb, re, p.rowptr.p, p.col.p, val, b, x, (XT)relax, ultra);
-    LGX_LAUNCH_CHECK();
+    LGX_CHECK(launch_rows<VT>(rb, re, p.max_row, p.rowptr.p, p.col.p, val, op, s));
   }
   return LGX_OK;
 }
@@ -416,13 +376,10 @@ lgx_status jacobi_csr(const Csr &a, double relax, const double *x_in, double *x_
                       const double *b, cudaStream_t s) {
   if (a.n == 0) return LGX_OK;
   if (a.storage == LGX_F64)
-    k_jacobi<double><<<grid_for(a.n, kSmRows), kSmRows, 0, s>>>(a.n, a.rowptr.p, a.col.p, a.v64.p,
-                                                                relax, x_in, x_out, b);
-  else
-    k_jacobi<float><<<grid_for(a.n, kSmRows), kSmRows, 0, s>>>(a.n, a.rowptr.p, a.col.p, a.v32.p,
-                                                               relax, x_in, x_out, b);
-  LGX_LAUNCH_CHECK();
-  return LGX_OK;
+    return launch_rows<double>(0, a.n, a.max_row, a.rowptr.p, a.col.p, a.v64.p,
+                               JacobiOp<double>{x_in, x_out, b, relax, 1.0 - relax}, s);
+  return launch_rows<float>(0, a.n, a.max_row, a.rowptr.p, a.col.p, a.v32.p,
+                            JacobiOp<float>{x_in, x_out, b, relax, 1.0 - relax}, s);
 }
 
 lgx_status jacobi_diag_zero(int64_t n, const double *d, double relax, const double *b, double *x,

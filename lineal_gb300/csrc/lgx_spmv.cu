@@ -12,130 +12,49 @@
 #include <cmath>
 
 #include "lgx_internal.cuh"
+#include "lgx_rows.cuh"
 
 namespace lgx {
 
 // ---------------------------------------------------------------------------
-// CSR row-block engine
+// CSR operations on the staged row engine (lgx_rows.cuh)
 // ---------------------------------------------------------------------------
-constexpr int kRows = 128;  // rows (= threads) per block
-
-template <typename VT>
-struct SegCap {
-  static constexpr int value = 48 * 1024 / (int)(sizeof(int32_t) + sizeof(VT));
+template <typename VT, typename XT>
+struct SpmvOp {
+  const XT *x;
+  XT *y;
+  static constexpr bool kReduce = false;
+  double *partials = nullptr;
+  unsigned *counter = nullptr;
+  __device__ __forceinline__ double row(int64_t i, const int32_t *c, const VT *v, int len) const {
+    y[i] = row_dot8<VT, XT>(c, v, len, x, XT(0));
+    return 0.0;
+  }
+  __device__ __forceinline__ void finish(double) const {}
 };
 
-// Loads the CSR segment of rows [r0, r1) into shared memory when it fits and
-// returns pointers to the calling thread's row (shared or global).
-template <typename VT>
-struct RowSlice {
-  const int32_t *c;
-  const VT *v;
-  int len;
-};
-
-template <typename VT>
-__device__ __forceinline__ bool stage_segment(const int64_t *__restrict__ rowptr,
-                                              const int32_t *__restrict__ col,
-                                              const VT *__restrict__ val, int64_t r0, int64_t r1,
-                                              int32_t *s_col, VT *s_val, int64_t &e0) {
-  constexpr int CAP = SegCap<VT>::value;
-  e0 = rowptr[r0];
-  const int64_t e1 = rowptr[r1];
-  if (e1 - e0 > CAP) return false;
-  const int cnt = (int)(e1 - e0);
-  for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
-    s_col[k] = __ldg(col + e0 + k);
-    s_val[k] = __ldg(val + e0 + k);
-  }
-  __syncthreads();
-  return true;
-}
-
-// sum_k fma(a_k, x[c_k], sum) in storage order, starting from `init`
-template <typename VT, typename XT>
-__device__ __forceinline__ XT row_dot(const int32_t *c, const VT *v, int len,
-                                      const XT *__restrict__ x, XT init) {
-  XT sum = init;
-  int k = 0;
-  for (; k + 4 <= len; k += 4) {
-    const int32_t c0 = c[k], c1 = c[k + 1], c2 = c[k + 2], c3 = c[k + 3];
-    const XT a0 = (XT)v[k], a1 = (XT)v[k + 1], a2 = (XT)v[k + 2], a3 = (XT)v[k + 3];
-    const XT x0 = __ldg(x + c0), x1 = __ldg(x + c1), x2 = __ldg(x + c2), x3 = __ldg(x + c3);
-    sum = fma(a0, x0, sum);
-    sum = fma(a1, x1, sum);
-    sum = fma(a2, x2, sum);
-    sum = fma(a3, x3, sum);
-  }
-  for (; k < len; ++k) sum = fma((XT)v[k], __ldg(x + c[k]), sum);
-  return sum;
-}
-
-template <typename VT, typename XT>
-__global__ void __launch_bounds__(kRows)
-  k_csr_spmv(int64_t n, const int64_t *__restrict__ rowptr, const int32_t *__restrict__ col,
-             const VT *__restrict__ val, const XT *__restrict__ x, XT *__restrict__ y) {
-  constexpr int CAP = SegCap<VT>::value;
-  __shared__ int32_t s_col[CAP];
-  __shared__ VT s_val[CAP];
-  const int64_t r0 = (int64_t)blockIdx.x * kRows;
-  const int64_t r1 = min(r0 + kRows, n);
-  const int64_t row = r0 + threadIdx.x;
-  int64_t e0;
-  if (stage_segment(rowptr, col, val, r0, r1, s_col, s_val, e0)) {
-    if (row < r1) {
-      const int64_t b = rowptr[row], e = rowptr[row + 1];
-      y[row] = row_dot(s_col + (b - e0), s_val + (b - e0), (int)(e - b), x, XT(0));
-    }
-  } else if (row < r1) {
-    const int64_t b = rowptr[row], e = rowptr[row + 1];
-    y[row] = row_dot(col + b, val + b, (int)(e - b), x, XT(0));
-  }
-}
-
-// r = b - A x, optionally reducing ||r||^2 deterministically
+// r = b - A x, optionally ||r||^2 into *out (deterministic)
 template <typename VT, typename XT, bool NORM>
-__global__ void __launch_bounds__(kRows)
-  k_csr_residual(int64_t n, const int64_t *__restrict__ rowptr, const int32_t *__restrict__ col,
-                 const VT *__restrict__ val, const XT *__restrict__ b, const XT *__restrict__ x,
-                 XT *__restrict__ r, double *norm, double *partials, unsigned *counter) {
-  constexpr int CAP = SegCap<VT>::value;
-  __shared__ int32_t s_col[CAP];
-  __shared__ VT s_val[CAP];
-  const int64_t r0 = (int64_t)blockIdx.x * kRows;
-  const int64_t r1 = min(r0 + kRows, n);
-  const int64_t row = r0 + threadIdx.x;
-  int64_t e0;
-  double contrib = 0.0;
-  if (stage_segment(rowptr, col, val, r0, r1, s_col, s_val, e0)) {
-    if (row < r1) {
-      const int64_t bb = rowptr[row], e = rowptr[row + 1];
-      const XT ax = row_dot(s_col + (bb - e0), s_val + (bb - e0), (int)(e - bb), x, XT(0));
-      const XT rv = b[row] - ax;
-      r[row] = rv;
-      contrib = (double)rv * (double)rv;
-    }
-  } else if (row < r1) {
-    const int64_t bb = rowptr[row], e = rowptr[row + 1];
-    const XT ax = row_dot(col + bb, val + bb, (int)(e - bb), x, XT(0));
-    const XT rv = b[row] - ax;
-    r[row] = rv;
-    contrib = (double)rv * (double)rv;
+struct ResidualOp {
+  const XT *b, *x;
+  XT *r;
+  double *out;
+  static constexpr bool kReduce = NORM;
+  double *partials;
+  unsigned *counter;
+  __device__ __forceinline__ double row(int64_t i, const int32_t *c, const VT *v, int len) const {
+    const XT ax = row_dot8<VT, XT>(c, v, len, x, XT(0));
+    const XT rv = b[i] - ax;
+    r[i] = rv;
+    return NORM ? (double)rv * (double)rv : 0.0;
   }
-  if constexpr (NORM) {
-    double t;
-    if (grid_reduce<kRows>(contrib, blockIdx.x, gridDim.x, partials, counter, &t) &&
-        threadIdx.x == 0)
-      norm[0] = t;
-  }
-}
+  __device__ __forceinline__ void finish(double t) const { *out = t; }
+};
 
 template <typename VT, typename XT>
 lgx_status csr_spmv(const Csr &a, const VT *val, const XT *x, XT *y, cudaStream_t s) {
   if (a.n == 0) return LGX_OK;
-  k_csr_spmv<VT, XT><<<grid_for(a.n, kRows), kRows, 0, s>>>(a.n, a.rowptr.p, a.col.p, val, x, y);
-  LGX_LAUNCH_CHECK();
-  return LGX_OK;
+  return launch_rows<VT>(0, a.n, a.max_row, a.rowptr.p, a.col.p, val, SpmvOp<VT, XT>{x, y}, s);
 }
 
 template <typename VT, typename XT>
@@ -145,18 +64,15 @@ lgx_status csr_residual(const Csr &a, const VT *val, const XT *b, const XT *x, X
     if (norm) LGX_CUDA(cudaMemsetAsync(norm, 0, sizeof(double), s));
     return LGX_OK;
   }
-  if (norm) {
-    k_csr_residual<VT, XT, true><<<grid_for(a.n, kRows), kRows, 0, s>>>(
-      a.n, a.rowptr.p, a.col.p, val, b, x, r, norm, partials, counter);
-  } else {
-    k_csr_residual<VT, XT, false><<<grid_for(a.n, kRows), kRows, 0, s>>>(
-      a.n, a.rowptr.p, a.col.p, val, b, x, r, nullptr, nullptr, nullptr);
-  }
-  LGX_LAUNCH_CHECK();
-  return LGX_OK;
+  if (norm)
+    return launch_rows<VT>(0, a.n, a.max_row, a.rowptr.p, a.col.p, val,
+                           ResidualOp<VT, XT, true>{b, x, r, norm, partials, counter}, s);
+  return launch_rows<VT>(0, a.n, a.max_row, a.rowptr.p, a.col.p, val,
+                         ResidualOp<VT, XT, false>{b, x, r, nullptr, nullptr, nullptr}, s);
 }
 
-int64_t csr_partials(int64_t n) { return std::max<int64_t>(1, grid_for(n, kRows)); }
+// partial-sum slots of a reducing row launch (persistent grid <= SM count)
+int64_t csr_partials(int64_t /*n*/) { return sm_count(); }
 
 template lgx_status csr_spmv<double, double>(const Csr &, const double *, const double *,
                                              double *, cudaStream_t);
