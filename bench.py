@@ -400,12 +400,53 @@ def run_gb300(args):
         torch.distributed.destroy_process_group()
 
 
+def run_kernels(args):
+    """Times the row kernels alone on the --grid matrix (also the ncu target):
+    FP64 SpMV, one multicolour SOR sweep and the residual."""
+    import torch
+
+    import lineal_gb300 as g
+
+    g.build.build()
+    stream = torch.cuda.current_stream()
+    dims, k, b_host = make_problem(args.grid)
+    n = int(np.prod(dims))
+    a = g.gen_27pt(dims, k)
+    nnz = a.non_zero_num()
+    col = g.Colouring.from_array(a, parity_colours(dims), 8)
+    x = torch.randn(n, dtype=torch.float64, device="cuda")
+    y = torch.empty_like(x)
+    b = torch.as_tensor(b_host, device="cuda")
+    out = {}
+    for name, fn, nbytes in (
+            ("spmv_fp64", lambda: g.spmv(a, x, out=y), csr_bytes(n, nnz, 8, 8)),
+            ("sor_sweep_fp64", lambda: g.sor_sweep(a, col, b, x, out=y),
+             csr_bytes(n, nnz, 8, 8) + 8 * n),
+            ("residual_fp64", lambda: g.residual(a, b, x, with_norm=False),
+             csr_bytes(n, nnz, 8, 8) + 8 * n)):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        out[name] = {"ms": ms, "gbs": nbytes / (ms * 1e-3) / 1e9}
+        log(f"[kernels] {name}: {ms:.3f} ms {out[name]['gbs']:.0f} GB/s")
+    print(json.dumps({"grid": args.grid, "kernels": out}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--mode", default="solve", choices=["solve", "kernels"])
     ap.add_argument("--grid", type=int, default=256)
     ap.add_argument("--partition-size", type=int, default=4096)
     ap.add_argument("--cpu-sample-edge", type=int, default=64)
@@ -421,6 +462,8 @@ def main():
         ap.error("--warmup must be at least 3")
     if args.impl == "reference":
         run_reference(args)
+    elif args.mode == "kernels":
+        run_kernels(args)
     else:
         run_gb300(args)
 

@@ -197,7 +197,9 @@ lgx_status lgx_sor_sweep(const lgx_matrix *a, const lgx_colouring *c, double rel
 typedef struct {
   int32_t min_aggregate_size;  /* AggregationParams (aggregation/params.hpp:13-20) */
   int32_t max_aggregate_size;
-  int64_t partition_size;      /* vertices per sequential aggregation partition */
+  int64_t partition_size;      /* vertices per aggregation partition on the finest level */
+  double partition_growth;     /* level l uses partition_size * growth^l: coarse levels
+                                  keep partitions that span several fine planes */
   int64_t max_partitions;      /* clamp on the partition count */
   double strong_threshold;     /* DuneDependencyCriterion (dependency/criterion.hpp:103-118) */
   double aggressive_threshold;

@@ -376,6 +376,7 @@ struct AggregationParams {
   int32_t min_aggregate_size = 6;
   int32_t max_aggregate_size = 9;
   int64_t partition_size = 4096;
+  double partition_growth = 4.0;
 };
 
 struct DuneDependencyCriterion {
@@ -409,6 +410,7 @@ struct MultiGridSolver : SharedStationaryIterativeSolverBase {
       p.min_aggregate_size = s.aggregation.min_aggregate_size;
       p.max_aggregate_size = s.aggregation.max_aggregate_size;
       p.partition_size = s.aggregation.partition_size;
+      p.partition_growth = s.aggregation.partition_growth;
       p.strong_threshold = s.criterion.strong_threshold;
       p.aggressive_threshold = s.criterion.aggressive_strong_threshold;
       p.relax = s.relax;

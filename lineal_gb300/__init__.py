@@ -57,6 +57,7 @@ class _AmgParams(C.Structure):
         ("min_aggregate_size", C.c_int32),
         ("max_aggregate_size", C.c_int32),
         ("partition_size", C.c_int64),
+        ("partition_growth", C.c_double),
         ("max_partitions", C.c_int64),
         ("strong_threshold", C.c_double),
         ("aggressive_threshold", C.c_double),
@@ -470,6 +471,7 @@ class HierarchyWright:
     min_aggregate_size: int = 6
     max_aggregate_size: int = 9
     partition_size: int = 4096
+    partition_growth: float = 4.0
     max_partitions: int = 1 << 30
     coarse_f32: bool = False
     cycle_f32: bool = False

@@ -137,11 +137,26 @@ lgx_status strength(const Csr &a, double theta, uint8_t *dep, uint8_t *inf, uint
 }
 
 // ===========================================================================
-// Greedy aggregation, one thread per contiguous partition
+// Greedy aggregation, one warp per contiguous partition
 // (aggregation/base.hpp:28-711 via independent.hpp:47-216).  The subgraph of
-// a partition keeps only edges whose head lies inside it.  All scratch lives
-// in n-sized arrays indexed by vertex, so partition p owns the slots
-// [pb, pe) (and [pb*max, pe*max) of the aggregate blocks).
+// a partition keeps only edges whose head lies inside it.
+//
+// The reference algorithm is sequential within a partition; here the 32 lanes
+// of a warp share each of its steps while producing the same decisions:
+//  - the front (AggregateFront, base.hpp:28-74) is an unordered set with a
+//    position index; the reference iterates it in ascending vertex order, so
+//    every selection below takes the smallest vertex ids explicitly;
+//  - grow_aggregate (base.hpp:532-585) evaluates every front vertex in
+//    parallel.  Its sequential scan keeps the vertices whose key equals the
+//    maximum key, where the key is (two-way count, connectivity, front
+//    neighbours) if any front vertex has a two-way connection and
+//    (one-way count, ...) otherwise, and then adds the smallest `room` ids;
+//  - round_aggregate (base.hpp:601-636) adds the smallest id that passes;
+//  - add_help (base.hpp:263-287) handles the edges of a vertex in parallel;
+//    its effects (connected-aggregate set, front set) do not depend on the
+//    edge order, and "connected" is an O(1) flag per local aggregate.
+// All scratch lives in n-sized arrays indexed by vertex (or by local
+// aggregate id), so partition p owns the slots [pb, pe).
 // ===========================================================================
 struct AggDev {
   const int64_t *rowptr;
@@ -151,12 +166,13 @@ struct AggDev {
   int64_t n, nparts;
   int32_t min_size, max_size;
   int aggressive;
-  int32_t *front;       // sorted front, slots [pb, pe)
-  uint8_t *front_mark;  // by vertex
+  int32_t *front;       // front members (unordered), slots [pb, pe)
+  int32_t *front_pos;   // position in `front` by vertex, -1 when absent
   int32_t *conn;        // connected local aggregate ids, slots [pb, pe)
-  int32_t *cand;        // candidates, slots [pb, pe)
+  uint8_t *conn_flag;   // by local aggregate id, slot pb + ag
   int32_t *blocks;      // aggregate k of partition p: [(pb + k) * max, ...)
   int32_t *block_len;   // aggregate k of partition p: slot pb + k
+  int32_t *eval;        // per front position: 4 ints of evaluation results
   int64_t *pcount;      // aggregates per partition
   int64_t *stats;       // 5 counters (atomic adds)
 };
@@ -166,163 +182,241 @@ __device__ __forceinline__ int64_t part_begin(int64_t n, int64_t p, int64_t k) {
   return k * base + (k < rem ? k : rem);
 }
 
-struct AggThread {
+constexpr unsigned kFull = 0xffffffffu;
+
+struct AggWarp {
   const AggDev &D;
   int64_t pb, pe;
-  int64_t front_len = 0, conn_len = 0, cand_len = 0, counter = 0;
+  int lane;
+  // warp-uniform state
+  int64_t front_len = 0, conn_len = 0, counter = 0;
   int64_t st[5] = {0, 0, 0, 0, 0};
 
-  __device__ AggThread(const AggDev &d, int64_t b, int64_t e) : D(d), pb(b), pe(e) {}
-
+  __device__ AggWarp(const AggDev &d, int64_t b, int64_t e) : D(d), pb(b), pe(e) {
+    lane = threadIdx.x & 31;
+  }
   __device__ bool in_range(int64_t v) const { return v >= pb && v < pe; }
-  __device__ bool front_contains(int64_t v) const { return D.front_mark[v]; }
-  __device__ void front_insert(int64_t v) {
-    int32_t *f = D.front + pb;
-    int64_t lo = 0, hi = front_len;
-    while (lo < hi) {
-      const int64_t mid = (lo + hi) / 2;
-      if (f[mid] < v) lo = mid + 1; else hi = mid;
-    }
-    if (lo < front_len && f[lo] == v) return;
-    for (int64_t k = front_len; k > lo; --k) f[k] = f[k - 1];
-    f[lo] = (int32_t)v;
-    ++front_len;
-    D.front_mark[v] = 1;
-  }
-  __device__ void front_erase(int64_t v) {
-    int32_t *f = D.front + pb;
-    int64_t lo = 0, hi = front_len;
-    while (lo < hi) {
-      const int64_t mid = (lo + hi) / 2;
-      if (f[mid] < v) lo = mid + 1; else hi = mid;
-    }
-    if (lo < front_len && f[lo] == v) {
-      for (int64_t k = lo; k + 1 < front_len; ++k) f[k] = f[k + 1];
-      --front_len;
-    }
-    D.front_mark[v] = 0;
-  }
-  __device__ void helpers_clear() {
-    const int32_t *f = D.front + pb;
-    for (int64_t k = 0; k < front_len; ++k) D.front_mark[f[k]] = 0;
-    front_len = 0;
-    conn_len = 0;
-  }
-  __device__ bool is_connected(uint32_t ag) const {
-    const int32_t *c = D.conn + pb;
-    for (int64_t k = 0; k < conn_len; ++k)
-      if ((uint32_t)c[k] == ag) return true;
-    return false;
-  }
   __device__ int32_t &blen(uint32_t ag) const { return D.block_len[pb + ag]; }
   __device__ int32_t *block(uint32_t ag) const {
     return D.blocks + (pb + (int64_t)ag) * D.max_size;
   }
 
-  // AggregateManager::add_help (base.hpp:263-287)
+  // AggregateManager::add_help: v joins aggregate ag; its in-range
+  // neighbours update the connected set and the front.
   __device__ void add_help(int64_t v, uint32_t ag, int64_t &size) {
     ++size;
-    D.agg[v] = ag;
-    block(ag)[blen(ag)++] = (int32_t)v;
-    for (int64_t e = D.rowptr[v]; e < D.rowptr[v + 1]; ++e) {
-      const int64_t t = D.col[e];
-      if (t == v || !in_range(t)) continue;
-      const uint32_t ta = D.agg[t];
-      if (ta < kIsolated && !is_connected(ta)) D.conn[pb + conn_len++] = (int32_t)ta;
-      if (ta == kUnaggregated && !front_contains(t)) front_insert(t);
+    if (lane == 0) {
+      D.agg[v] = ag;
+      block(ag)[blen(ag)++] = (int32_t)v;
+    }
+    __syncwarp();
+    const int64_t eb = D.rowptr[v], ee = D.rowptr[v + 1];
+    for (int64_t e0 = eb; e0 < ee; e0 += 32) {
+      const int64_t e = e0 + lane;
+      bool want_conn = false, want_front = false;
+      uint32_t ta = kUnaggregated;
+      int64_t t = -1;
+      if (e < ee) {
+        t = D.col[e];
+        if (t != v && in_range(t)) {
+          ta = D.agg[t];
+          want_conn = ta < kIsolated && !D.conn_flag[pb + ta];
+          want_front = ta == kUnaggregated && D.front_pos[t] < 0;
+        }
+      }
+      // several lanes may name the same aggregate: the lowest lane records it
+      const unsigned cmask = __ballot_sync(kFull, want_conn);
+      bool leader = false;
+      if (want_conn) {
+        const unsigned same = __match_any_sync(cmask, ta);
+        leader = (__ffs(same) - 1) == lane;
+      }
+      const unsigned lmask = __ballot_sync(kFull, leader);
+      const unsigned below = (1u << lane) - 1u;
+      if (leader) {
+        const int64_t pos = conn_len + __popc(lmask & below);
+        D.conn[pb + pos] = (int32_t)ta;
+        D.conn_flag[pb + ta] = 1;
+      }
+      conn_len += __popc(lmask);
+      const unsigned fmask = __ballot_sync(kFull, want_front);
+      if (want_front) {
+        const int64_t pos = front_len + __popc(fmask & below);
+        D.front[pb + pos] = (int32_t)t;
+        D.front_pos[t] = (int32_t)pos;
+      }
+      front_len += __popc(fmask);
+      __syncwarp();
     }
   }
-  __device__ void add_candidates(uint32_t ag, int64_t &size) {
-    for (int64_t k = 0; k < cand_len; ++k) {
-      const int64_t v = D.cand[pb + k];
-      front_erase(v);
-      add_help(v, ag, size);
+
+  __device__ void front_erase(int64_t v) {
+    if (lane == 0) {
+      const int32_t pos = D.front_pos[v];
+      if (pos >= 0) {
+        const int32_t last = D.front[pb + front_len - 1];
+        D.front[pb + pos] = last;
+        D.front_pos[last] = pos;
+        D.front_pos[v] = -1;
+      }
     }
+    __syncwarp();
+    --front_len;
+  }
+
+  __device__ void helpers_clear() {
+    for (int64_t i = lane; i < front_len; i += 32) D.front_pos[D.front[pb + i]] = -1;
+    for (int64_t i = lane; i < conn_len; i += 32) D.conn_flag[pb + D.conn[pb + i]] = 0;
+    front_len = 0;
+    conn_len = 0;
+    __syncwarp();
+  }
+
+  // per in-range edge of front vertex vtx: calls f(edge, head, head aggregate)
+  template <class F>
+  __device__ __forceinline__ void edges(int64_t vtx, F &&f) const {
+    const int64_t eb = D.rowptr[vtx], ee = D.rowptr[vtx + 1];
+    for (int64_t e = eb; e < ee; ++e) {
+      const int64_t t = D.col[e];
+      if (t == vtx || !in_range(t)) continue;
+      f(e, t, D.agg[t]);
+    }
+  }
+
+  // smallest vertex id > floor among the lane's front positions with mark set
+  __device__ int64_t warp_min_marked(int64_t floor) const {
+    int64_t best = INT64_MAX;
+    for (int64_t i = lane; i < front_len; i += 32) {
+      if (!D.eval[4 * (pb + i) + 3]) continue;
+      const int64_t v = D.front[pb + i];
+      if (v > floor && v < best) best = v;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const int64_t other = __shfl_xor_sync(kFull, best, o);
+      best = other < best ? other : best;
+    }
+    return best;
   }
 
   // grow_aggregate (base.hpp:532-585)
   __device__ void grow(uint32_t ag, int64_t &size) {
     while (size < D.min_size) {
-      int64_t m0 = 0, m2 = 0;
-      double m1 = 0.0;
-      bool has_cons2 = false;
-      cand_len = 0;
-      const int32_t *f = D.front + pb;
-      for (int64_t fi = 0; fi < front_len; ++fi) {
-        const int64_t vtx = f[fi];
-        if (D.iso[vtx]) continue;
-        int64_t con = 0, nbs = 0, cons2 = 0, cons1 = 0;
-        for (int64_t e = D.rowptr[vtx]; e < D.rowptr[vtx + 1]; ++e) {
-          const int64_t t = D.col[e];
-          if (t == vtx || !in_range(t)) continue;
-          const uint32_t ha = D.agg[t];
-          const bool dep = D.dep[e], inf = D.inf[e];
-          con += (ha < kIsolated) && is_connected(ha);
-          nbs += front_contains(t);
-          cons2 += (ha == ag) && (inf && dep);
-          cons1 += (ha == ag) && (!inf && dep);
+      // evaluate every front vertex: eval = (cons2, cons1, con, nbs); adj
+      // (full off-diagonal count) is re-read from the row offsets
+      bool any2 = false;
+      for (int64_t i = lane; i < front_len; i += 32) {
+        const int64_t vtx = D.front[pb + i];
+        int32_t *ev = D.eval + 4 * (pb + i);
+        if (D.iso[vtx]) {
+          ev[0] = ev[1] = 0;
+          ev[3] = 0;
+          continue;
         }
+        int32_t con = 0, nbs = 0, c2 = 0, c1 = 0;
+        edges(vtx, [&](int64_t e, int64_t t, uint32_t ha) {
+          const bool dep = D.dep[e], inf = D.inf[e];
+          con += (ha < kIsolated) && D.conn_flag[pb + ha];
+          nbs += D.front_pos[t] >= 0;
+          c2 += (ha == ag) && (inf && dep);
+          c1 += (ha == ag) && (!inf && dep);
+        });
+        ev[0] = c2;
+        ev[1] = c1;
+        ev[2] = con;
+        ev[3] = nbs;
+        any2 = any2 || c2 > 0;
+      }
+      __syncwarp();
+      const bool mode2 = __any_sync(kFull, any2);
+      // maximum key among eligible vertices
+      int32_t k0 = 0, kn = 0;
+      double kc = 0.0;
+      bool have = false;
+      for (int64_t i = lane; i < front_len; i += 32) {
+        const int64_t vtx = D.front[pb + i];
+        if (D.iso[vtx]) continue;
+        const int32_t *ev = D.eval + 4 * (pb + i);
+        const int32_t c = mode2 ? ev[0] : ev[1];
+        if (c <= 0) continue;
         const int64_t adj = (D.rowptr[vtx + 1] - D.rowptr[vtx]) - 1;
-        const double cond = (double)con / (double)adj;
-        if (cons2 > 0 && !has_cons2) {
-          has_cons2 = true;
-          m0 = cons2;
-          m1 = cond;
-          m2 = nbs;
-          cand_len = 0;
-          D.cand[pb + cand_len++] = (int32_t)vtx;
-        } else {
-          const int64_t t0 = has_cons2 ? cons2 : cons1;
-          if (t0 > 0) {
-            int cmp;
-            if (t0 != m0) cmp = t0 > m0 ? 1 : -1;
-            else if (cond != m1) cmp = cond > m1 ? 1 : (cond < m1 ? -1 : 2);
-            else if (nbs != m2) cmp = nbs > m2 ? 1 : -1;
-            else cmp = 0;
-            if (cmp == 1) {
-              m0 = t0;
-              m1 = cond;
-              m2 = nbs;
-              cand_len = 0;
-              D.cand[pb + cand_len++] = (int32_t)vtx;
-            } else if (cmp == 0) {
-              D.cand[pb + cand_len++] = (int32_t)vtx;
-            }
-          }
+        const double con = (double)ev[2] / (double)adj;
+        if (!have || c > k0 || (c == k0 && (con > kc || (con == kc && ev[3] > kn)))) {
+          k0 = c;
+          kc = con;
+          kn = ev[3];
+          have = true;
         }
       }
-      if (cand_len == 0) break;
+      for (int o = 16; o > 0; o >>= 1) {
+        const int32_t o0 = __shfl_xor_sync(kFull, k0, o);
+        const double oc = __shfl_xor_sync(kFull, kc, o);
+        const int32_t on = __shfl_xor_sync(kFull, kn, o);
+        const bool oh = __shfl_xor_sync(kFull, have, o);
+        if (oh && (!have || o0 > k0 || (o0 == k0 && (oc > kc || (oc == kc && on > kn))))) {
+          k0 = o0;
+          kc = oc;
+          kn = on;
+          have = true;
+        }
+      }
+      if (!have) break;  // no candidates (warp-uniform after the reduction)
+      // mark the vertices whose key equals the maximum (eval[3] reused as mark)
+      for (int64_t i = lane; i < front_len; i += 32) {
+        const int64_t vtx = D.front[pb + i];
+        int32_t *ev = D.eval + 4 * (pb + i);
+        bool m = false;
+        if (!D.iso[vtx]) {
+          const int32_t c = mode2 ? ev[0] : ev[1];
+          if (c > 0) {
+            const int64_t adj = (D.rowptr[vtx + 1] - D.rowptr[vtx]) - 1;
+            const double con = (double)ev[2] / (double)adj;
+            m = c == k0 && con == kc && ev[3] == kn;
+          }
+        }
+        ev[3] = m;
+      }
+      __syncwarp();
+      // add the smallest `room` candidates in ascending order
       const int64_t room = D.max_size - size;
-      if (cand_len > room) cand_len = room;
-      add_candidates(ag, size);
+      int64_t floor = -1;
+      int64_t picked[64];
+      int64_t npick = 0;
+      for (int64_t k = 0; k < room; ++k) {
+        const int64_t v = warp_min_marked(floor);
+        if (v == INT64_MAX) break;
+        picked[npick++] = v;
+        floor = v;
+      }
+      for (int64_t k = 0; k < npick; ++k) {
+        front_erase(picked[k]);
+        add_help(picked[k], ag, size);
+      }
     }
   }
 
   // round_aggregate (base.hpp:601-636)
   __device__ void round(uint32_t ag, int64_t &size) {
     while (size < D.max_size) {
-      cand_len = 0;
-      const int32_t *f = D.front + pb;
-      for (int64_t fi = 0; fi < front_len; ++fi) {
-        const int64_t vtx = f[fi];
-        if (D.iso[vtx]) continue;
-        int64_t cons = 0, unagg = 0, inagg = 0;
-        for (int64_t e = D.rowptr[vtx]; e < D.rowptr[vtx + 1]; ++e) {
-          const int64_t t = D.col[e];
-          if (t == vtx || !in_range(t)) continue;
-          const uint32_t ha = D.agg[t];
+      int64_t best = INT64_MAX;
+      for (int64_t i = lane; i < front_len; i += 32) {
+        const int64_t vtx = D.front[pb + i];
+        if (D.iso[vtx] || vtx >= best) continue;
+        int32_t cons = 0, unagg = 0, inagg = 0;
+        edges(vtx, [&](int64_t e, int64_t, uint32_t ha) {
           cons += (ha == ag) && D.dep[e];
           unagg += ha == kUnaggregated;
           inagg += ha == ag;
-        }
+        });
         if (cons == 0 || unagg >= inagg) continue;
-        D.cand[pb + cand_len++] = (int32_t)vtx;
-        break;
+        best = vtx;
       }
-      if (cand_len == 0) break;
-      const int64_t room = D.max_size - size;
-      if (cand_len > room) cand_len = room;
-      add_candidates(ag, size);
+      for (int o = 16; o > 0; o >>= 1) {
+        const int64_t other = __shfl_xor_sync(kFull, best, o);
+        best = other < best ? other : best;
+      }
+      if (best == INT64_MAX) break;
+      front_erase(best);
+      add_help(best, ag, size);
     }
   }
 
@@ -330,7 +424,8 @@ struct AggThread {
   __device__ void handle(int64_t seed) {
     if (D.agg[seed] != kUnaggregated) return;
     if (D.iso[seed]) {
-      D.agg[seed] = kIsolated;
+      if (lane == 0) D.agg[seed] = kIsolated;
+      __syncwarp();
       ++st[4];
       return;
     }
@@ -340,28 +435,41 @@ struct AggThread {
     grow(ag, size);
     round(ag, size);
     if (size == 1 && D.max_size > 1) {
+      // find_merge_aggregate (base.hpp:487-503): first strong in-range edge
+      // (ascending column) whose head lies in an aggregate with room
       uint32_t target = kUnaggregated;
-      for (int64_t e = D.rowptr[seed]; e < D.rowptr[seed + 1]; ++e) {
-        const int64_t t = D.col[e];
-        if (t == seed || !in_range(t)) continue;
-        if (!(D.dep[e] || D.inf[e])) continue;
-        const uint32_t ta = D.agg[t];
-        if (ta < kIsolated && blen(ta) < D.max_size) {
-          target = ta;
-          break;
+      const int64_t eb = D.rowptr[seed], ee = D.rowptr[seed + 1];
+      for (int64_t e0 = eb; e0 < ee && target == kUnaggregated; e0 += 32) {
+        const int64_t e = e0 + lane;
+        bool ok = false;
+        uint32_t ta = kUnaggregated;
+        if (e < ee) {
+          const int64_t t = D.col[e];
+          if (t != seed && in_range(t) && (D.dep[e] || D.inf[e])) {
+            ta = D.agg[t];
+            ok = ta < kIsolated && blen(ta) < D.max_size;
+          }
         }
+        const unsigned m = __ballot_sync(kFull, ok);
+        if (m) target = __shfl_sync(kFull, ta, __ffs(m) - 1);
       }
       if (target != kUnaggregated) {
-        blen(ag) = 0;
-        D.agg[seed] = target;
-        block(target)[blen(target)++] = (int32_t)seed;
+        if (lane == 0) {
+          blen(ag) = 0;
+          D.agg[seed] = target;
+          block(target)[blen(target)++] = (int32_t)seed;
+        }
+        __syncwarp();
         ++st[3];
         helpers_clear();
         return;
       }
       if (D.aggressive) {
-        blen(ag) = 0;
-        D.agg[seed] = kIsolated;
+        if (lane == 0) {
+          blen(ag) = 0;
+          D.agg[seed] = kIsolated;
+        }
+        __syncwarp();
         ++st[4];
         helpers_clear();
         return;
@@ -375,44 +483,69 @@ struct AggThread {
   }
 };
 
-__global__ void k_aggregate(AggDev D) {
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < D.nparts;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t pb = part_begin(D.n, D.nparts, p), pe = part_begin(D.n, D.nparts, p + 1);
-    for (int64_t v = pb; v < pe; ++v) D.block_len[v] = 0;
-    AggThread T(D, pb, pe);
-    for (int64_t v = pb; v < pe; ++v) T.handle(v);
-    D.pcount[p] = T.counter;
-    T.st[0] = T.counter;
+constexpr int kAggWarpsPerBlock = 4;
+
+__global__ void __launch_bounds__(32 * kAggWarpsPerBlock) k_aggregate(AggDev D) {
+  const int64_t p = (int64_t)blockIdx.x * kAggWarpsPerBlock + (threadIdx.x >> 5);
+  if (p >= D.nparts) return;  // whole warps leave together
+  const int64_t pb = part_begin(D.n, D.nparts, p), pe = part_begin(D.n, D.nparts, p + 1);
+  const int lane = threadIdx.x & 31;
+  for (int64_t v = pb + lane; v < pe; v += 32) D.block_len[v] = 0;
+  __syncwarp();
+  AggWarp W(D, pb, pe);
+  for (int64_t v = pb; v < pe; ++v) W.handle(v);
+  if (lane == 0) {
+    D.pcount[p] = W.counter;
+    W.st[0] = W.counter;
     for (int k = 0; k < 5; ++k)
-      if (T.st[k]) atomicAdd((unsigned long long *)&D.stats[k], (unsigned long long)T.st[k]);
+      if (W.st[k]) atomicAdd((unsigned long long *)&D.stats[k], (unsigned long long)W.st[k]);
   }
 }
 
-// merge (aggregate-map/multithread.hpp:107-143): global ids and the list
-// lengths of every aggregate in global order
-__global__ void k_agg_merge(AggDev D, const int64_t *poff, int64_t *glen) {
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < D.nparts;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t pb = part_begin(D.n, D.nparts, p), pe = part_begin(D.n, D.nparts, p + 1);
-    const uint32_t off = (uint32_t)poff[p];
-    for (int64_t v = pb; v < pe; ++v)
-      if (D.agg[v] < kIsolated) D.agg[v] += off;
-    for (int64_t k = 0; k < D.pcount[p]; ++k) glen[off + k] = D.block_len[pb + k];
+// merge (aggregate-map/multithread.hpp:107-143): aggregate ids become global
+// through the per-partition offsets; the coarse-to-fine lists are laid out
+// partition by partition, aggregates in creation order.
+__device__ __forceinline__ int64_t part_of(int64_t n, int64_t P, int64_t v) {
+  const int64_t base = n / P, rem = n % P;
+  const int64_t big = rem * (base + 1);
+  return v < big ? v / (base + 1) : rem + (v - big) / base;
+}
+
+// partition of global aggregate c: the last p with poff[p] <= c
+__device__ __forceinline__ int64_t part_of_aggregate(const int64_t *poff, int64_t P, int64_t c) {
+  int64_t lo = 0, hi = P;
+  while (hi - lo > 1) {
+    const int64_t mid = (lo + hi) / 2;
+    if (poff[mid] <= c) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+__global__ void k_agg_fix(AggDev D, const int64_t *poff) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < D.n;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t a = D.agg[v];
+    if (a < kIsolated) D.agg[v] = a + (uint32_t)poff[part_of(D.n, D.nparts, v)];
   }
 }
 
-__global__ void k_agg_lists(AggDev D, const int64_t *poff, const int64_t *list_ptr,
+__global__ void k_agg_glen(AggDev D, const int64_t *poff, int64_t nc, int64_t *glen) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nc;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = part_of_aggregate(poff, D.nparts, c);
+    glen[c] = D.block_len[part_begin(D.n, D.nparts, p) + (c - poff[p])];
+  }
+}
+
+__global__ void k_agg_lists(AggDev D, const int64_t *poff, int64_t nc, const int64_t *list_ptr,
                             int32_t *list) {
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < D.nparts;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t pb = part_begin(D.n, D.nparts, p);
-    const int64_t off = poff[p];
-    for (int64_t k = 0; k < D.pcount[p]; ++k) {
-      const int32_t *blk = D.blocks + (pb + k) * D.max_size;
-      int64_t o = list_ptr[off + k];
-      for (int32_t m = 0; m < D.block_len[pb + k]; ++m) list[o++] = blk[m];
-    }
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nc;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = part_of_aggregate(poff, D.nparts, c);
+    const int64_t k = part_begin(D.n, D.nparts, p) + (c - poff[p]);
+    const int32_t *blk = D.blocks + k * D.max_size;
+    int64_t o = list_ptr[c];
+    for (int32_t m = 0; m < D.block_len[k]; ++m) list[o++] = blk[m];
   }
 }
 
@@ -436,26 +569,28 @@ lgx_status aggregate(const Csr &a, const uint8_t *dep, const uint8_t *inf, const
     LGX_CHECK(out.agg.alloc(n));
     agg = out.agg.p;
   }
-  DBuf<int32_t> front, conn, cand, blocks, blen;
-  DBuf<uint8_t> mark;
+  DBuf<int32_t> front, front_pos, conn, blocks, blen, eval;
+  DBuf<uint8_t> conn_flag;
   DBuf<int64_t> pcount, poff, stats, glen;
   LGX_CHECK(front.alloc(n));
+  LGX_CHECK(front_pos.alloc(n));
   LGX_CHECK(conn.alloc(n));
-  LGX_CHECK(cand.alloc(n));
+  LGX_CHECK(conn_flag.alloc(n));
   LGX_CHECK(blocks.alloc(n * max_size));
   LGX_CHECK(blen.alloc(n));
-  LGX_CHECK(mark.alloc(n));
+  LGX_CHECK(eval.alloc(4 * n));
   LGX_CHECK(pcount.alloc(nparts));
   LGX_CHECK(poff.alloc(nparts + 1));
   LGX_CHECK(stats.alloc(5));
   LGX_CUDA(cudaMemsetAsync(agg, 0xFF, sizeof(uint32_t) * std::max<int64_t>(n, 1), s));
-  LGX_CUDA(cudaMemsetAsync(mark.p, 0, std::max<int64_t>(n, 1), s));
+  LGX_CUDA(cudaMemsetAsync(front_pos.p, 0xFF, sizeof(int32_t) * std::max<int64_t>(n, 1), s));
+  LGX_CUDA(cudaMemsetAsync(conn_flag.p, 0, std::max<int64_t>(n, 1), s));
   LGX_CUDA(cudaMemsetAsync(stats.p, 0, sizeof(int64_t) * 5, s));
-  AggDev D{a.rowptr.p, a.col.p, dep,      inf,    iso,      agg,      n,         nparts,
-           min_size,   max_size, aggressive, front.p, mark.p, conn.p, cand.p, blocks.p,
-           blen.p,     pcount.p, stats.p};
+  AggDev D{a.rowptr.p, a.col.p,     dep,     inf,         iso,      agg,    n,
+           nparts,     min_size,    max_size, aggressive, front.p, front_pos.p, conn.p,
+           conn_flag.p, blocks.p,   blen.p,   eval.p,     pcount.p, stats.p};
   if (n > 0) {
-    k_aggregate<<<grid_for(nparts, 64), 64, 0, s>>>(D);
+    k_aggregate<<<grid_for(nparts, kAggWarpsPerBlock), 32 * kAggWarpsPerBlock, 0, s>>>(D);
     LGX_LAUNCH_CHECK();
   }
   LGX_CHECK(inclusive_offsets(nparts, pcount.p, poff.p, s));
@@ -467,7 +602,11 @@ lgx_status aggregate(const Csr &a, const uint8_t *dep, const uint8_t *inf, const
   LGX_CHECK(glen.alloc(nc));
   LGX_CHECK(out.list_ptr.alloc(nc + 1));
   if (n > 0) {
-    k_agg_merge<<<grid_for(nparts, 64), 64, 0, s>>>(D, poff.p, glen.p);
+    k_agg_fix<<<std::min<int64_t>(grid_for(n, 256), 16384), 256, 0, s>>>(D, poff.p);
+    LGX_LAUNCH_CHECK();
+  }
+  if (nc > 0) {
+    k_agg_glen<<<std::min<int64_t>(grid_for(nc, 256), 16384), 256, 0, s>>>(D, poff.p, nc, glen.p);
     LGX_LAUNCH_CHECK();
   }
   LGX_CHECK(inclusive_offsets(nc, glen.p, out.list_ptr.p, s));
@@ -477,7 +616,8 @@ lgx_status aggregate(const Csr &a, const uint8_t *dep, const uint8_t *inf, const
   LGX_CUDA(cudaStreamSynchronize(s));
   LGX_CHECK(out.list.alloc(total));
   if (n > 0 && nc > 0) {
-    k_agg_lists<<<grid_for(nparts, 64), 64, 0, s>>>(D, poff.p, out.list_ptr.p, out.list.p);
+    k_agg_lists<<<std::min<int64_t>(grid_for(nc, 256), 16384), 256, 0, s>>>(
+      D, poff.p, nc, out.list_ptr.p, out.list.p);
     LGX_LAUNCH_CHECK();
   }
   LGX_CUDA(cudaStreamSynchronize(s));
@@ -800,8 +940,10 @@ struct lgx_amg {
 
 namespace lgx {
 
-int64_t amg_partitions(int64_t n, const lgx_amg_params &p) {
-  int64_t parts = p.partition_size > 0 ? n / p.partition_size : 1;
+int64_t amg_partitions(int64_t n, int64_t level, const lgx_amg_params &p) {
+  double ps = (double)p.partition_size;
+  for (int64_t l = 0; l < level; ++l) ps *= p.partition_growth;
+  int64_t parts = ps >= 1.0 ? (int64_t)((double)n / ps) : n;
   if (parts < 1) parts = 1;
   if (parts > p.max_partitions) parts = p.max_partitions;
   return parts;
@@ -841,7 +983,7 @@ static lgx_status amg_build(const lgx_matrix *m, const lgx_amg_params &p,
                        iso.p, s));
     timer.mark(s, "strength", level);
     LGX_CHECK(aggregate(a, dep.p, inf.p, iso.p, p.min_aggregate_size, p.max_aggregate_size,
-                        amg_partitions(a.n, p), aggressive, s, fine.agg));
+                        amg_partitions(a.n, level, p), aggressive, s, fine.agg));
     timer.mark(s, "aggregate", level);
     if (level < 32)
       for (int k = 0; k < 5; ++k) h.stats[level][k] = fine.agg.stats[k];
@@ -1053,6 +1195,7 @@ void lgx_amg_default_params(lgx_amg_params *p) {
   p->min_aggregate_size = 6;
   p->max_aggregate_size = 9;
   p->partition_size = 4096;
+  p->partition_growth = 4.0;
   p->max_partitions = 1 << 30;
   p->strong_threshold = 1.0 / 3.0;
   p->aggressive_threshold = 1.0 / 3.0;
@@ -1079,6 +1222,8 @@ lgx_status lgx_amg_setup(const lgx_matrix *a, const lgx_amg_params *p,
       p->min_aggregate_size > p->max_aggregate_size)
     return fail(LGX_ERR_INVALID, "aggregate sizes must satisfy 1 <= min <= max <= 64");
   if (!(p->relax != 0.0)) return fail(LGX_ERR_INVALID, "relax must be non-zero");
+  if (!(p->partition_growth >= 1.0))
+    return fail(LGX_ERR_INVALID, "partition_growth must be at least 1");
   auto *h = new lgx_amg();
   lgx_status st = amg_build(a, *p, finest_colouring, stream, *h);
   if (st != LGX_OK) {

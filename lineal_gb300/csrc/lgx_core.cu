@@ -109,7 +109,7 @@ lgx_status csr_from_device(int64_t n, int64_t nnz, const int64_t *rowptr, const 
   out.nnz = nnz;
   out.symmetric = symmetric;
   out.storage = storage;
-  LGX_CHECK(out.rowptr.alloc(n + 1));
+  LGX_CHECK(out.rowptr.alloc(n + 3));  // +2: staged row-offset spans
   LGX_CHECK(csr_alloc_arrays(out, nnz, storage));
   LGX_CUDA(cudaMemcpyAsync(out.rowptr.p, rowptr, sizeof(int64_t) * (n + 1),
                            cudaMemcpyDeviceToDevice, s));
@@ -399,7 +399,7 @@ static lgx_status gen_structured(const int64_t dims[3], const double *d_k, int n
     return fail(LGX_ERR_INVALID, "invalid grid dimensions");
   DBuf<int64_t> rowlen, rowptr;
   LGX_CHECK(rowlen.alloc(n));
-  LGX_CHECK(rowptr.alloc(n + 1));
+  LGX_CHECK(rowptr.alloc(n + 3));  // +2: staged row-offset spans
   const unsigned g = (unsigned)std::min<int64_t>(grid_for(n, 256), 65535);
   k_gen_count<<<g, 256, 0, s>>>(dims[0], dims[1], dims[2], npts, rowlen.p);
   LGX_LAUNCH_CHECK();

@@ -32,15 +32,17 @@ struct TileCap {
   static constexpr int value = sizeof(VT) == 8 ? 8192 : 12288;
 };
 
-// per stage: columns (CAP + 8) * 4 bytes, values (CAP + 8) * sizeof(VT) bytes
-// (an aligned span exceeds the segment by at most 6 elements); two barriers
+// per stage: row offsets (kTileRows + 4) * 8 bytes, columns (CAP + 8) * 4
+// bytes, values (CAP + 8) * sizeof(VT) bytes (an aligned span exceeds its
+// segment by at most 6 elements); then per stage a bounds record and a barrier
 template <typename VT>
-constexpr size_t stage_bytes() {
-  return (size_t)(TileCap<VT>::value + 8) * 4 + (size_t)(TileCap<VT>::value + 8) * sizeof(VT);
+__host__ __device__ constexpr size_t stage_bytes() {
+  return (size_t)(kTileRows + 4) * 8 + (size_t)(TileCap<VT>::value + 8) * 4 +
+         (size_t)(TileCap<VT>::value + 8) * sizeof(VT);
 }
 template <typename VT>
-constexpr size_t tile_smem_bytes() {
-  return 2 * stage_bytes<VT>() + 64;
+__host__ __device__ constexpr size_t tile_smem_bytes() {
+  return 2 * stage_bytes<VT>() + 2 * 32 + 64;
 }
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) {
@@ -98,21 +100,32 @@ __device__ __forceinline__ void fence_mbar_init() {
 
 template <typename VT>
 struct Stage {
+  int64_t *rp;   // kTileRows + 4 row offsets, 16-byte aligned
   int32_t *col;  // CAP + 8 entries, 16-byte aligned
   VT *val;       // CAP + 8 entries, 16-byte aligned
 };
 
-// Issue the two bulk copies of tile rows [r0, r1) (segment [e0, e1)).  Returns
-// the element offsets of e0 inside the staged spans.
+// What thread 0 knows about a tile when it issues its copies; read by the
+// other threads after the barrier that follows the issue.
+struct TileRec {
+  int64_t r0, r1, e0, e1;
+};
+
+// Issue the bulk copies of tile rows [r0, r1): row offsets r0..r1 and the
+// segment [e0, e1) of columns and values, each as a 16-byte-aligned span.
 template <typename VT>
-__device__ __forceinline__ void issue_tile(const int32_t *col, const VT *val, int64_t e0,
-                                           int64_t e1, Stage<VT> st, uint64_t *bar) {
+__device__ __forceinline__ void issue_tile(const int64_t *rowptr, const int32_t *col,
+                                           const VT *val, const TileRec &t, Stage<VT> st,
+                                           uint64_t *bar) {
   constexpr int64_t CA = 16 / 4, VA = 16 / (int64_t)sizeof(VT);
-  const int64_t c0 = e0 & ~(CA - 1), c1 = (e1 + CA - 1) & ~(CA - 1);
-  const int64_t v0 = e0 & ~(VA - 1), v1 = (e1 + VA - 1) & ~(VA - 1);
-  const unsigned cb = (unsigned)((c1 - c0) * 4), vb = (unsigned)((v1 - v0) * sizeof(VT));
+  const int64_t p0 = t.r0 & ~1ll, p1 = (t.r1 + 2) & ~1ll;
+  const int64_t c0 = t.e0 & ~(CA - 1), c1 = (t.e1 + CA - 1) & ~(CA - 1);
+  const int64_t v0 = t.e0 & ~(VA - 1), v1 = (t.e1 + VA - 1) & ~(VA - 1);
+  const unsigned pb = (unsigned)((p1 - p0) * 8), cb = (unsigned)((c1 - c0) * 4),
+                 vb = (unsigned)((v1 - v0) * sizeof(VT));
   fence_proxy_async();
-  mbar_expect_tx(bar, cb + vb);
+  mbar_expect_tx(bar, pb + cb + vb);
+  bulk_g2s(st.rp, rowptr + p0, pb, bar);
   if (cb) bulk_g2s(st.col, col + c0, cb, bar);
   if (vb) bulk_g2s(st.val, val + v0, vb, bar);
 }
@@ -129,56 +142,62 @@ __global__ void __launch_bounds__(kTileRows)
   constexpr int CAP = TileCap<VT>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   static_assert((CAP + 8) * 4 % 16 == 0 && (CAP + 8) * sizeof(VT) % 16 == 0);
-  Stage<VT> st[2];
-  {
-    unsigned char *p = smem_raw;
-    for (int s = 0; s < 2; ++s) {
-      st[s].col = reinterpret_cast<int32_t *>(p);
-      p += (size_t)(CAP + 8) * 4;
-      st[s].val = reinterpret_cast<VT *>(p);
-      p += (size_t)(CAP + 8) * sizeof(VT);
-    }
-  }
-  uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw + 2 * stage_bytes<VT>());
+  // stage s starts at smem_raw + s * stage_bytes (computed, not indexed, so
+  // the pointers stay in registers)
+  auto stage = [&](int s) {
+    unsigned char *p = smem_raw + (size_t)s * stage_bytes<VT>();
+    Stage<VT> r;
+    r.rp = reinterpret_cast<int64_t *>(p);
+    r.col = reinterpret_cast<int32_t *>(p + (size_t)(kTileRows + 4) * 8);
+    r.val = reinterpret_cast<VT *>(p + (size_t)(kTileRows + 4) * 8 + (size_t)(CAP + 8) * 4);
+    return r;
+  };
+  TileRec *rec = reinterpret_cast<TileRec *>(smem_raw + 2 * stage_bytes<VT>());
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw + 2 * stage_bytes<VT>() + 2 * 32);
   const int64_t nrows = re - rb;
   const int64_t ntiles = (nrows + rows_per_tile - 1) / rows_per_tile;
+  const int64_t G = gridDim.x;
+
+  auto bounds = [&](int64_t t) {
+    TileRec r;
+    r.r0 = rb + t * rows_per_tile;
+    r.r1 = min(r.r0 + rows_per_tile, re);
+    r.e0 = rowptr[r.r0];
+    r.e1 = rowptr[r.r1];
+    return r;
+  };
+
+  // thread 0 = producer: issues tile t+G while tile t is computed, and loads
+  // the bounds of tile t+2G one iteration ahead of their use
+  TileRec ahead{};
+  int64_t t = blockIdx.x;
   if (threadIdx.x == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
     fence_mbar_init();
+    if (t < ntiles) {
+      rec[0] = bounds(t);
+      if (rec[0].e1 - rec[0].e0 <= CAP)
+        issue_tile<VT>(rowptr, col, val, rec[0], stage(0), &bar[0]);
+    }
+    if (t + G < ntiles) ahead = bounds(t + G);
   }
   __syncthreads();
-
-  auto tile_bounds = [&](int64_t t, int64_t &r0, int64_t &r1, int64_t &e0, int64_t &e1) {
-    r0 = rb + t * rows_per_tile;
-    r1 = min(r0 + rows_per_tile, re);
-    e0 = rowptr[r0];
-    e1 = rowptr[r1];
-  };
 
   unsigned phase[2] = {0u, 0u};
   double contrib = 0.0;
   bool ok = true;
-  int64_t t = blockIdx.x;
-  // prologue: first tile into stage 0
-  if (t < ntiles && threadIdx.x == 0) {
-    int64_t r0, r1, e0, e1;
-    tile_bounds(t, r0, r1, e0, e1);
-    if (e1 - e0 <= CAP) issue_tile<VT>(col, val, e0, e1, st[0], &bar[0]);
-  }
-  for (int64_t j = 0; t < ntiles; ++j, t += gridDim.x) {
+  for (int64_t j = 0; t < ntiles; ++j, t += G) {
     const int s = (int)(j & 1);
-    // prefetch the next tile into the other stage (freed by the sync below)
-    const int64_t tn = t + gridDim.x;
-    if (tn < ntiles && threadIdx.x == 0) {
-      int64_t r0, r1, e0, e1;
-      tile_bounds(tn, r0, r1, e0, e1);
-      if (e1 - e0 <= CAP) issue_tile<VT>(col, val, e0, e1, st[s ^ 1], &bar[s ^ 1]);
+    if (threadIdx.x == 0 && t + G < ntiles) {
+      (s ? rec[0] : rec[1]) = ahead;
+      if (ahead.e1 - ahead.e0 <= CAP)
+        issue_tile<VT>(rowptr, col, val, ahead, stage(s ^ 1), &bar[s ^ 1]);
+      if (t + 2 * G < ntiles) ahead = bounds(t + 2 * G);
     }
-    int64_t r0, r1, e0, e1;
-    tile_bounds(t, r0, r1, e0, e1);
-    const int64_t row = r0 + threadIdx.x;
-    if (e1 - e0 <= CAP) {
+    const TileRec cur = s ? rec[1] : rec[0];
+    const int64_t row = cur.r0 + threadIdx.x;
+    if (cur.e1 - cur.e0 <= CAP) {
       const bool waited = mbar_wait_bounded(&bar[s], phase[s]);
       // uniform decision: every thread leaves the loop if any wait gave up
       if (__syncthreads_or(!waited)) {
@@ -187,12 +206,13 @@ __global__ void __launch_bounds__(kTileRows)
       }
       phase[s] ^= 1u;
       constexpr int64_t CA = 4, VA = 16 / (int64_t)sizeof(VT);
-      const int64_t c0 = e0 & ~(CA - 1), v0 = e0 & ~(VA - 1);
-      if (row < r1) {
-        const int64_t b = rowptr[row], e = rowptr[row + 1];
-        contrib += op.row(row, st[s].col + (b - c0), st[s].val + (b - v0), (int)(e - b));
+      const int64_t p0 = cur.r0 & ~1ll, c0 = cur.e0 & ~(CA - 1), v0 = cur.e0 & ~(VA - 1);
+      if (row < cur.r1) {
+        const Stage<VT> sg = stage(s);
+        const int64_t b = sg.rp[row - p0], e = sg.rp[row + 1 - p0];
+        contrib += op.row(row, sg.col + (b - c0), sg.val + (b - v0), (int)(e - b));
       }
-    } else if (row < r1) {
+    } else if (row < cur.r1) {
       const int64_t b = rowptr[row], e = rowptr[row + 1];
       contrib += op.row(row, col + b, val + b, (int)(e - b));
     }
@@ -266,23 +286,22 @@ inline int64_t rows_partials(int64_t nrows, int64_t max_row) {
 }
 
 // ---- row operations ---------------------------------------------------------
-// sum_k fma(a_k, x[c_k], init) in storage order; the column and x loads are
-// issued eight at a time ahead of the dependent FMA chain.
+// sum_k fma(a_k, x[c_k], init) in storage order.  The column and x loads of
+// up to 32 entries are issued together ahead of the dependent FMA chain, so a
+// 27-point row costs one round of gather latency.
 template <typename VT, typename XT>
-__device__ __forceinline__ XT row_dot8(const int32_t *c, const VT *v, int len,
-                                       const XT *__restrict__ x, XT sum) {
-  int k = 0;
-  for (; k + 8 <= len; k += 8) {
-    int32_t cc[8];
-    XT xv[8];
+__device__ __forceinline__ XT row_dot(const int32_t *c, const VT *v, int len,
+                                      const XT *__restrict__ x, XT sum) {
+  for (int k = 0; k < len; k += 32) {
+    const int m = len - k < 32 ? len - k : 32;
+    XT xv[32];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) cc[u] = c[k + u];
+    for (int u = 0; u < 32; ++u)
+      if (u < m) xv[u] = __ldg(x + c[k + u]);
 #pragma unroll
-    for (int u = 0; u < 8; ++u) xv[u] = __ldg(x + cc[u]);
-#pragma unroll
-    for (int u = 0; u < 8; ++u) sum = fma((XT)v[k + u], xv[u], sum);
+    for (int u = 0; u < 32; ++u)
+      if (u < m) sum = fma((XT)v[k + u], xv[u], sum);
   }
-  for (; k < len; ++k) sum = fma((XT)v[k], __ldg(x + c[k]), sum);
   return sum;
 }
 

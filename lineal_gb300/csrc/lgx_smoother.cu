@@ -269,7 +269,7 @@ lgx_status colouring_build(const Csr &a, const int32_t *d_colour, int32_t ncolou
   p.symmetric = a.symmetric;
   p.storage = a.storage;
   p.max_row = a.max_row;
-  LGX_CHECK(p.rowptr.alloc(n + 1));
+  LGX_CHECK(p.rowptr.alloc(n + 3));  // +2: staged row-offset spans
   LGX_CHECK(csr_alloc_arrays(p, a.nnz, a.storage));
   k_perm_rowlen<<<g, 256, 0, s>>>(n, a.rowptr.p, out.perm.p, flag.p);
   LGX_LAUNCH_CHECK();
@@ -311,33 +311,23 @@ struct SorOp {
   __device__ __forceinline__ double row(int64_t i, const int32_t *c, const VT *v, int len) const {
     XT accum = b[i], diag = XT(0);
     const XT xi = x[i];
-    int k = 0;
-    for (; k + 8 <= len; k += 8) {
-      int32_t cc[8];
-      XT xv[8];
+    for (int k = 0; k < len; k += 32) {
+      const int m = len - k < 32 ? len - k : 32;
+      XT xv[32];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) cc[u] = c[k + u];
+      for (int u = 0; u < 32; ++u)
+        if (u < m) xv[u] = x[c[k + u]];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) xv[u] = x[cc[u]];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const XT a = (XT)v[k + u];
-        if (cc[u] == i) {
-          diag = a;
-          if (ultra) accum = fma(-a, xi, accum);
-        } else {
-          accum = fma(-a, xv[u], accum);
+      for (int u = 0; u < 32; ++u) {
+        if (u < m) {
+          const XT a = (XT)v[k + u];
+          if (c[k + u] == i) {
+            diag = a;
+            if (ultra) accum = fma(-a, xi, accum);
+          } else {
+            accum = fma(-a, xv[u], accum);
+          }
         }
-      }
-    }
-    for (; k < len; ++k) {
-      const int32_t j = c[k];
-      const XT a = (XT)v[k];
-      if (j == i) {
-        diag = a;
-        if (ultra) accum = fma(-a, xi, accum);
-      } else {
-        accum = fma(-a, x[j], accum);
       }
     }
     if (ultra) {

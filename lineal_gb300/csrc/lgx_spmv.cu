@@ -27,7 +27,7 @@ struct SpmvOp {
   double *partials = nullptr;
   unsigned *counter = nullptr;
   __device__ __forceinline__ double row(int64_t i, const int32_t *c, const VT *v, int len) const {
-    y[i] = row_dot8<VT, XT>(c, v, len, x, XT(0));
+    y[i] = row_dot<VT, XT>(c, v, len, x, XT(0));
     return 0.0;
   }
   __device__ __forceinline__ void finish(double) const {}
@@ -43,7 +43,7 @@ struct ResidualOp {
   double *partials;
   unsigned *counter;
   __device__ __forceinline__ double row(int64_t i, const int32_t *c, const VT *v, int len) const {
-    const XT ax = row_dot8<VT, XT>(c, v, len, x, XT(0));
+    const XT ax = row_dot<VT, XT>(c, v, len, x, XT(0));
     const XT rv = b[i] - ax;
     r[i] = rv;
     return NORM ? (double)rv * (double)rv : 0.0;

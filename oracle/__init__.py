@@ -73,6 +73,7 @@ class _AmgParams(C.Structure):
         ("min_aggregate_size", C.c_int32),
         ("max_aggregate_size", C.c_int32),
         ("partition_size", C.c_int64),
+        ("partition_growth", C.c_double),
         ("max_partitions", C.c_int64),
         ("strong_threshold", C.c_double),
         ("aggressive_threshold", C.c_double),
@@ -165,7 +166,7 @@ def _setup_signatures(L):
     L.lo_cholesky_solve.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]
     L.lo_amg_default_params.argtypes = [P(_AmgParams)]
     L.lo_amg_partitions.restype = C.c_int64
-    L.lo_amg_partitions.argtypes = [C.c_int64, P(_AmgParams)]
+    L.lo_amg_partitions.argtypes = [C.c_int64, C.c_int64, P(_AmgParams)]
     L.lo_amg_strength.argtypes = [P(_Csr), C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]
     L.lo_amg_aggregate.restype = C.c_int64
     L.lo_amg_aggregate.argtypes = [P(_Csr), C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
@@ -440,9 +441,9 @@ def amg_params(**kw) -> _AmgParams:
     return p
 
 
-def amg_partitions(n: int, **kw) -> int:
+def amg_partitions(n: int, level: int = 0, **kw) -> int:
     p = amg_params(**kw)
-    return int(lib().lo_amg_partitions(n, C.byref(p)))
+    return int(lib().lo_amg_partitions(n, level, C.byref(p)))
 
 
 def amg_strength(a: Csr, theta: float = 1.0 / 3.0):

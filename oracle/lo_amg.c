@@ -13,6 +13,7 @@ void lo_amg_default_params(lo_amg_params *p) {
   p->min_aggregate_size = 6;
   p->max_aggregate_size = 9;
   p->partition_size = 4096;
+  p->partition_growth = 4.0;
   p->max_partitions = 1 << 30;
   p->strong_threshold = 1.0 / 3.0;
   p->aggressive_threshold = 1.0 / 3.0;
@@ -538,8 +539,10 @@ static void level_vectors(lo_amg_level *l, const lo_amg_params *p, int64_t idx) 
   }
 }
 
-int64_t lo_amg_partitions(int64_t n, const lo_amg_params *p) {
-  int64_t parts = p->partition_size > 0 ? n / p->partition_size : 1;
+int64_t lo_amg_partitions(int64_t n, int64_t level, const lo_amg_params *p) {
+  double ps = (double)p->partition_size;
+  for (int64_t l = 0; l < level; ++l) ps *= p->partition_growth;
+  int64_t parts = ps >= 1.0 ? (int64_t)((double)n / ps) : n;
   if (parts < 1) parts = 1;
   if (parts > p->max_partitions) parts = p->max_partitions;
   return parts;
@@ -564,7 +567,8 @@ int lo_amg_setup(const lo_csr *a0, const lo_amg_params *p, lo_amg *h) {
     int64_t stats[5];
     const int64_t nc =
       lo_amg_aggregate(a, dep, inf, iso, p->min_aggregate_size, p->max_aggregate_size,
-                       lo_amg_partitions(a->n, p), aggressive, fine->agg, &fine->list_ptr,
+                       lo_amg_partitions(a->n, level, p), aggressive, fine->agg,
+                       &fine->list_ptr,
                        &fine->list, stats);
     free(dep);
     free(inf);
