@@ -377,6 +377,7 @@ struct AggregationParams {
   int32_t max_aggregate_size = 9;
   int64_t partition_size = 4096;
   double partition_growth = 4.0;
+  int64_t min_partitions = 16;
 };
 
 struct DuneDependencyCriterion {
@@ -411,6 +412,7 @@ struct MultiGridSolver : SharedStationaryIterativeSolverBase {
       p.max_aggregate_size = s.aggregation.max_aggregate_size;
       p.partition_size = s.aggregation.partition_size;
       p.partition_growth = s.aggregation.partition_growth;
+      p.min_partitions = s.aggregation.min_partitions;
       p.strong_threshold = s.criterion.strong_threshold;
       p.aggressive_threshold = s.criterion.aggressive_strong_threshold;
       p.relax = s.relax;

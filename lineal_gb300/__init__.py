@@ -58,6 +58,7 @@ class _AmgParams(C.Structure):
         ("max_aggregate_size", C.c_int32),
         ("partition_size", C.c_int64),
         ("partition_growth", C.c_double),
+        ("min_partitions", C.c_int64),
         ("max_partitions", C.c_int64),
         ("strong_threshold", C.c_double),
         ("aggressive_threshold", C.c_double),
@@ -472,6 +473,7 @@ class HierarchyWright:
     max_aggregate_size: int = 9
     partition_size: int = 4096
     partition_growth: float = 4.0
+    min_partitions: int = 16
     max_partitions: int = 1 << 30
     coarse_f32: bool = False
     cycle_f32: bool = False

@@ -272,14 +272,35 @@ struct AggWarp {
     __syncwarp();
   }
 
-  // per in-range edge of front vertex vtx: calls f(edge, head, head aggregate)
+  // Per in-range edge of front vertex vtx calls f(edge, head, head aggregate,
+  // head in front, head aggregate connected).  Edges are loaded eight at a
+  // time with independent loads so the dependent chain col -> agg ->
+  // connected-flag costs one round of latency per batch.
   template <class F>
   __device__ __forceinline__ void edges(int64_t vtx, F &&f) const {
     const int64_t eb = D.rowptr[vtx], ee = D.rowptr[vtx + 1];
-    for (int64_t e = eb; e < ee; ++e) {
-      const int64_t t = D.col[e];
-      if (t == vtx || !in_range(t)) continue;
-      f(e, t, D.agg[t]);
+    for (int64_t e0 = eb; e0 < ee; e0 += 8) {
+      int64_t t[8];
+      bool ok[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int64_t e = e0 + u;
+        t[u] = e < ee ? (int64_t)D.col[e] : vtx;
+        ok[u] = e < ee && t[u] != vtx && in_range(t[u]);
+      }
+      uint32_t ha[8];
+      bool fr[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        ha[u] = ok[u] ? D.agg[t[u]] : kUnaggregated;
+        fr[u] = ok[u] && D.front_pos[t[u]] >= 0;
+      }
+      bool cf[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) cf[u] = ok[u] && ha[u] < kIsolated && D.conn_flag[pb + ha[u]];
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (ok[u]) f(e0 + u, t[u], ha[u], fr[u], cf[u]);
     }
   }
 
@@ -313,10 +334,10 @@ struct AggWarp {
           continue;
         }
         int32_t con = 0, nbs = 0, c2 = 0, c1 = 0;
-        edges(vtx, [&](int64_t e, int64_t t, uint32_t ha) {
+        edges(vtx, [&](int64_t e, int64_t, uint32_t ha, bool in_front, bool connected) {
           const bool dep = D.dep[e], inf = D.inf[e];
-          con += (ha < kIsolated) && D.conn_flag[pb + ha];
-          nbs += D.front_pos[t] >= 0;
+          con += connected;
+          nbs += in_front;
           c2 += (ha == ag) && (inf && dep);
           c1 += (ha == ag) && (!inf && dep);
         });
@@ -402,7 +423,7 @@ struct AggWarp {
         const int64_t vtx = D.front[pb + i];
         if (D.iso[vtx] || vtx >= best) continue;
         int32_t cons = 0, unagg = 0, inagg = 0;
-        edges(vtx, [&](int64_t e, int64_t, uint32_t ha) {
+        edges(vtx, [&](int64_t e, int64_t, uint32_t ha, bool, bool) {
           cons += (ha == ag) && D.dep[e];
           unagg += ha == kUnaggregated;
           inagg += ha == ag;
@@ -944,6 +965,8 @@ int64_t amg_partitions(int64_t n, int64_t level, const lgx_amg_params &p) {
   double ps = (double)p.partition_size;
   for (int64_t l = 0; l < level; ++l) ps *= p.partition_growth;
   int64_t parts = ps >= 1.0 ? (int64_t)((double)n / ps) : n;
+  const int64_t floor_parts = p.min_partitions < n / 1024 ? p.min_partitions : n / 1024;
+  if (parts < floor_parts) parts = floor_parts;
   if (parts < 1) parts = 1;
   if (parts > p.max_partitions) parts = p.max_partitions;
   return parts;
@@ -1196,6 +1219,7 @@ void lgx_amg_default_params(lgx_amg_params *p) {
   p->max_aggregate_size = 9;
   p->partition_size = 4096;
   p->partition_growth = 4.0;
+  p->min_partitions = 16;
   p->max_partitions = 1 << 30;
   p->strong_threshold = 1.0 / 3.0;
   p->aggressive_threshold = 1.0 / 3.0;

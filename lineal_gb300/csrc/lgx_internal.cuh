@@ -28,6 +28,9 @@ lgx_status cuda_fail(cudaError_t e, const char *what);
     if (lgx_s_ != LGX_OK) return lgx_s_;         \
   } while (0)
 void count_launch();
+// adds the kernel nodes of a replayed graph to the launch count
+void count_launches(uint64_t k);
+uint64_t launch_count();
 // Every kernel launch site is followed by this check, which also counts the
 // launch (lgx_kernel_launches).
 #define LGX_LAUNCH_CHECK()     \

@@ -347,6 +347,7 @@ struct lgx_krylov {
   cudaStream_t user_stream = nullptr;
   cudaStream_t capture_stream = nullptr;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  uint64_t graph_kernels[2] = {0, 0};  // kernels recorded in each graph
   ~lgx_krylov() {
     for (auto &g : graph)
       if (g) cudaGraphExecDestroy(g);
@@ -493,8 +494,12 @@ static lgx_status capture_iteration(lgx_krylov &K, int rere) {
   K.it = rere ? K.p.rere_period : 1;
   K.S.s = K.capture_stream;
   cudaGraph_t g = nullptr;
+  const uint64_t before = launch_count();
   cudaError_t e = cudaStreamBeginCapture(K.capture_stream, cudaStreamCaptureModeThreadLocal);
   lgx_status st = e == cudaSuccess ? iterate_body(K) : cuda_fail(e, "cudaStreamBeginCapture");
+  // recording does not launch: move the count to the replays
+  K.graph_kernels[rere] = launch_count() - before;
+  count_launches(0 - K.graph_kernels[rere]);
   cudaError_t e2 = cudaStreamEndCapture(K.capture_stream, &g);
   K.S.s = K.user_stream;
   K.it = saved_it;
@@ -516,6 +521,7 @@ static lgx_status krylov_iterate(lgx_krylov &K) {
     // attributes); later iterations replay captured graphs
     if (!K.graph[rere]) LGX_CHECK(capture_iteration(K, rere ? 1 : 0));
     LGX_CUDA(cudaGraphLaunch(K.graph[rere], K.user_stream));
+    count_launches(K.graph_kernels[rere]);
   } else {
     LGX_CHECK(iterate_body(K));
   }

@@ -2,14 +2,16 @@
 //
 // A CSR tile of R consecutive rows owns one contiguous segment of the column
 // and value arrays.  Each CTA walks its tiles (t = blockIdx.x, +gridDim.x, ...)
-// with two shared-memory stages: while the threads compute tile j from stage
-// j&1 (one thread per row, the row's products in storage order), thread 0 has
-// already issued the bulk copies (cp.async.bulk global->shared, completion
-// counted on an mbarrier) of tile j+1 into the other stage.  The copies are
-// whole 16-byte-aligned spans, so the segment's first entry sits at a small
-// offset inside the stage.  Column and value buffers of every CSR in this
-// library carry kCsrPad trailing elements, so the aligned span never leaves
-// the allocation.
+// and stages each tile's row offsets, columns and values into shared memory
+// with bulk copies (cp.async.bulk global->shared, completion counted on an
+// mbarrier); then one thread per row computes the row from shared memory,
+// the row's products in storage order.  Copy and compute overlap either
+// inside a CTA (two stages: tile j+1 is in flight while tile j is computed)
+// or between the two CTAs resident on an SM (one stage each); RowCfg lists
+// the configurations.  The copies are whole 16-byte-aligned spans, so the
+// segment's first entry sits at a small offset inside the stage.  Column and
+// value buffers of every CSR in this library carry kCsrPad trailing
+// elements, so the aligned span never leaves the allocation.
 //
 // Every wait on an mbarrier is bounded (about one second of SM clock); on
 // timeout the kernel records an error in the library's device error flag,
@@ -26,23 +28,37 @@ namespace lgx {
 
 constexpr int kTileRows = 256;     // threads per CTA, maximum rows per tile
 
+// Engine configurations (the tuning space of the row kernels):
+//   kind 0: two stages of CAP entries, one CTA per SM (prefetch overlap
+//           inside the CTA);
+//   kind 1: one stage, two CTAs per SM (the other CTA overlaps the copy);
+//   kind 2: two smaller stages, two CTAs per SM.
+template <typename VT, int KIND>
+struct RowCfg {
+  static constexpr int stages = KIND == 1 ? 1 : 2;
+  static constexpr int ctas_per_sm = KIND == 0 ? 1 : 2;
+  static constexpr int cap = KIND == 2 ? (sizeof(VT) == 8 ? 4096 : 6144)
+                                       : (sizeof(VT) == 8 ? 8192 : 12288);
+  // entries gathered per round of a row (register budget: 255 registers per
+  // thread at one CTA per SM, 128 at two)
+  static constexpr int gather = KIND == 0 ? 32 : 16;
+};
 template <typename VT>
 struct TileCap {
-  // entries per stage: 2 stages x (4 + sizeof(VT)) bytes x CAP <= 208 KB
-  static constexpr int value = sizeof(VT) == 8 ? 8192 : 12288;
+  static constexpr int value = RowCfg<VT, 0>::cap;
 };
 
 // per stage: row offsets (kTileRows + 4) * 8 bytes, columns (CAP + 8) * 4
 // bytes, values (CAP + 8) * sizeof(VT) bytes (an aligned span exceeds its
 // segment by at most 6 elements); then per stage a bounds record and a barrier
-template <typename VT>
+template <typename VT, int KIND>
 __host__ __device__ constexpr size_t stage_bytes() {
-  return (size_t)(kTileRows + 4) * 8 + (size_t)(TileCap<VT>::value + 8) * 4 +
-         (size_t)(TileCap<VT>::value + 8) * sizeof(VT);
+  return (size_t)(kTileRows + 4) * 8 + (size_t)(RowCfg<VT, KIND>::cap + 8) * 4 +
+         (size_t)(RowCfg<VT, KIND>::cap + 8) * sizeof(VT);
 }
-template <typename VT>
+template <typename VT, int KIND>
 __host__ __device__ constexpr size_t tile_smem_bytes() {
-  return 2 * stage_bytes<VT>() + 2 * 32 + 64;
+  return RowCfg<VT, KIND>::stages * stage_bytes<VT, KIND>() + 2 * 32 + 64;
 }
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) {
@@ -131,29 +147,32 @@ __device__ __forceinline__ void issue_tile(const int64_t *rowptr, const int32_t 
 }
 
 // Op interface:
-//   __device__ double row(int64_t row, const int32_t *c, const VT *v, int len) const;
-//     (returns the row's contribution to an optional sum)
+//   template <int W> __device__ double row(int64_t row, const int32_t *c, const VT *v,
+//                                          int len) const;
+//     (returns the row's contribution to an optional sum; W = entries whose
+//     gathers are issued together)
 //   static constexpr bool kReduce;  __device__ void finish(double total) const;
 //   double *partials; unsigned *counter;  (when kReduce)
-template <typename VT, class Op>
-__global__ void __launch_bounds__(kTileRows)
+template <typename VT, class Op, int KIND>
+__global__ void __launch_bounds__(kTileRows, RowCfg<VT, KIND>::ctas_per_sm)
   k_rows(int64_t rb, int64_t re, int rows_per_tile, const int64_t *__restrict__ rowptr,
          const int32_t *__restrict__ col, const VT *__restrict__ val, Op op, int *err) {
-  constexpr int CAP = TileCap<VT>::value;
+  constexpr int CAP = RowCfg<VT, KIND>::cap;
+  constexpr int NST = RowCfg<VT, KIND>::stages;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   static_assert((CAP + 8) * 4 % 16 == 0 && (CAP + 8) * sizeof(VT) % 16 == 0);
   // stage s starts at smem_raw + s * stage_bytes (computed, not indexed, so
   // the pointers stay in registers)
   auto stage = [&](int s) {
-    unsigned char *p = smem_raw + (size_t)s * stage_bytes<VT>();
+    unsigned char *p = smem_raw + (size_t)s * stage_bytes<VT, KIND>();
     Stage<VT> r;
     r.rp = reinterpret_cast<int64_t *>(p);
     r.col = reinterpret_cast<int32_t *>(p + (size_t)(kTileRows + 4) * 8);
     r.val = reinterpret_cast<VT *>(p + (size_t)(kTileRows + 4) * 8 + (size_t)(CAP + 8) * 4);
     return r;
   };
-  TileRec *rec = reinterpret_cast<TileRec *>(smem_raw + 2 * stage_bytes<VT>());
-  uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw + 2 * stage_bytes<VT>() + 2 * 32);
+  TileRec *rec = reinterpret_cast<TileRec *>(smem_raw + NST * stage_bytes<VT, KIND>());
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw + NST * stage_bytes<VT, KIND>() + 2 * 32);
   const int64_t nrows = re - rb;
   const int64_t ntiles = (nrows + rows_per_tile - 1) / rows_per_tile;
   const int64_t G = gridDim.x;
@@ -188,8 +207,10 @@ __global__ void __launch_bounds__(kTileRows)
   double contrib = 0.0;
   bool ok = true;
   for (int64_t j = 0; t < ntiles; ++j, t += G) {
-    const int s = (int)(j & 1);
-    if (threadIdx.x == 0 && t + G < ntiles) {
+    // stage of tile j; with a single stage the next tile is issued after the
+    // current one has been consumed (end of the iteration)
+    const int s = NST == 2 ? (int)(j & 1) : 0;
+    if (NST == 2 && threadIdx.x == 0 && t + G < ntiles) {
       (s ? rec[0] : rec[1]) = ahead;
       if (ahead.e1 - ahead.e0 <= CAP)
         issue_tile<VT>(rowptr, col, val, ahead, stage(s ^ 1), &bar[s ^ 1]);
@@ -210,20 +231,27 @@ __global__ void __launch_bounds__(kTileRows)
       if (row < cur.r1) {
         const Stage<VT> sg = stage(s);
         const int64_t b = sg.rp[row - p0], e = sg.rp[row + 1 - p0];
-        contrib += op.row(row, sg.col + (b - c0), sg.val + (b - v0), (int)(e - b));
+        contrib += op.template row<RowCfg<VT, KIND>::gather>(row, sg.col + (b - c0), sg.val + (b - v0),
+                                                             (int)(e - b));
       }
     } else if (row < cur.r1) {
       const int64_t b = rowptr[row], e = rowptr[row + 1];
-      contrib += op.row(row, col + b, val + b, (int)(e - b));
+      contrib += op.template row<RowCfg<VT, KIND>::gather>(row, col + b, val + b, (int)(e - b));
     }
     __syncthreads();
+    if (NST == 1 && threadIdx.x == 0 && t + G < ntiles) {
+      rec[0] = ahead;
+      if (ahead.e1 - ahead.e0 <= CAP) issue_tile<VT>(rowptr, col, val, ahead, stage(0), &bar[0]);
+      if (t + 2 * G < ntiles) ahead = bounds(t + 2 * G);
+    }
+    if (NST == 1) __syncthreads();
   }
   if (!ok) {
     // a copy did not complete in time: report, drain the copies still in
     // flight (bounded) and leave
     if (threadIdx.x == 0) {
       atomicExch(err, 1);
-      for (int s = 0; s < 2; ++s) (void)mbar_wait_bounded(&bar[s], phase[s]);
+      for (int s = 0; s < NST; ++s) (void)mbar_wait_bounded(&bar[s], phase[s]);
     }
     return;
   }
@@ -240,66 +268,62 @@ int sm_count();
 int *device_error_flag();
 
 // rows per tile so that every tile's segment fits one stage
-template <typename VT>
+template <typename VT, int KIND>
 inline int rows_per_tile(int64_t max_row) {
   if (max_row <= 0) return kTileRows;
-  const int64_t r = TileCap<VT>::value / max_row;
+  const int64_t r = RowCfg<VT, KIND>::cap / max_row;
   if (r < 1) return 1;  // rows longer than a stage run on the unstaged path
   return (int)(r < kTileRows ? r : kTileRows);
 }
 
-// CTAs for a persistent launch over `tiles` tiles
-template <typename VT>
-inline unsigned rows_grid(int64_t tiles) {
-  const int64_t per_sm = 1;  // one CTA per SM: the two stages use ~200 KB
-  const int64_t g = (int64_t)sm_count() * per_sm;
-  return (unsigned)(tiles < g ? (tiles > 0 ? tiles : 1) : g);
-}
+// engine configuration used by launch_rows (LGX_ROWS_CONFIG selects another
+// entry of the tuning space)
+int rows_config();
 
-// sets the dynamic shared memory limit once per kernel instantiation
-template <typename VT, class Op>
-inline cudaError_t rows_prepare() {
-  static cudaError_t e = cudaFuncSetAttribute(k_rows<VT, Op>,
-                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)tile_smem_bytes<VT>());
-  return e;
+template <typename VT, class Op, int KIND>
+inline lgx_status launch_rows_cfg(int64_t rb, int64_t re, int64_t max_row, const int64_t *rowptr,
+                                  const int32_t *col, const VT *val, const Op &op,
+                                  cudaStream_t s) {
+  static const cudaError_t attr = cudaFuncSetAttribute(
+    k_rows<VT, Op, KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    (int)tile_smem_bytes<VT, KIND>());
+  LGX_CUDA(attr);
+  const int rpt = rows_per_tile<VT, KIND>(max_row);
+  const int64_t tiles = (re - rb + rpt - 1) / rpt;
+  const int64_t g = (int64_t)sm_count() * RowCfg<VT, KIND>::ctas_per_sm;
+  const unsigned grid = (unsigned)(tiles < g ? (tiles > 0 ? tiles : 1) : g);
+  k_rows<VT, Op, KIND><<<grid, kTileRows, tile_smem_bytes<VT, KIND>(), s>>>(
+    rb, re, rpt, rowptr, col, val, op, device_error_flag());
+  LGX_LAUNCH_CHECK();
+  return LGX_OK;
 }
 
 template <typename VT, class Op>
 inline lgx_status launch_rows(int64_t rb, int64_t re, int64_t max_row, const int64_t *rowptr,
                               const int32_t *col, const VT *val, const Op &op, cudaStream_t s) {
   if (re <= rb) return LGX_OK;
-  LGX_CUDA(rows_prepare<VT, Op>());
-  const int rpt = rows_per_tile<VT>(max_row);
-  const int64_t tiles = (re - rb + rpt - 1) / rpt;
-  k_rows<VT, Op><<<rows_grid<VT>(tiles), kTileRows, tile_smem_bytes<VT>(), s>>>(
-    rb, re, rpt, rowptr, col, val, op, device_error_flag());
-  LGX_LAUNCH_CHECK();
-  return LGX_OK;
-}
-
-// grid size of a reducing launch (the partial buffer needs that many slots)
-template <typename VT>
-inline int64_t rows_partials(int64_t nrows, int64_t max_row) {
-  const int rpt = rows_per_tile<VT>(max_row);
-  return rows_grid<VT>((nrows + rpt - 1) / rpt);
+  switch (rows_config()) {
+    case 1: return launch_rows_cfg<VT, Op, 1>(rb, re, max_row, rowptr, col, val, op, s);
+    case 2: return launch_rows_cfg<VT, Op, 2>(rb, re, max_row, rowptr, col, val, op, s);
+    default: return launch_rows_cfg<VT, Op, 0>(rb, re, max_row, rowptr, col, val, op, s);
+  }
 }
 
 // ---- row operations ---------------------------------------------------------
 // sum_k fma(a_k, x[c_k], init) in storage order.  The column and x loads of
-// up to 32 entries are issued together ahead of the dependent FMA chain, so a
-// 27-point row costs one round of gather latency.
-template <typename VT, typename XT>
+// up to W entries are issued together ahead of the dependent FMA chain, so a
+// 27-point row costs one (W = 32) or two (W = 16) rounds of gather latency.
+template <int W, typename VT, typename XT>
 __device__ __forceinline__ XT row_dot(const int32_t *c, const VT *v, int len,
                                       const XT *__restrict__ x, XT sum) {
-  for (int k = 0; k < len; k += 32) {
-    const int m = len - k < 32 ? len - k : 32;
-    XT xv[32];
+  for (int k = 0; k < len; k += W) {
+    const int m = len - k < W ? len - k : W;
+    XT xv[W];
 #pragma unroll
-    for (int u = 0; u < 32; ++u)
+    for (int u = 0; u < W; ++u)
       if (u < m) xv[u] = __ldg(x + c[k + u]);
 #pragma unroll
-    for (int u = 0; u < 32; ++u)
+    for (int u = 0; u < W; ++u)
       if (u < m) sum = fma((XT)v[k + u], xv[u], sum);
   }
   return sum;

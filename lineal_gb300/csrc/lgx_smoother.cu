@@ -29,6 +29,7 @@ struct JacobiOp {
   static constexpr bool kReduce = false;
   double *partials = nullptr;
   unsigned *counter = nullptr;
+  template <int W>
   __device__ __forceinline__ double row(int64_t i, const int32_t *c, const VT *v, int len) const {
     double accum = b[i], diag = 0.0;
     for (int k = 0; k < len; ++k) {
@@ -308,17 +309,18 @@ struct SorOp {
   static constexpr bool kReduce = false;
   double *partials = nullptr;
   unsigned *counter = nullptr;
+  template <int W>
   __device__ __forceinline__ double row(int64_t i, const int32_t *c, const VT *v, int len) const {
     XT accum = b[i], diag = XT(0);
     const XT xi = x[i];
-    for (int k = 0; k < len; k += 32) {
-      const int m = len - k < 32 ? len - k : 32;
-      XT xv[32];
+    for (int k = 0; k < len; k += W) {
+      const int m = len - k < W ? len - k : W;
+      XT xv[W];
 #pragma unroll
-      for (int u = 0; u < 32; ++u)
+      for (int u = 0; u < W; ++u)
         if (u < m) xv[u] = x[c[k + u]];
 #pragma unroll
-      for (int u = 0; u < 32; ++u) {
+      for (int u = 0; u < W; ++u) {
         if (u < m) {
           const XT a = (XT)v[k + u];
           if (c[k + u] == i) {

@@ -26,8 +26,9 @@ struct SpmvOp {
   static constexpr bool kReduce = false;
   double *partials = nullptr;
   unsigned *counter = nullptr;
+  template <int W>
   __device__ __forceinline__ double row(int64_t i, const int32_t *c, const VT *v, int len) const {
-    y[i] = row_dot<VT, XT>(c, v, len, x, XT(0));
+    y[i] = row_dot<W, VT, XT>(c, v, len, x, XT(0));
     return 0.0;
   }
   __device__ __forceinline__ void finish(double) const {}
@@ -42,8 +43,9 @@ struct ResidualOp {
   static constexpr bool kReduce = NORM;
   double *partials;
   unsigned *counter;
+  template <int W>
   __device__ __forceinline__ double row(int64_t i, const int32_t *c, const VT *v, int len) const {
-    const XT ax = row_dot<VT, XT>(c, v, len, x, XT(0));
+    const XT ax = row_dot<W, VT, XT>(c, v, len, x, XT(0));
     const XT rv = b[i] - ax;
     r[i] = rv;
     return NORM ? (double)rv * (double)rv : 0.0;

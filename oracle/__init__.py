@@ -74,6 +74,7 @@ class _AmgParams(C.Structure):
         ("max_aggregate_size", C.c_int32),
         ("partition_size", C.c_int64),
         ("partition_growth", C.c_double),
+        ("min_partitions", C.c_int64),
         ("max_partitions", C.c_int64),
         ("strong_threshold", C.c_double),
         ("aggressive_threshold", C.c_double),

@@ -155,6 +155,8 @@ typedef struct {
   int32_t max_aggregate_size;     /* 9 */
   int64_t partition_size;         /* vertices per aggregation partition on level 0 */
   double partition_growth;        /* level l uses partition_size * growth^l */
+  int64_t min_partitions;         /* at least this many partitions while each keeps
+                                     >= 1024 vertices */
   int64_t max_partitions;         /* upper clamp on the partition count */
   double strong_threshold;        /* 1/3 */
   double aggressive_threshold;    /* 1/3 */
@@ -171,7 +173,8 @@ typedef struct {
 
 void lo_amg_default_params(lo_amg_params *p);
 /* number of aggregation partitions for n vertices on `level`:
- * clamp(n / (partition_size * growth^level), 1, max_partitions)
+ * clamp(max(n / (partition_size * growth^level),
+ *           min(min_partitions, n / 1024)), 1, max_partitions)
  * (independent.hpp:183-186 with partition_size in the role of min_per_thread
  * and max_partitions in the role of the thread count) */
 int64_t lo_amg_partitions(int64_t n, int64_t level, const lo_amg_params *p);

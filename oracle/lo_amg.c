@@ -14,6 +14,7 @@ void lo_amg_default_params(lo_amg_params *p) {
   p->max_aggregate_size = 9;
   p->partition_size = 4096;
   p->partition_growth = 4.0;
+  p->min_partitions = 16;
   p->max_partitions = 1 << 30;
   p->strong_threshold = 1.0 / 3.0;
   p->aggressive_threshold = 1.0 / 3.0;
@@ -543,6 +544,8 @@ int64_t lo_amg_partitions(int64_t n, int64_t level, const lo_amg_params *p) {
   double ps = (double)p->partition_size;
   for (int64_t l = 0; l < level; ++l) ps *= p->partition_growth;
   int64_t parts = ps >= 1.0 ? (int64_t)((double)n / ps) : n;
+  const int64_t floor_parts = p->min_partitions < n / 1024 ? p->min_partitions : n / 1024;
+  if (parts < floor_parts) parts = floor_parts;
   if (parts < 1) parts = 1;
   if (parts > p->max_partitions) parts = p->max_partitions;
   return parts;
