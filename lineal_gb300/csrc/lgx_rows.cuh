@@ -43,10 +43,9 @@ struct RowCfg {
   // thread at one CTA per SM, 128 at two)
   static constexpr int gather = KIND == 0 ? 32 : 16;
 };
-template <typename VT>
-struct TileCap {
-  static constexpr int value = RowCfg<VT, 0>::cap;
-};
+// upper bound of RowCfg::ctas_per_sm: reduction partials of row kernels are
+// sized sm_count() * kRowsMaxCtasPerSm
+constexpr int kRowsMaxCtasPerSm = 2;
 
 // per stage: row offsets (kTileRows + 4) * 8 bytes, columns (CAP + 8) * 4
 // bytes, values (CAP + 8) * sizeof(VT) bytes (an aligned span exceeds its
@@ -159,6 +158,7 @@ __global__ void __launch_bounds__(kTileRows, RowCfg<VT, KIND>::ctas_per_sm)
          const int32_t *__restrict__ col, const VT *__restrict__ val, Op op, int *err) {
   constexpr int CAP = RowCfg<VT, KIND>::cap;
   constexpr int NST = RowCfg<VT, KIND>::stages;
+  static_assert(RowCfg<VT, KIND>::ctas_per_sm <= kRowsMaxCtasPerSm);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   static_assert((CAP + 8) * 4 % 16 == 0 && (CAP + 8) * sizeof(VT) % 16 == 0);
   // stage s starts at smem_raw + s * stage_bytes (computed, not indexed, so

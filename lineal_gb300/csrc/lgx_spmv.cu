@@ -74,7 +74,8 @@ lgx_status csr_residual(const Csr &a, const VT *val, const XT *b, const XT *x, X
 }
 
 // partial-sum slots of a reducing row launch (persistent grid <= SM count)
-int64_t csr_partials(int64_t /*n*/) { return sm_count(); }
+// the row engine's grid never exceeds sm_count() * kRowsMaxCtasPerSm blocks
+int64_t csr_partials(int64_t /*n*/) { return (int64_t)sm_count() * kRowsMaxCtasPerSm; }
 
 template lgx_status csr_spmv<double, double>(const Csr &, const double *, const double *,
                                              double *, cudaStream_t);
