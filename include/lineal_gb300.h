@@ -153,6 +153,30 @@ lgx_status lgx_gen_7pt(const int64_t dims[3], const double *d_k, lgx_dtype stora
 lgx_status lgx_dot(int64_t n, const double *d_a, const double *d_b, double *d_out,
                    lgx_stream stream);
 lgx_status lgx_norm2sq(int64_t n, const double *d_a, double *d_out, lgx_stream stream);
+
+/* lgx_dot without any device allocation.  No reference counterpart: lineal's
+ * dot (sink/accumulator.hpp:151-157) is a CPU reduction with no scratch.
+ *
+ * lgx_dot allocates and frees its partial sums on every call, and cudaFree
+ * waits for the whole device.  Callers that must not allocate (code whose
+ * device memory is all handed to its own pool, or a loop that keeps several
+ * streams busy and cannot afford that device-wide wait) call this instead:
+ * the partial sums live in a fixed static device array of the library.
+ *
+ * - Result: the same as lgx_dot (same grid, same summation order), written to
+ *   d_out in stream order; the call does not synchronise.
+ * - Maximum size: n <= 2,097,152 elements (1024 partial sums of 2048
+ *   elements); a larger n returns LGX_ERR_INVALID with a message.
+ * - Set-up: the first call on each device looks up the scratch address
+ *   (cudaGetSymbolAddress) with that device current; make that first call
+ *   before any stream capture.
+ * - The scratch is shared: two calls that overlap in time on one device (two
+ *   streams, or two host threads) race on it and give wrong results.  Calls on
+ *   one stream are ordered and safe.
+ * - The scratch's arrival counter must be zero when a call starts; it is zero
+ *   when the library loads and every completed call leaves it at zero. */
+lgx_status lgx_dot_static(int64_t n, const double *d_a, const double *d_b, double *d_out,
+                          lgx_stream stream);
 lgx_status lgx_max_norm(int64_t n, const double *d_a, double *d_out, lgx_stream stream);
 /* y = y + alpha * x */
 lgx_status lgx_axpy(int64_t n, double alpha, const double *d_x, double *d_y, lgx_stream stream);

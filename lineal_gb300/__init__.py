@@ -132,6 +132,7 @@ def _signatures(L):
         "lgx_gen_27pt": [V, V, C.c_int, V, P(V)],
         "lgx_gen_7pt": [V, V, C.c_int, V, P(V)],
         "lgx_dot": [I64, V, V, V, V],
+        "lgx_dot_static": [I64, V, V, V, V],
         "lgx_norm2sq": [I64, V, V, V],
         "lgx_max_norm": [I64, V, V, V],
         "lgx_axpy": [I64, D, V, V, V],

@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -251,6 +252,44 @@ struct ReduceScratch {
     return LGX_OK;
   }
 };
+
+// Scratch of lgx_dot_static: one partial sum per block of k_dot and the
+// block-arrival counter, in the module's static device memory (8 KB + 8 B).
+// The counter must be zero when a call starts: static device memory is
+// zero-initialised when the module loads, and every completed k_dot leaves
+// its counter at zero again (the last block resets it).
+constexpr int kDotStaticPartials = 1024;
+struct DotStaticScratch {
+  double partials[kDotStaticPartials];
+  unsigned counter;
+};
+static __device__ __align__(256) DotStaticScratch g_dot_static_scratch;
+
+// Device address of g_dot_static_scratch, looked up once per device (with
+// that device current) on the first lgx_dot_static call there.
+constexpr int kDotStaticMaxDevices = 64;
+static std::mutex g_dot_static_mutex;
+static DotStaticScratch *g_dot_static_ptr[kDotStaticMaxDevices] = {};
+
+static lgx_status dot_static_scratch(DotStaticScratch **out) {
+  int dev = 0;
+  LGX_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kDotStaticMaxDevices)
+    return fail(LGX_ERR_UNSUPPORTED, "lgx_dot_static: device ordinal " + std::to_string(dev) +
+                                       " beyond the " + std::to_string(kDotStaticMaxDevices) +
+                                       " devices it keeps scratch addresses for");
+  std::lock_guard<std::mutex> lock(g_dot_static_mutex);
+  if (!g_dot_static_ptr[dev]) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_dot_static_scratch);
+    if (e != cudaSuccess)
+      return fail(LGX_ERR_CUDA, std::string("lgx_dot_static: cudaGetSymbolAddress failed: ") +
+                                  cudaGetErrorString(e));
+    g_dot_static_ptr[dev] = static_cast<DotStaticScratch *>(p);
+  }
+  *out = g_dot_static_ptr[dev];
+  return LGX_OK;
+}
 
 __global__ void k_axpy(int64_t n, double alpha, const double *x, double *y) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -591,6 +630,21 @@ lgx_status lgx_dot(int64_t n, const double *d_a, const double *d_b, double *d_ou
   LGX_CHECK(dot(n, d_a, d_b, d_out, rs.partials.p, rs.counter.p, stream));
   LGX_CUDA(cudaStreamSynchronize(stream));
   return LGX_OK;
+}
+
+lgx_status lgx_dot_static(int64_t n, const double *d_a, const double *d_b, double *d_out,
+                          lgx_stream stream) {
+  if (n < 0 || (n > 0 && (!d_a || !d_b)) || !d_out) return fail(LGX_ERR_INVALID, "bad argument");
+  // same grid as lgx_dot (so the same result); its partial sums must fit the
+  // static scratch
+  if (reduce_blocks(n) > kDotStaticPartials)
+    return fail(LGX_ERR_INVALID,
+                "lgx_dot_static: n = " + std::to_string(n) + " exceeds the maximum of " +
+                  std::to_string((int64_t)kDotStaticPartials * kReduceThreads * 8) +
+                  " elements its static scratch holds; use lgx_dot");
+  DotStaticScratch *sc = nullptr;
+  LGX_CHECK(dot_static_scratch(&sc));
+  return dot(n, d_a, d_b, d_out, sc->partials, &sc->counter, stream);
 }
 
 lgx_status lgx_norm2sq(int64_t n, const double *d_a, double *d_out, lgx_stream stream) {
