@@ -222,7 +222,9 @@ def run_gb300(args):
     torch.cuda.synchronize()
     log(f"[gb300] generated {dims} nnz={nnz} in {time.perf_counter() - t0:.2f}s")
 
-    wright = g.HierarchyWright(min_coarsen_size=2000, partition_size=args.partition_size)
+    hier_kw = dict(min_coarsen_size=2000, partition_size=args.partition_size,
+                   partition_growth=args.partition_growth, min_partitions=args.min_partitions)
+    wright = g.HierarchyWright(**hier_kw)
     t0 = time.perf_counter()
     h64 = wright.instantiate(a, finest_colouring=col)
     torch.cuda.synchronize()
@@ -268,8 +270,7 @@ def run_gb300(args):
     log(f"[gb300] FP64 AMG-PCG {ms64:.1f} ms, {res.iterations} it, rel {rel64:.2e}")
 
     # ---- mixed precision: float cycle under the FP64 CG ---------------------
-    wright32 = g.HierarchyWright(min_coarsen_size=2000, partition_size=args.partition_size,
-                                 cycle_f32=True)
+    wright32 = g.HierarchyWright(cycle_f32=True, **hier_kw)
     t0 = time.perf_counter()
     h32 = wright32.instantiate(a, finest_colouring=col)
     torch.cuda.synchronize()
@@ -342,8 +343,8 @@ def run_gb300(args):
             m = g.CsrMatrix.from_device(d_rowptr, d_col, d_val, symmetric=True)
             del d_rowptr, d_col, d_val
             c = g.Colouring.from_array(m, d_colours, 8)
-            hh = g.HierarchyWright(min_coarsen_size=2000, partition_size=args.partition_size,
-                                   cycle_f32=True).instantiate(m, finest_colouring=c)
+            hh = g.HierarchyWright(cycle_f32=True, **hier_kw).instantiate(
+                m, finest_colouring=c)
             rr = g.pcg(m, d_b, precon=g.PRECON_AMG, amg=hh, rtol=1e-8, maxit=500)
             xh = rr.x.cpu()
             torch.cuda.synchronize()
@@ -376,6 +377,8 @@ def run_gb300(args):
             "rows": n, "nnz": nnz, "parallelism": f"replicas x{world}",
             "l2": "inputs (5.7 GB matrix) larger than L2; no flush",
             "amg": {"levels": rows, "level_nnz": nnzs, "partition_size": args.partition_size,
+                    "partition_growth": args.partition_growth,
+                    "min_partitions": args.min_partitions,
                     "finest_colouring": "grid parity, 8 colours"},
         },
         "iterations": iters64, "final_rel_residual": rel64, "setup_ms": setup64 * 1e3,
@@ -449,6 +452,8 @@ def main():
     ap.add_argument("--mode", default="solve", choices=["solve", "kernels"])
     ap.add_argument("--grid", type=int, default=256)
     ap.add_argument("--partition-size", type=int, default=4096)
+    ap.add_argument("--partition-growth", type=float, default=4.0)
+    ap.add_argument("--min-partitions", type=int, default=8)
     ap.add_argument("--cpu-sample-edge", type=int, default=64)
     ap.add_argument("--reference-iterations", type=int, default=0,
                     help="iterations of the full-size solve used to extrapolate the CPU sample")

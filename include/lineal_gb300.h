@@ -224,7 +224,7 @@ typedef struct {
   int64_t partition_size;      /* vertices per aggregation partition on the finest level */
   double partition_growth;     /* level l uses partition_size * growth^l: coarse levels
                                   keep partitions that span several fine planes */
-  int64_t min_partitions;      /* but at least this many partitions while each keeps
+  int64_t min_partitions;      /* but at least this many partitions (default 8) while each keeps
                                   1024 vertices (parallelism on coarse levels) */
   int64_t max_partitions;      /* clamp on the partition count */
   double strong_threshold;     /* DuneDependencyCriterion (dependency/criterion.hpp:103-118) */

@@ -377,7 +377,7 @@ struct AggregationParams {
   int32_t max_aggregate_size = 9;
   int64_t partition_size = 4096;
   double partition_growth = 4.0;
-  int64_t min_partitions = 16;
+  int64_t min_partitions = 8;
 };
 
 struct DuneDependencyCriterion {

@@ -474,7 +474,7 @@ class HierarchyWright:
     max_aggregate_size: int = 9
     partition_size: int = 4096
     partition_growth: float = 4.0
-    min_partitions: int = 16
+    min_partitions: int = 8
     max_partitions: int = 1 << 30
     coarse_f32: bool = False
     cycle_f32: bool = False

@@ -1219,7 +1219,7 @@ void lgx_amg_default_params(lgx_amg_params *p) {
   p->max_aggregate_size = 9;
   p->partition_size = 4096;
   p->partition_growth = 4.0;
-  p->min_partitions = 16;
+  p->min_partitions = 8;
   p->max_partitions = 1 << 30;
   p->strong_threshold = 1.0 / 3.0;
   p->aggressive_threshold = 1.0 / 3.0;

@@ -155,7 +155,7 @@ typedef struct {
   int32_t max_aggregate_size;     /* 9 */
   int64_t partition_size;         /* vertices per aggregation partition on level 0 */
   double partition_growth;        /* level l uses partition_size * growth^l */
-  int64_t min_partitions;         /* at least this many partitions while each keeps
+  int64_t min_partitions;         /* 8: at least this many partitions while each keeps
                                      >= 1024 vertices */
   int64_t max_partitions;         /* upper clamp on the partition count */
   double strong_threshold;        /* 1/3 */
