@@ -34,11 +34,12 @@ int sm_count() {
 
 int rows_config() {
   static const int c = [] {
-    // kind 1 (one stage, two CTAs per SM) measured fastest at 256^3:
-    // FP64 SpMV 1.36 ms vs 1.55 ms (kind 0) and 1.45 ms (kind 2)
+    // FP64 SpMV / SOR sweep at 256^3 (27-point, 449M nnz), ms:
+    //   CTA tiles kind 0 1.55 / 2.63, kind 1 1.37 / 1.98, kind 2 1.45 / 2.33;
+    //   warp tiles 3: 1.08 / 1.69, 4: 1.38 / 2.48, 5: 1.16 / 1.80, 6: 1.37 / 2.30
     const char *e = std::getenv("LGX_ROWS_CONFIG");
-    const int v = e ? std::atoi(e) : 1;
-    return (v >= 0 && v <= 2) ? v : 1;
+    const int v = e ? std::atoi(e) : 3;
+    return (v >= 0 && v <= 6) ? v : 3;
   }();
   return c;
 }
@@ -96,7 +97,7 @@ __global__ void k_f32_to_f64(int64_t n, const float *src, double *dst) {
 
 // validates sortedness / diagonal presence and records the longest row
 __global__ void k_csr_check(int64_t n, int64_t nnz, const int64_t *rowptr, const int32_t *col,
-                            unsigned long long *max_row, int *bad) {
+                            unsigned long long *max_row, unsigned long long *max_win, int *bad) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = rowptr[i], e = rowptr[i + 1];
@@ -105,6 +106,8 @@ __global__ void k_csr_check(int64_t n, int64_t nnz, const int64_t *rowptr, const
       continue;
     }
     atomicMax(max_row, (unsigned long long)(e - b));
+    const int64_t we = rowptr[i + kWarpTileRows < n ? i + kWarpTileRows : n];
+    if (we >= b) atomicMax(max_win, (unsigned long long)(we - b));
     int has_diag = 0;
     for (int64_t k = b; k < e; ++k) {
       const int32_t c = col[k];
@@ -156,25 +159,51 @@ lgx_status csr_alloc_arrays(Csr &a, int64_t nnz, lgx_dtype storage) {
 lgx_status csr_compute_max_row(Csr &a, cudaStream_t s) {
   DBuf<unsigned long long> mx;
   DBuf<int> bad;
-  LGX_CHECK(mx.alloc(1));
+  LGX_CHECK(mx.alloc(2));
   LGX_CHECK(bad.alloc(1));
-  LGX_CUDA(cudaMemsetAsync(mx.p, 0, sizeof(unsigned long long), s));
+  LGX_CUDA(cudaMemsetAsync(mx.p, 0, 2 * sizeof(unsigned long long), s));
   LGX_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), s));
   if (a.n) {
     k_csr_check<<<std::min<int64_t>(grid_for(a.n, 256), 4096), 256, 0, s>>>(
-      a.n, a.nnz, a.rowptr.p, a.col.p, mx.p, bad.p);
+      a.n, a.nnz, a.rowptr.p, a.col.p, mx.p, mx.p + 1, bad.p);
     LGX_LAUNCH_CHECK();
   }
-  unsigned long long h_mx = 0;
+  unsigned long long h_mx[2] = {0, 0};
   int h_bad = 0;
-  LGX_CUDA(cudaMemcpyAsync(&h_mx, mx.p, sizeof(h_mx), cudaMemcpyDeviceToHost, s));
+  LGX_CUDA(cudaMemcpyAsync(h_mx, mx.p, sizeof(h_mx), cudaMemcpyDeviceToHost, s));
   LGX_CUDA(cudaMemcpyAsync(&h_bad, bad.p, sizeof(h_bad), cudaMemcpyDeviceToHost, s));
   LGX_CUDA(cudaStreamSynchronize(s));
   if (h_bad & 1) return fail(LGX_ERR_INVALID, "CSR row offsets are not monotone");
   if (h_bad & 2) return fail(LGX_ERR_INVALID, "CSR column index out of range");
   if (h_bad & 4) return fail(LGX_ERR_INVALID, "CSR columns are not strictly ascending");
   if (h_bad & 8) return fail(LGX_ERR_INVALID, "CSR row without stored diagonal");
-  a.max_row = (int64_t)h_mx;
+  a.max_row = (int64_t)h_mx[0];
+  a.max_win = (int64_t)h_mx[1];
+  return LGX_OK;
+}
+
+__global__ void k_csr_window(int64_t n, const int64_t *rowptr, unsigned long long *max_win) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = rowptr[i];
+    const int64_t we = rowptr[i + kWarpTileRows < n ? i + kWarpTileRows : n];
+    atomicMax(max_win, (unsigned long long)(we - b));
+  }
+}
+
+lgx_status csr_compute_max_window(Csr &a, cudaStream_t s) {
+  DBuf<unsigned long long> mx;
+  LGX_CHECK(mx.alloc(1));
+  LGX_CUDA(cudaMemsetAsync(mx.p, 0, sizeof(unsigned long long), s));
+  if (a.n) {
+    k_csr_window<<<std::min<int64_t>(grid_for(a.n, 256), 4096), 256, 0, s>>>(a.n, a.rowptr.p,
+                                                                              mx.p);
+    LGX_LAUNCH_CHECK();
+  }
+  unsigned long long h = 0;
+  LGX_CUDA(cudaMemcpyAsync(&h, mx.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+  LGX_CUDA(cudaStreamSynchronize(s));
+  a.max_win = (int64_t)h;
   return LGX_OK;
 }
 
@@ -496,6 +525,7 @@ static lgx_status gen_structured(const int64_t dims[3], const double *d_k, int n
     cudaStreamSynchronize(s);
   }
   c.max_row = npts;
+  c.max_win = (int64_t)npts * kWarpTileRows;
   *out = m;
   return LGX_OK;
 }

@@ -83,6 +83,7 @@ constexpr uint32_t kIsolated = 0xFFFFFFFEu;
 struct Csr {
   int64_t n = 0, nnz = 0;
   int64_t max_row = 0;
+  int64_t max_win = 0;  // most entries in any kWarpTileRows consecutive rows
   int symmetric = 0;
   lgx_dtype storage = LGX_F64;
   DBuf<int64_t> rowptr;
@@ -145,6 +146,11 @@ lgx_status csr_from_device(int64_t n, int64_t nnz, const int64_t *rowptr, const 
                            const double *val, int symmetric, lgx_dtype storage,
                            cudaStream_t s, Csr &out);
 lgx_status csr_compute_max_row(Csr &a, cudaStream_t s);
+// rows per tile of the warp-tile row engine; Csr::max_win is measured over
+// windows of this many rows
+constexpr int kWarpTileRows = 32;
+// sets a.max_win from the row offsets (for matrices whose rows were permuted)
+lgx_status csr_compute_max_window(Csr &a, cudaStream_t s);
 
 // y = A x for CSR with value type VT and vector type XT (accumulation in XT)
 template <typename VT, typename XT>

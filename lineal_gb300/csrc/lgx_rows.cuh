@@ -43,9 +43,9 @@ struct RowCfg {
   // thread at one CTA per SM, 128 at two)
   static constexpr int gather = KIND == 0 ? 32 : 16;
 };
-// upper bound of RowCfg::ctas_per_sm: reduction partials of row kernels are
-// sized sm_count() * kRowsMaxCtasPerSm
-constexpr int kRowsMaxCtasPerSm = 2;
+// upper bound of the CTAs per SM of every row-engine configuration:
+// reduction partials of row kernels are sized sm_count() * kRowsMaxCtasPerSm
+constexpr int kRowsMaxCtasPerSm = 16;
 
 // per stage: row offsets (kTileRows + 4) * 8 bytes, columns (CAP + 8) * 4
 // bytes, values (CAP + 8) * sizeof(VT) bytes (an aligned span exceeds its
@@ -276,9 +276,188 @@ inline int rows_per_tile(int64_t max_row) {
   return (int)(r < kTileRows ? r : kTileRows);
 }
 
+// ---- warp-tile engine ---------------------------------------------------------
+// Every warp owns its own tiles of kWarpTileRows (32) consecutive rows and its
+// own S shared-memory stages and mbarriers: lane 0 issues the bulk copies of
+// the warp's next tiles while the lanes compute the current one (lane = row),
+// and no barrier couples the warps of a CTA, so the SM always holds warps in
+// every phase (copy in flight, gathers in flight, FMA chain).  A stage holds
+// the tile's row offsets and up to `capw` entries; capw >= Csr::max_win (the
+// most entries in any 32 consecutive rows), so every tile fits.  Tiles are
+// dealt round-robin over all warps of the grid (tile = warp id + j * warps),
+// which keeps the active rows, and so the x gathers, in a compact window.
+// dynamic shared memory limit of a warp-tile CTA (227 KB per CTA minus room
+// for the static reduction buffers, up to 2 KB + 16 B)
+constexpr int kWrowsSmemMax = 224 * 1024;
+
+__host__ __device__ constexpr size_t wstage_bytes(int capw, size_t vsize) {
+  return (size_t)(kWarpTileRows + 4) * 8 + (size_t)(capw + 8) * 4 + (size_t)(capw + 8) * vsize;
+}
+// per CTA: WPC * S barriers and WPC * S "unstaged" flags, then the stages
+__host__ __device__ constexpr size_t wheader_bytes(int wpc, int nst) {
+  return (((size_t)wpc * nst * 12) + 15) & ~(size_t)15;
+}
+__host__ __device__ constexpr size_t wsmem_bytes(int wpc, int nst, int capw, size_t vsize) {
+  return wheader_bytes(wpc, nst) + (size_t)wpc * nst * wstage_bytes(capw, vsize);
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+template <int WPC>
+struct WrowsBounds {
+  // 4 warps per CTA: registers <= 65536 / (5 * 128) so that five CTAs (20
+  // warps) fit an SM, and 8 gathers per round to stay within them;
+  // 8 warps per CTA: two CTAs (16 warps), 16 gathers per round
+  static constexpr int min_blocks = WPC == 4 ? 5 : 2;
+  static constexpr int gather = WPC == 4 ? 8 : 16;
+};
+
+template <typename VT, class Op, int WPC, int S>
+__global__ void __launch_bounds__(WPC * 32, WrowsBounds<WPC>::min_blocks)
+  k_wrows(int64_t rb, int64_t re, int capw, const int64_t *__restrict__ rowptr,
+          const int32_t *__restrict__ col, const VT *__restrict__ val, Op op, int *err) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int W = WrowsBounds<WPC>::gather;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const size_t sb = wstage_bytes(capw, sizeof(VT));
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw) + warp * S;
+  int *unstaged = reinterpret_cast<int *>(smem_raw + (size_t)WPC * S * 8) + warp * S;
+  unsigned char *base = smem_raw + wheader_bytes(WPC, S) + (size_t)warp * S * sb;
+  auto stage = [&](int s) {
+    unsigned char *p = base + (size_t)s * sb;
+    Stage<VT> r;
+    r.rp = reinterpret_cast<int64_t *>(p);
+    r.col = reinterpret_cast<int32_t *>(p + (size_t)(kWarpTileRows + 4) * 8);
+    r.val = reinterpret_cast<VT *>(p + (size_t)(kWarpTileRows + 4) * 8 + (size_t)(capw + 8) * 4);
+    return r;
+  };
+  const int64_t ntiles = (re - rb + kWarpTileRows - 1) / kWarpTileRows;
+  const int64_t GW = (int64_t)gridDim.x * WPC;
+  int64_t t = (int64_t)blockIdx.x * WPC + warp;
+  auto bounds = [&](int64_t tt) {
+    TileRec r;
+    r.r0 = rb + tt * kWarpTileRows;
+    r.r1 = min(r.r0 + kWarpTileRows, re);
+    r.e0 = rowptr[r.r0];
+    r.e1 = rowptr[r.r1];
+    return r;
+  };
+  // lane 0: stage s receives tile `tr` (bulk copies, or an empty arrival that
+  // sends the lanes to global memory when the tile does not fit)
+  auto issue = [&](const TileRec &tr, int s) {
+    if (tr.e1 - tr.e0 <= capw) {
+      unstaged[s] = 0;
+      issue_tile<VT>(rowptr, col, val, tr, stage(s), &bar[s]);
+    } else {
+      unstaged[s] = 1;
+      mbar_arrive(&bar[s]);
+    }
+  };
+
+  TileRec ahead{};
+  unsigned pending = 0;  // stages with an issued, not yet consumed tile
+  if (lane == 0) {
+    for (int s = 0; s < S; ++s) mbar_init(&bar[s], 1);
+    fence_mbar_init();
+    for (int s = 0; s < S; ++s) {
+      if (t + s * GW < ntiles) {
+        issue(bounds(t + s * GW), s);
+        pending |= 1u << s;
+      }
+    }
+    if (t + S * GW < ntiles) ahead = bounds(t + S * GW);
+  }
+  __syncwarp();
+
+  unsigned phase = 0;
+  double contrib = 0.0;
+  bool ok = true;
+  for (int64_t j = 0; t < ntiles; ++j, t += GW) {
+    const int s = S == 1 ? 0 : (int)(j % S);
+    const bool waited = mbar_wait_bounded(&bar[s], (phase >> s) & 1u);
+    if (__any_sync(0xffffffffu, !waited)) {
+      ok = false;
+      break;
+    }
+    phase ^= 1u << s;
+    pending &= ~(1u << s);
+    const int64_t r0 = rb + t * kWarpTileRows;
+    const int64_t row = r0 + lane;
+    const int64_t r1 = min(r0 + kWarpTileRows, re);
+    if (!unstaged[s]) {
+      constexpr int64_t CA = 4, VA = 16 / (int64_t)sizeof(VT);
+      const Stage<VT> sg = stage(s);
+      const int64_t p0 = r0 & ~1ll;
+      const int64_t e0 = sg.rp[r0 - p0];
+      const int64_t c0 = e0 & ~(CA - 1), v0 = e0 & ~(VA - 1);
+      if (row < r1) {
+        const int64_t b = sg.rp[row - p0], e = sg.rp[row + 1 - p0];
+        contrib += op.template row<W>(row, sg.col + (b - c0), sg.val + (b - v0), (int)(e - b));
+      }
+    } else if (row < r1) {
+      const int64_t b = rowptr[row], e = rowptr[row + 1];
+      contrib += op.template row<W>(row, col + b, val + b, (int)(e - b));
+    }
+    __syncwarp();
+    if (lane == 0 && t + S * GW < ntiles) {
+      issue(ahead, s);
+      pending |= 1u << s;
+      if (t + (S + 1) * GW < ntiles) ahead = bounds(t + (S + 1) * GW);
+    }
+  }
+  if (!ok) {
+    // a copy did not complete in time: report, drain this warp's copies still
+    // in flight (bounded) and join the CTA's exit
+    if (lane == 0) {
+      atomicExch(err, 1);
+      for (int s = 0; s < S; ++s)
+        if (pending & (1u << s)) (void)mbar_wait_bounded(&bar[s], (phase >> s) & 1u);
+    }
+    __syncwarp();
+  }
+  if constexpr (Op::kReduce) {
+    double total;
+    if (grid_reduce<WPC * 32>(contrib, blockIdx.x, gridDim.x, op.partials, op.counter, &total) &&
+        threadIdx.x == 0)
+      op.finish(total);
+  }
+}
+
 // engine configuration used by launch_rows (LGX_ROWS_CONFIG selects another
-// entry of the tuning space)
+// entry of the tuning space): 0-2 CTA tiles (RowCfg kinds); warp tiles with
+// 3: 4 warps x 1 stage, 4: 4 warps x 2 stages, 5: 8 warps x 1 stage,
+// 6: 8 warps x 2 stages per CTA
 int rows_config();
+
+template <typename VT, class Op, int WPC, int S>
+inline lgx_status launch_wrows(int64_t rb, int64_t re, const Csr &a, const VT *val, const Op &op,
+                               cudaStream_t s, bool *done) {
+  *done = false;
+  const int64_t mw = a.max_win > 4 ? a.max_win : 4;
+  if (mw > (1 << 20)) return LGX_OK;
+  const int capw = (int)((mw + 3) & ~3ll);
+  const size_t smem = wsmem_bytes(WPC, S, capw, sizeof(VT));
+  if (smem > (size_t)kWrowsSmemMax) return LGX_OK;  // too long rows: CTA tiles
+  static const cudaError_t attr = cudaFuncSetAttribute(
+    k_wrows<VT, Op, WPC, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, kWrowsSmemMax);
+  LGX_CUDA(attr);
+  int per_sm = 0;
+  LGX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wrows<VT, Op, WPC, S>,
+                                                         WPC * 32, smem));
+  if (per_sm < 1) return LGX_OK;
+  if (per_sm > kRowsMaxCtasPerSm) per_sm = kRowsMaxCtasPerSm;
+  const int64_t tiles = (re - rb + kWarpTileRows - 1) / kWarpTileRows;
+  const int64_t need = (tiles + WPC - 1) / WPC;
+  const int64_t g = (int64_t)sm_count() * per_sm;
+  const unsigned grid = (unsigned)(need < g ? (need > 0 ? need : 1) : g);
+  k_wrows<VT, Op, WPC, S><<<grid, WPC * 32, smem, s>>>(rb, re, capw, a.rowptr.p, a.col.p, val,
+                                                        op, device_error_flag());
+  LGX_LAUNCH_CHECK();
+  *done = true;
+  return LGX_OK;
+}
 
 template <typename VT, class Op, int KIND>
 inline lgx_status launch_rows_cfg(int64_t rb, int64_t re, int64_t max_row, const int64_t *rowptr,
@@ -298,14 +477,27 @@ inline lgx_status launch_rows_cfg(int64_t rb, int64_t re, int64_t max_row, const
   return LGX_OK;
 }
 
+// rows [rb, re) of `a` (values `val`) through the configured engine
 template <typename VT, class Op>
-inline lgx_status launch_rows(int64_t rb, int64_t re, int64_t max_row, const int64_t *rowptr,
-                              const int32_t *col, const VT *val, const Op &op, cudaStream_t s) {
+inline lgx_status launch_rows(int64_t rb, int64_t re, const Csr &a, const VT *val, const Op &op,
+                              cudaStream_t s) {
   if (re <= rb) return LGX_OK;
+  bool done = false;
   switch (rows_config()) {
-    case 1: return launch_rows_cfg<VT, Op, 1>(rb, re, max_row, rowptr, col, val, op, s);
-    case 2: return launch_rows_cfg<VT, Op, 2>(rb, re, max_row, rowptr, col, val, op, s);
-    default: return launch_rows_cfg<VT, Op, 0>(rb, re, max_row, rowptr, col, val, op, s);
+    case 3: LGX_CHECK((launch_wrows<VT, Op, 4, 1>(rb, re, a, val, op, s, &done))); break;
+    case 4: LGX_CHECK((launch_wrows<VT, Op, 4, 2>(rb, re, a, val, op, s, &done))); break;
+    case 5: LGX_CHECK((launch_wrows<VT, Op, 8, 1>(rb, re, a, val, op, s, &done))); break;
+    case 6: LGX_CHECK((launch_wrows<VT, Op, 8, 2>(rb, re, a, val, op, s, &done))); break;
+    default: break;
+  }
+  if (done) return LGX_OK;
+  switch (rows_config()) {
+    case 0:
+      return launch_rows_cfg<VT, Op, 0>(rb, re, a.max_row, a.rowptr.p, a.col.p, val, op, s);
+    case 2:
+      return launch_rows_cfg<VT, Op, 2>(rb, re, a.max_row, a.rowptr.p, a.col.p, val, op, s);
+    default:
+      return launch_rows_cfg<VT, Op, 1>(rb, re, a.max_row, a.rowptr.p, a.col.p, val, op, s);
   }
 }
 

@@ -283,8 +283,7 @@ lgx_status colouring_build(const Csr &a, const int32_t *d_colour, int32_t ncolou
                                          p.rowptr.p, p.col.p, p.v32.p);
   }
   LGX_LAUNCH_CHECK();
-  LGX_CUDA(cudaStreamSynchronize(s));
-  return LGX_OK;
+  return csr_compute_max_window(p, s);
 }
 
 lgx_status colouring_make_f32(lgx_colouring &c, cudaStream_t s) {
@@ -351,7 +350,7 @@ lgx_status mc_sor_sweep(const lgx_colouring &c, const VT *val, double relax, int
   for (int32_t k = 0; k < c.ncolours; ++k) {
     const int32_t col_id = forward ? k : c.ncolours - 1 - k;
     const int64_t rb = c.offsets[col_id], re = c.offsets[col_id + 1];
-    LGX_CHECK(launch_rows<VT>(rb, re, p.max_row, p.rowptr.p, p.col.p, val, op, s));
+    LGX_CHECK(launch_rows<VT>(rb, re, p, val, op, s));
   }
   return LGX_OK;
 }
@@ -368,9 +367,9 @@ lgx_status jacobi_csr(const Csr &a, double relax, const double *x_in, double *x_
                       const double *b, cudaStream_t s) {
   if (a.n == 0) return LGX_OK;
   if (a.storage == LGX_F64)
-    return launch_rows<double>(0, a.n, a.max_row, a.rowptr.p, a.col.p, a.v64.p,
+    return launch_rows<double>(0, a.n, a, a.v64.p,
                                JacobiOp<double>{x_in, x_out, b, relax, 1.0 - relax}, s);
-  return launch_rows<float>(0, a.n, a.max_row, a.rowptr.p, a.col.p, a.v32.p,
+  return launch_rows<float>(0, a.n, a, a.v32.p,
                             JacobiOp<float>{x_in, x_out, b, relax, 1.0 - relax}, s);
 }
 

@@ -56,7 +56,7 @@ struct ResidualOp {
 template <typename VT, typename XT>
 lgx_status csr_spmv(const Csr &a, const VT *val, const XT *x, XT *y, cudaStream_t s) {
   if (a.n == 0) return LGX_OK;
-  return launch_rows<VT>(0, a.n, a.max_row, a.rowptr.p, a.col.p, val, SpmvOp<VT, XT>{x, y}, s);
+  return launch_rows<VT>(0, a.n, a, val, SpmvOp<VT, XT>{x, y}, s);
 }
 
 template <typename VT, typename XT>
@@ -67,13 +67,13 @@ lgx_status csr_residual(const Csr &a, const VT *val, const XT *b, const XT *x, X
     return LGX_OK;
   }
   if (norm)
-    return launch_rows<VT>(0, a.n, a.max_row, a.rowptr.p, a.col.p, val,
+    return launch_rows<VT>(0, a.n, a, val,
                            ResidualOp<VT, XT, true>{b, x, r, norm, partials, counter}, s);
-  return launch_rows<VT>(0, a.n, a.max_row, a.rowptr.p, a.col.p, val,
+  return launch_rows<VT>(0, a.n, a, val,
                          ResidualOp<VT, XT, false>{b, x, r, nullptr, nullptr, nullptr}, s);
 }
 
-// partial-sum slots of a reducing row launch (persistent grid <= SM count)
+// partial-sum slots of a reducing row launch
 // the row engine's grid never exceeds sm_count() * kRowsMaxCtasPerSm blocks
 int64_t csr_partials(int64_t /*n*/) { return (int64_t)sm_count() * kRowsMaxCtasPerSm; }
 
