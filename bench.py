@@ -405,7 +405,8 @@ def run_gb300(args):
 
 def run_kernels(args):
     """Times the row kernels alone on the --grid matrix (also the ncu target):
-    FP64 SpMV, one multicolour SOR sweep and the residual."""
+    FP64 SpMV, one multicolour SOR sweep, the residual and the FP32 SpMV; with
+    --vcycle also one V-cycle of the FP64 and of the mixed hierarchy."""
     import torch
 
     import lineal_gb300 as g
@@ -420,13 +421,39 @@ def run_kernels(args):
     x = torch.randn(n, dtype=torch.float64, device="cuda")
     y = torch.empty_like(x)
     b = torch.as_tensor(b_host, device="cuda")
+    a32 = g.gen_27pt(dims, k, storage=g.F32)
+    x32 = x.float()
+    y32 = torch.empty_like(x32)
+    kernels = [
+        ("spmv_fp64", lambda: g.spmv(a, x, out=y), csr_bytes(n, nnz, 8, 8)),
+        ("sor_sweep_fp64", lambda: g.sor_sweep(a, col, b, x, out=y),
+         csr_bytes(n, nnz, 8, 8) + 8 * n),
+        ("residual_fp64", lambda: g.residual(a, b, x, with_norm=False),
+         csr_bytes(n, nnz, 8, 8) + 8 * n),
+        ("spmv_fp32", lambda: g.spmv_f32(a32, x32, out=y32), csr_bytes(n, nnz, 4, 4)),
+    ]
+    # sweeps in the colouring's row order (no permutation traffic)
+    bp = g.permute(col, b)
+    xp = g.permute(col, x)
+    bp32, xp32 = bp.float(), xp.float()
+    kernels += [
+        ("sor_sweep_permuted_fp64", lambda: g.sor_sweep_permuted(col, bp, xp),
+         csr_bytes(n, nnz, 8, 8) + 8 * n),
+        ("sor_sweep_permuted_fp32", lambda: g.sor_sweep_permuted(col, bp32, xp32),
+         csr_bytes(n, nnz, 4, 4) + 4 * n),
+    ]
+    if args.vcycle:
+        hier = {}
+        for tag, f32 in (("fp64", False), ("mixed", True)):
+            hier[tag] = g.HierarchyWright(min_coarsen_size=2000, cycle_f32=f32,
+                                          partition_size=args.partition_size,
+                                          partition_growth=args.partition_growth,
+                                          min_partitions=args.min_partitions).instantiate(
+                                              a, finest_colouring=col)
+        kernels.append(("vcycle_fp64", lambda: hier["fp64"].vcycle(b, out=y), 0))
+        kernels.append(("vcycle_mixed", lambda: hier["mixed"].vcycle(b, out=y), 0))
     out = {}
-    for name, fn, nbytes in (
-            ("spmv_fp64", lambda: g.spmv(a, x, out=y), csr_bytes(n, nnz, 8, 8)),
-            ("sor_sweep_fp64", lambda: g.sor_sweep(a, col, b, x, out=y),
-             csr_bytes(n, nnz, 8, 8) + 8 * n),
-            ("residual_fp64", lambda: g.residual(a, b, x, with_norm=False),
-             csr_bytes(n, nnz, 8, 8) + 8 * n)):
+    for name, fn, nbytes in kernels:
         for _ in range(args.warmup):
             fn()
         torch.cuda.synchronize()
@@ -438,8 +465,9 @@ def run_kernels(args):
         e1.record(stream)
         e1.synchronize()
         ms = e0.elapsed_time(e1) / args.steps
-        out[name] = {"ms": ms, "gbs": nbytes / (ms * 1e-3) / 1e9}
-        log(f"[kernels] {name}: {ms:.3f} ms {out[name]['gbs']:.0f} GB/s")
+        out[name] = {"ms": ms, "gbs": nbytes / (ms * 1e-3) / 1e9 if nbytes else None}
+        log(f"[kernels] {name}: {ms:.3f} ms" +
+            (f" {out[name]['gbs']:.0f} GB/s" if nbytes else ""))
     print(json.dumps({"grid": args.grid, "kernels": out}), flush=True)
 
 
@@ -457,6 +485,8 @@ def main():
     ap.add_argument("--cpu-sample-edge", type=int, default=64)
     ap.add_argument("--reference-iterations", type=int, default=0,
                     help="iterations of the full-size solve used to extrapolate the CPU sample")
+    ap.add_argument("--vcycle", action="store_true",
+                    help="--mode kernels: also time one FP64 and one mixed V-cycle")
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")

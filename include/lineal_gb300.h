@@ -145,6 +145,15 @@ lgx_status lgx_gen_27pt(const int64_t dims[3], const double *d_k, lgx_dtype stor
 lgx_status lgx_gen_7pt(const int64_t dims[3], const double *d_k, lgx_dtype storage,
                        lgx_stream stream, lgx_matrix **out);
 
+/* Configuration of the CSR row kernels (SpMV, residual, Jacobi, SOR) used by
+ * later launches, process-wide; no reference counterpart (tuning):
+ * 0-2 CTA tiles (two stages / one CTA per SM, one stage / two CTAs, two small
+ * stages / two CTAs), 3-6 warp tiles (4 warps x 1 stage, 4 x 2, 8 x 1, 8 x 2
+ * per CTA).  Every configuration gives bit-identical results.  Default 3, or
+ * the environment variable LGX_ROWS_CONFIG. */
+lgx_status lgx_row_engine_set(int config);
+int lgx_row_engine_get(void);
+
 /* ------------------------------------------------------------------------
  * Vector reductions and updates (component-wise/sink/accumulator.hpp:151-218,
  * vector-expression.hpp:67-92).  Reductions are deterministic: fixed block
@@ -214,6 +223,24 @@ lgx_status lgx_colouring_export(const lgx_colouring *c, int32_t *d_colour, int32
 lgx_status lgx_sor_sweep(const lgx_matrix *a, const lgx_colouring *c, double relax, int forward,
                          int ultra, const double *d_x_in, double *d_x_out, const double *d_b,
                          lgx_stream stream);
+
+/* Sweeps in the colouring's own row order: row r of the permuted space is
+ * row perm[r] of the matrix, colours occupy contiguous ranges, and the sweep
+ * updates d_x in place (the in-situ apply of broom.hpp:27-124) without the
+ * gathers and scatters of lgx_sor_sweep.  lgx_colouring_permute /
+ * lgx_colouring_unpermute move vectors between the natural and the permuted
+ * order (dst[r] = src[perm[r]] and dst[perm[r]] = src[r]).  The _f32 sweep
+ * computes in float with float values (the matrix's float storage, or a float
+ * copy of its values made by the first call) -- the smoother of the
+ * precision form. */
+lgx_status lgx_colouring_permute(const lgx_colouring *c, const double *d_src, double *d_dst,
+                                 lgx_stream stream);
+lgx_status lgx_colouring_unpermute(const lgx_colouring *c, const double *d_src, double *d_dst,
+                                   lgx_stream stream);
+lgx_status lgx_sor_sweep_permuted(const lgx_colouring *c, double relax, int forward, int ultra,
+                                  double *d_x, const double *d_b, lgx_stream stream);
+lgx_status lgx_sor_sweep_permuted_f32(lgx_colouring *c, float relax, int forward, int ultra,
+                                      float *d_x, const float *d_b, lgx_stream stream);
 
 /* ------------------------------------------------------------------------
  * Aggregation AMG (linear-solver/multigrid/).

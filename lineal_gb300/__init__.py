@@ -27,8 +27,9 @@ from . import build as _build
 __all__ = [
     "LinealError", "LinealLibraryMissing", "lib", "CsrMatrix", "StencilMatrix", "Colouring",
     "HierarchyWright", "Hierarchy", "pcg", "pbicgstab", "spmv", "residual", "jacobi_sweep",
-    "sor_sweep", "gen_27pt", "gen_7pt", "amg_strength", "amg_aggregate", "dot", "norm2sq",
-    "max_norm", "PRECON_NONE", "PRECON_JACOBI", "PRECON_SSOR", "PRECON_AMG",
+    "sor_sweep", "sor_sweep_permuted", "permute", "unpermute", "gen_27pt", "gen_7pt",
+    "amg_strength", "amg_aggregate", "dot", "norm2sq", "max_norm", "PRECON_NONE",
+    "PRECON_JACOBI", "PRECON_SSOR", "PRECON_AMG",
 ]
 
 PRECON_NONE, PRECON_JACOBI, PRECON_SSOR, PRECON_AMG = 0, 1, 2, 3
@@ -113,6 +114,10 @@ def _signatures(L):
     L.lgx_status_string.argtypes = [C.c_int]
     L.lgx_last_error.restype = C.c_char_p
     L.lgx_version.restype = C.c_char_p
+    L.lgx_row_engine_get.restype = C.c_int
+    L.lgx_row_engine_get.argtypes = []
+    L.lgx_row_engine_set.restype = C.c_int
+    L.lgx_row_engine_set.argtypes = [C.c_int]
     L.lgx_kernel_launches.restype = C.c_uint64
     L.lgx_kernel_launches.argtypes = []
     sigs = {
@@ -142,6 +147,10 @@ def _signatures(L):
         "lgx_colouring_destroy": [V],
         "lgx_colouring_export": [V, V, P(I32), V],
         "lgx_sor_sweep": [V, V, D, C.c_int, C.c_int, V, V, V, V],
+        "lgx_colouring_permute": [V, V, V, V],
+        "lgx_colouring_unpermute": [V, V, V, V],
+        "lgx_sor_sweep_permuted": [V, D, C.c_int, C.c_int, V, V, V],
+        "lgx_sor_sweep_permuted_f32": [V, C.c_float, C.c_int, C.c_int, V, V, V],
         "lgx_amg_setup": [V, P(_AmgParams), V, V, P(V)],
         "lgx_amg_destroy": [V],
         "lgx_amg_info": [V, P(I64), V, V, I64],
@@ -444,6 +453,47 @@ class Colouring:
             self.close()
         except Exception:
             pass
+
+
+def row_engine(config: int | None = None) -> int:
+    """Returns the CSR row-kernel configuration; sets it first when given."""
+    if config is not None:
+        _check(lib().lgx_row_engine_set(int(config)))
+    return int(lib().lgx_row_engine_get())
+
+
+def permute(colouring: Colouring, v):
+    """v in the colouring's row order (out[r] = v[perm[r]])."""
+    v = _dvec(v)
+    out = _empty(v.numel())
+    _check(lib().lgx_colouring_permute(colouring.handle, _ptr(v), _ptr(out), _stream()))
+    return out
+
+
+def unpermute(colouring: Colouring, v):
+    """Inverse of permute (out[perm[r]] = v[r])."""
+    v = _dvec(v)
+    out = _empty(v.numel())
+    _check(lib().lgx_colouring_unpermute(colouring.handle, _ptr(v), _ptr(out), _stream()))
+    return out
+
+
+def sor_sweep_permuted(colouring: Colouring, b_perm, x_perm, relax=1.0, forward=True,
+                       ultra=False):
+    """One multicolour SOR sweep in the colouring's row order, in place on
+    x_perm (float64 vectors: FP64 arithmetic; float32 vectors: the float
+    smoother of the precision form)."""
+    torch = _torch()
+    if x_perm.dtype == torch.float32:
+        b_perm = _dvec(b_perm, torch.float32)
+        _check(lib().lgx_sor_sweep_permuted_f32(colouring.handle, float(relax), int(forward),
+                                                int(ultra), _ptr(x_perm), _ptr(b_perm),
+                                                _stream()))
+    else:
+        b_perm = _dvec(b_perm)
+        _check(lib().lgx_sor_sweep_permuted(colouring.handle, float(relax), int(forward),
+                                            int(ultra), _ptr(x_perm), _ptr(b_perm), _stream()))
+    return x_perm
 
 
 def sor_sweep(a: CsrMatrix, colouring: Colouring, b, x_in=None, relax=1.0, forward=True,

@@ -32,17 +32,18 @@ int sm_count() {
   return n;
 }
 
-int rows_config() {
-  static const int c = [] {
-    // FP64 SpMV / SOR sweep at 256^3 (27-point, 449M nnz), ms:
-    //   CTA tiles kind 0 1.55 / 2.63, kind 1 1.37 / 1.98, kind 2 1.45 / 2.33;
-    //   warp tiles 3: 1.08 / 1.69, 4: 1.38 / 2.48, 5: 1.16 / 1.80, 6: 1.37 / 2.30
-    const char *e = std::getenv("LGX_ROWS_CONFIG");
-    const int v = e ? std::atoi(e) : 3;
-    return (v >= 0 && v <= 6) ? v : 3;
-  }();
-  return c;
-}
+// Row-engine configuration (see launch_rows).  FP64 SpMV / SOR sweep at
+// 256^3 (27-point, 449M nnz), ms:
+//   CTA tiles kind 0 1.55 / 2.63, kind 1 1.37 / 1.98, kind 2 1.45 / 2.33;
+//   warp tiles 3: 1.08 / 1.69, 4: 1.38 / 2.48, 5: 1.16 / 1.80, 6: 1.37 / 2.30
+// Default 3; LGX_ROWS_CONFIG or lgx_row_engine_set choose another.
+static std::atomic<int> g_rows_config{[] {
+  const char *e = std::getenv("LGX_ROWS_CONFIG");
+  const int v = e ? std::atoi(e) : 3;
+  return (v >= 0 && v <= 6) ? v : 3;
+}()};
+
+int rows_config() { return g_rows_config.load(std::memory_order_relaxed); }
 
 int *device_error_flag() {
   static int *p = [] {
@@ -661,6 +662,15 @@ lgx_status lgx_dot(int64_t n, const double *d_a, const double *d_b, double *d_ou
   LGX_CUDA(cudaStreamSynchronize(stream));
   return LGX_OK;
 }
+
+lgx_status lgx_row_engine_set(int config) {
+  if (config < 0 || config > 6)
+    return fail(LGX_ERR_INVALID, "row engine configuration must be in [0, 6]");
+  g_rows_config.store(config, std::memory_order_relaxed);
+  return LGX_OK;
+}
+
+int lgx_row_engine_get(void) { return rows_config(); }
 
 lgx_status lgx_dot_static(int64_t n, const double *d_a, const double *d_b, double *d_out,
                           lgx_stream stream) {

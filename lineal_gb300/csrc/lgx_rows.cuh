@@ -483,7 +483,8 @@ inline lgx_status launch_rows(int64_t rb, int64_t re, const Csr &a, const VT *va
                               cudaStream_t s) {
   if (re <= rb) return LGX_OK;
   bool done = false;
-  switch (rows_config()) {
+  const int cfg = rows_config();
+  switch (cfg) {
     case 3: LGX_CHECK((launch_wrows<VT, Op, 4, 1>(rb, re, a, val, op, s, &done))); break;
     case 4: LGX_CHECK((launch_wrows<VT, Op, 4, 2>(rb, re, a, val, op, s, &done))); break;
     case 5: LGX_CHECK((launch_wrows<VT, Op, 8, 1>(rb, re, a, val, op, s, &done))); break;
@@ -491,7 +492,7 @@ inline lgx_status launch_rows(int64_t rb, int64_t re, const Csr &a, const VT *va
     default: break;
   }
   if (done) return LGX_OK;
-  switch (rows_config()) {
+  switch (cfg) {
     case 0:
       return launch_rows_cfg<VT, Op, 0>(rb, re, a.max_row, a.rowptr.p, a.col.p, val, op, s);
     case 2:

@@ -481,4 +481,36 @@ lgx_status lgx_sor_sweep(const lgx_matrix *a, const lgx_colouring *c, double rel
                                  d_x_out, d_b, stream);
 }
 
+lgx_status lgx_colouring_permute(const lgx_colouring *c, const double *d_src, double *d_dst,
+                                 lgx_stream stream) {
+  if (!c || (c->n > 0 && (!d_src || !d_dst))) return fail(LGX_ERR_INVALID, "null argument");
+  return gather<double, double>(c->n, c->perm.p, d_src, d_dst, stream);
+}
+
+lgx_status lgx_colouring_unpermute(const lgx_colouring *c, const double *d_src, double *d_dst,
+                                   lgx_stream stream) {
+  if (!c || (c->n > 0 && (!d_src || !d_dst))) return fail(LGX_ERR_INVALID, "null argument");
+  return scatter<double, double>(c->n, c->perm.p, d_src, d_dst, stream);
+}
+
+lgx_status lgx_sor_sweep_permuted(const lgx_colouring *c, double relax, int forward, int ultra,
+                                  double *d_x, const double *d_b, lgx_stream stream) {
+  if (!c || (c->n > 0 && (!d_x || !d_b))) return fail(LGX_ERR_INVALID, "null argument");
+  if (c->pcsr.storage == LGX_F64)
+    return mc_sor_sweep<double, double>(*c, c->pcsr.v64.p, relax, forward, ultra, d_b, d_x,
+                                        stream);
+  return mc_sor_sweep<float, double>(*c, c->pcsr.v32.p, relax, forward, ultra, d_b, d_x, stream);
+}
+
+lgx_status lgx_sor_sweep_permuted_f32(lgx_colouring *c, float relax, int forward, int ultra,
+                                      float *d_x, const float *d_b, lgx_stream stream) {
+  if (!c || (c->n > 0 && (!d_x || !d_b))) return fail(LGX_ERR_INVALID, "null argument");
+  const float *v = c->pcsr.v32.p;
+  if (c->pcsr.storage == LGX_F64) {
+    LGX_CHECK(colouring_make_f32(*c, stream));
+    v = c->pv32.p;
+  }
+  return mc_sor_sweep<float, float>(*c, v, relax, forward, ultra, d_b, d_x, stream);
+}
+
 }  // extern "C"

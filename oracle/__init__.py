@@ -400,6 +400,19 @@ def sor_sweep(a: Csr, b, x_in=None, relax=1.0, forward=True, ultra=False, nparts
     return out
 
 
+def sor_sweep_f32(a: Csr, b, order, x_in=None, relax=1.0, forward=True,
+                  ultra=False) -> np.ndarray:
+    """Ordered SOR sweep in float arithmetic (the precision form's smoother)."""
+    c = a._c()
+    b = np.ascontiguousarray(b, dtype=np.float32)
+    out = np.zeros(a.n, dtype=np.float32)
+    xi = None if x_in is None else np.ascontiguousarray(x_in, dtype=np.float32)
+    o = np.ascontiguousarray(order, dtype=np.int32)
+    lib().lo_sor_sweep_ordered_f32(C.byref(c), C.c_float(relax), None if xi is None else _ptr(xi),
+                                   _ptr(out), _ptr(b), int(forward), int(ultra), _ptr(o))
+    return out
+
+
 def colour_jp(a: Csr, seed: int):
     c = a._c()
     col = np.empty(a.n, dtype=np.int32)

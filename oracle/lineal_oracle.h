@@ -135,6 +135,9 @@ void lo_sor_sweep(const lo_csr *a, double relax, const double *x_in, double *x_o
  * multicolour sweep the GPU performs. */
 void lo_sor_sweep_ordered(const lo_csr *a, double relax, const double *x_in, double *x_out,
                           const double *b, int forward, int ultra, const int32_t *order);
+/* lo_sor_sweep_ordered in float arithmetic on float-rounded values */
+void lo_sor_sweep_ordered_f32(const lo_csr *a, float relax, const float *x_in, float *x_out,
+                              const float *b, int forward, int ultra, const int32_t *order);
 
 /* Jones-Plassmann colouring with priority hash(seed, i), ties by index.
  * Deterministic; returns the number of colours. */

@@ -97,6 +97,42 @@ void lo_sor_sweep_ordered(const lo_csr *a, double relax, const double *x_in, dou
   free(rank);
 }
 
+/* The float smoother of the precision form: the row of sor_row in float
+ * arithmetic (fmaf, float division) on the matrix values rounded to float,
+ * rows visited in `order` (rank-based new/old choice, so ultra adds no
+ * off-range term). */
+void lo_sor_sweep_ordered_f32(const lo_csr *a, float relax, const float *x_in, float *x_out,
+                              const float *b, int forward, int ultra, const int32_t *order) {
+  const float m1 = 1.0f - relax;
+  const int64_t n = a->n;
+  int32_t *rank = (int32_t *)malloc((size_t)(n > 0 ? n : 1) * sizeof(int32_t));
+  for (int64_t k = 0; k < n; ++k) rank[order[k]] = (int32_t)k;
+  for (int64_t kk = 0; kk < n; ++kk) {
+    const int64_t i = order[forward ? kk : n - 1 - kk];
+    float accum = b[i], diag = 0.0f;
+    const float xi = x_in ? x_in[i] : 0.0f;
+    for (int64_t e = a->rowptr[i]; e < a->rowptr[i + 1]; ++e) {
+      const int64_t j = a->col[e];
+      const float aij = (float)a->val[e];
+      if (j == i) {
+        diag = aij;
+        if (ultra) accum = fmaf(-aij, xi, accum);
+        continue;
+      }
+      const int use_new = forward ? (rank[j] < rank[i]) : (rank[j] > rank[i]);
+      const float xj = use_new ? x_out[j] : (x_in ? x_in[j] : 0.0f);
+      accum = fmaf(-aij, xj, accum);
+    }
+    if (ultra) {
+      x_out[i] = xi + relax * accum / fabsf(diag);
+    } else {
+      const float quot = accum / diag;
+      x_out[i] = fmaf(relax, quot, m1 * xi);
+    }
+  }
+  free(rank);
+}
+
 /* ---- Cholesky (cholesky/decomposition.hpp:52-107) -------------------- */
 int lo_cholesky_factor(const lo_csr *a, double *l) {
   const int64_t n = a->n;
