@@ -57,6 +57,11 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def red_black_colours(dims):
+    i, j, k = np.meshgrid(*[np.arange(d, dtype=np.int32) for d in dims], indexing="ij")
+    return ((i + j + k) % 2).ravel().astype(np.int32)
+
+
 def parity_colours(dims):
     i, j, k = np.meshgrid(*[np.arange(d, dtype=np.int32) for d in dims], indexing="ij")
     return ((i % 2) * 4 + (j % 2) * 2 + (k % 2)).ravel().astype(np.int32)
@@ -198,6 +203,53 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 # GB300 arm
 # ---------------------------------------------------------------------------
+def precision_form(g, args, stream):
+    """The precision form on its own workload: 7-point lognormal(sigma=3)
+    diffusion (seed 2) at --grid^3 solved to 1e-10 by the plain FP64 AMG-PCG
+    and by flexible CG over the float V-cycle; residuals verified in FP64."""
+    import torch
+
+    dims, k, b_host = make_problem(args.grid, seed_k=2, seed_b=0, sigma=3.0)
+    a = g.gen_7pt(dims, k)
+    col = g.Colouring.from_array(a, red_black_colours(dims), 2)
+    b = torch.as_tensor(b_host, device="cuda")
+    bn = float(torch.linalg.norm(b).item())
+    hier_kw = dict(min_coarsen_size=2000, partition_size=args.partition_size,
+                   partition_growth=args.partition_growth, min_partitions=args.min_partitions)
+    out = {"workload": f"{args.grid}^3 7-point lognormal(sigma=3, seed 2), AMG-PCG to 1e-10",
+           "rows": a.row_num(), "nnz": a.non_zero_num()}
+    xs = {}
+    for tag, f32, flexible in (("fp64", False, False), ("mixed_fcg", True, True)):
+        t0 = time.perf_counter()
+        h = g.HierarchyWright(cycle_f32=f32, **hier_kw).instantiate(a, finest_colouring=col)
+        torch.cuda.synchronize()
+        setup = time.perf_counter() - t0
+        for _ in range(args.warmup):
+            res = g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=1e-10, maxit=1000,
+                        flexible=flexible)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            res = g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=1e-10, maxit=1000,
+                        flexible=flexible)
+        e1.record(stream)
+        e1.synchronize()
+        _, rn = g.residual(a, b, res.x)
+        xs[tag] = res.x
+        out[tag] = {"ms": e0.elapsed_time(e1) / args.steps, "iterations": res.iterations,
+                    "rel_residual_fp64": float(np.sqrt(rn)) / bn, "setup_ms": setup * 1e3,
+                    "levels": h.sizes()[0]}
+        log(f"[precision] {tag}: {out[tag]['ms']:.1f} ms, {res.iterations} it, "
+            f"rel {out[tag]['rel_residual_fp64']:.2e}")
+        del h
+    out["mixed_fcg"]["rel_error_vs_fp64_solution"] = float(
+        torch.linalg.norm(xs["mixed_fcg"] - xs["fp64"]).item() /
+        torch.linalg.norm(xs["fp64"]).item())
+    out["speedup_vs_fp64"] = out["fp64"]["ms"] / out["mixed_fcg"]["ms"]
+    return out
+
 def run_gb300(args):
     import torch
 
@@ -357,6 +409,8 @@ def run_gb300(args):
         log(f"[gb300] e2e {e2e['value']:.0f} ms")
 
     # ---- CPU baseline (bounded sample) -----------------------------------------
+    prec = precision_form(g, args, stream) if args.precision_form else None
+
     cpu = None
     if rank == 0 and args.cpu_baseline:
         threads = os.cpu_count() or 1
@@ -388,7 +442,8 @@ def run_gb300(args):
         "spmv": {"fp64_ms": t_spmv64, "fp64_gbs": gbs64, "fp64_frac": gbs64 / peak,
                  "fp32_ms": t_spmv32, "fp32_gbs": gbs32, "fp32_frac": gbs32 / peak,
                  "bytes_fp64": bytes64, "bytes_fp32": bytes32},
-        "roofline": {"bound": "hbm", "kernel": "k_csr_spmv<double,double>",
+        "precision_form": prec,
+        "roofline": {"bound": "hbm", "kernel": "k_wrows<double, SpmvOp<double,double>, 4, 1>",
                      "achieved": gbs64, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": gbs64 / peak, "traffic": args.spmv_traffic},
         "cpu_baseline": cpu,
@@ -487,6 +542,8 @@ def main():
                     help="iterations of the full-size solve used to extrapolate the CPU sample")
     ap.add_argument("--vcycle", action="store_true",
                     help="--mode kernels: also time one FP64 and one mixed V-cycle")
+    ap.add_argument("--no-precision-form", dest="precision_form", action="store_false",
+                    help="skip the 7-point sigma=3 precision-form solves")
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")

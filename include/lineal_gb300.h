@@ -339,6 +339,10 @@ typedef struct {
   int64_t rere_period;          /* 0 disables true-residual recomputation */
   int use_graphs;               /* capture each iteration (SpMV, reductions, updates and
                                    the whole V-cycle) in a CUDA graph and replay it */
+  int flexible;                 /* CG: flexible CG, beta = r+.(z+ - z) / r.z (Notay 2000),
+                                   for preconditioners that are not exactly linear (the
+                                   float V-cycle of the precision form); no counterpart
+                                   in the reference's CG (solver.hpp:105-107) */
 } lgx_solve_params;
 
 void lgx_solve_default_params(lgx_solve_params *p);

@@ -457,6 +457,7 @@ template <lgx_krylov_kind tKind, typename TPrecon>
 struct KrylovSolver : SharedNonStationaryIterativeSolverBase {
   std::size_t rere_period = 8;  // rere_controller: iter > 0 && iter % 8 == 0
   std::optional<TPrecon> precon;
+  bool flexible = false;        // CG: flexible beta (float V-cycle preconditioners)
 
   KrylovSolver() = default;
   explicit KrylovSolver(TPrecon p, std::size_t rere = 8) : rere_period(rere), precon(std::move(p)) {}
@@ -474,6 +475,7 @@ struct KrylovSolver : SharedNonStationaryIterativeSolverBase {
         lgx_solve_params p;
         lgx_solve_default_params(&p);
         p.rere_period = (int64_t)inst.solver.rere_period;
+        p.flexible = inst.solver.flexible ? 1 : 0;
         if constexpr (std::is_same_v<TPrecon, JacobiSolver>) {
           p.precon = LGX_PRECON_JACOBI;
           p.relax = inst.solver.precon->relax;

@@ -86,6 +86,7 @@ class _SolveParams(C.Structure):
         ("maxit", C.c_int64),
         ("rere_period", C.c_int64),
         ("use_graphs", C.c_int),
+        ("flexible", C.c_int),
     ]
 
 
@@ -631,7 +632,7 @@ class SolveResult:
 
 def _solve(fn, a: _Matrix, b, x0=None, precon=PRECON_NONE, relax=1.0, ultra=False,
            colouring: Colouring | None = None, amg: Hierarchy | None = None, rtol=1e-8,
-           maxit=1000, rere_period=8, use_graphs=True) -> SolveResult:
+           maxit=1000, rere_period=8, use_graphs=True, flexible=False) -> SolveResult:
     b = _dvec(b)
     x = _dvec(x0) if x0 is not None else _empty(b.numel()).zero_()
     if x0 is not None:
@@ -647,6 +648,7 @@ def _solve(fn, a: _Matrix, b, x0=None, precon=PRECON_NONE, relax=1.0, ultra=Fals
     p.maxit = maxit
     p.rere_period = rere_period
     p.use_graphs = int(use_graphs)
+    p.flexible = int(flexible)
     it = C.c_int64()
     rel = C.c_double()
     hist = np.zeros(maxit + 1)
@@ -656,7 +658,8 @@ def _solve(fn, a: _Matrix, b, x0=None, precon=PRECON_NONE, relax=1.0, ultra=Fals
 
 
 def pcg(a: _Matrix, b, **kw) -> SolveResult:
-    """Preconditioned CG (ConjugateGradientsSolver)."""
+    """Preconditioned CG (ConjugateGradientsSolver); flexible=True selects the
+    flexible-CG beta for the float V-cycle of the precision form."""
     return _solve(lib().lgx_pcg, a, b, **kw)
 
 

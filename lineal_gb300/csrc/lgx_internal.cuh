@@ -131,6 +131,8 @@ struct lgx_colouring {
   lgx::DBuf<int32_t> iperm;      // natural -> permuted
   lgx::Csr pcsr;                 // permuted matrix (values in the source storage type)
   lgx::DBuf<float> pv32;         // float copy of the permuted values (float cycles)
+  lgx::DBuf<double> rdiag;       // FP64 values: 1 / a_rr correctly rounded, or 0 where
+                                 // the SOR row must divide (permuted order)
   lgx::DBuf<double> work_b, work_x;  // natural<->permuted staging for the public sweep API
 };
 

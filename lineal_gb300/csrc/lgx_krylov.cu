@@ -37,7 +37,7 @@ __device__ __forceinline__ void set_flags(KScalars *ks, double num, double den) 
   if (den == 0.0) ks->flag |= 1;
 }
 
-enum Post { POST_ALPHA = 0, POST_RHO_BETA = 1, POST_OMEGA = 2, POST_RHO = 3 };
+enum Post { POST_ALPHA = 0, POST_RHO_BETA = 1, POST_OMEGA = 2, POST_RHO = 3, POST_FCG = 4 };
 
 // dot(a, b) with a post operation in the last block
 __global__ void __launch_bounds__(kKT)
@@ -86,6 +86,11 @@ __global__ void __launch_bounds__(kKT)
     if (post == POST_OMEGA) {  // omega = (t.r) / (t.t)
       set_flags(ks, u1, t2);
       ks->omega = u1 / t2;
+    } else if (post == POST_FCG) {  // rho = r.z, beta = (r.z - r.z_old) / rho_old
+      ks->rho_old = ks->rho;
+      ks->rho = u1;
+      set_flags(ks, u1, ks->rho_old);
+      ks->beta = (u1 - t2) / ks->rho_old;
     }
   }
 }
@@ -134,6 +139,18 @@ __global__ void k_xpby(int64_t n, const KScalars *ks, const double *__restrict__
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
     p[i] = fma(p[i], beta, z[i]);
+}
+
+// p = z + beta p and z_old = z (flexible CG)
+__global__ void k_xpby_save(int64_t n, const KScalars *ks, const double *__restrict__ z,
+                            double *__restrict__ p, double *__restrict__ z_old) {
+  const double beta = ks->beta;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double zi = z[i];
+    p[i] = fma(p[i], beta, zi);
+    z_old[i] = zi;
+  }
 }
 
 // x += s y with s = ks->alpha (which == 0) or ks->omega (which == 1)
@@ -363,7 +380,8 @@ static lgx_status krylov_init(lgx_krylov &K, const double *d_b, const double *d_
   Solver &S = K.S;
   const int64_t n = S.n;
   const bool cg = K.kind == LGX_KRYLOV_CG;
-  LGX_CHECK(K.V.alloc(cg ? 5 : 8, n));
+  const bool flexible = cg && K.p.flexible && S.precon != LGX_PRECON_NONE;
+  LGX_CHECK(K.V.alloc(cg ? (flexible ? 6 : 5) : 8, n));
   double *b = K.V[0], *x = K.V[1], *r = K.V[2];
   cudaStream_t s = S.s;
   if (S.perm) {
@@ -383,6 +401,8 @@ static lgx_status krylov_init(lgx_krylov &K, const double *d_b, const double *d_
       LGX_CHECK(S.precondition(r, pd));
       k_dot_post<<<rg, kKT, 0, s>>>(n, pd, r, POST_RHO, ks, S.partials.p, S.counters.p);
       LGX_LAUNCH_CHECK();
+      if (flexible)
+        LGX_CUDA(cudaMemcpyAsync(K.V[5], pd, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
     } else {
       LGX_CUDA(cudaMemcpyAsync(pd, r, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
       k_cg_plain_rho<<<1, 1, 0, s>>>(ks);
@@ -426,7 +446,14 @@ static lgx_status cg_iterate(lgx_krylov &K) {
       LGX_LAUNCH_CHECK();
     }
   }
-  if (precon) {
+  if (precon && K.p.flexible) {
+    double *z_old = K.V[5];
+    LGX_CHECK(S.precondition(r, q));
+    k_dot2_post<<<rg, kKT, 0, s>>>(n, r, q, r, z_old, POST_FCG, ks, S.partials.p,
+                                   S.partials2.p, S.counters.p, S.counters.p + 1);
+    LGX_LAUNCH_CHECK();
+    k_xpby_save<<<S.vgrid(), 256, 0, s>>>(n, ks, q, pd, z_old);
+  } else if (precon) {
     LGX_CHECK(S.precondition(r, q));
     k_dot_post<<<rg, kKT, 0, s>>>(n, r, q, POST_RHO_BETA, ks, S.partials.p, S.counters.p);
     LGX_LAUNCH_CHECK();
@@ -592,6 +619,7 @@ void lgx_solve_default_params(lgx_solve_params *p) {
   p->maxit = 1000;
   p->rere_period = 8;
   p->use_graphs = 1;
+  p->flexible = 0;
 }
 
 lgx_status lgx_pcg(const lgx_matrix *a, const double *d_b, double *d_x,

@@ -146,6 +146,7 @@ __device__ __forceinline__ void issue_tile(const int64_t *rowptr, const int32_t 
 }
 
 // Op interface:
+//   using X = <type of the gathered vector entries>;
 //   template <int W> __device__ double row(int64_t row, const int32_t *c, const VT *v,
 //                                          int len) const;
 //     (returns the row's contribution to an optional sum; W = entries whose
@@ -305,21 +306,22 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-template <int WPC>
+// XT = the type of the gathered x values (Op::X)
+template <int WPC, typename XT>
 struct WrowsBounds {
   // 4 warps per CTA: registers <= 65536 / (5 * 128) so that five CTAs (20
-  // warps) fit an SM, and 8 gathers per round to stay within them;
-  // 8 warps per CTA: two CTAs (16 warps), 16 gathers per round
+  // warps) fit an SM, and 8 double (16 float) gathers per round to stay
+  // within them; 8 warps per CTA: two CTAs (16 warps), 16 gathers per round
   static constexpr int min_blocks = WPC == 4 ? 5 : 2;
-  static constexpr int gather = WPC == 4 ? 8 : 16;
+  static constexpr int gather = (WPC == 4 && sizeof(XT) == 8) ? 8 : 16;
 };
 
 template <typename VT, class Op, int WPC, int S>
-__global__ void __launch_bounds__(WPC * 32, WrowsBounds<WPC>::min_blocks)
+__global__ void __launch_bounds__(WPC * 32, WrowsBounds<WPC, typename Op::X>::min_blocks)
   k_wrows(int64_t rb, int64_t re, int capw, const int64_t *__restrict__ rowptr,
           const int32_t *__restrict__ col, const VT *__restrict__ val, Op op, int *err) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int W = WrowsBounds<WPC>::gather;
+  constexpr int W = WrowsBounds<WPC, typename Op::X>::gather;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const size_t sb = wstage_bytes(capw, sizeof(VT));
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw) + warp * S;

@@ -26,6 +26,7 @@ struct JacobiOp {
   double *x_out;
   const double *b;
   double relax, m1;
+  using X = double;
   static constexpr bool kReduce = false;
   double *partials = nullptr;
   unsigned *counter = nullptr;
@@ -214,6 +215,21 @@ __global__ void k_perm_fill(int64_t n, const int64_t *rowptr, const int32_t *col
   }
 }
 
+// Reciprocal of every permuted row's diagonal, rounded once by the IEEE
+// division; 0 marks rows whose diagonal lies outside [2^-400, 2^400] in
+// magnitude (or is not finite), where the sweep divides directly.
+__global__ void k_colour_rdiag(int64_t n, const int64_t *rowptr, const int32_t *col,
+                               const double *val, double *rdiag) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    double d = 0.0;
+    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k)
+      if (col[k] == r) d = val[k];
+    const int e = (int)((__double_as_longlong(d) >> 52) & 0x7ff);
+    rdiag[r] = (e > 1023 - 400 && e < 1023 + 400) ? 1.0 / d : 0.0;
+  }
+}
+
 __global__ void k_to_f32(int64_t n, const double *src, float *dst) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
@@ -283,6 +299,11 @@ lgx_status colouring_build(const Csr &a, const int32_t *d_colour, int32_t ncolou
                                          p.rowptr.p, p.col.p, p.v32.p);
   }
   LGX_LAUNCH_CHECK();
+  if (a.storage == LGX_F64 && n > 0) {
+    LGX_CHECK(out.rdiag.alloc(n));
+    k_colour_rdiag<<<g, 256, 0, s>>>(n, p.rowptr.p, p.col.p, p.v64.p, out.rdiag.p);
+    LGX_LAUNCH_CHECK();
+  }
   return csr_compute_max_window(p, s);
 }
 
@@ -296,15 +317,51 @@ lgx_status colouring_make_f32(lgx_colouring &c, cudaStream_t s) {
 }
 
 // ---- multicolour SOR -------------------------------------------------------
+// a / d rounded to nearest from y = RN(1/d): q0 = a*y is within 1.5 ulp of
+// a/d, one correction q1 = q0 + (a - d*q0)*y makes it faithful, and a second
+// one with the then exact residual gives the correctly rounded quotient
+// (P. Markstein, "Computation of elementary functions on the IBM RISC
+// System/6000 processor", IBM J. Res. Dev. 34(1), 1990: a faithful quotient
+// corrected once with the correctly rounded reciprocal rounds correctly).
+// Five FP64 operations instead of a full division.  Valid while a and d stay
+// within [2^-400, 2^400] in magnitude; the caller checks a, the reciprocal
+// table marks d.
+__device__ __forceinline__ double div_by_recip(double a, double d, double y) {
+  const double q0 = a * y;
+  const double r0 = fma(-d, q0, a);
+  const double q1 = fma(r0, y, q0);
+  const double r1 = fma(-d, q1, a);
+  return fma(r1, y, q1);
+}
+
+// integer tests on the bit pattern (they keep FP64 comparisons off the FP64
+// pipe)
+__device__ __forceinline__ int exponent_field(double v) {
+  return (int)((__double_as_longlong(v) >> 52) & 0x7ff);
+}
+__device__ __forceinline__ bool exponent_within_400(double v) {
+  const int e = exponent_field(v);
+  return e > 1023 - 400 && e < 1023 + 400;
+}
+__device__ __forceinline__ bool nonzero_bits(double v) {
+  return (__double_as_longlong(v) << 1) != 0;
+}
+
 // One row of gauss-seidel-variant/sweep.hpp:134-200 in place: rows of other
 // colours already visited in this sweep hold their new values in x, the rest
 // their input values; rows of the same colour are never adjacent.
+// With rdiag (FP64 values and vectors) the regular row divides through the
+// reciprocal table (same quotient), and relax == 1 skips the (1 - relax) x_i
+// term where it cannot change the result (q nonzero, x_i finite).
 template <typename VT, typename XT>
 struct SorOp {
   const XT *b;
   XT *x;
   XT relax, m1;
   int ultra;
+  const double *rdiag = nullptr;
+  int relax_one = 0;
+  using X = XT;
   static constexpr bool kReduce = false;
   double *partials = nullptr;
   unsigned *counter = nullptr;
@@ -333,10 +390,21 @@ struct SorOp {
     }
     if (ultra) {
       x[i] = xi + relax * accum / fabs(diag);
-    } else {
-      const XT quot = accum / diag;
-      x[i] = fma(relax, quot, m1 * xi);
+      return 0.0;
     }
+    XT quot;
+    if constexpr (sizeof(XT) == 8) {
+      const double y = rdiag ? rdiag[i] : 0.0;
+      quot = (nonzero_bits(y) && exponent_within_400(accum)) ? div_by_recip(accum, diag, y)
+                                                             : accum / diag;
+      if (relax_one && nonzero_bits(quot) && exponent_field(xi) != 0x7ff) {
+        x[i] = quot;  // fma(1, q, 0 * x_i) == q for nonzero q and finite x_i
+        return 0.0;
+      }
+    } else {
+      quot = accum / diag;
+    }
+    x[i] = fma(relax, quot, m1 * xi);
     return 0.0;
   }
   __device__ __forceinline__ void finish(double) const {}
@@ -346,7 +414,11 @@ template <typename VT, typename XT>
 lgx_status mc_sor_sweep(const lgx_colouring &c, const VT *val, double relax, int forward,
                         int ultra, const XT *b, XT *x, cudaStream_t s) {
   const Csr &p = c.pcsr;
-  const SorOp<VT, XT> op{b, x, (XT)relax, XT(1) - (XT)relax, ultra};
+  SorOp<VT, XT> op{b, x, (XT)relax, XT(1) - (XT)relax, ultra};
+  if constexpr (sizeof(VT) == 8 && sizeof(XT) == 8) {
+    op.rdiag = c.rdiag.p;
+    op.relax_one = relax == 1.0;
+  }
   for (int32_t k = 0; k < c.ncolours; ++k) {
     const int32_t col_id = forward ? k : c.ncolours - 1 - k;
     const int64_t rb = c.offsets[col_id], re = c.offsets[col_id + 1];

@@ -23,6 +23,7 @@ template <typename VT, typename XT>
 struct SpmvOp {
   const XT *x;
   XT *y;
+  using X = XT;
   static constexpr bool kReduce = false;
   double *partials = nullptr;
   unsigned *counter = nullptr;
@@ -40,6 +41,7 @@ struct ResidualOp {
   const XT *b, *x;
   XT *r;
   double *out;
+  using X = XT;
   static constexpr bool kReduce = NORM;
   double *partials;
   unsigned *counter;

@@ -112,3 +112,26 @@ def test_sor_permuted_matches_natural_and_oracle(engine, config, forward):
 def test_row_engine_rejects_unknown_configuration(cuda):
     with pytest.raises(cuda.LinealError):
         cuda.row_engine(7)
+
+
+@pytest.mark.parametrize("relax", [1.0, 0.7])
+def test_sor_division_through_reciprocals(engine, relax):
+    """The FP64 sweep divides through a table of correctly rounded
+    reciprocals; two million rows of a 7-point matrix with diagonals spread
+    over 2^-30..2^30 and right-hand sides over 2^-300..2^300 (some beyond
+    2^400, which take the direct division) give the oracle's quotients."""
+    dims = (128, 128, 128)
+    n = int(np.prod(dims))
+    rng = np.random.default_rng(21)
+    k = np.exp(rng.uniform(-20.0, 20.0, n))
+    ref = lo.gen_7pt(dims, k)
+    m = engine.CsrMatrix.from_host(ref.rowptr, ref.col, ref.val)
+    colours = ((np.arange(n) % 128) + (np.arange(n) // 128) % 128 + np.arange(n) // 16384) % 2
+    col = engine.Colouring.from_array(m, colours.astype(np.int32), 2)
+    order = lo.colour_order(colours.astype(np.int32), 2)
+    b = rng.uniform(-1, 1, n) * np.exp2(rng.uniform(-300, 300, n))
+    b[::1000] *= 2.0 ** 500
+    x = rng.uniform(-1, 1, n)
+    got = engine.sor_sweep(m, col, b, x, relax=relax).cpu().numpy()
+    want = lo.sor_sweep(ref, b, x_in=x, relax=relax, order=order)
+    np.testing.assert_array_equal(got, want)

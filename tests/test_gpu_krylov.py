@@ -118,3 +118,32 @@ def test_breakdown_reported_as_status(cuda):
     with pytest.raises(cuda.LinealError) as e:
         cuda.pcg(csr, b, rtol=1e-8, maxit=5)
     assert e.value.status in (4, 5)
+
+
+def test_flexible_cg_precision_form(cuda):
+    """Precision form: flexible CG over the float V-cycle reaches 1e-10 on a
+    high-contrast 7-point problem (lognormal sigma = 3), verified in FP64 on
+    the oracle, within a few iterations of the plain FP64 AMG-PCG; on a
+    linear (FP64) preconditioner flexible CG follows plain CG."""
+    dims = (24, 24, 24)
+    n = int(np.prod(dims))
+    k = np.exp(3.0 * np.random.default_rng(2).standard_normal(n))
+    ref = lo.gen_7pt(dims, k)
+    b = np.random.default_rng(0).uniform(-1, 1, n)
+    m = cuda.gen_7pt(dims, k)
+    params = dict(min_coarsen_size=200, partition_size=1000)
+    h64 = cuda.HierarchyWright(**params).instantiate(m)
+    h32 = cuda.HierarchyWright(cycle_f32=True, **params).instantiate(m)
+    plain = cuda.pcg(m, b, precon=cuda.PRECON_AMG, amg=h64, rtol=1e-10, maxit=500)
+    flex64 = cuda.pcg(m, b, precon=cuda.PRECON_AMG, amg=h64, rtol=1e-10, maxit=500,
+                      flexible=True)
+    flex32 = cuda.pcg(m, b, precon=cuda.PRECON_AMG, amg=h32, rtol=1e-10, maxit=500,
+                      flexible=True)
+    for res in (plain, flex64, flex32):
+        assert res.rel_residual <= 1e-10
+        xr = res.x.cpu().numpy()
+        assert np.linalg.norm(b - lo.spmv(ref, xr)) <= 1.2e-10 * np.linalg.norm(b)
+    assert abs(flex64.iterations - plain.iterations) <= 2
+    assert flex32.iterations <= plain.iterations + max(2, plain.iterations // 10)
+    x64 = plain.x.cpu().numpy()
+    assert np.linalg.norm(flex32.x.cpu().numpy() - x64) <= 1e-7 * np.linalg.norm(x64)

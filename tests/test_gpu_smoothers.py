@@ -56,10 +56,11 @@ def test_jp_colouring_matches_oracle(cuda, npts):
     assert nc == rnc
 
 
+@pytest.mark.parametrize("relax", [0.9, 1.0])
 @pytest.mark.parametrize("forward", [True, False])
 @pytest.mark.parametrize("ultra", [False, True])
 @pytest.mark.parametrize("with_input", [False, True])
-def test_multicolour_sor_bitexact(cuda, forward, ultra, with_input):
+def test_multicolour_sor_bitexact(cuda, forward, ultra, with_input, relax):
     ref, _ = _case()
     m = cuda.CsrMatrix.from_host(ref.rowptr, ref.col, ref.val)
     col = cuda.Colouring.jp(m, seed=7)
@@ -68,8 +69,9 @@ def test_multicolour_sor_bitexact(cuda, forward, ultra, with_input):
     rng = np.random.default_rng(11)
     b = rng.uniform(-1, 1, ref.n)
     x_in = rng.uniform(-1, 1, ref.n) if with_input else None
-    got = cuda.sor_sweep(m, col, b, x_in, relax=0.9, forward=forward, ultra=ultra)
-    want = lo.sor_sweep(ref, b, x_in=x_in, relax=0.9, forward=forward, ultra=ultra, order=order)
+    got = cuda.sor_sweep(m, col, b, x_in, relax=relax, forward=forward, ultra=ultra)
+    want = lo.sor_sweep(ref, b, x_in=x_in, relax=relax, forward=forward, ultra=ultra,
+                        order=order)
     np.testing.assert_array_equal(got.cpu().numpy(), want)
 
 
