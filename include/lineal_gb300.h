@@ -375,6 +375,24 @@ lgx_status lgx_krylov_state(const lgx_krylov *k, int64_t *iteration, double *res
 lgx_status lgx_krylov_solution(lgx_krylov *k, double *d_x);
 lgx_status lgx_krylov_destroy(lgx_krylov *k);
 
+/* ------------------------------------------------------------------------
+ * Differentiation form: for x = A(theta)^-1 b and a loss L(x) the adjoint
+ * lambda = A^-T dL/dx is one more Krylov solve (lgx_pcg when A is symmetric,
+ * lgx_pbicgstab on the transpose otherwise) and dL/dtheta = -lambda^T
+ * (dA/dtheta) x.  No reference counterpart (lineal has no derivatives).
+ * ---------------------------------------------------------------------- */
+/* d_out[e] = alpha * d_u[row(e)] * d_v[col(e)] for every stored entry e of
+ * the CSR matrix a, in storage order: the outer product u v^T sampled on the
+ * sparsity pattern (alpha = -1, u = lambda, v = x gives dL/dA on the
+ * pattern).  d_out holds nnz doubles. */
+lgx_status lgx_sampled_outer(const lgx_matrix *a, double alpha, const double *d_u,
+                             const double *d_v, double *d_out, lgx_stream stream);
+/* dL/dtheta for the 7-point operator of lgx_gen_7pt with k = exp(theta) per
+ * cell (harmonic-mean faces, 2 k on axis-0 boundary faces), given
+ * k, lambda and x: one deterministic pass, one thread per cell. */
+lgx_status lgx_diffusion7_grad(const int64_t dims[3], const double *d_k, const double *d_lambda,
+                               const double *d_x, double *d_grad, lgx_stream stream);
+
 #ifdef __cplusplus
 }
 #endif

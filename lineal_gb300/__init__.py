@@ -28,7 +28,8 @@ __all__ = [
     "LinealError", "LinealLibraryMissing", "lib", "CsrMatrix", "StencilMatrix", "Colouring",
     "HierarchyWright", "Hierarchy", "pcg", "pbicgstab", "spmv", "residual", "jacobi_sweep",
     "sor_sweep", "sor_sweep_permuted", "permute", "unpermute", "gen_27pt", "gen_7pt",
-    "amg_strength", "amg_aggregate", "dot", "norm2sq", "max_norm", "PRECON_NONE",
+    "amg_strength", "amg_aggregate", "dot", "norm2sq", "max_norm", "sampled_outer",
+    "diffusion7_grad", "PRECON_NONE",
     "PRECON_JACOBI", "PRECON_SSOR", "PRECON_AMG",
 ]
 
@@ -159,6 +160,8 @@ def _signatures(L):
         "lgx_amg_vcycle": [V, V, V, V],
         "lgx_amg_strength": [V, D, V, V, V, V],
         "lgx_amg_aggregate": [V, V, V, V, I32, I32, I64, C.c_int, V, P(I64), V],
+        "lgx_sampled_outer": [V, D, V, V, V, V],
+        "lgx_diffusion7_grad": [V, V, V, V, V, V],
         "lgx_pcg": [V, V, V, P(_SolveParams), V, P(I64), P(D), V],
         "lgx_pbicgstab": [V, V, V, P(_SolveParams), V, P(I64), P(D), V],
     }
@@ -655,6 +658,27 @@ def _solve(fn, a: _Matrix, b, x0=None, precon=PRECON_NONE, relax=1.0, ultra=Fals
     _check(fn(a.handle, _ptr(b), _ptr(x), C.byref(p), _stream(), C.byref(it), C.byref(rel),
               _ptr(hist)))
     return SolveResult(x, it.value, rel.value, hist[: it.value + 1])
+
+
+def sampled_outer(a: CsrMatrix, u, v, alpha=1.0):
+    """alpha * u[row(e)] * v[col(e)] for every stored entry e of a (nnz
+    values in storage order)."""
+    u, v = _dvec(u), _dvec(v)
+    out = _empty(a.non_zero_num())
+    _check(lib().lgx_sampled_outer(a.handle, float(alpha), _ptr(u), _ptr(v), _ptr(out),
+                                   _stream()))
+    return out
+
+
+def diffusion7_grad(dims, k, lam, x):
+    """dL/dtheta of the 7-point operator of gen_7pt with k = exp(theta), from
+    the adjoint lam and the solution x."""
+    d = np.ascontiguousarray(dims, dtype=np.int64)
+    k, lam, x = _dvec(k), _dvec(lam), _dvec(x)
+    out = _empty(k.numel())
+    _check(lib().lgx_diffusion7_grad(_ptr(d), _ptr(k), _ptr(lam), _ptr(x), _ptr(out),
+                                     _stream()))
+    return out
 
 
 def pcg(a: _Matrix, b, **kw) -> SolveResult:

@@ -1,0 +1,77 @@
+"""Differentiable solves (the differentiation form), an optional thin torch
+binding over the C ABI.
+
+``diffusion7_solve(theta, b, dims)`` returns x = A(theta)^-1 b for the 7-point
+operator of ``gen_7pt`` with per-cell conductivity k = exp(theta)
+(harmonic-mean faces, Dirichlet rows on the axis-0 boundary), solved by
+AMG-PCG on the GPU.  Its backward pass solves the adjoint system
+A lambda = dL/dx with the same hierarchy (A is symmetric) and contracts
+dL/dtheta = -lambda^T (dA/dtheta) x in one kernel (lgx_diffusion7_grad);
+dL/db = lambda.  With ``mixed=True`` both solves run flexible CG over the
+float V-cycle (FP64 outer iteration and residuals).
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import (PRECON_AMG, Colouring, HierarchyWright, diffusion7_grad, gen_7pt, pcg)
+
+
+@dataclass
+class SolveOptions:
+    rtol: float = 1e-10
+    maxit: int = 2000
+    mixed: bool = False
+    min_coarsen_size: int = 2000
+    partition_size: int = 4096
+
+
+def _red_black(dims):
+    i, j, k = np.meshgrid(*[np.arange(d, dtype=np.int32) for d in dims], indexing="ij")
+    return ((i + j + k) % 2).ravel().astype(np.int32)
+
+
+def _function():
+    import torch
+
+    class Diffusion7Solve(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, theta, b, dims, opts):
+            k = torch.exp(theta.detach().to(torch.float64)).contiguous()
+            a = gen_7pt(dims, k)
+            col = Colouring.from_array(a, _red_black(dims), 2)
+            h = HierarchyWright(cycle_f32=opts.mixed, min_coarsen_size=opts.min_coarsen_size,
+                                partition_size=opts.partition_size).instantiate(
+                                    a, finest_colouring=col)
+            res = pcg(a, b.detach().to(torch.float64), precon=PRECON_AMG, amg=h,
+                      rtol=opts.rtol, maxit=opts.maxit, flexible=opts.mixed)
+            ctx.save_for_backward(k, res.x)
+            ctx.state = (a, h, dims, opts)
+            ctx.iterations = res.iterations
+            return res.x
+
+        @staticmethod
+        def backward(ctx, gx):
+            k, x = ctx.saved_tensors
+            a, h, dims, opts = ctx.state
+            lam = pcg(a, gx.contiguous().to(torch.float64), precon=PRECON_AMG, amg=h,
+                      rtol=opts.rtol, maxit=opts.maxit, flexible=opts.mixed).x
+            gtheta = diffusion7_grad(dims, k, lam, x) if ctx.needs_input_grad[0] else None
+            gb = lam if ctx.needs_input_grad[1] else None
+            return gtheta, gb, None, None
+
+    return Diffusion7Solve
+
+
+_FN = None
+
+
+def diffusion7_solve(theta, b, dims, opts: SolveOptions | None = None):
+    """x = A(theta)^-1 b, differentiable in theta and b."""
+    global _FN
+    if _FN is None:
+        _FN = _function()
+    return _FN.apply(theta, b, tuple(int(d) for d in dims), opts or SolveOptions())

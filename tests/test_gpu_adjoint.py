@@ -1,0 +1,120 @@
+"""Differentiation form: the adjoint gradient of x = A(theta)^-1 b for the
+7-point diffusion operator with k = exp(theta), through the torch binding,
+against FP64 central finite differences along random directions and against
+the gradient formed from the oracle's CPU solves."""
+
+import numpy as np
+import pytest
+
+import oracle as lo
+
+pytestmark = pytest.mark.gpu
+
+
+def _bump(dims):
+    i, j, k = np.meshgrid(*[np.arange(d, dtype=np.float64) for d in dims], indexing="ij")
+    c = [(d - 1) / 2 for d in dims]
+    s = max(dims) / 6.0
+    return np.exp(-((i - c[0]) ** 2 + (j - c[1]) ** 2 + (k - c[2]) ** 2) / (2 * s * s)).ravel()
+
+
+def _grad_reference(dims, k, lam, x):
+    """dL/dtheta from the face formula, in numpy."""
+    n0, n1, n2 = dims
+    K, L, X = (v.reshape(dims) for v in (k, lam, x))
+    g = np.zeros(dims)
+    for axis in range(3):
+        sl_a = [slice(None)] * 3
+        sl_b = [slice(None)] * 3
+        sl_a[axis] = slice(0, dims[axis] - 1)
+        sl_b[axis] = slice(1, dims[axis])
+        ka, kb = K[tuple(sl_a)], K[tuple(sl_b)]
+        t = (L[tuple(sl_a)] - L[tuple(sl_b)]) * (X[tuple(sl_a)] - X[tuple(sl_b)])
+        s = ka + kb
+        g[tuple(sl_a)] += 2 * ka * kb * kb / (s * s) * t
+        g[tuple(sl_b)] += 2 * kb * ka * ka / (s * s) * t
+    nb = np.zeros(dims)
+    nb[0] += 1
+    nb[n0 - 1] += 1
+    g += nb * 2 * K * L * X
+    return -g.ravel()
+
+
+def test_sampled_outer(cuda):
+    ref = lo.gen_27pt((7, 8, 9), np.exp(np.random.default_rng(0).standard_normal(504)))
+    m = cuda.CsrMatrix.from_host(ref.rowptr, ref.col, ref.val)
+    rng = np.random.default_rng(1)
+    u, v = rng.standard_normal(ref.n), rng.standard_normal(ref.n)
+    got = cuda.sampled_outer(m, u, v, alpha=-1.0).cpu().numpy()
+    rows = np.repeat(np.arange(ref.n), np.diff(ref.rowptr))
+    np.testing.assert_array_equal(got, (-1.0 * u[rows]) * v[ref.col])
+
+
+def _problem(dims, seed=4):
+    n = int(np.prod(dims))
+    rng = np.random.default_rng(seed)
+    theta = rng.standard_normal(n)
+    theta_t = theta + 0.3 * rng.standard_normal(n)
+    return theta, theta_t, _bump(dims)
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_adjoint_gradient_matches_finite_differences(cuda, mixed):
+    import torch
+
+    from lineal_gb300.autograd import SolveOptions, diffusion7_solve
+
+    dims = (12, 13, 11)
+    theta0, theta_t, b0 = _problem(dims)
+    opts = SolveOptions(rtol=1e-13, mixed=mixed, min_coarsen_size=100, partition_size=500)
+    b = torch.as_tensor(b0, device="cuda")
+    x_t = diffusion7_solve(torch.as_tensor(theta_t, device="cuda"), b, dims, opts).detach()
+
+    def loss(th):
+        x = diffusion7_solve(th, b, dims, opts)
+        return 0.5 * torch.sum((x - x_t) ** 2)
+
+    theta = torch.as_tensor(theta0, device="cuda").requires_grad_(True)
+    loss(theta).backward()
+    g = theta.grad.detach().cpu().numpy()
+    rng = np.random.default_rng(5)
+    h = 1e-6
+    worst = 0.0
+    for _ in range(8):
+        v = rng.standard_normal(theta0.size)
+        v /= np.linalg.norm(v)
+        vt = torch.as_tensor(v, device="cuda")
+        with torch.no_grad():
+            fd = (float(loss(theta.detach() + h * vt)) - float(loss(theta.detach() - h * vt))) / (2 * h)
+        worst = max(worst, abs(fd - g @ v) / abs(g @ v))
+    assert worst <= 1e-6, worst
+
+
+def test_adjoint_gradient_matches_oracle_solves(cuda):
+    import torch
+
+    from lineal_gb300.autograd import SolveOptions, diffusion7_solve
+
+    dims = (10, 9, 8)
+    theta0, theta_t, b0 = _problem(dims, seed=7)
+    opts = SolveOptions(rtol=1e-12, min_coarsen_size=100, partition_size=500)
+    b = torch.as_tensor(b0, device="cuda")
+    # oracle: x, x_t and lambda from CPU AMG-PCG solves, gradient by the face formula
+    k, kt = np.exp(theta0), np.exp(theta_t)
+    A, At = lo.gen_7pt(dims, k), lo.gen_7pt(dims, kt)
+    kw = dict(precon=lo.PRECON_AMG, rtol=1e-12, maxit=500)
+    x, _, _ = lo.pcg(A, b0, amg=lo.Amg(A, min_coarsen_size=100), **kw)
+    xt, _, _ = lo.pcg(At, b0, amg=lo.Amg(At, min_coarsen_size=100), **kw)
+    lam, _, _ = lo.pcg(A, x - xt, amg=lo.Amg(A, min_coarsen_size=100), **kw)
+    want = _grad_reference(dims, k, lam, x)
+    x_t = diffusion7_solve(torch.as_tensor(theta_t, device="cuda"), b, dims, opts).detach()
+    theta = torch.as_tensor(theta0, device="cuda").requires_grad_(True)
+    xg = diffusion7_solve(theta, b, dims, opts)
+    (0.5 * torch.sum((xg - x_t) ** 2)).backward()
+    got = theta.grad.cpu().numpy()
+    assert np.linalg.norm(got - want) <= 1e-8 * np.linalg.norm(want)
+    # the fused kernel equals the formula on the same inputs
+    lam_d = torch.as_tensor(lam, device="cuda")
+    direct = cuda.diffusion7_grad(dims, torch.as_tensor(k, device="cuda"), lam_d,
+                                  torch.as_tensor(x, device="cuda")).cpu().numpy()
+    np.testing.assert_allclose(direct, want, rtol=1e-12, atol=1e-14 * np.abs(want).max())
