@@ -376,6 +376,34 @@ lgx_status lgx_krylov_solution(lgx_krylov *k, double *d_x);
 lgx_status lgx_krylov_destroy(lgx_krylov *k);
 
 /* ------------------------------------------------------------------------
+ * Batching form: independent first-order upwind convection-diffusion
+ * systems (D = 1, unit spacing, constant velocity v per system, zero
+ * Dirichlet values outside the grid; the assembled row of cell i holds
+ * -(1 + max(+-v_d, 0)) toward each neighbour and the sum of the six
+ * magnitudes on the diagonal) solved by Jacobi-preconditioned BiCGStab
+ * (bicgstab/solver.hpp:73-151, Jacobi from zero with `relax`) in one
+ * persistent launch: each CTA solves whole systems taken from a work queue,
+ * largest first, with the termination rule of run_iterative_solver
+ * (runner.hpp:17-84) evaluated on the device.  No reference counterpart for
+ * the batching itself.
+ * ---------------------------------------------------------------------- */
+typedef struct {
+  int64_t dims[3];
+  double v[3];
+} lgx_convdiff_system;
+/* d_b / d_x: the systems' vectors concatenated in list order (row-major
+ * grids, last axis contiguous); d_x holds the initial guesses and receives the
+ * solutions.  Host outputs per system (optional): iterations, final
+ * ||r|| / ||r0||, status (0 converged, 1 breakdown, 2 non-finite, 3 maxit).
+ * Returns LGX_ERR_BREAKDOWN / LGX_ERR_NONFINITE if any system hit one.
+ * Synchronises `stream`. */
+lgx_status lgx_batch_convdiff_bicgstab(int32_t nsys, const lgx_convdiff_system *h_systems,
+                                       const double *d_b, double *d_x, double rtol, int64_t maxit,
+                                       int64_t rere_period, double relax, lgx_stream stream,
+                                       int64_t *h_iterations, double *h_rel_residual,
+                                       int32_t *h_status);
+
+/* ------------------------------------------------------------------------
  * Differentiation form: for x = A(theta)^-1 b and a loss L(x) the adjoint
  * lambda = A^-T dL/dx is one more Krylov solve (lgx_pcg when A is symmetric,
  * lgx_pbicgstab on the transpose otherwise) and dL/dtheta = -lambda^T

@@ -29,7 +29,7 @@ __all__ = [
     "HierarchyWright", "Hierarchy", "pcg", "pbicgstab", "spmv", "residual", "jacobi_sweep",
     "sor_sweep", "sor_sweep_permuted", "permute", "unpermute", "gen_27pt", "gen_7pt",
     "amg_strength", "amg_aggregate", "dot", "norm2sq", "max_norm", "sampled_outer",
-    "diffusion7_grad", "PRECON_NONE",
+    "diffusion7_grad", "batch_convdiff_bicgstab", "PRECON_NONE",
     "PRECON_JACOBI", "PRECON_SSOR", "PRECON_AMG",
 ]
 
@@ -160,6 +160,7 @@ def _signatures(L):
         "lgx_amg_vcycle": [V, V, V, V],
         "lgx_amg_strength": [V, D, V, V, V, V],
         "lgx_amg_aggregate": [V, V, V, V, I32, I32, I64, C.c_int, V, P(I64), V],
+        "lgx_batch_convdiff_bicgstab": [C.c_int32, V, V, V, D, I64, I64, D, V, V, V, V],
         "lgx_sampled_outer": [V, D, V, V, V, V],
         "lgx_diffusion7_grad": [V, V, V, V, V, V],
         "lgx_pcg": [V, V, V, P(_SolveParams), V, P(I64), P(D), V],
@@ -658,6 +659,38 @@ def _solve(fn, a: _Matrix, b, x0=None, precon=PRECON_NONE, relax=1.0, ultra=Fals
     _check(fn(a.handle, _ptr(b), _ptr(x), C.byref(p), _stream(), C.byref(it), C.byref(rel),
               _ptr(hist)))
     return SolveResult(x, it.value, rel.value, hist[: it.value + 1])
+
+
+class _ConvDiffSystem(C.Structure):
+    _fields_ = [("dims", C.c_int64 * 3), ("v", C.c_double * 3)]
+
+
+@dataclass
+class BatchResult:
+    x: object
+    iterations: np.ndarray
+    rel_residual: np.ndarray
+    status: np.ndarray
+
+
+def batch_convdiff_bicgstab(systems, b, x0=None, rtol=1e-8, maxit=1000, rere_period=8,
+                            relax=1.0) -> BatchResult:
+    """Jacobi-BiCGStab on many convection-diffusion systems in one persistent
+    launch; systems = [(dims, v), ...], b the concatenated right-hand sides."""
+    ns = len(systems)
+    arr = (_ConvDiffSystem * max(ns, 1))()
+    for i, (dims, v) in enumerate(systems):
+        arr[i].dims[:] = [int(d) for d in dims]
+        arr[i].v[:] = [float(c) for c in v]
+    b = _dvec(b)
+    x = _dvec(x0).clone() if x0 is not None else _empty(b.numel()).zero_()
+    it = np.zeros(max(ns, 1), dtype=np.int64)
+    rel = np.zeros(max(ns, 1))
+    st = np.zeros(max(ns, 1), dtype=np.int32)
+    _check(lib().lgx_batch_convdiff_bicgstab(ns, arr, _ptr(b), _ptr(x), float(rtol), int(maxit),
+                                             int(rere_period), float(relax), _stream(),
+                                             _ptr(it), _ptr(rel), _ptr(st)))
+    return BatchResult(x, it[:ns], rel[:ns], st[:ns])
 
 
 def sampled_outer(a: CsrMatrix, u, v, alpha=1.0):

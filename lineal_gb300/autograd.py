@@ -66,6 +66,36 @@ def _function():
     return Diffusion7Solve
 
 
+def diffusion7_forward(theta, b, dims, opts: SolveOptions | None = None, x0=None):
+    """x = A(theta)^-1 b without the autograd graph, optionally from the
+    initial guess x0 (the tolerance is relative to the initial residual)."""
+    import torch
+
+    opts = opts or SolveOptions()
+    dims = tuple(int(d) for d in dims)
+    k = torch.exp(theta.detach().to(torch.float64)).contiguous()
+    a = gen_7pt(dims, k)
+    col = Colouring.from_array(a, _red_black(dims), 2)
+    h = HierarchyWright(cycle_f32=opts.mixed, min_coarsen_size=opts.min_coarsen_size,
+                        partition_size=opts.partition_size).instantiate(a, finest_colouring=col)
+    return pcg(a, b.detach().to(torch.float64), x0=x0, precon=PRECON_AMG, amg=h, rtol=opts.rtol,
+               maxit=opts.maxit, flexible=opts.mixed).x
+
+
+def loss_difference_fd(theta, v, h, b, dims, x, x_target, opts: SolveOptions | None = None):
+    """Central difference of L = 0.5 ||x - x_target||^2 along v:
+    (L(theta + h v) - L(theta - h v)) / (2 h), with both solves started from the
+    solution x at theta and the difference of the losses formed as
+    0.5 sum (x+ - x-)(x+ + x- - 2 x_target), which keeps the solver and
+    rounding errors of the two large losses from cancelling."""
+    import torch
+
+    xp = diffusion7_forward(theta + h * v, b, dims, opts, x0=x)
+    xm = diffusion7_forward(theta - h * v, b, dims, opts, x0=x)
+    num = 0.5 * torch.sum((xp - xm) * (xp + xm - 2.0 * x_target))
+    return float(num) / (2.0 * h)
+
+
 _FN = None
 
 
