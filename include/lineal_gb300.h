@@ -415,6 +415,12 @@ lgx_status lgx_batch_convdiff_bicgstab(int32_t nsys, const lgx_convdiff_system *
  * pattern).  d_out holds nnz doubles. */
 lgx_status lgx_sampled_outer(const lgx_matrix *a, double alpha, const double *d_u,
                              const double *d_v, double *d_out, lgx_stream stream);
+/* r = b - A x with each row summed by the compensated dot product Dot2
+ * (Ogita, Rump, Oishi 2005): as accurate as twice-FP64 arithmetic rounded
+ * once.  The residual of iterative refinement to full FP64 accuracy (FP64
+ * CSR matrices only). */
+lgx_status lgx_residual_compensated(const lgx_matrix *a, const double *d_b, const double *d_x,
+                                   double *d_r, lgx_stream stream);
 /* dL/dtheta for the 7-point operator of lgx_gen_7pt with k = exp(theta) per
  * cell (harmonic-mean faces, 2 k on axis-0 boundary faces), given
  * k, lambda and x: one deterministic pass, one thread per cell. */

@@ -29,7 +29,7 @@ __all__ = [
     "HierarchyWright", "Hierarchy", "pcg", "pbicgstab", "spmv", "residual", "jacobi_sweep",
     "sor_sweep", "sor_sweep_permuted", "permute", "unpermute", "gen_27pt", "gen_7pt",
     "amg_strength", "amg_aggregate", "dot", "norm2sq", "max_norm", "sampled_outer",
-    "diffusion7_grad", "batch_convdiff_bicgstab", "PRECON_NONE",
+    "diffusion7_grad", "residual_compensated", "batch_convdiff_bicgstab", "PRECON_NONE",
     "PRECON_JACOBI", "PRECON_SSOR", "PRECON_AMG",
 ]
 
@@ -162,6 +162,7 @@ def _signatures(L):
         "lgx_amg_aggregate": [V, V, V, V, I32, I32, I64, C.c_int, V, P(I64), V],
         "lgx_batch_convdiff_bicgstab": [C.c_int32, V, V, V, D, I64, I64, D, V, V, V, V],
         "lgx_sampled_outer": [V, D, V, V, V, V],
+        "lgx_residual_compensated": [V, V, V, V, V],
         "lgx_diffusion7_grad": [V, V, V, V, V, V],
         "lgx_pcg": [V, V, V, P(_SolveParams), V, P(I64), P(D), V],
         "lgx_pbicgstab": [V, V, V, P(_SolveParams), V, P(I64), P(D), V],
@@ -701,6 +702,14 @@ def sampled_outer(a: CsrMatrix, u, v, alpha=1.0):
     _check(lib().lgx_sampled_outer(a.handle, float(alpha), _ptr(u), _ptr(v), _ptr(out),
                                    _stream()))
     return out
+
+
+def residual_compensated(a: CsrMatrix, b, x):
+    """b - A x with compensated (twice-FP64-accurate) row sums."""
+    b, x = _dvec(b), _dvec(x)
+    r = _empty(a.row_num())
+    _check(lib().lgx_residual_compensated(a.handle, _ptr(b), _ptr(x), _ptr(r), _stream()))
+    return r
 
 
 def diffusion7_grad(dims, k, lam, x):

@@ -17,7 +17,8 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from . import (PRECON_AMG, Colouring, HierarchyWright, diffusion7_grad, gen_7pt, pcg)
+from . import (PRECON_AMG, Colouring, HierarchyWright, diffusion7_grad, gen_7pt, pcg,
+               residual_compensated)
 
 
 @dataclass
@@ -82,16 +83,80 @@ def diffusion7_forward(theta, b, dims, opts: SolveOptions | None = None, x0=None
                maxit=opts.maxit, flexible=opts.mixed).x
 
 
-def loss_difference_fd(theta, v, h, b, dims, x, x_target, opts: SolveOptions | None = None):
-    """Central difference of L = 0.5 ||x - x_target||^2 along v:
-    (L(theta + h v) - L(theta - h v)) / (2 h), with both solves started from the
-    solution x at theta and the difference of the losses formed as
-    0.5 sum (x+ - x-)(x+ + x- - 2 x_target), which keeps the solver and
-    rounding errors of the two large losses from cancelling."""
+def refined_solve(a, b, x0, hierarchy, steps=6, rtol=1e-10):
+    """Iterative refinement to full FP64 accuracy: residuals with compensated
+    row sums (residual_compensated), corrections by AMG-PCG.  Returns x."""
     import torch
 
-    xp = diffusion7_forward(theta + h * v, b, dims, opts, x0=x)
-    xm = diffusion7_forward(theta - h * v, b, dims, opts, x0=x)
+    x = x0.clone()
+    bn = float(torch.linalg.norm(b))
+    for _ in range(steps):
+        r = residual_compensated(a, b, x)
+        rn = float(torch.linalg.norm(r))
+        if rn <= 1e-17 * bn:
+            break
+        d = pcg(a, r, precon=PRECON_AMG, amg=hierarchy, rtol=rtol, maxit=2000).x
+        x = x + d
+        if float(torch.linalg.norm(d)) <= 1e-16 * float(torch.linalg.norm(x)):
+            break
+    return x
+
+
+def _operator(theta, dims):
+    import torch
+
+    k = torch.exp(theta.detach().to(torch.float64)).contiguous()
+    a = gen_7pt(dims, k)
+    col = Colouring.from_array(a, _red_black(dims), 2)
+    return a, col
+
+
+def accurate_forward(theta, b, dims, opts: SolveOptions | None = None, x0=None):
+    """x = A(theta)^-1 b to full FP64 accuracy (refined solve)."""
+    import torch
+
+    opts = opts or SolveOptions()
+    dims = tuple(int(d) for d in dims)
+    a, col = _operator(theta, dims)
+    h = HierarchyWright(min_coarsen_size=opts.min_coarsen_size,
+                        partition_size=opts.partition_size).instantiate(a, finest_colouring=col)
+    b = b.detach().to(torch.float64)
+    if x0 is None:
+        x0 = pcg(a, b, precon=PRECON_AMG, amg=h, rtol=opts.rtol, maxit=opts.maxit).x
+    return refined_solve(a, b, x0, h)
+
+
+def accurate_gradient(theta, b, dims, x_target, opts: SolveOptions | None = None):
+    """dL/dtheta of L = 0.5 ||x - x_target||^2 with x and the adjoint lambda
+    refined to full FP64 accuracy (the reference gradient of checks)."""
+    import torch
+
+    opts = opts or SolveOptions()
+    dims = tuple(int(d) for d in dims)
+    a, col = _operator(theta, dims)
+    h = HierarchyWright(min_coarsen_size=opts.min_coarsen_size,
+                        partition_size=opts.partition_size).instantiate(a, finest_colouring=col)
+    b = b.detach().to(torch.float64)
+    x = refined_solve(a, b, pcg(a, b, precon=PRECON_AMG, amg=h, rtol=opts.rtol,
+                                maxit=opts.maxit).x, h)
+    g = (x - x_target).contiguous()
+    lam = refined_solve(a, g, pcg(a, g, precon=PRECON_AMG, amg=h, rtol=opts.rtol,
+                                  maxit=opts.maxit).x, h)
+    k = torch.exp(theta.detach().to(torch.float64)).contiguous()
+    return diffusion7_grad(dims, k, lam, x)
+
+
+def loss_difference_fd(theta, v, h, b, dims, x, x_target, opts: SolveOptions | None = None):
+    """Central difference of L = 0.5 ||x - x_target||^2 along v:
+    (L(theta + h v) - L(theta - h v)) / (2 h).  Both solves start from the
+    solution x at theta and are refined to full FP64 accuracy (compensated
+    residuals), and the loss difference is formed as
+    0.5 sum (x+ - x-)(x+ + x- - 2 x_target), so neither solver error nor the
+    rounding of the two large losses swamps the O(h) difference."""
+    import torch
+
+    xp = accurate_forward(theta + h * v, b, dims, opts, x0=x)
+    xm = accurate_forward(theta - h * v, b, dims, opts, x0=x)
     num = 0.5 * torch.sum((xp - xm) * (xp + xm - 2.0 * x_target))
     return float(num) / (2.0 * h)
 
