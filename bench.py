@@ -126,6 +126,12 @@ def make_problem(n_edge, seed_k=1, seed_b=0, sigma=1.5):
     return dims, k, b
 
 
+# DRAM bytes per FP64 SpMV launch over algorithmic bytes, from the ncu capture
+# of k_wrows<double, SpmvOp> on the 128^3 27-point matrix: (702.512 + 17.138)
+# MB read + write / 719.247 MB algorithmic
+NCU_SPMV_TRAFFIC_RATIO = (702.512128e6 + 17.137920e6) / 719247272.0
+
+
 def csr_bytes(n, nnz, val_bytes=8, vec_bytes=8):
     # values + int32 columns + int64 row offsets + x once + y once
     return nnz * (val_bytes + 4) + 8 * (n + 1) + vec_bytes * n + vec_bytes * n
@@ -445,7 +451,12 @@ def run_gb300(args):
         "precision_form": prec,
         "roofline": {"bound": "hbm", "kernel": "k_wrows<double, SpmvOp<double,double>, 4, 1>",
                      "achieved": gbs64, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-                     "frac": gbs64 / peak, "traffic": args.spmv_traffic},
+                     "frac": gbs64 / peak,
+                     "traffic": (args.spmv_traffic if args.spmv_traffic is not None
+                                 else bytes64 * NCU_SPMV_TRAFFIC_RATIO),
+                     "traffic_source": "ncu dram__bytes_read+write of one launch at 128^3 "
+                                       "(profiles/k_wrows_spmv_fp64_128cube.md), scaled to "
+                                       "this matrix by its algorithmic bytes"},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": int(launches),
