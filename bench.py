@@ -699,8 +699,9 @@ def main():
     ap.add_argument("--partition-growth", type=float, default=4.0)
     ap.add_argument("--min-partitions", type=int, default=8)
     ap.add_argument("--cpu-sample-edge", type=int, default=64)
-    ap.add_argument("--reference-iterations", type=int, default=0,
-                    help="iterations of the full-size solve used to extrapolate the CPU sample")
+    ap.add_argument("--reference-iterations", type=int, default=61,
+                    help="iterations of the full-size solve used to extrapolate the CPU sample "
+                         "(61: the 256^3 AMG-PCG iteration count of the same algorithm)")
     ap.add_argument("--vcycle", action="store_true",
                     help="--mode kernels: also time one FP64 and one mixed V-cycle")
     ap.add_argument("--no-precision-form", dest="precision_form", action="store_false",
