@@ -317,36 +317,6 @@ lgx_status colouring_make_f32(lgx_colouring &c, cudaStream_t s) {
 }
 
 // ---- multicolour SOR -------------------------------------------------------
-// a / d rounded to nearest from y = RN(1/d): q0 = a*y is within 1.5 ulp of
-// a/d, one correction q1 = q0 + (a - d*q0)*y makes it faithful, and a second
-// one with the then exact residual gives the correctly rounded quotient
-// (P. Markstein, "Computation of elementary functions on the IBM RISC
-// System/6000 processor", IBM J. Res. Dev. 34(1), 1990: a faithful quotient
-// corrected once with the correctly rounded reciprocal rounds correctly).
-// Five FP64 operations instead of a full division.  Valid while a and d stay
-// within [2^-400, 2^400] in magnitude; the caller checks a, the reciprocal
-// table marks d.
-__device__ __forceinline__ double div_by_recip(double a, double d, double y) {
-  const double q0 = a * y;
-  const double r0 = fma(-d, q0, a);
-  const double q1 = fma(r0, y, q0);
-  const double r1 = fma(-d, q1, a);
-  return fma(r1, y, q1);
-}
-
-// integer tests on the bit pattern (they keep FP64 comparisons off the FP64
-// pipe)
-__device__ __forceinline__ int exponent_field(double v) {
-  return (int)((__double_as_longlong(v) >> 52) & 0x7ff);
-}
-__device__ __forceinline__ bool exponent_within_400(double v) {
-  const int e = exponent_field(v);
-  return e > 1023 - 400 && e < 1023 + 400;
-}
-__device__ __forceinline__ bool nonzero_bits(double v) {
-  return (__double_as_longlong(v) << 1) != 0;
-}
-
 // One row of gauss-seidel-variant/sweep.hpp:134-200 in place: rows of other
 // colours already visited in this sweep hold their new values in x, the rest
 // their input values; rows of the same colour are never adjacent.
