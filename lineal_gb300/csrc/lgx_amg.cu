@@ -825,6 +825,8 @@ __global__ void k_gj_update(int64_t n, int64_t k, double *a, const double *prow,
 // x = A^-1 b, one warp per row
 template <typename XT>
 __global__ void k_dense_apply(int64_t n, const double *ainv, const XT *b, XT *x) {
+  pdl_trigger();
+  pdl_wait();
   const int lane = threadIdx.x & 31;
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -906,6 +908,8 @@ __global__ void k_rlist_fill(int64_t nc, const int32_t *perm_c, const int64_t *l
 template <typename XT>
 __global__ void k_restrict(int64_t nc, const int64_t *rptr, const int32_t *rlist,
                            const XT *__restrict__ r, XT *__restrict__ bc) {
+  pdl_trigger();
+  pdl_wait();
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nc;
        c += (int64_t)gridDim.x * blockDim.x) {
     XT s = XT(0);
@@ -918,6 +922,8 @@ __global__ void k_restrict(int64_t nc, const int64_t *rptr, const int32_t *rlist
 template <typename XT>
 __global__ void k_prolong(int64_t n, const uint32_t *__restrict__ agg_p, const XT *__restrict__ xc,
                           XT inv_relax, XT *__restrict__ x) {
+  pdl_trigger();
+  pdl_wait();
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const uint32_t a = agg_p[i];
@@ -928,6 +934,8 @@ __global__ void k_prolong(int64_t n, const uint32_t *__restrict__ agg_p, const X
 
 template <typename T, typename U>
 __global__ void k_convert(int64_t n, const T *src, U *dst) {
+  pdl_trigger();
+  pdl_wait();
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
     dst[i] = (U)src[i];
@@ -1099,17 +1107,19 @@ static lgx_status amg_build(const lgx_matrix *m, const lgx_amg_params &p,
 // float values (the stored floats or the float copy of a double level).
 template <typename XT>
 static lgx_status level_sor(lgx_amg_level &lv, const lgx_amg &h, int forward, const XT *b, XT *x,
-                            cudaStream_t s) {
+                            cudaStream_t s, int from_zero = 0) {
   const lgx_colouring &c = *lv.col;
   const double relax = h.p.smoother_relax;
   const int ultra = h.p.smoother_ultra;
   if constexpr (sizeof(XT) == 8) {
     if (c.pcsr.storage == LGX_F64)
-      return mc_sor_sweep<double, double>(c, c.pcsr.v64.p, relax, forward, ultra, b, x, s);
-    return mc_sor_sweep<float, double>(c, c.pcsr.v32.p, relax, forward, ultra, b, x, s);
+      return mc_sor_sweep<double, double>(c, c.pcsr.v64.p, relax, forward, ultra, b, x, s,
+                                          from_zero);
+    return mc_sor_sweep<float, double>(c, c.pcsr.v32.p, relax, forward, ultra, b, x, s,
+                                       from_zero);
   } else {
     const float *v = c.pcsr.storage == LGX_F32 ? c.pcsr.v32.p : c.pv32.p;
-    return mc_sor_sweep<float, float>(c, v, relax, forward, ultra, b, x, s);
+    return mc_sor_sweep<float, float>(c, v, relax, forward, ultra, b, x, s, from_zero);
   }
 }
 
@@ -1151,15 +1161,16 @@ static lgx_status vcycle_impl(lgx_amg &h, const XT *b0, XT *x0, cudaStream_t s) 
     XT *x = l == 0 ? x0 : level_vec<XT>(lv, 1);
     const int64_t n = lv.a->n;
     if (n == 0) continue;
-    LGX_CUDA(cudaMemsetAsync(x, 0, sizeof(XT) * n, s));
-    LGX_CHECK(level_sor<XT>(lv, h, 1, b, x, s));
+    LGX_CHECK(level_sor<XT>(lv, h, 1, b, x, s, 1));  // forward sweep from x = 0
     LGX_CHECK(level_residual<XT>(lv, b, x, level_vec<XT>(lv, 2), s));
     lgx_amg_level &cv = *h.lv[l + 1];
     const int64_t nc = cv.a->n;
     if (nc) {
-      k_restrict<XT><<<std::min<int64_t>(grid_for(nc, 128), 65535), 128, 0, s>>>(
-        nc, lv.rptr.p, lv.rlist.p, level_vec<XT>(lv, 2), level_vec<XT>(cv, 0));
-      LGX_LAUNCH_CHECK();
+      LGX_CUDA(launch_pdl(k_restrict<XT>, dim3(std::min<int64_t>(grid_for(nc, 128), 65535)),
+                          dim3(128), 0, s, nc, (const int64_t *)lv.rptr.p,
+                          (const int32_t *)lv.rlist.p, (const XT *)level_vec<XT>(lv, 2),
+                          level_vec<XT>(cv, 0)));
+      count_launch();
     }
   }
   {
@@ -1168,9 +1179,10 @@ static lgx_status vcycle_impl(lgx_amg &h, const XT *b0, XT *x0, cudaStream_t s) 
     if (nc) {
       XT *bl = L == 1 ? const_cast<XT *>(b0) : level_vec<XT>(last, 0);
       XT *xl = L == 1 ? x0 : level_vec<XT>(last, 1);
-      k_dense_apply<XT><<<(unsigned)std::min<int64_t>(grid_for(nc * 32, 256), 4096), 256, 0, s>>>(
-        nc, h.inv.p, bl, xl);
-      LGX_LAUNCH_CHECK();
+      LGX_CUDA(launch_pdl(k_dense_apply<XT>,
+                          dim3((unsigned)std::min<int64_t>(grid_for(nc * 32, 256), 4096)),
+                          dim3(256), 0, s, nc, (const double *)h.inv.p, (const XT *)bl, xl));
+      count_launch();
     }
   }
   const XT inv_relax = (XT)(1.0 / h.p.relax);
@@ -1180,9 +1192,10 @@ static lgx_status vcycle_impl(lgx_amg &h, const XT *b0, XT *x0, cudaStream_t s) 
     XT *x = l == 0 ? x0 : level_vec<XT>(lv, 1);
     const int64_t n = lv.a->n;
     if (n == 0) continue;
-    k_prolong<XT><<<std::min<int64_t>(grid_for(n, 256), 65535), 256, 0, s>>>(
-      n, lv.agg_p.p, level_vec<XT>(*h.lv[l + 1], 1), inv_relax, x);
-    LGX_LAUNCH_CHECK();
+    LGX_CUDA(launch_pdl(k_prolong<XT>, dim3(std::min<int64_t>(grid_for(n, 256), 65535)),
+                        dim3(256), 0, s, n, (const uint32_t *)lv.agg_p.p,
+                        (const XT *)level_vec<XT>(*h.lv[l + 1], 1), inv_relax, x));
+    count_launch();
     LGX_CHECK(level_sor<XT>(lv, h, 0, b, x, s));
   }
   return LGX_OK;
@@ -1197,13 +1210,13 @@ lgx_status amg_apply_permuted(lgx_amg &h, const double *b, double *x, cudaStream
   lgx_amg_level &l0 = *h.lv[0];
   const int64_t n = l0.a->n;
   if (!h.f32) return vcycle_impl<double>(h, b, x, s);
-  k_convert<double, float><<<std::min<int64_t>(grid_for(n, 256), 16384), 256, 0, s>>>(
-    n, b, l0.b32.p);
-  LGX_LAUNCH_CHECK();
+  LGX_CUDA(launch_pdl(k_convert<double, float>, dim3(std::min<int64_t>(grid_for(n, 256), 16384)),
+                      dim3(256), 0, s, n, b, l0.b32.p));
+  count_launch();
   LGX_CHECK(vcycle_impl<float>(h, l0.b32.p, l0.x32.p, s));
-  k_convert<float, double><<<std::min<int64_t>(grid_for(n, 256), 16384), 256, 0, s>>>(
-    n, l0.x32.p, x);
-  LGX_LAUNCH_CHECK();
+  LGX_CUDA(launch_pdl(k_convert<float, double>, dim3(std::min<int64_t>(grid_for(n, 256), 16384)),
+                      dim3(256), 0, s, n, (const float *)l0.x32.p, x));
+  count_launch();
   return LGX_OK;
 }
 

@@ -45,6 +45,14 @@ static std::atomic<int> g_rows_config{[] {
 
 int rows_config() { return g_rows_config.load(std::memory_order_relaxed); }
 
+bool pdl_enabled() {
+  static const bool on = [] {
+    const char *e = std::getenv("LGX_PDL");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
 int *device_error_flag() {
   static int *p = [] {
     int *q = nullptr;

@@ -183,9 +183,10 @@ lgx_status colouring_jp(const Csr &a, uint64_t seed, cudaStream_t s, DBuf<int32_
                         int32_t &ncolours);
 // One multicolour sweep on the permuted matrix (vectors in permuted order,
 // in place).  VT value type, XT vector/arithmetic type.
+// from_zero: the sweep starts from x = 0 (x need not be cleared).
 template <typename VT, typename XT>
 lgx_status mc_sor_sweep(const lgx_colouring &c, const VT *val, double relax, int forward,
-                        int ultra, const XT *b, XT *x, cudaStream_t s);
+                        int ultra, const XT *b, XT *x, cudaStream_t s, int from_zero = 0);
 
 lgx_status jacobi_csr(const Csr &a, double relax, const double *x_in, double *x_out,
                       const double *b, cudaStream_t s);
@@ -215,6 +216,37 @@ lgx_status csr_alloc_arrays(Csr &a, int64_t nnz, lgx_dtype storage);
 int64_t csr_partials(int64_t n);
 int64_t matrix_partials(const lgx_matrix *a);
 lgx_status stencil_ensure(lgx_matrix *a, cudaStream_t s);
+
+// ---- programmatic dependent launch ---------------------------------------
+// Kernels of the solve chains are launched with the programmatic-stream-
+// serialization attribute: a kernel may be scheduled while its predecessor in
+// the stream drains, runs its prologue (barrier set-up, bulk copies of the
+// constant matrix data), and calls pdl_wait() before it touches anything the
+// predecessor wrote; griddepcontrol.wait returns once the predecessor has
+// completed and its memory is visible.  pdl_trigger() lets the successor be
+// scheduled as soon as every CTA of this grid has started.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+// false when LGX_PDL=0 (plain stream ordering, for comparison)
+bool pdl_enabled();
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                              cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
 
 // ---- device helpers ------------------------------------------------------
 // a / d rounded to nearest from y = RN(1/d): q0 = a*y is within 1.5 ulp of

@@ -261,13 +261,13 @@ struct Solver {
     switch (precon) {
       case LGX_PRECON_JACOBI: return jacobi_diag_zero(n, diag, relax, r, z, s);
       case LGX_PRECON_SSOR: {
-        LGX_CUDA(cudaMemsetAsync(z, 0, sizeof(double) * n, s));
+        // forward sweep from zero (x need not be cleared), backward in place
         const Csr &p = col->pcsr;
         if (p.storage == LGX_F64) {
-          LGX_CHECK(mc_sor_sweep<double, double>(*col, p.v64.p, relax, 1, ultra, r, z, s));
+          LGX_CHECK(mc_sor_sweep<double, double>(*col, p.v64.p, relax, 1, ultra, r, z, s, 1));
           return mc_sor_sweep<double, double>(*col, p.v64.p, relax, 0, ultra, r, z, s);
         }
-        LGX_CHECK(mc_sor_sweep<float, double>(*col, p.v32.p, relax, 1, ultra, r, z, s));
+        LGX_CHECK(mc_sor_sweep<float, double>(*col, p.v32.p, relax, 1, ultra, r, z, s, 1));
         return mc_sor_sweep<float, double>(*col, p.v32.p, relax, 0, ultra, r, z, s);
       }
       case LGX_PRECON_AMG: return amg_apply_permuted(*amg, r, z, s);

@@ -187,6 +187,7 @@ __global__ void __launch_bounds__(kTileRows, RowCfg<VT, KIND>::ctas_per_sm)
     return r;
   };
 
+  pdl_trigger();
   // thread 0 = producer: issues tile t+G while tile t is computed, and loads
   // the bounds of tile t+2G one iteration ahead of their use
   TileRec ahead{};
@@ -203,6 +204,7 @@ __global__ void __launch_bounds__(kTileRows, RowCfg<VT, KIND>::ctas_per_sm)
     if (t + G < ntiles) ahead = bounds(t + G);
   }
   __syncthreads();
+  pdl_wait();
 
   unsigned phase[2] = {0u, 0u};
   double contrib = 0.0;
@@ -358,6 +360,7 @@ __global__ void __launch_bounds__(WPC * 32, WrowsBounds<WPC, typename Op::X>::mi
     }
   };
 
+  pdl_trigger();
   TileRec ahead{};
   unsigned pending = 0;  // stages with an issued, not yet consumed tile
   if (lane == 0) {
@@ -372,6 +375,8 @@ __global__ void __launch_bounds__(WPC * 32, WrowsBounds<WPC, typename Op::X>::mi
     if (t + S * GW < ntiles) ahead = bounds(t + S * GW);
   }
   __syncwarp();
+  // the matrix copies above only read constant data; vectors come after
+  pdl_wait();
 
   unsigned phase = 0;
   double contrib = 0.0;
@@ -454,9 +459,10 @@ inline lgx_status launch_wrows(int64_t rb, int64_t re, const Csr &a, const VT *v
   const int64_t need = (tiles + WPC - 1) / WPC;
   const int64_t g = (int64_t)sm_count() * per_sm;
   const unsigned grid = (unsigned)(need < g ? (need > 0 ? need : 1) : g);
-  k_wrows<VT, Op, WPC, S><<<grid, WPC * 32, smem, s>>>(rb, re, capw, a.rowptr.p, a.col.p, val,
-                                                        op, device_error_flag());
-  LGX_LAUNCH_CHECK();
+  LGX_CUDA(launch_pdl(k_wrows<VT, Op, WPC, S>, dim3(grid), dim3(WPC * 32), smem, s, rb, re, capw,
+                      (const int64_t *)a.rowptr.p, (const int32_t *)a.col.p, val, op,
+                      device_error_flag()));
+  count_launch();
   *done = true;
   return LGX_OK;
 }
@@ -473,9 +479,10 @@ inline lgx_status launch_rows_cfg(int64_t rb, int64_t re, int64_t max_row, const
   const int64_t tiles = (re - rb + rpt - 1) / rpt;
   const int64_t g = (int64_t)sm_count() * RowCfg<VT, KIND>::ctas_per_sm;
   const unsigned grid = (unsigned)(tiles < g ? (tiles > 0 ? tiles : 1) : g);
-  k_rows<VT, Op, KIND><<<grid, kTileRows, tile_smem_bytes<VT, KIND>(), s>>>(
-    rb, re, rpt, rowptr, col, val, op, device_error_flag());
-  LGX_LAUNCH_CHECK();
+  LGX_CUDA(launch_pdl(k_rows<VT, Op, KIND>, dim3(grid), dim3(kTileRows),
+                      tile_smem_bytes<VT, KIND>(), s, rb, re, rpt, rowptr, col, val, op,
+                      device_error_flag()));
+  count_launch();
   return LGX_OK;
 }
 

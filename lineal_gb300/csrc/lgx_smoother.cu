@@ -331,6 +331,10 @@ struct SorOp {
   int ultra;
   const double *rdiag = nullptr;
   int relax_one = 0;
+  // forward sweep from x = 0 without clearing x first: rows of colours not
+  // yet visited in this sweep (index >= visit_end) read as 0, this row too
+  int from_zero = 0;
+  int64_t visit_end = 0;
   using X = XT;
   static constexpr bool kReduce = false;
   double *partials = nullptr;
@@ -338,13 +342,13 @@ struct SorOp {
   template <int W>
   __device__ __forceinline__ double row(int64_t i, const int32_t *c, const VT *v, int len) const {
     XT accum = b[i], diag = XT(0);
-    const XT xi = x[i];
+    const XT xi = from_zero ? XT(0) : x[i];
     for (int k = 0; k < len; k += W) {
       const int m = len - k < W ? len - k : W;
       XT xv[W];
 #pragma unroll
       for (int u = 0; u < W; ++u)
-        if (u < m) xv[u] = x[c[k + u]];
+        if (u < m) xv[u] = (from_zero && c[k + u] >= visit_end) ? XT(0) : x[c[k + u]];
 #pragma unroll
       for (int u = 0; u < W; ++u) {
         if (u < m) {
@@ -382,16 +386,20 @@ struct SorOp {
 
 template <typename VT, typename XT>
 lgx_status mc_sor_sweep(const lgx_colouring &c, const VT *val, double relax, int forward,
-                        int ultra, const XT *b, XT *x, cudaStream_t s) {
+                        int ultra, const XT *b, XT *x, cudaStream_t s, int from_zero) {
   const Csr &p = c.pcsr;
   SorOp<VT, XT> op{b, x, (XT)relax, XT(1) - (XT)relax, ultra};
   if constexpr (sizeof(VT) == 8 && sizeof(XT) == 8) {
     op.rdiag = c.rdiag.p;
     op.relax_one = relax == 1.0;
   }
+  op.from_zero = from_zero && forward;
+  if (from_zero && !forward && c.n > 0)
+    LGX_CUDA(cudaMemsetAsync(x, 0, sizeof(XT) * c.n, s));
   for (int32_t k = 0; k < c.ncolours; ++k) {
     const int32_t col_id = forward ? k : c.ncolours - 1 - k;
     const int64_t rb = c.offsets[col_id], re = c.offsets[col_id + 1];
+    op.visit_end = rb;  // forward: exactly the rows before this colour are visited
     LGX_CHECK(launch_rows<VT>(rb, re, p, val, op, s));
   }
   return LGX_OK;
@@ -399,11 +407,11 @@ lgx_status mc_sor_sweep(const lgx_colouring &c, const VT *val, double relax, int
 
 template lgx_status mc_sor_sweep<double, double>(const lgx_colouring &, const double *, double,
                                                  int, int, const double *, double *,
-                                                 cudaStream_t);
+                                                 cudaStream_t, int);
 template lgx_status mc_sor_sweep<float, double>(const lgx_colouring &, const float *, double, int,
-                                                int, const double *, double *, cudaStream_t);
+                                                int, const double *, double *, cudaStream_t, int);
 template lgx_status mc_sor_sweep<float, float>(const lgx_colouring &, const float *, double, int,
-                                               int, const float *, float *, cudaStream_t);
+                                               int, const float *, float *, cudaStream_t, int);
 
 lgx_status jacobi_csr(const Csr &a, double relax, const double *x_in, double *x_out,
                       const double *b, cudaStream_t s) {
@@ -435,17 +443,14 @@ lgx_status colouring_sweep_natural(lgx_colouring &c, double relax, int forward, 
     LGX_CHECK(c.work_x.alloc(n));
   }
   LGX_CHECK(gather<double, double>(n, c.perm.p, b, c.work_b.p, s));
-  if (x_in) {
-    LGX_CHECK(gather<double, double>(n, c.perm.p, x_in, c.work_x.p, s));
-  } else {
-    LGX_CUDA(cudaMemsetAsync(c.work_x.p, 0, sizeof(double) * n, s));
-  }
+  if (x_in) LGX_CHECK(gather<double, double>(n, c.perm.p, x_in, c.work_x.p, s));
+  const int from_zero = x_in == nullptr;
   if (c.pcsr.storage == LGX_F64) {
     LGX_CHECK(mc_sor_sweep<double, double>(c, c.pcsr.v64.p, relax, forward, ultra, c.work_b.p,
-                                           c.work_x.p, s));
+                                           c.work_x.p, s, from_zero));
   } else {
     LGX_CHECK(mc_sor_sweep<float, double>(c, c.pcsr.v32.p, relax, forward, ultra, c.work_b.p,
-                                          c.work_x.p, s));
+                                          c.work_x.p, s, from_zero));
   }
   return scatter<double, double>(n, c.perm.p, c.work_x.p, x_out, s);
 }
