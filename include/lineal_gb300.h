@@ -357,6 +357,20 @@ lgx_status lgx_pbicgstab(const lgx_matrix *a, const double *d_b, double *d_x,
                          const lgx_solve_params *p, lgx_stream stream, int64_t *iterations,
                          double *final_rel_residual, double *h_history);
 
+/* Blocked multi-right-hand-side AMG-PCG (batching form; no reference
+ * counterpart): nrhs <= 32 systems A X = B with the same matrix and hierarchy,
+ * d_b / d_x row-major n x nrhs blocks (entry (i, k) at i * nrhs + k), d_x the
+ * initial guesses on entry.  Every pass over a matrix serves all columns;
+ * each column runs its own CG recurrence (FP64 outer iteration and dots, the
+ * hierarchy's V-cycle as preconditioner -- float for cycle_f32 hierarchies --
+ * with the FP64 dense coarsest solve) and is frozen once
+ * ||r_k|| <= rtol ||r0_k||.  The hierarchy must have been built from `a`.
+ * Host outputs per column (optional): iterations and final relative residual.
+ * Synchronises `stream`. */
+lgx_status lgx_pcg_multi(const lgx_matrix *a, lgx_amg *amg, int32_t nrhs, const double *d_b,
+                         double *d_x, double rtol, int64_t maxit, lgx_stream stream,
+                         int64_t *h_iterations, double *h_rel_residual);
+
 /* Step-wise form of the same solvers: lgx_krylov_create performs the
  * SystemInstance construction (initial residual, first preconditioner
  * application), lgx_krylov_iterate one SystemInstance::iterate, and

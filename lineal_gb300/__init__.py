@@ -29,7 +29,8 @@ __all__ = [
     "HierarchyWright", "Hierarchy", "pcg", "pbicgstab", "spmv", "residual", "jacobi_sweep",
     "sor_sweep", "sor_sweep_permuted", "permute", "unpermute", "gen_27pt", "gen_7pt",
     "amg_strength", "amg_aggregate", "dot", "norm2sq", "max_norm", "sampled_outer",
-    "diffusion7_grad", "residual_compensated", "batch_convdiff_bicgstab", "PRECON_NONE",
+    "diffusion7_grad", "residual_compensated", "batch_convdiff_bicgstab", "pcg_multi",
+    "PRECON_NONE",
     "PRECON_JACOBI", "PRECON_SSOR", "PRECON_AMG",
 ]
 
@@ -165,6 +166,7 @@ def _signatures(L):
         "lgx_residual_compensated": [V, V, V, V, V],
         "lgx_diffusion7_grad": [V, V, V, V, V, V],
         "lgx_pcg": [V, V, V, P(_SolveParams), V, P(I64), P(D), V],
+        "lgx_pcg_multi": [V, V, C.c_int32, V, V, D, I64, V, V, V],
         "lgx_pbicgstab": [V, V, V, P(_SolveParams), V, P(I64), P(D), V],
     }
     for name, args in sigs.items():
@@ -727,6 +729,25 @@ def pcg(a: _Matrix, b, **kw) -> SolveResult:
     """Preconditioned CG (ConjugateGradientsSolver); flexible=True selects the
     flexible-CG beta for the float V-cycle of the precision form."""
     return _solve(lib().lgx_pcg, a, b, **kw)
+
+
+def pcg_multi(a: CsrMatrix, amg: Hierarchy, b, x0=None, rtol=1e-8, maxit=1000):
+    """Blocked AMG-PCG on up to 32 right-hand sides (columns of the n x k
+    array b); returns (X, iterations per column, relative residual per
+    column)."""
+    torch = _torch()
+    b = _dvec(b)
+    if b.dim() == 1:
+        b = b.reshape(-1, 1)
+    n, k = b.shape
+    b = b.contiguous()
+    x = (_dvec(x0).reshape(n, k).clone() if x0 is not None
+         else torch.zeros((n, k), dtype=torch.float64, device="cuda"))
+    it = np.zeros(k, dtype=np.int64)
+    rel = np.zeros(k)
+    _check(lib().lgx_pcg_multi(a.handle, amg.handle, int(k), _ptr(b), _ptr(x), float(rtol),
+                               int(maxit), _stream(), _ptr(it), _ptr(rel)))
+    return x, it, rel
 
 
 def pbicgstab(a: _Matrix, b, **kw) -> SolveResult:

@@ -15,6 +15,7 @@
 #include <memory>
 #include <vector>
 
+#include "lgx_amg.cuh"
 #include "lgx_internal.cuh"
 
 namespace lgx {
@@ -570,14 +571,6 @@ __global__ void k_agg_lists(AggDev D, const int64_t *poff, int64_t nc, const int
   }
 }
 
-struct AggResult {
-  int64_t ncoarse = 0;
-  DBuf<uint32_t> agg;
-  DBuf<int64_t> list_ptr;
-  DBuf<int32_t> list;
-  int64_t stats[5] = {0, 0, 0, 0, 0};
-};
-
 lgx_status aggregate(const Csr &a, const uint8_t *dep, const uint8_t *inf, const uint8_t *iso,
                      int32_t min_size, int32_t max_size, int64_t nparts, int aggressive,
                      cudaStream_t s, AggResult &out, uint32_t *agg_out = nullptr) {
@@ -946,27 +939,6 @@ __global__ void k_convert(int64_t n, const T *src, U *dst) {
 // ===========================================================================
 // Hierarchy
 // ===========================================================================
-struct lgx_amg_level {
-  lgx::Csr own;                      // natural-order matrix (levels >= 1)
-  const lgx::Csr *a = nullptr;       // natural-order matrix of this level
-  lgx::AggResult agg;                // this level -> next (non-coarsest levels)
-  std::unique_ptr<lgx_colouring> col;  // smoother colouring and permuted matrix
-  lgx::DBuf<uint32_t> agg_p;         // permuted fine -> permuted coarse
-  lgx::DBuf<int64_t> rptr;           // permuted coarse row -> fine rows (permuted)
-  lgx::DBuf<int32_t> rlist;
-  lgx::DBuf<double> b64, x64, r64;   // cycle vectors (permuted order)
-  lgx::DBuf<float> b32, x32, r32;
-};
-
-struct lgx_amg {
-  lgx_amg_params p{};
-  std::vector<std::unique_ptr<lgx_amg_level>> lv;
-  lgx::DBuf<double> inv;             // dense inverse of the coarsest matrix
-  int64_t stats[32][5] = {};
-  lgx::DBuf<double> nat_b, nat_x;    // natural-order staging for lgx_amg_vcycle
-  bool f32 = false;
-};
-
 namespace lgx {
 
 int64_t amg_partitions(int64_t n, int64_t level, const lgx_amg_params &p) {
