@@ -296,6 +296,8 @@ def run_gb300(args):
         return g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=1e-8, maxit=500)
 
     # ---- plain FP64: warm-up then K timed solves --------------------------
+    # (library launch counts mark the solves in profiler launch lists)
+    log(f"[gb300] launches before the FP64 solves: {g.kernel_launches()}")
     for _ in range(args.warmup):
         res = solve(h64)
     iters64 = res.iterations
@@ -333,6 +335,7 @@ def run_gb300(args):
     h32 = wright32.instantiate(a, finest_colouring=col)
     torch.cuda.synchronize()
     setup32 = time.perf_counter() - t0
+    log(f"[gb300] launches before the mixed solves: {g.kernel_launches()}")
     for _ in range(args.warmup):
         res32 = solve(h32)
     torch.cuda.synchronize()
@@ -603,6 +606,32 @@ def run_batch(args):
     print(json.dumps(out), flush=True)
 
 
+def run_profile(args):
+    """Profiler target: one untimed AMG-PCG solve of the --grid^3 27-point
+    workload (FP64, or the float cycle with --mixed), then one more inside the
+    NVTX range "solve" (ncu --nvtx --nvtx-include solve/ selects its kernels)."""
+    import torch
+
+    import lineal_gb300 as g
+
+    g.build.build()
+    dims, k, b_host = make_problem(args.grid)
+    a = g.gen_27pt(dims, k)
+    col = g.Colouring.from_array(a, parity_colours(dims), 8)
+    h = g.HierarchyWright(min_coarsen_size=2000, cycle_f32=args.mixed,
+                          partition_size=args.partition_size,
+                          partition_growth=args.partition_growth,
+                          min_partitions=args.min_partitions).instantiate(a, finest_colouring=col)
+    b = torch.as_tensor(b_host, device="cuda")
+    res = g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=1e-8, maxit=500)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("solve")
+    res = g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=1e-8, maxit=500)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    log(f"[profile] {'mixed' if args.mixed else 'fp64'} solve: {res.iterations} it")
+
+
 def run_multi(args):
     """Batching form, second part: a --grid^3 (default 128^3) 7-point Poisson
     CSR with 32 right-hand sides uniform in [-1, 1], solved to 1e-8 by blocked
@@ -746,7 +775,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--mode", default="solve",
-                    choices=["solve", "kernels", "adjoint", "batch", "multi"])
+                    choices=["solve", "kernels", "adjoint", "batch", "multi", "profile"])
+    ap.add_argument("--mixed", action="store_true", help="--mode profile: the float cycle")
     ap.add_argument("--batch-systems", type=int, default=1024)
     ap.add_argument("--batch-cpu-sample", type=int, default=16)
     ap.add_argument("--fd-directions", type=int, default=64)
@@ -780,6 +810,8 @@ def main():
         run_batch(args)
     elif args.mode == "multi":
         run_multi(args)
+    elif args.mode == "profile":
+        run_profile(args)
     else:
         run_gb300(args)
 
