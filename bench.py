@@ -225,9 +225,12 @@ def precision_form(g, args, stream):
     out = {"workload": f"{args.grid}^3 7-point lognormal(sigma=3, seed 2), AMG-PCG to 1e-10",
            "rows": a.row_num(), "nnz": a.non_zero_num()}
     xs = {}
-    for tag, f32, flexible in (("fp64", False, False), ("mixed_fcg", True, True)):
+    for tag, f32, bf16, flexible in (("fp64", False, False, False),
+                                     ("mixed_fcg", True, False, True),
+                                     ("mixed_bf16_fcg", True, True, True)):
         t0 = time.perf_counter()
-        h = g.HierarchyWright(cycle_f32=f32, **hier_kw).instantiate(a, finest_colouring=col)
+        h = g.HierarchyWright(cycle_f32=f32, cycle_bf16=bf16, **hier_kw).instantiate(
+            a, finest_colouring=col)
         torch.cuda.synchronize()
         setup = time.perf_counter() - t0
         for _ in range(args.warmup):
@@ -250,9 +253,10 @@ def precision_form(g, args, stream):
         log(f"[precision] {tag}: {out[tag]['ms']:.1f} ms, {res.iterations} it, "
             f"rel {out[tag]['rel_residual_fp64']:.2e}")
         del h
-    out["mixed_fcg"]["rel_error_vs_fp64_solution"] = float(
-        torch.linalg.norm(xs["mixed_fcg"] - xs["fp64"]).item() /
-        torch.linalg.norm(xs["fp64"]).item())
+    for tag in ("mixed_fcg", "mixed_bf16_fcg"):
+        out[tag]["rel_error_vs_fp64_solution"] = float(
+            torch.linalg.norm(xs[tag] - xs["fp64"]).item() / torch.linalg.norm(xs["fp64"]).item())
+        out[tag]["speedup_vs_fp64"] = out["fp64"]["ms"] / out[tag]["ms"]
     out["speedup_vs_fp64"] = out["fp64"]["ms"] / out["mixed_fcg"]["ms"]
     return out
 
@@ -349,6 +353,24 @@ def run_gb300(args):
     rel32 = float(np.sqrt(rn32)) / float(torch.linalg.norm(b).item())
     err = float(torch.linalg.norm(res32.x - x).item() / torch.linalg.norm(x).item())
     log(f"[gb300] mixed AMG-PCG {ms32:.1f} ms, {res32.iterations} it, rel {rel32:.2e}")
+
+    # ---- mixed with bfloat16 level values (precision form option) ----------
+    h16 = g.HierarchyWright(cycle_f32=True, cycle_bf16=True, **hier_kw).instantiate(
+        a, finest_colouring=col)
+    for _ in range(args.warmup):
+        res16 = solve(h16)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        res16 = solve(h16)
+    e1.record(stream)
+    e1.synchronize()
+    ms16 = e0.elapsed_time(e1) / args.steps
+    _, rn16 = g.residual(a, b, res16.x)
+    rel16 = float(np.sqrt(rn16)) / float(torch.linalg.norm(b).item())
+    err16 = float(torch.linalg.norm(res16.x - x).item() / torch.linalg.norm(x).item())
+    log(f"[gb300] mixed bf16 AMG-PCG {ms16:.1f} ms, {res16.iterations} it, rel {rel16:.2e}")
+    del h16
 
     # ---- SpMV bandwidth (FP64 values, and float values) ---------------------
     xs = torch.randn(n, dtype=torch.float64, device="cuda")
@@ -448,6 +470,9 @@ def run_gb300(args):
         "mixed": {"ms": ms32, "iterations": res32.iterations, "rel_residual_fp64": rel32,
                   "setup_ms": setup32 * 1e3, "speedup_vs_fp64": ms64 / ms32,
                   "rel_error_vs_fp64_solution": err},
+        "mixed_bf16": {"ms": ms16, "iterations": res16.iterations, "rel_residual_fp64": rel16,
+                       "speedup_vs_fp64": ms64 / ms16, "rel_error_vs_fp64_solution": err16,
+                       "what": "float cycle with bfloat16 level values (diagonal row scales)"},
         "spmv": {"fp64_ms": t_spmv64, "fp64_gbs": gbs64, "fp64_frac": gbs64 / peak,
                  "fp32_ms": t_spmv32, "fp32_gbs": gbs32, "fp32_frac": gbs32 / peak,
                  "bytes_fp64": bytes64, "bytes_fp32": bytes32},

@@ -268,6 +268,9 @@ typedef struct {
   double smoother_relax;       /* SOR relax */
   int smoother_ultra;          /* SorVariant::ultra */
   uint64_t colour_seed;        /* JP colouring seed of the coarse levels */
+  int cycle_bf16;              /* with cycle_f32: smoothers and residuals read bfloat16
+                                  values a_ij / a_ii with the diagonal a_ii as a per-row
+                                  float scale (2 bytes per entry instead of 4) */
 } lgx_amg_params;
 
 void lgx_amg_default_params(lgx_amg_params *p);

@@ -397,6 +397,7 @@ struct MultiGridSolver : SharedStationaryIterativeSolverBase {
   DuneDependencyCriterion criterion{};
   double smoother_relax = 1.0;
   bool float_cycle = false;
+  bool bf16_values = false;  // with float_cycle: bfloat16 level values, diagonal row scales
 
   class Instance {
    public:
@@ -418,6 +419,7 @@ struct MultiGridSolver : SharedStationaryIterativeSolverBase {
       p.relax = s.relax;
       p.smoother_relax = s.smoother_relax;
       p.cycle_f32 = s.float_cycle;
+      p.cycle_bf16 = s.bf16_values;
       check(lgx_amg_setup(lhs.handle(), &p, nullptr, env.stream(), &h_));
     }
     Instance(const Instance &) = delete;

@@ -74,6 +74,7 @@ class _AmgParams(C.Structure):
         ("smoother_relax", C.c_double),
         ("smoother_ultra", C.c_int),
         ("colour_seed", C.c_uint64),
+        ("cycle_bf16", C.c_int),
     ]
 
 
@@ -540,6 +541,7 @@ class HierarchyWright:
     smoother_relax: float = 1.0
     smoother_ultra: bool = False
     colour_seed: int = 0x5EED
+    cycle_bf16: bool = False
 
     def params(self) -> _AmgParams:
         p = _AmgParams()

@@ -1023,6 +1023,7 @@ static lgx_status amg_build(const lgx_matrix *m, const lgx_amg_params &p,
       LGX_CHECK(colouring_build(*lv.a, lv.col->colour.p, nc, s, *lv.col));
     }
     if (h.f32) LGX_CHECK(colouring_make_f32(*lv.col, s));
+    if (h.f32 && p.cycle_bf16) LGX_CHECK(colouring_make_bf16(*lv.col, s));
     timer.mark(s, "colouring", l);
   }
   // transfers in permuted spaces
@@ -1090,14 +1091,17 @@ static lgx_status level_sor(lgx_amg_level &lv, const lgx_amg &h, int forward, co
     return mc_sor_sweep<float, double>(c, c.pcsr.v32.p, relax, forward, ultra, b, x, s,
                                        from_zero);
   } else {
+    if (h.p.cycle_bf16)
+      return mc_sor_sweep<bf16, float>(c, c.pv16.p, relax, forward, ultra, b, x, s, from_zero,
+                                       c.pscale.p);
     const float *v = c.pcsr.storage == LGX_F32 ? c.pcsr.v32.p : c.pv32.p;
     return mc_sor_sweep<float, float>(c, v, relax, forward, ultra, b, x, s, from_zero);
   }
 }
 
 template <typename XT>
-static lgx_status level_residual(lgx_amg_level &lv, const XT *b, const XT *x, XT *r,
-                                 cudaStream_t s) {
+static lgx_status level_residual(lgx_amg_level &lv, const lgx_amg &h, const XT *b, const XT *x,
+                                 XT *r, cudaStream_t s) {
   const lgx_colouring &c = *lv.col;
   if constexpr (sizeof(XT) == 8) {
     if (c.pcsr.storage == LGX_F64)
@@ -1106,6 +1110,9 @@ static lgx_status level_residual(lgx_amg_level &lv, const XT *b, const XT *x, XT
     return csr_residual<float, double>(c.pcsr, c.pcsr.v32.p, b, x, r, nullptr, nullptr, nullptr,
                                        s);
   } else {
+    if (h.p.cycle_bf16)
+      return csr_residual<bf16, float>(c.pcsr, c.pv16.p, b, x, r, nullptr, nullptr, nullptr, s,
+                                       c.pscale.p);
     const float *v = c.pcsr.storage == LGX_F32 ? c.pcsr.v32.p : c.pv32.p;
     return csr_residual<float, float>(c.pcsr, v, b, x, r, nullptr, nullptr, nullptr, s);
   }
@@ -1134,11 +1141,12 @@ static lgx_status vcycle_impl(lgx_amg &h, const XT *b0, XT *x0, cudaStream_t s) 
     const int64_t n = lv.a->n;
     if (n == 0) continue;
     LGX_CHECK(level_sor<XT>(lv, h, 1, b, x, s, 1));  // forward sweep from x = 0
-    LGX_CHECK(level_residual<XT>(lv, b, x, level_vec<XT>(lv, 2), s));
+    LGX_CHECK(level_residual<XT>(lv, h, b, x, level_vec<XT>(lv, 2), s));
     lgx_amg_level &cv = *h.lv[l + 1];
     const int64_t nc = cv.a->n;
     if (nc) {
-      LGX_CUDA(launch_pdl(k_restrict<XT>, dim3(std::min<int64_t>(grid_for(nc, 128), 65535)),
+      LGX_CUDA(launch_pdl(sizeof(XT) == 4, k_restrict<XT>,
+                          dim3(std::min<int64_t>(grid_for(nc, 128), 65535)),
                           dim3(128), 0, s, nc, (const int64_t *)lv.rptr.p,
                           (const int32_t *)lv.rlist.p, (const XT *)level_vec<XT>(lv, 2),
                           level_vec<XT>(cv, 0)));
@@ -1151,7 +1159,7 @@ static lgx_status vcycle_impl(lgx_amg &h, const XT *b0, XT *x0, cudaStream_t s) 
     if (nc) {
       XT *bl = L == 1 ? const_cast<XT *>(b0) : level_vec<XT>(last, 0);
       XT *xl = L == 1 ? x0 : level_vec<XT>(last, 1);
-      LGX_CUDA(launch_pdl(k_dense_apply<XT>,
+      LGX_CUDA(launch_pdl(sizeof(XT) == 4, k_dense_apply<XT>,
                           dim3((unsigned)std::min<int64_t>(grid_for(nc * 32, 256), 4096)),
                           dim3(256), 0, s, nc, (const double *)h.inv.p, (const XT *)bl, xl));
       count_launch();
@@ -1164,7 +1172,8 @@ static lgx_status vcycle_impl(lgx_amg &h, const XT *b0, XT *x0, cudaStream_t s) 
     XT *x = l == 0 ? x0 : level_vec<XT>(lv, 1);
     const int64_t n = lv.a->n;
     if (n == 0) continue;
-    LGX_CUDA(launch_pdl(k_prolong<XT>, dim3(std::min<int64_t>(grid_for(n, 256), 65535)),
+    LGX_CUDA(launch_pdl(sizeof(XT) == 4, k_prolong<XT>,
+                        dim3(std::min<int64_t>(grid_for(n, 256), 65535)),
                         dim3(256), 0, s, n, (const uint32_t *)lv.agg_p.p,
                         (const XT *)level_vec<XT>(*h.lv[l + 1], 1), inv_relax, x));
     count_launch();
@@ -1182,11 +1191,13 @@ lgx_status amg_apply_permuted(lgx_amg &h, const double *b, double *x, cudaStream
   lgx_amg_level &l0 = *h.lv[0];
   const int64_t n = l0.a->n;
   if (!h.f32) return vcycle_impl<double>(h, b, x, s);
-  LGX_CUDA(launch_pdl(k_convert<double, float>, dim3(std::min<int64_t>(grid_for(n, 256), 16384)),
+  LGX_CUDA(launch_pdl(true, k_convert<double, float>,
+                      dim3(std::min<int64_t>(grid_for(n, 256), 16384)),
                       dim3(256), 0, s, n, b, l0.b32.p));
   count_launch();
   LGX_CHECK(vcycle_impl<float>(h, l0.b32.p, l0.x32.p, s));
-  LGX_CUDA(launch_pdl(k_convert<float, double>, dim3(std::min<int64_t>(grid_for(n, 256), 16384)),
+  LGX_CUDA(launch_pdl(true, k_convert<float, double>,
+                      dim3(std::min<int64_t>(grid_for(n, 256), 16384)),
                       dim3(256), 0, s, n, (const float *)l0.x32.p, x));
   count_launch();
   return LGX_OK;
@@ -1217,6 +1228,7 @@ void lgx_amg_default_params(lgx_amg_params *p) {
   p->smoother_relax = 1.0;
   p->smoother_ultra = 0;
   p->colour_seed = 0x5eed;
+  p->cycle_bf16 = 0;
 }
 
 lgx_status lgx_amg_setup(const lgx_matrix *a, const lgx_amg_params *p,

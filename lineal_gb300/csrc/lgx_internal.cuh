@@ -1,6 +1,7 @@
 // Internal definitions shared by the lineal_gb300 CUDA sources.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -11,6 +12,25 @@
 #include "lineal_gb300.h"
 
 namespace lgx {
+
+// ---- value types ---------------------------------------------------------
+// Stored matrix values are double, float or (precision form) bfloat16 with a
+// per-row float scale.  cvt<XT>(v) widens a stored value to the arithmetic
+// type.
+using bf16 = __nv_bfloat16;
+template <typename XT, typename VT>
+__host__ __device__ __forceinline__ XT cvt(VT v) {
+  return static_cast<XT>(v);
+}
+template <>
+__host__ __device__ __forceinline__ float cvt<float, bf16>(bf16 v) {
+  return __bfloat162float(v);
+}
+template <typename VT>
+inline constexpr bool kIsBf16 = false;
+template <>
+inline constexpr bool kIsBf16<bf16> = true;
+
 
 // ---- error handling -----------------------------------------------------
 void set_error(const std::string &msg);
@@ -131,6 +151,8 @@ struct lgx_colouring {
   lgx::DBuf<int32_t> iperm;      // natural -> permuted
   lgx::Csr pcsr;                 // permuted matrix (values in the source storage type)
   lgx::DBuf<float> pv32;         // float copy of the permuted values (float cycles)
+  lgx::DBuf<lgx::bf16> pv16;     // bfloat16 values a_ij / a_ii (bf16 float cycles)
+  lgx::DBuf<float> pscale;       // per-row scale of pv16: the diagonal a_ii
   lgx::DBuf<double> rdiag;       // FP64 values: 1 / a_rr correctly rounded, or 0 where
                                  // the SOR row must divide (permuted order)
   lgx::DBuf<double> work_b, work_x;  // natural<->permuted staging for the public sweep API
@@ -158,9 +180,11 @@ lgx_status csr_compute_max_window(Csr &a, cudaStream_t s);
 template <typename VT, typename XT>
 lgx_status csr_spmv(const Csr &a, const VT *val, const XT *x, XT *y, cudaStream_t s);
 // r = b - A x; if norm != nullptr, norm[0] = ||r||^2 (double, deterministic)
+// scale: per-row factor of bfloat16 values (value = scale[row] * stored)
 template <typename VT, typename XT>
 lgx_status csr_residual(const Csr &a, const VT *val, const XT *b, const XT *x, XT *r,
-                        double *norm, double *partials, unsigned *counter, cudaStream_t s);
+                        double *norm, double *partials, unsigned *counter, cudaStream_t s,
+                        const float *scale = nullptr);
 
 lgx_status stencil_spmv(const StencilDesc &st, const double *x, double *y, cudaStream_t s);
 lgx_status stencil_residual(const StencilDesc &st, const double *b, const double *x, double *r,
@@ -183,10 +207,13 @@ lgx_status colouring_jp(const Csr &a, uint64_t seed, cudaStream_t s, DBuf<int32_
                         int32_t &ncolours);
 // One multicolour sweep on the permuted matrix (vectors in permuted order,
 // in place).  VT value type, XT vector/arithmetic type.
-// from_zero: the sweep starts from x = 0 (x need not be cleared).
+// from_zero: the sweep starts from x = 0 (x need not be cleared); scale: the
+// per-row factor of bfloat16 values.
 template <typename VT, typename XT>
 lgx_status mc_sor_sweep(const lgx_colouring &c, const VT *val, double relax, int forward,
-                        int ultra, const XT *b, XT *x, cudaStream_t s, int from_zero = 0);
+                        int ultra, const XT *b, XT *x, cudaStream_t s, int from_zero = 0,
+                        const float *scale = nullptr);
+lgx_status colouring_make_bf16(lgx_colouring &c, cudaStream_t s);
 
 lgx_status jacobi_csr(const Csr &a, double relax, const double *x_in, double *x_out,
                       const double *b, cudaStream_t s);
@@ -232,9 +259,13 @@ __device__ __forceinline__ void pdl_trigger() {
 // false when LGX_PDL=0 (plain stream ordering, for comparison)
 bool pdl_enabled();
 
+// want: the caller's choice for this launch.  Measured at 256^3: the float
+// V-cycle gains (mixed solve 382 -> 376 ms) while the FP64 chain, whose row
+// kernels are FP64-pipe bound, loses (536 -> 550 ms); FP64 chains therefore
+// launch without the attribute.
 template <typename... KArgs, typename... Args>
-inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
-                              cudaStream_t s, Args... args) {
+inline cudaError_t launch_pdl(bool want, void (*kernel)(KArgs...), dim3 grid, dim3 block,
+                              size_t smem, cudaStream_t s, Args... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = grid;
   cfg.blockDim = block;
@@ -244,7 +275,7 @@ inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, s
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  cfg.numAttrs = want && pdl_enabled() ? 1 : 0;
   return cudaLaunchKernelEx(&cfg, kernel, args...);
 }
 

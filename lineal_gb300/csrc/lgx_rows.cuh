@@ -444,7 +444,7 @@ inline lgx_status launch_wrows(int64_t rb, int64_t re, const Csr &a, const VT *v
   *done = false;
   const int64_t mw = a.max_win > 4 ? a.max_win : 4;
   if (mw > (1 << 20)) return LGX_OK;
-  const int capw = (int)((mw + 3) & ~3ll);
+  const int capw = (int)((mw + 7) & ~7ll);  // 16-byte value spans also for 2-byte values
   const size_t smem = wsmem_bytes(WPC, S, capw, sizeof(VT));
   if (smem > (size_t)kWrowsSmemMax) return LGX_OK;  // too long rows: CTA tiles
   static const cudaError_t attr = cudaFuncSetAttribute(
@@ -459,7 +459,8 @@ inline lgx_status launch_wrows(int64_t rb, int64_t re, const Csr &a, const VT *v
   const int64_t need = (tiles + WPC - 1) / WPC;
   const int64_t g = (int64_t)sm_count() * per_sm;
   const unsigned grid = (unsigned)(need < g ? (need > 0 ? need : 1) : g);
-  LGX_CUDA(launch_pdl(k_wrows<VT, Op, WPC, S>, dim3(grid), dim3(WPC * 32), smem, s, rb, re, capw,
+  LGX_CUDA(launch_pdl(sizeof(typename Op::X) == 4, k_wrows<VT, Op, WPC, S>, dim3(grid),
+                      dim3(WPC * 32), smem, s, rb, re, capw,
                       (const int64_t *)a.rowptr.p, (const int32_t *)a.col.p, val, op,
                       device_error_flag()));
   count_launch();
@@ -479,7 +480,8 @@ inline lgx_status launch_rows_cfg(int64_t rb, int64_t re, int64_t max_row, const
   const int64_t tiles = (re - rb + rpt - 1) / rpt;
   const int64_t g = (int64_t)sm_count() * RowCfg<VT, KIND>::ctas_per_sm;
   const unsigned grid = (unsigned)(tiles < g ? (tiles > 0 ? tiles : 1) : g);
-  LGX_CUDA(launch_pdl(k_rows<VT, Op, KIND>, dim3(grid), dim3(kTileRows),
+  LGX_CUDA(launch_pdl(sizeof(typename Op::X) == 4, k_rows<VT, Op, KIND>, dim3(grid),
+                      dim3(kTileRows),
                       tile_smem_bytes<VT, KIND>(), s, rb, re, rpt, rowptr, col, val, op,
                       device_error_flag()));
   count_launch();
@@ -526,7 +528,7 @@ __device__ __forceinline__ XT row_dot(const int32_t *c, const VT *v, int len,
       if (u < m) xv[u] = __ldg(x + c[k + u]);
 #pragma unroll
     for (int u = 0; u < W; ++u)
-      if (u < m) sum = fma((XT)v[k + u], xv[u], sum);
+      if (u < m) sum = fma(cvt<XT>(v[k + u]), xv[u], sum);
   }
   return sum;
 }

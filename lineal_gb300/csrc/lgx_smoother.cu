@@ -316,6 +316,41 @@ lgx_status colouring_make_f32(lgx_colouring &c, cudaStream_t s) {
   return LGX_OK;
 }
 
+// bfloat16 copy of the permuted values scaled by the row's diagonal:
+// pv16 = bf16(a_ij / a_ii) (the diagonal becomes exactly 1), pscale = a_ii.
+// Rows without a nonzero diagonal keep scale 1 and bf16(a_ij).
+template <typename VT>
+__global__ void k_to_bf16_scaled(int64_t n, const int64_t *rowptr, const int32_t *col,
+                                 const VT *val, bf16 *out, float *scale) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    double d = 0.0;
+    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k)
+      if (col[k] == r) d = (double)val[k];
+    const bool use = d != 0.0 && isfinite(d);
+    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k)
+      out[k] = __float2bfloat16_rn((float)(use ? (double)val[k] / d : (double)val[k]));
+    scale[r] = use ? (float)d : 1.0f;
+  }
+}
+
+lgx_status colouring_make_bf16(lgx_colouring &c, cudaStream_t s) {
+  if (c.pv16.p) return LGX_OK;
+  const Csr &p = c.pcsr;
+  LGX_CHECK(c.pv16.alloc(p.nnz + kCsrPad));
+  LGX_CHECK(c.pscale.alloc(std::max<int64_t>(p.n, 1)));
+  if (p.n == 0) return LGX_OK;
+  const unsigned g = (unsigned)std::min<int64_t>(grid_for(p.n, 256), 16384);
+  if (p.storage == LGX_F64)
+    k_to_bf16_scaled<double><<<g, 256, 0, s>>>(p.n, p.rowptr.p, p.col.p, p.v64.p, c.pv16.p,
+                                               c.pscale.p);
+  else
+    k_to_bf16_scaled<float><<<g, 256, 0, s>>>(p.n, p.rowptr.p, p.col.p, p.v32.p, c.pv16.p,
+                                              c.pscale.p);
+  LGX_LAUNCH_CHECK();
+  return LGX_OK;
+}
+
 // ---- multicolour SOR -------------------------------------------------------
 // One row of gauss-seidel-variant/sweep.hpp:134-200 in place: rows of other
 // colours already visited in this sweep hold their new values in x, the rest
@@ -335,12 +370,16 @@ struct SorOp {
   // yet visited in this sweep (index >= visit_end) read as 0, this row too
   int from_zero = 0;
   int64_t visit_end = 0;
+  const float *scale = nullptr;  // bfloat16 values: row factor (the diagonal)
   using X = XT;
   static constexpr bool kReduce = false;
   double *partials = nullptr;
   unsigned *counter = nullptr;
   template <int W>
   __device__ __forceinline__ double row(int64_t i, const int32_t *c, const VT *v, int len) const {
+    if constexpr (kIsBf16<VT>) {
+      return row_scaled<W>(i, c, v, len);
+    }
     XT accum = b[i], diag = XT(0);
     const XT xi = from_zero ? XT(0) : x[i];
     for (int k = 0; k < len; k += W) {
@@ -352,7 +391,7 @@ struct SorOp {
 #pragma unroll
       for (int u = 0; u < W; ++u) {
         if (u < m) {
-          const XT a = (XT)v[k + u];
+          const XT a = cvt<XT>(v[k + u]);
           if (c[k + u] == i) {
             diag = a;
             if (ultra) accum = fma(-a, xi, accum);
@@ -381,14 +420,54 @@ struct SorOp {
     x[i] = fma(relax, quot, m1 * xi);
     return 0.0;
   }
+  // bfloat16 values v with a_ij = s_i v_ij: accum = b_i - s_i sum_{j != i} v_ij x_j,
+  // a_ii = s_i v_ii (float arithmetic; a precision-form smoother, not the
+  // reference's bits)
+  template <int W>
+  __device__ __forceinline__ double row_scaled(int64_t i, const int32_t *c, const VT *v,
+                                               int len) const {
+    const XT si = scale[i];
+    const XT xi = from_zero ? XT(0) : x[i];
+    XT t = XT(0), vd = XT(0);
+    for (int k = 0; k < len; k += W) {
+      const int m = len - k < W ? len - k : W;
+      XT xv[W];
+#pragma unroll
+      for (int u = 0; u < W; ++u)
+        if (u < m) xv[u] = (from_zero && c[k + u] >= visit_end) ? XT(0) : x[c[k + u]];
+#pragma unroll
+      for (int u = 0; u < W; ++u) {
+        if (u < m) {
+          const XT a = cvt<XT>(v[k + u]);
+          if (c[k + u] == i) {
+            vd = a;
+          } else {
+            t = fma(a, xv[u], t);
+          }
+        }
+      }
+    }
+    const XT diag = si * vd;
+    XT accum = fma(-si, t, b[i]);
+    if (ultra) {
+      accum = fma(-diag, xi, accum);
+      x[i] = xi + relax * accum / fabs(diag);
+    } else {
+      x[i] = fma(relax, accum / diag, m1 * xi);
+    }
+    return 0.0;
+  }
   __device__ __forceinline__ void finish(double) const {}
 };
 
 template <typename VT, typename XT>
 lgx_status mc_sor_sweep(const lgx_colouring &c, const VT *val, double relax, int forward,
-                        int ultra, const XT *b, XT *x, cudaStream_t s, int from_zero) {
+                        int ultra, const XT *b, XT *x, cudaStream_t s, int from_zero,
+                        const float *scale) {
   const Csr &p = c.pcsr;
   SorOp<VT, XT> op{b, x, (XT)relax, XT(1) - (XT)relax, ultra};
+  op.scale = scale;
+  if (kIsBf16<VT> && !scale) return fail(LGX_ERR_INVALID, "bfloat16 values need row scales");
   if constexpr (sizeof(VT) == 8 && sizeof(XT) == 8) {
     op.rdiag = c.rdiag.p;
     op.relax_one = relax == 1.0;
@@ -407,11 +486,16 @@ lgx_status mc_sor_sweep(const lgx_colouring &c, const VT *val, double relax, int
 
 template lgx_status mc_sor_sweep<double, double>(const lgx_colouring &, const double *, double,
                                                  int, int, const double *, double *,
-                                                 cudaStream_t, int);
+                                                 cudaStream_t, int, const float *);
 template lgx_status mc_sor_sweep<float, double>(const lgx_colouring &, const float *, double, int,
-                                                int, const double *, double *, cudaStream_t, int);
+                                                int, const double *, double *, cudaStream_t, int,
+                                                const float *);
 template lgx_status mc_sor_sweep<float, float>(const lgx_colouring &, const float *, double, int,
-                                               int, const float *, float *, cudaStream_t, int);
+                                               int, const float *, float *, cudaStream_t, int,
+                                               const float *);
+template lgx_status mc_sor_sweep<bf16, float>(const lgx_colouring &, const bf16 *, double, int,
+                                              int, const float *, float *, cudaStream_t, int,
+                                              const float *);
 
 lgx_status jacobi_csr(const Csr &a, double relax, const double *x_in, double *x_out,
                       const double *b, cudaStream_t s) {

@@ -45,9 +45,11 @@ struct ResidualOp {
   static constexpr bool kReduce = NORM;
   double *partials;
   unsigned *counter;
+  const float *scale = nullptr;  // bfloat16 values: row factor
   template <int W>
   __device__ __forceinline__ double row(int64_t i, const int32_t *c, const VT *v, int len) const {
-    const XT ax = row_dot<W, VT, XT>(c, v, len, x, XT(0));
+    XT ax = row_dot<W, VT, XT>(c, v, len, x, XT(0));
+    if constexpr (kIsBf16<VT>) ax = ax * scale[i];
     const XT rv = b[i] - ax;
     r[i] = rv;
     return NORM ? (double)rv * (double)rv : 0.0;
@@ -63,16 +65,18 @@ lgx_status csr_spmv(const Csr &a, const VT *val, const XT *x, XT *y, cudaStream_
 
 template <typename VT, typename XT>
 lgx_status csr_residual(const Csr &a, const VT *val, const XT *b, const XT *x, XT *r,
-                        double *norm, double *partials, unsigned *counter, cudaStream_t s) {
+                        double *norm, double *partials, unsigned *counter, cudaStream_t s,
+                        const float *scale) {
   if (a.n == 0) {
     if (norm) LGX_CUDA(cudaMemsetAsync(norm, 0, sizeof(double), s));
     return LGX_OK;
   }
   if (norm)
     return launch_rows<VT>(0, a.n, a, val,
-                           ResidualOp<VT, XT, true>{b, x, r, norm, partials, counter}, s);
+                           ResidualOp<VT, XT, true>{b, x, r, norm, partials, counter, scale}, s);
   return launch_rows<VT>(0, a.n, a, val,
-                         ResidualOp<VT, XT, false>{b, x, r, nullptr, nullptr, nullptr}, s);
+                         ResidualOp<VT, XT, false>{b, x, r, nullptr, nullptr, nullptr, scale},
+                         s);
 }
 
 // partial-sum slots of a reducing row launch
@@ -87,13 +91,16 @@ template lgx_status csr_spmv<float, float>(const Csr &, const float *, const flo
                                            cudaStream_t);
 template lgx_status csr_residual<double, double>(const Csr &, const double *, const double *,
                                                  const double *, double *, double *, double *,
-                                                 unsigned *, cudaStream_t);
+                                                 unsigned *, cudaStream_t, const float *);
 template lgx_status csr_residual<float, double>(const Csr &, const float *, const double *,
                                                 const double *, double *, double *, double *,
-                                                unsigned *, cudaStream_t);
+                                                unsigned *, cudaStream_t, const float *);
 template lgx_status csr_residual<float, float>(const Csr &, const float *, const float *,
                                                const float *, float *, double *, double *,
-                                               unsigned *, cudaStream_t);
+                                               unsigned *, cudaStream_t, const float *);
+template lgx_status csr_residual<bf16, float>(const Csr &, const bf16 *, const float *,
+                                              const float *, float *, double *, double *,
+                                              unsigned *, cudaStream_t, const float *);
 
 // ---------------------------------------------------------------------------
 // Matrix-free 7-point diffusion stencil

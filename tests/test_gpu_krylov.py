@@ -147,3 +147,29 @@ def test_flexible_cg_precision_form(cuda):
     assert flex32.iterations <= plain.iterations + max(2, plain.iterations // 10)
     x64 = plain.x.cpu().numpy()
     assert np.linalg.norm(flex32.x.cpu().numpy() - x64) <= 1e-7 * np.linalg.norm(x64)
+
+
+@pytest.mark.parametrize("dims,npts", [((20, 20, 20), 27), ((24, 24, 24), 7)])
+def test_bf16_cycle_precision_form(cuda, dims, npts):
+    """Precision form with bfloat16 level values (diagonal row scales): flexible
+    CG over the bf16 float cycle reaches 1e-10, verified in FP64 on the
+    oracle, in at most a few more iterations than the float-valued cycle."""
+    n = int(np.prod(dims))
+    k = np.exp(1.5 * np.random.default_rng(3).standard_normal(n))
+    ref = (lo.gen_27pt if npts == 27 else lo.gen_7pt)(dims, k)
+    m = (cuda.gen_27pt if npts == 27 else cuda.gen_7pt)(dims, k)
+    b = np.random.default_rng(0).uniform(-1, 1, n)
+    params = dict(min_coarsen_size=200, partition_size=1000)
+    h32 = cuda.HierarchyWright(cycle_f32=True, **params).instantiate(m)
+    h16 = cuda.HierarchyWright(cycle_f32=True, cycle_bf16=True, **params).instantiate(m)
+    f32 = cuda.pcg(m, b, precon=cuda.PRECON_AMG, amg=h32, rtol=1e-10, maxit=500, flexible=True)
+    f16 = cuda.pcg(m, b, precon=cuda.PRECON_AMG, amg=h16, rtol=1e-10, maxit=500, flexible=True)
+    assert f16.rel_residual <= 1e-10
+    xr = f16.x.cpu().numpy()
+    assert np.linalg.norm(b - lo.spmv(ref, xr)) <= 1.2e-10 * np.linalg.norm(b)
+    assert f16.iterations <= f32.iterations + max(3, f32.iterations // 5)
+    # the bf16 cycle is a nearby preconditioner: one application differs from
+    # the float cycle's by about the bfloat16 precision
+    z32 = h32.vcycle(b).cpu().numpy()
+    z16 = h16.vcycle(b).cpu().numpy()
+    assert np.linalg.norm(z16 - z32) <= 0.05 * np.linalg.norm(z32)
