@@ -12,10 +12,7 @@
 // (||r|| <= rtol ||r0||, maxit, rho == 0, as run_iterative_solver) is taken
 // on the device.  No host round trip and no further launch happens until
 // every system is done.  A system that the alpha step solves exactly (r = 0,
-// where the reference's omega = 0 / 0 would give NaN) ends as converged.  The Jacobi preconditioner from zero
-// (fma(relax, r / d, (1 - relax) * 0), jacobi/sweep.hpp:66-87) divides
-// through the correctly rounded reciprocal of the diagonal (Markstein
-// correction, the same quotient as the division).
+// where the reference's omega = 0 / 0 would give NaN) ends as converged.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -39,24 +36,14 @@ struct BatchSys {
 
 namespace {
 
-__device__ __forceinline__ double recip_div(double a, double d, double y) {
-  const double q0 = a * y;
-  const double r0 = fma(-d, q0, a);
-  const double q1 = fma(r0, y, q0);
-  const double r1 = fma(-d, q1, a);
-  return fma(r1, y, q1);
-}
-
-__device__ __forceinline__ bool exp_within_400(double v) {
-  const int e = (int)((__double_as_longlong(v) >> 52) & 0x7ff);
-  return e > 1023 - 400 && e < 1023 + 400;
-}
-
-// Jacobi from zero: fma(relax, p / d, m1 * 0)
-__device__ __forceinline__ double jacobi0(const BatchSys &S, double p, double relax, double m1) {
-  const double q =
-    (S.rdiag != 0.0 && exp_within_400(p)) ? recip_div(p, S.diag, S.rdiag) : p / S.diag;
-  return fma(relax, q, m1 * 0.0);
+// Jacobi from zero, fma(relax, p / d, m1 * 0): the quotient as p times the
+// reciprocal of the system's constant diagonal (one FP64 multiply instead of
+// a division; within an ulp of the quotient), and for relax = 1 the product
+// itself (fma(1, q, +0) == q for q != 0; both are zero otherwise).
+__device__ __forceinline__ double jacobi0(const BatchSys &S, double p, double relax, double m1,
+                                          bool relax_one) {
+  const double q = S.rdiag != 0.0 ? p * S.rdiag : p / S.diag;
+  return relax_one ? q + 0.0 : fma(relax, q, m1 * 0.0);
 }
 
 // (A x)_i in the assembled row's column order
@@ -136,6 +123,7 @@ __global__ void __launch_bounds__(kBatchThreads)
   __shared__ double sh[3 * T];
   __shared__ int s_q;
   const double m1 = 1.0 - relax;
+  const bool relax_one = relax == 1.0;
   for (;;) {
     if (threadIdx.x == 0) s_q = (int)atomicAdd(queue, 1u);
     __syncthreads();
@@ -168,7 +156,7 @@ __global__ void __launch_bounds__(kBatchThreads)
     if (!isfinite(res2)) status = 2;
     while (status == 0 && it < maxit && sqrt(res2) > rtol * r0n && rho != 0.0) {
       // z = J(p)
-      for (int64_t i = threadIdx.x; i < n; i += T) z[i] = jacobi0(S, p[i], relax, m1);
+      for (int64_t i = threadIdx.x; i < n; i += T) z[i] = jacobi0(S, p[i], relax, m1, relax_one);
       __syncthreads();
       // v = A z ; den = r0.v ; alpha = rho / den
       double den = 0.0;
@@ -190,7 +178,7 @@ __global__ void __launch_bounds__(kBatchThreads)
         const double rv = fma(-alpha, v[i], r[i]);
         r[i] = rv;
         ss = fma(rv, rv, ss);
-        z[i] = jacobi0(S, rv, relax, m1);
+        z[i] = jacobi0(S, rv, relax, m1, relax_one);
       }
       __syncthreads();
       // t = A z ; omega = t.r / t.t

@@ -55,13 +55,13 @@ def test_batch_initial_guess_and_empty(cuda):
 
 
 def test_batch_exact_alpha_step(cuda):
-    """A 1x1x1 system is solved exactly by the first alpha step; the batch
-    reports it converged with x = b / a_11 (the reference's omega would be
-    0 / 0 there)."""
+    """A 1x1x1 system is solved (to rounding) by the first alpha step; the
+    batch reports it converged with x = b / a_11 (the reference's omega would
+    be 0 / 0 there when the step is exact)."""
     systems = [((1, 1, 1), (5.0, -3.0, 0.0)), ((6, 7, 8), (1.0, 2.0, 3.0))]
     b = np.random.default_rng(8).uniform(-1, 1, 1 + 336)
     res = cuda.batch_convdiff_bicgstab(systems, b, rtol=1e-8)
     assert (res.status == 0).all()
     diag = lo.gen_convdiff((1, 1, 1), (5.0, -3.0, 0.0)).val[0]
-    assert abs(res.x.cpu().numpy()[0] - b[0] / diag) <= 1e-15 * abs(b[0] / diag)
-    assert res.iterations[0] == 1
+    assert abs(res.x.cpu().numpy()[0] - b[0] / diag) <= 4e-16 * abs(b[0] / diag)
+    assert res.iterations[0] <= 2
