@@ -155,6 +155,7 @@ struct lgx_colouring {
   lgx::DBuf<float> pscale;       // per-row scale of pv16: the diagonal a_ii
   lgx::DBuf<double> rdiag;       // FP64 values: 1 / a_rr correctly rounded, or 0 where
                                  // the SOR row must divide (permuted order)
+  lgx::DBuf<double> pdiag;       // the stored diagonal a_rr, widened (permuted order)
   lgx::DBuf<double> work_b, work_x;  // natural<->permuted staging for the public sweep API
 };
 

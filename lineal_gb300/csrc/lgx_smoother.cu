@@ -218,15 +218,19 @@ __global__ void k_perm_fill(int64_t n, const int64_t *rowptr, const int32_t *col
 // Reciprocal of every permuted row's diagonal, rounded once by the IEEE
 // division; 0 marks rows whose diagonal lies outside [2^-400, 2^400] in
 // magnitude (or is not finite), where the sweep divides directly.
+template <typename VT>
 __global__ void k_colour_rdiag(int64_t n, const int64_t *rowptr, const int32_t *col,
-                               const double *val, double *rdiag) {
+                               const VT *val, double *rdiag, double *pdiag) {
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n;
        r += (int64_t)gridDim.x * blockDim.x) {
     double d = 0.0;
     for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k)
-      if (col[k] == r) d = val[k];
-    const int e = (int)((__double_as_longlong(d) >> 52) & 0x7ff);
-    rdiag[r] = (e > 1023 - 400 && e < 1023 + 400) ? 1.0 / d : 0.0;
+      if (col[k] == r) d = (double)val[k];
+    pdiag[r] = d;
+    if (rdiag) {
+      const int e = (int)((__double_as_longlong(d) >> 52) & 0x7ff);
+      rdiag[r] = (e > 1023 - 400 && e < 1023 + 400) ? 1.0 / d : 0.0;
+    }
   }
 }
 
@@ -299,9 +303,16 @@ lgx_status colouring_build(const Csr &a, const int32_t *d_colour, int32_t ncolou
                                          p.rowptr.p, p.col.p, p.v32.p);
   }
   LGX_LAUNCH_CHECK();
-  if (a.storage == LGX_F64 && n > 0) {
-    LGX_CHECK(out.rdiag.alloc(n));
-    k_colour_rdiag<<<g, 256, 0, s>>>(n, p.rowptr.p, p.col.p, p.v64.p, out.rdiag.p);
+  if (n > 0) {
+    LGX_CHECK(out.pdiag.alloc(n));
+    if (a.storage == LGX_F64) {
+      LGX_CHECK(out.rdiag.alloc(n));
+      k_colour_rdiag<double><<<g, 256, 0, s>>>(n, p.rowptr.p, p.col.p, p.v64.p, out.rdiag.p,
+                                               out.pdiag.p);
+    } else {
+      k_colour_rdiag<float><<<g, 256, 0, s>>>(n, p.rowptr.p, p.col.p, p.v32.p, nullptr,
+                                              out.pdiag.p);
+    }
     LGX_LAUNCH_CHECK();
   }
   return csr_compute_max_window(p, s);
@@ -460,6 +471,49 @@ struct SorOp {
   __device__ __forceinline__ void finish(double) const {}
 };
 
+// First colour of a forward sweep from x = 0: every neighbour still reads 0,
+// so the row's products with them leave accum = b_i (an fma with a zero
+// product; where only the sign of a zero could differ, the row's result is
+// +0 either way) and the row needs only b_i and its diagonal: 32 bytes per
+// row instead of the whole row.  Same quotient and update as SorOp.
+template <typename VT, typename XT>
+__global__ void k_sor_first_colour(int64_t rb, int64_t re, const double *__restrict__ pdiag,
+                                   const double *__restrict__ rdiag,
+                                   const float *__restrict__ scale, const XT *__restrict__ b,
+                                   XT *__restrict__ x, XT relax, XT m1, int ultra,
+                                   int relax_one) {
+  pdl_trigger();
+  pdl_wait();
+  for (int64_t i = rb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < re;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const XT accum = b[i];
+    XT diag;
+    if constexpr (kIsBf16<VT>) {
+      diag = scale[i];  // s_i * v_ii with v_ii = 1 (scaled by the diagonal)
+    } else {
+      diag = (XT)pdiag[i];
+    }
+    const XT xi = XT(0);
+    if (ultra) {
+      x[i] = xi + relax * accum / fabs(diag);
+      continue;
+    }
+    XT quot;
+    if constexpr (sizeof(XT) == 8 && !kIsBf16<VT>) {
+      const double y = rdiag ? rdiag[i] : 0.0;
+      quot = (nonzero_bits(y) && exponent_within_400(accum)) ? div_by_recip(accum, diag, y)
+                                                             : accum / diag;
+      if (relax_one && nonzero_bits(quot)) {
+        x[i] = quot;
+        continue;
+      }
+    } else {
+      quot = accum / diag;
+    }
+    x[i] = fma(relax, quot, m1 * xi);
+  }
+}
+
 template <typename VT, typename XT>
 lgx_status mc_sor_sweep(const lgx_colouring &c, const VT *val, double relax, int forward,
                         int ultra, const XT *b, XT *x, cudaStream_t s, int from_zero,
@@ -478,6 +532,16 @@ lgx_status mc_sor_sweep(const lgx_colouring &c, const VT *val, double relax, int
   for (int32_t k = 0; k < c.ncolours; ++k) {
     const int32_t col_id = forward ? k : c.ncolours - 1 - k;
     const int64_t rb = c.offsets[col_id], re = c.offsets[col_id + 1];
+    if (op.from_zero && k == 0 && c.pdiag.p) {
+      if (re > rb) {
+        const unsigned g = (unsigned)std::min<int64_t>(grid_for(re - rb, 256), 16384);
+        LGX_CUDA(launch_pdl(sizeof(XT) == 4, k_sor_first_colour<VT, XT>, dim3(g), dim3(256), 0,
+                            s, rb, re, (const double *)c.pdiag.p, (const double *)op.rdiag,
+                            scale, b, x, op.relax, op.m1, ultra, op.relax_one));
+        count_launch();
+      }
+      continue;
+    }
     op.visit_end = rb;  // forward: exactly the rows before this colour are visited
     LGX_CHECK(launch_rows<VT>(rb, re, p, val, op, s));
   }
