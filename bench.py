@@ -41,6 +41,23 @@ def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
 
+def autotune_log(name, h):
+    """Runs the row-engine autotuner on hierarchy `h`, logs each choice and
+    returns its wall time in ms."""
+    import torch
+
+    t0 = time.perf_counter()
+    entries = h.autotune(reps=3)
+    torch.cuda.synchronize()
+    ms_total = (time.perf_counter() - t0) * 1e3
+    log(f"[gb300] {name} autotune {ms_total / 1e3:.2f}s")
+    for e in entries:
+        ms = " ".join(f"{t:.3f}" for t in e["ms"])
+        log(f"[gb300]   level {e['level']} {e['op']:7s} {e['value_bytes']}B -> "
+            f"config {e['config']} (fastest alone {e['fastest']}: {ms} ms)")
+    return ms_total
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -293,6 +310,7 @@ def run_gb300(args):
     setup64 = time.perf_counter() - t0
     rows, nnzs = h64.sizes()
     log(f"[gb300] FP64 hierarchy {rows} in {setup64:.2f}s")
+    tune64 = autotune_log("FP64", h64) if args.autotune else None
 
     b = torch.as_tensor(b_host, device="cuda")
 
@@ -339,6 +357,7 @@ def run_gb300(args):
     h32 = wright32.instantiate(a, finest_colouring=col)
     torch.cuda.synchronize()
     setup32 = time.perf_counter() - t0
+    tune32 = autotune_log("mixed", h32) if args.autotune else None
     log(f"[gb300] launches before the mixed solves: {g.kernel_launches()}")
     for _ in range(args.warmup):
         res32 = solve(h32)
@@ -357,6 +376,7 @@ def run_gb300(args):
     # ---- mixed with bfloat16 level values (precision form option) ----------
     h16 = g.HierarchyWright(cycle_f32=True, cycle_bf16=True, **hier_kw).instantiate(
         a, finest_colouring=col)
+    tune16 = autotune_log("bf16", h16) if args.autotune else None
     for _ in range(args.warmup):
         res16 = solve(h16)
     torch.cuda.synchronize()
@@ -464,14 +484,19 @@ def run_gb300(args):
             "amg": {"levels": rows, "level_nnz": nnzs, "partition_size": args.partition_size,
                     "partition_growth": args.partition_growth,
                     "min_partitions": args.min_partitions,
-                    "finest_colouring": "grid parity, 8 colours"},
+                    "finest_colouring": "grid parity, 8 colours",
+                    "row_engine": ("autotuned per level (lgx_amg_autotune, setup-time, "
+                                   "outside the timed solves; e2e untuned)"
+                                   if args.autotune else "process-wide configuration 3")},
         },
         "iterations": iters64, "final_rel_residual": rel64, "setup_ms": setup64 * 1e3,
+        "autotune_ms": tune64,
         "mixed": {"ms": ms32, "iterations": res32.iterations, "rel_residual_fp64": rel32,
-                  "setup_ms": setup32 * 1e3, "speedup_vs_fp64": ms64 / ms32,
-                  "rel_error_vs_fp64_solution": err},
+                  "setup_ms": setup32 * 1e3, "autotune_ms": tune32,
+                  "speedup_vs_fp64": ms64 / ms32, "rel_error_vs_fp64_solution": err},
         "mixed_bf16": {"ms": ms16, "iterations": res16.iterations, "rel_residual_fp64": rel16,
-                       "speedup_vs_fp64": ms64 / ms16, "rel_error_vs_fp64_solution": err16,
+                       "autotune_ms": tune16, "speedup_vs_fp64": ms64 / ms16,
+                       "rel_error_vs_fp64_solution": err16,
                        "what": "float cycle with bfloat16 level values (diagonal row scales)"},
         "spmv": {"fp64_ms": t_spmv64, "fp64_gbs": gbs64, "fp64_frac": gbs64 / peak,
                  "fp32_ms": t_spmv32, "fp32_gbs": gbs32, "fp32_frac": gbs32 / peak,
@@ -813,6 +838,9 @@ def main():
     ap.add_argument("--reference-iterations", type=int, default=61,
                     help="iterations of the full-size solve used to extrapolate the CPU sample "
                          "(61: the 256^3 AMG-PCG iteration count of the same algorithm)")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="skip the row-engine autotuner of the solve-mode hierarchies "
+                         "(setup-time: every level's shapes timed before the timed solves)")
     ap.add_argument("--vcycle", action="store_true",
                     help="--mode kernels: also time one FP64 and one mixed V-cycle")
     ap.add_argument("--no-precision-form", dest="precision_form", action="store_false",

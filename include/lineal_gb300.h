@@ -154,6 +154,30 @@ lgx_status lgx_gen_7pt(const int64_t dims[3], const double *d_k, lgx_dtype stora
 lgx_status lgx_row_engine_set(int config);
 int lgx_row_engine_get(void);
 
+/* Autotuner of the row-engine configuration per matrix; no reference
+ * counterpart (the reference's loops have a compile-time shape).  For each
+ * (matrix, operation class, value type) it times all LGX_TUNE_CONFIGS
+ * configurations with CUDA events on `stream` (two untimed launches, then
+ * `reps` timed ones, reps in [1, 1000]) and keeps the fastest on that matrix;
+ * later launches on the matrix use it instead of the process-wide
+ * configuration.  Products and sweeps stay bit-identical; only the grouping
+ * of norm reductions follows the grid.  Vectors are scratch (allocated and
+ * freed by the call); matrix values are not touched.  Synchronises `stream`.
+ * Tune before the first solve of a Krylov solver that captures CUDA graphs:
+ * a captured iteration keeps the shapes it was recorded with. */
+#define LGX_TUNE_CONFIGS 7
+typedef struct lgx_tune_entry {
+  int32_t level;       /* hierarchy level (0 for a single matrix) */
+  int32_t op;          /* 0 products (SpMV, residual), 1 SOR sweeps */
+  int32_t value_bytes; /* stored values read: 8 FP64, 4 FP32, 2 BF16 */
+  int32_t config;      /* configuration kept (-1: nothing to tune) */
+  int32_t fastest;     /* configuration with the least time in ms[] */
+  float ms[LGX_TUNE_CONFIGS]; /* mean milliseconds of one operation per configuration */
+} lgx_tune_entry;
+/* y = A x with FP64 vectors on a CSR matrix (lgx_spmv's product): one
+ * entry into *out (NULL skips the report). */
+lgx_status lgx_matrix_autotune(lgx_matrix *a, int reps, lgx_tune_entry *out, lgx_stream stream);
+
 /* ------------------------------------------------------------------------
  * Vector reductions and updates (component-wise/sink/accumulator.hpp:151-218,
  * vector-expression.hpp:67-92).  Reductions are deterministic: fixed block
@@ -299,6 +323,18 @@ lgx_status lgx_amg_level_download(const lgx_amg *h, int64_t level, int64_t *h_ro
 /* One V-cycle from a zero initial guess: x = M^-1 b (MultiGridSolver::
  * Instance::apply, multigrid/solver.hpp:41-176, REGULAR cycle, 1 iteration). */
 lgx_status lgx_amg_vcycle(lgx_amg *h, const double *d_b, double *d_x, lgx_stream stream);
+/* Autotunes (see lgx_matrix_autotune) every smoothed level of a hierarchy:
+ * its residual and its forward SOR sweep in the value and vector types its
+ * cycles read, and with cycle_f32 also the finest level's FP64 product (the
+ * outer Krylov SpMV).  A level keeps its fastest shapes only if a whole
+ * V-cycle (graph replays, timed) is also faster with them than with the
+ * process-wide configuration there; otherwise `config` reports the
+ * process-wide one.  Writes up to max_out entries to *out and the number
+ * of entries to *n_out (either may be NULL). */
+lgx_status lgx_amg_autotune(lgx_amg *h, int reps, lgx_tune_entry *out, int max_out, int *n_out,
+                            lgx_stream stream);
+/* Drops the tuned choices: launches use the process-wide configuration. */
+lgx_status lgx_amg_autotune_reset(lgx_amg *h);
 
 /* The individual setup steps, for parity checks.
  * Strength of connection (dependency/criterion.hpp:35-78): per stored entry
@@ -368,11 +404,16 @@ lgx_status lgx_pbicgstab(const lgx_matrix *a, const double *d_b, double *d_x,
  * hierarchy's V-cycle as preconditioner -- float for cycle_f32 hierarchies --
  * with the FP64 dense coarsest solve) and is frozen once
  * ||r_k|| <= rtol ||r0_k||.  The hierarchy must have been built from `a`.
+ * The CG scalars of all columns stay on the device; with use_graphs != 0 the
+ * second iteration is recorded as a CUDA graph (one per residual-recompute
+ * variant: V-cycle, products, dots, scalars and updates) and replayed, the
+ * host reading one small state block per iteration for the stopping test.
+ * Both modes give bit-identical results.
  * Host outputs per column (optional): iterations and final relative residual.
  * Synchronises `stream`. */
 lgx_status lgx_pcg_multi(const lgx_matrix *a, lgx_amg *amg, int32_t nrhs, const double *d_b,
-                         double *d_x, double rtol, int64_t maxit, lgx_stream stream,
-                         int64_t *h_iterations, double *h_rel_residual);
+                         double *d_x, double rtol, int64_t maxit, int use_graphs,
+                         lgx_stream stream, int64_t *h_iterations, double *h_rel_residual);
 
 /* Step-wise form of the same solvers: lgx_krylov_create performs the
  * SystemInstance construction (initial residual, first preconditioner

@@ -15,6 +15,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <concepts>
 #include <cstddef>
@@ -439,6 +440,15 @@ struct MultiGridSolver : SharedStationaryIterativeSolverBase {
       int64_t l = 0;
       check(lgx_amg_info(h_, &l, nullptr, nullptr, 0));
       return (std::size_t)l;
+    }
+    // times the row-kernel shapes of every level and keeps the fastest
+    // (lgx_amg_autotune); returns the per-level report
+    std::vector<lgx_tune_entry> autotune(const Environment &env, int reps = 3) {
+      std::vector<lgx_tune_entry> out(2 * level_num() + 1);
+      int n = 0;
+      check(lgx_amg_autotune(h_, reps, out.data(), (int)out.size(), &n, env.stream()));
+      out.resize(std::min<std::size_t>((std::size_t)n, out.size()));
+      return out;
     }
 
    private:

@@ -55,6 +55,21 @@ class LinealLibraryMissing(ImportError):
 _lib = None
 
 
+TUNE_CONFIGS = 7  # LGX_TUNE_CONFIGS
+
+
+class _TuneEntry(C.Structure):
+    _fields_ = [("level", C.c_int32), ("op", C.c_int32), ("value_bytes", C.c_int32),
+                ("config", C.c_int32), ("fastest", C.c_int32),
+                ("ms", C.c_float * TUNE_CONFIGS)]
+
+    def as_dict(self):
+        return {"level": self.level, "op": ("product", "sor")[self.op],
+                "value_bytes": self.value_bytes, "config": self.config,
+                "fastest": self.fastest,
+                "ms": [float(t) for t in self.ms]}
+
+
 class _AmgParams(C.Structure):
     _fields_ = [
         ("min_aggregate_size", C.c_int32),
@@ -160,6 +175,9 @@ def _signatures(L):
         "lgx_amg_info": [V, P(I64), V, V, I64],
         "lgx_amg_level_download": [V, I64, V, V, V, V, V],
         "lgx_amg_vcycle": [V, V, V, V],
+        "lgx_matrix_autotune": [V, C.c_int, P(_TuneEntry), V],
+        "lgx_amg_autotune": [V, C.c_int, P(_TuneEntry), C.c_int, P(C.c_int), V],
+        "lgx_amg_autotune_reset": [V],
         "lgx_amg_strength": [V, D, V, V, V, V],
         "lgx_amg_aggregate": [V, V, V, V, I32, I32, I64, C.c_int, V, P(I64), V],
         "lgx_batch_convdiff_bicgstab": [C.c_int32, V, V, V, D, I64, I64, D, V, V, V, V],
@@ -167,7 +185,7 @@ def _signatures(L):
         "lgx_residual_compensated": [V, V, V, V, V],
         "lgx_diffusion7_grad": [V, V, V, V, V, V],
         "lgx_pcg": [V, V, V, P(_SolveParams), V, P(I64), P(D), V],
-        "lgx_pcg_multi": [V, V, C.c_int32, V, V, D, I64, V, V, V],
+        "lgx_pcg_multi": [V, V, C.c_int32, V, V, D, I64, C.c_int, V, V, V],
         "lgx_pbicgstab": [V, V, V, P(_SolveParams), V, P(I64), P(D), V],
     }
     for name, args in sigs.items():
@@ -255,6 +273,13 @@ class _Matrix:
 
     def spmv(self, x, out=None):
         return spmv(self, x, out)
+
+    def autotune(self, reps: int = 5) -> dict:
+        """Times every row-engine configuration on this CSR matrix's FP64
+        SpMV and keeps the fastest for it; returns the timings."""
+        e = _TuneEntry()
+        _check(lib().lgx_matrix_autotune(self._h, int(reps), C.byref(e), _stream()))
+        return e.as_dict()
 
     def diagonal(self):
         d = _empty(self.row_num())
@@ -596,6 +621,19 @@ class Hierarchy:
         _check(lib().lgx_amg_vcycle(self._h, _ptr(b), _ptr(x), _stream()))
         return x
 
+    def autotune(self, reps: int = 5) -> list:
+        """Times every row-engine configuration on each smoothed level's
+        residual and SOR sweep (and, for FP32 cycles, the finest FP64
+        product) and keeps the fastest per level; returns the timings."""
+        n = C.c_int()
+        cap = 2 * self.level_num() + 1  # residual and sweep per level, finest product
+        entries = (_TuneEntry * cap)()
+        _check(lib().lgx_amg_autotune(self._h, int(reps), entries, cap, C.byref(n), _stream()))
+        return [entries[i].as_dict() for i in range(min(n.value, cap))]
+
+    def autotune_reset(self):
+        _check(lib().lgx_amg_autotune_reset(self._h))
+
     def close(self):
         if self._h:
             lib().lgx_amg_destroy(self._h)
@@ -733,10 +771,11 @@ def pcg(a: _Matrix, b, **kw) -> SolveResult:
     return _solve(lib().lgx_pcg, a, b, **kw)
 
 
-def pcg_multi(a: CsrMatrix, amg: Hierarchy, b, x0=None, rtol=1e-8, maxit=1000):
+def pcg_multi(a: CsrMatrix, amg: Hierarchy, b, x0=None, rtol=1e-8, maxit=1000,
+              use_graphs=True):
     """Blocked AMG-PCG on up to 32 right-hand sides (columns of the n x k
     array b); returns (X, iterations per column, relative residual per
-    column)."""
+    column).  use_graphs replays a CUDA-graph recording of the iteration."""
     torch = _torch()
     b = _dvec(b)
     if b.dim() == 1:
@@ -748,7 +787,7 @@ def pcg_multi(a: CsrMatrix, amg: Hierarchy, b, x0=None, rtol=1e-8, maxit=1000):
     it = np.zeros(k, dtype=np.int64)
     rel = np.zeros(k)
     _check(lib().lgx_pcg_multi(a.handle, amg.handle, int(k), _ptr(b), _ptr(x), float(rtol),
-                               int(maxit), _stream(), _ptr(it), _ptr(rel)))
+                               int(maxit), int(use_graphs), _stream(), _ptr(it), _ptr(rel)))
     return x, it, rel
 
 

@@ -1145,7 +1145,7 @@ static lgx_status vcycle_impl(lgx_amg &h, const XT *b0, XT *x0, cudaStream_t s) 
     lgx_amg_level &cv = *h.lv[l + 1];
     const int64_t nc = cv.a->n;
     if (nc) {
-      LGX_CUDA(launch_pdl(sizeof(XT) == 4, k_restrict<XT>,
+      LGX_CUDA(launch_pdl(sizeof(XT) == 4 || nc <= pdl_fp64_rows(), k_restrict<XT>,
                           dim3(std::min<int64_t>(grid_for(nc, 128), 65535)),
                           dim3(128), 0, s, nc, (const int64_t *)lv.rptr.p,
                           (const int32_t *)lv.rlist.p, (const XT *)level_vec<XT>(lv, 2),
@@ -1159,7 +1159,7 @@ static lgx_status vcycle_impl(lgx_amg &h, const XT *b0, XT *x0, cudaStream_t s) 
     if (nc) {
       XT *bl = L == 1 ? const_cast<XT *>(b0) : level_vec<XT>(last, 0);
       XT *xl = L == 1 ? x0 : level_vec<XT>(last, 1);
-      LGX_CUDA(launch_pdl(sizeof(XT) == 4, k_dense_apply<XT>,
+      LGX_CUDA(launch_pdl(sizeof(XT) == 4 || nc <= pdl_fp64_rows(), k_dense_apply<XT>,
                           dim3((unsigned)std::min<int64_t>(grid_for(nc * 32, 256), 4096)),
                           dim3(256), 0, s, nc, (const double *)h.inv.p, (const XT *)bl, xl));
       count_launch();
@@ -1172,7 +1172,7 @@ static lgx_status vcycle_impl(lgx_amg &h, const XT *b0, XT *x0, cudaStream_t s) 
     XT *x = l == 0 ? x0 : level_vec<XT>(lv, 1);
     const int64_t n = lv.a->n;
     if (n == 0) continue;
-    LGX_CUDA(launch_pdl(sizeof(XT) == 4, k_prolong<XT>,
+    LGX_CUDA(launch_pdl(sizeof(XT) == 4 || n <= pdl_fp64_rows(), k_prolong<XT>,
                         dim3(std::min<int64_t>(grid_for(n, 256), 65535)),
                         dim3(256), 0, s, n, (const uint32_t *)lv.agg_p.p,
                         (const XT *)level_vec<XT>(*h.lv[l + 1], 1), inv_relax, x));

@@ -53,6 +53,14 @@ bool pdl_enabled() {
   return on;
 }
 
+int64_t pdl_fp64_rows() {
+  static const int64_t rows = [] {
+    const char *e = std::getenv("LGX_PDL_FP64_ROWS");
+    return e ? (int64_t)std::atoll(e) : (int64_t)262144;
+  }();
+  return rows;
+}
+
 int *device_error_flag() {
   static int *p = [] {
     int *q = nullptr;

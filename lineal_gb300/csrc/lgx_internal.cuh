@@ -104,6 +104,10 @@ struct Csr {
   int64_t n = 0, nnz = 0;
   int64_t max_row = 0;
   int64_t max_win = 0;  // most entries in any kWarpTileRows consecutive rows
+  // row-engine configuration chosen by the autotuner per operation class
+  // (0 products: SpMV and residual, 1 SOR sweeps) and value type (0 FP64,
+  // 1 FP32, 2 BF16); -1 = the process-wide configuration
+  int8_t tuned[2][3] = {{-1, -1, -1}, {-1, -1, -1}};
   int symmetric = 0;
   lgx_dtype storage = LGX_F64;
   DBuf<int64_t> rowptr;
@@ -111,6 +115,12 @@ struct Csr {
   DBuf<double> v64;
   DBuf<float> v32;
 };
+
+// Csr::tuned index of a value type
+template <typename VT>
+constexpr int tune_value_index() {
+  return sizeof(VT) == 8 ? 0 : sizeof(VT) == 4 ? 1 : 2;
+}
 
 struct StencilDesc {
   int64_t dims[3];
@@ -259,6 +269,10 @@ __device__ __forceinline__ void pdl_trigger() {
 }
 // false when LGX_PDL=0 (plain stream ordering, for comparison)
 bool pdl_enabled();
+// FP64 row launches over at most this many rows also use programmatic
+// dependent launch (small launches are latency-bound; large FP64 ones lose
+// occupancy to the early-scheduled successor).  LGX_PDL_FP64_ROWS overrides.
+int64_t pdl_fp64_rows();
 
 // want: the caller's choice for this launch.  Measured at 256^3: the float
 // V-cycle gains (mixed solve 382 -> 376 ms) while the FP64 chain, whose row

@@ -328,45 +328,145 @@ static lgx_status m_vcycle(const lgx_amg &h, int K, MWork<XT> &w, const XT *b0, 
   return LGX_OK;
 }
 
-// per-column dots through the block partials, summed on the host in order
-static lgx_status m_dots(int64_t n, int K, const double *u, const double *v, const double *w,
-                         DBuf<double> &partials, std::vector<double> &h_part, double *out1,
-                         double *out2, cudaStream_t s) {
-  const unsigned g = std::min<unsigned>(mgrid(n), 1024);
-  k_mdot<<<g, kMThreads, 0, s>>>(n, K, u, v, w, partials.p);
-  LGX_LAUNCH_CHECK();
-  LGX_CUDA(cudaMemcpyAsync(h_part.data(), partials.p, sizeof(double) * g * 2 * kMaxRhs,
-                           cudaMemcpyDeviceToHost, s));
-  LGX_CUDA(cudaStreamSynchronize(s));
-  for (int k = 0; k < K; ++k) {
-    double a = 0.0, b = 0.0;
-    for (unsigned q = 0; q < g; ++q) {
-      a += h_part[((size_t)q * 2 + 0) * kMaxRhs + k];
-      b += h_part[((size_t)q * 2 + 1) * kMaxRhs + k];
-    }
-    out1[k] = a;
-    if (out2) out2[k] = b;
-  }
-  return LGX_OK;
+// Per-column CG scalars of the blocked solver.  They stay on the device, so
+// that an iteration needs no host round trip and is captured once as a
+// CUDA graph; the host reads the block once per iteration for the stopping
+// test.
+struct MState {
+  double rho[kMaxRhs], r0[kMaxRhs], res2[kMaxRhs];
+  int64_t it_done[kMaxRhs];  // last iteration each column took part in
+  int active[kMaxRhs];
+  int64_t it;                // iterations completed
+  int n_active;
+  int flags;                 // 1: p.Ap = 0 (breakdown), 2: non-finite
+  int bad_col;               // lowest column that raised `flags`
+};
+
+// column k of the k_mdot block partials (`which` 0: u.v, 1: w.w), summed in
+// block order
+__device__ double m_column_sum(const double *partials, unsigned g, int which, int k) {
+  double a = 0.0;
+  for (unsigned q = 0; q < g; ++q) a += partials[((size_t)q * 2 + which) * kMaxRhs + k];
+  return a;
 }
+
+__device__ void m_raise(MState *st, unsigned mask, int flag) {
+  if (mask && threadIdx.x == 0) {
+    st->flags |= flag;
+    st->bad_col = __ffs(mask) - 1;
+  }
+}
+
+// rho = R.Z, r0 = ||R||, active = r0 > 0 and rho != 0 (one warp)
+__global__ void k_minit(unsigned g, int K, const double *__restrict__ partials, int64_t maxit,
+                        MState *st) {
+  const int k = threadIdx.x;
+  int act = 0, bad = 0;
+  if (k < K) {
+    const double rho = m_column_sum(partials, g, 0, k);
+    const double res2 = m_column_sum(partials, g, 1, k);
+    bad = !isfinite(res2) || !isfinite(rho);
+    st->rho[k] = rho;
+    st->res2[k] = res2;
+    st->r0[k] = sqrt(res2);
+    act = !bad && st->r0[k] > 0.0 && rho != 0.0 && maxit > 0;
+    st->active[k] = act;
+    st->it_done[k] = 0;
+  }
+  const unsigned am = __ballot_sync(~0u, act), bm = __ballot_sync(~0u, bad);
+  if (k == 0) {
+    st->n_active = __popc(am);
+    st->it = 0;
+    st->flags = 0;
+    st->bad_col = -1;
+  }
+  __syncwarp();
+  m_raise(st, bm, 2);
+}
+
+// alpha = rho / P.Q for active columns, 0 for the others
+__global__ void k_malpha(unsigned g, int K, const double *__restrict__ partials, MState *st,
+                         double *__restrict__ alpha) {
+  const int k = threadIdx.x;
+  double a = 0.0;
+  int zero = 0, bad = 0;
+  if (k < K && st->active[k]) {
+    const double den = m_column_sum(partials, g, 0, k);
+    bad = !isfinite(den);
+    zero = den == 0.0;
+    if (!bad && !zero) a = st->rho[k] / den;
+  }
+  if (k < K) alpha[k] = a;
+  const unsigned zm = __ballot_sync(~0u, zero), bm = __ballot_sync(~0u, bad);
+  m_raise(st, zm, 1);
+  __syncwarp();
+  m_raise(st, bm, 2);
+}
+
+// stopping test and beta = rho_new / rho; converged and inactive columns get
+// a NaN beta (k_mxpby leaves their P frozen)
+__global__ void k_mbeta(unsigned g, int K, const double *__restrict__ partials, double rtol,
+                        MState *st, double *__restrict__ beta) {
+  const int k = threadIdx.x;
+  const int64_t it = st->it + 1;
+  double b = __longlong_as_double(0x7ff8000000000000ll);
+  int act = 0;
+  if (k < K) {
+    const double rho_new = m_column_sum(partials, g, 0, k);
+    const double res2 = m_column_sum(partials, g, 1, k);
+    st->res2[k] = res2;
+    if (st->active[k]) {
+      st->it_done[k] = it;
+      if (sqrt(res2) <= rtol * st->r0[k] || rho_new == 0.0) {
+        st->active[k] = 0;
+      } else {
+        b = rho_new / st->rho[k];
+        st->rho[k] = rho_new;
+        act = 1;
+      }
+    }
+    beta[k] = b;
+  }
+  const unsigned am = __ballot_sync(~0u, act);
+  if (k == 0) {
+    st->n_active = __popc(am);
+    st->it = it;
+  }
+}
+
+// owns the captured iterations and the stream they are recorded on
+struct MGraphs {
+  cudaStream_t capture = nullptr;
+  cudaGraphExec_t exec[2] = {nullptr, nullptr};
+  ~MGraphs() {
+    for (auto &e : exec)
+      if (e) cudaGraphExecDestroy(e);
+    if (capture) cudaStreamDestroy(capture);
+  }
+};
 
 template <typename XT>
 static lgx_status pcg_multi(const lgx_matrix *a, lgx_amg &h, int K, const double *d_b,
-                            double *d_x, double rtol, int64_t maxit, cudaStream_t s,
-                            int64_t *h_it, double *h_rel) {
+                            double *d_x, double rtol, int64_t maxit, int use_graphs,
+                            cudaStream_t user_stream, int64_t *h_it, double *h_rel) {
   const int64_t n = a->n;
   const int64_t L = (int64_t)h.lv.size();
   const bool permuted = L > 1;
   const Csr &A = permuted ? h.lv[0]->col->pcsr : a->csr;
   const int32_t *perm = permuted ? h.lv[0]->col->perm.p : nullptr;
   const int64_t nk = n * K;
+  // the stream every launch below goes to: the caller's, or the capture
+  // stream while an iteration is recorded
+  cudaStream_t s = user_stream;
   // outer vectors (permuted order): B, X, R, P, Q, Z
   DBuf<double> B, X, R, P, Q, Z, alpha_d, beta_d, partials;
+  DBuf<MState> state;
   for (DBuf<double> *v : {&B, &X, &R, &P, &Q, &Z}) LGX_CHECK(v->alloc(std::max<int64_t>(nk, 1)));
   LGX_CHECK(alpha_d.alloc(kMaxRhs));
   LGX_CHECK(beta_d.alloc(kMaxRhs));
   LGX_CHECK(partials.alloc(1024 * 2 * kMaxRhs));
-  std::vector<double> h_part(1024 * 2 * kMaxRhs);
+  LGX_CHECK(state.alloc(1));
+  const unsigned gdot = std::min<unsigned>(mgrid(n), 1024);
   if (perm) {
     k_mpermute<<<egrid(nk), 256, 0, s>>>(n, perm, K, 0, d_b, B.p);
     k_mpermute<<<egrid(nk), 256, 0, s>>>(n, perm, K, 0, d_x, X.p);
@@ -410,63 +510,86 @@ static lgx_status pcg_multi(const lgx_matrix *a, lgx_amg &h, int K, const double
     LGX_LAUNCH_CHECK();
     return LGX_OK;
   };
-  double rho[kMaxRhs], res2[kMaxRhs], r0[kMaxRhs], den[kMaxRhs], alpha[kMaxRhs], beta[kMaxRhs];
-  bool active[kMaxRhs];
+  auto dots = [&](const double *u, const double *v, const double *ww) -> lgx_status {
+    k_mdot<<<gdot, kMThreads, 0, s>>>(n, K, u, v, ww, partials.p);
+    LGX_LAUNCH_CHECK();
+    return LGX_OK;
+  };
+  // one iteration (conjugate-gradients/solver.hpp:75-117 per column); with
+  // `rere` the residual is recomputed as B - A X (every 8th iteration)
+  auto iteration = [&](int rere) -> lgx_status {
+    // Q = A P ; alpha = rho / P.Q ; X += alpha P ; R -= alpha Q
+    LGX_CHECK(apply(nullptr, P.p, Q.p));
+    LGX_CHECK(dots(P.p, Q.p, nullptr));
+    k_malpha<<<1, 32, 0, s>>>(gdot, K, partials.p, state.p, alpha_d.p);
+    k_mupdate<<<egrid(nk), 256, 0, s>>>(n, K, alpha_d.p, P.p, Q.p, X.p, R.p);
+    LGX_LAUNCH_CHECK();
+    if (rere) LGX_CHECK(apply(B.p, X.p, R.p));
+    // Z = M R ; beta = R.Z / rho ; P = Z + beta P
+    LGX_CHECK(precondition(R.p, Z.p));
+    LGX_CHECK(dots(R.p, Z.p, R.p));
+    k_mbeta<<<1, 32, 0, s>>>(gdot, K, partials.p, rtol, state.p, beta_d.p);
+    k_mxpby<<<egrid(nk), 256, 0, s>>>(n, K, beta_d.p, Z.p, P.p);
+    LGX_LAUNCH_CHECK();
+    return LGX_OK;
+  };
+  MGraphs graphs;
+  auto capture = [&](int rere) -> lgx_status {
+    if (!graphs.capture)
+      LGX_CUDA(cudaStreamCreateWithFlags(&graphs.capture, cudaStreamNonBlocking));
+    s = graphs.capture;
+    cudaGraph_t gr = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    lgx_status st = e == cudaSuccess ? iteration(rere) : cuda_fail(e, "cudaStreamBeginCapture");
+    const cudaError_t e2 = cudaStreamEndCapture(s, &gr);
+    s = user_stream;
+    if (st != LGX_OK) {
+      if (gr) cudaGraphDestroy(gr);
+      return st;
+    }
+    if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&graphs.exec[rere], gr, 0);
+    cudaGraphDestroy(gr);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    return LGX_OK;
+  };
+  MState hs{};
+  auto read_state = [&]() -> lgx_status {
+    LGX_CUDA(cudaMemcpyAsync(&hs, state.p, sizeof(MState), cudaMemcpyDeviceToHost, s));
+    LGX_CUDA(cudaStreamSynchronize(s));
+    return LGX_OK;
+  };
   // R = B - A X ; Z = M R ; rho = R.Z ; P = Z (conjugate-gradients/solver.hpp:50-73)
   LGX_CHECK(apply(B.p, X.p, R.p));
   LGX_CHECK(precondition(R.p, Z.p));
-  LGX_CHECK(m_dots(n, K, R.p, Z.p, R.p, partials, h_part, rho, res2, s));
+  LGX_CHECK(dots(R.p, Z.p, R.p));
+  k_minit<<<1, 32, 0, s>>>(gdot, K, partials.p, maxit, state.p);
+  LGX_LAUNCH_CHECK();
   LGX_CUDA(cudaMemcpyAsync(P.p, Z.p, sizeof(double) * nk, cudaMemcpyDeviceToDevice, s));
-  int n_active = 0;
-  for (int k = 0; k < K; ++k) {
-    if (!std::isfinite(res2[k]) || !std::isfinite(rho[k]))
-      return fail(LGX_ERR_NONFINITE, "non-finite initial residual in column " + std::to_string(k));
-    r0[k] = std::sqrt(res2[k]);
-    active[k] = r0[k] > 0.0 && rho[k] != 0.0 && maxit > 0;
-    h_it[k] = 0;
-    n_active += active[k];
-  }
+  LGX_CHECK(read_state());
+  if (hs.flags & 2)
+    return fail(LGX_ERR_NONFINITE,
+                "non-finite initial residual in column " + std::to_string(hs.bad_col));
   int64_t it = 0;
-  while (n_active > 0 && it < maxit) {
-    // Q = A P ; alpha = rho / P.Q
-    LGX_CHECK(apply(nullptr, P.p, Q.p));
-    LGX_CHECK(m_dots(n, K, P.p, Q.p, nullptr, partials, h_part, den, nullptr, s));
-    for (int k = 0; k < K; ++k) {
-      alpha[k] = 0.0;
-      if (!active[k]) continue;
-      if (!std::isfinite(den[k]) || den[k] == 0.0)
-        return fail(den[k] == 0.0 ? LGX_ERR_BREAKDOWN : LGX_ERR_NONFINITE,
-                    "column " + std::to_string(k) + ": p.Ap is zero or non-finite");
-      alpha[k] = rho[k] / den[k];
+  while (hs.n_active > 0 && it < maxit) {
+    const int rere = (it + 1) % 8 == 0;
+    if (use_graphs && it > 0) {
+      // the first iteration ran eagerly; later ones replay the recording
+      if (!graphs.exec[rere]) LGX_CHECK(capture(rere));
+      LGX_CUDA(cudaGraphLaunch(graphs.exec[rere], s));
+    } else {
+      LGX_CHECK(iteration(rere));
     }
-    LGX_CUDA(cudaMemcpyAsync(alpha_d.p, alpha, sizeof(double) * K, cudaMemcpyHostToDevice, s));
-    k_mupdate<<<egrid(nk), 256, 0, s>>>(n, K, alpha_d.p, P.p, Q.p, X.p, R.p);
-    LGX_LAUNCH_CHECK();
     ++it;
-    // true residual every 8 iterations (the rere controller of the tests)
-    if (it % 8 == 0) LGX_CHECK(apply(B.p, X.p, R.p));
-    LGX_CHECK(precondition(R.p, Z.p));
-    double rho_new[kMaxRhs];
-    LGX_CHECK(m_dots(n, K, R.p, Z.p, R.p, partials, h_part, rho_new, res2, s));
-    n_active = 0;
-    for (int k = 0; k < K; ++k) {
-      beta[k] = std::nan("");  // frozen unless set below
-      if (!active[k]) continue;
-      h_it[k] = it;
-      if (std::sqrt(res2[k]) <= rtol * r0[k] || rho_new[k] == 0.0) {
-        active[k] = false;
-        continue;
-      }
-      beta[k] = rho_new[k] / rho[k];
-      rho[k] = rho_new[k];
-      ++n_active;
-    }
-    // frozen columns keep P (their alpha is 0 from now on)
-    LGX_CUDA(cudaMemcpyAsync(beta_d.p, beta, sizeof(double) * K, cudaMemcpyHostToDevice, s));
-    k_mxpby<<<egrid(nk), 256, 0, s>>>(n, K, beta_d.p, Z.p, P.p);
-    LGX_LAUNCH_CHECK();
+    LGX_CHECK(read_state());
+    if (hs.flags)
+      return fail(hs.flags & 2 ? LGX_ERR_NONFINITE : LGX_ERR_BREAKDOWN,
+                  "column " + std::to_string(hs.bad_col) + ": p.Ap is zero or non-finite");
   }
-  for (int k = 0; k < K; ++k) h_rel[k] = r0[k] > 0.0 ? std::sqrt(res2[k]) / r0[k] : 0.0;
+  for (int k = 0; k < K; ++k) {
+    h_it[k] = hs.it_done[k];
+    h_rel[k] = hs.r0[k] > 0.0 ? std::sqrt(hs.res2[k]) / hs.r0[k] : 0.0;
+  }
   if (perm) {
     k_mpermute<<<egrid(nk), 256, 0, s>>>(n, perm, K, 1, X.p, d_x);
     LGX_LAUNCH_CHECK();
@@ -474,8 +597,8 @@ static lgx_status pcg_multi(const lgx_matrix *a, lgx_amg &h, int K, const double
     LGX_CUDA(cudaMemcpyAsync(d_x, X.p, sizeof(double) * nk, cudaMemcpyDeviceToDevice, s));
   }
   LGX_CUDA(cudaStreamSynchronize(s));
-  for (int k = 0; k < K; ++k)
-    if (active[k]) return fail(LGX_ERR_NOT_CONVERGED, "maxit reached before every column converged");
+  if (hs.n_active > 0)
+    return fail(LGX_ERR_NOT_CONVERGED, "maxit reached before every column converged");
   return LGX_OK;
 }
 
@@ -486,8 +609,8 @@ using namespace lgx;
 extern "C" {
 
 lgx_status lgx_pcg_multi(const lgx_matrix *a, lgx_amg *amg, int32_t nrhs, const double *d_b,
-                         double *d_x, double rtol, int64_t maxit, lgx_stream stream,
-                         int64_t *h_iterations, double *h_rel_residual) {
+                         double *d_x, double rtol, int64_t maxit, int use_graphs,
+                         lgx_stream stream, int64_t *h_iterations, double *h_rel_residual) {
   if (!a || !amg) return fail(LGX_ERR_INVALID, "null matrix or hierarchy");
   if (nrhs < 1 || nrhs > kMaxRhs) return fail(LGX_ERR_INVALID, "nrhs must be in [1, 32]");
   if (a->kind != LGX_MATRIX_CSR || amg->lv.empty() || amg->lv[0]->a != &a->csr)
@@ -495,10 +618,10 @@ lgx_status lgx_pcg_multi(const lgx_matrix *a, lgx_amg *amg, int32_t nrhs, const 
   if (a->n > 0 && (!d_b || !d_x)) return fail(LGX_ERR_INVALID, "null vector");
   std::vector<int64_t> it(nrhs, 0);
   std::vector<double> rel(nrhs, 0.0);
-  lgx_status st = amg->f32 ? pcg_multi<float>(a, *amg, nrhs, d_b, d_x, rtol, maxit, stream,
-                                               it.data(), rel.data())
-                           : pcg_multi<double>(a, *amg, nrhs, d_b, d_x, rtol, maxit, stream,
-                                                it.data(), rel.data());
+  lgx_status st = amg->f32 ? pcg_multi<float>(a, *amg, nrhs, d_b, d_x, rtol, maxit, use_graphs,
+                                               stream, it.data(), rel.data())
+                           : pcg_multi<double>(a, *amg, nrhs, d_b, d_x, rtol, maxit, use_graphs,
+                                                stream, it.data(), rel.data());
   if (h_iterations) std::copy(it.begin(), it.end(), h_iterations);
   if (h_rel_residual) std::copy(rel.begin(), rel.end(), h_rel_residual);
   return st;

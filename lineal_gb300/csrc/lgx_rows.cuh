@@ -20,7 +20,9 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
+#include <type_traits>
 
 #include "lgx_internal.cuh"
 
@@ -450,16 +452,27 @@ inline lgx_status launch_wrows(int64_t rb, int64_t re, const Csr &a, const VT *v
   static const cudaError_t attr = cudaFuncSetAttribute(
     k_wrows<VT, Op, WPC, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, kWrowsSmemMax);
   LGX_CUDA(attr);
+  // occupancy of the last shared-memory size asked for (one query per
+  // matrix shape instead of one per launch): smem in the high, CTAs per SM
+  // in the low 32 bits
+  static std::atomic<uint64_t> occ_cache{0};
   int per_sm = 0;
-  LGX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wrows<VT, Op, WPC, S>,
-                                                         WPC * 32, smem));
+  const uint64_t cached = occ_cache.load(std::memory_order_relaxed);
+  if (cached >> 32 == (uint64_t)smem) {
+    per_sm = (int)(uint32_t)cached;
+  } else {
+    LGX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wrows<VT, Op, WPC, S>,
+                                                           WPC * 32, smem));
+    occ_cache.store(((uint64_t)smem << 32) | (uint32_t)per_sm, std::memory_order_relaxed);
+  }
   if (per_sm < 1) return LGX_OK;
   if (per_sm > kRowsMaxCtasPerSm) per_sm = kRowsMaxCtasPerSm;
   const int64_t tiles = (re - rb + kWarpTileRows - 1) / kWarpTileRows;
   const int64_t need = (tiles + WPC - 1) / WPC;
   const int64_t g = (int64_t)sm_count() * per_sm;
   const unsigned grid = (unsigned)(need < g ? (need > 0 ? need : 1) : g);
-  LGX_CUDA(launch_pdl(sizeof(typename Op::X) == 4, k_wrows<VT, Op, WPC, S>, dim3(grid),
+  const bool pdl = sizeof(typename Op::X) == 4 || re - rb <= pdl_fp64_rows();
+  LGX_CUDA(launch_pdl(pdl, k_wrows<VT, Op, WPC, S>, dim3(grid),
                       dim3(WPC * 32), smem, s, rb, re, capw,
                       (const int64_t *)a.rowptr.p, (const int32_t *)a.col.p, val, op,
                       device_error_flag()));
@@ -480,7 +493,8 @@ inline lgx_status launch_rows_cfg(int64_t rb, int64_t re, int64_t max_row, const
   const int64_t tiles = (re - rb + rpt - 1) / rpt;
   const int64_t g = (int64_t)sm_count() * RowCfg<VT, KIND>::ctas_per_sm;
   const unsigned grid = (unsigned)(tiles < g ? (tiles > 0 ? tiles : 1) : g);
-  LGX_CUDA(launch_pdl(sizeof(typename Op::X) == 4, k_rows<VT, Op, KIND>, dim3(grid),
+  const bool pdl = sizeof(typename Op::X) == 4 || re - rb <= pdl_fp64_rows();
+  LGX_CUDA(launch_pdl(pdl, k_rows<VT, Op, KIND>, dim3(grid),
                       dim3(kTileRows),
                       tile_smem_bytes<VT, KIND>(), s, rb, re, rpt, rowptr, col, val, op,
                       device_error_flag()));
@@ -488,13 +502,26 @@ inline lgx_status launch_rows_cfg(int64_t rb, int64_t re, int64_t max_row, const
   return LGX_OK;
 }
 
-// rows [rb, re) of `a` (values `val`) through the configured engine
+// autotuner slot of an operation: Op::kTuneClass when declared (SOR sweeps
+// declare 1), else 0 (products)
+template <class Op, class = void>
+struct TuneClass {
+  static constexpr int value = 0;
+};
+template <class Op>
+struct TuneClass<Op, std::void_t<decltype(Op::kTuneClass)>> {
+  static constexpr int value = Op::kTuneClass;
+};
+
+// rows [rb, re) of `a` (values `val`) through the engine configuration the
+// autotuner chose for this matrix and operation, else the process-wide one
 template <typename VT, class Op>
 inline lgx_status launch_rows(int64_t rb, int64_t re, const Csr &a, const VT *val, const Op &op,
                               cudaStream_t s) {
   if (re <= rb) return LGX_OK;
   bool done = false;
-  const int cfg = rows_config();
+  const int tuned = a.tuned[TuneClass<Op>::value][tune_value_index<VT>()];
+  const int cfg = tuned >= 0 ? tuned : rows_config();
   switch (cfg) {
     case 3: LGX_CHECK((launch_wrows<VT, Op, 4, 1>(rb, re, a, val, op, s, &done))); break;
     case 4: LGX_CHECK((launch_wrows<VT, Op, 4, 2>(rb, re, a, val, op, s, &done))); break;

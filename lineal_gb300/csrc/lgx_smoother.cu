@@ -384,6 +384,7 @@ struct SorOp {
   const float *scale = nullptr;  // bfloat16 values: row factor (the diagonal)
   using X = XT;
   static constexpr bool kReduce = false;
+  static constexpr int kTuneClass = 1;
   double *partials = nullptr;
   unsigned *counter = nullptr;
   template <int W>
@@ -535,7 +536,8 @@ lgx_status mc_sor_sweep(const lgx_colouring &c, const VT *val, double relax, int
     if (op.from_zero && k == 0 && c.pdiag.p) {
       if (re > rb) {
         const unsigned g = (unsigned)std::min<int64_t>(grid_for(re - rb, 256), 16384);
-        LGX_CUDA(launch_pdl(sizeof(XT) == 4, k_sor_first_colour<VT, XT>, dim3(g), dim3(256), 0,
+        LGX_CUDA(launch_pdl(sizeof(XT) == 4 || re - rb <= pdl_fp64_rows(),
+                            k_sor_first_colour<VT, XT>, dim3(g), dim3(256), 0,
                             s, rb, re, (const double *)c.pdiag.p, (const double *)op.rdiag,
                             scale, b, x, op.relax, op.m1, ultra, op.relax_one));
         count_launch();

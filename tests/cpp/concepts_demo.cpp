@@ -67,7 +67,16 @@ int main() {
       den += b[i] * b[i];
     }
     const double true_rel = std::sqrt(num / den);
-    const auto levels = solver.instantiate(lhs, env).amg->level_num();
+    auto inst = solver.instantiate(lhs, env);
+    const auto levels = inst.amg->level_num();
+    // the block/tile-shape autotuner reports two entries per smoothed level
+    const auto report = inst.amg->autotune(env, 2);
+    bool tuned_ok = report.size() == 2 * (levels - 1);
+    for (const auto &e : report) tuned_ok = tuned_ok && e.config >= 0 && e.config < 7;
+    if (!tuned_ok) {
+      std::printf("concepts_demo failed: autotune report of %zu entries\n", report.size());
+      return 1;
+    }
     if (!(res <= 1e-8) || !(true_rel <= 1.1e-8)) {
       std::printf("concepts_demo failed: residual %.3e true %.3e\n", res, true_rel);
       return 1;
