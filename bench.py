@@ -599,6 +599,73 @@ def batch_systems(count=1024, seed=3):
     return [((int(e),) * 3, tuple(float(c) for c in v)) for e, v in zip(edges, vs)]
 
 
+# FP64 FMA rate of GB300 (nominal 1.25 TFLOP/s; 1.2 measured with a
+# dependent-chain-free FMA loop): the roof of the matrix-free stencils, whose
+# 7 FMAs per cell outweigh their 25-48 bytes
+FP64_PEAK_TFLOPS = 1.25
+
+
+def run_stencil(args):
+    """Matrix-free 7-point stencil products at --grid^3 with both stencil
+    kernels (thread per cell; plane march with TMA-staged x planes): time,
+    algorithmic GB/s and FP64 rate against their roofs."""
+    import torch
+
+    import lineal_gb300 as g
+
+    g.build.build()
+    stream = torch.cuda.current_stream()
+    peak, peak_kind = measured_peaks()
+    dims, k, b_host = make_problem(args.grid)
+    n0, n1, n2 = dims
+    n = int(np.prod(dims))
+    # products per cell: diagonal + one per neighbour inside the grid
+    fmas = n + 2 * ((n0 - 1) * n1 * n2 + n0 * (n1 - 1) * n2 + n0 * n1 * (n2 - 1))
+    mat = np.random.default_rng(2).integers(0, 4, n).astype(np.uint8)
+    st = {"lookup": g.StencilMatrix.lookup(dims, (1.0, 1.0, 1.0), (0.5, 1.0, 2.0, 4.0), mat),
+          "value": g.StencilMatrix.value(dims, (1.0, 1.0, 1.0), k)}
+    cell_bytes = {"lookup": 1 + 8 + 8 + 8, "value": 24 + 8 + 8 + 8}
+    x = torch.randn(n, dtype=torch.float64, device="cuda")
+    y = torch.empty_like(x)
+    b = torch.as_tensor(b_host, device="cuda")
+    r = torch.empty_like(x)
+    out = {}
+    for engine, etag in ((0, "cells"), (1, "planes")):
+        g.stencil_engine(engine)
+        for kind, m in st.items():
+            for op in ("spmv", "residual"):
+                if op == "spmv":
+                    fn = lambda: g.spmv(m, x, out=y)  # noqa: E731
+                    nbytes, flops = cell_bytes[kind] * n, 2 * fmas
+                else:
+                    fn = lambda: g.lib().lgx_residual(  # noqa: E731
+                        m.handle, g._ptr(b), g._ptr(x), g._ptr(r), None, g._stream())
+                    nbytes, flops = (cell_bytes[kind] + 8) * n, 2 * fmas + n
+                for _ in range(args.warmup):
+                    fn()
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(args.steps):
+                    fn()
+                e1.record(stream)
+                e1.synchronize()
+                ms = e0.elapsed_time(e1) / args.steps
+                name = f"{kind}_{op}_{etag}"
+                gbs = nbytes / (ms * 1e-3) / 1e9
+                tf = flops / (ms * 1e-3) / 1e12
+                out[name] = {"ms": ms, "gbs": gbs, "hbm_frac": gbs / peak, "fp64_tflops": tf,
+                             "fp64_frac": tf / FP64_PEAK_TFLOPS}
+                log(f"[stencil] {name}: {ms:.3f} ms {gbs:.0f} GB/s ({gbs / peak:.0%} of HBM) "
+                    f"{tf:.2f} FP64 TFLOP/s ({tf / FP64_PEAK_TFLOPS:.0%} of nominal)")
+    g.stencil_engine(0)
+    print(json.dumps({"mode": "stencil", "grid": args.grid, "cells": n, "fp64_fmas": fmas,
+                      "hbm_peak_gbs": peak, "hbm_peak_kind": peak_kind,
+                      "fp64_peak_tflops": FP64_PEAK_TFLOPS, "fp64_peak_kind": "nominal",
+                      "kernels": out}), flush=True)
+
+
 def run_batch(args):
     """Batching form: Jacobi-BiCGStab to 1e-8 on 1024 uneven convection-diffusion
     systems in one persistent launch (per step: the whole batch, b resident)."""
@@ -825,7 +892,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--mode", default="solve",
-                    choices=["solve", "kernels", "adjoint", "batch", "multi", "profile"])
+                    choices=["solve", "kernels", "stencil", "adjoint", "batch", "multi",
+                             "profile"])
     ap.add_argument("--mixed", action="store_true", help="--mode profile: the float cycle")
     ap.add_argument("--batch-systems", type=int, default=1024)
     ap.add_argument("--batch-cpu-sample", type=int, default=16)
@@ -855,6 +923,8 @@ def main():
         ap.error("--warmup must be at least 3")
     if args.impl == "reference":
         run_reference(args)
+    elif args.mode == "stencil":
+        run_stencil(args)
     elif args.mode == "kernels":
         run_kernels(args)
     elif args.mode == "adjoint":

@@ -154,6 +154,16 @@ lgx_status lgx_gen_7pt(const int64_t dims[3], const double *d_k, lgx_dtype stora
 lgx_status lgx_row_engine_set(int config);
 int lgx_row_engine_get(void);
 
+/* Kernel of the matrix-free stencil products (lgx_spmv, lgx_residual on
+ * stencil matrices), process-wide; no reference counterpart: 0 thread per
+ * cell (default), 1 plane march with the x planes of each 8 x 64 tile staged
+ * through TMA (cp.async.bulk.tensor.3d, halo on both plane axes) into a
+ * four-plane ring in shared memory (used when the axis-2 length is even and
+ * x is 16-byte aligned; otherwise the thread-per-cell kernel runs).  Both
+ * give bit-identical results.  Default 0, or 1 with LGX_STENCIL_PLANES=1. */
+lgx_status lgx_stencil_engine_set(int engine);
+int lgx_stencil_engine_get(void);
+
 /* Autotuner of the row-engine configuration per matrix; no reference
  * counterpart (the reference's loops have a compile-time shape).  For each
  * (matrix, operation class, value type) it times all LGX_TUNE_CONFIGS

@@ -30,7 +30,7 @@ __all__ = [
     "sor_sweep", "sor_sweep_permuted", "permute", "unpermute", "gen_27pt", "gen_7pt",
     "amg_strength", "amg_aggregate", "dot", "norm2sq", "max_norm", "sampled_outer",
     "diffusion7_grad", "residual_compensated", "batch_convdiff_bicgstab", "pcg_multi",
-    "PRECON_NONE",
+    "row_engine", "stencil_engine", "PRECON_NONE",
     "PRECON_JACOBI", "PRECON_SSOR", "PRECON_AMG",
 ]
 
@@ -137,6 +137,10 @@ def _signatures(L):
     L.lgx_row_engine_get.argtypes = []
     L.lgx_row_engine_set.restype = C.c_int
     L.lgx_row_engine_set.argtypes = [C.c_int]
+    L.lgx_stencil_engine_get.restype = C.c_int
+    L.lgx_stencil_engine_get.argtypes = []
+    L.lgx_stencil_engine_set.restype = C.c_int
+    L.lgx_stencil_engine_set.argtypes = [C.c_int]
     L.lgx_kernel_launches.restype = C.c_uint64
     L.lgx_kernel_launches.argtypes = []
     sigs = {
@@ -487,6 +491,14 @@ class Colouring:
             self.close()
         except Exception:
             pass
+
+
+def stencil_engine(engine: int | None = None) -> int:
+    """Selects (when given) and returns the stencil kernel: 0 thread per
+    cell, 1 plane march with TMA-staged x planes."""
+    if engine is not None:
+        _check(lib().lgx_stencil_engine_set(int(engine)))
+    return int(lib().lgx_stencil_engine_get())
 
 
 def row_engine(config: int | None = None) -> int:

@@ -6,10 +6,14 @@
 // thread per row (27 FMAs for a 27-point row, no shuffle reductions whose
 // FP64 adds would multiply the pipe load) and stage each block's contiguous
 // CSR segment in shared memory so the global reads stay fully coalesced.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <cstdint>
+#include <cstdlib>
 
 #include "lgx_internal.cuh"
 #include "lgx_rows.cuh"
@@ -315,6 +319,163 @@ __global__ void k_st_rhs(int n0, int n1, int n2, const double *cell_value, doubl
   b[i] = sum;
 }
 
+// ---- plane-marching stencil kernel: x planes staged by TMA -----------------
+// A CTA owns a tile of kStT1 x kStT2 cells of the (axis 1, axis 2) plane and
+// marches along axis 0 through a slab of planes.  Every x plane of the tile,
+// with a one-cell halo on axis 1 and a two-cell halo on axis 2 (so that the
+// copy starts on a 16-byte boundary), arrives in shared memory through one
+// cp.async.bulk.tensor.3d copy issued by thread 0 into a ring of four
+// stages; planes p0 - 1, p0 and p0 + 1 are resident while plane p0 is
+// computed and plane p0 + 2 is in flight.  Coordinates outside the grid read
+// as 0 (they are never used: the has[] flags exclude them).  Each cell forms
+// its sum in the order of k_st_apply, so results are bit-identical.
+constexpr int kStT1 = 8, kStT2 = 64;
+constexpr int kStHalo2 = 2;  // two doubles = 16 bytes
+constexpr int kStBox1 = kStT1 + 2, kStBox2 = kStT2 + 2 * kStHalo2;
+constexpr int kStStages = 4;
+constexpr int kStPlaneBytes = kStBox1 * kStBox2 * 8;
+constexpr int kStStageStride = (kStPlaneBytes + 127) & ~127;
+constexpr int kStPlaneThreads = kStT1 * kStT2;
+static_assert(kStBox2 * 8 % 16 == 0, "TMA rows must be whole 16-byte units");
+
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int c0, int c1,
+                                            int c2, uint64_t *bar) {
+  asm volatile(
+    "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+    " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+    "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+    : "memory");
+}
+
+template <bool LOOKUP, bool RESID, bool NORM>
+__global__ void __launch_bounds__(kStPlaneThreads)
+  k_st_apply_planes(const __grid_constant__ CUtensorMap xmap, StencilDev S, int slab,
+                    const double *__restrict__ b, double *__restrict__ y, double *norm,
+                    double *partials, unsigned *counter, int *err) {
+  __shared__ __align__(128) unsigned char planes[kStStages * kStStageStride];
+  __shared__ uint64_t bar[kStStages];
+  __shared__ double sh_conn[48];
+  __shared__ bool last;
+  const double *conn = stage_conn(S, sh_conn);
+  const int t = threadIdx.x;
+  const int t1 = t / kStT2, t2 = t % kStT2;
+  const int c1 = blockIdx.y * kStT1, c2 = blockIdx.x * kStT2;
+  const int p1 = c1 + t1, p2 = c2 + t2;
+  const int z0 = blockIdx.z * slab, z1 = min(z0 + slab, S.n0);
+  const bool in = p1 < S.n1 && p2 < S.n2;
+  // plane q lives in stage (q - z0 + 1) mod 4, in its ((q - z0 + 1) / 4)-th use
+  auto stage_of = [&](int q) { return (q - z0 + 1) & (kStStages - 1); };
+  auto parity_of = [&](int q) { return (unsigned)(((q - z0 + 1) >> 2) & 1); };
+  auto plane = [&](int q) {
+    return reinterpret_cast<const double *>(planes + stage_of(q) * kStStageStride);
+  };
+  auto issue = [&](int q) {
+    const int st = stage_of(q);
+    if (q < 0 || q >= S.n0) {
+      // planes outside the grid are never read (has[] excludes them): the
+      // stage's phase completes without a copy
+      mbar_arrive(&bar[st]);
+      return;
+    }
+    fence_proxy_async();
+    mbar_expect_tx(&bar[st], kStPlaneBytes);
+    tma_load_3d(planes + st * kStStageStride, &xmap, c2 - kStHalo2, c1 - 1, q, &bar[st]);
+  };
+  if (t == 0) {
+    for (int st = 0; st < kStStages; ++st) mbar_init(&bar[st], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  // planes z0 - 1 .. z1 are read; the first four are issued up front
+  int issued = min(z0 + 2, z1);
+  if (t == 0)
+    for (int q = z0 - 1; q <= issued; ++q) issue(q);
+  int awaited = z0 - 2;
+  bool ok = true;
+  double contrib = 0.0;
+  const int r = (t1 + 1) * kStBox2 + (t2 + kStHalo2);
+  for (int p0 = z0; p0 < z1; ++p0) {
+    bool mine = true;
+    for (int q = awaited + 1; q <= p0 + 1; ++q)
+      mine = mine && mbar_wait_bounded(&bar[stage_of(q)], parity_of(q));
+    if (__syncthreads_or(!mine)) {
+      ok = false;
+      break;
+    }
+    awaited = p0 + 1;
+    if (in) {
+      const int64_t i = ((int64_t)p0 * S.n1 + p1) * S.n2 + p2;
+      double cv[6];
+      int64_t cj[6];
+      bool has[6];
+      st_row<LOOKUP>(S, conn, p0, p1, p2, i, cv, cj, has);
+      const double *P0 = plane(p0);
+      const double xv[6] = {plane(p0 - 1)[r], P0[r - kStBox2], P0[r - 1],
+                            P0[r + 1],        P0[r + kStBox2], plane(p0 + 1)[r]};
+      double sum = 0.0;
+#pragma unroll
+      for (int e = 0; e < 6; ++e)
+        if (has[e]) sum = fma(-cv[e], xv[e], sum);
+      sum = fma(S.diag[i], P0[r], sum);
+      if constexpr (RESID) {
+        const double rv = b[i] - sum;
+        y[i] = rv;
+        if constexpr (NORM) contrib += rv * rv;
+      } else {
+        y[i] = sum;
+      }
+    }
+    __syncthreads();  // plane p0 - 1 is no longer read: its stage takes plane p0 + 3
+    if (t == 0 && p0 + 3 <= z1) {
+      issue(p0 + 3);
+      issued = p0 + 3;
+    }
+  }
+  if (!ok) {
+    // a copy did not land in time: record it, let this CTA's copies finish
+    // (bounded) and leave without a result
+    if (t == 0) {
+      atomicExch(err, 1);
+      for (int q = awaited + 1; q <= issued; ++q)
+        mbar_wait_bounded(&bar[stage_of(q)], parity_of(q));
+    }
+    return;
+  }
+  if constexpr (NORM) {
+    const unsigned bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    const unsigned nb = gridDim.x * gridDim.y * gridDim.z;
+    // fixed-order block sum: lanes by shuffle-free halving in shared memory
+    __shared__ double sh[kStPlaneThreads];
+    sh[t] = contrib;
+    __syncthreads();
+    for (unsigned h = kStPlaneThreads / 2; h > 0; h >>= 1) {
+      if (t < h) sh[t] += sh[t + h];
+      __syncthreads();
+    }
+    if (t == 0) {
+      partials[bid] = sh[0];
+      __threadfence();
+      last = atomicAdd(counter, 1u) == nb - 1;
+    }
+    __syncthreads();
+    if (last) {
+      __threadfence();
+      double acc = 0.0;
+      for (unsigned k = t; k < nb; k += kStPlaneThreads) acc += ((volatile double *)partials)[k];
+      sh[t] = acc;
+      __syncthreads();
+      for (unsigned h = kStPlaneThreads / 2; h > 0; h >>= 1) {
+        if (t < h) sh[t] += sh[t + h];
+        __syncthreads();
+      }
+      if (t == 0) {
+        norm[0] = sh[0];
+        *counter = 0;
+      }
+    }
+  }
+}
+
 static dim3 st_grid(const StencilDesc &st) {
   return dim3((unsigned)((st.dims[2] + 31) / 32), (unsigned)((st.dims[1] + 7) / 8),
               (unsigned)st.dims[0]);
@@ -388,11 +549,112 @@ lgx_status stencil_ensure(lgx_matrix *a, cudaStream_t s) {
   return LGX_OK;
 }
 
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                   const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                   const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against libcuda)
+static EncodeTiledFn encode_tiled() {
+  static const EncodeTiledFn fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      return (EncodeTiledFn) nullptr;
+    }
+    return (EncodeTiledFn)p;
+  }();
+  return fn;
+}
+
+// Stencil engine: 0 thread per cell (default), 1 plane march with TMA-staged
+// x planes.  Both are FP64-pipe bound on GB300 (7 FMAs per cell against 25-48
+// bytes); the thread-per-cell kernel keeps more cells in flight and is the
+// faster one (256^3: 0.204-0.214 ms against 0.267-0.275 ms).
+static std::atomic<int> g_stencil_engine{[] {
+  const char *e = std::getenv("LGX_STENCIL_PLANES");
+  return (e && e[0] == '1') ? 1 : 0;
+}()};
+
+static bool stencil_planes_enabled() { return g_stencil_engine.load(std::memory_order_relaxed); }
+
+template <bool LOOKUP, bool RESID, bool NORM>
+static lgx_status launch_planes(const StencilDesc &st, const CUtensorMap &map,
+                                const StencilDev &S, const double *b, double *y, double *norm,
+                                double *partials, unsigned *counter, cudaStream_t s) {
+  static int per_sm = -1;
+  if (per_sm < 0) {
+    int v = 0;
+    LGX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &v, k_st_apply_planes<LOOKUP, RESID, NORM>, kStPlaneThreads, 0));
+    per_sm = std::max(v, 1);
+  }
+  const int64_t n0 = st.dims[0], n1 = st.dims[1], n2 = st.dims[2];
+  const int64_t gx = (n2 + kStT2 - 1) / kStT2, gy = (n1 + kStT1 - 1) / kStT1;
+  // slabs along axis 0 so that about one wave of CTAs is resident
+  const int64_t slots = (int64_t)sm_count() * per_sm;
+  const int64_t slabs = std::min<int64_t>(std::max<int64_t>(slots / (gx * gy), 1), n0);
+  const int slab = (int)((n0 + slabs - 1) / slabs);
+  const dim3 g((unsigned)gx, (unsigned)gy, (unsigned)((n0 + slab - 1) / slab));
+  k_st_apply_planes<LOOKUP, RESID, NORM><<<g, kStPlaneThreads, 0, s>>>(
+    map, S, slab, b, y, norm, partials, counter, device_error_flag());
+  LGX_LAUNCH_CHECK();
+  count_launch();
+  return LGX_OK;
+}
+
+// Runs the plane-marching kernel when its TMA preconditions hold (x on a
+// 16-byte boundary, even axis-2 length so every plane row is a whole number
+// of 16-byte units); *done tells whether it ran.
+static lgx_status stencil_apply_planes(const lgx_matrix *a, const double *x, const double *b,
+                                       double *y, double *norm, double *partials,
+                                       unsigned *counter, cudaStream_t s, bool *done) {
+  *done = false;
+  const StencilDesc &st = a->st;
+  const EncodeTiledFn encode = encode_tiled();
+  if (!stencil_planes_enabled() || !encode || st.dims[2] % 2 != 0 ||
+      (reinterpret_cast<uintptr_t>(x) & 15) != 0 || st.dims[1] > (int64_t)kStT1 * 65535)
+    return LGX_OK;
+  CUtensorMap map;
+  const cuuint64_t gdim[3] = {(cuuint64_t)st.dims[2], (cuuint64_t)st.dims[1],
+                              (cuuint64_t)st.dims[0]};
+  const cuuint64_t gstride[2] = {(cuuint64_t)st.dims[2] * 8,
+                                 (cuuint64_t)st.dims[2] * st.dims[1] * 8};
+  const cuuint32_t box[3] = {(cuuint32_t)kStBox2, (cuuint32_t)kStBox1, 1};
+  const cuuint32_t estride[3] = {1, 1, 1};
+  if (encode(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<double *>(x), gdim, gstride, box,
+             estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+             CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return LGX_OK;
+  const StencilDev S = dev_of(a);
+  const bool lk = st.lookup;
+  if (!b) {
+    LGX_CHECK((lk ? launch_planes<true, false, false> : launch_planes<false, false, false>)(
+      st, map, S, b, y, norm, partials, counter, s));
+  } else if (!norm) {
+    LGX_CHECK((lk ? launch_planes<true, true, false> : launch_planes<false, true, false>)(
+      st, map, S, b, y, norm, partials, counter, s));
+  } else {
+    LGX_CHECK((lk ? launch_planes<true, true, true> : launch_planes<false, true, true>)(
+      st, map, S, b, y, norm, partials, counter, s));
+  }
+  *done = true;
+  return LGX_OK;
+}
+
 static lgx_status stencil_apply(const lgx_matrix *ac, const double *x, const double *b, double *y,
                                 double *norm, double *partials, unsigned *counter,
                                 cudaStream_t s) {
   lgx_matrix *a = const_cast<lgx_matrix *>(ac);
   LGX_CHECK(stencil_ensure(a, s));
+  bool done = false;
+  LGX_CHECK(stencil_apply_planes(a, x, b, y, norm, partials, counter, s, &done));
+  if (done) return LGX_OK;
   StencilDev S = dev_of(a);
   const dim3 g = st_grid(a->st);
   const bool lk = a->st.lookup;
@@ -413,6 +675,7 @@ static lgx_status stencil_apply(const lgx_matrix *ac, const double *x, const dou
                                                               counter);
   }
   LGX_LAUNCH_CHECK();
+  count_launch();
   return LGX_OK;
 }
 
@@ -608,6 +871,14 @@ lgx_status lgx_stencil_create_value(const int64_t dims[3], const double q[3], co
   return stencil_create(dims, q, nullptr, nullptr, d_k, sol_start, sol_end, zero_to_one, stream,
                         out);
 }
+
+lgx_status lgx_stencil_engine_set(int engine) {
+  if (engine != 0 && engine != 1) return fail(LGX_ERR_INVALID, "stencil engine must be 0 or 1");
+  g_stencil_engine.store(engine, std::memory_order_relaxed);
+  return LGX_OK;
+}
+
+int lgx_stencil_engine_get(void) { return g_stencil_engine.load(std::memory_order_relaxed); }
 
 lgx_status lgx_spmv(const lgx_matrix *a, const double *d_x, double *d_y, lgx_stream stream) {
   if (!a || (a->n > 0 && (!d_x || !d_y))) return fail(LGX_ERR_INVALID, "null argument");

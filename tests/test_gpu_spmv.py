@@ -110,6 +110,50 @@ def test_stencil_value_bitexact(cuda, dims):
     assert abs(nrm - rr @ rr) <= 1e-13 * (rr @ rr)
 
 
+# with engine 1, even axis-2 lengths run the plane-marching kernel (x planes
+# staged by TMA); the cases cover partial tiles on both plane axes, single
+# planes, tiny grids and several slabs per column of tiles (the 1600 x 64
+# planes); odd lengths fall back to the thread-per-cell kernel
+PLANE_DIMS = [(6, 9, 130), (1, 17, 66), (2, 1, 2), (12, 1600, 64), (70, 3, 64), (3, 8, 192),
+              (5, 7, 9)]
+
+
+@pytest.fixture(params=[0, 1], ids=["cells", "planes"])
+def stencil_engine(cuda, request):
+    before = cuda.stencil_engine()
+    cuda.stencil_engine(request.param)
+    yield request.param
+    cuda.stencil_engine(before)
+
+
+@pytest.mark.parametrize("dims", PLANE_DIMS)
+@pytest.mark.parametrize("valuator", ["lookup", "value"])
+def test_stencil_engines_bitexact(cuda, stencil_engine, dims, valuator):
+    n = int(np.prod(dims))
+    q = lo.axis_quotients(dims, (1.1, 0.9, 1.7))
+    if valuator == "lookup":
+        mat = _lookup_case(dims, 13)
+        coeffs = (0.5, 1.0, 2.0, 3.0)
+        ref = lo.Stencil(dims, q=q, mat=mat, coeffs=coeffs, sol_start=1.0, sol_end=0.25)
+        m = cuda.StencilMatrix.lookup(dims, q, coeffs, mat, 1.0, 0.25)
+    else:
+        k = np.exp(np.random.default_rng(10).standard_normal(n))
+        ref = lo.Stencil(dims, q=q, k=k, sol_start=1.0, sol_end=0.0)
+        m = cuda.StencilMatrix.value(dims, q, k, 1.0, 0.0)
+    x = np.random.default_rng(11).uniform(-1, 1, n)
+    np.testing.assert_array_equal(cuda.spmv(m, x).cpu().numpy(), ref.spmv(x))
+    b = np.random.default_rng(12).uniform(-1, 1, n)
+    r, nrm = cuda.residual(m, b, x)
+    rr = b - ref.spmv(x)
+    np.testing.assert_array_equal(r.cpu().numpy(), rr)
+    assert abs(nrm - rr @ rr) <= 1e-13 * (rr @ rr)
+
+
+def test_stencil_engine_rejects_unknown(cuda):
+    with pytest.raises(cuda.LinealError):
+        cuda.stencil_engine(2)
+
+
 def test_reductions(cuda):
     rng = np.random.default_rng(0)
     for n in (1, 255, 256 * 8 + 3, 1 << 20):
