@@ -148,9 +148,10 @@ lgx_status lgx_gen_7pt(const int64_t dims[3], const double *d_k, lgx_dtype stora
 /* Configuration of the CSR row kernels (SpMV, residual, Jacobi, SOR) used by
  * later launches, process-wide; no reference counterpart (tuning):
  * 0-2 CTA tiles (two stages / one CTA per SM, one stage / two CTAs, two small
- * stages / two CTAs), 3-6 warp tiles (4 warps x 1 stage, 4 x 2, 8 x 1, 8 x 2
- * per CTA).  Every configuration gives bit-identical results.  Default 3, or
- * the environment variable LGX_ROWS_CONFIG. */
+ * stages / two CTAs), 3-7 warp tiles (4 warps x 1 stage, 4 x 2, 8 x 1, 8 x 2
+ * per CTA; 7: 4 x 1 with registers capped for seven CTAs per SM).  Every
+ * configuration gives bit-identical results.  Default 3, or the environment
+ * variable LGX_ROWS_CONFIG. */
 lgx_status lgx_row_engine_set(int config);
 int lgx_row_engine_get(void);
 
@@ -175,7 +176,7 @@ int lgx_stencil_engine_get(void);
  * freed by the call); matrix values are not touched.  Synchronises `stream`.
  * Tune before the first solve of a Krylov solver that captures CUDA graphs:
  * a captured iteration keeps the shapes it was recorded with. */
-#define LGX_TUNE_CONFIGS 7
+#define LGX_TUNE_CONFIGS 8
 typedef struct lgx_tune_entry {
   int32_t level;       /* hierarchy level (0 for a single matrix) */
   int32_t op;          /* 0 products (SpMV, residual), 1 SOR sweeps */

@@ -55,7 +55,7 @@ class LinealLibraryMissing(ImportError):
 _lib = None
 
 
-TUNE_CONFIGS = 7  # LGX_TUNE_CONFIGS
+TUNE_CONFIGS = 8  # LGX_TUNE_CONFIGS
 
 
 class _TuneEntry(C.Structure):

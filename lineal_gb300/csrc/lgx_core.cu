@@ -40,7 +40,7 @@ int sm_count() {
 static std::atomic<int> g_rows_config{[] {
   const char *e = std::getenv("LGX_ROWS_CONFIG");
   const int v = e ? std::atoi(e) : 3;
-  return (v >= 0 && v <= 6) ? v : 3;
+  return (v >= 0 && v <= 7) ? v : 3;
 }()};
 
 int rows_config() { return g_rows_config.load(std::memory_order_relaxed); }
@@ -680,8 +680,8 @@ lgx_status lgx_dot(int64_t n, const double *d_a, const double *d_b, double *d_ou
 }
 
 lgx_status lgx_row_engine_set(int config) {
-  if (config < 0 || config > 6)
-    return fail(LGX_ERR_INVALID, "row engine configuration must be in [0, 6]");
+  if (config < 0 || config > 7)
+    return fail(LGX_ERR_INVALID, "row engine configuration must be in [0, 7]");
   g_rows_config.store(config, std::memory_order_relaxed);
   return LGX_OK;
 }

@@ -311,21 +311,25 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
 }
 
 // XT = the type of the gathered x values (Op::X)
-template <int WPC, typename XT>
+// MB = CTAs per SM the registers are capped for (0: the default of WPC)
+template <int WPC, typename XT, int MB = 0>
 struct WrowsBounds {
   // 4 warps per CTA: registers <= 65536 / (5 * 128) so that five CTAs (20
   // warps) fit an SM, and 8 double (16 float) gathers per round to stay
-  // within them; 8 warps per CTA: two CTAs (16 warps), 16 gathers per round
-  static constexpr int min_blocks = WPC == 4 ? 5 : 2;
+  // within them; 8 warps per CTA: two CTAs (16 warps), 16 gathers per round;
+  // MB = 7 (4 warps): seven CTAs (28 warps) where shared memory allows it
+  // (float and bfloat16 stages), 16 float (8 double) gathers per round
+  // within 73 registers
+  static constexpr int min_blocks = MB ? MB : (WPC == 4 ? 5 : 2);
   static constexpr int gather = (WPC == 4 && sizeof(XT) == 8) ? 8 : 16;
 };
 
-template <typename VT, class Op, int WPC, int S>
-__global__ void __launch_bounds__(WPC * 32, WrowsBounds<WPC, typename Op::X>::min_blocks)
+template <typename VT, class Op, int WPC, int S, int MB = 0>
+__global__ void __launch_bounds__(WPC * 32, WrowsBounds<WPC, typename Op::X, MB>::min_blocks)
   k_wrows(int64_t rb, int64_t re, int capw, const int64_t *__restrict__ rowptr,
           const int32_t *__restrict__ col, const VT *__restrict__ val, Op op, int *err) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int W = WrowsBounds<WPC, typename Op::X>::gather;
+  constexpr int W = WrowsBounds<WPC, typename Op::X, MB>::gather;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const size_t sb = wstage_bytes(capw, sizeof(VT));
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw) + warp * S;
@@ -437,10 +441,11 @@ __global__ void __launch_bounds__(WPC * 32, WrowsBounds<WPC, typename Op::X>::mi
 // engine configuration used by launch_rows (LGX_ROWS_CONFIG selects another
 // entry of the tuning space): 0-2 CTA tiles (RowCfg kinds); warp tiles with
 // 3: 4 warps x 1 stage, 4: 4 warps x 2 stages, 5: 8 warps x 1 stage,
-// 6: 8 warps x 2 stages per CTA
+// 6: 8 warps x 2 stages per CTA, 7: 4 warps x 1 stage with registers capped
+// for seven CTAs per SM
 int rows_config();
 
-template <typename VT, class Op, int WPC, int S>
+template <typename VT, class Op, int WPC, int S, int MB = 0>
 inline lgx_status launch_wrows(int64_t rb, int64_t re, const Csr &a, const VT *val, const Op &op,
                                cudaStream_t s, bool *done) {
   *done = false;
@@ -450,7 +455,7 @@ inline lgx_status launch_wrows(int64_t rb, int64_t re, const Csr &a, const VT *v
   const size_t smem = wsmem_bytes(WPC, S, capw, sizeof(VT));
   if (smem > (size_t)kWrowsSmemMax) return LGX_OK;  // too long rows: CTA tiles
   static const cudaError_t attr = cudaFuncSetAttribute(
-    k_wrows<VT, Op, WPC, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, kWrowsSmemMax);
+    k_wrows<VT, Op, WPC, S, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize, kWrowsSmemMax);
   LGX_CUDA(attr);
   // occupancy of the last shared-memory size asked for (one query per
   // matrix shape instead of one per launch): smem in the high, CTAs per SM
@@ -461,7 +466,7 @@ inline lgx_status launch_wrows(int64_t rb, int64_t re, const Csr &a, const VT *v
   if (cached >> 32 == (uint64_t)smem) {
     per_sm = (int)(uint32_t)cached;
   } else {
-    LGX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wrows<VT, Op, WPC, S>,
+    LGX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wrows<VT, Op, WPC, S, MB>,
                                                            WPC * 32, smem));
     occ_cache.store(((uint64_t)smem << 32) | (uint32_t)per_sm, std::memory_order_relaxed);
   }
@@ -472,7 +477,7 @@ inline lgx_status launch_wrows(int64_t rb, int64_t re, const Csr &a, const VT *v
   const int64_t g = (int64_t)sm_count() * per_sm;
   const unsigned grid = (unsigned)(need < g ? (need > 0 ? need : 1) : g);
   const bool pdl = sizeof(typename Op::X) == 4 || re - rb <= pdl_fp64_rows();
-  LGX_CUDA(launch_pdl(pdl, k_wrows<VT, Op, WPC, S>, dim3(grid),
+  LGX_CUDA(launch_pdl(pdl, k_wrows<VT, Op, WPC, S, MB>, dim3(grid),
                       dim3(WPC * 32), smem, s, rb, re, capw,
                       (const int64_t *)a.rowptr.p, (const int32_t *)a.col.p, val, op,
                       device_error_flag()));
@@ -527,6 +532,7 @@ inline lgx_status launch_rows(int64_t rb, int64_t re, const Csr &a, const VT *va
     case 4: LGX_CHECK((launch_wrows<VT, Op, 4, 2>(rb, re, a, val, op, s, &done))); break;
     case 5: LGX_CHECK((launch_wrows<VT, Op, 8, 1>(rb, re, a, val, op, s, &done))); break;
     case 6: LGX_CHECK((launch_wrows<VT, Op, 8, 2>(rb, re, a, val, op, s, &done))); break;
+    case 7: LGX_CHECK((launch_wrows<VT, Op, 4, 1, 7>(rb, re, a, val, op, s, &done))); break;
     default: break;
   }
   if (done) return LGX_OK;

@@ -1,9 +1,10 @@
 // Autotuner of the CSR row-engine configuration (block and tile shapes).
 //
-// The row engine (lgx_rows.cuh) has seven configurations: three CTA-tile
-// shapes and four warp-tile shapes (warps per CTA x pipeline stages).  Which
-// one is fastest depends on the matrix (rows, entries per row, how many
-// rows there are to spread over 152 SMs) and on the operation: a product
+// The row engine (lgx_rows.cuh) has eight configurations: three CTA-tile
+// shapes and five warp-tile shapes (warps per CTA x pipeline stages x CTAs
+// per SM).  Which one is fastest depends on the matrix (rows, entries per
+// row, how many rows there are to spread over 152 SMs) and on the
+// operation: a product
 // streams values once, an SOR sweep runs one launch per colour over a
 // fraction of the rows.  The tuner times every configuration on the matrix
 // itself (replays of a CUDA graph of the operation, timed with CUDA events,
@@ -28,7 +29,7 @@ namespace lgx {
 lgx_status amg_apply_permuted(lgx_amg &h, const double *b, double *x, cudaStream_t s);
 int rows_config();
 
-constexpr int kTuneConfigs = 7;
+constexpr int kTuneConfigs = 8;
 static_assert(kTuneConfigs == LGX_TUNE_CONFIGS, "tuning space and ABI disagree");
 
 namespace {

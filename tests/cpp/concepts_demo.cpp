@@ -72,7 +72,7 @@ int main() {
     // the block/tile-shape autotuner reports two entries per smoothed level
     const auto report = inst.amg->autotune(env, 2);
     bool tuned_ok = report.size() == 2 * (levels - 1);
-    for (const auto &e : report) tuned_ok = tuned_ok && e.config >= 0 && e.config < 7;
+    for (const auto &e : report) tuned_ok = tuned_ok && e.config >= 0 && e.config < LGX_TUNE_CONFIGS;
     if (!tuned_ok) {
       std::printf("concepts_demo failed: autotune report of %zu entries\n", report.size());
       return 1;

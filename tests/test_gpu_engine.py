@@ -11,7 +11,7 @@ import oracle as lo
 
 pytestmark = pytest.mark.gpu
 
-CONFIGS = list(range(7))
+CONFIGS = list(range(8))
 
 
 @pytest.fixture
@@ -111,7 +111,7 @@ def test_sor_permuted_matches_natural_and_oracle(engine, config, forward):
 
 def test_row_engine_rejects_unknown_configuration(cuda):
     with pytest.raises(cuda.LinealError):
-        cuda.row_engine(7)
+        cuda.row_engine(8)
 
 
 @pytest.mark.parametrize("relax", [1.0, 0.7])
