@@ -302,14 +302,17 @@ def run_gb300(args):
     log(f"[gb300] generated {dims} nnz={nnz} in {time.perf_counter() - t0:.2f}s")
 
     hier_kw = dict(min_coarsen_size=2000, partition_size=args.partition_size,
-                   partition_growth=args.partition_growth, min_partitions=args.min_partitions)
+                   partition_growth=args.partition_growth, min_partitions=args.min_partitions,
+                   grid27=args.grid27)
     wright = g.HierarchyWright(**hier_kw)
     t0 = time.perf_counter()
     h64 = wright.instantiate(a, finest_colouring=col)
     torch.cuda.synchronize()
     setup64 = time.perf_counter() - t0
     rows, nnzs = h64.sizes()
-    log(f"[gb300] FP64 hierarchy {rows} in {setup64:.2f}s")
+    grid_on = h64.grid27_active()
+    log(f"[gb300] FP64 hierarchy {rows} in {setup64:.2f}s"
+        f"{' (finest level: 27-point grid kernels)' if grid_on else ''}")
     tune64 = autotune_log("FP64", h64) if args.autotune else None
 
     b = torch.as_tensor(b_host, device="cuda")
@@ -444,6 +447,8 @@ def run_gb300(args):
             d_b = h_b.to("cuda", non_blocking=True)
             d_colours = h_col_colours.to("cuda", non_blocking=True)
             m = g.CsrMatrix.from_device(d_rowptr, d_col, d_val, symmetric=True)
+            if args.grid27:
+                m.set_grid27(dims)  # the caller knows its operator is the 27-point grid
             del d_rowptr, d_col, d_val
             c = g.Colouring.from_array(m, d_colours, 8)
             hh = g.HierarchyWright(cycle_f32=True, **hier_kw).instantiate(
@@ -485,6 +490,9 @@ def run_gb300(args):
                     "partition_growth": args.partition_growth,
                     "min_partitions": args.min_partitions,
                     "finest_colouring": "grid parity, 8 colours",
+                    "finest_kernels": ("27-point grid rows, column indices computed "
+                                       "(lgx_amg_params.grid27)" if grid_on
+                                       else "CSR row engine"),
                     "row_engine": ("autotuned per level (lgx_amg_autotune, setup-time, "
                                    "outside the timed solves; e2e untuned)"
                                    if args.autotune else "process-wide configuration 3")},
@@ -725,8 +733,10 @@ def run_batch(args):
 
 def run_profile(args):
     """Profiler target: one untimed AMG-PCG solve of the --grid^3 27-point
-    workload (FP64, or the float cycle with --mixed), then one more inside the
-    NVTX range "solve" (ncu --nvtx --nvtx-include solve/ selects its kernels)."""
+    workload (FP64, or the float cycle with --mixed, with bfloat16 level values
+    with --bf16; row engine autotuned unless --no-autotune), then one more
+    inside the NVTX range "solve" (ncu --nvtx --nvtx-include solve/ selects
+    its kernels)."""
     import torch
 
     import lineal_gb300 as g
@@ -735,10 +745,13 @@ def run_profile(args):
     dims, k, b_host = make_problem(args.grid)
     a = g.gen_27pt(dims, k)
     col = g.Colouring.from_array(a, parity_colours(dims), 8)
-    h = g.HierarchyWright(min_coarsen_size=2000, cycle_f32=args.mixed,
+    mixed = args.mixed or args.bf16
+    h = g.HierarchyWright(min_coarsen_size=2000, cycle_f32=mixed, cycle_bf16=args.bf16,
                           partition_size=args.partition_size,
                           partition_growth=args.partition_growth,
                           min_partitions=args.min_partitions).instantiate(a, finest_colouring=col)
+    if args.autotune:
+        h.autotune(reps=3)
     b = torch.as_tensor(b_host, device="cuda")
     res = g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=1e-8, maxit=500)
     torch.cuda.synchronize()
@@ -746,7 +759,8 @@ def run_profile(args):
     res = g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=1e-8, maxit=500)
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
-    log(f"[profile] {'mixed' if args.mixed else 'fp64'} solve: {res.iterations} it")
+    form = "bf16" if args.bf16 else "mixed" if args.mixed else "fp64"
+    log(f"[profile] {form} solve: {res.iterations} it")
 
 
 def run_multi(args):
@@ -895,6 +909,8 @@ def main():
                     choices=["solve", "kernels", "stencil", "adjoint", "batch", "multi",
                              "profile"])
     ap.add_argument("--mixed", action="store_true", help="--mode profile: the float cycle")
+    ap.add_argument("--bf16", action="store_true",
+                    help="--mode profile: the float cycle with bfloat16 level values")
     ap.add_argument("--batch-systems", type=int, default=1024)
     ap.add_argument("--batch-cpu-sample", type=int, default=16)
     ap.add_argument("--fd-directions", type=int, default=64)
@@ -906,6 +922,8 @@ def main():
     ap.add_argument("--reference-iterations", type=int, default=61,
                     help="iterations of the full-size solve used to extrapolate the CPU sample "
                          "(61: the 256^3 AMG-PCG iteration count of the same algorithm)")
+    ap.add_argument("--no-grid27", dest="grid27", action="store_false",
+                    help="finest level on the CSR row engine even for the 27-point grid")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="skip the row-engine autotuner of the solve-mode hierarchies "
                          "(setup-time: every level's shapes timed before the timed solves)")

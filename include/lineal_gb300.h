@@ -144,6 +144,11 @@ lgx_status lgx_gen_27pt(const int64_t dims[3], const double *d_k, lgx_dtype stor
                         lgx_stream stream, lgx_matrix **out);
 lgx_status lgx_gen_7pt(const int64_t dims[3], const double *d_k, lgx_dtype storage,
                        lgx_stream stream, lgx_matrix **out);
+/* Declares that a CSR matrix is a 27-point operator on an n0 x n1 x n2 grid
+ * (row (i n1 + j) n2 + k couples the cell to its in-grid neighbours), as
+ * lgx_gen_27pt's matrices are; an AMG hierarchy checks the structure on the
+ * device before it relies on it.  No reference counterpart. */
+lgx_status lgx_csr_set_grid27(lgx_matrix *a, const int64_t dims[3]);
 
 /* Configuration of the CSR row kernels (SpMV, residual, Jacobi, SOR) used by
  * later launches, process-wide; no reference counterpart (tuning):
@@ -306,6 +311,12 @@ typedef struct {
   int cycle_bf16;              /* with cycle_f32: smoothers and residuals read bfloat16
                                   values a_ij / a_ii with the diagonal a_ii as a per-row
                                   float scale (2 bytes per entry instead of 4) */
+  int grid27;                  /* 1 (default): when the finest matrix is a 27-point
+                                  operator on an even grid (lgx_gen_27pt, or declared by
+                                  lgx_csr_set_grid27) and the finest colouring is the
+                                  parity colouring, its products and sweeps compute the
+                                  column indices from the grid instead of reading them
+                                  (bit-identical results); 0: always the CSR kernels */
 } lgx_amg_params;
 
 void lgx_amg_default_params(lgx_amg_params *p);
@@ -346,6 +357,9 @@ lgx_status lgx_amg_autotune(lgx_amg *h, int reps, lgx_tune_entry *out, int max_o
                             lgx_stream stream);
 /* Drops the tuned choices: launches use the process-wide configuration. */
 lgx_status lgx_amg_autotune_reset(lgx_amg *h);
+/* 1 when the finest level runs the 27-point grid kernels (see
+ * lgx_amg_params.grid27), else 0. */
+int lgx_amg_grid27(const lgx_amg *h);
 
 /* The individual setup steps, for parity checks.
  * Strength of connection (dependency/criterion.hpp:35-78): per stored entry

@@ -399,6 +399,7 @@ struct MultiGridSolver : SharedStationaryIterativeSolverBase {
   double smoother_relax = 1.0;
   bool float_cycle = false;
   bool bf16_values = false;  // with float_cycle: bfloat16 level values, diagonal row scales
+  bool grid27 = true;        // 27-point grid finest level without column indices
 
   class Instance {
    public:
@@ -421,6 +422,7 @@ struct MultiGridSolver : SharedStationaryIterativeSolverBase {
       p.smoother_relax = s.smoother_relax;
       p.cycle_f32 = s.float_cycle;
       p.cycle_bf16 = s.bf16_values;
+      p.grid27 = s.grid27;
       check(lgx_amg_setup(lhs.handle(), &p, nullptr, env.stream(), &h_));
     }
     Instance(const Instance &) = delete;

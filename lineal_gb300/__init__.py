@@ -90,6 +90,7 @@ class _AmgParams(C.Structure):
         ("smoother_ultra", C.c_int),
         ("colour_seed", C.c_uint64),
         ("cycle_bf16", C.c_int),
+        ("grid27", C.c_int),
     ]
 
 
@@ -141,6 +142,8 @@ def _signatures(L):
     L.lgx_stencil_engine_get.argtypes = []
     L.lgx_stencil_engine_set.restype = C.c_int
     L.lgx_stencil_engine_set.argtypes = [C.c_int]
+    L.lgx_amg_grid27.restype = C.c_int
+    L.lgx_amg_grid27.argtypes = [C.c_void_p]
     L.lgx_kernel_launches.restype = C.c_uint64
     L.lgx_kernel_launches.argtypes = []
     sigs = {
@@ -159,6 +162,7 @@ def _signatures(L):
         "lgx_stencil_to_csr": [V, V, V, P(V)],
         "lgx_gen_27pt": [V, V, C.c_int, V, P(V)],
         "lgx_gen_7pt": [V, V, C.c_int, V, P(V)],
+        "lgx_csr_set_grid27": [V, V],
         "lgx_dot": [I64, V, V, V, V],
         "lgx_dot_static": [I64, V, V, V, V],
         "lgx_norm2sq": [I64, V, V, V],
@@ -277,6 +281,12 @@ class _Matrix:
 
     def spmv(self, x, out=None):
         return spmv(self, x, out)
+
+    def set_grid27(self, dims):
+        """Declares this CSR matrix a 27-point operator on the grid `dims`
+        (as gen_27pt's matrices are)."""
+        d = np.ascontiguousarray(dims, dtype=np.int64)
+        _check(lib().lgx_csr_set_grid27(self._h, _ptr(d)))
 
     def autotune(self, reps: int = 5) -> dict:
         """Times every row-engine configuration on this CSR matrix's FP64
@@ -579,6 +589,7 @@ class HierarchyWright:
     smoother_ultra: bool = False
     colour_seed: int = 0x5EED
     cycle_bf16: bool = False
+    grid27: bool = True
 
     def params(self) -> _AmgParams:
         p = _AmgParams()
@@ -645,6 +656,10 @@ class Hierarchy:
 
     def autotune_reset(self):
         _check(lib().lgx_amg_autotune_reset(self._h))
+
+    def grid27_active(self) -> bool:
+        """Whether the finest level runs the 27-point grid kernels."""
+        return bool(lib().lgx_amg_grid27(self._h))
 
     def close(self):
         if self._h:

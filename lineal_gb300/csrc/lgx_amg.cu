@@ -1024,6 +1024,10 @@ static lgx_status amg_build(const lgx_matrix *m, const lgx_amg_params &p,
     }
     if (h.f32) LGX_CHECK(colouring_make_f32(*lv.col, s));
     if (h.f32 && p.cycle_bf16) LGX_CHECK(colouring_make_bf16(*lv.col, s));
+    if (l == 0 && p.grid27 && m->grid27[0] > 0) {
+      bool attached = false;
+      LGX_CHECK(grid27_attach(*lv.col, m->grid27, s, &attached));
+    }
     timer.mark(s, "colouring", l);
   }
   // transfers in permuted spaces
@@ -1229,6 +1233,7 @@ void lgx_amg_default_params(lgx_amg_params *p) {
   p->smoother_ultra = 0;
   p->colour_seed = 0x5eed;
   p->cycle_bf16 = 0;
+  p->grid27 = 1;
 }
 
 lgx_status lgx_amg_setup(const lgx_matrix *a, const lgx_amg_params *p,
@@ -1325,6 +1330,10 @@ lgx_status lgx_amg_vcycle(lgx_amg *h, const double *d_b, double *d_x, lgx_stream
     return scatter<double, double>(n, perm, h->nat_x.p, d_x, stream);
   }
   return amg_apply_permuted(*h, d_b, d_x, stream);
+}
+
+int lgx_amg_grid27(const lgx_amg *h) {
+  return h && !h->lv.empty() && h->lv[0]->col && h->lv[0]->col->pcsr.grid ? 1 : 0;
 }
 
 lgx_status lgx_amg_strength(const lgx_matrix *a, double theta, uint8_t *d_depends,

@@ -661,7 +661,18 @@ lgx_status lgx_matrix_info(const lgx_matrix *a, int *kind, int64_t *n, int64_t *
 
 lgx_status lgx_gen_27pt(const int64_t dims[3], const double *d_k, lgx_dtype storage,
                         lgx_stream stream, lgx_matrix **out) {
-  return gen_structured(dims, d_k, 27, storage, stream, out);
+  LGX_CHECK(gen_structured(dims, d_k, 27, storage, stream, out));
+  for (int d = 0; d < 3; ++d) (*out)->grid27[d] = dims[d];
+  return LGX_OK;
+}
+
+lgx_status lgx_csr_set_grid27(lgx_matrix *a, const int64_t dims[3]) {
+  if (!a || !dims) return fail(LGX_ERR_INVALID, "null argument");
+  if (a->kind != LGX_MATRIX_CSR) return fail(LGX_ERR_INVALID, "not a CSR matrix");
+  if (dims[0] < 1 || dims[1] < 1 || dims[2] < 1 || dims[0] * dims[1] * dims[2] != a->n)
+    return fail(LGX_ERR_INVALID, "grid does not have one cell per row");
+  for (int d = 0; d < 3; ++d) a->grid27[d] = dims[d];
+  return LGX_OK;
 }
 
 lgx_status lgx_gen_7pt(const int64_t dims[3], const double *d_k, lgx_dtype storage,

@@ -1,0 +1,458 @@
+// Finest level of a 27-point grid matrix without column indices.
+//
+// When the finest matrix of a hierarchy is a 27-point operator on an
+// n0 x n1 x n2 grid (even edges) and its colouring is the parity colouring,
+// row r of the colour-permuted matrix is the cell (i, j, k) with
+//   c = r / B,  q = r % B,  (i, j, k) = 2 (q / (h1 h2), q / h2 % h1, q % h2)
+//                                       + (c >> 2, (c >> 1) & 1, c & 1),
+// B = n / 8, h = n / 2, and the neighbour at offset (dz, dy, dx) sits at
+//   r' = c' B + ((i' >> 1) h1 + (j' >> 1)) h2 + (k' >> 1),
+//   c' = 4 (i' & 1) + 2 (j' & 1) + (k' & 1).
+// The kernels compute those indices instead of reading column indices
+// (4 bytes per entry less: a third of the FP64 bytes, half of the float
+// bytes, two thirds of the bfloat16 bytes), and consecutive rows of a colour
+// -- consecutive k -- gather consecutive entries of every neighbour colour,
+// so the x reads of a warp are contiguous.  The values are stored per
+// offset (v[e S + r], S the padded plane stride); each row sums its entries in offset order, which is
+// the CSR row order, with the arithmetic of the CSR row operations (SpmvOp,
+// ResidualOp, SorOp), so every result is bit-identical to the CSR path.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "lgx_internal.cuh"
+
+namespace lgx {
+
+// kernel view; delta[c][e] = r' - r for a row of colour c and its in-grid
+// neighbour at offset e (the same for every row of a colour)
+struct G27 {
+  int n0, n1, n2, h1, h2;
+  int64_t n, block, stride;
+  int32_t delta[8][27];
+};
+
+static G27 view(const Grid27 &g) {
+  G27 v{g.n0, g.n1, g.n2, g.n1 / 2, g.n2 / 2, g.n, g.block, g.stride, {}};
+  for (int c = 0; c < 8; ++c) {
+    const int pi = c >> 2, pj = (c >> 1) & 1, pk = c & 1;
+    for (int e = 0; e < 27; ++e) {
+      const int dz = e / 9 - 1, dy = (e / 3) % 3 - 1, dx = e % 3 - 1;
+      const int c2 = ((pi + dz) & 1) * 4 + ((pj + dy) & 1) * 2 + ((pk + dx) & 1);
+      // floor((p + d) / 2) for p + d in [-1, 2]
+      const int fz = (pi + dz + 2) / 2 - 1, fy = (pj + dy + 2) / 2 - 1, fx = (pk + dx + 2) / 2 - 1;
+      v.delta[c][e] = (int32_t)((int64_t)(c2 - c) * g.block +
+                                ((int64_t)fz * v.h1 + fy) * v.h2 + fx);
+    }
+  }
+  return v;
+}
+
+// cell of row r (n < 2^31: 32-bit divisions); returns the colour
+__device__ __forceinline__ int g27_cell(const G27 &g, int64_t r, int &i, int &j, int &k) {
+  const unsigned ur = (unsigned)r, blk = (unsigned)g.block;
+  const unsigned c = ur / blk, q = ur - c * blk;
+  const unsigned hh = (unsigned)g.h1 * (unsigned)g.h2;
+  const unsigned a = q / hh, rem = q - a * hh;
+  const unsigned bq = rem / (unsigned)g.h2, d = rem - bq * (unsigned)g.h2;
+  i = 2 * (int)a + (int)(c >> 2);
+  j = 2 * (int)bq + (int)((c >> 1) & 1);
+  k = 2 * (int)d + (int)(c & 1);
+  return (int)c;
+}
+
+// in-grid tests of a row's neighbours: bit 0/1 lower/upper neighbour exists
+// along axis 0, bits 2/3 axis 1, bits 4/5 axis 2
+__device__ __forceinline__ unsigned g27_sides(const G27 &g, int i, int j, int k) {
+  return (unsigned)(i > 0) | (unsigned)(i + 1 < g.n0) << 1 | (unsigned)(j > 0) << 2 |
+         (unsigned)(j + 1 < g.n1) << 3 | (unsigned)(k > 0) << 4 | (unsigned)(k + 1 < g.n2) << 5;
+}
+
+__device__ __forceinline__ bool g27_in(unsigned sides, int e) {
+  const int dz = e / 9 - 1, dy = (e / 3) % 3 - 1, dx = e % 3 - 1;
+  unsigned need = 0;
+  if (dz < 0) need |= 1u;
+  if (dz > 0) need |= 2u;
+  if (dy < 0) need |= 4u;
+  if (dy > 0) need |= 8u;
+  if (dx < 0) need |= 16u;
+  if (dx > 0) need |= 32u;
+  return (sides & need) == need;
+}
+
+// permuted index of the in-grid cell (i, j, k)
+__device__ __forceinline__ int64_t g27_row(const G27 &g, int i, int j, int k) {
+  const int64_t c = (i & 1) * 4 + (j & 1) * 2 + (k & 1);
+  return c * g.block + ((int64_t)(i >> 1) * g.h1 + (j >> 1)) * g.h2 + (k >> 1);
+}
+
+__device__ __forceinline__ bool g27_has(const G27 &g, int i, int j, int k, int e) {
+  const int i2 = i + e / 9 - 1, j2 = j + (e / 3) % 3 - 1, k2 = k + e % 3 - 1;
+  return (unsigned)i2 < (unsigned)g.n0 && (unsigned)j2 < (unsigned)g.n1 &&
+         (unsigned)k2 < (unsigned)g.n2;
+}
+
+__device__ __forceinline__ int64_t g27_nb(const G27 &g, int i, int j, int k, int e) {
+  return g27_row(g, i + e / 9 - 1, j + (e / 3) % 3 - 1, k + e % 3 - 1);
+}
+
+// ---- build: CSR rows -> per-offset values, checking the structure --------
+// bad |= 1: a row is not the cell the parity order puts there; 2: a row's
+// entries are not exactly its in-grid neighbours in offset order; 4: the
+// delta table disagrees with the coordinates
+template <typename VT>
+__global__ void k_g27_fill(G27 g, const int64_t *__restrict__ rowptr,
+                           const int32_t *__restrict__ col, const VT *__restrict__ val,
+                           const int32_t *__restrict__ perm, VT *__restrict__ out, int *bad) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < g.n;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    int i, j, k;
+    const int c = g27_cell(g, r, i, j, k);
+    if (perm && perm[r] != ((int64_t)i * g.n1 + j) * g.n2 + k) atomicOr(bad, 1);
+    int64_t p = rowptr[r];
+    const int64_t pe = rowptr[r + 1];
+    for (int e = 0; e < 27; ++e) {
+      VT v = static_cast<VT>(0.0f);
+      if (g27_has(g, i, j, k, e)) {
+        // the row kernels reach the neighbour through the colour's delta
+        if (r + g.delta[c][e] != g27_nb(g, i, j, k, e)) atomicOr(bad, 4);
+        if (p < pe && (int64_t)col[p] == g27_nb(g, i, j, k, e)) {
+          v = val[p];
+          ++p;
+        } else {
+          atomicOr(bad, 2);
+        }
+      }
+      out[(int64_t)e * g.stride + r] = v;
+    }
+    if (p != pe) atomicOr(bad, 2);
+  }
+}
+
+// ---- row operations ---------------------------------------------------------
+// MODE 0: y = A x; 1: r = b - A x (bf16: A x scaled by the row factor);
+// 2: SOR row in place (the arithmetic of SorOp, lgx_smoother.cu)
+struct G27Sor {
+  double relax, m1;
+  int ultra, relax_one, from_zero;
+  int64_t visit_end;
+  const double *rdiag;
+};
+
+// Loads through the non-coherent path as volatile asm: the compiler keeps
+// them where they stand -- all loads of a batch ahead of its FMAs -- instead
+// of sinking each into the branch that uses it.  Every address read is valid
+// (values exist for all 27 offsets; a neighbour outside the grid reads the
+// row itself), and no launch writes what it reads this way (a sweep writes
+// one colour and reads the others).
+__device__ __forceinline__ double g27_ld(const double *p) {
+  double v;
+  asm volatile("ld.global.nc.f64 %0, [%1];" : "=d"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ float g27_ld(const float *p) {
+  float v;
+  asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ bf16 g27_ld(const bf16 *p) {
+  unsigned short v;
+  asm volatile("ld.global.nc.u16 %0, [%1];" : "=h"(v) : "l"(p));
+  return __ushort_as_bfloat16(v);
+}
+
+// entries whose loads are issued together before their FMAs: three rounds
+// of 9.  g27_hold makes the loaded values pass through an empty volatile asm
+// after the last load of the round, so no FMA is scheduled between the loads
+// (an FMA waiting on its load would hold back the loads after it).
+template <typename XT>
+__host__ __device__ constexpr int g27_batch() {
+  return 9;
+}
+__device__ __forceinline__ void g27_hold(double (&a)[9], double (&b)[9]) {
+  asm volatile(""
+               : "+d"(a[0]), "+d"(a[1]), "+d"(a[2]), "+d"(a[3]), "+d"(a[4]), "+d"(a[5]),
+                 "+d"(a[6]), "+d"(a[7]), "+d"(a[8]), "+d"(b[0]), "+d"(b[1]), "+d"(b[2]),
+                 "+d"(b[3]), "+d"(b[4]), "+d"(b[5]), "+d"(b[6]), "+d"(b[7]), "+d"(b[8]));
+}
+__device__ __forceinline__ void g27_hold(float (&a)[9], float (&b)[9]) {
+  asm volatile(""
+               : "+f"(a[0]), "+f"(a[1]), "+f"(a[2]), "+f"(a[3]), "+f"(a[4]), "+f"(a[5]),
+                 "+f"(a[6]), "+f"(a[7]), "+f"(a[8]), "+f"(b[0]), "+f"(b[1]), "+f"(b[2]),
+                 "+f"(b[3]), "+f"(b[4]), "+f"(b[5]), "+f"(b[6]), "+f"(b[7]), "+f"(b[8]));
+}
+
+template <typename VT, typename XT, int MODE>
+__global__ void __launch_bounds__(256)
+  k_g27_rows(G27 g, int64_t rb, int64_t re, const VT *__restrict__ v, const XT *__restrict__ b,
+             XT *x, XT *__restrict__ y, const float *__restrict__ scale, G27Sor so) {
+  pdl_trigger();
+  pdl_wait();
+  const int64_t r = rb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= re) return;
+  int i, j, k;
+  const int col = g27_cell(g, r, i, j, k);
+  const unsigned sides = g27_sides(g, i, j, k);
+  const int32_t *dl = g.delta[col];
+  constexpr int B = g27_batch<XT>();
+  // stored value of entry e (0 outside the grid) and x of its neighbour
+  // (0 for unvisited colours in a forward sweep from zero).  The loads do
+  // not branch -- a neighbour outside the grid reads x of the row itself,
+  // which the FMA loops then skip -- so all of a batch are issued together.
+  auto load = [&](int e, XT &xe, XT &ae) {
+    ae = cvt<XT>(g27_ld(v + (int64_t)e * g.stride + r));
+    if (MODE == 2 && e == 13) {
+      xe = XT(0);
+      return;
+    }
+    const int64_t c = g27_in(sides, e) ? r + dl[e] : r;
+    const XT xl = g27_ld(x + c);
+    xe = (MODE == 2 && so.from_zero && c >= so.visit_end) ? XT(0) : xl;
+  };
+  if constexpr (MODE != 2) {
+    XT sum = XT(0);
+#pragma unroll
+    for (int e0 = 0; e0 < 27; e0 += B) {
+      XT xv[B], av[B];
+#pragma unroll
+      for (int u = 0; u < B; ++u) load(e0 + u, xv[u], av[u]);
+      g27_hold(xv, av);
+#pragma unroll
+      for (int u = 0; u < B; ++u)
+        if (g27_in(sides, e0 + u)) sum = fma(av[u], xv[u], sum);
+    }
+    if constexpr (MODE == 0) {
+      y[r] = sum;
+    } else {
+      if constexpr (kIsBf16<VT>) sum = sum * scale[r];
+      y[r] = b[r] - sum;
+    }
+  } else {
+    const XT relax = (XT)so.relax, m1 = (XT)so.m1;
+    const XT xi = so.from_zero ? XT(0) : x[r];
+    if constexpr (kIsBf16<VT>) {
+      const XT si = scale[r];
+      XT t = XT(0), vd = XT(0);
+#pragma unroll
+      for (int e0 = 0; e0 < 27; e0 += B) {
+        XT xv[B], av[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u) load(e0 + u, xv[u], av[u]);
+        g27_hold(xv, av);
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+          const int e = e0 + u;
+          if (!g27_in(sides, e)) continue;
+          if (e == 13) vd = av[u];
+          else t = fma(av[u], xv[u], t);
+        }
+      }
+      const XT diag = si * vd;
+      XT accum = fma(-si, t, b[r]);
+      if (so.ultra) {
+        accum = fma(-diag, xi, accum);
+        x[r] = xi + relax * accum / fabs(diag);
+      } else {
+        x[r] = fma(relax, accum / diag, m1 * xi);
+      }
+    } else {
+      XT accum = b[r], diag = XT(0);
+#pragma unroll
+      for (int e0 = 0; e0 < 27; e0 += B) {
+        XT xv[B], av[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u) load(e0 + u, xv[u], av[u]);
+        g27_hold(xv, av);
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+          const int e = e0 + u;
+          if (!g27_in(sides, e)) continue;
+          if (e == 13) {
+            diag = av[u];
+            if (so.ultra) accum = fma(-av[u], xi, accum);
+          } else {
+            accum = fma(-av[u], xv[u], accum);
+          }
+        }
+      }
+      if (so.ultra) {
+        x[r] = xi + relax * accum / fabs(diag);
+        return;
+      }
+      XT quot;
+      if constexpr (sizeof(XT) == 8) {
+        const double yr = so.rdiag ? so.rdiag[r] : 0.0;
+        quot = (nonzero_bits(yr) && exponent_within_400(accum)) ? div_by_recip(accum, diag, yr)
+                                                                : accum / diag;
+        if (so.relax_one && nonzero_bits(quot) && exponent_field(xi) != 0x7ff) {
+          x[r] = quot;
+          return;
+        }
+      } else {
+        quot = accum / diag;
+      }
+      x[r] = fma(relax, quot, m1 * xi);
+    }
+  }
+}
+
+template <typename VT>
+static const VT *grid_values(const Grid27 &g, const VT *src) {
+  if constexpr (sizeof(VT) == 8) return src == g.src64 ? (const VT *)g.v64.p : nullptr;
+  else if constexpr (kIsBf16<VT>) return src == g.src16 ? (const VT *)g.v16.p : nullptr;
+  else return src == g.src32 ? (const VT *)g.v32.p : nullptr;
+}
+
+template <typename VT, typename XT, int MODE>
+static lgx_status launch_g27(const Grid27 &gr, const VT *v, int64_t rb, int64_t re, const XT *b,
+                             XT *x, XT *y, const float *scale, const G27Sor &so,
+                             cudaStream_t s) {
+  if (re <= rb) return LGX_OK;
+  const int64_t rows = re - rb;
+  const bool pdl = sizeof(XT) == 4 || rows <= pdl_fp64_rows();
+  LGX_CUDA(launch_pdl(pdl, k_g27_rows<VT, XT, MODE>, dim3((unsigned)((rows + 255) / 256)),
+                      dim3(256), 0, s, view(gr), rb, re, v, b, x, y, scale, so));
+  count_launch();
+  return LGX_OK;
+}
+
+template <typename VT, typename XT>
+lgx_status grid_spmv(const Csr &a, const VT *val, const XT *x, XT *y, cudaStream_t s,
+                     bool *done) {
+  *done = false;
+  if (!a.grid) return LGX_OK;
+  const VT *v = grid_values(*a.grid, val);
+  if (!v) return LGX_OK;
+  LGX_CHECK((launch_g27<VT, XT, 0>(*a.grid, v, 0, a.n, nullptr, const_cast<XT *>(x), y, nullptr,
+                                   G27Sor{}, s)));
+  *done = true;
+  return LGX_OK;
+}
+
+template <typename VT, typename XT>
+lgx_status grid_residual(const Csr &a, const VT *val, const XT *b, const XT *x, XT *r,
+                         const float *scale, cudaStream_t s, bool *done) {
+  *done = false;
+  if (!a.grid) return LGX_OK;
+  const VT *v = grid_values(*a.grid, val);
+  if (!v) return LGX_OK;
+  LGX_CHECK((launch_g27<VT, XT, 1>(*a.grid, v, 0, a.n, b, const_cast<XT *>(x), r, scale,
+                                   G27Sor{}, s)));
+  *done = true;
+  return LGX_OK;
+}
+
+template <typename VT, typename XT>
+lgx_status grid_sor_rows(const Csr &a, const VT *val, int64_t rb, int64_t re, const XT *b, XT *x,
+                         double relax, int ultra, const double *rdiag, int relax_one,
+                         int from_zero, int64_t visit_end, const float *scale, cudaStream_t s,
+                         bool *done) {
+  *done = false;
+  if (!a.grid) return LGX_OK;
+  const VT *v = grid_values(*a.grid, val);
+  if (!v) return LGX_OK;
+  G27Sor so{relax, 1.0 - relax, ultra, relax_one, from_zero, visit_end, rdiag};
+  // the float SOR of SorOp forms XT(1) - XT(relax): the same in XT
+  so.m1 = (double)((XT)1 - (XT)relax);
+  LGX_CHECK((launch_g27<VT, XT, 2>(*a.grid, v, rb, re, b, x, nullptr, scale, so, s)));
+  *done = true;
+  return LGX_OK;
+}
+
+template lgx_status grid_spmv<double, double>(const Csr &, const double *, const double *,
+                                              double *, cudaStream_t, bool *);
+template lgx_status grid_spmv<float, double>(const Csr &, const float *, const double *, double *,
+                                             cudaStream_t, bool *);
+template lgx_status grid_spmv<float, float>(const Csr &, const float *, const float *, float *,
+                                            cudaStream_t, bool *);
+template lgx_status grid_residual<double, double>(const Csr &, const double *, const double *,
+                                                  const double *, double *, const float *,
+                                                  cudaStream_t, bool *);
+template lgx_status grid_residual<float, double>(const Csr &, const float *, const double *,
+                                                 const double *, double *, const float *,
+                                                 cudaStream_t, bool *);
+template lgx_status grid_residual<float, float>(const Csr &, const float *, const float *,
+                                                const float *, float *, const float *,
+                                                cudaStream_t, bool *);
+template lgx_status grid_residual<bf16, float>(const Csr &, const bf16 *, const float *,
+                                               const float *, float *, const float *,
+                                               cudaStream_t, bool *);
+template lgx_status grid_sor_rows<double, double>(const Csr &, const double *, int64_t, int64_t,
+                                                  const double *, double *, double, int,
+                                                  const double *, int, int, int64_t,
+                                                  const float *, cudaStream_t, bool *);
+template lgx_status grid_sor_rows<float, double>(const Csr &, const float *, int64_t, int64_t,
+                                                 const double *, double *, double, int,
+                                                 const double *, int, int, int64_t,
+                                                 const float *, cudaStream_t, bool *);
+template lgx_status grid_sor_rows<float, float>(const Csr &, const float *, int64_t, int64_t,
+                                                const float *, float *, double, int,
+                                                const double *, int, int, int64_t, const float *,
+                                                cudaStream_t, bool *);
+template lgx_status grid_sor_rows<bf16, float>(const Csr &, const bf16 *, int64_t, int64_t,
+                                               const float *, float *, double, int,
+                                               const double *, int, int, int64_t, const float *,
+                                               cudaStream_t, bool *);
+
+// ---- attach -------------------------------------------------------------------
+template <typename VT>
+static lgx_status fill_one(const G27 &g, const Csr &p, const VT *src, const int32_t *perm,
+                           DBuf<VT> &out, int *bad, cudaStream_t s) {
+  LGX_CHECK(out.alloc(27 * g.stride));
+  const unsigned grid = (unsigned)std::min<int64_t>(grid_for(g.n, 256), 16384);
+  k_g27_fill<VT><<<grid, 256, 0, s>>>(g, p.rowptr.p, p.col.p, src, perm, out.p, bad);
+  LGX_LAUNCH_CHECK();
+  count_launch();
+  return LGX_OK;
+}
+
+lgx_status grid27_attach(lgx_colouring &c, const int64_t dims[3], cudaStream_t s,
+                         bool *attached) {
+  *attached = false;
+  const int64_t n = dims[0] * dims[1] * dims[2];
+  if (dims[0] < 2 || dims[1] < 2 || dims[2] < 2 || dims[0] % 2 || dims[1] % 2 || dims[2] % 2 ||
+      dims[0] > (1 << 30) || dims[1] > (1 << 30) || dims[2] > (1 << 30) ||
+      n + 64 > (int64_t)INT32_MAX)  // 32-bit row arithmetic in the kernels
+    return LGX_OK;
+  if (c.n != n || c.ncolours != 8 || c.pcsr.n != n) return LGX_OK;
+  for (int q = 0; q <= 8; ++q)
+    if (c.offsets[q] != q * (n / 8)) return LGX_OK;
+  auto gr = std::make_shared<Grid27>();
+  gr->n0 = (int)dims[0];
+  gr->n1 = (int)dims[1];
+  gr->n2 = (int)dims[2];
+  gr->n = n;
+  gr->block = n / 8;
+  gr->stride = ((n + 31) / 32) * 32;
+  if ((gr->stride / 32) % 2 == 0) gr->stride += 32;
+  const G27 g = view(*gr);
+  DBuf<int> bad;
+  LGX_CHECK(bad.alloc(1));
+  LGX_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), s));
+  const Csr &p = c.pcsr;
+  if (p.storage == LGX_F64) {
+    LGX_CHECK(fill_one<double>(g, p, p.v64.p, c.perm.p, gr->v64, bad.p, s));
+    gr->src64 = p.v64.p;
+  } else {
+    LGX_CHECK(fill_one<float>(g, p, p.v32.p, c.perm.p, gr->v32, bad.p, s));
+    gr->src32 = p.v32.p;
+  }
+  if (c.pv32.p) {
+    LGX_CHECK(fill_one<float>(g, p, c.pv32.p, nullptr, gr->v32, bad.p, s));
+    gr->src32 = c.pv32.p;
+  }
+  if (c.pv16.p) {
+    LGX_CHECK(fill_one<bf16>(g, p, c.pv16.p, nullptr, gr->v16, bad.p, s));
+    gr->src16 = c.pv16.p;
+  }
+  int h_bad = 0;
+  LGX_CUDA(cudaMemcpyAsync(&h_bad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  LGX_CUDA(cudaStreamSynchronize(s));
+  if (h_bad) return LGX_OK;  // not this structure: the CSR path stays
+  c.pcsr.grid = gr;
+  *attached = true;
+  return LGX_OK;
+}
+
+}  // namespace lgx

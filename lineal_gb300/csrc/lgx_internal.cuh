@@ -6,6 +6,7 @@
 
 #include <cstdint>
 #include <cstdio>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -100,6 +101,8 @@ constexpr int kCsrPad = 16;
 constexpr uint32_t kIsolated = 0xFFFFFFFEu;
 
 // ---- matrices -------------------------------------------------------------
+struct Grid27;
+
 struct Csr {
   int64_t n = 0, nnz = 0;
   int64_t max_row = 0;
@@ -114,6 +117,27 @@ struct Csr {
   DBuf<int32_t> col;
   DBuf<double> v64;
   DBuf<float> v32;
+  // rows of a 27-point grid matrix in parity-colour order, stored without
+  // column indices (products and sweeps use it when set; see lgx_grid.cu)
+  std::shared_ptr<const Grid27> grid;
+};
+
+// Colour-permuted 27-point grid matrix (even edge lengths, parity colouring
+// c = 4 (i & 1) + 2 (j & 1) + (k & 1), colour c in rows [c B, (c + 1) B) with
+// B = n / 8, natural order inside a colour).  Row values are stored per
+// stencil offset e = 9 (dz + 1) + 3 (dy + 1) + (dx + 1) -- the CSR row order
+// -- offset-major (v[e S + r], S = n padded to an odd multiple of 32
+// entries so that the 27 planes of one row do not sit a power of two apart),
+// 0 where the neighbour lies outside the grid.
+// Each array mirrors the CSR value array it was built from (src*): products
+// and sweeps switch to the grid only when given that array.
+struct Grid27 {
+  int n0 = 0, n1 = 0, n2 = 0;
+  int64_t n = 0, block = 0, stride = 0;
+  DBuf<double> v64;
+  DBuf<float> v32;
+  DBuf<bf16> v16;
+  const void *src64 = nullptr, *src32 = nullptr, *src16 = nullptr;
 };
 
 // Csr::tuned index of a value type
@@ -146,6 +170,7 @@ struct lgx_matrix {
   lgx::DBuf<uint8_t> mat;       // stencil lookup materials (owned copy)
   lgx::DBuf<double> k;          // stencil value conductivities (owned copy)
   lgx::DBuf<double> diag;       // cached diagonal (lazily computed)
+  int64_t grid27[3] = {0, 0, 0};  // CSR kinds: 27-point operator on this grid (0: unknown)
 };
 
 // Colour-permuted copy of a CSR matrix used by the multicolour smoothers.
@@ -197,6 +222,20 @@ lgx_status csr_residual(const Csr &a, const VT *val, const XT *b, const XT *x, X
                         double *norm, double *partials, unsigned *counter, cudaStream_t s,
                         const float *scale = nullptr);
 
+// 27-point grid rows without column indices (lgx_grid.cu): each runs when
+// `a` carries a grid mirroring `val` (*done), else leaves the work to the
+// CSR kernels
+template <typename VT, typename XT>
+lgx_status grid_spmv(const Csr &a, const VT *val, const XT *x, XT *y, cudaStream_t s, bool *done);
+template <typename VT, typename XT>
+lgx_status grid_residual(const Csr &a, const VT *val, const XT *b, const XT *x, XT *r,
+                         const float *scale, cudaStream_t s, bool *done);
+template <typename VT, typename XT>
+lgx_status grid_sor_rows(const Csr &a, const VT *val, int64_t rb, int64_t re, const XT *b, XT *x,
+                         double relax, int ultra, const double *rdiag, int relax_one,
+                         int from_zero, int64_t visit_end, const float *scale, cudaStream_t s,
+                         bool *done);
+
 lgx_status stencil_spmv(const StencilDesc &st, const double *x, double *y, cudaStream_t s);
 lgx_status stencil_residual(const StencilDesc &st, const double *b, const double *x, double *r,
                             double *norm, double *partials, unsigned *counter, cudaStream_t s);
@@ -225,6 +264,10 @@ lgx_status mc_sor_sweep(const lgx_colouring &c, const VT *val, double relax, int
                         int ultra, const XT *b, XT *x, cudaStream_t s, int from_zero = 0,
                         const float *scale = nullptr);
 lgx_status colouring_make_bf16(lgx_colouring &c, cudaStream_t s);
+// gives c.pcsr a Grid27 when it is the parity-coloured 27-point operator on
+// `dims` (checked on the device; *attached tells whether it was)
+lgx_status grid27_attach(lgx_colouring &c, const int64_t dims[3], cudaStream_t s,
+                         bool *attached);
 
 lgx_status jacobi_csr(const Csr &a, double relax, const double *x_in, double *x_out,
                       const double *b, cudaStream_t s);

@@ -545,6 +545,10 @@ lgx_status mc_sor_sweep(const lgx_colouring &c, const VT *val, double relax, int
       continue;
     }
     op.visit_end = rb;  // forward: exactly the rows before this colour are visited
+    bool done = false;
+    LGX_CHECK((grid_sor_rows<VT, XT>(p, val, rb, re, b, x, relax, ultra, op.rdiag, op.relax_one,
+                                     op.from_zero, op.visit_end, scale, s, &done)));
+    if (done) continue;
     LGX_CHECK(launch_rows<VT>(rb, re, p, val, op, s));
   }
   return LGX_OK;

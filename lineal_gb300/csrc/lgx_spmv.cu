@@ -64,6 +64,9 @@ struct ResidualOp {
 template <typename VT, typename XT>
 lgx_status csr_spmv(const Csr &a, const VT *val, const XT *x, XT *y, cudaStream_t s) {
   if (a.n == 0) return LGX_OK;
+  bool done = false;
+  LGX_CHECK((grid_spmv<VT, XT>(a, val, x, y, s, &done)));
+  if (done) return LGX_OK;
   return launch_rows<VT>(0, a.n, a, val, SpmvOp<VT, XT>{x, y}, s);
 }
 
@@ -78,6 +81,9 @@ lgx_status csr_residual(const Csr &a, const VT *val, const XT *b, const XT *x, X
   if (norm)
     return launch_rows<VT>(0, a.n, a, val,
                            ResidualOp<VT, XT, true>{b, x, r, norm, partials, counter, scale}, s);
+  bool done = false;
+  LGX_CHECK((grid_residual<VT, XT>(a, val, b, x, r, scale, s, &done)));
+  if (done) return LGX_OK;
   return launch_rows<VT>(0, a.n, a, val,
                          ResidualOp<VT, XT, false>{b, x, r, nullptr, nullptr, nullptr, scale},
                          s);

@@ -1,0 +1,97 @@
+"""The finest level of a parity-coloured 27-point grid matrix runs kernels
+that compute column indices from the grid: V-cycles and AMG-PCG solves must
+equal the CSR kernels' bit for bit, in every precision form, and the grid
+path must stay off wherever the structure does not hold."""
+
+import numpy as np
+import pytest
+
+import oracle as lo
+
+pytestmark = pytest.mark.gpu
+
+PARAMS = dict(min_coarsen_size=64, partition_size=512, max_partitions=1 << 30)
+FORMS = {"fp64": {}, "f32": dict(cycle_f32=True), "bf16": dict(cycle_f32=True, cycle_bf16=True),
+         "f32_coarse": dict(coarse_f32=True, cycle_f32=True)}
+
+
+def _parity(dims):
+    i, j, k = np.meshgrid(*[np.arange(d) for d in dims], indexing="ij")
+    return ((i % 2) * 4 + (j % 2) * 2 + (k % 2)).ravel().astype(np.int32)
+
+
+def _k(dims, seed=3):
+    return np.exp(1.5 * np.random.default_rng(seed).standard_normal(int(np.prod(dims))))
+
+
+def _pair(cuda, m, dims, **kw):
+    col = cuda.Colouring.from_array(m, _parity(dims), 8)
+    hg = cuda.HierarchyWright(grid27=True, **PARAMS, **kw).instantiate(m, finest_colouring=col)
+    hc = cuda.HierarchyWright(grid27=False, **PARAMS, **kw).instantiate(m, finest_colouring=col)
+    return hg, hc
+
+
+@pytest.mark.parametrize("form", list(FORMS))
+@pytest.mark.parametrize("dims", [(8, 10, 12), (16, 16, 16), (2, 4, 6)])
+def test_grid_vcycle_equals_csr(cuda, form, dims):
+    m = cuda.gen_27pt(dims, _k(dims))
+    hg, hc = _pair(cuda, m, dims, **FORMS[form])
+    assert hg.grid27_active() and not hc.grid27_active()
+    b = np.random.default_rng(5).uniform(-1, 1, m.row_num())
+    np.testing.assert_array_equal(hg.vcycle(b).cpu().numpy(), hc.vcycle(b).cpu().numpy())
+
+
+@pytest.mark.parametrize("form", ["fp64", "f32", "bf16"])
+def test_grid_pcg_equals_csr(cuda, form):
+    dims = (20, 18, 22)
+    m = cuda.gen_27pt(dims, _k(dims, 7))
+    hg, hc = _pair(cuda, m, dims, **FORMS[form])
+    b = np.random.default_rng(6).uniform(-1, 1, m.row_num())
+    flexible = form != "fp64"
+    rg = cuda.pcg(m, b, precon=cuda.PRECON_AMG, amg=hg, rtol=1e-8, maxit=300, flexible=flexible)
+    rc = cuda.pcg(m, b, precon=cuda.PRECON_AMG, amg=hc, rtol=1e-8, maxit=300, flexible=flexible)
+    assert rg.iterations == rc.iterations
+    np.testing.assert_array_equal(rg.x.cpu().numpy(), rc.x.cpu().numpy())
+    if form == "fp64":
+        ref = lo.gen_27pt(dims, _k(dims, 7))
+        x = rg.x.cpu().numpy()
+        assert np.linalg.norm(b - lo.spmv(ref, x)) <= 1.01e-8 * np.linalg.norm(b)
+
+
+def test_grid_declared_on_host_matrix(cuda):
+    dims = (6, 8, 10)
+    ref = lo.gen_27pt(dims, _k(dims))
+    m = cuda.CsrMatrix.from_host(ref.rowptr, ref.col, ref.val, symmetric=True)
+    col = cuda.Colouring.from_array(m, _parity(dims), 8)
+    h0 = cuda.HierarchyWright(**PARAMS).instantiate(m, finest_colouring=col)
+    assert not h0.grid27_active()  # nothing declared
+    m.set_grid27(dims)
+    h1 = cuda.HierarchyWright(**PARAMS).instantiate(m, finest_colouring=col)
+    assert h1.grid27_active()
+    b = np.random.default_rng(2).uniform(-1, 1, ref.n)
+    np.testing.assert_array_equal(h1.vcycle(b).cpu().numpy(), h0.vcycle(b).cpu().numpy())
+    with pytest.raises(cuda.LinealError):
+        m.set_grid27((6, 8, 11))
+
+
+def test_grid_stays_off_without_the_structure(cuda):
+    # a 7-point matrix declared as a 27-point grid fails the device check
+    dims = (6, 8, 10)
+    ref = lo.gen_7pt(dims, _k(dims))
+    m = cuda.CsrMatrix.from_host(ref.rowptr, ref.col, ref.val, symmetric=True)
+    m.set_grid27(dims)
+    col = cuda.Colouring.from_array(m, _parity(dims), 8)
+    h = cuda.HierarchyWright(**PARAMS).instantiate(m, finest_colouring=col)
+    assert not h.grid27_active()
+    b = np.random.default_rng(4).uniform(-1, 1, ref.n)
+    # the CSR path runs instead, the same as without the declaration
+    m2 = cuda.CsrMatrix.from_host(ref.rowptr, ref.col, ref.val, symmetric=True)
+    h2 = cuda.HierarchyWright(**PARAMS).instantiate(
+        m2, finest_colouring=cuda.Colouring.from_array(m2, _parity(dims), 8))
+    np.testing.assert_array_equal(h.vcycle(b).cpu().numpy(), h2.vcycle(b).cpu().numpy())
+    # odd edges and a Jones-Plassmann finest colouring keep the CSR path too
+    for d, colouring in (((7, 8, 10), "parity"), ((6, 8, 10), "jp")):
+        g27 = cuda.gen_27pt(d, _k(d))
+        c = (cuda.Colouring.from_array(g27, _parity(d), 8) if colouring == "parity" else None)
+        hh = cuda.HierarchyWright(**PARAMS).instantiate(g27, finest_colouring=c)
+        assert not hh.grid27_active()
