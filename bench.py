@@ -749,7 +749,8 @@ def run_profile(args):
     h = g.HierarchyWright(min_coarsen_size=2000, cycle_f32=mixed, cycle_bf16=args.bf16,
                           partition_size=args.partition_size,
                           partition_growth=args.partition_growth,
-                          min_partitions=args.min_partitions).instantiate(a, finest_colouring=col)
+                          min_partitions=args.min_partitions,
+                          grid27=args.grid27).instantiate(a, finest_colouring=col)
     if args.autotune:
         h.autotune(reps=3)
     b = torch.as_tensor(b_host, device="cuda")
