@@ -140,12 +140,12 @@ struct G27Sor {
   const double *rdiag;
 };
 
-// Loads through the non-coherent path as volatile asm: the compiler keeps
-// them where they stand -- all loads of a batch ahead of its FMAs -- instead
-// of sinking each into the branch that uses it.  Every address read is valid
-// (values exist for all 27 offsets; a neighbour outside the grid reads the
-// row itself), and no launch writes what it reads this way (a sweep writes
-// one colour and reads the others).
+// Loads through the non-coherent path as volatile asm, which the compiler
+// does not sink into the branches that use them: every load of a round is
+// issued unconditionally.  Every address read is valid (values exist for all
+// 27 offsets; a neighbour outside the grid reads the row itself), and no
+// launch writes what it reads this way (a sweep writes one colour and reads
+// the others).
 __device__ __forceinline__ double g27_ld(const double *p) {
   double v;
   asm volatile("ld.global.nc.f64 %0, [%1];" : "=d"(v) : "l"(p));
@@ -162,26 +162,13 @@ __device__ __forceinline__ bf16 g27_ld(const bf16 *p) {
   return __ushort_as_bfloat16(v);
 }
 
-// entries whose loads are issued together before their FMAs: three rounds
-// of 9.  g27_hold makes the loaded values pass through an empty volatile asm
-// after the last load of the round, so no FMA is scheduled between the loads
-// (an FMA waiting on its load would hold back the loads after it).
-template <typename XT>
-__host__ __device__ constexpr int g27_batch() {
-  return 9;
-}
-__device__ __forceinline__ void g27_hold(double (&a)[9], double (&b)[9]) {
-  asm volatile(""
-               : "+d"(a[0]), "+d"(a[1]), "+d"(a[2]), "+d"(a[3]), "+d"(a[4]), "+d"(a[5]),
-                 "+d"(a[6]), "+d"(a[7]), "+d"(a[8]), "+d"(b[0]), "+d"(b[1]), "+d"(b[2]),
-                 "+d"(b[3]), "+d"(b[4]), "+d"(b[5]), "+d"(b[6]), "+d"(b[7]), "+d"(b[8]));
-}
-__device__ __forceinline__ void g27_hold(float (&a)[9], float (&b)[9]) {
-  asm volatile(""
-               : "+f"(a[0]), "+f"(a[1]), "+f"(a[2]), "+f"(a[3]), "+f"(a[4]), "+f"(a[5]),
-                 "+f"(a[6]), "+f"(a[7]), "+f"(a[8]), "+f"(b[0]), "+f"(b[1]), "+f"(b[2]),
-                 "+f"(b[3]), "+f"(b[4]), "+f"(b[5]), "+f"(b[6]), "+f"(b[7]), "+f"(b[8]));
-}
+// entries whose loads are issued together before their FMAs: nine rounds of
+// three.  Measured at 256^3 (AMG-PCG, FP64 / float cycle): rounds of 27
+// (float) 346 ms mixed; of 9: FP64 456, mixed 296 ms; of 3: FP64 432, mixed
+// 274 ms; single loads: FP64 452, mixed 297 ms -- short rounds keep the
+// registers low and more warps resident, which hides the gathers better
+// than deeper rounds in fewer warps.
+constexpr int kG27Batch = 3;
 
 template <typename VT, typename XT, int MODE>
 __global__ void __launch_bounds__(256)
@@ -195,7 +182,7 @@ __global__ void __launch_bounds__(256)
   const int col = g27_cell(g, r, i, j, k);
   const unsigned sides = g27_sides(g, i, j, k);
   const int32_t *dl = g.delta[col];
-  constexpr int B = g27_batch<XT>();
+  constexpr int B = kG27Batch;
   // stored value of entry e (0 outside the grid) and x of its neighbour
   // (0 for unvisited colours in a forward sweep from zero).  The loads do
   // not branch -- a neighbour outside the grid reads x of the row itself,
@@ -217,7 +204,6 @@ __global__ void __launch_bounds__(256)
       XT xv[B], av[B];
 #pragma unroll
       for (int u = 0; u < B; ++u) load(e0 + u, xv[u], av[u]);
-      g27_hold(xv, av);
 #pragma unroll
       for (int u = 0; u < B; ++u)
         if (g27_in(sides, e0 + u)) sum = fma(av[u], xv[u], sum);
@@ -239,7 +225,6 @@ __global__ void __launch_bounds__(256)
         XT xv[B], av[B];
 #pragma unroll
         for (int u = 0; u < B; ++u) load(e0 + u, xv[u], av[u]);
-        g27_hold(xv, av);
 #pragma unroll
         for (int u = 0; u < B; ++u) {
           const int e = e0 + u;
@@ -263,7 +248,6 @@ __global__ void __launch_bounds__(256)
         XT xv[B], av[B];
 #pragma unroll
         for (int u = 0; u < B; ++u) load(e0 + u, xv[u], av[u]);
-        g27_hold(xv, av);
 #pragma unroll
         for (int u = 0; u < B; ++u) {
           const int e = e0 + u;
