@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <cstdlib>
 
 #include "lgx_internal.cuh"
 
@@ -170,6 +171,87 @@ __device__ __forceinline__ bf16 g27_ld(const bf16 *p) {
 // than deeper rounds in fewer warps.
 constexpr int kG27Batch = 3;
 
+// One row's state through its 27 entries, in the arithmetic of SpmvOp
+// (MODE 0), ResidualOp (MODE 1) and SorOp (MODE 2, lgx_smoother.cu).
+template <typename VT, typename XT, int MODE>
+struct G27Row {
+  XT acc = XT(0), diag = XT(0), xi = XT(0);  // sum | SOR accum (bf16: t), diagonal (bf16: v_ii)
+  __device__ __forceinline__ void init(int64_t r, const XT *b, const XT *x, const G27Sor &so) {
+    if constexpr (MODE == 2) {
+      xi = so.from_zero ? XT(0) : x[r];
+      if constexpr (!kIsBf16<VT>) acc = b[r];
+    }
+  }
+  // entry e with value a and neighbour value xv (in: inside the grid)
+  __device__ __forceinline__ void step(int e, bool in, XT a, XT xv, const G27Sor &so) {
+    if (!in) return;
+    if constexpr (MODE != 2) {
+      acc = fma(a, xv, acc);
+    } else if constexpr (kIsBf16<VT>) {
+      if (e == 13) diag = a;
+      else acc = fma(a, xv, acc);
+    } else {
+      if (e == 13) {
+        diag = a;
+        if (so.ultra) acc = fma(-a, xi, acc);
+      } else {
+        acc = fma(-a, xv, acc);
+      }
+    }
+  }
+  __device__ __forceinline__ void finish(int64_t r, const XT *b, XT *x, XT *y, const float *scale,
+                                         const G27Sor &so) {
+    if constexpr (MODE == 0) {
+      y[r] = acc;
+    } else if constexpr (MODE == 1) {
+      XT sum = acc;
+      if constexpr (kIsBf16<VT>) sum = sum * scale[r];
+      y[r] = b[r] - sum;
+    } else {
+      const XT relax = (XT)so.relax, m1 = (XT)so.m1;
+      if constexpr (kIsBf16<VT>) {
+        const XT si = scale[r];
+        const XT dg = si * diag;
+        XT accum = fma(-si, acc, b[r]);
+        if (so.ultra) {
+          accum = fma(-dg, xi, accum);
+          x[r] = xi + relax * accum / fabs(dg);
+        } else {
+          x[r] = fma(relax, accum / dg, m1 * xi);
+        }
+      } else {
+        if (so.ultra) {
+          x[r] = xi + relax * acc / fabs(diag);
+          return;
+        }
+        XT quot;
+        if constexpr (sizeof(XT) == 8) {
+          const double yr = so.rdiag ? so.rdiag[r] : 0.0;
+          quot = (nonzero_bits(yr) && exponent_within_400(acc)) ? div_by_recip(acc, diag, yr)
+                                                                : acc / diag;
+          if (so.relax_one && nonzero_bits(quot) && exponent_field(xi) != 0x7ff) {
+            x[r] = quot;
+            return;
+          }
+        } else {
+          quot = acc / diag;
+        }
+        x[r] = fma(relax, quot, m1 * xi);
+      }
+    }
+  }
+};
+
+// x of neighbour c for entry e of a row (0 for unvisited colours in a
+// forward sweep from zero; the diagonal's x is not read here)
+template <typename XT, int MODE>
+__device__ __forceinline__ XT g27_x(const XT *x, int64_t c, int e, const G27Sor &so) {
+  if (MODE == 2 && e == 13) return XT(0);
+  const XT xl = g27_ld(x + c);
+  return (MODE == 2 && so.from_zero && c >= so.visit_end) ? XT(0) : xl;
+}
+
+// one row per thread
 template <typename VT, typename XT, int MODE>
 __global__ void __launch_bounds__(256)
   k_g27_rows(G27 g, int64_t rb, int64_t re, const VT *__restrict__ v, const XT *__restrict__ b,
@@ -183,102 +265,95 @@ __global__ void __launch_bounds__(256)
   const unsigned sides = g27_sides(g, i, j, k);
   const int32_t *dl = g.delta[col];
   constexpr int B = kG27Batch;
-  // stored value of entry e (0 outside the grid) and x of its neighbour
-  // (0 for unvisited colours in a forward sweep from zero).  The loads do
-  // not branch -- a neighbour outside the grid reads x of the row itself,
-  // which the FMA loops then skip -- so all of a batch are issued together.
-  auto load = [&](int e, XT &xe, XT &ae) {
-    ae = cvt<XT>(g27_ld(v + (int64_t)e * g.stride + r));
-    if (MODE == 2 && e == 13) {
-      xe = XT(0);
-      return;
+  G27Row<VT, XT, MODE> row;
+  row.init(r, b, x, so);
+  // the loads of a round do not branch -- a neighbour outside the grid reads
+  // x of the row itself, which step() then skips -- so they go out together
+#pragma unroll
+  for (int e0 = 0; e0 < 27; e0 += B) {
+    XT xv[B], av[B];
+#pragma unroll
+    for (int u = 0; u < B; ++u) {
+      const int e = e0 + u;
+      av[u] = cvt<XT>(g27_ld(v + (int64_t)e * g.stride + r));
+      xv[u] = g27_x<XT, MODE>(x, g27_in(sides, e) ? r + dl[e] : r, e, so);
     }
-    const int64_t c = g27_in(sides, e) ? r + dl[e] : r;
-    const XT xl = g27_ld(x + c);
-    xe = (MODE == 2 && so.from_zero && c >= so.visit_end) ? XT(0) : xl;
-  };
-  if constexpr (MODE != 2) {
-    XT sum = XT(0);
 #pragma unroll
-    for (int e0 = 0; e0 < 27; e0 += B) {
-      XT xv[B], av[B];
-#pragma unroll
-      for (int u = 0; u < B; ++u) load(e0 + u, xv[u], av[u]);
-#pragma unroll
-      for (int u = 0; u < B; ++u)
-        if (g27_in(sides, e0 + u)) sum = fma(av[u], xv[u], sum);
-    }
-    if constexpr (MODE == 0) {
-      y[r] = sum;
-    } else {
-      if constexpr (kIsBf16<VT>) sum = sum * scale[r];
-      y[r] = b[r] - sum;
-    }
-  } else {
-    const XT relax = (XT)so.relax, m1 = (XT)so.m1;
-    const XT xi = so.from_zero ? XT(0) : x[r];
-    if constexpr (kIsBf16<VT>) {
-      const XT si = scale[r];
-      XT t = XT(0), vd = XT(0);
-#pragma unroll
-      for (int e0 = 0; e0 < 27; e0 += B) {
-        XT xv[B], av[B];
-#pragma unroll
-        for (int u = 0; u < B; ++u) load(e0 + u, xv[u], av[u]);
-#pragma unroll
-        for (int u = 0; u < B; ++u) {
-          const int e = e0 + u;
-          if (!g27_in(sides, e)) continue;
-          if (e == 13) vd = av[u];
-          else t = fma(av[u], xv[u], t);
-        }
-      }
-      const XT diag = si * vd;
-      XT accum = fma(-si, t, b[r]);
-      if (so.ultra) {
-        accum = fma(-diag, xi, accum);
-        x[r] = xi + relax * accum / fabs(diag);
-      } else {
-        x[r] = fma(relax, accum / diag, m1 * xi);
-      }
-    } else {
-      XT accum = b[r], diag = XT(0);
-#pragma unroll
-      for (int e0 = 0; e0 < 27; e0 += B) {
-        XT xv[B], av[B];
-#pragma unroll
-        for (int u = 0; u < B; ++u) load(e0 + u, xv[u], av[u]);
-#pragma unroll
-        for (int u = 0; u < B; ++u) {
-          const int e = e0 + u;
-          if (!g27_in(sides, e)) continue;
-          if (e == 13) {
-            diag = av[u];
-            if (so.ultra) accum = fma(-av[u], xi, accum);
-          } else {
-            accum = fma(-av[u], xv[u], accum);
-          }
-        }
-      }
-      if (so.ultra) {
-        x[r] = xi + relax * accum / fabs(diag);
-        return;
-      }
-      XT quot;
-      if constexpr (sizeof(XT) == 8) {
-        const double yr = so.rdiag ? so.rdiag[r] : 0.0;
-        quot = (nonzero_bits(yr) && exponent_within_400(accum)) ? div_by_recip(accum, diag, yr)
-                                                                : accum / diag;
-        if (so.relax_one && nonzero_bits(quot) && exponent_field(xi) != 0x7ff) {
-          x[r] = quot;
-          return;
-        }
-      } else {
-        quot = accum / diag;
-      }
-      x[r] = fma(relax, quot, m1 * xi);
-    }
+    for (int u = 0; u < B; ++u) row.step(e0 + u, g27_in(sides, e0 + u), av[u], xv[u], so);
   }
+  row.finish(r, b, x, y, scale, so);
+}
+
+// four consecutive rows of a colour per thread (float vectors): the value
+// planes load as one 16-byte (float) or 8-byte (bfloat16) vector per entry.
+// The host uses it when rows come in aligned fours inside one line of the
+// grid (h2 and the colour block size multiples of 4), so the four cells
+// differ only in k (by 2 each).
+template <typename VT, int R>
+__device__ __forceinline__ void g27_ldv(const VT *p, float (&out)[R]);
+template <>
+__device__ __forceinline__ void g27_ldv<float, 4>(const float *p, float (&out)[4]) {
+  asm volatile("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(out[0]), "=f"(out[1]), "=f"(out[2]), "=f"(out[3])
+               : "l"(p));
+}
+template <>
+__device__ __forceinline__ void g27_ldv<bf16, 4>(const bf16 *p, float (&out)[4]) {
+  unsigned short h[4];
+  asm volatile("ld.global.nc.v4.u16 {%0, %1, %2, %3}, [%4];"
+               : "=h"(h[0]), "=h"(h[1]), "=h"(h[2]), "=h"(h[3])
+               : "l"(p));
+#pragma unroll
+  for (int q = 0; q < 4; ++q) out[q] = __bfloat162float(__ushort_as_bfloat16(h[q]));
+}
+
+template <typename VT, int MODE>
+__global__ void __launch_bounds__(256)
+  k_g27_rows4(G27 g, int64_t rb, int64_t re, const VT *__restrict__ v,
+              const float *__restrict__ b, float *x, float *__restrict__ y,
+              const float *__restrict__ scale, G27Sor so) {
+  constexpr int R = 4;
+  pdl_trigger();
+  pdl_wait();
+  const int64_t r0 = rb + (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) * R;
+  if (r0 >= re) return;
+  int i, j, k;
+  const int col = g27_cell(g, r0, i, j, k);
+  const int32_t *dl = g.delta[col];
+  unsigned sides[R];
+#pragma unroll
+  for (int q = 0; q < R; ++q) sides[q] = g27_sides(g, i, j, k + 2 * q);
+  G27Row<VT, float, MODE> row[R];
+#pragma unroll
+  for (int q = 0; q < R; ++q) row[q].init(r0 + q, b, x, so);
+  constexpr int B = kG27Batch;
+#pragma unroll
+  for (int e0 = 0; e0 < 27; e0 += B) {
+    float av[B][R], xv[B][R];
+#pragma unroll
+    for (int u = 0; u < B; ++u) {
+      const int e = e0 + u;
+      g27_ldv<VT, R>(v + (int64_t)e * g.stride + r0, av[u]);
+#pragma unroll
+      for (int q = 0; q < R; ++q)
+        xv[u][q] = g27_x<float, MODE>(x, g27_in(sides[q], e) ? r0 + q + dl[e] : r0 + q, e, so);
+    }
+#pragma unroll
+    for (int u = 0; u < B; ++u)
+#pragma unroll
+      for (int q = 0; q < R; ++q) row[q].step(e0 + u, g27_in(sides[q], e0 + u), av[u][q], xv[u][q], so);
+  }
+#pragma unroll
+  for (int q = 0; q < R; ++q) row[q].finish(r0 + q, b, x, y, scale, so);
+}
+
+// four-row kernels for bfloat16 values (LGX_G27_ROWS4=0 switches them off)
+static bool g27_rows4_enabled() {
+  static const bool on = [] {
+    const char *e = std::getenv("LGX_G27_ROWS4");
+    return !(e && e[0] == '0');
+  }();
+  return on;
 }
 
 template <typename VT>
@@ -295,6 +370,19 @@ static lgx_status launch_g27(const Grid27 &gr, const VT *v, int64_t rb, int64_t 
   if (re <= rb) return LGX_OK;
   const int64_t rows = re - rb;
   const bool pdl = sizeof(XT) == 4 || rows <= pdl_fp64_rows();
+  if constexpr (kIsBf16<VT>) {
+    // bfloat16 values: four rows per thread (8-byte value loads) when every
+    // thread's four rows are whole, in one colour block and in one grid line.
+    // Measured at 256^3: bf16 cycle 296 -> 273 ms; float values lose with it
+    // (272 -> 281 ms: their rows run one per thread)
+    if (g27_rows4_enabled() && (gr.n2 / 2) % 4 == 0 && gr.block % 4 == 0 && rb % 4 == 0 &&
+        re % 4 == 0) {
+      LGX_CUDA(launch_pdl(pdl, k_g27_rows4<VT, MODE>, dim3((unsigned)((rows / 4 + 255) / 256)),
+                          dim3(256), 0, s, view(gr), rb, re, v, b, x, y, scale, so));
+      count_launch();
+      return LGX_OK;
+    }
+  }
   LGX_CUDA(launch_pdl(pdl, k_g27_rows<VT, XT, MODE>, dim3((unsigned)((rows + 255) / 256)),
                       dim3(256), 0, s, view(gr), rb, re, v, b, x, y, scale, so));
   count_launch();

@@ -41,9 +41,11 @@ def test_grid_vcycle_equals_csr(cuda, form, dims):
     np.testing.assert_array_equal(hg.vcycle(b).cpu().numpy(), hc.vcycle(b).cpu().numpy())
 
 
+# (16, 24, 32): rows in aligned fours along axis 2 (the four-row float
+# kernels); (20, 18, 22): one row per thread
+@pytest.mark.parametrize("dims", [(20, 18, 22), (16, 24, 32)])
 @pytest.mark.parametrize("form", ["fp64", "f32", "bf16"])
-def test_grid_pcg_equals_csr(cuda, form):
-    dims = (20, 18, 22)
+def test_grid_pcg_equals_csr(cuda, form, dims):
     m = cuda.gen_27pt(dims, _k(dims, 7))
     hg, hc = _pair(cuda, m, dims, **FORMS[form])
     b = np.random.default_rng(6).uniform(-1, 1, m.row_num())
