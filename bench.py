@@ -427,6 +427,29 @@ def run_gb300(args):
     log(f"[gb300] SpMV fp64 {t_spmv64:.3f} ms {gbs64:.0f} GB/s; fp32 {t_spmv32:.3f} ms "
         f"{gbs32:.0f} GB/s")
 
+    # ---- the finest-level smoother: one multicolour SOR sweep (8 colour
+    # launches) through the grid kernels, in the colouring's row order;
+    # algorithmic bytes = stored values + b, x read once, x written
+    smoother = None
+    colg = g.Colouring.from_array(a, colours, 8)
+    if colg.use_grid27(dims, with_float=True):
+        bp = g.permute(colg, b)
+        xg = g.permute(colg, xs)
+        xg32, bp32 = xg.float(), bp.float()
+        t_sw64 = time_spmv(colg, xg, bp, lambda c_, x_, b_: g.sor_sweep_permuted(c_, b_, x_))
+        t_sw32 = time_spmv(colg, xg32, bp32,
+                           lambda c_, x_, b_: g.sor_sweep_permuted(c_, b_, x_))
+        sb64, sb32 = nnz * 8 + 24 * n, nnz * 4 + 12 * n
+        smoother = {"kernel": "k_g27_rows<VT, XT, 2> (8 colour launches)",
+                    "fp64_ms": t_sw64, "fp64_gbs": sb64 / (t_sw64 * 1e-3) / 1e9,
+                    "fp64_fma_tflops": 2 * nnz / (t_sw64 * 1e-3) / 1e12,
+                    "fp32_ms": t_sw32, "fp32_gbs": sb32 / (t_sw32 * 1e-3) / 1e9,
+                    "fp32_frac": sb32 / (t_sw32 * 1e-3) / 1e9 / peak,
+                    "bytes_fp64": sb64, "bytes_fp32": sb32}
+        log(f"[gb300] SOR sweep (grid) fp64 {t_sw64:.3f} ms; fp32 {t_sw32:.3f} ms "
+            f"{smoother['fp32_gbs']:.0f} GB/s ({smoother['fp32_frac']:.0%} of peak)")
+        del colg, bp, xg, xg32, bp32
+
     # ---- end to end through the C ABI with host buffers -----------------------
     e2e = None
     if args.e2e:
@@ -509,6 +532,7 @@ def run_gb300(args):
         "spmv": {"fp64_ms": t_spmv64, "fp64_gbs": gbs64, "fp64_frac": gbs64 / peak,
                  "fp32_ms": t_spmv32, "fp32_gbs": gbs32, "fp32_frac": gbs32 / peak,
                  "bytes_fp64": bytes64, "bytes_fp32": bytes32},
+        "smoother": smoother,
         "precision_form": prec,
         "roofline": {"bound": "hbm", "kernel": "k_wrows<double, SpmvOp<double,double>, 4, 1>",
                      "achieved": gbs64, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
@@ -569,6 +593,17 @@ def run_kernels(args):
         ("sor_sweep_permuted_fp32", lambda: g.sor_sweep_permuted(col, bp32, xp32),
          csr_bytes(n, nnz, 4, 4) + 4 * n),
     ]
+    # the same sweeps through the 27-point grid kernels (no column indices):
+    # algorithmic bytes = stored values + b, x read once and x written
+    colg = g.Colouring.from_array(a, parity_colours(dims), 8)
+    if colg.use_grid27(dims, with_float=True):
+        xg, xg32 = xp.clone(), xp32.clone()
+        kernels += [
+            ("sor_sweep_grid_fp64", lambda: g.sor_sweep_permuted(colg, bp, xg),
+             nnz * 8 + 3 * 8 * n),
+            ("sor_sweep_grid_fp32", lambda: g.sor_sweep_permuted(colg, bp32, xg32),
+             nnz * 4 + 3 * 4 * n),
+        ]
     if args.vcycle:
         hier = {}
         for tag, f32 in (("fp64", False), ("mixed", True)):

@@ -251,6 +251,15 @@ lgx_status lgx_colouring_create_jp(const lgx_matrix *a, uint64_t seed, lgx_strea
  * the parity colouring of a structured grid).  Validated on the device. */
 lgx_status lgx_colouring_create(const lgx_matrix *a, const int32_t *d_colour, int32_t ncolours,
                                 lgx_stream stream, lgx_colouring **out);
+/* Gives a parity colouring of a 27-point grid matrix (see
+ * lgx_amg_params.grid27) the grid kernels for its sweeps through
+ * lgx_sor_sweep_permuted[_f32]; with_float also prepares the float copy of
+ * the values that lgx_sor_sweep_permuted_f32 reads.  The structure is
+ * checked on the device: *attached (may be NULL) is 0 when it does not hold
+ * and the CSR kernels stay.  Results are bit-identical either way.  No
+ * reference counterpart. */
+lgx_status lgx_colouring_grid27(lgx_colouring *c, const int64_t dims[3], int with_float,
+                                lgx_stream stream, int *attached);
 lgx_status lgx_colouring_destroy(lgx_colouring *c);
 /* Copies the colour of every row to d_colour; *ncolours receives the count.
  * Synchronises `stream`. */

@@ -172,6 +172,7 @@ def _signatures(L):
         "lgx_colouring_create_jp": [V, C.c_uint64, V, P(V)],
         "lgx_colouring_create": [V, V, I32, V, P(V)],
         "lgx_colouring_destroy": [V],
+        "lgx_colouring_grid27": [V, V, C.c_int, V, P(C.c_int)],
         "lgx_colouring_export": [V, V, P(I32), V],
         "lgx_sor_sweep": [V, V, D, C.c_int, C.c_int, V, V, V, V],
         "lgx_colouring_permute": [V, V, V, V],
@@ -486,6 +487,16 @@ class Colouring:
         nc = C.c_int32()
         _check(lib().lgx_colouring_export(self._h, _ptr(out), C.byref(nc), _stream()))
         return out, nc.value
+
+    def use_grid27(self, dims, with_float: bool = True) -> bool:
+        """Sweeps through the 27-point grid kernels when this is the parity
+        colouring of a 27-point operator on `dims`; returns whether they
+        were attached (bit-identical results either way)."""
+        d = np.ascontiguousarray(dims, dtype=np.int64)
+        att = C.c_int()
+        _check(lib().lgx_colouring_grid27(self._h, _ptr(d), int(with_float), _stream(),
+                                          C.byref(att)))
+        return bool(att.value)
 
     @property
     def handle(self):

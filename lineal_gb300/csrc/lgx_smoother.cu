@@ -657,6 +657,16 @@ lgx_status lgx_colouring_create(const lgx_matrix *a, const int32_t *d_colour, in
   return LGX_OK;
 }
 
+lgx_status lgx_colouring_grid27(lgx_colouring *c, const int64_t dims[3], int with_float,
+                                lgx_stream stream, int *attached) {
+  if (!c || !dims) return fail(LGX_ERR_INVALID, "null argument");
+  if (with_float && c->pcsr.storage == LGX_F64) LGX_CHECK(colouring_make_f32(*c, stream));
+  bool att = false;
+  LGX_CHECK(grid27_attach(*c, dims, stream, &att));
+  if (attached) *attached = att ? 1 : 0;
+  return LGX_OK;
+}
+
 lgx_status lgx_colouring_destroy(lgx_colouring *c) {
   delete c;
   return LGX_OK;

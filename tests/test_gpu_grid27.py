@@ -97,3 +97,26 @@ def test_grid_stays_off_without_the_structure(cuda):
         c = (cuda.Colouring.from_array(g27, _parity(d), 8) if colouring == "parity" else None)
         hh = cuda.HierarchyWright(**PARAMS).instantiate(g27, finest_colouring=c)
         assert not hh.grid27_active()
+
+
+@pytest.mark.parametrize("forward", [1, 0])
+def test_standalone_colouring_grid_sweeps(cuda, forward):
+    dims = (8, 12, 16)
+    m = cuda.gen_27pt(dims, _k(dims, 9))
+    plain = cuda.Colouring.from_array(m, _parity(dims), 8)
+    grid = cuda.Colouring.from_array(m, _parity(dims), 8)
+    assert grid.use_grid27(dims, with_float=True)
+    rng = np.random.default_rng(10)
+    b = cuda.permute(plain, rng.uniform(-1, 1, m.row_num()))
+    x0 = cuda.permute(plain, rng.uniform(-1, 1, m.row_num()))
+    xa, xb = x0.clone(), x0.clone()
+    cuda.sor_sweep_permuted(plain, b, xa, forward=forward)
+    cuda.sor_sweep_permuted(grid, b, xb, forward=forward)
+    np.testing.assert_array_equal(xa.cpu().numpy(), xb.cpu().numpy())
+    fa, fb = x0.float(), x0.float()
+    cuda.sor_sweep_permuted(plain, b.float(), fa, forward=forward)
+    cuda.sor_sweep_permuted(grid, b.float(), fb, forward=forward)
+    np.testing.assert_array_equal(fa.cpu().numpy(), fb.cpu().numpy())
+    # a 7-point matrix's parity colouring does not take the grid kernels
+    m7 = cuda.gen_7pt(dims, _k(dims, 9))
+    assert not cuda.Colouring.from_array(m7, _parity(dims), 8).use_grid27(dims)
