@@ -238,9 +238,11 @@ def precision_form(g, args, stream):
     b = torch.as_tensor(b_host, device="cuda")
     bn = float(torch.linalg.norm(b).item())
     hier_kw = dict(min_coarsen_size=2000, partition_size=args.partition_size,
-                   partition_growth=args.partition_growth, min_partitions=args.min_partitions)
+                   partition_growth=args.partition_growth, min_partitions=args.min_partitions,
+                   grid27=args.grid27)
     out = {"workload": f"{args.grid}^3 7-point lognormal(sigma=3, seed 2), AMG-PCG to 1e-10",
-           "rows": a.row_num(), "nnz": a.non_zero_num()}
+           "rows": a.row_num(), "nnz": a.non_zero_num(),
+           "finest_kernels": "7-point grid rows, red-black order" if args.grid27 else "CSR"}
     xs = {}
     for tag, f32, bf16, flexible in (("fp64", False, False, False),
                                      ("mixed_fcg", True, False, True),
@@ -250,6 +252,8 @@ def precision_form(g, args, stream):
             a, finest_colouring=col)
         torch.cuda.synchronize()
         setup = time.perf_counter() - t0
+        if args.autotune:
+            h.autotune(reps=3)
         for _ in range(args.warmup):
             res = g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=1e-10, maxit=1000,
                         flexible=flexible)

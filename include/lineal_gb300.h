@@ -149,6 +149,8 @@ lgx_status lgx_gen_7pt(const int64_t dims[3], const double *d_k, lgx_dtype stora
  * lgx_gen_27pt's matrices are; an AMG hierarchy checks the structure on the
  * device before it relies on it.  No reference counterpart. */
 lgx_status lgx_csr_set_grid27(lgx_matrix *a, const int64_t dims[3]);
+/* The same for a 7-point operator (lgx_gen_7pt's matrices are declared). */
+lgx_status lgx_csr_set_grid7(lgx_matrix *a, const int64_t dims[3]);
 
 /* Configuration of the CSR row kernels (SpMV, residual, Jacobi, SOR) used by
  * later launches, process-wide; no reference counterpart (tuning):
@@ -321,11 +323,13 @@ typedef struct {
                                   values a_ij / a_ii with the diagonal a_ii as a per-row
                                   float scale (2 bytes per entry instead of 4) */
   int grid27;                  /* 1 (default): when the finest matrix is a 27-point
-                                  operator on an even grid (lgx_gen_27pt, or declared by
-                                  lgx_csr_set_grid27) and the finest colouring is the
-                                  parity colouring, its products and sweeps compute the
-                                  column indices from the grid instead of reading them
-                                  (bit-identical results); 0: always the CSR kernels */
+                                  operator on an even grid with the parity colouring, or a
+                                  7-point operator (even n2) with the red-black colouring
+                                  (lgx_gen_27pt / lgx_gen_7pt, or declared by
+                                  lgx_csr_set_grid27 / lgx_csr_set_grid7), its products
+                                  and sweeps compute the column indices from the grid
+                                  instead of reading them (bit-identical results); 0:
+                                  always the CSR kernels */
 } lgx_amg_params;
 
 void lgx_amg_default_params(lgx_amg_params *p);

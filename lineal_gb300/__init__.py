@@ -163,6 +163,7 @@ def _signatures(L):
         "lgx_gen_27pt": [V, V, C.c_int, V, P(V)],
         "lgx_gen_7pt": [V, V, C.c_int, V, P(V)],
         "lgx_csr_set_grid27": [V, V],
+        "lgx_csr_set_grid7": [V, V],
         "lgx_dot": [I64, V, V, V, V],
         "lgx_dot_static": [I64, V, V, V, V],
         "lgx_norm2sq": [I64, V, V, V],
@@ -288,6 +289,12 @@ class _Matrix:
         (as gen_27pt's matrices are)."""
         d = np.ascontiguousarray(dims, dtype=np.int64)
         _check(lib().lgx_csr_set_grid27(self._h, _ptr(d)))
+
+    def set_grid7(self, dims):
+        """Declares this CSR matrix a 7-point operator on the grid `dims`
+        (as gen_7pt's matrices are)."""
+        d = np.ascontiguousarray(dims, dtype=np.int64)
+        _check(lib().lgx_csr_set_grid7(self._h, _ptr(d)))
 
     def autotune(self, reps: int = 5) -> dict:
         """Times every row-engine configuration on this CSR matrix's FP64

@@ -1024,9 +1024,9 @@ static lgx_status amg_build(const lgx_matrix *m, const lgx_amg_params &p,
     }
     if (h.f32) LGX_CHECK(colouring_make_f32(*lv.col, s));
     if (h.f32 && p.cycle_bf16) LGX_CHECK(colouring_make_bf16(*lv.col, s));
-    if (l == 0 && p.grid27 && m->grid27[0] > 0) {
+    if (l == 0 && p.grid27 && m->grid_points) {
       bool attached = false;
-      LGX_CHECK(grid27_attach(*lv.col, m->grid27, s, &attached));
+      LGX_CHECK(grid27_attach(*lv.col, m->grid_dims, m->grid_points, s, &attached));
     }
     timer.mark(s, "colouring", l);
   }

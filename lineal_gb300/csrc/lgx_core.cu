@@ -662,22 +662,35 @@ lgx_status lgx_matrix_info(const lgx_matrix *a, int *kind, int64_t *n, int64_t *
 lgx_status lgx_gen_27pt(const int64_t dims[3], const double *d_k, lgx_dtype storage,
                         lgx_stream stream, lgx_matrix **out) {
   LGX_CHECK(gen_structured(dims, d_k, 27, storage, stream, out));
-  for (int d = 0; d < 3; ++d) (*out)->grid27[d] = dims[d];
+  for (int d = 0; d < 3; ++d) (*out)->grid_dims[d] = dims[d];
+  (*out)->grid_points = 27;
   return LGX_OK;
 }
 
-lgx_status lgx_csr_set_grid27(lgx_matrix *a, const int64_t dims[3]) {
+static lgx_status csr_set_grid(lgx_matrix *a, const int64_t dims[3], int points) {
   if (!a || !dims) return fail(LGX_ERR_INVALID, "null argument");
   if (a->kind != LGX_MATRIX_CSR) return fail(LGX_ERR_INVALID, "not a CSR matrix");
   if (dims[0] < 1 || dims[1] < 1 || dims[2] < 1 || dims[0] * dims[1] * dims[2] != a->n)
     return fail(LGX_ERR_INVALID, "grid does not have one cell per row");
-  for (int d = 0; d < 3; ++d) a->grid27[d] = dims[d];
+  for (int d = 0; d < 3; ++d) a->grid_dims[d] = dims[d];
+  a->grid_points = points;
   return LGX_OK;
+}
+
+lgx_status lgx_csr_set_grid27(lgx_matrix *a, const int64_t dims[3]) {
+  return csr_set_grid(a, dims, 27);
+}
+
+lgx_status lgx_csr_set_grid7(lgx_matrix *a, const int64_t dims[3]) {
+  return csr_set_grid(a, dims, 7);
 }
 
 lgx_status lgx_gen_7pt(const int64_t dims[3], const double *d_k, lgx_dtype storage,
                        lgx_stream stream, lgx_matrix **out) {
-  return gen_structured(dims, d_k, 7, storage, stream, out);
+  LGX_CHECK(gen_structured(dims, d_k, 7, storage, stream, out));
+  for (int d = 0; d < 3; ++d) (*out)->grid_dims[d] = dims[d];
+  (*out)->grid_points = 7;
+  return LGX_OK;
 }
 
 lgx_status lgx_dot(int64_t n, const double *d_a, const double *d_b, double *d_out,

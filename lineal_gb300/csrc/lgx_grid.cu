@@ -1,21 +1,28 @@
-// Finest level of a 27-point grid matrix without column indices.
+// Finest level of a grid matrix without column indices.
 //
-// When the finest matrix of a hierarchy is a 27-point operator on an
-// n0 x n1 x n2 grid (even edges) and its colouring is the parity colouring,
-// row r of the colour-permuted matrix is the cell (i, j, k) with
-//   c = r / B,  q = r % B,  (i, j, k) = 2 (q / (h1 h2), q / h2 % h1, q % h2)
-//                                       + (c >> 2, (c >> 1) & 1, c & 1),
-// B = n / 8, h = n / 2, and the neighbour at offset (dz, dy, dx) sits at
-//   r' = c' B + ((i' >> 1) h1 + (j' >> 1)) h2 + (k' >> 1),
-//   c' = 4 (i' & 1) + 2 (j' & 1) + (k' & 1).
+// Two patterns, each with the colouring whose colour classes are contiguous
+// grid sub-lattices:
+//  * 27 points, parity colouring (even edges): row r of the colour-permuted
+//    matrix is the cell (i, j, k) with
+//      c = r / B,  q = r % B,  (i, j, k) = 2 (q / (h1 h2), q / h2 % h1, q % h2)
+//                                          + (c >> 2, (c >> 1) & 1, c & 1),
+//    B = n / 8, h = n / 2, and the neighbour at offset (dz, dy, dx) sits at
+//      r' = c' B + ((i' >> 1) h1 + (j' >> 1)) h2 + (k' >> 1),
+//      c' = 4 (i' & 1) + 2 (j' & 1) + (k' & 1),
+//    i.e. at r + delta[c][e] for a table of 8 x 27 deltas;
+//  * 7 points, red-black colouring c = (i + j + k) & 1 (even n2): B = n / 2,
+//    line L = q / h2 = i n1 + j, k = 2 (q % h2) + s with s = (c + i + j) & 1,
+//    and the neighbours (other colour) at q -+ n1 h2 (axis 0), q -+ h2
+//    (axis 1), q - 1 + s and q + s (axis 2), plus (1 - c) B.
 // The kernels compute those indices instead of reading column indices
 // (4 bytes per entry less: a third of the FP64 bytes, half of the float
 // bytes, two thirds of the bfloat16 bytes), and consecutive rows of a colour
 // -- consecutive k -- gather consecutive entries of every neighbour colour,
 // so the x reads of a warp are contiguous.  The values are stored per
-// offset (v[e S + r], S the padded plane stride); each row sums its entries in offset order, which is
-// the CSR row order, with the arithmetic of the CSR row operations (SpmvOp,
-// ResidualOp, SorOp), so every result is bit-identical to the CSR path.
+// offset (v[e S + r], S the padded plane stride); each row sums its entries
+// in offset order, which is the CSR row order, with the arithmetic of the
+// CSR row operations (SpmvOp, ResidualOp, SorOp), so every result is
+// bit-identical to the CSR path.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -26,16 +33,19 @@
 
 namespace lgx {
 
-// kernel view; delta[c][e] = r' - r for a row of colour c and its in-grid
-// neighbour at offset e (the same for every row of a colour)
+// kernel view; pts = 27 or 7; delta[c][e] = r' - r for a row of colour c
+// and its in-grid neighbour at offset e (27 points: the same for every row
+// of a colour)
 struct G27 {
-  int n0, n1, n2, h1, h2;
-  int64_t n, block, stride;
+  int pts, n0, n1, n2, h1, h2;
+  int64_t n, block, stride, n1h2;
   int32_t delta[8][27];
 };
 
 static G27 view(const Grid27 &g) {
-  G27 v{g.n0, g.n1, g.n2, g.n1 / 2, g.n2 / 2, g.n, g.block, g.stride, {}};
+  G27 v{g.points, g.n0, g.n1, g.n2, g.n1 / 2, g.n2 / 2, g.n, g.block, g.stride,
+        (int64_t)g.n1 * (g.n2 / 2), {}};
+  if (g.points != 27) return v;
   for (int c = 0; c < 8; ++c) {
     const int pi = c >> 2, pj = (c >> 1) & 1, pk = c & 1;
     for (int e = 0; e < 27; ++e) {
@@ -50,17 +60,73 @@ static G27 view(const Grid27 &g) {
   return v;
 }
 
-// cell of row r (n < 2^31: 32-bit divisions); returns the colour
-__device__ __forceinline__ int g27_cell(const G27 &g, int64_t r, int &i, int &j, int &k) {
+// offsets of entry e in CSR row order: 27 points lexicographic (dz, dy, dx);
+// 7 points (-1,0,0) (0,-1,0) (0,0,-1) (0,0,0) (0,0,1) (0,1,0) (1,0,0)
+template <int PTS>
+__host__ __device__ constexpr int g_dz(int e) {
+  return PTS == 27 ? e / 9 - 1 : (e == 0 ? -1 : e == 6 ? 1 : 0);
+}
+template <int PTS>
+__host__ __device__ constexpr int g_dy(int e) {
+  return PTS == 27 ? (e / 3) % 3 - 1 : (e == 1 ? -1 : e == 5 ? 1 : 0);
+}
+template <int PTS>
+__host__ __device__ constexpr int g_dx(int e) {
+  return PTS == 27 ? e % 3 - 1 : (e == 2 ? -1 : e == 4 ? 1 : 0);
+}
+template <int PTS>
+__host__ __device__ constexpr int g_diag() {
+  return PTS == 27 ? 13 : 3;
+}
+
+// a row's cell and what its neighbour indices need
+struct GCell {
+  int i, j, k, c, s;
+  int64_t q;
+};
+
+template <int PTS>
+__device__ __forceinline__ GCell g_cell(const G27 &g, int64_t r) {
+  GCell x;
   const unsigned ur = (unsigned)r, blk = (unsigned)g.block;
   const unsigned c = ur / blk, q = ur - c * blk;
-  const unsigned hh = (unsigned)g.h1 * (unsigned)g.h2;
-  const unsigned a = q / hh, rem = q - a * hh;
-  const unsigned bq = rem / (unsigned)g.h2, d = rem - bq * (unsigned)g.h2;
-  i = 2 * (int)a + (int)(c >> 2);
-  j = 2 * (int)bq + (int)((c >> 1) & 1);
-  k = 2 * (int)d + (int)(c & 1);
-  return (int)c;
+  x.c = (int)c;
+  x.q = q;
+  if constexpr (PTS == 27) {
+    const unsigned hh = (unsigned)g.h1 * (unsigned)g.h2;
+    const unsigned a = q / hh, rem = q - a * hh;
+    const unsigned bq = rem / (unsigned)g.h2, d = rem - bq * (unsigned)g.h2;
+    x.i = 2 * (int)a + (int)(c >> 2);
+    x.j = 2 * (int)bq + (int)((c >> 1) & 1);
+    x.k = 2 * (int)d + (int)(c & 1);
+    x.s = 0;
+  } else {
+    const unsigned L = q / (unsigned)g.h2, d = q - L * (unsigned)g.h2;
+    x.i = (int)(L / (unsigned)g.n1);
+    x.j = (int)(L - (unsigned)x.i * (unsigned)g.n1);
+    x.s = (int)((c + (unsigned)x.i + (unsigned)x.j) & 1u);
+    x.k = 2 * (int)d + x.s;
+  }
+  return x;
+}
+
+// permuted index of the in-grid neighbour at offset e
+template <int PTS>
+__device__ __forceinline__ int64_t g_nb(const G27 &g, const GCell &x, int64_t r, int e) {
+  if constexpr (PTS == 27) {
+    return r + g.delta[x.c][e];
+  } else {
+    const int64_t base = (int64_t)(1 - x.c) * g.block + x.q;
+    switch (e) {
+      case 0: return base - g.n1h2;
+      case 1: return base - g.h2;
+      case 2: return base - 1 + x.s;
+      case 4: return base + x.s;
+      case 5: return base + g.h2;
+      case 6: return base + g.n1h2;
+      default: return r;
+    }
+  }
 }
 
 // in-grid tests of a row's neighbours: bit 0/1 lower/upper neighbour exists
@@ -70,8 +136,9 @@ __device__ __forceinline__ unsigned g27_sides(const G27 &g, int i, int j, int k)
          (unsigned)(j + 1 < g.n1) << 3 | (unsigned)(k > 0) << 4 | (unsigned)(k + 1 < g.n2) << 5;
 }
 
-__device__ __forceinline__ bool g27_in(unsigned sides, int e) {
-  const int dz = e / 9 - 1, dy = (e / 3) % 3 - 1, dx = e % 3 - 1;
+template <int PTS>
+__device__ __forceinline__ bool g_in(unsigned sides, int e) {
+  const int dz = g_dz<PTS>(e), dy = g_dy<PTS>(e), dx = g_dx<PTS>(e);
   unsigned need = 0;
   if (dz < 0) need |= 1u;
   if (dz > 0) need |= 2u;
@@ -82,43 +149,42 @@ __device__ __forceinline__ bool g27_in(unsigned sides, int e) {
   return (sides & need) == need;
 }
 
-// permuted index of the in-grid cell (i, j, k)
-__device__ __forceinline__ int64_t g27_row(const G27 &g, int i, int j, int k) {
-  const int64_t c = (i & 1) * 4 + (j & 1) * 2 + (k & 1);
-  return c * g.block + ((int64_t)(i >> 1) * g.h1 + (j >> 1)) * g.h2 + (k >> 1);
-}
-
-__device__ __forceinline__ bool g27_has(const G27 &g, int i, int j, int k, int e) {
-  const int i2 = i + e / 9 - 1, j2 = j + (e / 3) % 3 - 1, k2 = k + e % 3 - 1;
-  return (unsigned)i2 < (unsigned)g.n0 && (unsigned)j2 < (unsigned)g.n1 &&
-         (unsigned)k2 < (unsigned)g.n2;
-}
-
-__device__ __forceinline__ int64_t g27_nb(const G27 &g, int i, int j, int k, int e) {
-  return g27_row(g, i + e / 9 - 1, j + (e / 3) % 3 - 1, k + e % 3 - 1);
+// the permuted index of an in-grid cell from its coordinates (the build's
+// independent check of g_nb)
+template <int PTS>
+__device__ __forceinline__ int64_t g_row_of(const G27 &g, int i, int j, int k) {
+  if constexpr (PTS == 27) {
+    const int64_t c = (i & 1) * 4 + (j & 1) * 2 + (k & 1);
+    return c * g.block + ((int64_t)(i >> 1) * g.h1 + (j >> 1)) * g.h2 + (k >> 1);
+  } else {
+    const int64_t c = (i + j + k) & 1;
+    return c * g.block + ((int64_t)i * g.n1 + j) * g.h2 + (k >> 1);
+  }
 }
 
 // ---- build: CSR rows -> per-offset values, checking the structure --------
-// bad |= 1: a row is not the cell the parity order puts there; 2: a row's
+// bad |= 1: a row is not the cell the colour order puts there; 2: a row's
 // entries are not exactly its in-grid neighbours in offset order; 4: the
-// delta table disagrees with the coordinates
-template <typename VT>
+// kernels' neighbour index disagrees with the coordinates
+template <typename VT, int PTS>
 __global__ void k_g27_fill(G27 g, const int64_t *__restrict__ rowptr,
                            const int32_t *__restrict__ col, const VT *__restrict__ val,
                            const int32_t *__restrict__ perm, VT *__restrict__ out, int *bad) {
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < g.n;
        r += (int64_t)gridDim.x * blockDim.x) {
-    int i, j, k;
-    const int c = g27_cell(g, r, i, j, k);
-    if (perm && perm[r] != ((int64_t)i * g.n1 + j) * g.n2 + k) atomicOr(bad, 1);
+    const GCell x = g_cell<PTS>(g, r);
+    if (perm && perm[r] != ((int64_t)x.i * g.n1 + x.j) * g.n2 + x.k) atomicOr(bad, 1);
+    if (g_row_of<PTS>(g, x.i, x.j, x.k) != r) atomicOr(bad, 1);
     int64_t p = rowptr[r];
     const int64_t pe = rowptr[r + 1];
-    for (int e = 0; e < 27; ++e) {
+    for (int e = 0; e < PTS; ++e) {
       VT v = static_cast<VT>(0.0f);
-      if (g27_has(g, i, j, k, e)) {
-        // the row kernels reach the neighbour through the colour's delta
-        if (r + g.delta[c][e] != g27_nb(g, i, j, k, e)) atomicOr(bad, 4);
-        if (p < pe && (int64_t)col[p] == g27_nb(g, i, j, k, e)) {
+      const int i2 = x.i + g_dz<PTS>(e), j2 = x.j + g_dy<PTS>(e), k2 = x.k + g_dx<PTS>(e);
+      if ((unsigned)i2 < (unsigned)g.n0 && (unsigned)j2 < (unsigned)g.n1 &&
+          (unsigned)k2 < (unsigned)g.n2) {
+        const int64_t want = g_row_of<PTS>(g, i2, j2, k2);
+        if (g_nb<PTS>(g, x, r, e) != want) atomicOr(bad, 4);
+        if (p < pe && (int64_t)col[p] == want) {
           v = val[p];
           ++p;
         } else {
@@ -171,10 +237,11 @@ __device__ __forceinline__ bf16 g27_ld(const bf16 *p) {
 // than deeper rounds in fewer warps.
 constexpr int kG27Batch = 3;
 
-// One row's state through its 27 entries, in the arithmetic of SpmvOp
+// One row's state through its entries, in the arithmetic of SpmvOp
 // (MODE 0), ResidualOp (MODE 1) and SorOp (MODE 2, lgx_smoother.cu).
-template <typename VT, typename XT, int MODE>
+template <typename VT, typename XT, int MODE, int PTS>
 struct G27Row {
+  static constexpr int kDiag = g_diag<PTS>();
   XT acc = XT(0), diag = XT(0), xi = XT(0);  // sum | SOR accum (bf16: t), diagonal (bf16: v_ii)
   __device__ __forceinline__ void init(int64_t r, const XT *b, const XT *x, const G27Sor &so) {
     if constexpr (MODE == 2) {
@@ -188,10 +255,10 @@ struct G27Row {
     if constexpr (MODE != 2) {
       acc = fma(a, xv, acc);
     } else if constexpr (kIsBf16<VT>) {
-      if (e == 13) diag = a;
+      if (e == kDiag) diag = a;
       else acc = fma(a, xv, acc);
     } else {
-      if (e == 13) {
+      if (e == kDiag) {
         diag = a;
         if (so.ultra) acc = fma(-a, xi, acc);
       } else {
@@ -244,15 +311,15 @@ struct G27Row {
 
 // x of neighbour c for entry e of a row (0 for unvisited colours in a
 // forward sweep from zero; the diagonal's x is not read here)
-template <typename XT, int MODE>
+template <typename XT, int MODE, int PTS>
 __device__ __forceinline__ XT g27_x(const XT *x, int64_t c, int e, const G27Sor &so) {
-  if (MODE == 2 && e == 13) return XT(0);
+  if (MODE == 2 && e == g_diag<PTS>()) return XT(0);
   const XT xl = g27_ld(x + c);
   return (MODE == 2 && so.from_zero && c >= so.visit_end) ? XT(0) : xl;
 }
 
 // one row per thread
-template <typename VT, typename XT, int MODE>
+template <typename VT, typename XT, int MODE, int PTS>
 __global__ void __launch_bounds__(256)
   k_g27_rows(G27 g, int64_t rb, int64_t re, const VT *__restrict__ v, const XT *__restrict__ b,
              XT *x, XT *__restrict__ y, const float *__restrict__ scale, G27Sor so) {
@@ -260,26 +327,29 @@ __global__ void __launch_bounds__(256)
   pdl_wait();
   const int64_t r = rb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (r >= re) return;
-  int i, j, k;
-  const int col = g27_cell(g, r, i, j, k);
-  const unsigned sides = g27_sides(g, i, j, k);
-  const int32_t *dl = g.delta[col];
+  const GCell cell = g_cell<PTS>(g, r);
+  const unsigned sides = g27_sides(g, cell.i, cell.j, cell.k);
   constexpr int B = kG27Batch;
-  G27Row<VT, XT, MODE> row;
+  G27Row<VT, XT, MODE, PTS> row;
   row.init(r, b, x, so);
   // the loads of a round do not branch -- a neighbour outside the grid reads
   // x of the row itself, which step() then skips -- so they go out together
 #pragma unroll
-  for (int e0 = 0; e0 < 27; e0 += B) {
+  for (int e0 = 0; e0 < PTS; e0 += B) {
     XT xv[B], av[B];
 #pragma unroll
     for (int u = 0; u < B; ++u) {
       const int e = e0 + u;
+      if (e >= PTS) break;
       av[u] = cvt<XT>(g27_ld(v + (int64_t)e * g.stride + r));
-      xv[u] = g27_x<XT, MODE>(x, g27_in(sides, e) ? r + dl[e] : r, e, so);
+      xv[u] = g27_x<XT, MODE, PTS>(x, g_in<PTS>(sides, e) ? g_nb<PTS>(g, cell, r, e) : r, e, so);
     }
 #pragma unroll
-    for (int u = 0; u < B; ++u) row.step(e0 + u, g27_in(sides, e0 + u), av[u], xv[u], so);
+    for (int u = 0; u < B; ++u) {
+      const int e = e0 + u;
+      if (e >= PTS) break;
+      row.step(e, g_in<PTS>(sides, e), av[u], xv[u], so);
+    }
   }
   row.finish(r, b, x, y, scale, so);
 }
@@ -307,7 +377,7 @@ __device__ __forceinline__ void g27_ldv<bf16, 4>(const bf16 *p, float (&out)[4])
   for (int q = 0; q < 4; ++q) out[q] = __bfloat162float(__ushort_as_bfloat16(h[q]));
 }
 
-template <typename VT, int MODE>
+template <typename VT, int MODE, int PTS>
 __global__ void __launch_bounds__(256)
   k_g27_rows4(G27 g, int64_t rb, int64_t re, const VT *__restrict__ v,
               const float *__restrict__ b, float *x, float *__restrict__ y,
@@ -317,31 +387,41 @@ __global__ void __launch_bounds__(256)
   pdl_wait();
   const int64_t r0 = rb + (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) * R;
   if (r0 >= re) return;
-  int i, j, k;
-  const int col = g27_cell(g, r0, i, j, k);
-  const int32_t *dl = g.delta[col];
+  // the four cells share i, j and colour; k grows by 2 and q by 1
+  GCell cell[R];
+  cell[0] = g_cell<PTS>(g, r0);
   unsigned sides[R];
 #pragma unroll
-  for (int q = 0; q < R; ++q) sides[q] = g27_sides(g, i, j, k + 2 * q);
-  G27Row<VT, float, MODE> row[R];
+  for (int q = 0; q < R; ++q) {
+    cell[q] = cell[0];
+    cell[q].k += 2 * q;
+    cell[q].q += q;
+    sides[q] = g27_sides(g, cell[q].i, cell[q].j, cell[q].k);
+  }
+  G27Row<VT, float, MODE, PTS> row[R];
 #pragma unroll
   for (int q = 0; q < R; ++q) row[q].init(r0 + q, b, x, so);
   constexpr int B = kG27Batch;
 #pragma unroll
-  for (int e0 = 0; e0 < 27; e0 += B) {
+  for (int e0 = 0; e0 < PTS; e0 += B) {
     float av[B][R], xv[B][R];
 #pragma unroll
     for (int u = 0; u < B; ++u) {
       const int e = e0 + u;
+      if (e >= PTS) break;
       g27_ldv<VT, R>(v + (int64_t)e * g.stride + r0, av[u]);
 #pragma unroll
       for (int q = 0; q < R; ++q)
-        xv[u][q] = g27_x<float, MODE>(x, g27_in(sides[q], e) ? r0 + q + dl[e] : r0 + q, e, so);
+        xv[u][q] = g27_x<float, MODE, PTS>(
+          x, g_in<PTS>(sides[q], e) ? g_nb<PTS>(g, cell[q], r0 + q, e) : r0 + q, e, so);
     }
 #pragma unroll
-    for (int u = 0; u < B; ++u)
+    for (int u = 0; u < B; ++u) {
+      const int e = e0 + u;
+      if (e >= PTS) break;
 #pragma unroll
-      for (int q = 0; q < R; ++q) row[q].step(e0 + u, g27_in(sides[q], e0 + u), av[u][q], xv[u][q], so);
+      for (int q = 0; q < R; ++q) row[q].step(e, g_in<PTS>(sides[q], e), av[u][q], xv[u][q], so);
+    }
   }
 #pragma unroll
   for (int q = 0; q < R; ++q) row[q].finish(r0 + q, b, x, y, scale, so);
@@ -363,30 +443,40 @@ static const VT *grid_values(const Grid27 &g, const VT *src) {
   else return src == g.src32 ? (const VT *)g.v32.p : nullptr;
 }
 
-template <typename VT, typename XT, int MODE>
-static lgx_status launch_g27(const Grid27 &gr, const VT *v, int64_t rb, int64_t re, const XT *b,
-                             XT *x, XT *y, const float *scale, const G27Sor &so,
-                             cudaStream_t s) {
-  if (re <= rb) return LGX_OK;
+template <typename VT, typename XT, int MODE, int PTS>
+static lgx_status launch_g27_pts(const Grid27 &gr, const VT *v, int64_t rb, int64_t re,
+                                 const XT *b, XT *x, XT *y, const float *scale,
+                                 const G27Sor &so, cudaStream_t s) {
   const int64_t rows = re - rb;
   const bool pdl = sizeof(XT) == 4 || rows <= pdl_fp64_rows();
   if constexpr (kIsBf16<VT>) {
     // bfloat16 values: four rows per thread (8-byte value loads) when every
     // thread's four rows are whole, in one colour block and in one grid line.
-    // Measured at 256^3: bf16 cycle 296 -> 273 ms; float values lose with it
-    // (272 -> 281 ms: their rows run one per thread)
+    // Measured at 256^3 (27 points): bf16 cycle 296 -> 273 ms; float values
+    // lose with it (272 -> 281 ms: their rows run one per thread)
     if (g27_rows4_enabled() && (gr.n2 / 2) % 4 == 0 && gr.block % 4 == 0 && rb % 4 == 0 &&
         re % 4 == 0) {
-      LGX_CUDA(launch_pdl(pdl, k_g27_rows4<VT, MODE>, dim3((unsigned)((rows / 4 + 255) / 256)),
-                          dim3(256), 0, s, view(gr), rb, re, v, b, x, y, scale, so));
+      LGX_CUDA(launch_pdl(pdl, k_g27_rows4<VT, MODE, PTS>,
+                          dim3((unsigned)((rows / 4 + 255) / 256)), dim3(256), 0, s, view(gr),
+                          rb, re, v, b, x, y, scale, so));
       count_launch();
       return LGX_OK;
     }
   }
-  LGX_CUDA(launch_pdl(pdl, k_g27_rows<VT, XT, MODE>, dim3((unsigned)((rows + 255) / 256)),
+  LGX_CUDA(launch_pdl(pdl, k_g27_rows<VT, XT, MODE, PTS>, dim3((unsigned)((rows + 255) / 256)),
                       dim3(256), 0, s, view(gr), rb, re, v, b, x, y, scale, so));
   count_launch();
   return LGX_OK;
+}
+
+template <typename VT, typename XT, int MODE>
+static lgx_status launch_g27(const Grid27 &gr, const VT *v, int64_t rb, int64_t re, const XT *b,
+                             XT *x, XT *y, const float *scale, const G27Sor &so,
+                             cudaStream_t s) {
+  if (re <= rb) return LGX_OK;
+  if (gr.points == 7)
+    return launch_g27_pts<VT, XT, MODE, 7>(gr, v, rb, re, b, x, y, scale, so, s);
+  return launch_g27_pts<VT, XT, MODE, 27>(gr, v, rb, re, b, x, y, scale, so, s);
 }
 
 template <typename VT, typename XT>
@@ -471,31 +561,38 @@ template lgx_status grid_sor_rows<bf16, float>(const Csr &, const bf16 *, int64_
 template <typename VT>
 static lgx_status fill_one(const G27 &g, const Csr &p, const VT *src, const int32_t *perm,
                            DBuf<VT> &out, int *bad, cudaStream_t s) {
-  LGX_CHECK(out.alloc(27 * g.stride));
+  LGX_CHECK(out.alloc(g.pts * g.stride));
   const unsigned grid = (unsigned)std::min<int64_t>(grid_for(g.n, 256), 16384);
-  k_g27_fill<VT><<<grid, 256, 0, s>>>(g, p.rowptr.p, p.col.p, src, perm, out.p, bad);
+  if (g.pts == 27)
+    k_g27_fill<VT, 27><<<grid, 256, 0, s>>>(g, p.rowptr.p, p.col.p, src, perm, out.p, bad);
+  else
+    k_g27_fill<VT, 7><<<grid, 256, 0, s>>>(g, p.rowptr.p, p.col.p, src, perm, out.p, bad);
   LGX_LAUNCH_CHECK();
   count_launch();
   return LGX_OK;
 }
 
-lgx_status grid27_attach(lgx_colouring &c, const int64_t dims[3], cudaStream_t s,
+lgx_status grid27_attach(lgx_colouring &c, const int64_t dims[3], int points, cudaStream_t s,
                          bool *attached) {
   *attached = false;
   const int64_t n = dims[0] * dims[1] * dims[2];
-  if (dims[0] < 2 || dims[1] < 2 || dims[2] < 2 || dims[0] % 2 || dims[1] % 2 || dims[2] % 2 ||
-      dims[0] > (1 << 30) || dims[1] > (1 << 30) || dims[2] > (1 << 30) ||
+  const int ncol = points == 27 ? 8 : 2;
+  if (points != 27 && points != 7) return LGX_OK;
+  if (dims[0] < 1 || dims[1] < 1 || dims[2] < 2 || dims[2] % 2 || dims[0] > (1 << 30) ||
+      dims[1] > (1 << 30) || dims[2] > (1 << 30) ||
       n + 64 > (int64_t)INT32_MAX)  // 32-bit row arithmetic in the kernels
     return LGX_OK;
-  if (c.n != n || c.ncolours != 8 || c.pcsr.n != n) return LGX_OK;
-  for (int q = 0; q <= 8; ++q)
-    if (c.offsets[q] != q * (n / 8)) return LGX_OK;
+  if (points == 27 && (dims[0] % 2 || dims[1] % 2)) return LGX_OK;
+  if (c.n != n || c.ncolours != ncol || c.pcsr.n != n) return LGX_OK;
+  for (int q = 0; q <= ncol; ++q)
+    if (c.offsets[q] != q * (n / ncol)) return LGX_OK;
   auto gr = std::make_shared<Grid27>();
+  gr->points = points;
   gr->n0 = (int)dims[0];
   gr->n1 = (int)dims[1];
   gr->n2 = (int)dims[2];
   gr->n = n;
-  gr->block = n / 8;
+  gr->block = n / ncol;
   gr->stride = ((n + 31) / 32) * 32;
   if ((gr->stride / 32) % 2 == 0) gr->stride += 32;
   const G27 g = view(*gr);

@@ -122,9 +122,10 @@ struct Csr {
   std::shared_ptr<const Grid27> grid;
 };
 
-// Colour-permuted 27-point grid matrix (even edge lengths, parity colouring
-// c = 4 (i & 1) + 2 (j & 1) + (k & 1), colour c in rows [c B, (c + 1) B) with
-// B = n / 8, natural order inside a colour).  Row values are stored per
+// Colour-permuted grid matrix: 27 points (even edge lengths, parity
+// colouring c = 4 (i & 1) + 2 (j & 1) + (k & 1), B = n / 8) or 7 points (even
+// n2, red-black colouring c = (i + j + k) & 1, B = n / 2); colour c in rows
+// [c B, (c + 1) B), natural order inside a colour.  Row values are stored per
 // stencil offset e = 9 (dz + 1) + 3 (dy + 1) + (dx + 1) -- the CSR row order
 // -- offset-major (v[e S + r], S = n padded to an odd multiple of 32
 // entries so that the 27 planes of one row do not sit a power of two apart),
@@ -132,6 +133,7 @@ struct Csr {
 // Each array mirrors the CSR value array it was built from (src*): products
 // and sweeps switch to the grid only when given that array.
 struct Grid27 {
+  int points = 27;  // 27 (parity colouring) or 7 (red-black colouring, block n / 2)
   int n0 = 0, n1 = 0, n2 = 0;
   int64_t n = 0, block = 0, stride = 0;
   DBuf<double> v64;
@@ -170,7 +172,8 @@ struct lgx_matrix {
   lgx::DBuf<uint8_t> mat;       // stencil lookup materials (owned copy)
   lgx::DBuf<double> k;          // stencil value conductivities (owned copy)
   lgx::DBuf<double> diag;       // cached diagonal (lazily computed)
-  int64_t grid27[3] = {0, 0, 0};  // CSR kinds: 27-point operator on this grid (0: unknown)
+  int64_t grid_dims[3] = {0, 0, 0};  // CSR kinds: grid operator on this grid
+  int grid_points = 0;                // 27 or 7 points; 0: unknown
 };
 
 // Colour-permuted copy of a CSR matrix used by the multicolour smoothers.
@@ -264,9 +267,10 @@ lgx_status mc_sor_sweep(const lgx_colouring &c, const VT *val, double relax, int
                         int ultra, const XT *b, XT *x, cudaStream_t s, int from_zero = 0,
                         const float *scale = nullptr);
 lgx_status colouring_make_bf16(lgx_colouring &c, cudaStream_t s);
-// gives c.pcsr a Grid27 when it is the parity-coloured 27-point operator on
-// `dims` (checked on the device; *attached tells whether it was)
-lgx_status grid27_attach(lgx_colouring &c, const int64_t dims[3], cudaStream_t s,
+// gives c.pcsr a Grid27 when it is the parity-coloured 27-point (points 27)
+// or red-black 7-point (points 7) operator on `dims` (checked on the device;
+// *attached tells whether it was)
+lgx_status grid27_attach(lgx_colouring &c, const int64_t dims[3], int points, cudaStream_t s,
                          bool *attached);
 
 lgx_status jacobi_csr(const Csr &a, double relax, const double *x_in, double *x_out,

@@ -662,7 +662,7 @@ lgx_status lgx_colouring_grid27(lgx_colouring *c, const int64_t dims[3], int wit
   if (!c || !dims) return fail(LGX_ERR_INVALID, "null argument");
   if (with_float && c->pcsr.storage == LGX_F64) LGX_CHECK(colouring_make_f32(*c, stream));
   bool att = false;
-  LGX_CHECK(grid27_attach(*c, dims, stream, &att));
+  LGX_CHECK(grid27_attach(*c, dims, 27, stream, &att));
   if (attached) *attached = att ? 1 : 0;
   return LGX_OK;
 }

@@ -120,3 +120,61 @@ def test_standalone_colouring_grid_sweeps(cuda, forward):
     # a 7-point matrix's parity colouring does not take the grid kernels
     m7 = cuda.gen_7pt(dims, _k(dims, 9))
     assert not cuda.Colouring.from_array(m7, _parity(dims), 8).use_grid27(dims)
+
+
+def _red_black(dims):
+    i, j, k = np.meshgrid(*[np.arange(d) for d in dims], indexing="ij")
+    return ((i + j + k) % 2).ravel().astype(np.int32)
+
+
+@pytest.mark.parametrize("form", list(FORMS))
+@pytest.mark.parametrize("dims", [(7, 9, 12), (16, 16, 16), (3, 6, 8), (5, 7, 4)])
+def test_grid7_vcycle_equals_csr(cuda, form, dims):
+    """7-point operators with the red-black colouring (odd n0, n1 allowed;
+    (16, 16, 16) runs the four-row bfloat16 kernels)."""
+    m = cuda.gen_7pt(dims, _k(dims, 11))
+    col = cuda.Colouring.from_array(m, _red_black(dims), 2)
+    hg = cuda.HierarchyWright(grid27=True, **PARAMS, **FORMS[form]).instantiate(
+        m, finest_colouring=col)
+    hc = cuda.HierarchyWright(grid27=False, **PARAMS, **FORMS[form]).instantiate(
+        m, finest_colouring=col)
+    assert hg.grid27_active() and not hc.grid27_active()
+    b = np.random.default_rng(12).uniform(-1, 1, m.row_num())
+    np.testing.assert_array_equal(hg.vcycle(b).cpu().numpy(), hc.vcycle(b).cpu().numpy())
+
+
+@pytest.mark.parametrize("form", ["fp64", "f32", "bf16"])
+def test_grid7_pcg_equals_csr(cuda, form):
+    dims = (17, 20, 24)
+    m = cuda.gen_7pt(dims, np.exp(3.0 * np.random.default_rng(2).standard_normal(
+        int(np.prod(dims)))))
+    col = cuda.Colouring.from_array(m, _red_black(dims), 2)
+    kw = FORMS[form]
+    hg = cuda.HierarchyWright(grid27=True, **PARAMS, **kw).instantiate(m, finest_colouring=col)
+    hc = cuda.HierarchyWright(grid27=False, **PARAMS, **kw).instantiate(m, finest_colouring=col)
+    b = np.random.default_rng(6).uniform(-1, 1, m.row_num())
+    flexible = form != "fp64"
+    rg = cuda.pcg(m, b, precon=cuda.PRECON_AMG, amg=hg, rtol=1e-10, maxit=500, flexible=flexible)
+    rc = cuda.pcg(m, b, precon=cuda.PRECON_AMG, amg=hc, rtol=1e-10, maxit=500, flexible=flexible)
+    assert rg.iterations == rc.iterations
+    np.testing.assert_array_equal(rg.x.cpu().numpy(), rc.x.cpu().numpy())
+
+
+def test_grid7_stays_off_without_the_structure(cuda):
+    dims = (6, 8, 10)
+    # odd n2, a 27-point matrix declared as 7-point, a parity (8-colour)
+    # colouring of a 7-point matrix: the CSR path stays
+    m = cuda.gen_7pt((6, 8, 9), _k((6, 8, 9)))
+    h = cuda.HierarchyWright(**PARAMS).instantiate(
+        m, finest_colouring=cuda.Colouring.from_array(m, _red_black((6, 8, 9)), 2))
+    assert not h.grid27_active()
+    ref = lo.gen_27pt(dims, _k(dims))
+    m27 = cuda.CsrMatrix.from_host(ref.rowptr, ref.col, ref.val, symmetric=True)
+    m27.set_grid7(dims)
+    h = cuda.HierarchyWright(**PARAMS).instantiate(
+        m27, finest_colouring=cuda.Colouring.from_array(m27, _parity(dims), 8))
+    assert not h.grid27_active()
+    m7 = cuda.gen_7pt(dims, _k(dims))
+    h = cuda.HierarchyWright(**PARAMS).instantiate(
+        m7, finest_colouring=cuda.Colouring.from_array(m7, _parity(dims), 8))
+    assert not h.grid27_active()
