@@ -954,7 +954,8 @@ def main():
     ap.add_argument("--batch-systems", type=int, default=1024)
     ap.add_argument("--batch-cpu-sample", type=int, default=16)
     ap.add_argument("--fd-directions", type=int, default=64)
-    ap.add_argument("--grid", type=int, default=256)
+    ap.add_argument("--grid", type=int, default=None,
+                    help="grid edge (default 256; 128 for --mode adjoint and --mode multi)")
     ap.add_argument("--partition-size", type=int, default=4096)
     ap.add_argument("--partition-growth", type=float, default=4.0)
     ap.add_argument("--min-partitions", type=int, default=8)
@@ -977,6 +978,9 @@ def main():
     ap.add_argument("--spmv-traffic", type=float, default=None,
                     help="DRAM bytes per SpMV launch from an ncu capture")
     args = ap.parse_args()
+    if args.grid is None:
+        # the differentiation and multi-right-hand-side configurations are 128^3
+        args.grid = 128 if args.mode in ("adjoint", "multi") else 256
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
     if args.impl == "reference":
