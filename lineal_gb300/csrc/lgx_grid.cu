@@ -229,8 +229,8 @@ __device__ __forceinline__ bf16 g27_ld(const bf16 *p) {
   return __ushort_as_bfloat16(v);
 }
 
-// entries whose loads are issued together before their FMAs: nine rounds of
-// three.  Measured at 256^3 (AMG-PCG, FP64 / float cycle): rounds of 27
+// entries whose loads are issued together before their FMAs: rounds of
+// three (nine rounds for 27 points, three for 7).  Measured at 256^3 (AMG-PCG, FP64 / float cycle): rounds of 27
 // (float) 346 ms mixed; of 9: FP64 456, mixed 296 ms; of 3: FP64 432, mixed
 // 274 ms; single loads: FP64 452, mixed 297 ms -- short rounds keep the
 // registers low and more warps resident, which hides the gathers better

@@ -117,7 +117,7 @@ struct Csr {
   DBuf<int32_t> col;
   DBuf<double> v64;
   DBuf<float> v32;
-  // rows of a 27-point grid matrix in parity-colour order, stored without
+  // rows of a 27- or 7-point grid matrix in colour order, stored without
   // column indices (products and sweeps use it when set; see lgx_grid.cu)
   std::shared_ptr<const Grid27> grid;
 };
@@ -225,7 +225,7 @@ lgx_status csr_residual(const Csr &a, const VT *val, const XT *b, const XT *x, X
                         double *norm, double *partials, unsigned *counter, cudaStream_t s,
                         const float *scale = nullptr);
 
-// 27-point grid rows without column indices (lgx_grid.cu): each runs when
+// grid rows without column indices (lgx_grid.cu): each runs when
 // `a` carries a grid mirroring `val` (*done), else leaves the work to the
 // CSR kernels
 template <typename VT, typename XT>

@@ -284,7 +284,7 @@ lgx_status lgx_amg_autotune(lgx_amg *h, int reps, lgx_tune_entry *out, int max_o
   const int L = (int)h->lv.size();
   for (int l = 0; l < L; ++l) {
     lgx_amg_level &lv = *h->lv[l];
-    // the coarsest level is solved densely; it has no smoother; a 27-point
+    // the coarsest level is solved densely; it has no smoother; a
     // grid level runs its own kernels, not the row engine
     if (!lv.col || l == L - 1 || lv.col->pcsr.n == 0 || lv.col->pcsr.grid) continue;
     lgx_colouring &c = *lv.col;
