@@ -592,12 +592,15 @@ template <bool LOOKUP, bool RESID, bool NORM>
 static lgx_status launch_planes(const StencilDesc &st, const CUtensorMap &map,
                                 const StencilDev &S, const double *b, double *y, double *norm,
                                 double *partials, unsigned *counter, cudaStream_t s) {
-  static int per_sm = -1;
-  if (per_sm < 0) {
+  // CTAs per SM, queried once per kernel (0 until the first query succeeds)
+  static std::atomic<int> cached{0};
+  int per_sm = cached.load(std::memory_order_relaxed);
+  if (per_sm == 0) {
     int v = 0;
     LGX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
       &v, k_st_apply_planes<LOOKUP, RESID, NORM>, kStPlaneThreads, 0));
     per_sm = std::max(v, 1);
+    cached.store(per_sm, std::memory_order_relaxed);
   }
   const int64_t n0 = st.dims[0], n1 = st.dims[1], n2 = st.dims[2];
   const int64_t gx = (n2 + kStT2 - 1) / kStT2, gy = (n1 + kStT1 - 1) / kStT1;
