@@ -785,9 +785,11 @@ __global__ void k_dense_from_csr(int64_t n, const int64_t *rowptr, const int32_t
 
 // step k, part 1: pivot row scaled into prow, column factors into pcol
 __global__ void k_gj_pivot(int64_t n, int64_t k, double *a, double *prow, double *pcol,
-                           int *bad) {
+                           int *bad, int spd) {
   const double p = a[k * n + k];
-  if (!(p > 0.0)) {
+  // symmetric hierarchies: CholeskySolver's positive pivots; nonsymmetric:
+  // LuSolver's unpivoted elimination, which needs a nonzero finite pivot
+  if (spd ? !(p > 0.0) : !(p != 0.0 && isfinite(p))) {
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(bad, 1);
     return;
   }
@@ -832,6 +834,11 @@ __global__ void k_dense_apply(int64_t n, const double *ainv, const XT *b, XT *x)
   }
 }
 
+// Explicit inverse of the coarsest matrix by Gauss-Jordan elimination without
+// pivoting: the elimination of CholeskySolver (symmetric matrices: every
+// pivot must be positive) or of LuSolver (nonsymmetric: nonzero pivots;
+// lu/decomposition.hpp:31-122 does not pivot either), applied later as one
+// dense product per V-cycle.
 lgx_status dense_inverse(const Csr &a, cudaStream_t s, DBuf<double> &inv) {
   const int64_t n = a.n;
   LGX_CHECK(inv.alloc(n * n));
@@ -850,14 +857,16 @@ lgx_status dense_inverse(const Csr &a, cudaStream_t s, DBuf<double> &inv) {
   const unsigned g1 = (unsigned)std::min<int64_t>(grid_for(n, 256), 1024);
   const unsigned g2 = (unsigned)std::min<int64_t>(grid_for(n * n, 256), 4096);
   for (int64_t k = 0; k < n; ++k) {
-    k_gj_pivot<<<g1, 256, 0, s>>>(n, k, inv.p, prow.p, pcol.p, bad.p);
+    k_gj_pivot<<<g1, 256, 0, s>>>(n, k, inv.p, prow.p, pcol.p, bad.p, a.symmetric);
     k_gj_update<<<g2, 256, 0, s>>>(n, k, inv.p, prow.p, pcol.p, bad.p);
   }
   LGX_LAUNCH_CHECK();
   int h_bad = 0;
   LGX_CUDA(cudaMemcpyAsync(&h_bad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   LGX_CUDA(cudaStreamSynchronize(s));
-  if (h_bad) return fail(LGX_ERR_NOT_SPD, "coarsest matrix has a non-positive pivot");
+  if (h_bad)
+    return a.symmetric ? fail(LGX_ERR_NOT_SPD, "coarsest matrix has a non-positive pivot")
+                       : fail(LGX_ERR_BREAKDOWN, "coarsest matrix has a zero pivot");
   return LGX_OK;
 }
 

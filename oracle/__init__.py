@@ -165,6 +165,9 @@ def _setup_signatures(L):
     L.lo_cholesky_factor.restype = C.c_int
     L.lo_cholesky_factor.argtypes = [P(_Csr), C.c_void_p]
     L.lo_cholesky_solve.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.lo_lu_factor.restype = C.c_int
+    L.lo_lu_factor.argtypes = [P(_Csr), C.c_void_p]
+    L.lo_lu_solve.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]
     L.lo_amg_default_params.argtypes = [P(_AmgParams)]
     L.lo_amg_partitions.restype = C.c_int64
     L.lo_amg_partitions.argtypes = [C.c_int64, C.c_int64, P(_AmgParams)]
@@ -440,6 +443,24 @@ def cholesky_solve(l: np.ndarray, b: np.ndarray) -> np.ndarray:
     b = np.ascontiguousarray(b, dtype=np.float64)
     x = np.empty(len(b))
     lib().lo_cholesky_solve(len(b), _ptr(l), _ptr(b), _ptr(x))
+    return x
+
+
+def lu_factor(a: Csr) -> np.ndarray:
+    """Dense L (unit diagonal, below) and U (on and above the diagonal) of
+    the unpivoted LU (lu/decomposition.hpp)."""
+    c = a._c()
+    lu = np.zeros((a.n, a.n))
+    if lib().lo_lu_factor(C.byref(c), _ptr(lu)):
+        raise np.linalg.LinAlgError("zero pivot")
+    return lu
+
+
+def lu_solve(lu: np.ndarray, b: np.ndarray) -> np.ndarray:
+    lu = np.ascontiguousarray(lu, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.empty(len(b))
+    lib().lo_lu_solve(len(b), _ptr(lu), _ptr(b), _ptr(x))
     return x
 
 

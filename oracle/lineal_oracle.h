@@ -151,6 +151,11 @@ void lo_colour_order(int64_t n, const int32_t *colour, int32_t ncolours, int32_t
 int lo_cholesky_factor(const lo_csr *a, double *l);
 /* cholesky/solver.hpp:42-50, substitution.hpp:27-115 */
 void lo_cholesky_solve(int64_t n, const double *l, const double *b, double *x);
+/* lu/decomposition.hpp:31-122 (LU without pivoting), dense storage: L (unit
+ * diagonal) below, U on and above the diagonal.  Returns 0 on success. */
+int lo_lu_factor(const lo_csr *a, double *lu);
+/* lu/solver.hpp:37-60 */
+void lo_lu_solve(int64_t n, const double *lu, const double *b, double *x);
 
 /* ---- AMG ------------------------------------------------------------ */
 typedef struct {
@@ -211,7 +216,8 @@ typedef struct {
 typedef struct {
   int64_t nlevels;
   lo_amg_level lv[32];
-  double *chol;      /* dense lower factor of the coarsest matrix */
+  double *chol;      /* dense factor of the coarsest matrix: Cholesky lower
+                        factor (symmetric), L and U of an LU (nonsymmetric) */
   lo_amg_params p;
 } lo_amg;
 

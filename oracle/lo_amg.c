@@ -599,7 +599,10 @@ int lo_amg_setup(const lo_csr *a0, const lo_amg_params *p, lo_amg *h) {
   last->x = (double *)calloc((size_t)last->a.n + 1, sizeof(double));
   last->r = (double *)calloc((size_t)last->a.n + 1, sizeof(double));
   h->chol = (double *)malloc((size_t)(last->a.n * last->a.n + 1) * sizeof(double));
-  return lo_cholesky_factor(&last->a, h->chol);
+  /* coarse solver: CholeskySolver for symmetric, LuSolver for nonsymmetric
+   * hierarchies (test/aux/default.hpp:160-162) */
+  return last->a.symmetric ? lo_cholesky_factor(&last->a, h->chol)
+                           : lo_lu_factor(&last->a, h->chol);
 }
 
 void lo_amg_free(lo_amg *h) {
@@ -650,7 +653,10 @@ void lo_amg_vcycle(lo_amg *h, const double *b, double *x) {
     }
   }
   lo_amg_level *last = &h->lv[L - 1];
-  lo_cholesky_solve(last->a.n, h->chol, last->b, last->x);
+  if (last->a.symmetric)
+    lo_cholesky_solve(last->a.n, h->chol, last->b, last->x);
+  else
+    lo_lu_solve(last->a.n, h->chol, last->b, last->x);
   for (int64_t l = L - 2; l >= 0; --l) {
     lo_amg_level *lv = &h->lv[l];
     const double *bl = l == 0 ? b : lv->b;

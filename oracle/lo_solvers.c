@@ -202,6 +202,50 @@ void lo_cholesky_solve(int64_t n, const double *l, const double *b, double *x) {
   free(aux);
 }
 
+/* lu/decomposition.hpp:31-122 (row-wise LU without pivoting), dense storage:
+ * row i starts from A's row; each lower entry j < i, in increasing j (fill-in
+ * included), becomes l_ij = w_j / u_jj and subtracts l_ij times U's row j
+ * past its diagonal; then u_ii = w_i and u_ik = w_k for k > i (unit lower
+ * diagonal).  lu holds L below and U on and above the diagonal.  Returns 0,
+ * or -1 for a zero pivot. */
+int lo_lu_factor(const lo_csr *a, double *lu) {
+  const int64_t n = a->n;
+  memset(lu, 0, (size_t)(n * n) * sizeof(double));
+  for (int64_t i = 0; i < n; ++i) {
+    double *w = lu + i * n;
+    for (int64_t e = a->rowptr[i]; e < a->rowptr[i + 1]; ++e) w[a->col[e]] = a->val[e];
+    for (int64_t j = 0; j < i; ++j) {
+      if (w[j] == 0.0) continue;
+      const double *uj = lu + j * n;
+      const double l = w[j] / uj[j];
+      w[j] = l;
+      for (int64_t k = j + 1; k < n; ++k)
+        if (uj[k] != 0.0) w[k] -= l * uj[k];
+    }
+    if (w[i] == 0.0) return -1;
+  }
+  return 0;
+}
+
+/* lu/solver.hpp:37-60: forward substitution with the unit lower factor,
+ * backward substitution with the upper factor */
+void lo_lu_solve(int64_t n, const double *lu, const double *b, double *x) {
+  for (int64_t i = 0; i < n; ++i) {
+    double sum = b[i];
+    const double *li = lu + i * n;
+    for (int64_t j = 0; j < i; ++j)
+      if (li[j] != 0.0) sum -= li[j] * x[j];
+    x[i] = sum;
+  }
+  for (int64_t i = n - 1; i >= 0; --i) {
+    double sum = x[i];
+    const double *ui = lu + i * n;
+    for (int64_t k = i + 1; k < n; ++k)
+      if (ui[k] != 0.0) sum -= ui[k] * x[k];
+    x[i] = sum / ui[i];
+  }
+}
+
 /* ---- preconditioner application: z = M^-1 r from a zero start -------- */
 static void precon_apply(const lo_csr *a, const lo_precon *m, const double *r, double *z,
                          double *aux) {

@@ -122,3 +122,36 @@ def test_finest_parity_colouring(cuda):
     # one V-cycle reduces the residual of the error equation
     r = b - lo.spmv(ref, x)
     assert np.linalg.norm(r) < 0.5 * np.linalg.norm(b)
+
+
+def _convdiff():
+    # upwind convection-diffusion: nonsymmetric values and coarse operators
+    return lo.gen_convdiff((14, 13, 12), (8.0, -5.0, 3.0))
+
+
+def test_vcycle_nonsymmetric_lu_coarse_matches_oracle(cuda):
+    """Nonsymmetric hierarchy (coarsest solved like LuSolver: unpivoted
+    elimination) against the oracle's LU."""
+    ref = _convdiff()
+    m = cuda.CsrMatrix.from_host(ref.rowptr, ref.col, ref.val, symmetric=False)
+    h = cuda.HierarchyWright(**PARAMS).instantiate(m)
+    oh = lo.Amg(ref, smoother_parts=0, **PARAMS)
+    b = np.random.default_rng(4).uniform(-1, 1, ref.n)
+    got = h.vcycle(b).cpu().numpy()
+    want = oh.vcycle(b)
+    assert np.abs(got - want).max() <= 1e-11 * np.abs(want).max()
+
+
+def test_bicgstab_amg_nonsymmetric_matches_oracle(cuda):
+    """BiCGStab + AMG with the LU coarse solve (test/aux/iterative.hpp:175-181
+    runs this combination)."""
+    ref = _convdiff()
+    m = cuda.CsrMatrix.from_host(ref.rowptr, ref.col, ref.val, symmetric=False)
+    h = cuda.HierarchyWright(**PARAMS).instantiate(m)
+    oh = lo.Amg(ref, smoother_parts=0, **PARAMS)
+    b = np.random.default_rng(5).uniform(-1, 1, ref.n)
+    res = cuda.pbicgstab(m, b, precon=cuda.PRECON_AMG, amg=h, rtol=1e-8, maxit=300)
+    _, it, _ = lo.pbicgstab(ref, b, precon=lo.PRECON_AMG, amg=oh, rtol=1e-8, maxit=300)
+    assert abs(res.iterations - it) <= max(1, int(0.05 * it + 0.999))
+    x = res.x.cpu().numpy()
+    assert np.linalg.norm(b - lo.spmv(ref, x)) <= 1.01e-8 * np.linalg.norm(b)

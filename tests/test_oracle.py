@@ -226,3 +226,41 @@ def test_amg_pcg_27pt_converges():
     x, it, hist = lo.pcg(a, b, precon=lo.PRECON_AMG, amg=amg, rtol=1e-8, maxit=200)
     assert hist[-1] <= 1e-8 * hist[0]
     assert it < 60
+
+
+def test_lu_factor_solves_nonsymmetric():
+    """Unpivoted row-wise LU (lu/decomposition.hpp) of a nonsymmetric,
+    diagonally dominant sparse matrix against a dense solve; the factors
+    reproduce A."""
+    rng = np.random.default_rng(7)
+    n = 60
+    dense = np.where(rng.random((n, n)) < 0.1, rng.uniform(-1, 1, (n, n)), 0.0)
+    dense += np.diag(np.abs(dense).sum(axis=1) + 1.0)
+    rowptr = np.concatenate([[0], np.cumsum((dense != 0).sum(axis=1))]).astype(np.int64)
+    col = np.concatenate([np.flatnonzero(r) for r in dense]).astype(np.int32)
+    val = dense[dense != 0]
+    a = lo.Csr(rowptr, col, val, symmetric=False)
+    lu = lo.lu_factor(a)
+    lower = np.tril(lu, -1) + np.eye(n)
+    upper = np.triu(lu)
+    assert np.abs(lower @ upper - dense).max() <= 1e-13 * np.abs(dense).max()
+    b = rng.uniform(-1, 1, n)
+    np.testing.assert_allclose(lo.lu_solve(lu, b), np.linalg.solve(dense, b), rtol=1e-12,
+                               atol=1e-14)
+
+
+def test_amg_bicgstab_nonsymmetric_uses_lu():
+    """BiCGStab + AMG on an upwind convection-diffusion operator (values and
+    coarse operators nonsymmetric): the coarsest level is solved by LU, and
+    the solve reaches its tolerance (test/aux/iterative.hpp:175-181 runs
+    this combination)."""
+    a = lo.gen_convdiff((14, 13, 12), (8.0, -5.0, 3.0))
+    dense = np.zeros((a.n, a.n))
+    for i in range(a.n):
+        dense[i, a.col[a.rowptr[i]:a.rowptr[i + 1]]] = a.val[a.rowptr[i]:a.rowptr[i + 1]]
+    assert np.abs(dense - dense.T).max() > 0.1  # nonsymmetric values
+    amg = lo.Amg(a, min_coarsen_size=64, partition_size=512)
+    b = np.random.default_rng(3).uniform(-1, 1, a.n)
+    x, it, hist = lo.pbicgstab(a, b, precon=lo.PRECON_AMG, amg=amg, rtol=1e-8, maxit=300)
+    assert hist[-1] <= 1e-8 * hist[0] and it < 60
+    assert np.linalg.norm(b - dense @ x) <= 1.01e-8 * np.linalg.norm(b)
