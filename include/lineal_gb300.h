@@ -126,6 +126,19 @@ lgx_status lgx_diagonal(const lgx_matrix *a, double *d_diag, lgx_stream stream);
 /* Right-hand side of a stencil system (AdjacentStencilVector,
  * stencil/vector/shared.hpp:181-205). */
 lgx_status lgx_stencil_rhs(const lgx_matrix *a, double *d_b, lgx_stream stream);
+/* Effective diffusivity of a solution (EffDiffCalc, component-wise/sink/
+ * effective-diffusion.hpp:226-320): through the middle planes of axis 0,
+ *   area_part = (filled cells of planes n0/2 and n0/2 + 1) / (n1 n2) / 2,
+ *   eff = sum hm(c1, c2) (x(c2) - x(c1)) q0 / (area_part L1 L2) L0 / (u_end - u_start),
+ * hm the harmonic mean of the two cells' coefficients; lengths = the axis
+ * lengths L; none_materials flags "none" materials (bit m; lookup stencils;
+ * every cell of a value stencil is filled); d_compress_map (may be NULL)
+ * maps cells to the solution rows of a compressed system (-1: no row).
+ * Synchronises `stream`; results on the host. */
+lgx_status lgx_stencil_effective_diffusion(const lgx_matrix *a, const double lengths[3],
+                                           uint8_t none_materials, const double *d_sol,
+                                           const int64_t *d_compress_map, lgx_stream stream,
+                                           double *h_eff, double *h_area_part);
 /* Assembles a stencil matrix as CSR (csr_from_adjacent_stencil,
  * csr/create-from.hpp:37-246); zero off-diagonals are dropped.  With
  * zero_to_one == 0, rows with a zero diagonal are removed and d_compress_map

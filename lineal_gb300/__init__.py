@@ -159,6 +159,7 @@ def _signatures(L):
         "lgx_residual": [V, V, V, V, V, V],
         "lgx_diagonal": [V, V, V],
         "lgx_stencil_rhs": [V, V, V],
+        "lgx_stencil_effective_diffusion": [V, V, C.c_uint8, V, V, V, P(D), P(D)],
         "lgx_stencil_to_csr": [V, V, V, P(V)],
         "lgx_gen_27pt": [V, V, C.c_int, V, P(V)],
         "lgx_gen_7pt": [V, V, C.c_int, V, P(V)],
@@ -385,6 +386,19 @@ class StencilMatrix(_Matrix):
         b = _empty(self.row_num())
         _check(lib().lgx_stencil_rhs(self._h, _ptr(b), _stream()))
         return b
+
+    def effective_diffusion(self, lengths, sol, compress_map=None, none_mask=0):
+        """EffDiffCalc: (effective diffusivity, area part) of the solution
+        `sol` (with `compress_map` for a compressed system)."""
+        torch = _torch()
+        le = np.ascontiguousarray(lengths, dtype=np.float64)
+        x = _dvec(sol)
+        cm = _dvec(compress_map, torch.int64) if compress_map is not None else None
+        eff, ap = C.c_double(), C.c_double()
+        _check(lib().lgx_stencil_effective_diffusion(self._h, _ptr(le), int(none_mask), _ptr(x),
+                                                     _ptr(cm), _stream(), C.byref(eff),
+                                                     C.byref(ap)))
+        return eff.value, ap.value
 
     def to_csr(self, with_compress_map=False):
         torch = _torch()

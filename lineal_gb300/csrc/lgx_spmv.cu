@@ -482,6 +482,57 @@ __global__ void __launch_bounds__(kStPlaneThreads)
   }
 }
 
+// EffDiffCalc (component-wise/sink/effective-diffusion.hpp:226-320) over the
+// middle planes of the flow axis: one CTA, each thread sums its cells of
+// plane mid in order (stride 1024), then a fixed tree: out[0] = flux
+// sum hm(c1, c2) (x(c2) - x(c1)), out[1] = filled-cell count (AreaPartSink)
+constexpr int kEffThreads = 1024;
+__global__ void __launch_bounds__(kEffThreads)
+  k_st_effdiff(int64_t other, int64_t base, const uint8_t *__restrict__ mat,
+               const double *__restrict__ k, double c0, double c1, double c2, double c3,
+               unsigned none_mask, const double *__restrict__ sol,
+               const int64_t *__restrict__ cmap, double *out) {
+  __shared__ double shf[kEffThreads];
+  __shared__ double shn[kEffThreads];
+  const int t = threadIdx.x;
+  double flux = 0.0, filled = 0.0;
+  for (int64_t c = t; c < other; c += kEffThreads) {
+    const int64_t i1 = base + c, i2 = i1 + other;
+    double v1, v2;
+    if (mat) {
+      const unsigned m1 = mat[i1], m2 = mat[i2];
+      filled += (double)(((none_mask >> m1) & 1u) == 0u) + (double)(((none_mask >> m2) & 1u) == 0u);
+      v1 = m1 == 0 ? c0 : m1 == 1 ? c1 : m1 == 2 ? c2 : c3;
+      v2 = m2 == 0 ? c0 : m2 == 1 ? c1 : m2 == 2 ? c2 : c3;
+    } else {
+      filled += 2.0;
+      v1 = k[i1];
+      v2 = k[i2];
+    }
+    const double hm = hm_dev(v1, v2);
+    if (cmap) {
+      const int64_t k1 = cmap[i1], k2 = cmap[i2];
+      if (k1 >= 0 && k2 >= 0) flux = fma(hm, sol[k2] - sol[k1], flux);
+    } else {
+      flux = fma(hm, sol[i2] - sol[i1], flux);
+    }
+  }
+  shf[t] = flux;
+  shn[t] = filled;
+  __syncthreads();
+  for (int h = kEffThreads / 2; h > 0; h >>= 1) {
+    if (t < h) {
+      shf[t] += shf[t + h];
+      shn[t] += shn[t + h];
+    }
+    __syncthreads();
+  }
+  if (t == 0) {
+    out[0] = shf[0];
+    out[1] = shn[0];
+  }
+}
+
 static dim3 st_grid(const StencilDesc &st) {
   return dim3((unsigned)((st.dims[2] + 31) / 32), (unsigned)((st.dims[1] + 7) / 8),
               (unsigned)st.dims[0]);
@@ -922,6 +973,37 @@ lgx_status lgx_diagonal(const lgx_matrix *a, double *d_diag, lgx_stream stream) 
   LGX_CHECK(matrix_diagonal(const_cast<lgx_matrix *>(a), stream, &d));
   if (a->n)
     LGX_CUDA(cudaMemcpyAsync(d_diag, d, sizeof(double) * a->n, cudaMemcpyDeviceToDevice, stream));
+  return LGX_OK;
+}
+
+lgx_status lgx_stencil_effective_diffusion(const lgx_matrix *a, const double lengths[3],
+                                           uint8_t none_materials, const double *d_sol,
+                                           const int64_t *d_compress_map, lgx_stream stream,
+                                           double *h_eff, double *h_area_part) {
+  if (!a || !lengths || !d_sol || !h_eff) return fail(LGX_ERR_INVALID, "null argument");
+  if (a->kind == LGX_MATRIX_CSR) return fail(LGX_ERR_UNSUPPORTED, "not a stencil matrix");
+  const StencilDesc &st = a->st;
+  if (st.dims[0] < 2) return fail(LGX_ERR_INVALID, "the flow axis needs two planes");
+  const int64_t other = st.dims[1] * st.dims[2], mid = st.dims[0] / 2;
+  DBuf<double> out;
+  LGX_CHECK(out.alloc(2));
+  const cudaStream_t s = (cudaStream_t)stream;
+  k_st_effdiff<<<1, kEffThreads, 0, s>>>(other, mid * other, st.lookup ? a->mat.p : nullptr,
+                                         st.lookup ? nullptr : a->k.p, st.coeffs[0],
+                                         st.coeffs[1], st.coeffs[2], st.coeffs[3],
+                                         (unsigned)none_materials, d_sol, d_compress_map, out.p);
+  LGX_LAUNCH_CHECK();
+  count_launch();
+  double h[2] = {0.0, 0.0};
+  LGX_CUDA(cudaMemcpyAsync(h, out.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+  LGX_CUDA(cudaStreamSynchronize(s));
+  const double area_part = h[1] / (double)other * 0.5;
+  double eff = h[0];
+  eff *= st.q[0];
+  eff /= area_part * (lengths[1] * lengths[2]);
+  eff *= lengths[0];
+  *h_eff = eff / (st.sol_end - st.sol_start);
+  if (h_area_part) *h_area_part = area_part;
   return LGX_OK;
 }
 

@@ -165,6 +165,9 @@ def _setup_signatures(L):
     L.lo_cholesky_factor.restype = C.c_int
     L.lo_cholesky_factor.argtypes = [P(_Csr), C.c_void_p]
     L.lo_cholesky_solve.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.lo_effective_diffusion.restype = C.c_double
+    L.lo_effective_diffusion.argtypes = [P(_Stencil), C.c_void_p, C.c_uint8, C.c_void_p,
+                                         C.c_void_p, P(C.c_double)]
     L.lo_lu_factor.restype = C.c_int
     L.lo_lu_factor.argtypes = [P(_Csr), C.c_void_p]
     L.lo_lu_solve.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -318,6 +321,16 @@ class Stencil:
         b = np.empty(self.n)
         lib().lo_stencil_rhs(C.byref(self._s), _ptr(b))
         return b
+
+    def effective_diffusion(self, lengths, sol, compress_map=None, none_mask=0):
+        """EffDiffCalc: (effective diffusivity, area part) of `sol`."""
+        le = np.ascontiguousarray(lengths, dtype=np.float64)
+        x = np.ascontiguousarray(sol, dtype=np.float64)
+        cm = None if compress_map is None else np.ascontiguousarray(compress_map, np.int64)
+        ap = C.c_double()
+        eff = lib().lo_effective_diffusion(C.byref(self._s), _ptr(le), int(none_mask), _ptr(x),
+                                           None if cm is None else _ptr(cm), C.byref(ap))
+        return float(eff), float(ap.value)
 
     def to_csr(self):
         L = lib()

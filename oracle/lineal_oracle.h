@@ -81,6 +81,14 @@ typedef struct {
 } lo_stencil;
 
 void lo_stencil_init(lo_stencil *s);
+/* EffDiffCalc (component-wise/sink/effective-diffusion.hpp:226-320): the
+ * effective diffusivity of a solution through the middle planes of axis 0;
+ * lengths are the axis lengths, none_mask flags "none" materials (bit m),
+ * compress_map (NULL: identity) maps cells to solution rows (-1: removed).
+ * *area_part (may be NULL) receives AreaPartSink's value. */
+double lo_effective_diffusion(const lo_stencil *s, const double lengths[3], uint8_t none_mask,
+                              const double *sol, const int64_t *compress_map,
+                              double *area_part);
 /* y = A x, products accumulated with fma in the scalar unordered order:
  * before (dims 0,1,2), after (dims 2,1,0), diagonal
  * (matrix-vector-product.hpp:71-82 applied to algorithm.hpp:178-225). */

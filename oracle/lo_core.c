@@ -176,6 +176,50 @@ void lo_stencil_rhs(const lo_stencil *s, double *b) {
   }
 }
 
+/* EffDiffCalc (component-wise/sink/effective-diffusion.hpp:226-320) on the
+ * two middle planes of the flow axis (cells of plane mid = n0 / 2 and their
+ * neighbours in plane mid + 1):
+ *   area_part = sum(filled(c1) + filled(c2)) / (n1 n2) / 2      (AreaPartSink)
+ *   flux      = sum hm(c1, c2) (x(c2) - x(c1))                   (EffDiffSink)
+ *   eff       = flux q0 / (area_part L1 L2) L0 / (u_end - u_start)
+ * with hm the harmonic mean of the two cells' coefficients (the lookup or
+ * value valuator's diffusion_coeff), filled(c) = 0 for materials flagged in
+ * none_mask (lookup valuator; every cell is filled for the value valuator)
+ * and, with a compress map, only pairs whose cells both have a row.  Sums
+ * run in cell order. */
+double lo_effective_diffusion(const lo_stencil *s, const double lengths[3], uint8_t none_mask,
+                              const double *sol, const int64_t *compress_map,
+                              double *area_part) {
+  const int64_t n1 = s->dims[1], n2 = s->dims[2], other = n1 * n2;
+  const int64_t mid = s->dims[0] / 2;
+  int64_t filled = 0;
+  double flux = 0.0;
+  for (int64_t c = 0; c < other; ++c) {
+    const int64_t i1 = mid * other + c, i2 = i1 + other;
+    if (s->mat) {
+      filled += !((none_mask >> s->mat[i1]) & 1u);
+      filled += !((none_mask >> s->mat[i2]) & 1u);
+    } else {
+      filled += 2;
+    }
+    const double c1 = st_cell_value(s, i1), c2 = st_cell_value(s, i2);
+    const double hm = lo_harmonic_mean(c1, c2);
+    if (compress_map) {
+      const int64_t k1 = compress_map[i1], k2 = compress_map[i2];
+      if (k1 >= 0 && k2 >= 0) flux += hm * (sol[k2] - sol[k1]);
+    } else {
+      flux += hm * (sol[i2] - sol[i1]);
+    }
+  }
+  const double ap = (double)filled / (double)other * 0.5;
+  if (area_part) *area_part = ap;
+  double out = flux;
+  out *= s->q[0];
+  out /= ap * (lengths[1] * lengths[2]);
+  out *= lengths[0];
+  return out / (s->sol_end - s->sol_start);
+}
+
 /* csr/create-from.hpp:82-232: rows of the stencil matrix with zero
  * off-diagonals dropped and sorted columns; with ZeroToZero valuators rows
  * whose diagonal is 0 are removed (compress map). */

@@ -179,3 +179,39 @@ def test_invalid_csr_rejected(cuda):
         cuda.CsrMatrix.from_host(np.array([0, 1, 2]), np.array([1, 0]), np.array([1.0, 1.0]))
     with pytest.raises(cuda.LinealError):
         cuda.CsrMatrix.from_host(np.array([0, 2]), np.array([0, 0]), np.array([1.0, 1.0]))
+
+
+def _diagonal_lines(dims):
+    i, j, k = np.meshgrid(*[np.arange(d) for d in dims], indexing="ij")
+    return ((j + k) % 4).ravel().astype(np.uint8)
+
+
+@pytest.mark.parametrize("zero_to_one", [True, False])
+def test_effective_diffusion_matches_oracle(cuda, zero_to_one):
+    """EffDiffCalc on the reference suite's system (test/shared-stencil.hpp:
+    69-104, 225-238): the cross-section mean of the coefficients
+    (materials.hpp:236-250), on the stencil (ZeroToOne) or on the
+    compressed CSR system (ZeroToZero, compress map)."""
+    dims, coeffs, lengths = (4, 9, 7), (0.0, 1.0, 2.0, 3.0), (4.0, 9.0, 7.0)
+    q = lo.axis_quotients(dims, lengths)
+    mat = _diagonal_lines(dims)
+    st = cuda.StencilMatrix.lookup(dims, q, coeffs, mat, 1.0, 0.0, zero_to_one)
+    ref = lo.Stencil(dims, q=q, mat=mat, coeffs=coeffs, sol_start=1.0, sol_end=0.0,
+                     zero_to_one=zero_to_one)
+    if zero_to_one:
+        res = cuda.pcg(st, st.rhs(), precon=cuda.PRECON_JACOBI, rtol=1e-14, maxit=2000)
+        cmap = None
+    else:
+        csr, cmap = st.to_csr(with_compress_map=True)
+        rhs = st.rhs()[cmap >= 0]
+        res = cuda.pcg(csr, rhs, precon=cuda.PRECON_JACOBI, rtol=1e-14, maxit=2000)
+    eff, area = st.effective_diffusion(lengths, res.x, compress_map=cmap)
+    j, k = np.meshgrid(np.arange(9), np.arange(7), indexing="ij")
+    assert area == 1.0
+    assert abs(eff - np.mean(np.asarray(coeffs)[(j + k) % 4])) <= 1e-12
+    want, want_area = ref.effective_diffusion(
+        lengths, res.x.cpu().numpy(), None if cmap is None else cmap.cpu().numpy())
+    assert area == want_area and abs(eff - want) <= 1e-13 * abs(want)
+    # a "none" material leaves the area part
+    eff0, area0 = st.effective_diffusion(lengths, res.x, compress_map=cmap, none_mask=1)
+    assert area0 == pytest.approx(1.0 - np.mean((j + k) % 4 == 0))

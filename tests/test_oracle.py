@@ -264,3 +264,31 @@ def test_amg_bicgstab_nonsymmetric_uses_lu():
     x, it, hist = lo.pbicgstab(a, b, precon=lo.PRECON_AMG, amg=amg, rtol=1e-8, maxit=300)
     assert hist[-1] <= 1e-8 * hist[0] and it < 60
     assert np.linalg.norm(b - dense @ x) <= 1.01e-8 * np.linalg.norm(b)
+
+
+def _diagonal_lines(dims):
+    # test/aux/materials.hpp:214-232: material (j + k) mod 4, constant along
+    # the flow axis
+    i, j, k = np.meshgrid(*[np.arange(d) for d in dims], indexing="ij")
+    return ((j + k) % 4).ravel().astype(np.uint8)
+
+
+def test_effective_diffusion_diagonal_lines():
+    """EffDiffCalc on the reference suite's system (test/shared-stencil.hpp:
+    69-104, 225-238): materials constant along the flow axis give the
+    cross-section mean of the coefficients (materials.hpp:236-250)."""
+    dims, coeffs, lengths = (4, 9, 7), (0.0, 1.0, 2.0, 3.0), (4.0, 9.0, 7.0)
+    mat = _diagonal_lines(dims)
+    st = lo.Stencil(dims, q=lo.axis_quotients(dims, lengths), mat=mat, coeffs=coeffs,
+                    sol_start=1.0, sol_end=0.0)
+    a, _ = st.to_csr()
+    x, it, hist = lo.pcg(a, st.rhs(), precon=lo.PRECON_JACOBI, rtol=1e-14, maxit=1000)
+    eff, area = st.effective_diffusion(lengths, x)
+    j, k = np.meshgrid(np.arange(9), np.arange(7), indexing="ij")
+    want = np.mean(np.asarray(coeffs)[(j + k) % 4])
+    assert area == 1.0
+    assert abs(eff - want) <= 1e-12
+    # "none" materials leave the area part, not the flux
+    eff0, area0 = st.effective_diffusion(lengths, x, none_mask=0b0001)
+    assert area0 == pytest.approx(1.0 - np.mean((j + k) % 4 == 0))
+    assert eff0 == pytest.approx(eff / area0, rel=1e-13)
