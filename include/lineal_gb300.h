@@ -101,6 +101,16 @@ lgx_status lgx_stencil_create_lookup(const int64_t dims[3], const double q[3],
 lgx_status lgx_stencil_create_value(const int64_t dims[3], const double q[3], const double *d_k,
                                     double sol_start, double sol_end, int zero_to_one,
                                     lgx_stream stream, lgx_matrix **out);
+/* StationaryDiffusionValuesValuator (stencil/valuator/stationary-diffusion-
+ * values.hpp:30-211): a conductivity per cell and axis; the connection along
+ * axis d is hm(k_d(from), k_d(to)) * q_d and the Dirichlet terms of axis 0
+ * use k_0.  Same kernels and layout as the value valuator (matrix kind
+ * LGX_MATRIX_STENCIL_VALUE); no effective diffusion (the reference valuator
+ * has no diffusion coefficient). */
+lgx_status lgx_stencil_create_values(const int64_t dims[3], const double q[3], const double *d_k0,
+                                     const double *d_k1, const double *d_k2, double sol_start,
+                                     double sol_end, int zero_to_one, lgx_stream stream,
+                                     lgx_matrix **out);
 
 lgx_status lgx_matrix_destroy(lgx_matrix *a);
 /* kind, rows, stored non-zeros (stencils: the non-zeros of the assembled

@@ -152,6 +152,7 @@ def _signatures(L):
         "lgx_csr_download": [V, V, V, V, V],
         "lgx_stencil_create_lookup": [V, V, V, V, D, D, C.c_int, V, P(V)],
         "lgx_stencil_create_value": [V, V, V, D, D, C.c_int, V, P(V)],
+        "lgx_stencil_create_values": [V, V, V, V, V, D, D, C.c_int, V, P(V)],
         "lgx_matrix_destroy": [V],
         "lgx_matrix_info": [V, P(C.c_int), P(I64), P(I64), P(C.c_int)],
         "lgx_spmv": [V, V, V, V],
@@ -380,6 +381,19 @@ class StencilMatrix(_Matrix):
         h = C.c_void_p()
         _check(lib().lgx_stencil_create_value(_ptr(d), _ptr(qq), _ptr(kk), sol_start, sol_end,
                                               int(zero_to_one), _stream(), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def values(cls, dims, q, k_axes, sol_start=1.0, sol_end=0.0,
+               zero_to_one=True) -> "StencilMatrix":
+        """StationaryDiffusionValuesValuator: one conductivity array per axis."""
+        d = np.ascontiguousarray(dims, dtype=np.int64)
+        qq = np.ascontiguousarray(q, dtype=np.float64)
+        k0, k1, k2 = (_dvec(v) for v in k_axes)
+        h = C.c_void_p()
+        _check(lib().lgx_stencil_create_values(_ptr(d), _ptr(qq), _ptr(k0), _ptr(k1), _ptr(k2),
+                                               sol_start, sol_end, int(zero_to_one), _stream(),
+                                               C.byref(h)))
         return cls(h)
 
     def rhs(self):

@@ -156,6 +156,7 @@ struct StencilDesc {
   double sol_start, sol_end;
   int zero_to_one;
   int lookup;
+  int values;  // values valuator: a conductivity per cell and axis
   const uint8_t *mat;
   const double *k;
 };
@@ -300,7 +301,10 @@ lgx_status csr_alloc_arrays(Csr &a, int64_t nnz, lgx_dtype storage);
 // partial-sum slots needed by the fused reductions of the row-block kernels
 int64_t csr_partials(int64_t n);
 int64_t matrix_partials(const lgx_matrix *a);
-lgx_status stencil_ensure(lgx_matrix *a, cudaStream_t s);
+// faces (value kinds) and the cached diagonal; k1/k2: the axis-1/2
+// conductivities of a values stencil, read by the first call only
+lgx_status stencil_ensure(lgx_matrix *a, cudaStream_t s, const double *k1 = nullptr,
+                          const double *k2 = nullptr);
 
 // ---- programmatic dependent launch ---------------------------------------
 // Kernels of the solve chains are launched with the programmatic-stream-

@@ -195,18 +195,20 @@ __device__ __forceinline__ double hm_dev(double a, double b) {
 }
 
 // value valuator faces: face_d[i] = hm(k_i, k_{i+stride_d}) * q_d
-__global__ void k_st_faces(int n0, int n1, int n2, const double *k, double q0, double q1, double q2,
-                           double *f0, double *f1, double *f2) {
+// k0/k1/k2: the conductivities of axes 0/1/2 (all k for the value valuator;
+// one array per axis for the values valuator)
+__global__ void k_st_faces(int n0, int n1, int n2, const double *k0, const double *k1,
+                           const double *k2, double q0, double q1, double q2, double *f0,
+                           double *f1, double *f2) {
   const int p2 = blockIdx.x * blockDim.x + threadIdx.x;
   const int p1 = blockIdx.y * blockDim.y + threadIdx.y;
   const int p0 = blockIdx.z;
   if (p2 >= n2 || p1 >= n1) return;
   const int64_t s0 = (int64_t)n1 * n2;
   const int64_t i = (int64_t)p0 * s0 + (int64_t)p1 * n2 + p2;
-  const double ki = k[i];
-  f0[i] = p0 + 1 < n0 ? __dmul_rn(hm_dev(ki, k[i + s0]), q0) : 0.0;
-  f1[i] = p1 + 1 < n1 ? __dmul_rn(hm_dev(ki, k[i + n2]), q1) : 0.0;
-  f2[i] = p2 + 1 < n2 ? __dmul_rn(hm_dev(ki, k[i + 1]), q2) : 0.0;
+  f0[i] = p0 + 1 < n0 ? __dmul_rn(hm_dev(k0[i], k0[i + s0]), q0) : 0.0;
+  f1[i] = p1 + 1 < n1 ? __dmul_rn(hm_dev(k1[i], k1[i + n2]), q1) : 0.0;
+  f2[i] = p2 + 1 < n2 ? __dmul_rn(hm_dev(k2[i], k2[i + 1]), q2) : 0.0;
 }
 
 template <bool LOOKUP>
@@ -570,16 +572,16 @@ static StencilDev dev_of(const lgx_matrix *a) {
   return S;
 }
 
-lgx_status stencil_ensure(lgx_matrix *a, cudaStream_t s) {
+lgx_status stencil_ensure(lgx_matrix *a, cudaStream_t s, const double *k1, const double *k2) {
   if (a->diag.p) return LGX_OK;
   const StencilDesc &st = a->st;
   const int64_t n = a->n;
   if (!st.lookup) {
     // faces into k buffer slots 1..3
     double *base = a->k.p;
-    k_st_faces<<<st_grid(st), kStBlock, 0, s>>>((int)st.dims[0], (int)st.dims[1],
-                                                (int)st.dims[2], base, st.q[0], st.q[1], st.q[2],
-                                                base + n, base + 2 * n, base + 3 * n);
+    k_st_faces<<<st_grid(st), kStBlock, 0, s>>>(
+      (int)st.dims[0], (int)st.dims[1], (int)st.dims[2], base, k1 ? k1 : base, k2 ? k2 : base,
+      st.q[0], st.q[1], st.q[2], base + n, base + 2 * n, base + 3 * n);
     LGX_LAUNCH_CHECK();
   }
   DBuf<double> cellv;
@@ -861,7 +863,8 @@ extern "C" {
 static lgx_status stencil_create(const int64_t dims[3], const double q[3], const double coeffs[4],
                                  const uint8_t *d_mat, const double *d_k, double sol_start,
                                  double sol_end, int zero_to_one, lgx_stream stream,
-                                 lgx_matrix **out) {
+                                 lgx_matrix **out, const double *d_k1 = nullptr,
+                                 const double *d_k2 = nullptr) {
   if (!dims || !q || !out) return fail(LGX_ERR_INVALID, "null argument");
   if (dims[0] < 1 || dims[1] < 1 || dims[2] < 1)
     return fail(LGX_ERR_INVALID, "grid dimensions must be positive");
@@ -881,6 +884,7 @@ static lgx_status stencil_create(const int64_t dims[3], const double q[3], const
   st.sol_end = sol_end;
   st.zero_to_one = zero_to_one;
   st.lookup = d_mat != nullptr;
+  st.values = d_k1 != nullptr;
   lgx_status s = LGX_OK;
   if (d_mat) {
     for (int c = 0; c < 4; ++c) st.coeffs[c] = coeffs[c];
@@ -902,7 +906,7 @@ static lgx_status stencil_create(const int64_t dims[3], const double q[3], const
                                        stream) != cudaSuccess)
       s = fail(LGX_ERR_CUDA, "copying conductivities failed");
   }
-  if (s == LGX_OK) s = stencil_ensure(m, stream);
+  if (s == LGX_OK) s = stencil_ensure(m, stream, d_k1, d_k2);
   if (s != LGX_OK) {
     delete m;
     return s;
@@ -930,6 +934,15 @@ lgx_status lgx_stencil_create_value(const int64_t dims[3], const double q[3], co
   if (!d_k) return fail(LGX_ERR_INVALID, "null conductivities");
   return stencil_create(dims, q, nullptr, nullptr, d_k, sol_start, sol_end, zero_to_one, stream,
                         out);
+}
+
+lgx_status lgx_stencil_create_values(const int64_t dims[3], const double q[3], const double *d_k0,
+                                     const double *d_k1, const double *d_k2, double sol_start,
+                                     double sol_end, int zero_to_one, lgx_stream stream,
+                                     lgx_matrix **out) {
+  if (!d_k0 || !d_k1 || !d_k2) return fail(LGX_ERR_INVALID, "null conductivities");
+  return stencil_create(dims, q, nullptr, nullptr, d_k0, sol_start, sol_end, zero_to_one, stream,
+                        out, d_k1, d_k2);
 }
 
 lgx_status lgx_stencil_engine_set(int engine) {
@@ -983,6 +996,8 @@ lgx_status lgx_stencil_effective_diffusion(const lgx_matrix *a, const double len
   if (!a || !lengths || !d_sol || !h_eff) return fail(LGX_ERR_INVALID, "null argument");
   if (a->kind == LGX_MATRIX_CSR) return fail(LGX_ERR_UNSUPPORTED, "not a stencil matrix");
   const StencilDesc &st = a->st;
+  if (st.values)
+    return fail(LGX_ERR_UNSUPPORTED, "the values valuator has no diffusion coefficient");
   if (st.dims[0] < 2) return fail(LGX_ERR_INVALID, "the flow axis needs two planes");
   const int64_t other = st.dims[1] * st.dims[2], mid = st.dims[0] / 2;
   DBuf<double> out;

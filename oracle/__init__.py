@@ -65,6 +65,8 @@ class _Stencil(C.Structure):
         ("sol_start", C.c_double),
         ("sol_end", C.c_double),
         ("zero_to_one", C.c_int),
+        ("k1", C.POINTER(C.c_double)),
+        ("k2", C.POINTER(C.c_double)),
     ]
 
 
@@ -283,13 +285,18 @@ def material_flow_cylinder_gap(dims, radius: float) -> np.ndarray:
 
 class Stencil:
     """7-point diffusion stencil matrix (lookup valuator when ``k`` is None,
-    value valuator otherwise)."""
+    value valuator otherwise; values valuator with ``k_axes``, one
+    conductivity array per axis)."""
 
     def __init__(self, dims, q=(1.0, 1.0, 1.0), mat=None, coeffs=(0.0, 1.0, 2.0, 3.0), k=None,
-                 sol_start=1.0, sol_end=0.0, zero_to_one=True):
+                 sol_start=1.0, sol_end=0.0, zero_to_one=True, k_axes=None):
         self.dims = tuple(int(v) for v in dims)
         self.n = int(np.prod(self.dims))
         self._mat = None if mat is None else np.ascontiguousarray(mat, dtype=np.uint8)
+        self._kax = None
+        if k_axes is not None:
+            self._kax = [np.ascontiguousarray(v, dtype=np.float64) for v in k_axes]
+            k = self._kax[0]
         self._k = None if k is None else np.ascontiguousarray(k, dtype=np.float64)
         s = _Stencil()
         for i in range(3):
@@ -302,6 +309,9 @@ class Stencil:
         s.sol_start = sol_start
         s.sol_end = sol_end
         s.zero_to_one = int(zero_to_one)
+        if self._kax is not None:
+            s.k1 = self._kax[1].ctypes.data_as(C.POINTER(C.c_double))
+            s.k2 = self._kax[2].ctypes.data_as(C.POINTER(C.c_double))
         lib().lo_stencil_init(C.byref(s))
         self._s = s
         self.conn = np.array(s.conn[:])

@@ -78,6 +78,10 @@ typedef struct {
   double conn[48];        /* lookup tables (filled by lo_stencil_init) */
   double sol_start, sol_end;
   int zero_to_one;
+  /* values valuator (stationary-diffusion-values.hpp:30-211): conductivity
+   * per cell and axis, k for axis 0 (and the Dirichlet borders), k1 and k2
+   * for axes 1 and 2; NULL: the value valuator's single k */
+  const double *k1, *k2;
 } lo_stencil;
 
 void lo_stencil_init(lo_stencil *s);

@@ -91,9 +91,13 @@ void lo_stencil_init(lo_stencil *s) {
 static inline double st_cell_value(const lo_stencil *s, int64_t i) {
   return s->k ? s->k[i] : s->coeffs[s->mat[i]];
 }
-/* connection_value (lookup: table gather; value: hm(k_from, k_to) * q_d) */
+/* connection_value (lookup: table gather; value: hm(k_from, k_to) * q_d;
+ * values: the same with the conductivities of axis d) */
 static inline double st_conn(const lo_stencil *s, int d, int64_t from, int64_t to) {
-  if (s->k) return lo_harmonic_mean(s->k[from], s->k[to]) * s->q[d];
+  if (s->k) {
+    const double *kd = d == 1 && s->k1 ? s->k1 : d == 2 && s->k2 ? s->k2 : s->k;
+    return lo_harmonic_mean(kd[from], kd[to]) * s->q[d];
+  }
   return s->conn[d * 16 + s->mat[from] * 4 + s->mat[to]];
 }
 

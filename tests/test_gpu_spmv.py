@@ -215,3 +215,25 @@ def test_effective_diffusion_matches_oracle(cuda, zero_to_one):
     # a "none" material leaves the area part
     eff0, area0 = st.effective_diffusion(lengths, res.x, compress_map=cmap, none_mask=1)
     assert area0 == pytest.approx(1.0 - np.mean((j + k) % 4 == 0))
+
+
+def test_stencil_values_bitexact(cuda, stencil_engine):
+    dims = (6, 7, 10)
+    n = int(np.prod(dims))
+    rng = np.random.default_rng(22)
+    ks = [np.exp(rng.standard_normal(n)) for _ in range(3)]
+    q = lo.axis_quotients(dims, (1.5, 0.7, 2.0))
+    ref = lo.Stencil(dims, q=q, k_axes=ks, sol_start=1.0, sol_end=0.25)
+    m = cuda.StencilMatrix.values(dims, q, ks, 1.0, 0.25)
+    x = rng.uniform(-1, 1, n)
+    np.testing.assert_array_equal(cuda.spmv(m, x).cpu().numpy(), ref.spmv(x))
+    np.testing.assert_array_equal(m.diagonal().cpu().numpy(), ref.diagonal())
+    np.testing.assert_array_equal(m.rhs().cpu().numpy(), ref.rhs())
+    csr, _ = m.to_csr(with_compress_map=True)
+    rcsr, _ = ref.to_csr()
+    rowptr, col, val = csr.download()
+    np.testing.assert_array_equal(rowptr, rcsr.rowptr)
+    np.testing.assert_array_equal(col, rcsr.col)
+    np.testing.assert_array_equal(val, rcsr.val)
+    with pytest.raises(cuda.LinealError):
+        m.effective_diffusion((6.0, 7.0, 10.0), x)

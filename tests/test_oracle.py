@@ -292,3 +292,37 @@ def test_effective_diffusion_diagonal_lines():
     eff0, area0 = st.effective_diffusion(lengths, x, none_mask=0b0001)
     assert area0 == pytest.approx(1.0 - np.mean((j + k) % 4 == 0))
     assert eff0 == pytest.approx(eff / area0, rel=1e-13)
+
+
+def test_values_valuator_matches_explicit_operator():
+    """StationaryDiffusionValuesValuator (stationary-diffusion-values.hpp):
+    connections hm(k_d(i), k_d(j)) q_d along axis d, axis-0 Dirichlet terms
+    2 q_0 k_0(i); with equal axes it is the value valuator bit for bit."""
+    dims = (5, 4, 6)
+    n = int(np.prod(dims))
+    rng = np.random.default_rng(21)
+    ks = [np.exp(rng.standard_normal(n)) for _ in range(3)]
+    q = lo.axis_quotients(dims, (1.0, 2.0, 0.5))
+    st = lo.Stencil(dims, q=q, k_axes=ks, sol_start=1.0, sol_end=0.0)
+    same = lo.Stencil(dims, q=q, k_axes=[ks[0]] * 3, sol_start=1.0, sol_end=0.0)
+    val = lo.Stencil(dims, q=q, k=ks[0], sol_start=1.0, sol_end=0.0)
+    x = rng.uniform(-1, 1, n)
+    np.testing.assert_array_equal(same.spmv(x), val.spmv(x))
+    strides = (dims[1] * dims[2], dims[2], 1)
+    dense = np.zeros((n, n))
+    hm = lambda a, b: 2 * a * b / (a + b)  # noqa: E731
+    for i in range(n):
+        pos = np.unravel_index(i, dims)
+        for d in range(3):
+            for s in (-1, 1):
+                p = list(pos)
+                p[d] += s
+                if 0 <= p[d] < dims[d]:
+                    j = i + s * strides[d]
+                    c = hm(ks[d][i], ks[d][j]) * q[d]
+                    dense[i, j] -= c
+                    dense[i, i] += c
+        if pos[0] == 0 or pos[0] == dims[0] - 1:
+            dense[i, i] += 2 * q[0] * ks[0][i] * ((pos[0] == 0) + (pos[0] == dims[0] - 1))
+    np.testing.assert_allclose(st.spmv(x), dense @ x, rtol=1e-13, atol=1e-13)
+    assert not np.allclose(st.spmv(x), val.spmv(x))
