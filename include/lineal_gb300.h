@@ -98,6 +98,15 @@ lgx_status lgx_stencil_create_lookup(const int64_t dims[3], const double q[3],
                                      const double coeffs[4], const uint8_t *d_mat,
                                      double sol_start, double sol_end, int zero_to_one,
                                      lgx_stream stream, lgx_matrix **out);
+/* The lookup valuator with HenryDiffusionLookupProvider (lookup-wright.hpp:
+ * 38-60): the diffusion factor of materials a -> b is hm(c_a f_b, c_b f_a),
+ * f = henry_constant for the materials flagged in gaseous_materials (bit m),
+ * else 1; everything else as lgx_stencil_create_lookup. */
+lgx_status lgx_stencil_create_lookup_henry(const int64_t dims[3], const double q[3],
+                                           const double coeffs[4], uint8_t gaseous_materials,
+                                           double henry_constant, const uint8_t *d_mat,
+                                           double sol_start, double sol_end, int zero_to_one,
+                                           lgx_stream stream, lgx_matrix **out);
 lgx_status lgx_stencil_create_value(const int64_t dims[3], const double q[3], const double *d_k,
                                     double sol_start, double sol_end, int zero_to_one,
                                     lgx_stream stream, lgx_matrix **out);

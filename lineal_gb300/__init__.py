@@ -152,6 +152,7 @@ def _signatures(L):
         "lgx_csr_download": [V, V, V, V, V],
         "lgx_stencil_create_lookup": [V, V, V, V, D, D, C.c_int, V, P(V)],
         "lgx_stencil_create_value": [V, V, V, D, D, C.c_int, V, P(V)],
+        "lgx_stencil_create_lookup_henry": [V, V, V, C.c_uint8, D, V, D, D, C.c_int, V, P(V)],
         "lgx_stencil_create_values": [V, V, V, V, V, D, D, C.c_int, V, P(V)],
         "lgx_matrix_destroy": [V],
         "lgx_matrix_info": [V, P(C.c_int), P(I64), P(I64), P(C.c_int)],
@@ -381,6 +382,21 @@ class StencilMatrix(_Matrix):
         h = C.c_void_p()
         _check(lib().lgx_stencil_create_value(_ptr(d), _ptr(qq), _ptr(kk), sol_start, sol_end,
                                               int(zero_to_one), _stream(), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def lookup_henry(cls, dims, q, coeffs, materials, henry, gaseous_mask, sol_start=1.0,
+                     sol_end=0.0, zero_to_one=True) -> "StencilMatrix":
+        """Lookup valuator with the Henry-law diffusion factors."""
+        torch = _torch()
+        d = np.ascontiguousarray(dims, dtype=np.int64)
+        qq = np.ascontiguousarray(q, dtype=np.float64)
+        cc = np.ascontiguousarray(coeffs, dtype=np.float64)
+        mat = _dvec(materials, torch.uint8)
+        h = C.c_void_p()
+        _check(lib().lgx_stencil_create_lookup_henry(
+            _ptr(d), _ptr(qq), _ptr(cc), int(gaseous_mask), float(henry), _ptr(mat), sol_start,
+            sol_end, int(zero_to_one), _stream(), C.byref(h)))
         return cls(h)
 
     @classmethod

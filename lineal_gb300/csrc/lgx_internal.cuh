@@ -153,6 +153,7 @@ struct StencilDesc {
   double q[3];
   double coeffs[4];
   double conn[48];
+  double dfac[16];  // lookup: diffusion factor of materials a -> b at [4 a + b]
   double sol_start, sol_end;
   int zero_to_one;
   int lookup;

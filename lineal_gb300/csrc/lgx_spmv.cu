@@ -489,29 +489,28 @@ __global__ void __launch_bounds__(kStPlaneThreads)
 // plane mid in order (stride 1024), then a fixed tree: out[0] = flux
 // sum hm(c1, c2) (x(c2) - x(c1)), out[1] = filled-cell count (AreaPartSink)
 constexpr int kEffThreads = 1024;
+struct StDfac {
+  double v[16];
+};
 __global__ void __launch_bounds__(kEffThreads)
   k_st_effdiff(int64_t other, int64_t base, const uint8_t *__restrict__ mat,
-               const double *__restrict__ k, double c0, double c1, double c2, double c3,
-               unsigned none_mask, const double *__restrict__ sol,
-               const int64_t *__restrict__ cmap, double *out) {
+               const double *__restrict__ k, StDfac dfac, unsigned none_mask,
+               const double *__restrict__ sol, const int64_t *__restrict__ cmap, double *out) {
   __shared__ double shf[kEffThreads];
   __shared__ double shn[kEffThreads];
   const int t = threadIdx.x;
   double flux = 0.0, filled = 0.0;
   for (int64_t c = t; c < other; c += kEffThreads) {
     const int64_t i1 = base + c, i2 = i1 + other;
-    double v1, v2;
+    double hm;
     if (mat) {
       const unsigned m1 = mat[i1], m2 = mat[i2];
       filled += (double)(((none_mask >> m1) & 1u) == 0u) + (double)(((none_mask >> m2) & 1u) == 0u);
-      v1 = m1 == 0 ? c0 : m1 == 1 ? c1 : m1 == 2 ? c2 : c3;
-      v2 = m2 == 0 ? c0 : m2 == 1 ? c1 : m2 == 2 ? c2 : c3;
+      hm = dfac.v[m1 * 4 + m2];  // the lookup valuator's diffusion_coeff
     } else {
       filled += 2.0;
-      v1 = k[i1];
-      v2 = k[i2];
+      hm = hm_dev(k[i1], k[i2]);
     }
-    const double hm = hm_dev(v1, v2);
     if (cmap) {
       const int64_t k1 = cmap[i1], k2 = cmap[i2];
       if (k1 >= 0 && k2 >= 0) flux = fma(hm, sol[k2] - sol[k1], flux);
@@ -860,11 +859,14 @@ using namespace lgx;
 
 extern "C" {
 
+// henry < 0: SymmetricDiffusionLookupProvider; else HenryDiffusionLookupProvider
+// with that constant and the gaseous materials in gaseous_mask
 static lgx_status stencil_create(const int64_t dims[3], const double q[3], const double coeffs[4],
                                  const uint8_t *d_mat, const double *d_k, double sol_start,
                                  double sol_end, int zero_to_one, lgx_stream stream,
                                  lgx_matrix **out, const double *d_k1 = nullptr,
-                                 const double *d_k2 = nullptr) {
+                                 const double *d_k2 = nullptr, double henry = -1.0,
+                                 unsigned gaseous_mask = 0) {
   if (!dims || !q || !out) return fail(LGX_ERR_INVALID, "null argument");
   if (dims[0] < 1 || dims[1] < 1 || dims[2] < 1)
     return fail(LGX_ERR_INVALID, "grid dimensions must be positive");
@@ -888,14 +890,22 @@ static lgx_status stencil_create(const int64_t dims[3], const double q[3], const
   lgx_status s = LGX_OK;
   if (d_mat) {
     for (int c = 0; c < 4; ++c) st.coeffs[c] = coeffs[c];
-    // lookup-wright.hpp:73-85: conn[d][a*4+b] = hm(c_a, c_b) * q_d
-    for (int d = 0; d < 3; ++d)
-      for (int f = 0; f < 16; ++f) {
-        const double a = coeffs[f / 4], b = coeffs[f % 4];
-        const double p = a * b;
-        const double h = p != 0.0 ? (p + p) / (a + b) : 0.0;
-        st.conn[d * 16 + f] = h * q[d];
+    // lookup-wright.hpp:18-60: diffusion factor hm(c_a, c_b), or with the
+    // Henry provider hm(c_a f_b, c_b f_a) (f = henry for gaseous materials);
+    // lookup-wright.hpp:73-85: conn[d][a*4+b] = factor * q_d
+    for (int f = 0; f < 16; ++f) {
+      double a = coeffs[f / 4], b = coeffs[f % 4];
+      if (henry >= 0.0) {
+        const double fa = (gaseous_mask >> (f / 4)) & 1u ? henry : 1.0;
+        const double fb = (gaseous_mask >> (f % 4)) & 1u ? henry : 1.0;
+        a = coeffs[f / 4] * fb;
+        b = coeffs[f % 4] * fa;
       }
+      const double p = a * b;
+      st.dfac[f] = p != 0.0 ? (p + p) / (a + b) : 0.0;
+    }
+    for (int d = 0; d < 3; ++d)
+      for (int f = 0; f < 16; ++f) st.conn[d * 16 + f] = st.dfac[f] * q[d];
     s = m->mat.alloc(n);
     if (s == LGX_OK &&
         cudaMemcpyAsync(m->mat.p, d_mat, n, cudaMemcpyDeviceToDevice, stream) != cudaSuccess)
@@ -926,6 +936,17 @@ lgx_status lgx_stencil_create_lookup(const int64_t dims[3], const double q[3],
   if (!d_mat || !coeffs) return fail(LGX_ERR_INVALID, "null materials");
   return stencil_create(dims, q, coeffs, d_mat, nullptr, sol_start, sol_end, zero_to_one, stream,
                         out);
+}
+
+lgx_status lgx_stencil_create_lookup_henry(const int64_t dims[3], const double q[3],
+                                           const double coeffs[4], uint8_t gaseous_materials,
+                                           double henry_constant, const uint8_t *d_mat,
+                                           double sol_start, double sol_end, int zero_to_one,
+                                           lgx_stream stream, lgx_matrix **out) {
+  if (!d_mat || !coeffs) return fail(LGX_ERR_INVALID, "null materials");
+  if (!(henry_constant >= 0.0)) return fail(LGX_ERR_INVALID, "the Henry constant must be >= 0");
+  return stencil_create(dims, q, coeffs, d_mat, nullptr, sol_start, sol_end, zero_to_one, stream,
+                        out, nullptr, nullptr, henry_constant, gaseous_materials);
 }
 
 lgx_status lgx_stencil_create_value(const int64_t dims[3], const double q[3], const double *d_k,
@@ -1003,9 +1024,10 @@ lgx_status lgx_stencil_effective_diffusion(const lgx_matrix *a, const double len
   DBuf<double> out;
   LGX_CHECK(out.alloc(2));
   const cudaStream_t s = (cudaStream_t)stream;
+  StDfac dfac;
+  for (int f = 0; f < 16; ++f) dfac.v[f] = st.dfac[f];
   k_st_effdiff<<<1, kEffThreads, 0, s>>>(other, mid * other, st.lookup ? a->mat.p : nullptr,
-                                         st.lookup ? nullptr : a->k.p, st.coeffs[0],
-                                         st.coeffs[1], st.coeffs[2], st.coeffs[3],
+                                         st.lookup ? nullptr : a->k.p, dfac,
                                          (unsigned)none_materials, d_sol, d_compress_map, out.p);
   LGX_LAUNCH_CHECK();
   count_launch();

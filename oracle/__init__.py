@@ -67,6 +67,9 @@ class _Stencil(C.Structure):
         ("zero_to_one", C.c_int),
         ("k1", C.POINTER(C.c_double)),
         ("k2", C.POINTER(C.c_double)),
+        ("henry", C.c_int),
+        ("henry_constant", C.c_double),
+        ("gaseous_mask", C.c_int),
     ]
 
 
@@ -289,7 +292,8 @@ class Stencil:
     conductivity array per axis)."""
 
     def __init__(self, dims, q=(1.0, 1.0, 1.0), mat=None, coeffs=(0.0, 1.0, 2.0, 3.0), k=None,
-                 sol_start=1.0, sol_end=0.0, zero_to_one=True, k_axes=None):
+                 sol_start=1.0, sol_end=0.0, zero_to_one=True, k_axes=None, henry=None,
+                 gaseous_mask=0):
         self.dims = tuple(int(v) for v in dims)
         self.n = int(np.prod(self.dims))
         self._mat = None if mat is None else np.ascontiguousarray(mat, dtype=np.uint8)
@@ -312,6 +316,11 @@ class Stencil:
         if self._kax is not None:
             s.k1 = self._kax[1].ctypes.data_as(C.POINTER(C.c_double))
             s.k2 = self._kax[2].ctypes.data_as(C.POINTER(C.c_double))
+        if henry is not None:
+            # HenryDiffusionLookupProvider with this Henry constant
+            s.henry = 1
+            s.henry_constant = float(henry)
+            s.gaseous_mask = int(gaseous_mask)
         lib().lo_stencil_init(C.byref(s))
         self._s = s
         self.conn = np.array(s.conn[:])

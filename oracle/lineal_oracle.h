@@ -82,9 +82,18 @@ typedef struct {
    * per cell and axis, k for axis 0 (and the Dirichlet borders), k1 and k2
    * for axes 1 and 2; NULL: the value valuator's single k */
   const double *k1, *k2;
+  /* HenryDiffusionLookupProvider (lookup-wright.hpp:38-60) when henry != 0:
+   * diffusion factor hm(c_a f_b, c_b f_a), f = henry_constant for the
+   * gaseous materials (bit m of gaseous_mask), else 1 */
+  int henry;
+  double henry_constant;
+  int gaseous_mask;
 } lo_stencil;
 
 void lo_stencil_init(lo_stencil *s);
+/* diffusion factor of materials a -> b (SymmetricDiffusionLookupProvider or
+ * HenryDiffusionLookupProvider, lookup-wright.hpp:18-60) */
+double lo_diffusion_factor(const lo_stencil *s, int a, int b);
 /* EffDiffCalc (component-wise/sink/effective-diffusion.hpp:226-320): the
  * effective diffusivity of a solution through the middle planes of axis 0;
  * lengths are the axis lengths, none_mask flags "none" materials (bit m),

@@ -84,8 +84,19 @@ void lo_lookup_tables(const double coeffs[4], const double q[3], double conn[48]
       conn[d * 16 + f] = lo_harmonic_mean(coeffs[f / 4], coeffs[f % 4]) * q[d];
 }
 
+double lo_diffusion_factor(const lo_stencil *s, int a, int b) {
+  if (!s->henry) return lo_harmonic_mean(s->coeffs[a], s->coeffs[b]);
+  const double fa = (s->gaseous_mask >> a) & 1 ? s->henry_constant : 1.0;
+  const double fb = (s->gaseous_mask >> b) & 1 ? s->henry_constant : 1.0;
+  return lo_harmonic_mean(s->coeffs[a] * fb, s->coeffs[b] * fa);
+}
+
 void lo_stencil_init(lo_stencil *s) {
-  if (!s->k) lo_lookup_tables(s->coeffs, s->q, s->conn);
+  if (s->k) return;
+  lo_lookup_tables(s->coeffs, s->q, s->conn);
+  if (s->henry)
+    for (int d = 0; d < 3; ++d)
+      for (int f = 0; f < 16; ++f) s->conn[d * 16 + f] = lo_diffusion_factor(s, f / 4, f % 4) * s->q[d];
 }
 
 static inline double st_cell_value(const lo_stencil *s, int64_t i) {
@@ -206,8 +217,8 @@ double lo_effective_diffusion(const lo_stencil *s, const double lengths[3], uint
     } else {
       filled += 2;
     }
-    const double c1 = st_cell_value(s, i1), c2 = st_cell_value(s, i2);
-    const double hm = lo_harmonic_mean(c1, c2);
+    const double hm = s->mat ? lo_diffusion_factor(s, s->mat[i1], s->mat[i2])
+                             : lo_harmonic_mean(st_cell_value(s, i1), st_cell_value(s, i2));
     if (compress_map) {
       const int64_t k1 = compress_map[i1], k2 = compress_map[i2];
       if (k1 >= 0 && k2 >= 0) flux += hm * (sol[k2] - sol[k1]);

@@ -237,3 +237,21 @@ def test_stencil_values_bitexact(cuda, stencil_engine):
     np.testing.assert_array_equal(val, rcsr.val)
     with pytest.raises(cuda.LinealError):
         m.effective_diffusion((6.0, 7.0, 10.0), x)
+
+
+def test_stencil_henry_bitexact(cuda, stencil_engine):
+    dims = (6, 7, 10)
+    mat = _lookup_case(dims, 25)
+    coeffs = (0.5, 1.0, 2.0, 3.0)
+    lengths = (6.0, 3.5, 10.0)
+    q = lo.axis_quotients(dims, lengths)
+    ref = lo.Stencil(dims, q=q, mat=mat, coeffs=coeffs, sol_start=1.0, sol_end=0.0, henry=0.3,
+                     gaseous_mask=0b0110)
+    m = cuda.StencilMatrix.lookup_henry(dims, q, coeffs, mat, 0.3, 0b0110, 1.0, 0.0)
+    x = np.random.default_rng(26).uniform(-1, 1, ref.n)
+    np.testing.assert_array_equal(cuda.spmv(m, x).cpu().numpy(), ref.spmv(x))
+    np.testing.assert_array_equal(m.diagonal().cpu().numpy(), ref.diagonal())
+    np.testing.assert_array_equal(m.rhs().cpu().numpy(), ref.rhs())
+    eff, area = m.effective_diffusion(lengths, x, none_mask=0b1000)
+    want, want_area = ref.effective_diffusion(lengths, x, none_mask=0b1000)
+    assert area == want_area and abs(eff - want) <= 1e-13 * abs(want)

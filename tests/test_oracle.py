@@ -326,3 +326,26 @@ def test_values_valuator_matches_explicit_operator():
             dense[i, i] += 2 * q[0] * ks[0][i] * ((pos[0] == 0) + (pos[0] == dims[0] - 1))
     np.testing.assert_allclose(st.spmv(x), dense @ x, rtol=1e-13, atol=1e-13)
     assert not np.allclose(st.spmv(x), val.spmv(x))
+
+
+def test_henry_lookup_provider():
+    """HenryDiffusionLookupProvider (lookup-wright.hpp:38-60): factor
+    hm(c_a f_b, c_b f_a) with f = H for gaseous materials; H = 1 gives the
+    symmetric provider."""
+    dims = (5, 4, 6)
+    mat = np.random.default_rng(23).integers(0, 4, int(np.prod(dims))).astype(np.uint8)
+    coeffs = (0.5, 1.0, 2.0, 3.0)
+    q = lo.axis_quotients(dims, (1.0, 1.2, 0.8))
+    sym = lo.Stencil(dims, q=q, mat=mat, coeffs=coeffs)
+    h1 = lo.Stencil(dims, q=q, mat=mat, coeffs=coeffs, henry=1.0, gaseous_mask=0b1010)
+    np.testing.assert_array_equal(h1.conn, sym.conn)
+    h = lo.Stencil(dims, q=q, mat=mat, coeffs=coeffs, henry=0.3, gaseous_mask=0b1010)
+    hm = lambda a, b: 2 * a * b / (a + b)  # noqa: E731
+    for a in range(4):
+        for b in range(4):
+            fa = 0.3 if (0b1010 >> a) & 1 else 1.0
+            fb = 0.3 if (0b1010 >> b) & 1 else 1.0
+            want = hm(coeffs[a] * fb, coeffs[b] * fa) * q[1]
+            assert h.conn[16 + a * 4 + b] == pytest.approx(want, rel=1e-15)
+    x = np.random.default_rng(24).uniform(-1, 1, len(mat))
+    assert not np.allclose(h.spmv(x), sym.spmv(x))
