@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <concepts>
 #include <cstddef>
@@ -234,6 +235,57 @@ class StencilMatrix : public MatrixHandle {
                                    env.stream(), &h));
     return StencilMatrix(h);
   }
+  // StationaryDiffusionValuesValuator: one conductivity array per axis
+  static StencilMatrix values(const int64_t dims[3], const double q[3],
+                              const DenseVector<double> &k0, const DenseVector<double> &k1,
+                              const DenseVector<double> &k2, double sol_start, double sol_end,
+                              bool zero_to_one, const Environment &env) {
+    lgx_matrix *h = nullptr;
+    check(lgx_stencil_create_values(dims, q, k0.data(), k1.data(), k2.data(), sol_start, sol_end,
+                                    zero_to_one, env.stream(), &h));
+    return StencilMatrix(h);
+  }
+  // lookup valuator with HenryDiffusionLookupWright's diffusion factors
+  static StencilMatrix lookup_henry(const int64_t dims[3], const double q[3],
+                                    const double coeffs[4], uint8_t gaseous_materials,
+                                    double henry_constant, const DenseVector<uint8_t> &materials,
+                                    double sol_start, double sol_end, bool zero_to_one,
+                                    const Environment &env) {
+    lgx_matrix *h = nullptr;
+    check(lgx_stencil_create_lookup_henry(dims, q, coeffs, gaseous_materials, henry_constant,
+                                          materials.data(), sol_start, sol_end, zero_to_one,
+                                          env.stream(), &h));
+    return StencilMatrix(h);
+  }
+};
+
+// EffDiffCalc (component-wise/sink/effective-diffusion.hpp:226-320): the
+// effective diffusivity of a solution through the middle planes of axis 0.
+// Constructed from the stencil (its axis lengths and "none" materials);
+// the call takes the solution (and the compress map of a compressed system).
+class EffDiffCalc {
+ public:
+  EffDiffCalc(const StencilMatrix &valuator, const std::array<double, 3> &axis_lengths,
+              uint8_t none_materials = 0)
+      : lengths_(axis_lengths), none_(none_materials) {
+    (void)valuator;
+  }
+  double operator()(const StencilMatrix &valuator, const DenseVector<double> &sol,
+                    const Environment &env) const {
+    return (*this)(valuator, nullptr, sol, env);
+  }
+  double operator()(const StencilMatrix &valuator, const DenseVector<int64_t> *compress_map,
+                    const DenseVector<double> &sol, const Environment &env) const {
+    double eff = 0.0, area = 0.0;
+    check(lgx_stencil_effective_diffusion(valuator.handle(), lengths_.data(), none_,
+                                          sol.data(), compress_map ? compress_map->data() : nullptr,
+                                          env.stream(), &eff, &area));
+    return eff;
+  }
+
+ private:
+  std::array<double, 3> lengths_;
+  uint8_t none_;
 };
 
 // ---- component-wise operations (component-wise/*) ------------------------------
