@@ -60,3 +60,12 @@ def test_invalid_arguments_are_statuses(library):
     assert lib.lgx_amg_autotune(None, 5, None, 0, None, None) == 1
     assert lib.lgx_amg_autotune_reset(None) == 1
     assert b"null" in lib.lgx_last_error()
+
+
+def test_concept_layer_compiles_and_links(library):
+    """include/lineal_gb300/lineal.hpp compiles in a complete program (the
+    one the GPU suite runs) and links against the library."""
+    from lineal_gb300 import build
+
+    exe = build.build_cpp_demo()
+    assert os.path.isfile(exe) and os.access(exe, os.X_OK)
