@@ -387,6 +387,16 @@ lgx_status lgx_amg_info(const lgx_amg *h, int64_t *nlevels, int64_t *rows, int64
 lgx_status lgx_amg_level_download(const lgx_amg *h, int64_t level, int64_t *h_rowptr,
                                   int32_t *h_col, double *h_val, uint32_t *h_agg,
                                   lgx_stream stream);
+/* Coarse->fine lists of `level`'s aggregates (BaseMultithreadAggregateMap::
+ * coarse_row_to_fine_rows, aggregate-map/multithread.hpp:337-344; with the
+ * fine->coarse map of lgx_amg_level_download, what to_file writes, 346-349):
+ * h_list_ptr[ncoarse + 1] offsets and h_list[*list_len] fine vertices (natural
+ * ordering, in the order aggregation added them).  NULL pointers skip an
+ * output; *list_len = h_list_ptr[ncoarse] = the number of aggregated (not
+ * isolated) vertices.  The coarsest level has no lists.  Synchronises
+ * `stream`. */
+lgx_status lgx_amg_level_lists(const lgx_amg *h, int64_t level, int64_t *h_list_ptr,
+                               int32_t *h_list, int64_t *list_len, lgx_stream stream);
 /* One V-cycle from a zero initial guess: x = M^-1 b (MultiGridSolver::
  * Instance::apply, multigrid/solver.hpp:41-176, REGULAR cycle, 1 iteration). */
 lgx_status lgx_amg_vcycle(lgx_amg *h, const double *d_b, double *d_x, lgx_stream stream);

@@ -187,6 +187,7 @@ def _signatures(L):
         "lgx_amg_destroy": [V],
         "lgx_amg_info": [V, P(I64), V, V, I64],
         "lgx_amg_level_download": [V, I64, V, V, V, V, V],
+        "lgx_amg_level_lists": [V, I64, V, V, V, V],
         "lgx_amg_vcycle": [V, V, V, V],
         "lgx_matrix_autotune": [V, C.c_int, P(_TuneEntry), V],
         "lgx_amg_autotune": [V, C.c_int, P(_TuneEntry), C.c_int, P(C.c_int), V],
@@ -699,6 +700,36 @@ class Hierarchy:
         _check(lib().lgx_amg_level_download(self._h, l, _ptr(rowptr), _ptr(col), _ptr(val),
                                             _ptr(agg), _stream()))
         return rowptr, col, val, agg
+
+    def aggregate_map(self, l: int):
+        """Level l's aggregates as an ``io.AggregateMap``: the fine -> coarse
+        ids and the coarse -> fine lists in the order aggregation added the
+        vertices (natural ordering)."""
+        from . import io as _io
+
+        rows, _ = self.sizes()
+        if not 0 <= l < len(rows) - 1:
+            raise IndexError(f"level {l} has no aggregate map")
+        agg = np.empty(rows[l], dtype=np.uint32)
+        _check(lib().lgx_amg_level_download(self._h, l, None, None, None, _ptr(agg), _stream()))
+        list_ptr = np.empty(rows[l + 1] + 1, dtype=np.int64)
+        total = C.c_int64()
+        _check(lib().lgx_amg_level_lists(self._h, l, _ptr(list_ptr), None, C.byref(total),
+                                         _stream()))
+        lst = np.empty(max(total.value, 1), dtype=np.int32)
+        _check(lib().lgx_amg_level_lists(self._h, l, None, _ptr(lst), None, _stream()))
+        return _io.AggregateMap(agg, list_ptr, lst[: total.value])
+
+    def aggregate_maps(self) -> list:
+        return [self.aggregate_map(l) for l in range(self.level_num() - 1)]
+
+    def save_aggregates(self, base: str) -> list:
+        """Writes every level's aggregate map to ``<base><level>.aggs``, as
+        lineal's RefinedAggregator does with ``base_agg_map_path``
+        (aggregation/independent.hpp:264-272); returns the paths."""
+        from . import io as _io
+
+        return _io.save_aggregates(base, self.aggregate_maps())
 
     def vcycle(self, b, out=None):
         b = _dvec(b)

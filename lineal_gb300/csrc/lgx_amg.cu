@@ -1324,6 +1324,30 @@ lgx_status lgx_amg_level_download(const lgx_amg *h, int64_t level, int64_t *h_ro
   return LGX_OK;
 }
 
+lgx_status lgx_amg_level_lists(const lgx_amg *h, int64_t level, int64_t *h_list_ptr,
+                               int32_t *h_list, int64_t *list_len, lgx_stream stream) {
+  if (!h || level < 0 || level + 1 >= (int64_t)h->lv.size())
+    return fail(LGX_ERR_INVALID, "bad level (the coarsest level has no aggregate lists)");
+  const AggResult &g = h->lv[level]->agg;
+  const int64_t nc = g.ncoarse;
+  if (g.list_ptr.n < nc + 1) return fail(LGX_ERR_INVALID, "hierarchy holds no aggregate lists for this level");
+  int64_t total = 0;
+  LGX_CUDA(cudaMemcpyAsync(&total, g.list_ptr.p + nc, sizeof(int64_t), cudaMemcpyDeviceToHost,
+                           stream));
+  if (h_list_ptr)
+    LGX_CUDA(cudaMemcpyAsync(h_list_ptr, g.list_ptr.p, sizeof(int64_t) * (size_t)(nc + 1),
+                             cudaMemcpyDeviceToHost, stream));
+  LGX_CUDA(cudaStreamSynchronize(stream));
+  if (total < 0 || total > g.list.n) return fail(LGX_ERR_INVALID, "aggregate lists inconsistent");
+  if (list_len) *list_len = total;
+  if (h_list && total > 0) {
+    LGX_CUDA(cudaMemcpyAsync(h_list, g.list.p, sizeof(int32_t) * (size_t)total,
+                             cudaMemcpyDeviceToHost, stream));
+    LGX_CUDA(cudaStreamSynchronize(stream));
+  }
+  return LGX_OK;
+}
+
 lgx_status lgx_amg_vcycle(lgx_amg *h, const double *d_b, double *d_x, lgx_stream stream) {
   if (!h || !d_b || !d_x) return fail(LGX_ERR_INVALID, "null argument");
   lgx_amg_level &l0 = *h->lv[0];

@@ -117,6 +117,19 @@ class _Amg(C.Structure):
     ]
 
 
+class _AggMap(C.Structure):
+    _fields_ = [
+        ("n", C.c_int64),
+        ("ncoarse", C.c_int64),
+        ("agg", C.c_void_p),
+        ("list_ptr", C.c_void_p),
+        ("list", C.c_void_p),
+    ]
+
+
+LO_ERR_NO_MAP, LO_ERR_BAD_MAP = -2, -3
+
+
 class _Precon(C.Structure):
     _fields_ = [
         ("kind", C.c_int),
@@ -189,6 +202,10 @@ def _setup_signatures(L):
     L.lo_amg_setup.restype = C.c_int
     L.lo_amg_setup.argtypes = [P(_Csr), P(_AmgParams), P(_Amg)]
     L.lo_amg_free.argtypes = [P(_Amg)]
+    L.lo_agg_map_check.restype = C.c_int
+    L.lo_agg_map_check.argtypes = [P(_AggMap)]
+    L.lo_amg_setup_given.restype = C.c_int
+    L.lo_amg_setup_given.argtypes = [P(_Csr), P(_AmgParams), P(_AggMap), C.c_int64, P(_Amg)]
     L.lo_amg_vcycle.argtypes = [P(_Amg), C.c_void_p, C.c_void_p]
     L.lo_pcg.restype = C.c_int64
     L.lo_pcg.argtypes = [P(_Csr), C.c_void_p, C.c_void_p, P(_Precon), C.c_double, C.c_int64,
@@ -553,17 +570,52 @@ def amg_galerkin(a: Csr, nc: int, agg, list_ptr, lst, coarse_f32=False) -> Csr:
     return _take_csr(out, L)
 
 
-class Amg:
-    """Oracle aggregation-AMG hierarchy + V-cycle (owns C memory)."""
+def _agg_maps(maps):
+    """(agg, list_ptr, list) triples -> C maps plus the arrays they point into"""
+    keep, cm = [], (_AggMap * max(len(maps), 1))()
+    for k, (agg, list_ptr, lst) in enumerate(maps):
+        agg = np.ascontiguousarray(agg, dtype=np.uint32)
+        list_ptr = np.ascontiguousarray(list_ptr, dtype=np.int64)
+        lst = np.ascontiguousarray(lst, dtype=np.int32)
+        if list_ptr.ndim != 1 or len(list_ptr) < 1:
+            raise ValueError(f"aggregate map {k}: list_ptr needs ncoarse + 1 entries")
+        keep += [agg, list_ptr, lst]
+        cm[k] = _AggMap(len(agg), len(list_ptr) - 1, agg.ctypes.data, list_ptr.ctypes.data,
+                        lst.ctypes.data)
+    return cm, keep
 
-    def __init__(self, a: Csr, **params):
+
+def agg_map_check(agg, list_ptr, lst) -> bool:
+    """lo_agg_map_check: the fine->coarse map and the coarse->fine lists agree"""
+    cm, _keep = _agg_maps([(agg, list_ptr, lst)])
+    return lib().lo_agg_map_check(C.byref(cm[0])) == 0
+
+
+class Amg:
+    """Oracle aggregation-AMG hierarchy + V-cycle (owns C memory).
+
+    With ``maps`` (a sequence of (agg, list_ptr, list) per level) the
+    aggregation of level k is replaced by maps[k], as lineal's FileAggregator
+    does (aggregation/independent.hpp:279-298)."""
+
+    def __init__(self, a: Csr, maps=None, **params):
         self._a = a
         self._c = a._c()
         self._p = amg_params(**params)
         self._h = _Amg()
-        rc = lib().lo_amg_setup(C.byref(self._c), C.byref(self._p), C.byref(self._h))
+        if maps is None:
+            rc = lib().lo_amg_setup(C.byref(self._c), C.byref(self._p), C.byref(self._h))
+        else:
+            cm, _keep = _agg_maps(maps)
+            rc = lib().lo_amg_setup_given(C.byref(self._c), C.byref(self._p), cm, len(maps),
+                                          C.byref(self._h))
         if rc != 0:
             lib().lo_amg_free(C.byref(self._h))
+            self._h = None
+            if rc == LO_ERR_NO_MAP:
+                raise ValueError("no aggregate map for a level the hierarchy needs")
+            if rc == LO_ERR_BAD_MAP:
+                raise ValueError("aggregate map does not fit its level")
             raise np.linalg.LinAlgError("coarsest matrix not positive definite")
 
     @property
@@ -584,6 +636,17 @@ class Amg:
 
     def level_agg(self, l: int) -> np.ndarray:
         return np.ctypeslib.as_array(self._h.lv[l].agg, shape=(self.level_size(l),)).copy()
+
+    def level_map(self, l: int):
+        """(agg, list_ptr, list) of level l (fine -> coarse ids, coarse -> fine lists)"""
+        if not 0 <= l < self.nlevels - 1:
+            raise IndexError(f"level {l} has no aggregate map")
+        lv = self._h.lv[l]
+        nc = self.level_size(l + 1)
+        list_ptr = np.ctypeslib.as_array(lv.list_ptr, shape=(nc + 1,)).copy()
+        total = int(list_ptr[-1])
+        lst = np.ctypeslib.as_array(lv.list, shape=(max(total, 1),))[:total].copy()
+        return self.level_agg(l), list_ptr, lst
 
     def level_order(self, l: int):
         o = self._h.lv[l].order

@@ -244,6 +244,29 @@ typedef struct {
 
 /* hierarchy/wright.hpp:120-309 */
 int lo_amg_setup(const lo_csr *a, const lo_amg_params *p, lo_amg *h);
+
+/* An aggregate map of one level as BaseMultithreadAggregateMap holds it
+ * (aggregate-map/multithread.hpp:42-45, 294-302): fine -> coarse ids (n;
+ * LO_ISOLATED for isolated vertices) and the coarse -> fine lists
+ * (list_ptr[ncoarse + 1], list[list_ptr[ncoarse]]). */
+typedef struct {
+  int64_t n, ncoarse;
+  const uint32_t *agg;
+  const int64_t *list_ptr;
+  const int32_t *list;
+} lo_agg_map;
+enum { LO_ERR_NO_MAP = -2, LO_ERR_BAD_MAP = -3 };
+/* 0 when the two maps agree: every id below ncoarse or LO_ISOLATED, every
+ * aggregated vertex in exactly the list of its aggregate, no empty list;
+ * LO_ERR_BAD_MAP otherwise */
+int lo_agg_map_check(const lo_agg_map *m);
+/* lo_amg_setup with the aggregation of level k replaced by maps[k]
+ * (FileAggregator, aggregation/independent.hpp:279-298; the stop rules of
+ * wright.hpp:120-143 unchanged).  Returns LO_ERR_NO_MAP when a level needs
+ * a map beyond nmaps, LO_ERR_BAD_MAP when a map does not fit its level
+ * (size or consistency), else as lo_amg_setup.  h is freeable on return. */
+int lo_amg_setup_given(const lo_csr *a, const lo_amg_params *p, const lo_agg_map *maps,
+                       int64_t nmaps, lo_amg *h);
 void lo_amg_free(lo_amg *h);
 /* multigrid/solver.hpp:56-176, one REGULAR V-cycle from x_in = 0 */
 void lo_amg_vcycle(lo_amg *h, const double *b, double *x);

@@ -552,7 +552,67 @@ int64_t lo_amg_partitions(int64_t n, int64_t level, const lo_amg_params *p) {
 }
 
 /* hierarchy/wright.hpp:120-143 (level_action) and 146-309 (create_impl) */
-int lo_amg_setup(const lo_csr *a0, const lo_amg_params *p, lo_amg *h) {
+int lo_agg_map_check(const lo_agg_map *m) {
+  if (!m || m->n < 0 || m->ncoarse < 0 || (m->n > 0 && !m->agg) || !m->list_ptr ||
+      (m->ncoarse > 0 && !m->list) || m->list_ptr[0] != 0)
+    return LO_ERR_BAD_MAP;
+  int64_t aggregated = 0;
+  for (int64_t v = 0; v < m->n; ++v) {
+    if (m->agg[v] == LO_ISOLATED) continue;
+    if ((int64_t)m->agg[v] >= m->ncoarse) return LO_ERR_BAD_MAP;
+    ++aggregated;
+  }
+  if (m->list_ptr[m->ncoarse] != aggregated) return LO_ERR_BAD_MAP;
+  uint8_t *seen = (uint8_t *)calloc((size_t)m->n + 1, 1);
+  int rc = 0;
+  for (int64_t c = 0; c < m->ncoarse && rc == 0; ++c) {
+    if (m->list_ptr[c + 1] <= m->list_ptr[c]) rc = LO_ERR_BAD_MAP;  /* empty aggregate */
+    for (int64_t k = m->list_ptr[c]; k < m->list_ptr[c + 1] && rc == 0; ++k) {
+      const int32_t v = m->list[k];
+      if (v < 0 || v >= m->n || seen[v] || (int64_t)m->agg[v] != c) rc = LO_ERR_BAD_MAP;
+      else seen[v] = 1;
+    }
+  }
+  free(seen);
+  return rc;
+}
+
+/* the level's aggregate map: computed (strength + aggregation), or copied
+ * from a given map (FileAggregator, aggregation/independent.hpp:279-298) */
+static int level_aggregates(const lo_csr *a, const lo_amg_params *p, int64_t level, int aggressive,
+                            const lo_agg_map *given, lo_amg_level *fine, int64_t *nc_out) {
+  if (given) {
+    if (given->n != a->n) return LO_ERR_BAD_MAP;
+    const int rc = lo_agg_map_check(given);
+    if (rc) return rc;
+    const int64_t nc = given->ncoarse, len = given->list_ptr[nc];
+    fine->agg = (uint32_t *)malloc((size_t)(a->n + 1) * sizeof(uint32_t));
+    fine->list_ptr = (int64_t *)malloc((size_t)(nc + 1) * sizeof(int64_t));
+    fine->list = (int32_t *)malloc((size_t)(len + 1) * sizeof(int32_t));
+    if (a->n) memcpy(fine->agg, given->agg, (size_t)a->n * sizeof(uint32_t));
+    memcpy(fine->list_ptr, given->list_ptr, (size_t)(nc + 1) * sizeof(int64_t));
+    if (len) memcpy(fine->list, given->list, (size_t)len * sizeof(int32_t));
+    *nc_out = nc;
+    return 0;
+  }
+  const int64_t nnz = lo_csr_nnz(a);
+  uint8_t *dep = (uint8_t *)malloc((size_t)nnz + 1);
+  uint8_t *inf = (uint8_t *)malloc((size_t)nnz + 1);
+  uint8_t *iso = (uint8_t *)malloc((size_t)a->n + 1);
+  lo_amg_strength(a, aggressive ? p->aggressive_threshold : p->strong_threshold, dep, inf, iso);
+  fine->agg = (uint32_t *)malloc((size_t)(a->n + 1) * sizeof(uint32_t));
+  int64_t stats[5];
+  *nc_out = lo_amg_aggregate(a, dep, inf, iso, p->min_aggregate_size, p->max_aggregate_size,
+                             lo_amg_partitions(a->n, level, p), aggressive, fine->agg,
+                             &fine->list_ptr, &fine->list, stats);
+  free(dep);
+  free(inf);
+  free(iso);
+  return 0;
+}
+
+static int amg_setup(const lo_csr *a0, const lo_amg_params *p, const lo_agg_map *maps,
+                     int64_t nmaps, lo_amg *h) {
   memset(h, 0, sizeof(*h));
   h->p = *p;
   csr_copy(a0, &h->lv[0].a);
@@ -561,21 +621,14 @@ int lo_amg_setup(const lo_csr *a0, const lo_amg_params *p, lo_amg *h) {
   for (;;) {
     lo_amg_level *fine = &h->lv[level];
     const lo_csr *a = &fine->a;
-    const int64_t nnz = lo_csr_nnz(a);
-    uint8_t *dep = (uint8_t *)malloc((size_t)nnz + 1);
-    uint8_t *inf = (uint8_t *)malloc((size_t)nnz + 1);
-    uint8_t *iso = (uint8_t *)malloc((size_t)a->n + 1);
-    lo_amg_strength(a, aggressive ? p->aggressive_threshold : p->strong_threshold, dep, inf, iso);
-    fine->agg = (uint32_t *)malloc((size_t)(a->n + 1) * sizeof(uint32_t));
-    int64_t stats[5];
-    const int64_t nc =
-      lo_amg_aggregate(a, dep, inf, iso, p->min_aggregate_size, p->max_aggregate_size,
-                       lo_amg_partitions(a->n, level, p), aggressive, fine->agg,
-                       &fine->list_ptr,
-                       &fine->list, stats);
-    free(dep);
-    free(inf);
-    free(iso);
+    int64_t nc = 0;
+    int rc = 0;
+    if (maps && level >= nmaps) rc = LO_ERR_NO_MAP;
+    else rc = level_aggregates(a, p, level, aggressive, maps ? &maps[level] : NULL, fine, &nc);
+    if (rc) {
+      h->nlevels = level + 1;  /* what lo_amg_free releases */
+      return rc;
+    }
     lo_amg_level *coarse = &h->lv[level + 1];
     lo_amg_galerkin(a, nc, fine->agg, fine->list_ptr, fine->list, p->coarse_f32, &coarse->a);
     level_vectors(fine, p, level);
@@ -603,6 +656,19 @@ int lo_amg_setup(const lo_csr *a0, const lo_amg_params *p, lo_amg *h) {
    * hierarchies (test/aux/default.hpp:160-162) */
   return last->a.symmetric ? lo_cholesky_factor(&last->a, h->chol)
                            : lo_lu_factor(&last->a, h->chol);
+}
+
+int lo_amg_setup(const lo_csr *a, const lo_amg_params *p, lo_amg *h) {
+  return amg_setup(a, p, NULL, 0, h);
+}
+
+int lo_amg_setup_given(const lo_csr *a, const lo_amg_params *p, const lo_agg_map *maps,
+                       int64_t nmaps, lo_amg *h) {
+  if (!maps || nmaps < 1) {
+    memset(h, 0, sizeof(*h));
+    return LO_ERR_NO_MAP;
+  }
+  return amg_setup(a, p, maps, nmaps, h);
 }
 
 void lo_amg_free(lo_amg *h) {

@@ -58,6 +58,7 @@ def test_invalid_arguments_are_statuses(library):
     assert lib.lgx_matrix_info(None, None, None, None, None) == 1
     assert lib.lgx_matrix_autotune(None, 5, None, None) == 1
     assert lib.lgx_amg_autotune(None, 5, None, 0, None, None) == 1
+    assert lib.lgx_amg_level_lists(None, 0, None, None, None, None) == 1
     assert lib.lgx_amg_autotune_reset(None) == 1
     assert b"null" in lib.lgx_last_error()
 

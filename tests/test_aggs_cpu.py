@@ -1,0 +1,134 @@
+"""Aggregate-map files (lineal_gb300.io) and hierarchies built from given
+aggregate maps, lineal's RefinedAggregator / FileAggregator pair
+(linear-solver/multigrid/aggregation/independent.hpp:237-298), on the CPU:
+the oracle's maps survive a file round trip, a hierarchy rebuilt from them
+equals the one that computed them, and damaged maps or files are refused."""
+
+import os
+
+import numpy as np
+import pytest
+
+import oracle as lo
+from lineal_gb300 import io as lio
+
+PARAMS = dict(min_coarsen_size=20, partition_size=64, smoother_parts=0)
+
+
+def _case(dims=(10, 12, 14), seed=0, npts=27):
+    k = np.exp(1.5 * np.random.default_rng(seed).standard_normal(int(np.prod(dims))))
+    return (lo.gen_27pt if npts == 27 else lo.gen_7pt)(dims, k)
+
+
+def _maps(h):
+    return [lio.AggregateMap(*h.level_map(l)) for l in range(h.nlevels - 1)]
+
+
+def _assert_maps_equal(a, b):
+    assert len(a) == len(b)
+    for x, y in zip(a, b):
+        for u, v in zip(x, y):
+            np.testing.assert_array_equal(u, v)
+
+
+@pytest.mark.parametrize("npts", [27, 7])
+def test_file_round_trip_and_rebuild(tmp_path, npts):
+    a = _case(npts=npts)
+    h = lo.Amg(a, **PARAMS)
+    assert h.nlevels >= 3
+    maps = _maps(h)
+    for m in maps:
+        assert lo.agg_map_check(*m)
+        lio.check_aggregate_map(m)
+    base = str(tmp_path / "level")
+    paths = lio.save_aggregates(base, maps)
+    assert paths == [f"{base}{k}.aggs" for k in range(len(maps))]
+    back = lio.load_aggregates(base)
+    _assert_maps_equal(maps, back)
+    # FileAggregator: the rebuilt hierarchy equals the one that aggregated
+    g = lo.Amg(a, maps=back, **PARAMS)
+    assert g.nlevels == h.nlevels
+    for l in range(h.nlevels):
+        x, y = h.level_csr(l), g.level_csr(l)
+        np.testing.assert_array_equal(x.rowptr, y.rowptr)
+        np.testing.assert_array_equal(x.col, y.col)
+        np.testing.assert_array_equal(x.val, y.val)
+    b = np.random.default_rng(1).uniform(-1, 1, a.n)
+    np.testing.assert_array_equal(h.vcycle(b), g.vcycle(b))
+
+
+def test_given_maps_override_the_partitioning():
+    # maps computed with 64-vertex partitions, used by a setup whose own
+    # aggregation would run in one partition: the maps decide the hierarchy
+    a = _case(seed=3)
+    h = lo.Amg(a, **PARAMS)
+    one = dict(PARAMS, partition_size=1 << 20, max_partitions=1)
+    plain = lo.Amg(a, **one)
+    assert [plain.level_size(l) for l in range(plain.nlevels)] != \
+        [h.level_size(l) for l in range(h.nlevels)] or \
+        not np.array_equal(plain.level_agg(0), h.level_agg(0))
+    g = lo.Amg(a, maps=_maps(h), **one)
+    _assert_maps_equal(_maps(g), _maps(h))
+
+
+def test_missing_and_mismatched_maps_are_refused():
+    a = _case()
+    h = lo.Amg(a, **PARAMS)
+    maps = _maps(h)
+    with pytest.raises(ValueError, match="no aggregate map"):
+        lo.Amg(a, maps=maps[:1], **PARAMS)
+    # level 1's map given for level 0: wrong fine size
+    with pytest.raises(ValueError, match="does not fit"):
+        lo.Amg(a, maps=maps[1:] + maps[:1], **PARAMS)
+
+
+def _damaged(m):
+    agg, ptr, lst = (np.array(v) for v in m)
+    out = {}
+    bad = agg.copy()
+    bad[int(lst[0])] = len(ptr) + 5  # id beyond the coarse size
+    out["id"] = (bad, ptr, lst)
+    swap = lst.copy()
+    swap[[0, -1]] = swap[[-1, 0]]  # vertices listed under the wrong aggregate
+    out["owner"] = (agg, ptr, swap)
+    dup = lst.copy()
+    dup[1] = dup[0]
+    out["repeat"] = (agg, ptr, dup)
+    iso = agg.copy()
+    iso[int(lst[0])] = lio.ISOLATED  # an isolated vertex still listed
+    out["isolated"] = (iso, ptr, lst)
+    return out
+
+
+def test_damaged_maps_fail_both_checks():
+    h = lo.Amg(_case(), **PARAMS)
+    m = lio.AggregateMap(*h.level_map(0))
+    for name, d in _damaged(m).items():
+        assert not lo.agg_map_check(*d), name
+        with pytest.raises(ValueError):
+            lio.check_aggregate_map(lio.AggregateMap(*d))
+        with pytest.raises(ValueError, match="does not fit"):
+            lo.Amg(_case(), maps=[d] + _maps(h)[1:], **PARAMS)
+
+
+def test_damaged_files_are_refused(tmp_path):
+    h = lo.Amg(_case(), **PARAMS)
+    maps = _maps(h)
+    base = str(tmp_path / "m")
+    lio.save_aggregates(base, maps)
+    raw = open(lio.aggs_path(base, 0), "rb").read()
+    open(lio.aggs_path(base, 0), "wb").write(raw[:-4])
+    with pytest.raises(ValueError, match="size"):
+        lio.read_aggs(lio.aggs_path(base, 0))
+    open(lio.aggs_path(base, 0), "wb").write(b"NOTAGGS!" + raw[8:])
+    with pytest.raises(ValueError, match="not an aggregate-map"):
+        lio.read_aggs(lio.aggs_path(base, 0))
+    # levels that do not chain
+    lio.save_aggregates(base, [maps[0], maps[0]])
+    with pytest.raises(ValueError, match="coarse size"):
+        lio.load_aggregates(base)
+    with pytest.raises(FileNotFoundError):
+        lio.load_aggregates(str(tmp_path / "absent"))
+    with pytest.raises(ValueError):
+        lio.write_aggs(str(tmp_path / "x.aggs"), lio.AggregateMap(*_damaged(maps[0])["owner"]))
+    assert not os.path.exists(str(tmp_path / "x.aggs"))

@@ -1,0 +1,44 @@
+"""Aggregate maps of a GPU hierarchy: both halves (fine -> coarse ids and
+the coarse -> fine lists in aggregation order) equal the oracle's, and the
+files the GPU hierarchy writes (RefinedAggregator with base_agg_map_path,
+aggregation/independent.hpp:264-272) rebuild, through the oracle's
+FileAggregator path, the GPU's level matrices bit for bit."""
+
+import numpy as np
+import pytest
+
+import oracle as lo
+from lineal_gb300 import io as lio
+
+pytestmark = pytest.mark.gpu
+
+PARAMS = dict(min_coarsen_size=64, partition_size=512, max_partitions=1 << 30)
+
+
+def test_gpu_aggregate_maps_cross_check_the_oracle(cuda, tmp_path):
+    dims = (14, 15, 16)
+    ref = lo.gen_27pt(dims, np.exp(1.5 * np.random.default_rng(1).standard_normal(
+        int(np.prod(dims)))))
+    m = cuda.CsrMatrix.from_host(ref.rowptr, ref.col, ref.val, symmetric=True)
+    h = cuda.HierarchyWright(**PARAMS).instantiate(m)
+    oh = lo.Amg(ref, smoother_parts=0, **PARAMS)
+    maps = h.aggregate_maps()
+    assert len(maps) == oh.nlevels - 1 >= 2
+    for l, mm in enumerate(maps):
+        lio.check_aggregate_map(mm)
+        for got, want in zip(mm, oh.level_map(l)):
+            np.testing.assert_array_equal(got, want)
+    with pytest.raises(IndexError):
+        h.aggregate_map(len(maps))
+    base = str(tmp_path / "gpu")
+    assert h.save_aggregates(base) == [lio.aggs_path(base, k) for k in range(len(maps))]
+    # one partition of its own: only the files decide the aggregates
+    g = lo.Amg(ref, maps=lio.load_aggregates(base), smoother_parts=0,
+               **dict(PARAMS, partition_size=1 << 24, max_partitions=1))
+    assert g.nlevels == len(maps) + 1
+    for l in range(g.nlevels):
+        rowptr, col, val, _ = h.level(l, with_agg=False)
+        rl = g.level_csr(l)
+        np.testing.assert_array_equal(rowptr, rl.rowptr)
+        np.testing.assert_array_equal(col, rl.col)
+        np.testing.assert_array_equal(val, rl.val)
