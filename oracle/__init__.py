@@ -143,6 +143,15 @@ class _Precon(C.Structure):
 PRECON_NONE, PRECON_JACOBI, PRECON_SSOR, PRECON_AMG = 0, 1, 2, 3
 
 
+def set_threads(n: int) -> None:
+    """Thread count of the restatement's OpenMP loops from now on."""
+    lib().lo_set_threads(int(n))
+
+
+def max_threads() -> int:
+    return int(lib().lo_max_threads())
+
+
 def lib():
     global _lib
     if _lib is None:
@@ -155,6 +164,10 @@ def lib():
 def _setup_signatures(L):
     P = C.POINTER
     L.lo_csr_free.argtypes = [P(_Csr)]
+    L.lo_set_threads.restype = None
+    L.lo_set_threads.argtypes = [C.c_int]
+    L.lo_max_threads.restype = C.c_int
+    L.lo_max_threads.argtypes = []
     L.lo_part_begin.restype = C.c_int64
     L.lo_part_begin.argtypes = [C.c_int64, C.c_int64, C.c_int64]
     L.lo_harmonic_mean.restype = C.c_double

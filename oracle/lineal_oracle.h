@@ -51,6 +51,9 @@ int lo_csr_alloc(lo_csr *a, int64_t n, int64_t nnz);
  * k*(n/p) + min(k, n%p).  Stands in for thesauros' BlockedIndexSegmenter
  * (adaptive.hpp:266-268). */
 int64_t lo_part_begin(int64_t n, int64_t p, int64_t k);
+/* OpenMP threads of the later parallel loops (n > 0), and their number now */
+void lo_set_threads(int n);
+int lo_max_threads(void);
 
 /* ---- geometry and valuators ---------------------------------------- */
 /* box-equidistant.hpp:67-79 */

@@ -9,6 +9,26 @@
 
 #include "lineal_oracle.h"
 
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+void lo_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+
+int lo_max_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
 void lo_csr_free(lo_csr *a) {
   free(a->rowptr);
   free(a->col);

@@ -62,3 +62,16 @@ def test_warmup_below_three_is_rejected():
                        cwd=ROOT, capture_output=True, text=True, timeout=120)
     assert r.returncode != 0
     assert "warmup" in r.stderr
+
+
+def test_cpu_baseline_entry_all_threads_and_one_core():
+    code = ("import argparse, json, bench; a = argparse.Namespace(cpu_sample_edge=12, grid=256); "
+            "print(json.dumps(bench.cpu_baseline_entry(a, (3 * 256 - 2) ** 3, 61)))")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    d = _json_lines(r.stdout)[-1]
+    assert d["kind"] == "port" and d["unit"] == "ms" and d["value"] > 0
+    assert d["cores"] == (os.cpu_count() or 1) and d["sample"]
+    one = d["single_core"]
+    assert one["cores"] == 1 and one["unit"] == "ms" and one["value"] > 0 and one["sample"]
