@@ -377,6 +377,31 @@ typedef struct lgx_amg lgx_amg;
 lgx_status lgx_amg_setup(const lgx_matrix *a, const lgx_amg_params *p,
                          const lgx_colouring *finest_colouring, lgx_stream stream,
                          lgx_amg **out);
+/* One level's aggregates in host memory, the two halves of
+ * BaseMultithreadAggregateMap (aggregate-map/multithread.hpp:42-45,
+ * 299-303): agg[n] fine->coarse ids (0xFFFFFFFE for an isolated vertex) and
+ * the coarse->fine lists list_ptr[ncoarse + 1] / list[list_ptr[ncoarse]]. */
+typedef struct lgx_agg_map {
+  int64_t n;
+  int64_t ncoarse;
+  const uint32_t *agg;
+  const int64_t *list_ptr;
+  const int32_t *list;
+} lgx_agg_map;
+/* lgx_amg_setup with the strength and aggregation of level k replaced by
+ * maps[k] (FileAggregator, aggregation/independent.hpp:279-298; the stop
+ * rules of hierarchy/wright.hpp:120-143 unchanged).  Every map is checked on
+ * the host before it is copied: fine size equal to the level's rows, ids
+ * below ncoarse or isolated, every aggregated vertex in exactly the list of
+ * its aggregate, no empty aggregate; LGX_ERR_INVALID otherwise, or when a
+ * level needs a map beyond nmaps. */
+/* The checks lgx_amg_setup_given applies to a map for a level of n rows,
+ * on the host alone (no device work): LGX_OK or LGX_ERR_INVALID with the
+ * reason in lgx_last_error. */
+lgx_status lgx_agg_map_check(const lgx_agg_map *m, int64_t n);
+lgx_status lgx_amg_setup_given(const lgx_matrix *a, const lgx_amg_params *p,
+                               const lgx_colouring *finest_colouring, const lgx_agg_map *maps,
+                               int64_t nmaps, lgx_stream stream, lgx_amg **out);
 lgx_status lgx_amg_destroy(lgx_amg *h);
 /* Number of levels, and per level (up to max_levels entries) rows and
  * stored non-zeros. */

@@ -188,6 +188,8 @@ def _signatures(L):
         "lgx_amg_info": [V, P(I64), V, V, I64],
         "lgx_amg_level_download": [V, I64, V, V, V, V, V],
         "lgx_amg_level_lists": [V, I64, V, V, V, V],
+        "lgx_amg_setup_given": [V, P(_AmgParams), V, P(_AggMap), I64, V, P(V)],
+        "lgx_agg_map_check": [P(_AggMap), I64],
         "lgx_amg_vcycle": [V, V, V, V],
         "lgx_matrix_autotune": [V, C.c_int, P(_TuneEntry), V],
         "lgx_amg_autotune": [V, C.c_int, P(_TuneEntry), C.c_int, P(C.c_int), V],
@@ -662,13 +664,56 @@ class HierarchyWright:
             setattr(p, f, int(v) if isinstance(v, bool) else v)
         return p
 
-    def instantiate(self, a: CsrMatrix, finest_colouring: Colouring | None = None) -> "Hierarchy":
+    def instantiate(self, a: CsrMatrix, finest_colouring: Colouring | None = None,
+                    aggregates=None) -> "Hierarchy":
+        """The hierarchy of ``a``.  With ``aggregates`` (per level an
+        ``io.AggregateMap`` or an (agg, list_ptr, list) triple, e.g. from
+        ``io.load_aggregates``) level k takes aggregates[k] instead of
+        computing its aggregation, as lineal's FileAggregator does
+        (aggregation/independent.hpp:279-298)."""
         p = self.params()
         h = C.c_void_p()
-        _check(lib().lgx_amg_setup(a.handle, C.byref(p),
-                                   finest_colouring.handle if finest_colouring else None,
-                                   _stream(), C.byref(h)))
+        col = finest_colouring.handle if finest_colouring else None
+        if aggregates is None:
+            _check(lib().lgx_amg_setup(a.handle, C.byref(p), col, _stream(), C.byref(h)))
+        else:
+            maps, _keep = _agg_maps(aggregates)
+            _check(lib().lgx_amg_setup_given(a.handle, C.byref(p), col, maps, len(_keep) // 3,
+                                             _stream(), C.byref(h)))
         return Hierarchy(h, a)
+
+
+class _AggMap(C.Structure):
+    _fields_ = [("n", C.c_int64), ("ncoarse", C.c_int64), ("agg", C.c_void_p),
+                ("list_ptr", C.c_void_p), ("list", C.c_void_p)]
+
+
+def agg_map_check(m, n: int | None = None) -> None:
+    """The host-side checks of a given aggregate map (lgx_agg_map_check) for
+    a level of n rows (default: the map's own fine size); raises LinealError."""
+    maps, _keep = _agg_maps([m])
+    _check(lib().lgx_agg_map_check(maps, maps[0].n if n is None else int(n)))
+
+
+def _agg_maps(aggregates):
+    """host lgx_agg_map array for lgx_amg_setup_given, plus the arrays it
+    points into (kept alive by the caller)"""
+    keep = []
+    maps = (_AggMap * max(len(aggregates), 1))()
+    for k, (agg, list_ptr, lst) in enumerate(aggregates):
+        agg = np.ascontiguousarray(agg, dtype=np.uint32)
+        list_ptr = np.ascontiguousarray(list_ptr, dtype=np.int64)
+        lst = np.ascontiguousarray(lst, dtype=np.int32)
+        if list_ptr.ndim != 1 or len(list_ptr) < 1:
+            raise ValueError(f"aggregate map {k}: list_ptr needs ncoarse + 1 entries")
+        if int(list_ptr[-1]) > len(lst):
+            raise ValueError(f"aggregate map {k}: list shorter than its offsets say")
+        keep += [agg, list_ptr, lst]
+        maps[k] = _AggMap(len(agg), len(list_ptr) - 1, agg.ctypes.data, list_ptr.ctypes.data,
+                          lst.ctypes.data)
+    if not keep:
+        raise ValueError("no aggregate maps given")
+    return maps, keep
 
 
 class Hierarchy:

@@ -975,8 +975,65 @@ struct PhaseTimer {
   }
 };
 
+// A given aggregate map (host arrays) checked and copied into `out` in place
+// of strength + aggregation (FileAggregator, aggregation/independent.hpp:
+// 279-298).  The checks make it what aggregation produces: every id below
+// ncoarse or isolated, every aggregated vertex in exactly the list of its
+// aggregate, no empty aggregate; the later kernels index with these ids.
+static lgx_status check_map(const lgx_agg_map &m, int64_t n, const std::string &where) {
+  if (m.n != n) return fail(LGX_ERR_INVALID, where + "fine size does not match the level");
+  if (m.ncoarse < 1 && n > 0) return fail(LGX_ERR_INVALID, where + "no aggregates");
+  if (m.ncoarse < 0 || m.ncoarse > (int64_t)kIsolated || (n > 0 && !m.agg) || !m.list_ptr)
+    return fail(LGX_ERR_INVALID, where + "missing arrays or bad coarse size");
+  const int64_t nc = m.ncoarse;
+  if (m.list_ptr[0] != 0) return fail(LGX_ERR_INVALID, where + "list offsets must start at 0");
+  int64_t aggregated = 0;
+  for (int64_t v = 0; v < n; ++v) {
+    if (m.agg[v] == kIsolated) continue;
+    if ((int64_t)m.agg[v] >= nc) return fail(LGX_ERR_INVALID, where + "aggregate id out of range");
+    ++aggregated;
+  }
+  if (m.list_ptr[nc] != aggregated)
+    return fail(LGX_ERR_INVALID, where + "lists do not cover the aggregated vertices");
+  if (aggregated > 0 && !m.list) return fail(LGX_ERR_INVALID, where + "missing lists");
+  std::vector<uint8_t> seen((size_t)std::max<int64_t>(n, 1), 0);
+  for (int64_t c = 0; c < nc; ++c) {
+    if (m.list_ptr[c + 1] <= m.list_ptr[c])
+      return fail(LGX_ERR_INVALID, where + "empty or decreasing aggregate list");
+    for (int64_t k = m.list_ptr[c]; k < m.list_ptr[c + 1]; ++k) {
+      const int32_t v = m.list[k];
+      if (v < 0 || v >= n || seen[(size_t)v] || (int64_t)m.agg[v] != c)
+        return fail(LGX_ERR_INVALID, where + "list entry out of range, repeated or misplaced");
+      seen[(size_t)v] = 1;
+    }
+  }
+  return LGX_OK;
+}
+
+static lgx_status upload_map(const lgx_agg_map &m, int64_t level, int64_t n, cudaStream_t s,
+                             AggResult &out) {
+  LGX_CHECK(check_map(m, n, "aggregate map of level " + std::to_string(level) + ": "));
+  const int64_t nc = m.ncoarse, aggregated = m.list_ptr[nc];
+  LGX_CHECK(out.agg.alloc(n));
+  LGX_CHECK(out.list_ptr.alloc(nc + 1));
+  LGX_CHECK(out.list.alloc(aggregated));
+  if (n > 0)
+    LGX_CUDA(cudaMemcpyAsync(out.agg.p, m.agg, sizeof(uint32_t) * (size_t)n,
+                             cudaMemcpyHostToDevice, s));
+  LGX_CUDA(cudaMemcpyAsync(out.list_ptr.p, m.list_ptr, sizeof(int64_t) * (size_t)(nc + 1),
+                           cudaMemcpyHostToDevice, s));
+  if (aggregated > 0)
+    LGX_CUDA(cudaMemcpyAsync(out.list.p, m.list, sizeof(int32_t) * (size_t)aggregated,
+                             cudaMemcpyHostToDevice, s));
+  LGX_CUDA(cudaStreamSynchronize(s));
+  out.ncoarse = nc;
+  for (auto &x : out.stats) x = 0;
+  return LGX_OK;
+}
+
 static lgx_status amg_build(const lgx_matrix *m, const lgx_amg_params &p,
-                            const lgx_colouring *finest_colouring, cudaStream_t s, lgx_amg &h) {
+                            const lgx_colouring *finest_colouring, const lgx_agg_map *maps,
+                            int64_t nmaps, cudaStream_t s, lgx_amg &h) {
   PhaseTimer timer;
   h.p = p;
   h.f32 = p.cycle_f32 != 0;
@@ -987,16 +1044,23 @@ static lgx_status amg_build(const lgx_matrix *m, const lgx_amg_params &p,
   for (int64_t level = 0;; ++level) {
     lgx_amg_level &fine = *h.lv[level];
     const Csr &a = *fine.a;
-    DBuf<uint8_t> dep, inf, iso;
-    LGX_CHECK(dep.alloc(a.nnz));
-    LGX_CHECK(inf.alloc(a.nnz));
-    LGX_CHECK(iso.alloc(a.n));
-    LGX_CHECK(strength(a, aggressive ? p.aggressive_threshold : p.strong_threshold, dep.p, inf.p,
-                       iso.p, s));
-    timer.mark(s, "strength", level);
-    LGX_CHECK(aggregate(a, dep.p, inf.p, iso.p, p.min_aggregate_size, p.max_aggregate_size,
-                        amg_partitions(a.n, level, p), aggressive, s, fine.agg));
-    timer.mark(s, "aggregate", level);
+    if (maps) {
+      if (level >= nmaps)
+        return fail(LGX_ERR_INVALID, "no aggregate map for level " + std::to_string(level));
+      LGX_CHECK(upload_map(maps[level], level, a.n, s, fine.agg));
+      timer.mark(s, "given map", level);
+    } else {
+      DBuf<uint8_t> dep, inf, iso;
+      LGX_CHECK(dep.alloc(a.nnz));
+      LGX_CHECK(inf.alloc(a.nnz));
+      LGX_CHECK(iso.alloc(a.n));
+      LGX_CHECK(strength(a, aggressive ? p.aggressive_threshold : p.strong_threshold, dep.p,
+                         inf.p, iso.p, s));
+      timer.mark(s, "strength", level);
+      LGX_CHECK(aggregate(a, dep.p, inf.p, iso.p, p.min_aggregate_size, p.max_aggregate_size,
+                          amg_partitions(a.n, level, p), aggressive, s, fine.agg));
+      timer.mark(s, "aggregate", level);
+    }
     if (level < 32)
       for (int k = 0; k < 5; ++k) h.stats[level][k] = fine.agg.stats[k];
     if (fine.agg.ncoarse == 0 && a.n > 0)
@@ -1245,9 +1309,9 @@ void lgx_amg_default_params(lgx_amg_params *p) {
   p->grid27 = 1;
 }
 
-lgx_status lgx_amg_setup(const lgx_matrix *a, const lgx_amg_params *p,
-                         const lgx_colouring *finest_colouring, lgx_stream stream,
-                         lgx_amg **out) {
+static lgx_status amg_setup(const lgx_matrix *a, const lgx_amg_params *p,
+                            const lgx_colouring *finest_colouring, const lgx_agg_map *maps,
+                            int64_t nmaps, lgx_stream stream, lgx_amg **out) {
   if (!a || !p || !out) return fail(LGX_ERR_INVALID, "null argument");
   if (a->kind != LGX_MATRIX_CSR)
     return fail(LGX_ERR_UNSUPPORTED, "AMG setup needs a CSR matrix (assemble stencils first)");
@@ -1260,13 +1324,31 @@ lgx_status lgx_amg_setup(const lgx_matrix *a, const lgx_amg_params *p,
   if (!(p->partition_growth >= 1.0))
     return fail(LGX_ERR_INVALID, "partition_growth must be at least 1");
   auto *h = new lgx_amg();
-  lgx_status st = amg_build(a, *p, finest_colouring, stream, *h);
+  lgx_status st = amg_build(a, *p, finest_colouring, maps, nmaps, stream, *h);
   if (st != LGX_OK) {
     delete h;
     return st;
   }
   *out = h;
   return LGX_OK;
+}
+
+lgx_status lgx_amg_setup(const lgx_matrix *a, const lgx_amg_params *p,
+                         const lgx_colouring *finest_colouring, lgx_stream stream,
+                         lgx_amg **out) {
+  return amg_setup(a, p, finest_colouring, nullptr, 0, stream, out);
+}
+
+lgx_status lgx_agg_map_check(const lgx_agg_map *m, int64_t n) {
+  if (!m) return fail(LGX_ERR_INVALID, "null aggregate map");
+  return check_map(*m, n, "aggregate map: ");
+}
+
+lgx_status lgx_amg_setup_given(const lgx_matrix *a, const lgx_amg_params *p,
+                               const lgx_colouring *finest_colouring, const lgx_agg_map *maps,
+                               int64_t nmaps, lgx_stream stream, lgx_amg **out) {
+  if (!maps || nmaps < 1) return fail(LGX_ERR_INVALID, "no aggregate maps given");
+  return amg_setup(a, p, finest_colouring, maps, nmaps, stream, out);
 }
 
 lgx_status lgx_amg_destroy(lgx_amg *h) {

@@ -132,3 +132,26 @@ def test_damaged_files_are_refused(tmp_path):
     with pytest.raises(ValueError):
         lio.write_aggs(str(tmp_path / "x.aggs"), lio.AggregateMap(*_damaged(maps[0])["owner"]))
     assert not os.path.exists(str(tmp_path / "x.aggs"))
+
+
+def test_library_map_check_agrees_with_the_oracle():
+    """lgx_agg_map_check, the host-side check lgx_amg_setup_given runs
+    before it copies a map to the device, accepts the oracle's maps and
+    refuses every damaged one (no device work: it runs without a GPU)."""
+    import lineal_gb300 as g
+
+    h = lo.Amg(_case(), **PARAMS)
+    for m in _maps(h):
+        g.agg_map_check(m)
+    m = _maps(h)[0]
+    with pytest.raises(g.LinealError, match="fine size"):
+        g.agg_map_check(m, len(m.agg) + 1)
+    for name, d in _damaged(m).items():
+        with pytest.raises(g.LinealError):
+            g.agg_map_check(d)
+    agg, ptr, lst = (np.array(v) for v in m)
+    empty = np.concatenate([ptr[:1], ptr])  # an empty first aggregate
+    with pytest.raises(g.LinealError, match="empty"):
+        g.agg_map_check((np.where(agg == lio.ISOLATED, agg, agg + 1), empty, lst))
+    with pytest.raises(ValueError):
+        g.agg_map_check((agg, ptr, lst[:-1]))  # list shorter than its offsets

@@ -42,3 +42,39 @@ def test_gpu_aggregate_maps_cross_check_the_oracle(cuda, tmp_path):
         np.testing.assert_array_equal(rowptr, rl.rowptr)
         np.testing.assert_array_equal(col, rl.col)
         np.testing.assert_array_equal(val, rl.val)
+
+
+def test_gpu_setup_from_given_maps(cuda, tmp_path):
+    """lgx_amg_setup_given (FileAggregator, aggregation/independent.hpp:
+    279-298): a GPU hierarchy built from the maps of another hierarchy
+    equals it, whatever its own partitioning parameters say."""
+    dims = (12, 14, 16)
+    ref = lo.gen_27pt(dims, np.exp(1.5 * np.random.default_rng(4).standard_normal(
+        int(np.prod(dims)))))
+    m = cuda.CsrMatrix.from_host(ref.rowptr, ref.col, ref.val, symmetric=True)
+    one_part = dict(PARAMS, partition_size=1 << 24, max_partitions=1)
+    b = np.random.default_rng(5).uniform(-1, 1, ref.n)
+    # GPU maps through files -> GPU hierarchy
+    h = cuda.HierarchyWright(**PARAMS).instantiate(m)
+    base = str(tmp_path / "h")
+    h.save_aggregates(base)
+    g = cuda.HierarchyWright(**one_part).instantiate(m, aggregates=lio.load_aggregates(base))
+    assert g.sizes() == h.sizes()
+    np.testing.assert_array_equal(g.vcycle(b).cpu().numpy(), h.vcycle(b).cpu().numpy())
+    # the oracle's maps (64-vertex partitions) -> GPU level matrices = oracle's
+    oh = lo.Amg(ref, smoother_parts=0, **dict(PARAMS, partition_size=64))
+    omaps = [oh.level_map(l) for l in range(oh.nlevels - 1)]
+    go = cuda.HierarchyWright(**one_part).instantiate(m, aggregates=omaps)
+    rows, _ = go.sizes()
+    assert len(rows) == oh.nlevels
+    for l in range(oh.nlevels):
+        rowptr, col, val, _ = go.level(l, with_agg=False)
+        rl = oh.level_csr(l)
+        np.testing.assert_array_equal(rowptr, rl.rowptr)
+        np.testing.assert_array_equal(col, rl.col)
+        np.testing.assert_array_equal(val, rl.val)
+    # too few maps, or a map for another level, are refused before device work
+    with pytest.raises(cuda.LinealError, match="no aggregate map"):
+        cuda.HierarchyWright(**PARAMS).instantiate(m, aggregates=omaps[:1])
+    with pytest.raises(cuda.LinealError, match="fine size"):
+        cuda.HierarchyWright(**PARAMS).instantiate(m, aggregates=omaps[1:])
