@@ -422,6 +422,25 @@ lgx_status lgx_amg_level_download(const lgx_amg *h, int64_t level, int64_t *h_ro
  * `stream`. */
 lgx_status lgx_amg_level_lists(const lgx_amg *h, int64_t level, int64_t *h_list_ptr,
                                int32_t *h_list, int64_t *list_len, lgx_stream stream);
+/* ---- Direct solver ------------------------------------------------------ */
+/* CholeskySolver (direct/cholesky/solver.hpp:22-67, kind
+ * LGX_DIRECT_CHOLESKY) or LuSolver (direct/lu/solver.hpp:21-66, kind
+ * LGX_DIRECT_LU) as the dense FP64 solve the AMG uses on its coarsest level:
+ * lgx_direct_create inverts the CSR matrix once by Gauss-Jordan elimination
+ * without pivoting (Cholesky: every pivot positive, else LGX_ERR_NOT_SPD;
+ * LU: every pivot nonzero and finite, else LGX_ERR_BREAKDOWN — lineal's LU
+ * does not pivot either) and synchronises `stream`; lgx_direct_solve
+ * computes x = A^-1 b with one dense product (b and x distinct device
+ * vectors of n doubles).  Dense storage: n <= LGX_DIRECT_MAX_ROWS. */
+#define LGX_DIRECT_MAX_ROWS 8192
+enum { LGX_DIRECT_CHOLESKY = 0, LGX_DIRECT_LU = 1 };
+typedef struct lgx_direct lgx_direct;
+lgx_status lgx_direct_create(const lgx_matrix *a, int kind, lgx_stream stream,
+                             lgx_direct **out);
+lgx_status lgx_direct_solve(const lgx_direct *d, const double *d_b, double *d_x,
+                            lgx_stream stream);
+lgx_status lgx_direct_destroy(lgx_direct *d);
+
 /* One V-cycle from a zero initial guess: x = M^-1 b (MultiGridSolver::
  * Instance::apply, multigrid/solver.hpp:41-176, REGULAR cycle, 1 iteration). */
 lgx_status lgx_amg_vcycle(lgx_amg *h, const double *d_b, double *d_x, lgx_stream stream);

@@ -70,6 +70,8 @@ template <typename T>
 concept NonStationaryIterativeSolver =
   std::is_base_of_v<SharedNonStationaryIterativeSolverBase, std::decay_t<T>>;
 template <typename T>
+concept DirectSolver = std::is_base_of_v<SharedDirectSolverBase, std::decay_t<T>>;
+template <typename T>
 concept Env = std::is_base_of_v<EnvBase, std::decay_t<T>>;
 
 enum struct IsSymmetric : bool {};
@@ -411,6 +413,49 @@ struct SorSolver : SharedStationaryIterativeSolverBase {
     return Instance{lhs, Colouring(lhs, 0x5eed, env), relax};
   }
 };
+
+// ---- direct solvers (direct/cholesky/solver.hpp:22-67, direct/lu/solver.hpp:21-66)
+// The dense FP64 solve of the AMG's coarsest level on its own: the inverse is
+// formed once by instantiate, each solve is one dense product.  CholeskySolver
+// requires positive pivots (symmetric positive definite matrices), LuSolver
+// nonzero ones (no pivoting, as lineal's LU).
+template <int tKind>
+struct DenseDirectSolver : SharedDirectSolverBase {
+  class Instance {
+   public:
+    static constexpr std::size_t aux_size = 0;
+    Instance(const CsrMatrix &lhs, const Environment &env) : lhs_(&lhs) {
+      check(lgx_direct_create(lhs.handle(), tKind, env.stream(), &h_));
+    }
+    Instance(const Instance &) = delete;
+    Instance &operator=(const Instance &) = delete;
+    Instance(Instance &&o) noexcept : lhs_(o.lhs_), h_(std::exchange(o.h_, nullptr)) {}
+    ~Instance() {
+      if (h_) lgx_direct_destroy(h_);
+    }
+    // sol = lhs^-1 rhs (aux unused: the inverse needs no work vector)
+    template <typename TAux>
+    void solve(DenseVector<double> &sol, const DenseVector<double> &rhs, TAux && /*aux*/,
+               const Environment &env) const {
+      check(lgx_direct_solve(h_, rhs.data(), sol.data(), env.stream()));
+    }
+    void solve(DenseVector<double> &sol, const DenseVector<double> &rhs,
+               const Environment &env) const {
+      check(lgx_direct_solve(h_, rhs.data(), sol.data(), env.stream()));
+    }
+    [[nodiscard]] const CsrMatrix &lhs() const { return *lhs_; }
+
+   private:
+    const CsrMatrix *lhs_;
+    lgx_direct *h_ = nullptr;
+  };
+  Instance instantiate(const CsrMatrix &lhs, const Environment &env) const {
+    return Instance(lhs, env);
+  }
+};
+using CholeskySolver = DenseDirectSolver<LGX_DIRECT_CHOLESKY>;
+using LuSolver = DenseDirectSolver<LGX_DIRECT_LU>;
+static_assert(DirectSolver<CholeskySolver> && DirectSolver<LuSolver>);
 
 // ---- AMG (multigrid/*) -------------------------------------------------------------
 enum struct CycleKind : uint8_t { REGULAR, DECREASING };

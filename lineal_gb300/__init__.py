@@ -185,6 +185,9 @@ def _signatures(L):
         "lgx_sor_sweep_permuted_f32": [V, C.c_float, C.c_int, C.c_int, V, V, V],
         "lgx_amg_setup": [V, P(_AmgParams), V, V, P(V)],
         "lgx_amg_destroy": [V],
+        "lgx_direct_create": [V, C.c_int, V, P(V)],
+        "lgx_direct_solve": [V, V, V, V],
+        "lgx_direct_destroy": [V],
         "lgx_amg_info": [V, P(I64), V, V, I64],
         "lgx_amg_level_download": [V, I64, V, V, V, V, V],
         "lgx_amg_level_lists": [V, I64, V, V, V, V],
@@ -809,6 +812,47 @@ class Hierarchy:
             self.close()
         except Exception:
             pass
+
+
+class DirectSolver:
+    """Dense FP64 direct solver: lineal's CholeskySolver (positive pivots) or
+    LuSolver (nonzero pivots, no pivoting), direct/cholesky/solver.hpp:22-67,
+    direct/lu/solver.hpp:21-66.  ``lu=None`` picks Cholesky for a matrix
+    created symmetric.  The inverse is formed once, each solve is one dense
+    product.  At most DIRECT_MAX_ROWS rows."""
+
+    def __init__(self, a: CsrMatrix, lu: bool | None = None):
+        if lu is None:
+            lu = not a.info()[3]
+        h = C.c_void_p()
+        _check(lib().lgx_direct_create(a.handle, DIRECT_LU if lu else DIRECT_CHOLESKY, _stream(),
+                                       C.byref(h)))
+        self._h = h
+        self._a = a
+        self._n = a.row_num()
+
+    def solve(self, b, out=None):
+        b = _dvec(b)
+        if b.numel() != self._n:
+            raise ValueError(f"right-hand side has {b.numel()} entries, the matrix {self._n} rows")
+        x = out if out is not None else _empty(self._n)
+        _check(lib().lgx_direct_solve(self._h, _ptr(b), _ptr(x), _stream()))
+        return x
+
+    def close(self):
+        if self._h:
+            lib().lgx_direct_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+DIRECT_MAX_ROWS = 8192
+DIRECT_CHOLESKY, DIRECT_LU = 0, 1
 
 
 def amg_strength(a: CsrMatrix, theta: float = 1.0 / 3.0):

@@ -81,12 +81,13 @@ def build(verbose: bool = False, force: bool = False) -> str:
     return LIB
 
 
-def build_cpp_demo(verbose: bool = False) -> str:
-    """Compiles the C++ concept-layer program that drives the library through
+def build_cpp_demo(verbose: bool = False, name: str = "concepts_demo") -> str:
+    """Compiles a C++ concept-layer program of tests/cpp (concepts_demo,
+    direct_demo) that drives the library through
     include/lineal_gb300/lineal.hpp."""
     lib = build(verbose=verbose)
-    src = os.path.join(ROOT, "tests", "cpp", "concepts_demo.cpp")
-    out = os.path.join(OUT_DIR, "concepts_demo")
+    src = os.path.join(ROOT, "tests", "cpp", name + ".cpp")
+    out = os.path.join(OUT_DIR, name)
     if _stale(out, [src, lib, os.path.join(INCLUDE, "lineal_gb300", "lineal.hpp"),
                     os.path.join(INCLUDE, "lineal_gb300.h")]):
         cmd = [nvcc(), "-std=c++20", "-O2", "-I" + INCLUDE, src, "-o", out, "-L" + OUT_DIR,

@@ -839,7 +839,7 @@ __global__ void k_dense_apply(int64_t n, const double *ainv, const XT *b, XT *x)
 // pivot must be positive) or of LuSolver (nonsymmetric: nonzero pivots;
 // lu/decomposition.hpp:31-122 does not pivot either), applied later as one
 // dense product per V-cycle.
-lgx_status dense_inverse(const Csr &a, cudaStream_t s, DBuf<double> &inv) {
+lgx_status dense_inverse(const Csr &a, cudaStream_t s, DBuf<double> &inv, int spd) {
   const int64_t n = a.n;
   LGX_CHECK(inv.alloc(n * n));
   DBuf<double> prow, pcol;
@@ -857,7 +857,7 @@ lgx_status dense_inverse(const Csr &a, cudaStream_t s, DBuf<double> &inv) {
   const unsigned g1 = (unsigned)std::min<int64_t>(grid_for(n, 256), 1024);
   const unsigned g2 = (unsigned)std::min<int64_t>(grid_for(n * n, 256), 4096);
   for (int64_t k = 0; k < n; ++k) {
-    k_gj_pivot<<<g1, 256, 0, s>>>(n, k, inv.p, prow.p, pcol.p, bad.p, a.symmetric);
+    k_gj_pivot<<<g1, 256, 0, s>>>(n, k, inv.p, prow.p, pcol.p, bad.p, spd);
     k_gj_update<<<g2, 256, 0, s>>>(n, k, inv.p, prow.p, pcol.p, bad.p);
   }
   LGX_LAUNCH_CHECK();
@@ -865,9 +865,18 @@ lgx_status dense_inverse(const Csr &a, cudaStream_t s, DBuf<double> &inv) {
   LGX_CUDA(cudaMemcpyAsync(&h_bad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   LGX_CUDA(cudaStreamSynchronize(s));
   if (h_bad)
-    return a.symmetric ? fail(LGX_ERR_NOT_SPD, "coarsest matrix has a non-positive pivot")
-                       : fail(LGX_ERR_BREAKDOWN, "coarsest matrix has a zero pivot");
+    return spd ? fail(LGX_ERR_NOT_SPD, "matrix has a non-positive pivot")
+               : fail(LGX_ERR_BREAKDOWN, "matrix has a zero or non-finite pivot");
   return LGX_OK;
+}
+
+// the coarsest level: CholeskySolver for symmetric hierarchies, LuSolver for
+// nonsymmetric ones (test/aux/default.hpp:160-162)
+lgx_status dense_inverse(const Csr &a, cudaStream_t s, DBuf<double> &inv) {
+  const lgx_status st = dense_inverse(a, s, inv, a.symmetric ? 1 : 0);
+  if (st == LGX_ERR_NOT_SPD || st == LGX_ERR_BREAKDOWN)
+    return fail(st, "coarsest " + std::string(lgx_last_error()));
+  return st;
 }
 
 // ===========================================================================
@@ -1427,6 +1436,51 @@ lgx_status lgx_amg_level_lists(const lgx_amg *h, int64_t level, int64_t *h_list_
                              cudaMemcpyDeviceToHost, stream));
     LGX_CUDA(cudaStreamSynchronize(stream));
   }
+  return LGX_OK;
+}
+
+// Standalone dense direct solver: the coarsest-level solve on its own
+// (CholeskySolver / LuSolver, direct/cholesky/solver.hpp:22-67,
+// direct/lu/solver.hpp:21-66): the explicit inverse once, then one dense
+// product per solve.
+struct lgx_direct {
+  int64_t n = 0;
+  lgx::DBuf<double> inv;
+};
+
+lgx_status lgx_direct_create(const lgx_matrix *a, int kind, lgx_stream stream,
+                             lgx_direct **out) {
+  if (!a || !out) return fail(LGX_ERR_INVALID, "null argument");
+  if (kind != LGX_DIRECT_CHOLESKY && kind != LGX_DIRECT_LU)
+    return fail(LGX_ERR_INVALID, "kind must be LGX_DIRECT_CHOLESKY or LGX_DIRECT_LU");
+  if (a->kind != LGX_MATRIX_CSR)
+    return fail(LGX_ERR_UNSUPPORTED, "the direct solver needs a CSR matrix");
+  if (a->csr.n > LGX_DIRECT_MAX_ROWS)
+    return fail(LGX_ERR_INVALID, "the dense direct solver takes at most " +
+                                     std::to_string(LGX_DIRECT_MAX_ROWS) + " rows");
+  auto d = std::make_unique<lgx_direct>();
+  d->n = a->csr.n;
+  LGX_CHECK(dense_inverse(a->csr, (cudaStream_t)stream, d->inv, kind == LGX_DIRECT_CHOLESKY));
+  *out = d.release();
+  return LGX_OK;
+}
+
+lgx_status lgx_direct_solve(const lgx_direct *d, const double *d_b, double *d_x,
+                            lgx_stream stream) {
+  if (!d) return fail(LGX_ERR_INVALID, "null solver");
+  if (d->n == 0) return LGX_OK;
+  if (!d_b || !d_x) return fail(LGX_ERR_INVALID, "null vector");
+  if (d_b == d_x) return fail(LGX_ERR_INVALID, "b and x must not be the same vector");
+  const cudaStream_t s = (cudaStream_t)stream;
+  LGX_CUDA(launch_pdl(false, k_dense_apply<double>,
+                      dim3((unsigned)std::min<int64_t>(grid_for(d->n * 32, 256), 4096)), dim3(256),
+                      0, s, d->n, (const double *)d->inv.p, d_b, d_x));
+  count_launch();
+  return LGX_OK;
+}
+
+lgx_status lgx_direct_destroy(lgx_direct *d) {
+  delete d;
   return LGX_OK;
 }
 

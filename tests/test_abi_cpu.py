@@ -59,6 +59,9 @@ def test_invalid_arguments_are_statuses(library):
     assert lib.lgx_matrix_autotune(None, 5, None, None) == 1
     assert lib.lgx_amg_autotune(None, 5, None, 0, None, None) == 1
     assert lib.lgx_amg_level_lists(None, 0, None, None, None, None) == 1
+    assert lib.lgx_direct_create(None, 0, None, None) == 1
+    assert lib.lgx_direct_solve(None, None, None, None) == 1
+    assert lib.lgx_direct_destroy(None) == 0
     assert lib.lgx_amg_autotune_reset(None) == 1
     assert b"null" in lib.lgx_last_error()
 
@@ -68,5 +71,6 @@ def test_concept_layer_compiles_and_links(library):
     one the GPU suite runs) and links against the library."""
     from lineal_gb300 import build
 
-    exe = build.build_cpp_demo()
-    assert os.path.isfile(exe) and os.access(exe, os.X_OK)
+    for name in ("concepts_demo", "direct_demo"):
+        exe = build.build_cpp_demo(name=name)
+        assert os.path.isfile(exe) and os.access(exe, os.X_OK)

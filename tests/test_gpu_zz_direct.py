@@ -1,0 +1,85 @@
+"""The standalone dense direct solver (lgx_direct_*: CholeskySolver and
+LuSolver, direct/cholesky/solver.hpp:22-67, direct/lu/solver.hpp:21-66)
+against the reference's Cholesky golden solve and the UFZ_CT_02 system, its
+refusals, and the C++ concept layer's CholeskySolver/LuSolver program."""
+
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle as lo
+from lineal_gb300 import io as lio
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(cuda, a, symmetric):
+    return cuda.CsrMatrix.from_host(a.rowptr, a.col, a.val, symmetric=symmetric)
+
+
+def test_cholesky_golden_solve(cuda, golden_dir):
+    c = np.load(os.path.join(golden_dir, "cholesky_python_reference.npz"))
+    lhs = c["lhs"]
+    rows, cols = np.nonzero(lhs)
+    rowptr = np.zeros(lhs.shape[0] + 1, dtype=np.int64)
+    np.add.at(rowptr, rows + 1, 1)
+    a = lo.Csr(np.cumsum(rowptr), cols.astype(np.int32), lhs[rows, cols])
+    d = cuda.DirectSolver(_dev(cuda, a, True))
+    x = d.solve(c["rhs"]).cpu().numpy()
+    # test/python-reference/cholesky.py's solution; an explicit inverse
+    # carries about cond(A) * eps (cond 441)
+    np.testing.assert_allclose(x, c["sol"], rtol=0, atol=1e-12 * np.abs(c["sol"]).max())
+
+
+@pytest.mark.parametrize("lu", [True, False])
+def test_ufz_system(cuda, golden_dir, lu):
+    rowptr, col, val, _ = lio.read_smf(os.path.join(golden_dir, "UFZ_CT_02_LHS.smf"))
+    b = lio.read_dvf(os.path.join(golden_dir, "UFZ_CT_02_RHS.dvf"))
+    a = lo.Csr(rowptr, col, val, symmetric=False)
+    d = cuda.DirectSolver(_dev(cuda, a, False), lu=lu)
+    x = d.solve(b).cpu().numpy()
+    assert np.linalg.norm(b - lo.spmv(a, x)) <= 1e-12 * np.linalg.norm(b)
+    # against the oracle's unpivoted LU (lu/decomposition.hpp)
+    ref = lo.lu_solve(lo.lu_factor(a), b)
+    np.testing.assert_allclose(x, ref, rtol=0, atol=1e-12 * np.abs(ref).max())
+
+
+def _tridiagonal(n, lower, diag, upper):
+    rowptr, col, val = [0], [], []
+    for i in range(n):
+        for j, v in ((i - 1, lower), (i, diag), (i + 1, upper)):
+            if 0 <= j < n:
+                col.append(j)
+                val.append(v)
+        rowptr.append(len(col))
+    return lo.Csr(np.array(rowptr, np.int64), np.array(col, np.int32), np.array(val))
+
+
+def test_refusals(cuda):
+    indefinite = _dev(cuda, _tridiagonal(8, -1.0, 0.5, -1.0), True)
+    with pytest.raises(cuda.LinealError, match="non-positive pivot"):
+        cuda.DirectSolver(indefinite, lu=False)
+    lu = cuda.DirectSolver(indefinite, lu=True)
+    x = lu.solve(np.ones(8)).cpu().numpy()
+    a = _tridiagonal(8, -1.0, 0.5, -1.0)
+    assert np.linalg.norm(1.0 - lo.spmv(a, x)) <= 1e-12 * np.sqrt(8)
+    zero_pivot = _dev(cuda, _tridiagonal(6, 1.0, 0.0, 1.0), False)
+    with pytest.raises(cuda.LinealError, match="zero or non-finite pivot"):
+        cuda.DirectSolver(zero_pivot, lu=True)
+    big = cuda.gen_7pt((32, 32, 9), np.ones(32 * 32 * 9))
+    with pytest.raises(cuda.LinealError, match="at most"):
+        cuda.DirectSolver(big)
+    d = cuda.DirectSolver(_dev(cuda, _tridiagonal(4, -1.0, 2.0, -1.0), True))
+    with pytest.raises(ValueError):
+        d.solve(np.ones(5))
+
+
+def test_cpp_direct_solvers(cuda):
+    from lineal_gb300 import build
+
+    exe = build.build_cpp_demo(name="direct_demo")
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert "direct_demo ok" in out.stdout
