@@ -263,6 +263,16 @@ lgx_status lgx_dot_static(int64_t n, const double *d_a, const double *d_b, doubl
 lgx_status lgx_max_norm(int64_t n, const double *d_a, double *d_out, lgx_stream stream);
 /* y = y + alpha * x */
 lgx_status lgx_axpy(int64_t n, double alpha, const double *d_x, double *d_y, lgx_stream stream);
+/* out = alpha x + beta y, each product and the sum rounded separately, so
+ * that add(x, y) (alpha = beta = 1), subtract(x, y) (beta = -1),
+ * scale(x, alpha) (d_y = NULL) and add/subtract of scaled vectors give the
+ * bits of lineal's expression evaluation (component-wise/
+ * vector-expression.hpp:67-91, 150-167).  out may be x or y. */
+lgx_status lgx_lincomb(int64_t n, double alpha, const double *d_x, double beta,
+                       const double *d_y, double *d_out, lgx_stream stream);
+/* out = value everywhere (constant / constant_like, vector-expression.hpp:
+ * 140-147, assigned) */
+lgx_status lgx_fill(int64_t n, double value, double *d_out, lgx_stream stream);
 
 /* ------------------------------------------------------------------------
  * Smoothers (linear-solver/iterative-stationary/).

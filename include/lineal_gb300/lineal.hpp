@@ -24,6 +24,7 @@
 #include <optional>
 #include <stdexcept>
 #include <string>
+#include <tuple>
 #include <type_traits>
 #include <utility>
 #include <vector>
@@ -309,6 +310,89 @@ void assign(DenseVector<double> &y, const MatrixVectorProductExpr<TLhs, TRhs> &e
   check(lgx_spmv(e.lhs.handle(), e.rhs.data(), y.data(), pol.stream));
 }
 
+// add / subtract / scale and operator+ - * (component-wise/vector-expression.hpp:
+// 67-91, 150-167): a vector, a scaled vector, or the sum or difference of two
+// of them, assigned in one pass with lineal's rounding (each product and the
+// sum rounded once, lgx_lincomb); constant / constant_like (140-147) assign a
+// value.  Deeper trees (a scaled sum, three terms) are not expressions here.
+struct ScaledVector {
+  double scalar;
+  const DenseVector<double> *vec;
+};
+struct LinCombExpr {
+  double alpha;
+  const DenseVector<double> *x;
+  double beta;
+  const DenseVector<double> *y;
+};
+struct ConstantExpr {
+  std::size_t size;
+  double value;
+};
+
+template <typename T>
+concept LinTerm = std::same_as<std::decay_t<T>, DenseVector<double>> ||
+                  std::same_as<std::decay_t<T>, ScaledVector>;
+
+namespace detail {
+inline ScaledVector term(const DenseVector<double> &v) { return {1.0, &v}; }
+inline ScaledVector term(const ScaledVector &t) { return t; }
+}  // namespace detail
+
+inline ScaledVector scale(const DenseVector<double> &v, double scalar) { return {scalar, &v}; }
+inline ScaledVector operator*(const DenseVector<double> &v, double scalar) { return {scalar, &v}; }
+inline ScaledVector operator*(double scalar, const DenseVector<double> &v) { return {scalar, &v}; }
+template <LinTerm A, LinTerm B>
+LinCombExpr add(const A &a, const B &b) {
+  const ScaledVector ta = detail::term(a), tb = detail::term(b);
+  return {ta.scalar, ta.vec, tb.scalar, tb.vec};
+}
+template <LinTerm A, LinTerm B>
+LinCombExpr subtract(const A &a, const B &b) {
+  const ScaledVector ta = detail::term(a), tb = detail::term(b);
+  return {ta.scalar, ta.vec, -tb.scalar, tb.vec};
+}
+template <LinTerm A, LinTerm B>
+LinCombExpr operator+(const A &a, const B &b) {
+  return add(a, b);
+}
+template <LinTerm A, LinTerm B>
+LinCombExpr operator-(const A &a, const B &b) {
+  return subtract(a, b);
+}
+inline ConstantExpr constant(std::size_t size, double value) { return {size, value}; }
+inline ConstantExpr constant_like(const DenseVector<double> &v, double value) {
+  return {v.size(), value};
+}
+
+namespace detail {
+inline void same_size(std::size_t a, std::size_t b) {
+  if (a != b) throw Error(LGX_ERR_INVALID, "lineal_gb300: vector sizes differ");
+}
+}  // namespace detail
+
+inline void assign(DenseVector<double> &out, const LinCombExpr &e, const DevicePolicy &pol) {
+  detail::same_size(out.size(), e.x->size());
+  detail::same_size(out.size(), e.y->size());
+  check(lgx_lincomb((int64_t)out.size(), e.alpha, e.x->data(), e.beta, e.y->data(), out.data(),
+                    pol.stream));
+}
+inline void assign(DenseVector<double> &out, const ScaledVector &e, const DevicePolicy &pol) {
+  detail::same_size(out.size(), e.vec->size());
+  check(lgx_lincomb((int64_t)out.size(), e.scalar, e.vec->data(), 0.0, nullptr, out.data(),
+                    pol.stream));
+}
+inline void assign(DenseVector<double> &out, const ConstantExpr &e, const DevicePolicy &pol) {
+  detail::same_size(out.size(), e.size);
+  check(lgx_fill((int64_t)out.size(), e.value, out.data(), pol.stream));
+}
+
+// swap (sink/swap.hpp:31-123): the contents change places (here the storage)
+inline void swap(DenseVector<double> &a, DenseVector<double> &b, const DevicePolicy & /*pol*/) {
+  detail::same_size(a.size(), b.size());
+  std::swap(a, b);
+}
+
 inline double scalar_from_device(const double *d, cudaStream_t s) {
   double h = 0.0;
   check_cuda(cudaMemcpyAsync(&h, d, sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -336,6 +420,61 @@ TReal max_norm(const DenseVector<double> &a, const DevicePolicy &pol) {
   DenseVector<double> out(1);
   check(lgx_max_norm((int64_t)a.size(), a.data(), out.data(), pol.stream));
   return scalar_from_device(out.data(), pol.stream);
+}
+
+// multiconsume with dot / euclidean_squared / euclidean_norm / max_norm
+// consumers (sink/accumulator.hpp:126-218): the consumers name the vectors
+// they read by position; each consumer is one deterministic reduction
+// (lineal fuses them into one pass; the values are the same reductions)
+template <typename TReal, std::size_t tI, std::size_t tJ>
+struct DotConsumer {};
+template <typename TReal, std::size_t tI>
+struct EuclideanSquaredConsumer {};
+template <typename TReal, std::size_t tI>
+struct EuclideanNormConsumer {};
+template <typename TReal, std::size_t tI>
+struct MaxNormConsumer {};
+template <typename TReal, std::size_t tI, std::size_t tJ>
+constexpr DotConsumer<TReal, tI, tJ> dot_consumer() {
+  return {};
+}
+template <typename TReal, std::size_t tI>
+constexpr EuclideanSquaredConsumer<TReal, tI> euclidean_squared_consumer() {
+  return {};
+}
+template <typename TReal, std::size_t tI>
+constexpr EuclideanNormConsumer<TReal, tI> euclidean_norm_consumer() {
+  return {};
+}
+template <typename TReal, std::size_t tI>
+constexpr MaxNormConsumer<TReal, tI> max_norm_consumer() {
+  return {};
+}
+
+namespace detail {
+template <typename TReal, std::size_t tI, std::size_t tJ, typename TVecs>
+TReal consume(DotConsumer<TReal, tI, tJ>, const TVecs &v, const DevicePolicy &pol) {
+  return dot<TReal>(std::get<tI>(v), std::get<tJ>(v), pol);
+}
+template <typename TReal, std::size_t tI, typename TVecs>
+TReal consume(EuclideanSquaredConsumer<TReal, tI>, const TVecs &v, const DevicePolicy &pol) {
+  return euclidean_squared<TReal>(std::get<tI>(v), pol);
+}
+template <typename TReal, std::size_t tI, typename TVecs>
+TReal consume(EuclideanNormConsumer<TReal, tI>, const TVecs &v, const DevicePolicy &pol) {
+  return euclidean_norm<TReal>(std::get<tI>(v), pol);
+}
+template <typename TReal, std::size_t tI, typename TVecs>
+TReal consume(MaxNormConsumer<TReal, tI>, const TVecs &v, const DevicePolicy &pol) {
+  return max_norm<TReal>(std::get<tI>(v), pol);
+}
+}  // namespace detail
+
+template <typename... TConsumers, typename... TVecs>
+auto multiconsume(std::tuple<TConsumers...> consumers, std::tuple<TVecs...> vecs,
+                  const DevicePolicy &pol) {
+  return std::apply(
+    [&](auto... c) { return std::tuple{detail::consume(c, vecs, pol)...}; }, consumers);
 }
 
 // ---- stationary solvers (iterative-stationary/*) --------------------------------

@@ -186,6 +186,8 @@ def _signatures(L):
         "lgx_amg_setup": [V, P(_AmgParams), V, V, P(V)],
         "lgx_amg_destroy": [V],
         "lgx_direct_create": [V, C.c_int, V, P(V)],
+        "lgx_lincomb": [I64, D, V, D, V, V, V],
+        "lgx_fill": [I64, D, V, V],
         "lgx_direct_solve": [V, V, V, V],
         "lgx_direct_destroy": [V],
         "lgx_amg_info": [V, P(I64), V, V, I64],
@@ -506,6 +508,27 @@ def max_norm(a) -> float:
     out = _empty(1)
     _check(lib().lgx_max_norm(a.numel(), _ptr(a), _ptr(out), _stream()))
     return float(out.item())
+
+
+def lincomb(alpha: float, x, beta: float = 0.0, y=None, out=None):
+    """alpha x + beta y (y None: alpha x) with each product and the sum
+    rounded on its own, the bits of lineal's add / subtract / scale
+    expressions (component-wise/vector-expression.hpp:67-91)."""
+    x = _dvec(x)
+    if y is not None:
+        y = _dvec(y)
+        if y.numel() != x.numel():
+            raise ValueError("x and y differ in size")
+    out = out if out is not None else _empty(x.numel())
+    _check(lib().lgx_lincomb(x.numel(), float(alpha), _ptr(x), float(beta), _ptr(y), _ptr(out),
+                             _stream()))
+    return out
+
+
+def fill(n: int, value: float, out=None):
+    out = out if out is not None else _empty(n)
+    _check(lib().lgx_fill(out.numel(), float(value), _ptr(out), _stream()))
+    return out
 
 
 def jacobi_sweep(a: _Matrix, b, x_in=None, relax=1.0):

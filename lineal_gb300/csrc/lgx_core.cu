@@ -343,6 +343,24 @@ __global__ void k_axpy(int64_t n, double alpha, const double *x, double *y) {
     y[i] = fma(x[i], alpha, y[i]);
 }
 
+// out = alpha x + beta y with the products and the sum rounded one by one
+// (no contraction into an fma): the rounding of lineal's expression trees
+// add / subtract / scale (component-wise/vector-expression.hpp:67-91)
+__global__ void k_lincomb(int64_t n, double alpha, const double *x, double beta, const double *y,
+                          double *out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double ax = __dmul_rn(alpha, x[i]);
+    out[i] = y ? __dadd_rn(ax, __dmul_rn(beta, y[i])) : ax;
+  }
+}
+
+__global__ void k_fill(int64_t n, double value, double *out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = value;
+}
+
 template <typename T, typename U>
 __global__ void k_gather(int64_t n, const int32_t *idx, const T *src, U *dst) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -747,6 +765,26 @@ lgx_status lgx_axpy(int64_t n, double alpha, const double *d_x, double *d_y, lgx
   if (n == 0) return LGX_OK;
   k_axpy<<<std::min<int64_t>(grid_for(n, 256), 8192), 256, 0, stream>>>(n, alpha, d_x, d_y);
   LGX_LAUNCH_CHECK();
+  return LGX_OK;
+}
+
+lgx_status lgx_lincomb(int64_t n, double alpha, const double *d_x, double beta,
+                       const double *d_y, double *d_out, lgx_stream stream) {
+  if (n < 0 || (n > 0 && (!d_x || !d_out))) return fail(LGX_ERR_INVALID, "bad argument");
+  if (n == 0) return LGX_OK;
+  k_lincomb<<<std::min<int64_t>(grid_for(n, 256), 8192), 256, 0, stream>>>(n, alpha, d_x, beta,
+                                                                           d_y, d_out);
+  LGX_LAUNCH_CHECK();
+  count_launch();
+  return LGX_OK;
+}
+
+lgx_status lgx_fill(int64_t n, double value, double *d_out, lgx_stream stream) {
+  if (n < 0 || (n > 0 && !d_out)) return fail(LGX_ERR_INVALID, "bad argument");
+  if (n == 0) return LGX_OK;
+  k_fill<<<std::min<int64_t>(grid_for(n, 256), 8192), 256, 0, stream>>>(n, value, d_out);
+  LGX_LAUNCH_CHECK();
+  count_launch();
   return LGX_OK;
 }
 

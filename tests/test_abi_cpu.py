@@ -62,6 +62,9 @@ def test_invalid_arguments_are_statuses(library):
     assert lib.lgx_direct_create(None, 0, None, None) == 1
     assert lib.lgx_direct_solve(None, None, None, None) == 1
     assert lib.lgx_direct_destroy(None) == 0
+    assert lib.lgx_lincomb(-1, 1.0, None, 1.0, None, None, None) == 1
+    assert lib.lgx_lincomb(0, 1.0, None, 1.0, None, None, None) == 0
+    assert lib.lgx_fill(5, 1.0, None, None) == 1
     assert lib.lgx_amg_autotune_reset(None) == 1
     assert b"null" in lib.lgx_last_error()
 
@@ -71,6 +74,6 @@ def test_concept_layer_compiles_and_links(library):
     one the GPU suite runs) and links against the library."""
     from lineal_gb300 import build
 
-    for name in ("concepts_demo", "direct_demo"):
+    for name in ("concepts_demo", "direct_demo", "vector_demo"):
         exe = build.build_cpp_demo(name=name)
         assert os.path.isfile(exe) and os.access(exe, os.X_OK)
