@@ -500,6 +500,21 @@ struct JacobiSolver : SharedStationaryIterativeSolverBase {
       check(lgx_jacobi_sweep(lhs.handle(), relax, in ? in->data() : nullptr, out.data(),
                              rhs.data(), env.stream()));
     }
+    // lineal's call shapes (SingleSweepImpl, broom.hpp:36-51): ex situ with
+    // an aux tuple, and in situ, where sol moves to aux[0] and the sweep
+    // writes sol
+    template <typename TAux>
+    void apply(const DenseVector<double> &in, DenseVector<double> &out,
+               const DenseVector<double> &rhs, TAux && /*aux*/, const Environment &env) const {
+      apply(&in, out, rhs, env);
+    }
+    template <typename TAux>
+    void apply(DenseVector<double> &sol, const DenseVector<double> &rhs, TAux &&aux,
+               const Environment &env) const {
+      DenseVector<double> &tmp = std::get<0>(aux);
+      swap(sol, tmp, env.execution_policy());
+      apply(&tmp, sol, rhs, env);
+    }
   };
   template <AnyMatrix TLhs>
   Instance<TLhs> instantiate(const TLhs &lhs, const Environment & /*env*/) const {
@@ -546,6 +561,21 @@ struct SorSolver : SharedStationaryIterativeSolverBase {
     void apply(DenseVector<double> &sol, const DenseVector<double> &rhs,
                const Environment &env) const {
       apply(&sol, sol, rhs, env);
+    }
+    // lineal's call shapes with an aux tuple (broom.hpp:36-51); in situ, sol
+    // moves to aux[0] and the sweep writes sol (the multicolour sweep gives
+    // the same bits in place)
+    template <typename TAux>
+    void apply(const DenseVector<double> &in, DenseVector<double> &out,
+               const DenseVector<double> &rhs, TAux && /*aux*/, const Environment &env) const {
+      apply(&in, out, rhs, env);
+    }
+    template <typename TAux>
+    void apply(DenseVector<double> &sol, const DenseVector<double> &rhs, TAux &&aux,
+               const Environment &env) const {
+      DenseVector<double> &tmp = std::get<0>(aux);
+      swap(sol, tmp, env.execution_policy());
+      apply(&tmp, sol, rhs, env);
     }
   };
   Instance instantiate(const CsrMatrix &lhs, const Environment &env) const {
@@ -672,6 +702,16 @@ struct MultiGridSolver : SharedStationaryIterativeSolverBase {
     void apply(DenseVector<double> &out, const DenseVector<double> &rhs,
                const Environment &env) const {
       check(lgx_amg_vcycle(h_, rhs.data(), out.data(), env.stream()));
+    }
+    // lineal's call shape apply(constant_like(out, 0), out, rhs, aux, env)
+    // (multigrid/solver.hpp:41-56); the cycle starts from zero only
+    template <typename TAux>
+    void apply(const ConstantExpr &in, DenseVector<double> &out, const DenseVector<double> &rhs,
+               TAux && /*aux*/, const Environment &env) const {
+      if (in.value != 0.0 || in.size != out.size())
+        throw Error(LGX_ERR_UNSUPPORTED,
+                    "lineal_gb300: MultiGridSolver applies from a zero initial guess");
+      apply(out, rhs, env);
     }
     [[nodiscard]] lgx_amg *handle() const { return h_; }
     [[nodiscard]] std::size_t level_num() const {

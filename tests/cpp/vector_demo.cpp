@@ -2,7 +2,8 @@
 // vector-expression.hpp: add, subtract, scale, operator+ - *, constant,
 // constant_like; sink/swap.hpp: swap; sink/accumulator.hpp: multiconsume
 // with its consumers) against host arithmetic with lineal's rounding: every
-// product and every sum rounded on its own.
+// product and every sum rounded on its own; and the aux-tuple call shapes of
+// the stationary solvers (iterative-stationary/broom.hpp:36-51).
 //
 // Output: one line "vector_demo ok" (exit status 0) or the first mismatch
 // (exit status 1).
@@ -108,6 +109,47 @@ int main() {
       lg::assign(small, da + db, pol);
     } catch (const lg::Error &) {
       refused = true;
+    }
+    // lineal's stationary-solver call shapes with an aux tuple (broom.hpp:
+    // 36-51): in situ equals ex situ bit for bit, and aux receives the old
+    // solution; MultiGridSolver from constant_like(out, 0)
+    {
+      const int64_t dims[3] = {8, 8, 8};
+      const std::size_t m = 512;
+      std::vector<double> k(m), x0(m), rb(m);
+      for (auto &v : k) v = std::exp(uni(rng));
+      for (auto &v : x0) v = uni(rng);
+      for (auto &v : rb) v = uni(rng);
+      lg::DenseVector<double> kd(m, env), rhs(m, env), in(m, env), ex(m, env), sol(m, env),
+        tmp(m, env);
+      kd.upload(k, env);
+      rhs.upload(rb, env);
+      in.upload(x0, env);
+      const auto lhs = lg::CsrMatrix::diffusion_27pt(dims, kd, env);
+      auto check_shapes = [&](const auto &inst, const char *what) {
+        inst.apply(in, ex, rhs, std::tuple<>{}, env);
+        sol.upload(x0, env);
+        inst.apply(sol, rhs, std::tie(tmp), env);
+        const auto want = ex.download(env);
+        ok = ok && same(sol.download(env), [&](std::size_t i) { return want[i]; }, what);
+        ok = ok && same(tmp.download(env), [&](std::size_t i) { return x0[i]; }, what);
+      };
+      check_shapes(lg::JacobiSolver{0.8}.instantiate(lhs, env), "jacobi in situ");
+      check_shapes(lg::SorSolver<lg::forward_tag_t>{1.0}.instantiate(lhs, env), "sor in situ");
+      lg::MultiGridSolver mg;
+      mg.hierarchy.min_coarsen_size = 20;
+      const auto amg = mg.instantiate(lhs, env);
+      amg.apply(lg::constant_like(ex, 0.0), ex, rhs, std::tuple<>{}, env);
+      amg.apply(sol, rhs, env);
+      const auto want = sol.download(env);
+      ok = ok && same(ex.download(env), [&](std::size_t i) { return want[i]; }, "amg apply");
+      bool nonzero_refused = false;
+      try {
+        amg.apply(lg::constant_like(ex, 1.0), ex, rhs, std::tuple<>{}, env);
+      } catch (const lg::Error &) {
+        nonzero_refused = true;
+      }
+      ok = ok && nonzero_refused;
     }
     if (!ok || !refused) return 1;
     std::printf("vector_demo ok\n");
