@@ -422,6 +422,27 @@ lgx_status lgx_amg_info(const lgx_amg *h, int64_t *nlevels, int64_t *rows, int64
 lgx_status lgx_amg_level_download(const lgx_amg *h, int64_t level, int64_t *h_rowptr,
                                   int32_t *h_col, double *h_val, uint32_t *h_agg,
                                   lgx_stream stream);
+/* What lineal's hierarchy setup logs (hierarchy/wright.hpp:26-31, 120-143,
+ * 210-225; aggregation/stats.hpp:16-32), per level in level order: the
+ * dimensions, the stored non-zeros, the aggregation statistics of the level
+ * (zero on the coarsest level and for levels built from given maps), and
+ * whether the level was aggregated with the aggressive threshold; plus why
+ * coarsening stopped.  Host data only. */
+typedef struct lgx_amg_level_log {
+  int64_t rows, columns, nnz;
+  int64_t aggregate_num, multi_vertex_aggregate_num, single_vertex_aggregate_num,
+    merged_aggregate_num, isolated_aggregate_num;
+  int32_t aggressive;
+  int32_t given_map;
+} lgx_amg_level_log;
+enum {
+  LGX_STOP_TOO_SMALL = 1,       /* coarse size below min_coarsen_size */
+  LGX_STOP_TOO_MANY_LEVELS = 2, /* max_level_num reached */
+  LGX_STOP_TOO_SMALL_RATE = 3,  /* coarsening factor too small while aggressive */
+  LGX_STOP_LEVEL_CAP = 4        /* this library's 32-level storage limit */
+};
+lgx_status lgx_amg_setup_log(const lgx_amg *h, lgx_amg_level_log *levels, int64_t max_levels,
+                             int64_t *nlevels, int32_t *stop_reason);
 /* Coarse->fine lists of `level`'s aggregates (BaseMultithreadAggregateMap::
  * coarse_row_to_fine_rows, aggregate-map/multithread.hpp:337-344; with the
  * fine->coarse map of lgx_amg_level_download, what to_file writes, 346-349):

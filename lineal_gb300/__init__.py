@@ -70,6 +70,16 @@ class _TuneEntry(C.Structure):
                 "ms": [float(t) for t in self.ms]}
 
 
+class _AmgLevelLog(C.Structure):
+    _fields_ = [(f, C.c_int64) for f in (
+        "rows", "columns", "nnz", "aggregate_num", "multi_vertex_aggregate_num",
+        "single_vertex_aggregate_num", "merged_aggregate_num", "isolated_aggregate_num")] + [
+        ("aggressive", C.c_int32), ("given_map", C.c_int32)]
+
+
+STOP_REASONS = {1: "too_small", 2: "too_many_levels", 3: "too_small_rate", 4: "level_cap"}
+
+
 class _AmgParams(C.Structure):
     _fields_ = [
         ("min_aggregate_size", C.c_int32),
@@ -193,6 +203,7 @@ def _signatures(L):
         "lgx_amg_info": [V, P(I64), V, V, I64],
         "lgx_amg_level_download": [V, I64, V, V, V, V, V],
         "lgx_amg_level_lists": [V, I64, V, V, V, V],
+        "lgx_amg_setup_log": [V, P(_AmgLevelLog), I64, P(I64), P(C.c_int32)],
         "lgx_amg_setup_given": [V, P(_AmgParams), V, P(_AggMap), I64, V, P(V)],
         "lgx_agg_map_check": [P(_AggMap), I64],
         "lgx_amg_vcycle": [V, V, V, V],
@@ -771,6 +782,31 @@ class Hierarchy:
         _check(lib().lgx_amg_level_download(self._h, l, _ptr(rowptr), _ptr(col), _ptr(val),
                                             _ptr(agg), _stream()))
         return rowptr, col, val, agg
+
+    def setup_log(self) -> dict:
+        """The hierarchy setup in the shape of lineal's JSON log
+        (hierarchy/wright.hpp:26-31, 120-143, 210-225; aggregation/stats.hpp:
+        16-32): per level its dimensions, non-zeros, aggregation statistics
+        and aggressive mode, and why coarsening stopped."""
+        cap = 32
+        levels = (_AmgLevelLog * cap)()
+        n, reason = C.c_int64(), C.c_int32()
+        _check(lib().lgx_amg_setup_log(self._h, levels, cap, C.byref(n), C.byref(reason)))
+        out = []
+        for l in range(min(n.value, cap)):
+            e = levels[l]
+            entry = {"dimensions": {"rows": e.rows, "columns": e.columns}, "non_zeros": e.nnz}
+            if l + 1 < n.value:
+                entry["aggressive"] = bool(e.aggressive)
+                entry["given_map"] = bool(e.given_map)
+                entry["aggregation_stats"] = {
+                    k: getattr(e, k) for k in (
+                        "aggregate_num", "multi_vertex_aggregate_num",
+                        "single_vertex_aggregate_num", "merged_aggregate_num",
+                        "isolated_aggregate_num")}
+            out.append(entry)
+        return {"create_hierarchy": {"levels": out, "stop_coarsening": {
+            "reason": STOP_REASONS.get(reason.value, "unknown")}}}
 
     def aggregate_map(self, l: int):
         """Level l's aggregates as an ``io.AggregateMap``: the fine -> coarse

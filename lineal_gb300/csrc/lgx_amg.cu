@@ -1053,6 +1053,10 @@ static lgx_status amg_build(const lgx_matrix *m, const lgx_amg_params &p,
   for (int64_t level = 0;; ++level) {
     lgx_amg_level &fine = *h.lv[level];
     const Csr &a = *fine.a;
+    if (level < 32) {
+      h.aggressive[level] = aggressive;
+      h.given[level] = maps != nullptr;
+    }
     if (maps) {
       if (level >= nmaps)
         return fail(LGX_ERR_INVALID, "no aggregate map for level " + std::to_string(level));
@@ -1084,12 +1088,23 @@ static lgx_status amg_build(const lgx_matrix *m, const lgx_amg_params &p,
     bool stop = false;
     if (csize < p.min_coarsen_size) {
       stop = true;
+      h.stop_reason = LGX_STOP_TOO_SMALL;
     } else if (level + 1 >= p.max_level_num) {
       stop = true;
+      h.stop_reason = LGX_STOP_TOO_MANY_LEVELS;
     } else if (p.min_coarsen_factor * (double)csize > (double)fsize) {
-      if (aggressive) stop = true; else aggressive = true;
+      if (aggressive) {
+        stop = true;
+        h.stop_reason = LGX_STOP_TOO_SMALL_RATE;
+      } else {
+        aggressive = true;
+      }
     }
-    if (stop || level + 2 >= 32) break;
+    if (!stop && level + 2 >= 32) {
+      stop = true;
+      h.stop_reason = LGX_STOP_LEVEL_CAP;
+    }
+    if (stop) break;
   }
   const int64_t L = (int64_t)h.lv.size();
   // smoother colourings (all but the coarsest level)
@@ -1412,6 +1427,32 @@ lgx_status lgx_amg_level_download(const lgx_amg *h, int64_t level, int64_t *h_ro
                              stream));
   }
   LGX_CUDA(cudaStreamSynchronize(stream));
+  return LGX_OK;
+}
+
+lgx_status lgx_amg_setup_log(const lgx_amg *h, lgx_amg_level_log *levels, int64_t max_levels,
+                             int64_t *nlevels, int32_t *stop_reason) {
+  if (!h || (levels && max_levels < 0)) return fail(LGX_ERR_INVALID, "bad argument");
+  const int64_t L = (int64_t)h->lv.size();
+  if (nlevels) *nlevels = L;
+  if (stop_reason) *stop_reason = h->stop_reason;
+  for (int64_t l = 0; levels && l < std::min(L, max_levels); ++l) {
+    const Csr &c = *h->lv[l]->a;
+    lgx_amg_level_log &o = levels[l];
+    o = lgx_amg_level_log{};
+    o.rows = c.n;
+    o.columns = c.n;
+    o.nnz = c.nnz;
+    if (l + 1 < L && l < 32) {
+      o.aggregate_num = h->stats[l][0];
+      o.multi_vertex_aggregate_num = h->stats[l][1];
+      o.single_vertex_aggregate_num = h->stats[l][2];
+      o.merged_aggregate_num = h->stats[l][3];
+      o.isolated_aggregate_num = h->stats[l][4];
+      o.aggressive = h->aggressive[l];
+      o.given_map = h->given[l];
+    }
+  }
   return LGX_OK;
 }
 

@@ -37,6 +37,9 @@ struct lgx_amg {
   std::vector<std::unique_ptr<lgx_amg_level>> lv;
   lgx::DBuf<double> inv;             // dense inverse of the coarsest matrix
   int64_t stats[32][5] = {};
+  uint8_t aggressive[32] = {};       // level aggregated with the aggressive threshold
+  uint8_t given[32] = {};            // level took a given aggregate map
+  int32_t stop_reason = 0;           // LGX_STOP_* (hierarchy/wright.hpp:26-28)
   lgx::DBuf<double> nat_b, nat_x;    // natural-order staging for lgx_amg_vcycle
   bool f32 = false;
 };

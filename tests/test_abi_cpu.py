@@ -60,6 +60,7 @@ def test_invalid_arguments_are_statuses(library):
     assert lib.lgx_amg_autotune(None, 5, None, 0, None, None) == 1
     assert lib.lgx_amg_level_lists(None, 0, None, None, None, None) == 1
     assert lib.lgx_direct_create(None, 0, None, None) == 1
+    assert lib.lgx_amg_setup_log(None, None, 0, None, None) == 1
     assert lib.lgx_direct_solve(None, None, None, None) == 1
     assert lib.lgx_direct_destroy(None) == 0
     assert lib.lgx_lincomb(-1, 1.0, None, 1.0, None, None, None) == 1

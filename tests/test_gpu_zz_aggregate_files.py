@@ -78,3 +78,32 @@ def test_gpu_setup_from_given_maps(cuda, tmp_path):
         cuda.HierarchyWright(**PARAMS).instantiate(m, aggregates=omaps[:1])
     with pytest.raises(cuda.LinealError, match="fine size"):
         cuda.HierarchyWright(**PARAMS).instantiate(m, aggregates=omaps[1:])
+
+
+def test_gpu_setup_log_matches_the_oracle(cuda):
+    """Hierarchy.setup_log (lgx_amg_setup_log): lineal's setup log keys, the
+    level sizes, the level-0 aggregation statistics of the oracle's
+    aggregation with the same partitions, and the stop reason."""
+    import ctypes
+
+    dims = (14, 15, 16)
+    ref = lo.gen_27pt(dims, np.exp(1.5 * np.random.default_rng(1).standard_normal(
+        int(np.prod(dims)))))
+    m = cuda.CsrMatrix.from_host(ref.rowptr, ref.col, ref.val, symmetric=True)
+    h = cuda.HierarchyWright(**PARAMS).instantiate(m)
+    log = h.setup_log()["create_hierarchy"]
+    rows, nnz = h.sizes()
+    assert [e["dimensions"]["rows"] for e in log["levels"]] == rows
+    assert [e["non_zeros"] for e in log["levels"]] == nnz
+    assert "aggregation_stats" not in log["levels"][-1]
+    assert rows[-1] < PARAMS["min_coarsen_size"]
+    assert log["stop_coarsening"]["reason"] == "too_small"
+    nparts = lo.lib().lo_amg_partitions(ref.n, 0, ctypes.byref(lo.amg_params(**PARAMS)))
+    dep, inf, iso = lo.amg_strength(ref)
+    nc, _, _, _, stats = lo.amg_aggregate(ref, dep, inf, iso, 6, 9, nparts)
+    got = log["levels"][0]["aggregation_stats"]
+    assert got["aggregate_num"] == nc == rows[1]
+    assert [got[k] for k in ("aggregate_num", "multi_vertex_aggregate_num",
+                             "single_vertex_aggregate_num", "merged_aggregate_num",
+                             "isolated_aggregate_num")] == [int(v) for v in stats]
+    assert not log["levels"][0]["aggressive"] and not log["levels"][0]["given_map"]
