@@ -531,7 +531,9 @@ def run_gb300(args):
         "config": {
             "workload": f"{args.grid}^3 27-point lognormal(sigma=1.5) CSR, AMG-PCG to 1e-8",
             "rows": n, "nnz": nnz, "parallelism": f"replicas x{world}",
-            "l2": "inputs (5.7 GB matrix) larger than L2; no flush",
+            "l2": (f"inputs ({(12 * nnz + 24 * n) / 1e9:.2f} GB: matrix and vectors) "
+                   + ("larger than the 129 MB L2; no flush" if 12 * nnz + 24 * n > 129e6 else
+                      "fit in the 129 MB L2: a small case, not a bench configuration")),
             "amg": {"levels": rows, "level_nnz": nnzs, "partition_size": args.partition_size,
                     "partition_growth": args.partition_growth,
                     "min_partitions": args.min_partitions,
