@@ -17,10 +17,12 @@
 
 #include <algorithm>
 #include <array>
+#include <bit>
 #include <cmath>
 #include <concepts>
 #include <cstddef>
 #include <cstdint>
+#include <cstdio>
 #include <optional>
 #include <stdexcept>
 #include <string>
@@ -645,7 +647,116 @@ struct AggregationParams {
   int64_t partition_size = 4096;
   double partition_growth = 4.0;
   int64_t min_partitions = 8;
+  // RefinedAggregator::Params::base_agg_map_path (aggregation/independent.hpp:
+  // 243-272): every level's aggregate map is written to <path><level>.aggs
+  std::optional<std::string> base_agg_map_path{};
 };
+
+// ---- aggregate-map files (aggregation/independent.hpp:35-44, 237-298) ----------
+// Both halves of lineal's BaseMultithreadAggregateMap (aggregate-map/
+// multithread.hpp:299-303, 346-349).  lineal serialises them with its
+// thesauros containers; the byte layout here is this library's own (the
+// Python lineal_gb300.io module reads and writes the same files): 8 magic
+// bytes "LGXAGGS1", u64 fine size n, u64 coarse size nc, u32 aggregate per
+// fine vertex (0xFFFFFFFE: isolated), u64 list offsets[nc + 1], u32 fine
+// vertex per list entry; little-endian.
+struct AggregateMap {
+  std::vector<uint32_t> agg;
+  std::vector<int64_t> list_ptr{0};
+  std::vector<int32_t> list;
+  [[nodiscard]] lgx_agg_map view() const {
+    return {(int64_t)agg.size(), (int64_t)list_ptr.size() - 1, agg.data(), list_ptr.data(),
+            list.data()};
+  }
+};
+
+inline std::string aggs_path(const std::string &base, std::size_t level) {
+  return base + std::to_string(level) + ".aggs";
+}
+
+namespace detail {
+inline constexpr char kAggsMagic[8] = {'L', 'G', 'X', 'A', 'G', 'G', 'S', '1'};
+static_assert(std::endian::native == std::endian::little, "aggregate-map files are little-endian");
+
+template <typename T>
+void write_raw(std::FILE *f, const T *p, std::size_t n, const std::string &path) {
+  if (n && std::fwrite(p, sizeof(T), n, f) != n)
+    throw Error(LGX_ERR_INVALID, "lineal_gb300: cannot write " + path);
+}
+template <typename T>
+void read_raw(std::FILE *f, T *p, std::size_t n, const std::string &path) {
+  if (n && std::fread(p, sizeof(T), n, f) != n)
+    throw Error(LGX_ERR_INVALID, "lineal_gb300: " + path + " is truncated");
+}
+struct File {
+  std::FILE *f;
+  ~File() {
+    if (f) std::fclose(f);
+  }
+};
+}  // namespace detail
+
+// the checks lgx_agg_map_check applies (host only)
+inline void check_aggregate_map(const AggregateMap &m) {
+  if (m.list_ptr.empty() || (std::size_t)m.list_ptr.back() > m.list.size())
+    throw Error(LGX_ERR_INVALID, "lineal_gb300: aggregate map offsets exceed its list");
+  const lgx_agg_map v = m.view();
+  check(lgx_agg_map_check(&v, v.n));
+}
+
+inline void write_aggs(const std::string &path, const AggregateMap &m) {
+  check_aggregate_map(m);
+  detail::File file{std::fopen(path.c_str(), "wb")};
+  if (!file.f) throw Error(LGX_ERR_INVALID, "lineal_gb300: cannot open " + path);
+  const uint64_t sizes[2] = {(uint64_t)m.agg.size(), (uint64_t)m.list_ptr.size() - 1};
+  detail::write_raw(file.f, detail::kAggsMagic, 8, path);
+  detail::write_raw(file.f, sizes, 2, path);
+  detail::write_raw(file.f, m.agg.data(), m.agg.size(), path);
+  detail::write_raw(file.f, m.list_ptr.data(), m.list_ptr.size(), path);
+  const std::vector<uint32_t> list(m.list.begin(), m.list.begin() + m.list_ptr.back());
+  detail::write_raw(file.f, list.data(), list.size(), path);
+}
+
+inline AggregateMap read_aggs(const std::string &path) {
+  detail::File file{std::fopen(path.c_str(), "rb")};
+  if (!file.f) throw Error(LGX_ERR_INVALID, "lineal_gb300: cannot open " + path);
+  char magic[8];
+  uint64_t sizes[2];
+  detail::read_raw(file.f, magic, 8, path);
+  if (!std::equal(magic, magic + 8, detail::kAggsMagic))
+    throw Error(LGX_ERR_INVALID, "lineal_gb300: " + path + " is not an aggregate-map file");
+  detail::read_raw(file.f, sizes, 2, path);
+  if (sizes[0] > (uint64_t)INT32_MAX || sizes[1] > sizes[0])
+    throw Error(LGX_ERR_INVALID, "lineal_gb300: " + path + " has impossible sizes");
+  AggregateMap m;
+  m.agg.resize(sizes[0]);
+  m.list_ptr.resize(sizes[1] + 1);
+  detail::read_raw(file.f, m.agg.data(), m.agg.size(), path);
+  detail::read_raw(file.f, m.list_ptr.data(), m.list_ptr.size(), path);
+  if (m.list_ptr.back() < 0 || (uint64_t)m.list_ptr.back() > sizes[0])
+    throw Error(LGX_ERR_INVALID, "lineal_gb300: " + path + " has impossible list offsets");
+  std::vector<uint32_t> list((std::size_t)m.list_ptr.back());
+  detail::read_raw(file.f, list.data(), list.size(), path);
+  if (std::fgetc(file.f) != EOF)
+    throw Error(LGX_ERR_INVALID, "lineal_gb300: " + path + " is longer than its header says");
+  m.list.assign(list.begin(), list.end());
+  check_aggregate_map(m);
+  return m;
+}
+
+// FileAggregator (aggregation/independent.hpp:279-298): the maps of levels
+// 0, 1, ... up to the first missing file
+inline std::vector<AggregateMap> read_aggregates(const std::string &base) {
+  std::vector<AggregateMap> maps;
+  for (;;) {
+    const std::string path = aggs_path(base, maps.size());
+    detail::File probe{std::fopen(path.c_str(), "rb")};
+    if (!probe.f) break;
+    maps.push_back(read_aggs(path));
+  }
+  if (maps.empty()) throw Error(LGX_ERR_INVALID, "lineal_gb300: no " + aggs_path(base, 0));
+  return maps;
+}
 
 struct DuneDependencyCriterion {
   double strong_threshold = 1.0 / 3.0;
@@ -666,6 +777,9 @@ struct MultiGridSolver : SharedStationaryIterativeSolverBase {
   bool float_cycle = false;
   bool bf16_values = false;  // with float_cycle: bfloat16 level values, diagonal row scales
   bool grid27 = true;        // 27-point grid finest level without column indices
+  // FileAggregator::Params::base_agg_map_path (aggregation/independent.hpp:
+  // 279-298): when set, level k takes the aggregates of <path><k>.aggs
+  std::optional<std::string> file_agg_map_path{};
 
   class Instance {
    public:
@@ -689,7 +803,25 @@ struct MultiGridSolver : SharedStationaryIterativeSolverBase {
       p.cycle_f32 = s.float_cycle;
       p.cycle_bf16 = s.bf16_values;
       p.grid27 = s.grid27;
-      check(lgx_amg_setup(lhs.handle(), &p, nullptr, env.stream(), &h_));
+      if (s.file_agg_map_path) {
+        const std::vector<AggregateMap> maps = read_aggregates(*s.file_agg_map_path);
+        std::vector<lgx_agg_map> views;
+        for (const auto &m : maps) views.push_back(m.view());
+        check(lgx_amg_setup_given(lhs.handle(), &p, nullptr, views.data(), (int64_t)views.size(),
+                                  env.stream(), &h_));
+      } else {
+        check(lgx_amg_setup(lhs.handle(), &p, nullptr, env.stream(), &h_));
+      }
+      if (s.aggregation.base_agg_map_path) {
+        try {
+          const std::size_t L = level_num();
+          for (std::size_t l = 0; l + 1 < L; ++l)
+            write_aggs(aggs_path(*s.aggregation.base_agg_map_path, l), aggregate_map(l, env));
+        } catch (...) {
+          lgx_amg_destroy(std::exchange(h_, nullptr));
+          throw;
+        }
+      }
     }
     Instance(const Instance &) = delete;
     Instance(Instance &&o) noexcept : h_(std::exchange(o.h_, nullptr)) {}
@@ -714,6 +846,23 @@ struct MultiGridSolver : SharedStationaryIterativeSolverBase {
       apply(out, rhs, env);
     }
     [[nodiscard]] lgx_amg *handle() const { return h_; }
+    // level l's aggregates (lgx_amg_level_download + lgx_amg_level_lists)
+    [[nodiscard]] AggregateMap aggregate_map(std::size_t l, const Environment &env) const {
+      int64_t L = 0;
+      std::vector<int64_t> rows(64), nnz(64);
+      check(lgx_amg_info(h_, &L, rows.data(), nnz.data(), (int64_t)rows.size()));
+      if ((int64_t)l + 1 >= L) throw Error(LGX_ERR_INVALID, "lineal_gb300: level has no map");
+      AggregateMap m;
+      m.agg.resize((std::size_t)rows[l]);
+      m.list_ptr.resize((std::size_t)rows[l + 1] + 1);
+      check(lgx_amg_level_download(h_, (int64_t)l, nullptr, nullptr, nullptr, m.agg.data(),
+                                   env.stream()));
+      int64_t len = 0;
+      check(lgx_amg_level_lists(h_, (int64_t)l, m.list_ptr.data(), nullptr, &len, env.stream()));
+      m.list.resize((std::size_t)len);
+      check(lgx_amg_level_lists(h_, (int64_t)l, nullptr, m.list.data(), nullptr, env.stream()));
+      return m;
+    }
     [[nodiscard]] std::size_t level_num() const {
       int64_t l = 0;
       check(lgx_amg_info(h_, &l, nullptr, nullptr, 0));

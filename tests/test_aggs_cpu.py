@@ -155,3 +155,64 @@ def test_library_map_check_agrees_with_the_oracle():
         g.agg_map_check((np.where(agg == lio.ISOLATED, agg, agg + 1), empty, lst))
     with pytest.raises(ValueError):
         g.agg_map_check((agg, ptr, lst[:-1]))  # list shorter than its offsets
+
+
+def _cpp_aggs():
+    from lineal_gb300 import build
+
+    return build.build_cpp_demo(name="aggs_io_demo")
+
+
+def _run(*args):
+    import subprocess
+
+    return subprocess.run(list(args), capture_output=True, text=True, timeout=120)
+
+
+def test_cpp_and_python_files_agree(tmp_path):
+    """The C++ layer's write_aggs / read_aggregates and lineal_gb300.io read
+    and write the same bytes (host code only, no GPU)."""
+    exe = _cpp_aggs()
+    base = str(tmp_path / "cpp")
+    r = _run(exe, "write", base)
+    assert r.returncode == 0, r.stdout + r.stderr
+    maps = lio.load_aggregates(base)
+    assert len(maps) == 2
+    np.testing.assert_array_equal(maps[0].agg, [1, 1, 0, 0, lio.ISOLATED, 2, 2, 0, 1, 2])
+    np.testing.assert_array_equal(maps[0].list_ptr, [0, 3, 6, 9])
+    np.testing.assert_array_equal(maps[0].list, [3, 2, 7, 8, 0, 1, 9, 5, 6])
+    np.testing.assert_array_equal(maps[1].list, [1, 0, 2])
+    # Python writes the oracle's maps, C++ reads them back
+    h = lo.Amg(_case(), **PARAMS)
+    pbase = str(tmp_path / "py")
+    lio.save_aggregates(pbase, _maps(h))
+    r = _run(exe, "read", pbase)
+    assert r.returncode == 0, r.stdout + r.stderr
+    want = [f"level {k} n {len(m.agg)} nc {len(m.list_ptr) - 1} sum "
+            f"{int(m.agg.astype(np.int64).sum() + 3 * m.list.astype(np.int64).sum())}"
+            for k, m in enumerate(_maps(h))]
+    assert r.stdout.split("\n")[:-1] == want
+
+
+def test_cpp_reader_refuses_damaged_files(tmp_path):
+    exe = _cpp_aggs()
+    h = lo.Amg(_case(), **PARAMS)
+    m = _maps(h)[0]
+    good = str(tmp_path / "good.aggs")
+    lio.write_aggs(good, m)
+    raw = open(good, "rb").read()
+    cases = {"truncated": raw[:-4], "longer": raw + b"\0", "magic": b"NOTAGGS!" + raw[8:]}
+    # a consistent-looking file whose lists put a vertex under another aggregate
+    agg, ptr, lst = (np.array(v) for v in m)
+    swap = lst.copy()
+    swap[[0, -1]] = swap[[-1, 0]]
+    body = (b"LGXAGGS1" + np.array([len(agg), len(ptr) - 1], "<u8").tobytes()
+            + agg.astype("<u4").tobytes() + ptr.astype("<u8").tobytes()
+            + swap.astype("<u4").tobytes())
+    cases["owner"] = body
+    for name, data in cases.items():
+        path = str(tmp_path / f"{name}.aggs")
+        open(path, "wb").write(data)
+        r = _run(exe, "refuse", path)
+        assert r.returncode == 0 and "refused" in r.stdout, (name, r.stdout, r.stderr)
+    assert _run(exe, "refuse", good).returncode == 1

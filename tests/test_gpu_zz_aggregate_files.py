@@ -107,3 +107,20 @@ def test_gpu_setup_log_matches_the_oracle(cuda):
                              "single_vertex_aggregate_num", "merged_aggregate_num",
                              "isolated_aggregate_num")] == [int(v) for v in stats]
     assert not log["levels"][0]["aggressive"] and not log["levels"][0]["given_map"]
+
+
+def test_cpp_solver_writes_and_reads_maps(cuda, tmp_path):
+    """The C++ MultiGridSolver's base_agg_map_path / file_agg_map_path
+    (tests/cpp/aggs_solver_demo.cpp); the files it writes are the ones
+    lineal_gb300.io reads."""
+    import subprocess
+
+    from lineal_gb300 import build
+
+    exe = build.build_cpp_demo(name="aggs_solver_demo")
+    base = str(tmp_path / "cpp")
+    out = subprocess.run([exe, base], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert "aggs_solver_demo ok" in out.stdout
+    for m in lio.load_aggregates(base):
+        lio.check_aggregate_map(m)
