@@ -291,6 +291,15 @@ typedef struct lgx_colouring lgx_colouring;
 /* Jones-Plassmann colouring with splitmix64 priorities (deterministic). */
 lgx_status lgx_colouring_create_jp(const lgx_matrix *a, uint64_t seed, lgx_stream stream,
                                    lgx_colouring **out);
+/* Smallest-last greedy colouring of a CSR pattern in host memory (rows as
+ * adjacency lists, the diagonal ignored; a symmetric pattern gives a proper
+ * colouring): host code only, deterministic, O(nnz).  On coarse AMG levels
+ * it needs fewer colours than Jones-Plassmann (64^3 27-point hierarchy,
+ * levels 1-2: 11 and 12 against 14 and 16).  colour[n] receives the
+ * colours, *ncolours their number; pass the colours (copied to the device)
+ * to lgx_colouring_create. */
+lgx_status lgx_colour_smallest_last(int64_t n, const int64_t *rowptr, const int32_t *col,
+                                    int32_t *colour, int32_t *ncolours);
 /* User colouring (device array, one colour in [0, ncolours) per row; e.g.
  * the parity colouring of a structured grid).  Validated on the device. */
 lgx_status lgx_colouring_create(const lgx_matrix *a, const int32_t *d_colour, int32_t ncolours,

@@ -204,6 +204,7 @@ def _signatures(L):
         "lgx_amg_level_download": [V, I64, V, V, V, V, V],
         "lgx_amg_level_lists": [V, I64, V, V, V, V],
         "lgx_amg_setup_log": [V, P(_AmgLevelLog), I64, P(I64), P(C.c_int32)],
+        "lgx_colour_smallest_last": [I64, V, V, V, P(C.c_int32)],
         "lgx_amg_setup_given": [V, P(_AmgParams), V, P(_AggMap), I64, V, P(V)],
         "lgx_agg_map_check": [P(_AggMap), I64],
         "lgx_amg_vcycle": [V, V, V, V],
@@ -603,6 +604,20 @@ class Colouring:
             self.close()
         except Exception:
             pass
+
+
+def colour_smallest_last(rowptr, col):
+    """Smallest-last greedy colouring of a host CSR pattern
+    (lgx_colour_smallest_last, host code): (colour int32[n], ncolours); give
+    the colours to ``Colouring.from_array`` for a multicolour smoother."""
+    rowptr = np.ascontiguousarray(rowptr, dtype=np.int64)
+    col = np.ascontiguousarray(col, dtype=np.int32)
+    n = len(rowptr) - 1
+    colour = np.empty(max(n, 1), dtype=np.int32)
+    nc = C.c_int32()
+    _check(lib().lgx_colour_smallest_last(n, _ptr(rowptr), _ptr(col), _ptr(colour),
+                                          C.byref(nc)))
+    return colour[:n], nc.value
 
 
 def stencil_engine(engine: int | None = None) -> int:

@@ -643,6 +643,85 @@ lgx_status lgx_colouring_create_jp(const lgx_matrix *a, uint64_t seed, lgx_strea
   return LGX_OK;
 }
 
+// Smallest-last greedy colouring on the host.  Ordering: vertices sit in
+// buckets by their degree among the vertices not yet removed (off-diagonal
+// pattern entries), each bucket a list with the most recently inserted vertex
+// at its head; the initial insertion runs in index order; each step removes
+// the head of the lowest non-empty bucket and moves each remaining neighbour
+// (in CSR order) to the head of the bucket below.  Colouring: in the reverse
+// of the removal order, each vertex takes the smallest colour none of its
+// coloured neighbours has.  O(nnz); every step is fixed, so the colouring is
+// deterministic.
+lgx_status lgx_colour_smallest_last(int64_t n, const int64_t *rowptr, const int32_t *col,
+                                    int32_t *colour, int32_t *ncolours) {
+  if (n < 0 || n > INT32_MAX || (n > 0 && (!rowptr || !col || !colour)) || !ncolours)
+    return fail(LGX_ERR_INVALID, "bad argument");
+  *ncolours = 0;
+  if (n == 0) return LGX_OK;
+  if (rowptr[0] != 0) return fail(LGX_ERR_INVALID, "row offsets must start at 0");
+  for (int64_t i = 0; i < n; ++i)
+    if (rowptr[i + 1] < rowptr[i]) return fail(LGX_ERR_INVALID, "decreasing row offsets");
+  for (int64_t e = 0; e < rowptr[n]; ++e)
+    if (col[e] < 0 || col[e] >= n) return fail(LGX_ERR_INVALID, "column index out of range");
+  std::vector<int64_t> deg((size_t)n), next((size_t)n, -1), prev((size_t)n, -1);
+  int64_t maxdeg = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    int64_t d = 0;
+    for (int64_t e = rowptr[i]; e < rowptr[i + 1]; ++e) d += col[e] != i;
+    deg[(size_t)i] = d;
+    maxdeg = std::max(maxdeg, d);
+  }
+  std::vector<int64_t> head((size_t)maxdeg + 1, -1);
+  auto unlink = [&](int64_t v) {
+    const int64_t p = prev[(size_t)v], q = next[(size_t)v];
+    if (p >= 0) next[(size_t)p] = q; else head[(size_t)deg[(size_t)v]] = q;
+    if (q >= 0) prev[(size_t)q] = p;
+  };
+  auto push = [&](int64_t v) {
+    const int64_t h = head[(size_t)deg[(size_t)v]];
+    prev[(size_t)v] = -1;
+    next[(size_t)v] = h;
+    if (h >= 0) prev[(size_t)h] = v;
+    head[(size_t)deg[(size_t)v]] = v;
+  };
+  for (int64_t i = 0; i < n; ++i) push(i);
+  std::vector<uint8_t> removed((size_t)n, 0);
+  std::vector<int32_t> order;
+  order.reserve((size_t)n);
+  int64_t low = 0;
+  for (int64_t step = 0; step < n; ++step) {
+    while (head[(size_t)low] < 0) ++low;
+    const int64_t v = head[(size_t)low];
+    unlink(v);
+    removed[(size_t)v] = 1;
+    order.push_back((int32_t)v);
+    for (int64_t e = rowptr[v]; e < rowptr[v + 1]; ++e) {
+      const int64_t u = col[e];
+      if (u == v || removed[(size_t)u]) continue;
+      unlink(u);
+      --deg[(size_t)u];
+      push(u);
+    }
+    if (low > 0) --low;  // a neighbour may now sit one bucket lower
+  }
+  std::vector<int64_t> stamp((size_t)maxdeg + 2, -1);
+  for (int64_t i = 0; i < n; ++i) colour[i] = -1;
+  int32_t used = 0;
+  for (int64_t k = n - 1; k >= 0; --k) {
+    const int64_t v = order[(size_t)k];
+    for (int64_t e = rowptr[v]; e < rowptr[v + 1]; ++e) {
+      const int32_t c = colour[col[e]];
+      if (col[e] != v && c >= 0 && c <= maxdeg) stamp[(size_t)c] = v;
+    }
+    int32_t c = 0;
+    while (stamp[(size_t)c] == v) ++c;
+    colour[v] = c;
+    used = std::max(used, c + 1);
+  }
+  *ncolours = used;
+  return LGX_OK;
+}
+
 lgx_status lgx_colouring_create(const lgx_matrix *a, const int32_t *d_colour, int32_t ncolours,
                                 lgx_stream stream, lgx_colouring **out) {
   if (!a || !out || (a->n > 0 && !d_colour)) return fail(LGX_ERR_INVALID, "null argument");

@@ -190,6 +190,8 @@ def _setup_signatures(L):
                                C.c_int, C.c_int, C.c_int64]
     L.lo_sor_sweep_ordered.argtypes = [P(_Csr), C.c_double, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_int, C.c_int, C.c_void_p]
+    L.lo_colour_smallest_last.restype = C.c_int32
+    L.lo_colour_smallest_last.argtypes = [P(_Csr), C.c_void_p]
     L.lo_colour_jp.restype = C.c_int32
     L.lo_colour_jp.argtypes = [P(_Csr), C.c_uint64, C.c_void_p]
     L.lo_colour_order.argtypes = [C.c_int64, C.c_void_p, C.c_int32, C.c_void_p]
@@ -482,6 +484,13 @@ def colour_jp(a: Csr, seed: int):
     c = a._c()
     col = np.empty(a.n, dtype=np.int32)
     nc = lib().lo_colour_jp(C.byref(c), seed, _ptr(col))
+    return col, int(nc)
+
+
+def colour_smallest_last(a: Csr):
+    c = a._c()
+    col = np.empty(a.n, dtype=np.int32)
+    nc = lib().lo_colour_smallest_last(C.byref(c), _ptr(col))
     return col, int(nc)
 
 

@@ -166,6 +166,8 @@ void lo_sor_sweep_ordered_f32(const lo_csr *a, float relax, const float *x_in, f
 /* Jones-Plassmann colouring with priority hash(seed, i), ties by index.
  * Deterministic; returns the number of colours. */
 int32_t lo_colour_jp(const lo_csr *a, uint64_t seed, int32_t *colour);
+/* smallest-last greedy colouring (host restatement); returns the colours */
+int32_t lo_colour_smallest_last(const lo_csr *a, int32_t *colour);
 /* order = rows sorted by (colour, index) */
 void lo_colour_order(int64_t n, const int32_t *colour, int32_t ncolours, int32_t *order);
 

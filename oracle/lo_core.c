@@ -538,6 +538,81 @@ int32_t lo_colour_jp(const lo_csr *a, uint64_t seed, int32_t *colour) {
   return ncol;
 }
 
+/* Smallest-last greedy colouring, restated from its specification (the
+ * library's lgx_colour_smallest_last): buckets by remaining off-diagonal
+ * degree, each a list whose head is the most recent insertion (initial
+ * insertion in index order); repeatedly remove the head of the lowest
+ * non-empty bucket and move its remaining neighbours (CSR order) to the
+ * head of the bucket below; colour in reverse removal order with the
+ * smallest colour no coloured neighbour has. */
+int32_t lo_colour_smallest_last(const lo_csr *a, int32_t *colour) {
+  const int64_t n = a->n;
+  if (n == 0) return 0;
+  int64_t *d = (int64_t *)malloc((size_t)n * sizeof(int64_t));
+  int64_t *nx = (int64_t *)malloc((size_t)n * sizeof(int64_t));
+  int64_t *pv = (int64_t *)malloc((size_t)n * sizeof(int64_t));
+  unsigned char *gone = (unsigned char *)calloc((size_t)n, 1);
+  int64_t *order = (int64_t *)malloc((size_t)n * sizeof(int64_t));
+  int64_t dmax = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    d[i] = 0;
+    for (int64_t e = a->rowptr[i]; e < a->rowptr[i + 1]; ++e) d[i] += a->col[e] != i;
+    if (d[i] > dmax) dmax = d[i];
+  }
+  int64_t *top = (int64_t *)malloc((size_t)(dmax + 1) * sizeof(int64_t));
+  for (int64_t b = 0; b <= dmax; ++b) top[b] = -1;
+  for (int64_t i = 0; i < n; ++i) {  /* insert at the head of bucket d[i] */
+    pv[i] = -1;
+    nx[i] = top[d[i]];
+    if (nx[i] >= 0) pv[nx[i]] = i;
+    top[d[i]] = i;
+  }
+  int64_t b = 0;
+  for (int64_t k = 0; k < n; ++k) {
+    while (top[b] < 0) ++b;
+    const int64_t v = top[b];
+    top[b] = nx[v];
+    if (nx[v] >= 0) pv[nx[v]] = -1;
+    gone[v] = 1;
+    order[k] = v;
+    for (int64_t e = a->rowptr[v]; e < a->rowptr[v + 1]; ++e) {
+      const int64_t u = a->col[e];
+      if (u == v || gone[u]) continue;
+      /* out of bucket d[u] ... */
+      if (pv[u] >= 0) nx[pv[u]] = nx[u]; else top[d[u]] = nx[u];
+      if (nx[u] >= 0) pv[nx[u]] = pv[u];
+      /* ... into the head of bucket d[u] - 1 */
+      d[u] -= 1;
+      pv[u] = -1;
+      nx[u] = top[d[u]];
+      if (nx[u] >= 0) pv[nx[u]] = u;
+      top[d[u]] = u;
+    }
+    if (b > 0) b -= 1;
+  }
+  int64_t *seen = (int64_t *)malloc((size_t)(dmax + 2) * sizeof(int64_t));
+  for (int64_t c = 0; c <= dmax + 1; ++c) seen[c] = -1;
+  for (int64_t i = 0; i < n; ++i) colour[i] = -1;
+  int32_t nc = 0;
+  for (int64_t k = n - 1; k >= 0; --k) {
+    const int64_t v = order[k];
+    for (int64_t e = a->rowptr[v]; e < a->rowptr[v + 1]; ++e)
+      if (a->col[e] != v && colour[a->col[e]] >= 0) seen[colour[a->col[e]]] = v;
+    int32_t c = 0;
+    while (seen[c] == v) ++c;
+    colour[v] = c;
+    if (c + 1 > nc) nc = c + 1;
+  }
+  free(d);
+  free(nx);
+  free(pv);
+  free(gone);
+  free(order);
+  free(top);
+  free(seen);
+  return nc;
+}
+
 void lo_colour_order(int64_t n, const int32_t *colour, int32_t ncolours, int32_t *order) {
   int64_t pos = 0;
   for (int32_t c = 0; c < ncolours; ++c)

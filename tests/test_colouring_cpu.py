@@ -1,0 +1,59 @@
+"""The host smallest-last colouring (lgx_colour_smallest_last; no device
+work, so it runs without a GPU) against the oracle's restatement of the same
+procedure, bit for bit, and the properties that make it a smoother
+colouring: proper on the symmetric pattern, fewer colours than
+Jones-Plassmann on coarse AMG levels."""
+
+import numpy as np
+import pytest
+
+import lineal_gb300 as g
+import oracle as lo
+
+
+def _proper(a, colour):
+    rows = np.repeat(np.arange(a.n), np.diff(a.rowptr))
+    off = a.col != rows
+    return not np.any(colour[rows[off]] == colour[a.col[off]])
+
+
+@pytest.mark.parametrize("case", ["27pt", "7pt", "ufz", "coarse"])
+def test_library_equals_oracle(case, golden_dir):
+    import os
+
+    from lineal_gb300 import io as lio
+
+    if case == "ufz":
+        rowptr, col, val, _ = lio.read_smf(os.path.join(golden_dir, "UFZ_CT_02_LHS.smf"))
+        a = lo.Csr(rowptr, col, val, symmetric=False)
+    elif case == "coarse":
+        k = np.exp(1.5 * np.random.default_rng(1).standard_normal(24 ** 3))
+        h = lo.Amg(lo.gen_27pt((24, 24, 24), k), min_coarsen_size=50, partition_size=512,
+                   smoother_parts=0)
+        a = h.level_csr(1)
+    else:
+        dims = (9, 10, 11)
+        k = np.exp(np.random.default_rng(2).standard_normal(990))
+        a = (lo.gen_27pt if case == "27pt" else lo.gen_7pt)(dims, k)
+    got, nc = g.colour_smallest_last(a.rowptr, a.col)
+    want, wnc = lo.colour_smallest_last(a)
+    np.testing.assert_array_equal(got, want)
+    assert nc == wnc == got.max() + 1
+    assert _proper(a, got)
+    if case == "7pt":
+        assert nc == 2  # a bipartite grid graph
+    if case == "coarse":
+        _, jp = lo.colour_jp(a, 0x5EED)
+        assert nc < jp
+
+
+def test_edge_cases():
+    c, nc = g.colour_smallest_last(np.zeros(1, np.int64), np.zeros(0, np.int32))
+    assert len(c) == 0 and nc == 0
+    # diagonal only: one colour
+    c, nc = g.colour_smallest_last(np.arange(4, dtype=np.int64), np.arange(3, dtype=np.int32))
+    assert nc == 1 and not c.any()
+    with pytest.raises(g.LinealError):
+        g.colour_smallest_last(np.array([0, 1], np.int64), np.array([5], np.int32))
+    with pytest.raises(g.LinealError):
+        g.colour_smallest_last(np.array([0, 2, 1], np.int64), np.array([0, 1], np.int32))
