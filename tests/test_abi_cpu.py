@@ -79,3 +79,33 @@ def test_concept_layer_compiles_and_links(library):
                  "aggs_solver_demo"):
         exe = build.build_cpp_demo(name=name)
         assert os.path.isfile(exe) and os.access(exe, os.X_OK)
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """Every ABI struct the Python front end mirrors with ctypes has the C
+    header's size and field offsets (a compiled probe of the header)."""
+    import ctypes
+
+    import lineal_gb300 as g
+
+    pairs = {"lgx_tune_entry": g._TuneEntry, "lgx_amg_level_log": g._AmgLevelLog,
+             "lgx_amg_params": g._AmgParams, "lgx_solve_params": g._SolveParams,
+             "lgx_agg_map": g._AggMap, "lgx_convdiff_system": g._ConvDiffSystem}
+    lines = ["#include <cstddef>", "#include <cstdio>", '#include "lineal_gb300.h"',
+             "int main() {"]
+    for cname, py in pairs.items():
+        lines.append(f'  std::printf("{cname} size %zu\\n", sizeof({cname}));')
+        for field, _ in py._fields_:
+            lines.append(f'  std::printf("{cname} {field} %zu\\n", offsetof({cname}, {field}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "probe.cpp"
+    src.write_text("\n".join(lines) + "\n")
+    exe = str(tmp_path / "probe")
+    subprocess.run(["g++", "-std=c++17", "-I", os.path.join(ROOT, "include"),
+                    "-I", "/usr/local/cuda/include", str(src), "-o", exe], check=True)
+    out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {tuple(line.split()[:2]): int(line.split()[2]) for line in out if line}
+    for cname, py in pairs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for field, _ in py._fields_:
+            assert got[(cname, field)] == getattr(py, field).offset, (cname, field)

@@ -349,3 +349,31 @@ def test_henry_lookup_provider():
             assert h.conn[16 + a * 4 + b] == pytest.approx(want, rel=1e-15)
     x = np.random.default_rng(24).uniform(-1, 1, len(mat))
     assert not np.allclose(h.spmv(x), sym.spmv(x))
+
+
+def test_oracle_ctypes_structs_match_the_header(tmp_path):
+    """The oracle's ctypes mirrors have lineal_oracle.h's sizes and offsets."""
+    import ctypes
+    import subprocess
+
+    pairs = {"lo_csr": lo._Csr, "lo_stencil": lo._Stencil, "lo_amg_params": lo._AmgParams,
+             "lo_amg_level": lo._AmgLevel, "lo_amg": lo._Amg, "lo_agg_map": lo._AggMap,
+             "lo_precon": lo._Precon}
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "lineal_oracle.h"',
+             "int main(void) {"]
+    for cname, py in pairs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for field, _ in py._fields_:
+            lines.append(f'  printf("{cname} {field} %zu\\n", offsetof({cname}, {field}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "probe.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = str(tmp_path / "probe")
+    here = os.path.dirname(lo.__file__)
+    subprocess.run(["gcc", "-std=c11", "-I", here, str(src), "-o", exe], check=True)
+    out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {tuple(line.split()[:2]): int(line.split()[2]) for line in out if line}
+    for cname, py in pairs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for field, _ in py._fields_:
+            assert got[(cname, field)] == getattr(py, field).offset, (cname, field)
