@@ -216,3 +216,65 @@ def test_cpp_reader_refuses_damaged_files(tmp_path):
         r = _run(exe, "refuse", path)
         assert r.returncode == 0 and "refused" in r.stdout, (name, r.stdout, r.stderr)
     assert _run(exe, "refuse", good).returncode == 1
+
+
+def _random_map(rng, n, nc):
+    """a consistent map: nc non-empty aggregates, some isolated vertices"""
+    agg = np.full(n, lio.ISOLATED, dtype=np.uint32)
+    members = rng.permutation(n)[: rng.integers(nc, n + 1)]
+    owner = np.concatenate([np.arange(nc), rng.integers(0, nc, len(members) - nc)])
+    agg[members] = owner
+    order = np.argsort(owner, kind="stable")
+    lst = members[order].astype(np.int32)
+    ptr = np.concatenate([[0], np.cumsum(np.bincount(owner, minlength=nc))]).astype(np.int64)
+    return agg, ptr, lst
+
+
+def _damage(rng, agg, ptr, lst):
+    agg, ptr, lst = agg.copy(), ptr.copy(), lst.copy()
+    kind = rng.integers(0, 6)
+    if kind == 0 and len(lst):
+        agg[lst[rng.integers(len(lst))]] = len(ptr) + rng.integers(0, 3)  # id out of range
+    elif kind == 1 and len(lst) > 1:
+        i, j = rng.choice(len(lst), 2, replace=False)
+        if agg[lst[i]] != agg[lst[j]]:
+            lst[i], lst[j] = lst[j], lst[i]  # listed under another aggregate
+        else:
+            lst[i] = lst[j]  # repeated
+    elif kind == 2 and len(lst):
+        agg[lst[rng.integers(len(lst))]] = lio.ISOLATED  # listed but isolated
+    elif kind == 3 and len(lst):
+        lst[rng.integers(len(lst))] = len(agg) + rng.integers(0, 5)  # vertex out of range
+    elif kind == 4:
+        ptr[0] = 1  # offsets not from 0
+    else:
+        return agg, ptr, lst, True  # untouched
+    return agg, ptr, lst, False
+
+
+def test_three_checkers_agree_on_random_maps():
+    """lgx_agg_map_check (the library's guard before any device copy), the
+    oracle's lo_agg_map_check and io.check_aggregate_map accept and refuse
+    the same maps: 300 random maps, most of them damaged."""
+    import lineal_gb300 as g
+
+    rng = np.random.default_rng(12)
+    for _ in range(300):
+        n = int(rng.integers(1, 60))
+        nc = int(rng.integers(1, n + 1))
+        agg, ptr, lst, intact = _damage(rng, *_random_map(rng, n, nc))
+        votes = []
+        try:
+            g.agg_map_check((agg, ptr, lst))
+            votes.append(True)
+        except (g.LinealError, ValueError):
+            votes.append(False)
+        votes.append(lo.agg_map_check(agg, ptr, lst) if ptr[-1] <= len(lst) else False)
+        try:
+            lio.check_aggregate_map(lio.AggregateMap(agg, ptr, lst))
+            votes.append(True)
+        except ValueError:
+            votes.append(False)
+        assert votes[0] == votes[1] == votes[2], (votes, n, nc)
+        if intact:
+            assert votes[0]
