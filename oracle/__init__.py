@@ -92,6 +92,7 @@ class _AmgParams(C.Structure):
         ("smoother_ultra", C.c_int),
         ("smoother_parts", C.c_int64),
         ("colour_seed", C.c_uint64),
+        ("coarse_smallest_last", C.c_int),
     ]
 
 

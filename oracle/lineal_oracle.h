@@ -203,6 +203,8 @@ typedef struct {
   int smoother_ultra;             /* SorVariant::ultra */
   int64_t smoother_parts;         /* >0: hybrid partitioned SOR with this many parts */
   uint64_t colour_seed;           /* used when smoother_parts == 0: colour-ordered SOR */
+  int coarse_smallest_last;       /* with smoother_parts == 0: levels >= 1 coloured by
+                                     lo_colour_smallest_last instead of Jones-Plassmann */
 } lo_amg_params;
 
 void lo_amg_default_params(lo_amg_params *p);

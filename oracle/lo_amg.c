@@ -27,6 +27,7 @@ void lo_amg_default_params(lo_amg_params *p) {
   p->smoother_ultra = 0;
   p->smoother_parts = 0;
   p->colour_seed = 0x5eed;
+  p->coarse_smallest_last = 0;
 }
 
 static int64_t find_col(const lo_csr *a, int64_t row, int64_t col) {
@@ -533,7 +534,9 @@ static void level_vectors(lo_amg_level *l, const lo_amg_params *p, int64_t idx) 
   l->order = NULL;
   if (p->smoother_parts == 0) {
     int32_t *colour = (int32_t *)malloc((size_t)(n + 1) * sizeof(int32_t));
-    const int32_t nc = lo_colour_jp(&l->a, p->colour_seed + (uint64_t)idx, colour);
+    const int32_t nc = p->coarse_smallest_last && idx > 0
+                         ? lo_colour_smallest_last(&l->a, colour)
+                         : lo_colour_jp(&l->a, p->colour_seed + (uint64_t)idx, colour);
     l->order = (int32_t *)malloc((size_t)(n + 1) * sizeof(int32_t));
     lo_colour_order(n, colour, nc, l->order);
     free(colour);
