@@ -381,6 +381,10 @@ typedef struct {
                                   and sweeps compute the column indices from the grid
                                   instead of reading them (bit-identical results); 0:
                                   always the CSR kernels */
+  int coarse_smallest_last;    /* 0 (default): Jones-Plassmann colourings on every
+                                  level; 1: levels >= 1 coloured on the host by
+                                  lgx_colour_smallest_last (fewer colours, so fewer
+                                  sweep launches) */
 } lgx_amg_params;
 
 void lgx_amg_default_params(lgx_amg_params *p);

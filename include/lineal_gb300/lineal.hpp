@@ -777,6 +777,7 @@ struct MultiGridSolver : SharedStationaryIterativeSolverBase {
   bool float_cycle = false;
   bool bf16_values = false;  // with float_cycle: bfloat16 level values, diagonal row scales
   bool grid27 = true;        // 27-point grid finest level without column indices
+  bool coarse_smallest_last = false;  // smallest-last colourings on levels >= 1
   // FileAggregator::Params::base_agg_map_path (aggregation/independent.hpp:
   // 279-298): when set, level k takes the aggregates of <path><k>.aggs
   std::optional<std::string> file_agg_map_path{};
@@ -803,6 +804,7 @@ struct MultiGridSolver : SharedStationaryIterativeSolverBase {
       p.cycle_f32 = s.float_cycle;
       p.cycle_bf16 = s.bf16_values;
       p.grid27 = s.grid27;
+      p.coarse_smallest_last = s.coarse_smallest_last;
       if (s.file_agg_map_path) {
         const std::vector<AggregateMap> maps = read_aggregates(*s.file_agg_map_path);
         std::vector<lgx_agg_map> views;

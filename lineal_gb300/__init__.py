@@ -101,6 +101,7 @@ class _AmgParams(C.Structure):
         ("colour_seed", C.c_uint64),
         ("cycle_bf16", C.c_int),
         ("grid27", C.c_int),
+        ("coarse_smallest_last", C.c_int),
     ]
 
 
@@ -707,6 +708,7 @@ class HierarchyWright:
     colour_seed: int = 0x5EED
     cycle_bf16: bool = False
     grid27: bool = True
+    coarse_smallest_last: bool = False
 
     def params(self) -> _AmgParams:
         p = _AmgParams()

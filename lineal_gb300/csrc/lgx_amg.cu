@@ -1040,6 +1040,29 @@ static lgx_status upload_map(const lgx_agg_map &m, int64_t level, int64_t n, cud
   return LGX_OK;
 }
 
+// a level's smallest-last colouring: its pattern to the host,
+// lgx_colour_smallest_last there, the colours back to the device
+static lgx_status colouring_smallest_last(const Csr &a, cudaStream_t s, DBuf<int32_t> &colour,
+                                          int32_t &ncolours) {
+  const int64_t n = a.n;
+  std::vector<int64_t> rowptr((size_t)n + 1);
+  std::vector<int32_t> col((size_t)std::max<int64_t>(a.nnz, 1));
+  std::vector<int32_t> h_colour((size_t)std::max<int64_t>(n, 1));
+  LGX_CUDA(cudaMemcpyAsync(rowptr.data(), a.rowptr.p, sizeof(int64_t) * (size_t)(n + 1),
+                           cudaMemcpyDeviceToHost, s));
+  if (a.nnz > 0)
+    LGX_CUDA(cudaMemcpyAsync(col.data(), a.col.p, sizeof(int32_t) * (size_t)a.nnz,
+                             cudaMemcpyDeviceToHost, s));
+  LGX_CUDA(cudaStreamSynchronize(s));
+  LGX_CHECK(lgx_colour_smallest_last(n, rowptr.data(), col.data(), h_colour.data(), &ncolours));
+  LGX_CHECK(colour.alloc(n));
+  if (n > 0)
+    LGX_CUDA(cudaMemcpyAsync(colour.p, h_colour.data(), sizeof(int32_t) * (size_t)n,
+                             cudaMemcpyHostToDevice, s));
+  LGX_CUDA(cudaStreamSynchronize(s));
+  return LGX_OK;
+}
+
 static lgx_status amg_build(const lgx_matrix *m, const lgx_amg_params &p,
                             const lgx_colouring *finest_colouring, const lgx_agg_map *maps,
                             int64_t nmaps, cudaStream_t s, lgx_amg &h) {
@@ -1116,7 +1139,10 @@ static lgx_status amg_build(const lgx_matrix *m, const lgx_amg_params &p,
                                 *lv.col));
     } else {
       int32_t nc = 0;
-      LGX_CHECK(colouring_jp(*lv.a, p.colour_seed + (uint64_t)l, s, lv.col->colour, nc));
+      if (l > 0 && p.coarse_smallest_last)
+        LGX_CHECK(colouring_smallest_last(*lv.a, s, lv.col->colour, nc));
+      else
+        LGX_CHECK(colouring_jp(*lv.a, p.colour_seed + (uint64_t)l, s, lv.col->colour, nc));
       LGX_CHECK(colouring_build(*lv.a, lv.col->colour.p, nc, s, *lv.col));
     }
     if (h.f32) LGX_CHECK(colouring_make_f32(*lv.col, s));
@@ -1331,6 +1357,7 @@ void lgx_amg_default_params(lgx_amg_params *p) {
   p->colour_seed = 0x5eed;
   p->cycle_bf16 = 0;
   p->grid27 = 1;
+  p->coarse_smallest_last = 0;
 }
 
 static lgx_status amg_setup(const lgx_matrix *a, const lgx_amg_params *p,
