@@ -265,7 +265,7 @@ def precision_form(g, args, stream):
     bn = float(torch.linalg.norm(b).item())
     hier_kw = dict(min_coarsen_size=2000, partition_size=args.partition_size,
                    partition_growth=args.partition_growth, min_partitions=args.min_partitions,
-                   grid27=args.grid27)
+                   grid27=args.grid27, coarse_smallest_last=args.coarse_smallest_last)
     out = {"workload": f"{args.grid}^3 7-point lognormal(sigma=3, seed 2), AMG-PCG to 1e-10",
            "rows": a.row_num(), "nnz": a.non_zero_num(),
            "finest_kernels": "7-point grid rows, red-black order" if args.grid27 else "CSR"}
@@ -333,7 +333,7 @@ def run_gb300(args):
 
     hier_kw = dict(min_coarsen_size=2000, partition_size=args.partition_size,
                    partition_growth=args.partition_growth, min_partitions=args.min_partitions,
-                   grid27=args.grid27)
+                   grid27=args.grid27, coarse_smallest_last=args.coarse_smallest_last)
     wright = g.HierarchyWright(**hier_kw)
     t0 = time.perf_counter()
     h64 = wright.instantiate(a, finest_colouring=col)
@@ -538,6 +538,8 @@ def run_gb300(args):
                     "partition_growth": args.partition_growth,
                     "min_partitions": args.min_partitions,
                     "finest_colouring": "grid parity, 8 colours",
+                    "coarse_colouring": ("smallest-last (host)" if args.coarse_smallest_last
+                                         else "Jones-Plassmann"),
                     "finest_kernels": ("27-point grid rows, column indices computed "
                                        "(lgx_amg_params.grid27)" if grid_on
                                        else "CSR row engine"),
@@ -996,6 +998,8 @@ def main():
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--coarse-smallest-last", action="store_true",
+                    help="colour AMG levels >= 1 by the host smallest-last colouring")
     ap.add_argument("--spmv-traffic", type=float, default=None,
                     help="DRAM bytes per SpMV launch from an ncu capture")
     args = ap.parse_args()
