@@ -11,8 +11,9 @@ k = exp(1.5 N(0,1)) (numpy PCG64, seed 1), b ~ U[-1, 1] (seed 0).
 
 --impl reference times the CPU restatement of lineal's shared-memory path
 (oracle/, the reference itself cannot be built: its thesauros/grex
-dependencies are not vendored) on the host cores, on a bounded sample of the
-same workload, extrapolated to the full size.
+dependencies are not vendored) on all host cores, on the same 256^3 system
+and a hierarchy built with lineal's own partition rule; each timed step is
+one full solve to 1e-8.
 
 Multi-GPU: the solve path has no exchange step on one box; N > 1 runs N
 independent replicas (one system per rank, weak scaling) and reports the
@@ -149,60 +150,137 @@ def make_problem(n_edge, seed_k=1, seed_b=0, sigma=1.5):
 NCU_SPMV_TRAFFIC_RATIO = (702.512128e6 + 17.137920e6) / 719247272.0
 
 
+# FP64 FMA rate of GB300 (nominal 1.25 TFLOP/s; 1.2 measured with a
+# dependent-chain-free FMA loop): the roof of the matrix-free stencils, whose
+# 7 FMAs per cell outweigh their 25-48 bytes, and of the FP64 grid rows
+FP64_PEAK_TFLOPS = 1.25
+
+# One colour launch of the FP64 grid SOR sweep, k_g27_rows<double, double, 2,
+# 27>, on the 160^3 27-point matrix (512,000 rows): ncu dram__bytes_read +
+# write = 152.014 + 3.908 MB, FP64 pipe busy 74.1 % of the elapsed cycles,
+# DRAM throughput 31.0 % of peak
+NCU_G27_SOR64_DRAM_PER_ROW = (152.014336e6 + 3.908096e6) / 512000
+NCU_G27_SOR64_FP64_BUSY = 0.741
+NCU_G27_SOR64_DRAM_FRAC = 0.310
+
+
 def csr_bytes(n, nnz, val_bytes=8, vec_bytes=8):
     # values + int32 columns + int64 row offsets + x once + y once
     return nnz * (val_bytes + 4) + 8 * (n + 1) + vec_bytes * n + vec_bytes * n
 
 
 # ---------------------------------------------------------------------------
-# CPU restatement (reference arm and cpu_baseline)
+# CPU restatement (reference arm, cpu_baseline, parity at the bench size)
 # ---------------------------------------------------------------------------
-def cpu_amg_pcg_sample(n_edge_sample, threads):
-    """Oracle AMG-PCG on a smaller grid with the reference's shared-memory
-    semantics (aggregation partitions clamp(n/8, 1, threads), thread-hybrid
-    SOR with one part per thread).  Returns (setup_s, solve_s, iterations,
-    nnz)."""
+# iterations of a reference warm-up step (a slice of the solve)
+REF_SAMPLE_ITERS = 9
+
+
+def workload_config(args, n, nnz, world):
+    """The `config` of both arms' JSON lines (identical by construction)."""
+    return {"workload": f"{args.grid}^3 27-point lognormal(sigma=1.5) CSR, AMG-PCG to 1e-8",
+            "rows": n, "nnz": nnz, "parallelism": f"replicas x{world}",
+            "l2": (f"inputs ({(12 * nnz + 24 * n) / 1e9:.2f} GB: matrix and vectors) "
+                   + ("larger than the 129 MB L2; no flush" if 12 * nnz + 24 * n > 129e6 else
+                      "fit in the 129 MB L2: a small case, not a bench configuration"))}
+
+
+def lineal_amg_params(threads):
+    """lineal's shared-memory AMG on `threads` threads: aggregation partitions
+    clamp(n / 8, 1, threads) on every level (aggregation/independent.hpp:
+    183-186 with min_per_thread = 8, test/aux/default.hpp:184-186) and the
+    thread-hybrid SOR with one row range per thread (gauss-seidel-variant/
+    sweep.hpp:135-169)."""
+    return dict(min_coarsen_size=2000, partition_size=8, partition_growth=1.0, min_partitions=1,
+                max_partitions=threads, smoother_parts=threads)
+
+
+def gpu_amg_params(args):
+    """The oracle with the GPU hierarchy's parameters: the same aggregation
+    partitions per level and colour-ordered SOR (Jones-Plassmann colourings
+    with the same seeds, or smallest-last on the coarse levels)."""
+    return dict(min_coarsen_size=2000, partition_size=args.partition_size,
+                partition_growth=args.partition_growth, min_partitions=args.min_partitions,
+                smoother_parts=0, coarse_smallest_last=int(args.coarse_smallest_last))
+
+
+def oracle_problem(grid):
     import oracle as lo
 
-    os.environ["OMP_NUM_THREADS"] = str(threads)
-    lo.set_threads(threads)  # the runtime reads the variable only once
-    dims, k, b = make_problem(n_edge_sample)
-    a = lo.gen_27pt(dims, k)
+    dims, k, b = make_problem(grid)
     t0 = time.perf_counter()
-    amg = lo.Amg(a, min_coarsen_size=2000, partition_size=8, max_partitions=threads,
-                 smoother_parts=threads)
-    t1 = time.perf_counter()
-    x, it, hist = lo.pcg(a, b, precon=lo.PRECON_AMG, amg=amg, rtol=1e-8, maxit=500)
-    t2 = time.perf_counter()
-    return t1 - t0, t2 - t1, it, a.nnz
+    a = lo.gen_27pt(dims, k)
+    return dims, a, b, time.perf_counter() - t0
 
 
-def cpu_baseline_entry(args, full_nnz, iters):
-    """The bench line's cpu_baseline: the oracle's AMG-PCG on a bounded
-    sample, on all host threads and on one core, ms per iteration scaled by
-    nnz to the full workload and multiplied by its iteration count."""
+def oracle_pcg(a, b, amg, rtol=1e-8, maxit=500):
+    """Oracle AMG-PCG from x0 = 0; returns (x, iterations, seconds)."""
     import oracle as lo
 
+    t0 = time.perf_counter()
+    x, it, _ = lo.pcg(a, b, precon=lo.PRECON_AMG, amg=amg, rtol=rtol, maxit=maxit)
+    return x, it, time.perf_counter() - t0
+
+
+def oracle_legs(args, gpu_levels, gpu_iterations):
+    """The GPU line's CPU legs at the bench size, on all host threads:
+    (1) parity: the oracle with the GPU's partitions and colourings (finest
+    level: the grid parity colouring) builds its hierarchy and solves to
+    1e-8 -- level sizes and iteration count beside the GPU's; (2)
+    cpu_baseline: one full solve with lineal's own partitions and hybrid SOR,
+    timed around the solve only (setup reported separately)."""
+    import oracle as lo
+
+    lo.build()
     threads = os.cpu_count() or 1
-    setup_s, solve_s, it, snnz = cpu_amg_pcg_sample(args.cpu_sample_edge, threads)
-    est = solve_s / max(it, 1) * (full_nnz / snnz) * iters * 1e3
-    cpu = {"value": est, "unit": "ms", "cores": threads, "kind": "port",
-           "sample": f"oracle AMG-PCG on {args.cpu_sample_edge}^3 27-pt, {threads} threads, "
-                     f"{it} iterations in {solve_s:.2f}s (setup {setup_s:.2f}s); ms/iteration "
-                     f"scaled by nnz to {args.grid}^3 times the {iters} GPU iterations"}
-    # the same sample on one core (one aggregation partition, one SOR part)
-    setup1, solve1, it1, _ = cpu_amg_pcg_sample(args.cpu_sample_edge, 1)
     lo.set_threads(threads)
-    cpu["single_core"] = {
-        "value": solve1 / max(it1, 1) * (full_nnz / snnz) * iters * 1e3, "unit": "ms",
-        "cores": 1, "sample": f"{it1} iterations in {solve1:.2f}s (setup {setup1:.2f}s), "
-                              "scaled as above"}
-    log(f"[gb300] cpu baseline {est:.0f} ms ({threads} threads), "
-        f"{cpu['single_core']['value']:.0f} ms (1 core)")
-    return cpu
+    dims, a, b, gen_s = oracle_problem(args.grid)
+    bn = float(np.linalg.norm(b))
+    t0 = time.perf_counter()
+    oh = lo.Amg(a, finest_colours=parity_colours(dims), ncolours=8, **gpu_amg_params(args))
+    setup_s = time.perf_counter() - t0
+    levels = [oh.level_size(l) for l in range(oh.nlevels)]
+    x, it, solve_s = oracle_pcg(a, b, oh)
+    rel = float(np.linalg.norm(b - lo.spmv(a, x))) / bn
+    oh.close()
+    del oh, x
+    parity = {"oracle_iterations": it, "gpu_iterations": gpu_iterations,
+              "iterations_within_5pct": abs(it - gpu_iterations) <= max(1, 0.05 * it),
+              "oracle_levels": levels, "gpu_levels": list(gpu_levels),
+              "levels_equal": levels == list(gpu_levels), "oracle_rel_residual": rel,
+              "oracle_setup_s": setup_s, "oracle_solve_s": solve_s, "threads": threads,
+              "what": "oracle AMG-PCG with the GPU hierarchy's partitions and colourings "
+                      "(colour-ordered SOR), same system"}
+    log(f"[parity] oracle {it} it vs GPU {gpu_iterations}; levels {levels} "
+        f"{'==' if parity['levels_equal'] else '!='} GPU {list(gpu_levels)}; "
+        f"setup {setup_s:.1f}s solve {solve_s:.1f}s")
+    t0 = time.perf_counter()
+    amg = lo.Amg(a, **lineal_amg_params(threads))
+    rsetup = time.perf_counter() - t0
+    x, rit, rsolve = oracle_pcg(a, b, amg)
+    rrel = float(np.linalg.norm(b - lo.spmv(a, x))) / bn
+    amg.close()
+    cpu = {"value": rsolve * 1e3, "unit": "ms", "cores": threads, "kind": "port",
+           "sample": f"one full {args.grid}^3 oracle AMG-PCG solve to 1e-8 ({rit} iterations, "
+                     f"rel. residual {rrel:.2e}) with lineal's partitions clamp(n/8, 1, "
+                     f"{threads}) and {threads}-part hybrid SOR, {threads} threads, solve only "
+                     f"(setup {rsetup:.1f}s, generation {gen_s:.1f}s excluded)",
+           "iterations": rit, "setup_ms": rsetup * 1e3,
+           "single_core": {"omitted": "a one-core 256^3 solve takes several minutes, beyond "
+                                      "the bench's time budget"}}
+    log(f"[gb300] cpu baseline {rsolve * 1e3:.0f} ms ({threads} threads, {rit} it, "
+        f"setup {rsetup:.1f}s)")
+    return parity, cpu
 
 
 def run_reference(args):
+    """lineal's shared-memory AMG-PCG (the oracle, restated in C) on all host
+    threads on the bench workload itself: the --grid^3 system and its
+    hierarchy (lineal's partition rule, hybrid SOR) are built once outside
+    the timed region; each timed step is one full solve to 1e-8 from x0 = 0
+    (the oracle's own iteration count), timed around the solve only.  Warm-up
+    steps run REF_SAMPLE_ITERS iterations of the same solve (they touch every
+    array a full solve touches)."""
     rank, world, _ = dist_env()
     if world > 1:
         import torch.distributed as dist
@@ -215,29 +293,36 @@ def run_reference(args):
 
     lo.build()
     threads = os.cpu_count() or 1
-    full_nnz = (3 * args.grid - 2) ** 3
-    sample_edge = args.cpu_sample_edge
-    vals = []
-    iters_full = args.reference_iterations
-    for step in range(args.warmup + args.steps):
-        setup_s, solve_s, it, nnz = cpu_amg_pcg_sample(sample_edge, threads)
-        per_iter = solve_s / max(it, 1)
-        est_ms = per_iter * (full_nnz / nnz) * (iters_full or it) * 1e3
-        if step >= args.warmup:
-            vals.append(est_ms)
-        log(f"[reference] sample {sample_edge}^3: setup {setup_s:.2f}s solve {solve_s:.2f}s "
-            f"{it} it -> {est_ms:.0f} ms at {args.grid}^3")
-    value = float(np.mean(vals))
-    sample = (f"oracle AMG-PCG on {sample_edge}^3 27-pt (same generator), {threads} threads; "
-              f"ms/iteration scaled by nnz to {args.grid}^3 and multiplied by the "
-              f"{iters_full or it} iterations of the full-size solve")
+    lo.set_threads(threads)
+    dims, a, b, gen_s = oracle_problem(args.grid)
+    t0 = time.perf_counter()
+    amg = lo.Amg(a, **lineal_amg_params(threads))
+    setup_s = time.perf_counter() - t0
+    levels = [amg.level_size(l) for l in range(amg.nlevels)]
+    log(f"[reference] {args.grid}^3: generation {gen_s:.1f}s setup {setup_s:.1f}s, levels "
+        f"{levels}")
+    for _ in range(args.warmup):
+        oracle_pcg(a, b, amg, rtol=0.0, maxit=REF_SAMPLE_ITERS)
+    step_ms, iters = [], []
+    for _ in range(args.steps):
+        x, it, dt = oracle_pcg(a, b, amg)
+        step_ms.append(dt * 1e3)
+        iters.append(it)
+        log(f"[reference] solve {dt:.2f}s, {it} it")
+    rel = float(np.linalg.norm(b - lo.spmv(a, x))) / float(np.linalg.norm(b))
+    value = float(np.mean(step_ms))
+    sample = (f"the {args.grid}^3 system itself: oracle AMG-PCG to 1e-8 ({iters[-1]} iterations) "
+              f"with lineal's partitions clamp(n/8, 1, {threads}) and {threads}-part hybrid SOR, "
+              f"{threads} threads, each step one full solve from x0 = 0, solve only (setup "
+              f"{setup_s:.1f}s, generation {gen_s:.1f}s excluded)")
     out = {
         "metric": METRIC, "value": value, "unit": "ms", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "impl": "reference",
-        "config": {"workload": f"{args.grid}^3 27-point lognormal(sigma=1.5) CSR AMG-PCG to 1e-8",
-                   "parallelism": f"replicas x{world}"},
+        "config": workload_config(args, a.n, a.nnz, world),
+        "oracle_iterations": iters[-1], "final_rel_residual": rel, "setup_ms": setup_s * 1e3,
+        "levels": levels, "warmup_iterations_per_step": REF_SAMPLE_ITERS,
         "cpu_baseline": {"value": value, "unit": "ms", "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -480,6 +565,38 @@ def run_gb300(args):
             f"{smoother['fp32_gbs']:.0f} GB/s ({smoother['fp32_frac']:.0%} of peak)")
         del colg, bp, xg, xg32, bp32
 
+    # ---- roofline of the dominant kernel of the timed FP64 solve: the finest
+    # SOR colour launch k_g27_rows<double, double, 2, 27> (8 per sweep, 16 per
+    # V-cycle); achieved = algorithmic bytes per launch / average launch time
+    # (CUDA events over whole sweeps on the launching stream)
+    if smoother:
+        launch_ms = smoother["fp64_ms"] / 8
+        launch_bytes = smoother["bytes_fp64"] / 8
+        achieved = launch_bytes / (launch_ms * 1e-3) / 1e9
+        fma_tf = 2 * nnz / (smoother["fp64_ms"] * 1e-3) / 1e12
+        roofline = {
+            "bound": "hbm", "kernel": "k_g27_rows<double, double, 2, 27> (finest-level SOR "
+                                      "colour, 8 launches per sweep)",
+            "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+            "frac": achieved / peak, "launch_ms": launch_ms, "bytes_per_launch": launch_bytes,
+            "traffic": (n / 8) * NCU_G27_SOR64_DRAM_PER_ROW,
+            "traffic_source": "ncu dram__bytes_read+write of one colour launch of the 160^3 "
+                              "27-point matrix (512,000 rows), per row, times the rows of a "
+                              "256^3 colour launch; above the algorithmic bytes by the x of "
+                              "the other seven colours that every colour launch gathers",
+            "fp64_pipe": {"fma_tflops": fma_tf, "peak_tflops": FP64_PEAK_TFLOPS,
+                          "peak_kind": "nominal", "frac": fma_tf / FP64_PEAK_TFLOPS,
+                          "ncu_busy_160cube": NCU_G27_SOR64_FP64_BUSY},
+            "binding_roof": "FP64 pipe: at 160^3 ncu shows it busy for "
+                            f"{NCU_G27_SOR64_FP64_BUSY:.0%} of the launch while DRAM "
+                            f"throughput is {NCU_G27_SOR64_DRAM_FRAC:.0%} of peak"}
+    else:
+        roofline = {"bound": "hbm", "kernel": "k_wrows<double, SpmvOp<double,double>, 4, 1>",
+                    "achieved": gbs64, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                    "frac": gbs64 / peak, "traffic": bytes64 * NCU_SPMV_TRAFFIC_RATIO,
+                    "traffic_source": "ncu dram__bytes_read+write of one launch at 128^3, "
+                                      "scaled to this matrix by its algorithmic bytes"}
+
     # ---- end to end through the C ABI with host buffers -----------------------
     e2e = None
     if args.e2e:
@@ -520,33 +637,28 @@ def run_gb300(args):
     # ---- CPU baseline (bounded sample) -----------------------------------------
     prec = precision_form(g, args, stream) if args.precision_form else None
 
-    cpu = None
+    cpu = parity = None
     if rank == 0 and args.cpu_baseline:
-        cpu = cpu_baseline_entry(args, nnz, iters64)
+        parity, cpu = oracle_legs(args, rows, iters64)
 
     out = {
         "metric": METRIC, "value": ms64, "unit": "ms", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms64, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {
-            "workload": f"{args.grid}^3 27-point lognormal(sigma=1.5) CSR, AMG-PCG to 1e-8",
-            "rows": n, "nnz": nnz, "parallelism": f"replicas x{world}",
-            "l2": (f"inputs ({(12 * nnz + 24 * n) / 1e9:.2f} GB: matrix and vectors) "
-                   + ("larger than the 129 MB L2; no flush" if 12 * nnz + 24 * n > 129e6 else
-                      "fit in the 129 MB L2: a small case, not a bench configuration")),
-            "amg": {"levels": rows, "level_nnz": nnzs, "partition_size": args.partition_size,
-                    "partition_growth": args.partition_growth,
-                    "min_partitions": args.min_partitions,
-                    "finest_colouring": "grid parity, 8 colours",
-                    "coarse_colouring": ("smallest-last (host)" if args.coarse_smallest_last
-                                         else "Jones-Plassmann"),
-                    "finest_kernels": ("27-point grid rows, column indices computed "
-                                       "(lgx_amg_params.grid27)" if grid_on
-                                       else "CSR row engine"),
-                    "row_engine": ("autotuned per level (lgx_amg_autotune, setup-time, "
-                                   "outside the timed solves; e2e untuned)"
-                                   if args.autotune else "process-wide configuration 3")},
-        },
+        "config": workload_config(args, n, nnz, world),
+        "amg": {"levels": rows, "level_nnz": nnzs, "partition_size": args.partition_size,
+                "partition_growth": args.partition_growth,
+                "min_partitions": args.min_partitions,
+                "finest_colouring": "grid parity, 8 colours",
+                "coarse_colouring": ("smallest-last (host)" if args.coarse_smallest_last
+                                     else "Jones-Plassmann"),
+                "finest_kernels": ("27-point grid rows, column indices computed "
+                                   "(lgx_amg_params.grid27)" if grid_on else "CSR row engine"),
+                "row_engine": ("autotuned per level (lgx_amg_autotune, setup-time, outside "
+                               "the timed solves; e2e untuned)"
+                               if args.autotune else "process-wide configuration 3")},
+        "oracle_iterations": parity["oracle_iterations"] if parity else None,
+        "oracle_parity": parity,
         "iterations": iters64, "final_rel_residual": rel64, "setup_ms": setup64 * 1e3,
         "autotune_ms": tune64,
         "mixed": {"ms": ms32, "iterations": res32.iterations, "rel_residual_fp64": rel32,
@@ -561,14 +673,7 @@ def run_gb300(args):
                  "bytes_fp64": bytes64, "bytes_fp32": bytes32},
         "smoother": smoother,
         "precision_form": prec,
-        "roofline": {"bound": "hbm", "kernel": "k_wrows<double, SpmvOp<double,double>, 4, 1>",
-                     "achieved": gbs64, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-                     "frac": gbs64 / peak,
-                     "traffic": (args.spmv_traffic if args.spmv_traffic is not None
-                                 else bytes64 * NCU_SPMV_TRAFFIC_RATIO),
-                     "traffic_source": "ncu dram__bytes_read+write of one launch at 128^3 "
-                                       "(profiles/k_wrows_spmv_fp64_128cube.md), scaled to "
-                                       "this matrix by its algorithmic bytes"},
+        "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": int(launches),
@@ -669,10 +774,6 @@ def batch_systems(count=1024, seed=3):
     return [((int(e),) * 3, tuple(float(c) for c in v)) for e, v in zip(edges, vs)]
 
 
-# FP64 FMA rate of GB300 (nominal 1.25 TFLOP/s; 1.2 measured with a
-# dependent-chain-free FMA loop): the roof of the matrix-free stencils, whose
-# 7 FMAs per cell outweigh their 25-48 bytes
-FP64_PEAK_TFLOPS = 1.25
 
 
 def run_stencil(args):
@@ -982,10 +1083,6 @@ def main():
     ap.add_argument("--partition-size", type=int, default=4096)
     ap.add_argument("--partition-growth", type=float, default=4.0)
     ap.add_argument("--min-partitions", type=int, default=8)
-    ap.add_argument("--cpu-sample-edge", type=int, default=64)
-    ap.add_argument("--reference-iterations", type=int, default=61,
-                    help="iterations of the full-size solve used to extrapolate the CPU sample "
-                         "(61: the 256^3 AMG-PCG iteration count of the same algorithm)")
     ap.add_argument("--no-grid27", dest="grid27", action="store_false",
                     help="finest level on the CSR row engine even for the 27-point grid")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
@@ -1000,8 +1097,6 @@ def main():
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--coarse-smallest-last", action="store_true",
                     help="colour AMG levels >= 1 by the host smallest-last colouring")
-    ap.add_argument("--spmv-traffic", type=float, default=None,
-                    help="DRAM bytes per SpMV launch from an ncu capture")
     args = ap.parse_args()
     if args.grid is None:
         # the differentiation and multi-right-hand-side configurations are 128^3

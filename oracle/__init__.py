@@ -103,6 +103,9 @@ class _AmgLevel(C.Structure):
         ("list_ptr", C.POINTER(C.c_int64)),
         ("list", C.POINTER(C.c_int32)),
         ("order", C.POINTER(C.c_int32)),
+        ("colour", C.POINTER(C.c_int32)),
+        ("colour_ptr", C.POINTER(C.c_int64)),
+        ("ncolours", C.c_int32),
         ("b", C.POINTER(C.c_double)),
         ("x", C.POINTER(C.c_double)),
         ("r", C.POINTER(C.c_double)),
@@ -220,6 +223,8 @@ def _setup_signatures(L):
     L.lo_amg_free.argtypes = [P(_Amg)]
     L.lo_agg_map_check.restype = C.c_int
     L.lo_agg_map_check.argtypes = [P(_AggMap)]
+    L.lo_amg_setup_coloured.restype = C.c_int
+    L.lo_amg_setup_coloured.argtypes = [P(_Csr), P(_AmgParams), C.c_void_p, C.c_int32, P(_Amg)]
     L.lo_amg_setup_given.restype = C.c_int
     L.lo_amg_setup_given.argtypes = [P(_Csr), P(_AmgParams), P(_AggMap), C.c_int64, P(_Amg)]
     L.lo_amg_vcycle.argtypes = [P(_Amg), C.c_void_p, C.c_void_p]
@@ -619,14 +624,27 @@ class Amg:
 
     With ``maps`` (a sequence of (agg, list_ptr, list) per level) the
     aggregation of level k is replaced by maps[k], as lineal's FileAggregator
-    does (aggregation/independent.hpp:279-298)."""
+    does (aggregation/independent.hpp:279-298).  With ``finest_colours``
+    (colour per row, ``ncolours`` classes) the colour-ordered smoother
+    (smoother_parts=0) of level 0 follows that colouring instead of
+    Jones-Plassmann."""
 
-    def __init__(self, a: Csr, maps=None, **params):
+    def __init__(self, a: Csr, maps=None, finest_colours=None, ncolours=0, **params):
         self._a = a
         self._c = a._c()
         self._p = amg_params(**params)
         self._h = _Amg()
-        if maps is None:
+        if finest_colours is not None:
+            if maps is not None:
+                raise ValueError("finest_colours and maps do not combine")
+            fc = np.ascontiguousarray(finest_colours, dtype=np.int32)
+            if fc.shape != (a.n,):
+                raise ValueError("finest_colours needs one colour per row")
+            rc = lib().lo_amg_setup_coloured(C.byref(self._c), C.byref(self._p), _ptr(fc),
+                                             int(ncolours), C.byref(self._h))
+            if rc == LO_ERR_BAD_MAP:
+                raise ValueError("finest colour outside [0, ncolours)")
+        elif maps is None:
             rc = lib().lo_amg_setup(C.byref(self._c), C.byref(self._p), C.byref(self._h))
         else:
             cm, _keep = _agg_maps(maps)

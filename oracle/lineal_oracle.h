@@ -137,6 +137,8 @@ void lo_csr_spmv(const lo_csr *a, const double *x, double *y);
 /* r = b - A x */
 void lo_csr_residual(const lo_csr *a, const double *b, const double *x, double *r);
 /* sequential-order reductions (accumulator.hpp:151-179 restated with a fixed order) */
+/* fixed block partition of the reductions (thread-count independent) */
+enum { LO_DOT_BLOCKS = 256 };
 double lo_dot(int64_t n, const double *a, const double *b);
 double lo_norm2sq(int64_t n, const double *a);
 double lo_max_norm(int64_t n, const double *a);
@@ -159,6 +161,16 @@ void lo_sor_sweep(const lo_csr *a, double relax, const double *x_in, double *x_o
  * multicolour sweep the GPU performs. */
 void lo_sor_sweep_ordered(const lo_csr *a, double relax, const double *x_in, double *x_out,
                           const double *b, int forward, int ultra, const int32_t *order);
+/* lo_sor_sweep_ordered for a proper colouring (no entry joins two rows of
+ * one colour) whose order lists the rows colour by colour: colour_ptr[c] ..
+ * colour_ptr[c + 1] index the rows of colour c in order.  Rows of one colour
+ * do not read one another, so each colour runs in parallel and the result
+ * equals lo_sor_sweep_ordered bit for bit. */
+void lo_sor_sweep_coloured(const lo_csr *a, double relax, const double *x_in, double *x_out,
+                           const double *b, int forward, int ultra, const int32_t *order,
+                           const int32_t *colour, const int64_t *colour_ptr, int32_t ncolours);
+/* 1 when no stored entry (i, j), i != j, has colour[i] == colour[j] */
+int lo_colouring_is_proper(const lo_csr *a, const int32_t *colour);
 /* lo_sor_sweep_ordered in float arithmetic on float-rounded values */
 void lo_sor_sweep_ordered_f32(const lo_csr *a, float relax, const float *x_in, float *x_out,
                               const float *b, int forward, int ultra, const int32_t *order);
@@ -238,6 +250,10 @@ typedef struct {
   int64_t *list_ptr;
   int32_t *list;
   int32_t *order;    /* smoother row order (colour order) or NULL */
+  int32_t *colour;   /* the colour of each row (with order) */
+  int64_t *colour_ptr; /* rows of colour c: order[colour_ptr[c] .. colour_ptr[c+1]); NULL
+                          when the colouring is not proper (sequential sweep) */
+  int32_t ncolours;
   double *b, *x, *r; /* per-level work vectors */
 } lo_amg_level;
 
@@ -274,6 +290,12 @@ int lo_agg_map_check(const lo_agg_map *m);
  * (size or consistency), else as lo_amg_setup.  h is freeable on return. */
 int lo_amg_setup_given(const lo_csr *a, const lo_amg_params *p, const lo_agg_map *maps,
                        int64_t nmaps, lo_amg *h);
+/* lo_amg_setup with a given colouring of level 0 (colour[n], ncolours
+ * classes) for the colour-ordered smoother (smoother_parts == 0) instead of
+ * Jones-Plassmann, as a caller that hands the GPU hierarchy its finest
+ * colouring does */
+int lo_amg_setup_coloured(const lo_csr *a, const lo_amg_params *p, const int32_t *colour0,
+                          int32_t ncolours0, lo_amg *h);
 void lo_amg_free(lo_amg *h);
 /* multigrid/solver.hpp:56-176, one REGULAR V-cycle from x_in = 0 */
 void lo_amg_vcycle(lo_amg *h, const double *b, double *x);

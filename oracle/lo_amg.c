@@ -55,7 +55,11 @@ void lo_amg_strength(const lo_csr *a, double theta, uint8_t *depends, uint8_t *i
   memset(influences, 0, (size_t)nnz);
   double *strength = (double *)malloc((size_t)(nnz > 0 ? nnz : 1) * sizeof(double));
   double *diag = (double *)malloc((size_t)(n > 0 ? n : 1) * sizeof(double));
+#pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < n; ++i) diag[i] = a->val[diag_pos(a, i)];
+  /* row i writes depends of its own entries and influences of the entry
+   * (j, i) of each neighbour row j: no two rows write the same byte */
+#pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < n; ++i) {
     if (a->is_f32) {
       float maxs = 0.0f;
@@ -437,81 +441,104 @@ int64_t lo_amg_aggregate(const lo_csr *a, const uint8_t *depends, const uint8_t 
  * accumulated in double per coarse column in first-encounter order; the row
  * is sorted by column and stored in the coarse value type.  Columns whose
  * fine vertex is isolated are dropped. */
+/* one coarse row: distinct columns in first-encounter order with their
+ * double sums; where[J] holds J's slot in cols (or -1) and is reset on
+ * return.  Returns the column count. */
+static int64_t galerkin_row(const lo_csr *a, const uint32_t *agg, const int64_t *list_ptr,
+                            const int32_t *list, int coarse_f32, int64_t c, int64_t *where,
+                            int64_t *cols, double *vals) {
+  int64_t m = 0;
+  for (int64_t k = list_ptr[c]; k < list_ptr[c + 1]; ++k) {
+    const int64_t i = list[k];
+    for (int64_t e = a->rowptr[i]; e < a->rowptr[i + 1]; ++e) {
+      const uint32_t J = agg[a->col[e]];
+      if (J >= LO_ISOLATED) continue;
+      const double v = coarse_f32 ? (double)(float)a->val[e] : a->val[e];
+      const int64_t f = where[J];
+      if (f < 0) {
+        where[J] = m;
+        cols[m] = J;
+        vals[m] = v;
+        ++m;
+      } else {
+        vals[f] += v;
+      }
+    }
+  }
+  for (int64_t x = 0; x < m; ++x) where[cols[x]] = -1;
+  return m;
+}
+
 int lo_amg_galerkin(const lo_csr *a, int64_t ncoarse, const uint32_t *agg, const int64_t *list_ptr,
                     const int32_t *list, int coarse_f32, lo_csr *out) {
   int64_t *cnt = (int64_t *)calloc((size_t)ncoarse + 1, sizeof(int64_t));
   int64_t maxrow = 0;
+#pragma omp parallel for schedule(static) reduction(max : maxrow)
   for (int64_t c = 0; c < ncoarse; ++c) {
     int64_t u = 0;
     for (int64_t k = list_ptr[c]; k < list_ptr[c + 1]; ++k)
       u += a->rowptr[list[k] + 1] - a->rowptr[list[k]];
     if (u > maxrow) maxrow = u;
   }
-  int64_t *cols = (int64_t *)malloc((size_t)(maxrow + 1) * sizeof(int64_t));
-  double *vals = (double *)malloc((size_t)(maxrow + 1) * sizeof(double));
-  /* pass 1: count distinct columns */
-  for (int64_t c = 0; c < ncoarse; ++c) {
-    int64_t m = 0;
-    for (int64_t k = list_ptr[c]; k < list_ptr[c + 1]; ++k) {
-      const int64_t i = list[k];
-      for (int64_t e = a->rowptr[i]; e < a->rowptr[i + 1]; ++e) {
-        const uint32_t J = agg[a->col[e]];
-        if (J >= LO_ISOLATED) continue;
-        int64_t f = 0;
-        while (f < m && cols[f] != (int64_t)J) ++f;
-        if (f == m) cols[m++] = J;
+  int failed = 0;
+  /* pass 1: count distinct columns; pass 2: fill.  Rows are independent,
+   * each thread keeps its own slot map and row buffers. */
+  for (int pass = 0; pass < 2 && !failed; ++pass) {
+    if (pass == 1) {
+      int64_t nnz = 0;
+      for (int64_t c = 0; c < ncoarse; ++c) nnz += cnt[c];
+      if (lo_csr_alloc(out, ncoarse, nnz)) {
+        failed = 1;
+        break;
       }
+      int64_t pos = 0;
+      for (int64_t c = 0; c < ncoarse; ++c) {
+        out->rowptr[c] = pos;
+        pos += cnt[c];
+      }
+      out->rowptr[ncoarse] = pos;
     }
-    cnt[c] = m;
-  }
-  int64_t nnz = 0;
-  for (int64_t c = 0; c < ncoarse; ++c) nnz += cnt[c];
-  if (lo_csr_alloc(out, ncoarse, nnz)) return -1;
-  int64_t pos = 0;
-  for (int64_t c = 0; c < ncoarse; ++c) {
-    out->rowptr[c] = pos;
-    int64_t m = 0;
-    for (int64_t k = list_ptr[c]; k < list_ptr[c + 1]; ++k) {
-      const int64_t i = list[k];
-      for (int64_t e = a->rowptr[i]; e < a->rowptr[i + 1]; ++e) {
-        const uint32_t J = agg[a->col[e]];
-        if (J >= LO_ISOLATED) continue;
-        const double v = coarse_f32 ? (double)(float)a->val[e] : a->val[e];
-        int64_t f = 0;
-        while (f < m && cols[f] != (int64_t)J) ++f;
-        if (f == m) {
-          cols[m] = J;
-          vals[m] = v;
-          ++m;
-        } else {
-          vals[f] += v;
+#pragma omp parallel
+    {
+      int64_t *where = (int64_t *)malloc((size_t)(ncoarse + 1) * sizeof(int64_t));
+      int64_t *cols = (int64_t *)malloc((size_t)(maxrow + 1) * sizeof(int64_t));
+      double *vals = (double *)malloc((size_t)(maxrow + 1) * sizeof(double));
+      for (int64_t c = 0; c <= ncoarse; ++c) where[c] = -1;
+#pragma omp for schedule(static)
+      for (int64_t c = 0; c < ncoarse; ++c) {
+        const int64_t m = galerkin_row(a, agg, list_ptr, list, coarse_f32, c, where, cols, vals);
+        if (pass == 0) {
+          cnt[c] = m;
+          continue;
+        }
+        for (int64_t x = 1; x < m; ++x) { /* insertion sort by column */
+          const int64_t cc = cols[x];
+          const double vv = vals[x];
+          int64_t y = x - 1;
+          while (y >= 0 && cols[y] > cc) {
+            cols[y + 1] = cols[y];
+            vals[y + 1] = vals[y];
+            --y;
+          }
+          cols[y + 1] = cc;
+          vals[y + 1] = vv;
+        }
+        int64_t pos = out->rowptr[c];
+        for (int64_t x = 0; x < m; ++x) {
+          out->col[pos] = (int32_t)cols[x];
+          out->val[pos] = coarse_f32 ? (double)(float)vals[x] : vals[x];
+          ++pos;
         }
       }
-    }
-    for (int64_t x = 1; x < m; ++x) { /* insertion sort by column */
-      const int64_t cc = cols[x];
-      const double vv = vals[x];
-      int64_t y = x - 1;
-      while (y >= 0 && cols[y] > cc) {
-        cols[y + 1] = cols[y];
-        vals[y + 1] = vals[y];
-        --y;
-      }
-      cols[y + 1] = cc;
-      vals[y + 1] = vv;
-    }
-    for (int64_t x = 0; x < m; ++x) {
-      out->col[pos] = (int32_t)cols[x];
-      out->val[pos] = coarse_f32 ? (double)(float)vals[x] : vals[x];
-      ++pos;
+      free(where);
+      free(cols);
+      free(vals);
     }
   }
-  out->rowptr[ncoarse] = pos;
+  free(cnt);
+  if (failed) return -1;
   out->symmetric = a->symmetric;
   out->is_f32 = coarse_f32;
-  free(cnt);
-  free(cols);
-  free(vals);
   return 0;
 }
 
@@ -526,20 +553,36 @@ static void csr_copy(const lo_csr *a, lo_csr *b) {
   b->is_f32 = a->is_f32;
 }
 
-static void level_vectors(lo_amg_level *l, const lo_amg_params *p, int64_t idx) {
+static void level_vectors(lo_amg_level *l, const lo_amg_params *p, int64_t idx,
+                          const int32_t *given_colour, int32_t given_nc) {
   const int64_t n = l->a.n;
   l->b = (double *)calloc((size_t)n + 1, sizeof(double));
   l->x = (double *)calloc((size_t)n + 1, sizeof(double));
   l->r = (double *)calloc((size_t)n + 1, sizeof(double));
   l->order = NULL;
+  l->colour = NULL;
+  l->colour_ptr = NULL;
+  l->ncolours = 0;
   if (p->smoother_parts == 0) {
     int32_t *colour = (int32_t *)malloc((size_t)(n + 1) * sizeof(int32_t));
-    const int32_t nc = p->coarse_smallest_last && idx > 0
-                         ? lo_colour_smallest_last(&l->a, colour)
-                         : lo_colour_jp(&l->a, p->colour_seed + (uint64_t)idx, colour);
+    int32_t nc;
+    if (given_colour) {
+      memcpy(colour, given_colour, (size_t)n * sizeof(int32_t));
+      nc = given_nc;
+    } else {
+      nc = p->coarse_smallest_last && idx > 0
+             ? lo_colour_smallest_last(&l->a, colour)
+             : lo_colour_jp(&l->a, p->colour_seed + (uint64_t)idx, colour);
+    }
     l->order = (int32_t *)malloc((size_t)(n + 1) * sizeof(int32_t));
     lo_colour_order(n, colour, nc, l->order);
-    free(colour);
+    l->colour = colour;
+    l->ncolours = nc;
+    if (lo_colouring_is_proper(&l->a, colour)) {
+      l->colour_ptr = (int64_t *)calloc((size_t)nc + 1, sizeof(int64_t));
+      for (int64_t i = 0; i < n; ++i) ++l->colour_ptr[colour[i] + 1];
+      for (int32_t c = 0; c < nc; ++c) l->colour_ptr[c + 1] += l->colour_ptr[c];
+    }
   }
 }
 
@@ -615,7 +658,7 @@ static int level_aggregates(const lo_csr *a, const lo_amg_params *p, int64_t lev
 }
 
 static int amg_setup(const lo_csr *a0, const lo_amg_params *p, const lo_agg_map *maps,
-                     int64_t nmaps, lo_amg *h) {
+                     int64_t nmaps, const int32_t *colour0, int32_t nc0, lo_amg *h) {
   memset(h, 0, sizeof(*h));
   h->p = *p;
   csr_copy(a0, &h->lv[0].a);
@@ -634,7 +677,7 @@ static int amg_setup(const lo_csr *a0, const lo_amg_params *p, const lo_agg_map 
     }
     lo_amg_level *coarse = &h->lv[level + 1];
     lo_amg_galerkin(a, nc, fine->agg, fine->list_ptr, fine->list, p->coarse_f32, &coarse->a);
-    level_vectors(fine, p, level);
+    level_vectors(fine, p, level, level == 0 ? colour0 : NULL, nc0);
     /* level_action: coarse < min size -> stop; too many levels -> stop;
      * factor * coarse > fine -> aggressive (or stop if already aggressive) */
     int stop = 0;
@@ -662,7 +705,19 @@ static int amg_setup(const lo_csr *a0, const lo_amg_params *p, const lo_agg_map 
 }
 
 int lo_amg_setup(const lo_csr *a, const lo_amg_params *p, lo_amg *h) {
-  return amg_setup(a, p, NULL, 0, h);
+  return amg_setup(a, p, NULL, 0, NULL, 0, h);
+}
+
+int lo_amg_setup_coloured(const lo_csr *a, const lo_amg_params *p, const int32_t *colour0,
+                          int32_t ncolours0, lo_amg *h) {
+  if (colour0) {
+    for (int64_t i = 0; i < a->n; ++i)
+      if (colour0[i] < 0 || colour0[i] >= ncolours0) {
+        memset(h, 0, sizeof(*h));
+        return LO_ERR_BAD_MAP;
+      }
+  }
+  return amg_setup(a, p, NULL, 0, colour0, ncolours0, h);
 }
 
 int lo_amg_setup_given(const lo_csr *a, const lo_amg_params *p, const lo_agg_map *maps,
@@ -671,7 +726,7 @@ int lo_amg_setup_given(const lo_csr *a, const lo_amg_params *p, const lo_agg_map
     memset(h, 0, sizeof(*h));
     return LO_ERR_NO_MAP;
   }
-  return amg_setup(a, p, maps, nmaps, h);
+  return amg_setup(a, p, maps, nmaps, NULL, 0, h);
 }
 
 void lo_amg_free(lo_amg *h) {
@@ -681,6 +736,8 @@ void lo_amg_free(lo_amg *h) {
     free(h->lv[l].list_ptr);
     free(h->lv[l].list);
     free(h->lv[l].order);
+    free(h->lv[l].colour);
+    free(h->lv[l].colour_ptr);
     free(h->lv[l].b);
     free(h->lv[l].x);
     free(h->lv[l].r);
@@ -691,7 +748,10 @@ void lo_amg_free(lo_amg *h) {
 
 static void smooth(const lo_amg *h, const lo_amg_level *l, const double *x_in, double *x_out,
                    const double *b, int forward) {
-  if (l->order) {
+  if (l->colour_ptr) {
+    lo_sor_sweep_coloured(&l->a, h->p.smoother_relax, x_in, x_out, b, forward,
+                          h->p.smoother_ultra, l->order, l->colour, l->colour_ptr, l->ncolours);
+  } else if (l->order) {
     lo_sor_sweep_ordered(&l->a, h->p.smoother_relax, x_in, x_out, b, forward, h->p.smoother_ultra,
                          l->order);
   } else {
@@ -715,6 +775,7 @@ void lo_amg_vcycle(lo_amg *h, const double *b, double *x) {
     smooth(h, lv, NULL, xl, bl, 1);
     lo_csr_residual(&lv->a, bl, xl, lv->r);
     lo_amg_level *cv = &h->lv[l + 1];
+#pragma omp parallel for schedule(static)
     for (int64_t c = 0; c < cv->a.n; ++c) {
       double s = 0.0;
       for (int64_t k = lv->list_ptr[c]; k < lv->list_ptr[c + 1]; ++k) s += lv->r[lv->list[k]];
@@ -731,13 +792,15 @@ void lo_amg_vcycle(lo_amg *h, const double *b, double *x) {
     const double *bl = l == 0 ? b : lv->b;
     double *xl = l == 0 ? x : lv->x;
     const double *xc = h->lv[l + 1].x;
+#pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < lv->a.n; ++i) {
       const uint32_t ag = lv->agg[i];
       const double ref = ag < LO_ISOLATED ? xc[ag] : 0.0;
       xl[i] = xl[i] + ref * inv_relax;
     }
     /* in-situ post smoothing: swap(sol, aux); sweep(aux -> sol) */
-    memcpy(lv->r, xl, (size_t)lv->a.n * sizeof(double));
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < lv->a.n; ++i) lv->r[i] = xl[i];
     smooth(h, lv, lv->r, xl, bl, 0);
   }
 }

@@ -322,33 +322,50 @@ int lo_stencil_to_csr(const lo_stencil *s, lo_csr *out, int64_t *compress_map) {
   return 0;
 }
 
-/* Generic structured assembly used by the 27-point and 7-point generators. */
+/* Generic structured assembly used by the 27-point and 7-point generators.
+ * Rows are independent: a parallel count pass, offsets, a parallel fill. */
+static int64_t structured_row_len(const int64_t dims[3], int npts, int64_t i) {
+  const int64_t n0 = dims[0], n1 = dims[1], n2 = dims[2];
+  const int64_t p[3] = {i / (n1 * n2), (i / n2) % n1, i % n2};
+  int64_t c = 1;
+  for (int a = -1; a <= 1; ++a)
+    for (int b = -1; b <= 1; ++b)
+      for (int cc = -1; cc <= 1; ++cc) {
+        const int m = abs(a) + abs(b) + abs(cc);
+        if (m == 0 || (npts == 7 && m != 1)) continue;
+        if (p[0] + a < 0 || p[0] + a >= n0 || p[1] + b < 0 || p[1] + b >= n1 ||
+            p[2] + cc < 0 || p[2] + cc >= n2)
+          continue;
+        ++c;
+      }
+  return c;
+}
+
 static int gen_structured(const int64_t dims[3], const double *k, int npts, lo_csr *out) {
   const int64_t n0 = dims[0], n1 = dims[1], n2 = dims[2];
   const int64_t n = n0 * n1 * n2;
-  /* count */
+  int64_t *len = (int64_t *)malloc((size_t)(n + 1) * sizeof(int64_t));
+  if (!len) return -1;
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) len[i] = structured_row_len(dims, npts, i);
   int64_t nnz = 0;
-  for (int64_t i = 0; i < n; ++i) {
-    const int64_t p[3] = {i / (n1 * n2), (i / n2) % n1, i % n2};
-    int64_t c = 1;
-    for (int a = -1; a <= 1; ++a)
-      for (int b = -1; b <= 1; ++b)
-        for (int cc = -1; cc <= 1; ++cc) {
-          const int m = abs(a) + abs(b) + abs(cc);
-          if (m == 0 || (npts == 7 && m != 1)) continue;
-          if (p[0] + a < 0 || p[0] + a >= n0 || p[1] + b < 0 || p[1] + b >= n1 ||
-              p[2] + cc < 0 || p[2] + cc >= n2)
-            continue;
-          ++c;
-        }
-    nnz += c;
+  for (int64_t i = 0; i < n; ++i) nnz += len[i];
+  if (lo_csr_alloc(out, n, nnz)) {
+    free(len);
+    return -1;
   }
-  if (lo_csr_alloc(out, n, nnz)) return -1;
-  static const double w[4] = {0.0, 1.0, 0.5, 0.25};
   int64_t pos = 0;
   for (int64_t i = 0; i < n; ++i) {
-    const int64_t p[3] = {i / (n1 * n2), (i / n2) % n1, i % n2};
     out->rowptr[i] = pos;
+    pos += len[i];
+  }
+  out->rowptr[n] = pos;
+  free(len);
+  static const double w[4] = {0.0, 1.0, 0.5, 0.25};
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t p[3] = {i / (n1 * n2), (i / n2) % n1, i % n2};
+    int64_t pos_i = out->rowptr[i];
     const double ki = k[i];
     double diag = 0.0;
     if (p[0] == 0) diag = diag + 2.0 * ki;
@@ -364,21 +381,20 @@ static int gen_structured(const int64_t dims[3], const double *k, int npts, lo_c
               p[2] + cc < 0 || p[2] + cc >= n2)
             continue;
           const int64_t j = i + a * n1 * n2 + b * n2 + cc;
-          out->col[pos] = (int32_t)j;
+          out->col[pos_i] = (int32_t)j;
           if (m == 0) {
-            dpos = pos;
-            out->val[pos] = 0.0;
+            dpos = pos_i;
+            out->val[pos_i] = 0.0;
           } else {
             const double c = lo_harmonic_mean(ki, k[j]) * w[m];
-            out->val[pos] = -c;
+            out->val[pos_i] = -c;
             diag = diag + c;
           }
-          ++pos;
+          ++pos_i;
         }
     if (diag == 0.0) diag = 1.0;
     out->val[dpos] = diag;
   }
-  out->rowptr[n] = pos;
   out->symmetric = 1;
   return 0;
 }
@@ -456,9 +472,21 @@ void lo_csr_residual(const lo_csr *a, const double *b, const double *x, double *
   }
 }
 
+/* accumulator.hpp:28-48 sums per-thread partials (merged through
+ * atomic_ref, in arrival order).  Here the partials belong to LO_DOT_BLOCKS
+ * fixed contiguous blocks, each summed in index order and merged in block
+ * order, so the result is the same for every thread count. */
 double lo_dot(int64_t n, const double *a, const double *b) {
+  double part[LO_DOT_BLOCKS];
+#pragma omp parallel for schedule(static)
+  for (int64_t k = 0; k < LO_DOT_BLOCKS; ++k) {
+    const int64_t lo = lo_part_begin(n, LO_DOT_BLOCKS, k), hi = lo_part_begin(n, LO_DOT_BLOCKS, k + 1);
+    double s = 0.0;
+    for (int64_t i = lo; i < hi; ++i) s += a[i] * b[i];
+    part[k] = s;
+  }
   double s = 0.0;
-  for (int64_t i = 0; i < n; ++i) s += a[i] * b[i];
+  for (int64_t k = 0; k < LO_DOT_BLOCKS; ++k) s += part[k];
   return s;
 }
 double lo_norm2sq(int64_t n, const double *a) { return lo_dot(n, a, a); }
@@ -494,6 +522,8 @@ int32_t lo_colour_jp(const lo_csr *a, uint64_t seed, int32_t *colour) {
   int64_t left = n;
   int32_t ncol = 0;
   while (left > 0) {
+    /* a round reads colour[] only and writes next[i] of its own vertex */
+#pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; ++i) {
       next[i] = -1;
       if (colour[i] >= 0) continue;
@@ -526,12 +556,17 @@ int32_t lo_colour_jp(const lo_csr *a, uint64_t seed, int32_t *colour) {
       }
       next[i] = c;
     }
+    int64_t done = 0;
+    int32_t top = ncol;
+#pragma omp parallel for schedule(static) reduction(+ : done) reduction(max : top)
     for (int64_t i = 0; i < n; ++i)
       if (next[i] >= 0) {
         colour[i] = next[i];
-        --left;
-        if (next[i] + 1 > ncol) ncol = next[i] + 1;
+        ++done;
+        if (next[i] + 1 > top) top = next[i] + 1;
       }
+    left -= done;
+    ncol = top;
   }
   free(prio);
   free(next);

@@ -97,6 +97,30 @@ void lo_sor_sweep_ordered(const lo_csr *a, double relax, const double *x_in, dou
   free(rank);
 }
 
+void lo_sor_sweep_coloured(const lo_csr *a, double relax, const double *x_in, double *x_out,
+                           const double *b, int forward, int ultra, const int32_t *order,
+                           const int32_t *colour, const int64_t *colour_ptr, int32_t ncolours) {
+  const double m1 = 1.0 - relax;
+  for (int32_t cc = 0; cc < ncolours; ++cc) {
+    const int32_t c = forward ? cc : ncolours - 1 - cc;
+#pragma omp parallel for schedule(static)
+    for (int64_t k = colour_ptr[c]; k < colour_ptr[c + 1]; ++k) {
+      /* rank order = colour order for a proper colouring: colour[] stands in
+       * for the rank of sor_row */
+      sor_row(a, order[k], relax, m1, x_in, x_out, b, ultra, 0, a->n, colour, forward);
+    }
+  }
+}
+
+int lo_colouring_is_proper(const lo_csr *a, const int32_t *colour) {
+  int proper = 1;
+#pragma omp parallel for schedule(static) reduction(&& : proper)
+  for (int64_t i = 0; i < a->n; ++i)
+    for (int64_t e = a->rowptr[i]; e < a->rowptr[i + 1]; ++e)
+      if (a->col[e] != i && colour[a->col[e]] == colour[i]) proper = 0;
+  return proper;
+}
+
 /* The float smoother of the precision form: the row of sor_row in float
  * arithmetic (fmaf, float division) on the matrix values rounded to float,
  * rows visited in `order` (rank-based new/old choice, so ultra adds no
@@ -286,10 +310,12 @@ int64_t lo_pcg(const lo_csr *a, const double *b, double *x, const lo_precon *m, 
   while (it < maxit && sqrt(res2) > rtol * r0 && rho != 0.0) {
     lo_csr_spmv(a, p, q);
     const double alpha = rho / lo_dot(n, p, q);
+    #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; ++i) x[i] = x[i] + p[i] * alpha;
     if (rere_period > 0 && it > 0 && it % rere_period == 0) {
       lo_csr_residual(a, b, x, r);
     } else {
+      #pragma omp parallel for schedule(static)
       for (int64_t i = 0; i < n; ++i) r[i] = r[i] - q[i] * alpha;
     }
     res2 = lo_norm2sq(n, r);
@@ -298,10 +324,12 @@ int64_t lo_pcg(const lo_csr *a, const double *b, double *x, const lo_precon *m, 
       precon_apply(a, m, r, q, aux);
       rho = lo_dot(n, r, q);
       const double beta = rho / old_rho;
+      #pragma omp parallel for schedule(static)
       for (int64_t i = 0; i < n; ++i) p[i] = q[i] + p[i] * beta;
     } else {
       rho = res2;
       const double beta = rho / old_rho;
+      #pragma omp parallel for schedule(static)
       for (int64_t i = 0; i < n; ++i) p[i] = r[i] + p[i] * beta;
     }
     ++it;
@@ -341,7 +369,9 @@ int64_t lo_pbicgstab(const lo_csr *a, const double *b, double *x, const lo_preco
     }
     lo_csr_spmv(a, y, v);
     alpha = rho / lo_dot(n, r0v, v);
+    #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; ++i) x[i] = x[i] + y[i] * alpha;
+    #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; ++i) r[i] = r[i] - v[i] * alpha;
     res2 = lo_norm2sq(n, r);
     const double *z = r;
@@ -350,27 +380,21 @@ int64_t lo_pbicgstab(const lo_csr *a, const double *b, double *x, const lo_preco
       z = px;
     }
     lo_csr_spmv(a, z, t);
-    double on = 0.0, od = 0.0;
-    for (int64_t i = 0; i < n; ++i) {
-      on += t[i] * r[i];
-      od += t[i] * t[i];
-    }
+    const double on = lo_dot(n, t, r), od = lo_norm2sq(n, t);
     omega = on / od;
+    #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; ++i) x[i] = x[i] + z[i] * omega;
     const double old_rho = rho;
     if (rere_period > 0 && it > 0 && it % rere_period == 0) {
       lo_csr_residual(a, b, x, r);
     } else {
+      #pragma omp parallel for schedule(static)
       for (int64_t i = 0; i < n; ++i) r[i] = r[i] - t[i] * omega;
     }
-    double rr = 0.0, r2 = 0.0;
-    for (int64_t i = 0; i < n; ++i) {
-      rr += r[i] * r0v[i];
-      r2 += r[i] * r[i];
-    }
-    rho = rr;
-    res2 = r2;
+    rho = lo_dot(n, r, r0v);
+    res2 = lo_norm2sq(n, r);
     const double beta = (rho / old_rho) * (alpha / omega);
+    #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; ++i) p[i] = r[i] + (p[i] - v[i] * omega) * beta;
     ++it;
     if (history) history[it] = sqrt(res2);

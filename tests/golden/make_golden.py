@@ -2,7 +2,7 @@
 
 Run once, in a container that has the reference checkout:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path of the lineal checkout>
 
 It executes the reference's own Python scripts (nothing is re-implemented
 here) and stores their results as compressed numpy archives:
@@ -81,4 +81,6 @@ def main(ref: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <path of the lineal checkout>")
+    main(sys.argv[1])

@@ -27,7 +27,7 @@ def _free_port():
         return s.getsockname()[1]
 
 
-ARGS = ["--impl", "reference", "--steps", "1", "--warmup", "3", "--cpu-sample-edge", "12"]
+ARGS = ["--impl", "reference", "--steps", "2", "--warmup", "3", "--grid", "16"]
 
 
 def test_reference_arm_prints_contract_line():
@@ -38,11 +38,21 @@ def test_reference_arm_prints_contract_line():
     assert len(lines) == 1
     d = lines[0]
     assert d["impl"] == "reference" and d["unit"] == "ms" and d["higher_is_better"] is False
-    assert d["value"] > 0 and d["steps"] == 1 and d["warmup"] == 3 and d["n_gpus"] == 1
+    assert d["value"] > 0 and d["steps"] == 2 and d["warmup"] == 3 and d["n_gpus"] == 1
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": "ms", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}
+    # the workload itself: 16^3 27-point rows and non-zeros, each step one
+    # full solve to 1e-8
+    n, nnz = 16 ** 3, (3 * 16 - 2) ** 3
+    assert d["config"]["rows"] == n and d["config"]["nnz"] == nnz
+    assert d["oracle_iterations"] > 1 and d["final_rel_residual"] <= 1e-8
+    assert d["value"] == d["ms_per_step"]
+    import bench
+
+    args = bench.argparse.Namespace(grid=16)
+    assert d["config"] == bench.workload_config(args, n, nnz, 1)
 
 
 def test_reference_arm_two_gloo_ranks_print_one_line():
@@ -64,14 +74,21 @@ def test_warmup_below_three_is_rejected():
     assert "warmup" in r.stderr
 
 
-def test_cpu_baseline_entry_all_threads_and_one_core():
-    code = ("import argparse, json, bench; a = argparse.Namespace(cpu_sample_edge=12, grid=256); "
-            "print(json.dumps(bench.cpu_baseline_entry(a, (3 * 256 - 2) ** 3, 61)))")
+def test_oracle_legs_parity_and_cpu_baseline():
+    """The GPU line's CPU legs on a 16^3 case: the oracle with the GPU
+    hierarchy's parameters reports its levels and iterations beside the
+    given GPU figures; the CPU baseline is one full solve with lineal's
+    partitions, the one-core figure explicitly omitted."""
+    code = ("import argparse, json, bench; a = argparse.Namespace(grid=16, partition_size=512, "
+            "partition_growth=4.0, min_partitions=8, coarse_smallest_last=False); "
+            "p, c = bench.oracle_legs(a, [4096, 1], 7); print(json.dumps([p, c]))")
     r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True,
                        timeout=300)
     assert r.returncode == 0, r.stderr[-2000:]
-    d = _json_lines(r.stdout)[-1]
-    assert d["kind"] == "port" and d["unit"] == "ms" and d["value"] > 0
-    assert d["cores"] == (os.cpu_count() or 1) and d["sample"]
-    one = d["single_core"]
-    assert one["cores"] == 1 and one["unit"] == "ms" and one["value"] > 0 and one["sample"]
+    par, cpu = json.loads(r.stdout.strip().splitlines()[-1])
+    assert par["gpu_iterations"] == 7 and par["oracle_iterations"] > 0
+    assert par["oracle_levels"][0] == 4096 and par["levels_equal"] is False
+    assert par["oracle_rel_residual"] <= 1e-8
+    assert cpu["kind"] == "port" and cpu["unit"] == "ms" and cpu["value"] > 0
+    assert cpu["cores"] == (os.cpu_count() or 1) and cpu["iterations"] > 0
+    assert "omitted" in cpu["single_core"]
