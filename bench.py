@@ -355,9 +355,10 @@ def precision_form(g, args, stream):
            "rows": a.row_num(), "nnz": a.non_zero_num(),
            "finest_kernels": "7-point grid rows, red-black order" if args.grid27 else "CSR"}
     xs = {}
-    for tag, f32, bf16, flexible in (("fp64", False, False, False),
-                                     ("mixed_fcg", True, False, True),
-                                     ("mixed_bf16_fcg", True, True, True)):
+    for tag, f32, bf16, flexible, refine in (("fp64", False, False, False, False),
+                                             ("mixed_fcg", True, False, True, False),
+                                             ("mixed_refined", True, False, False, True),
+                                             ("mixed_bf16_fcg", True, True, True, False)):
         t0 = time.perf_counter()
         h = g.HierarchyWright(cycle_f32=f32, cycle_bf16=bf16, **hier_kw).instantiate(
             a, finest_colouring=col)
@@ -367,14 +368,14 @@ def precision_form(g, args, stream):
             h.autotune(reps=3)
         for _ in range(args.warmup):
             res = g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=1e-10, maxit=1000,
-                        flexible=flexible)
+                        flexible=flexible, refine=refine)
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(args.steps):
             res = g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=1e-10, maxit=1000,
-                        flexible=flexible)
+                        flexible=flexible, refine=refine)
         e1.record(stream)
         e1.synchronize()
         _, rn = g.residual(a, b, res.x)
@@ -385,11 +386,12 @@ def precision_form(g, args, stream):
         log(f"[precision] {tag}: {out[tag]['ms']:.1f} ms, {res.iterations} it, "
             f"rel {out[tag]['rel_residual_fp64']:.2e}")
         del h
-    for tag in ("mixed_fcg", "mixed_bf16_fcg"):
+    for tag in ("mixed_fcg", "mixed_refined", "mixed_bf16_fcg"):
         out[tag]["rel_error_vs_fp64_solution"] = float(
             torch.linalg.norm(xs[tag] - xs["fp64"]).item() / torch.linalg.norm(xs["fp64"]).item())
         out[tag]["speedup_vs_fp64"] = out["fp64"]["ms"] / out[tag]["ms"]
-    out["speedup_vs_fp64"] = out["fp64"]["ms"] / out["mixed_fcg"]["ms"]
+    out["speedup_vs_fp64"] = out["fp64"]["ms"] / min(out["mixed_fcg"]["ms"],
+                                                     out["mixed_refined"]["ms"])
     return out
 
 def run_gb300(args):
@@ -490,6 +492,26 @@ def run_gb300(args):
     rel32 = float(np.sqrt(rn32)) / float(torch.linalg.norm(b).item())
     err = float(torch.linalg.norm(res32.x - x).item() / torch.linalg.norm(x).item())
     log(f"[gb300] mixed AMG-PCG {ms32:.1f} ms, {res32.iterations} it, rel {rel32:.2e}")
+
+    # ---- mixed, FP64 iterative refinement over a float inner PCG (same float
+    # hierarchy): float products and V-cycles, FP64 dots, scalars, outer
+    # residual and stopping test
+    def solve_refined(h):
+        return g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=1e-8, maxit=500, refine=True)
+
+    for _ in range(args.warmup):
+        resr = solve_refined(h32)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        resr = solve_refined(h32)
+    e1.record(stream)
+    e1.synchronize()
+    msr = e0.elapsed_time(e1) / args.steps
+    _, rnr = g.residual(a, b, resr.x)
+    relr = float(np.sqrt(rnr)) / float(torch.linalg.norm(b).item())
+    errr = float(torch.linalg.norm(resr.x - x).item() / torch.linalg.norm(x).item())
+    log(f"[gb300] mixed refined AMG-PCG {msr:.1f} ms, {resr.iterations} it, rel {relr:.2e}")
 
     # ---- mixed with bfloat16 level values (precision form option) ----------
     h16 = g.HierarchyWright(cycle_f32=True, cycle_bf16=True, **hier_kw).instantiate(
@@ -637,6 +659,18 @@ def run_gb300(args):
     # ---- CPU baseline (bounded sample) -----------------------------------------
     prec = precision_form(g, args, stream) if args.precision_form else None
 
+    # ---- the other named configurations, each with its own check -------------
+    configs = {}
+    if args.configs:
+        a = h32 = b = None  # the 256^3 system is done with: free its device memory
+        torch.cuda.empty_cache()
+        sw = (max(3, args.warmup // 2), stream)
+        configs["config1_jacobi_pcg_64"] = config1_entry(g, min(args.steps, 10), *sw)
+        configs["batch_1024"] = batch_entry(g, min(args.steps, 5), *sw)
+        configs["multi_rhs_32"] = multi_entry(g, min(args.steps, 3), *sw,
+                                              partition_size=args.partition_size)
+        configs["adjoint_128"] = adjoint_entry(g, 128, args.bench_fd_directions)
+
     cpu = parity = None
     if rank == 0 and args.cpu_baseline:
         parity, cpu = oracle_legs(args, rows, iters64)
@@ -664,6 +698,12 @@ def run_gb300(args):
         "mixed": {"ms": ms32, "iterations": res32.iterations, "rel_residual_fp64": rel32,
                   "setup_ms": setup32 * 1e3, "autotune_ms": tune32,
                   "speedup_vs_fp64": ms64 / ms32, "rel_error_vs_fp64_solution": err},
+        "mixed_refined": {"ms": msr, "iterations": resr.iterations, "rel_residual_fp64": relr,
+                          "speedup_vs_fp64": ms64 / msr, "rel_error_vs_fp64_solution": errr,
+                          "what": "FP64 iterative refinement over a float-vector inner PCG "
+                                  "(float finest products and V-cycle; FP64 dots, CG scalars, "
+                                  "outer residual), inner tolerance 1e-4"},
+        "mixed_speedup_vs_fp64": ms64 / min(ms32, msr),
         "mixed_bf16": {"ms": ms16, "iterations": res16.iterations, "rel_residual_fp64": rel16,
                        "autotune_ms": tune16, "speedup_vs_fp64": ms64 / ms16,
                        "rel_error_vs_fp64_solution": err16,
@@ -674,6 +714,7 @@ def run_gb300(args):
         "smoother": smoother,
         "precision_form": prec,
         "roofline": roofline,
+        **configs,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": int(launches),
@@ -837,44 +878,95 @@ def run_stencil(args):
                       "kernels": out}), flush=True)
 
 
-def run_batch(args):
-    """Batching form: Jacobi-BiCGStab to 1e-8 on 1024 uneven convection-diffusion
-    systems in one persistent launch (per step: the whole batch, b resident)."""
+def timed(fn, steps, warmup, stream):
+    """Mean ms of `steps` calls of fn after `warmup` untimed ones (CUDA events
+    on the launching stream); returns (ms, last result)."""
     import torch
 
-    import lineal_gb300 as g
-
-    g.build.build()
-    systems = batch_systems(args.batch_systems)
-    rows = sum(int(np.prod(d)) for d, _ in systems)
-    b = torch.as_tensor(np.random.default_rng(0).uniform(-1, 1, rows), device="cuda")
-    for _ in range(args.warmup):
-        res = g.batch_convdiff_bicgstab(systems, b, rtol=1e-8, maxit=2000)
+    res = None
+    for _ in range(warmup):
+        res = fn()
     torch.cuda.synchronize()
-    stream = torch.cuda.current_stream()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(args.steps):
-        res = g.batch_convdiff_bicgstab(systems, b, rtol=1e-8, maxit=2000)
+    for _ in range(steps):
+        res = fn()
     e1.record(stream)
     e1.synchronize()
-    ms = e0.elapsed_time(e1) / args.steps
+    return e0.elapsed_time(e1) / steps, res
+
+
+def config1_entry(g, steps, warmup, stream, edge=64):
+    """Plain method, small: the 64^3 constant-coefficient Poisson system as a
+    matrix-free lookup stencil (one material, unit cells, Dirichlet values 0
+    on the axis-0 faces), b ~ U[-1, 1] (seed 0), x0 = 0, Jacobi-PCG to 1e-8,
+    FP64; iterations and the FP64 residual checked against the oracle."""
+    import oracle as lo
+
+    dims = (edge,) * 3
+    n = edge ** 3
+    mat = np.ones(n, dtype=np.uint8)
+    coeffs = (0.0, 1.0, 0.0, 0.0)
+    b = np.random.default_rng(0).uniform(-1, 1, n)
+    st = g.StencilMatrix.lookup(g.BoxInfo(dims, dims), None, coeffs, mat, 0.0, 0.0)
+    bd = g._dvec(b)
+    ms, res = timed(lambda: g.pcg(st, bd, precon=g.PRECON_JACOBI, rtol=1e-8, maxit=5000),
+                    steps, warmup, stream)
+    lo.build()
+    ref, _ = lo.Stencil(dims, mat=mat, coeffs=coeffs, sol_start=0, sol_end=0).to_csr()
+    _, it, _ = lo.pcg(ref, b, precon=lo.PRECON_JACOBI, rtol=1e-8, maxit=5000)
+    x = res.x.cpu().numpy()
+    rel = float(np.linalg.norm(b - lo.spmv(ref, x)) / np.linalg.norm(b))
+    out = {"workload": f"{edge}^3 7-point Poisson, lookup stencil, Jacobi-PCG to 1e-8",
+           "rows": n, "ms": ms, "iterations": res.iterations, "oracle_iterations": it,
+           "iterations_within_5pct": abs(res.iterations - it) <= max(1, 0.05 * it),
+           "rel_residual_fp64": rel,
+           "note": "about 4.5 MB of operator and vectors: an L2-resident case, no HBM claim"}
+    log(f"[config1] {ms:.2f} ms, {res.iterations} it (oracle {it}), rel {rel:.2e}")
+    return out
+
+
+def batch_entry(g, steps, warmup, stream, count=1024, cpu_sample=0, oracle_check=8):
+    """Batching form: Jacobi-BiCGStab to 1e-8 on `count` uneven upwind
+    convection-diffusion systems in one persistent launch (per step the
+    whole batch, b resident); the first `oracle_check` systems' iterations
+    and FP64 residuals checked against the oracle."""
+    import torch
+
+    import oracle as lo
+
+    systems = batch_systems(count)
+    rows = sum(int(np.prod(d)) for d, _ in systems)
+    bh = np.random.default_rng(0).uniform(-1, 1, rows)
+    b = torch.as_tensor(bh, device="cuda")
+    ms, res = timed(lambda: g.batch_convdiff_bicgstab(systems, b, rtol=1e-8, maxit=2000),
+                    steps, warmup, stream)
     row_iters = sum(int(np.prod(d)) * int(i) for (d, _), i in zip(systems, res.iterations))
-    # bytes per row and iteration: 2 operator passes (z read with neighbours
-    # from cache, one write) + the vector streams of the fused phases
-    out = {"mode": "batch", "systems": len(systems), "rows": rows, "ms": ms,
+    out = {"systems": len(systems), "rows": rows, "ms": ms,
            "systems_per_s": len(systems) / (ms * 1e-3),
            "iterations_mean": float(res.iterations.mean()),
            "iterations_max": int(res.iterations.max()),
            "converged": int((res.status == 0).sum()),
            "max_rel_residual": float(res.rel_residual.max()),
            "row_iterations_per_s": row_iters / (ms * 1e-3)}
-    if args.cpu_baseline:
-        import oracle as lo
-
-        lo.build()
-        sample = systems[:args.batch_cpu_sample]
+    lo.build()
+    x = res.x.cpu().numpy()
+    off, worst_it, worst_rel = 0, 0.0, 0.0
+    for k, (dims, v) in enumerate(systems):
+        m = int(np.prod(dims))
+        if k < oracle_check:
+            a = lo.gen_convdiff(dims, v)
+            _, it, _ = lo.pbicgstab(a, bh[off:off + m], precon=lo.PRECON_JACOBI, rtol=1e-8,
+                                    maxit=2000)
+            worst_it = max(worst_it, abs(int(res.iterations[k]) - it) / max(it, 1))
+            r = bh[off:off + m] - lo.spmv(a, x[off:off + m])
+            worst_rel = max(worst_rel, float(np.linalg.norm(r) / np.linalg.norm(bh[off:off + m])))
+        off += m
+    out["oracle_check"] = {"systems": oracle_check, "max_iteration_gap": worst_it,
+                           "max_rel_residual_fp64": worst_rel}
+    if cpu_sample:
+        sample = systems[:cpu_sample]
         rng = np.random.default_rng(0)
         t0 = time.perf_counter()
         srows = 0
@@ -891,6 +983,20 @@ def run_batch(args):
                                          f"by rows to the batch"}
     log(f"[batch] {len(systems)} systems, {rows} rows: {ms:.1f} ms, "
         f"mean {out['iterations_mean']:.1f} it, converged {out['converged']}")
+    return out
+
+
+def run_batch(args):
+    """Batching form: Jacobi-BiCGStab to 1e-8 on 1024 uneven convection-diffusion
+    systems in one persistent launch (per step: the whole batch, b resident)."""
+    import torch
+
+    import lineal_gb300 as g
+
+    g.build.build()
+    out = batch_entry(g, args.steps, args.warmup, torch.cuda.current_stream(),
+                      args.batch_systems, args.batch_cpu_sample if args.cpu_baseline else 0)
+    out["mode"] = "batch"
     print(json.dumps(out), flush=True)
 
 
@@ -927,50 +1033,31 @@ def run_profile(args):
     log(f"[profile] {form} solve: {res.iterations} it")
 
 
-def run_multi(args):
-    """Batching form, second part: a --grid^3 (default 128^3) 7-point Poisson
-    CSR with 32 right-hand sides uniform in [-1, 1], solved to 1e-8 by blocked
-    AMG-PCG (FP64 outer iteration, float V-cycle), against 32 single-vector
-    solves of the same hierarchy."""
+def multi_entry(g, steps, warmup, stream, grid=128, partition_size=4096):
+    """Batching form, second part: a grid^3 7-point Poisson CSR with 32
+    right-hand sides uniform in [-1, 1], solved to 1e-8 by blocked AMG-PCG
+    (FP64 outer iteration, float V-cycle), against 32 single-vector solves of
+    the same hierarchy."""
     import torch
 
-    import lineal_gb300 as g
-
-    g.build.build()
-    grid = args.grid
     dims = (grid,) * 3
     n = grid ** 3
     a = g.gen_7pt(dims, np.ones(n))
     col = g.Colouring.from_array(a, red_black_colours(dims), 2)
     h = g.HierarchyWright(min_coarsen_size=2000, cycle_f32=True,
-                          partition_size=args.partition_size).instantiate(a, finest_colouring=col)
+                          partition_size=partition_size).instantiate(a, finest_colouring=col)
     B = torch.as_tensor(np.random.default_rng(0).uniform(-1, 1, (n, 32)), device="cuda")
-    stream = torch.cuda.current_stream()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    for _ in range(args.warmup):
-        X, its, rels = g.pcg_multi(a, h, B, rtol=1e-8)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(args.steps):
-        X, its, rels = g.pcg_multi(a, h, B, rtol=1e-8)
-    e1.record(stream)
-    e1.synchronize()
-    ms_block = e0.elapsed_time(e1) / args.steps
+    ms_block, (X, its, rels) = timed(lambda: g.pcg_multi(a, h, B, rtol=1e-8), steps, warmup,
+                                     stream)
     cols = B.t().contiguous()
-    for _ in range(2):
-        g.pcg(a, cols[0], precon=g.PRECON_AMG, amg=h, rtol=1e-8, flexible=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    single_its = []
-    for c in range(32):
-        r = g.pcg(a, cols[c], precon=g.PRECON_AMG, amg=h, rtol=1e-8, flexible=True)
-        single_its.append(r.iterations)
-    e1.record(stream)
-    e1.synchronize()
-    ms_single = e0.elapsed_time(e1)
+
+    def singles():
+        return [g.pcg(a, cols[c], precon=g.PRECON_AMG, amg=h, rtol=1e-8, flexible=True)
+                .iterations for c in range(32)]
+
+    ms_single, single_its = timed(singles, 1, 2, stream)
     _, rn = g.residual(a, B[:, 0].contiguous(), X[:, 0].contiguous())
-    out = {"mode": "multi", "workload": f"{grid}^3 7-point Poisson CSR, 32 RHS, AMG-PCG to 1e-8",
+    out = {"workload": f"{grid}^3 7-point Poisson CSR, 32 RHS, AMG-PCG to 1e-8",
            "rows": n, "ms_blocked": ms_block, "ms_32_single_solves": ms_single,
            "speedup": ms_single / ms_block, "iterations_blocked_max": int(its.max()),
            "iterations_single_max": int(max(single_its)),
@@ -979,39 +1066,48 @@ def run_multi(args):
                                      float(torch.linalg.norm(B[:, 0]).item())}
     log(f"[multi] blocked {ms_block:.1f} ms vs 32 single solves {ms_single:.1f} ms, "
         f"{int(its.max())} it")
-    print(json.dumps(out), flush=True)
+    return out
 
 
-def run_adjoint(args):
-    """Differentiation form at --grid^3 (default workload 128^3): x = A(theta)^-1 b
-    for the 7-point operator with k = exp(theta), theta ~ N(0, 1) (seed 4), b a
-    Gaussian bump, x_target the solve at theta + 0.3 N(0, 1); loss
-    0.5 ||x - x_target||^2.  Times the forward (mixed: flexible CG over the float
-    V-cycle) and backward solves, checks the gradient against FP64 central
-    differences along --fd-directions random N(0, 1) directions (h = 1e-6; both
-    solves start from the solution at theta and are refined to full FP64
-    accuracy with compensated residuals, the loss difference is formed
-    directly) and against the all-FP64 gradient."""
+def run_multi(args):
+    """The 32-right-hand-side part of the batching form as its own line."""
     import torch
 
     import lineal_gb300 as g
-    from lineal_gb300.autograd import SolveOptions, diffusion7_solve
 
     g.build.build()
-    dims = (args.grid,) * 3
-    n = args.grid ** 3
+    out = multi_entry(g, args.steps, args.warmup, torch.cuda.current_stream(), args.grid,
+                      args.partition_size)
+    out["mode"] = "multi"
+    print(json.dumps(out), flush=True)
+
+
+def adjoint_entry(g, grid, directions, warmup=1):
+    """Differentiation form at grid^3 (workload 128^3): x = A(theta)^-1 b for
+    the 7-point operator with k = exp(theta), theta ~ N(0, 1) (seed 4), b a
+    Gaussian bump, x_target the solve at theta + 0.3 N(0, 1); loss
+    0.5 ||x - x_target||^2.  Times the forward (mixed: flexible CG over the
+    float V-cycle) and backward solves, checks the gradient against FP64
+    central differences along `directions` random N(0, 1) directions
+    (h = 1e-6; perturbed solutions from accurately formed right-hand sides
+    and compensated defect correction) and against the all-FP64 gradient."""
+    import torch
+
+    from lineal_gb300.autograd import (SolveOptions, accurate_gradient, accurate_system,
+                                       diffusion7_solve, loss_difference_fd)
+
+    dims = (grid,) * 3
+    n = grid ** 3
     rng = np.random.default_rng(4)
     theta0 = rng.standard_normal(n)
     theta_t = theta0 + 0.3 * rng.standard_normal(n)
     i, j, k = np.meshgrid(*[np.arange(d, dtype=np.float64) for d in dims], indexing="ij")
-    c, s = (args.grid - 1) / 2, args.grid / 6.0
+    c, s = (grid - 1) / 2, grid / 6.0
     b = torch.as_tensor(np.exp(-((i - c) ** 2 + (j - c) ** 2 + (k - c) ** 2) / (2 * s * s)).ravel(),
                         device="cuda")
     fp64 = SolveOptions(rtol=1e-11)
     mixed = SolveOptions(rtol=1e-10, mixed=True)
-    from lineal_gb300.autograd import accurate_forward, loss_difference_fd
-
-    x_t = accurate_forward(torch.as_tensor(theta_t, device="cuda"), b, dims)
+    _, _, x_t = accurate_system(torch.as_tensor(theta_t, device="cuda"), b, dims)
 
     def grad(opts):
         th = torch.as_tensor(theta0, device="cuda").requires_grad_(True)
@@ -1026,40 +1122,46 @@ def run_adjoint(args):
         t2 = time.perf_counter()
         return th.grad.detach(), float(loss), (t1 - t0) * 1e3, (t2 - t1) * 1e3
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         grad(mixed)
     g_mixed, loss_m, fwd_ms, bwd_ms = grad(mixed)
-    g_64, loss_64, fwd64_ms, bwd64_ms = grad(fp64)
+    g_64, _, fwd64_ms, bwd64_ms = grad(fp64)
     rel_vs_fp64 = float(torch.linalg.norm(g_mixed - g_64) / torch.linalg.norm(g_64))
-
-    from lineal_gb300.autograd import accurate_gradient
-
+    th0 = torch.as_tensor(theta0, device="cuda")
+    a0, h0, x0 = accurate_system(th0, b, dims)
+    g_ref = accurate_gradient(th0, b, dims, x_t)
     drng = np.random.default_rng(6)
     h = 1e-6
-    th0 = torch.as_tensor(theta0, device="cuda")
-    fd_opts = SolveOptions(rtol=1e-10)
-    x0 = accurate_forward(th0, b, dims)
-    g_ref = accurate_gradient(th0, b, dims, x_t)
     errs = {"mixed": [], "fp64": [], "refined": []}
-    for _ in range(args.fd_directions):
+    t0 = time.perf_counter()
+    for _ in range(directions):
         vt = torch.as_tensor(drng.standard_normal(n), device="cuda")
-        fd = loss_difference_fd(th0, vt, h, b, dims, x0, x_t, fd_opts)
+        fd = loss_difference_fd(th0, vt, h, dims, x0, x_t, a0, h0)
         for tag, gg in (("mixed", g_mixed), ("fp64", g_64), ("refined", g_ref)):
             gv = float(torch.dot(gg, vt))
             errs[tag].append(abs(fd - gv) / abs(gv))
-    worst = max(errs["mixed"])
+    fd_s = time.perf_counter() - t0
     fd_stats = {tag: {"max": float(np.max(e)), "median": float(np.median(e))}
                 for tag, e in errs.items()}
     rel_ref = float(torch.linalg.norm(g_mixed - g_ref) / torch.linalg.norm(g_ref))
-    out = {"mode": "adjoint", "workload": f"{args.grid}^3 7-point, k = exp(theta), theta ~ N(0,1)",
+    out = {"workload": f"{grid}^3 7-point, k = exp(theta), theta ~ N(0,1)",
            "forward_ms": fwd_ms, "backward_ms": bwd_ms, "forward_fp64_ms": fwd64_ms,
            "backward_fp64_ms": bwd64_ms, "loss": loss_m,
-           "grad_rel_error_vs_fp64": rel_vs_fp64,
-           "grad_rel_error_vs_refined": rel_ref,
-           "fd_directions": args.fd_directions, "fd_step": h, "fd_max_rel_error": worst,
-           "fd_rel_error_by_gradient": fd_stats}
-    log(f"[adjoint] fwd {fwd_ms:.1f} ms bwd {bwd_ms:.1f} ms; fd max rel {worst:.2e}; "
-        f"vs fp64 {rel_vs_fp64:.2e}")
+           "grad_rel_error_vs_fp64": rel_vs_fp64, "grad_rel_error_vs_refined": rel_ref,
+           "fd_directions": directions, "fd_step": h, "fd_max_rel_error": fd_stats["mixed"]["max"],
+           "fd_rel_error_by_gradient": fd_stats, "fd_seconds": fd_s}
+    log(f"[adjoint] fwd {fwd_ms:.1f} ms bwd {bwd_ms:.1f} ms; fd max rel "
+        f"{fd_stats['mixed']['max']:.2e}; vs fp64 {rel_vs_fp64:.2e}")
+    return out
+
+
+def run_adjoint(args):
+    """The differentiation form as its own line (all --fd-directions)."""
+    import lineal_gb300 as g
+
+    g.build.build()
+    out = adjoint_entry(g, args.grid, args.fd_directions, args.warmup)
+    out["mode"] = "adjoint"
     print(json.dumps(out), flush=True)
 
 
@@ -1095,6 +1197,10 @@ def main():
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-configs", dest="configs", action="store_false",
+                    help="skip the 64^3 Jacobi-PCG, batch, 32-RHS and adjoint keys")
+    ap.add_argument("--bench-fd-directions", type=int, default=16,
+                    help="finite-difference directions of the default line's adjoint key")
     ap.add_argument("--coarse-smallest-last", action="store_true",
                     help="colour AMG levels >= 1 by the host smallest-last colouring")
     args = ap.parse_args()

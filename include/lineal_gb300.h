@@ -94,6 +94,17 @@ lgx_status lgx_csr_download(const lgx_matrix *a, int64_t *h_rowptr, int32_t *h_c
  * .hpp:67-79).  Lookup: d_mat holds one material index (< 4) per cell and
  * coeffs the material conductivities.  Value: d_k holds one conductivity per
  * cell.  zero_to_one selects ZeroToOneTag (a zero diagonal becomes 1). */
+/* BoxInfo (discretization/box-equidistant.hpp:57-110): an equidistant box of
+ * cells[d] cells along axis d with axis lengths lengths[d].  The axis
+ * quotients (67-79) are q_d = prod_{e != d} h_e / h_d with h = L / N, the
+ * geometric factors the stencil valuators take as q.  Host-only; refuses
+ * non-positive counts and non-positive or non-finite lengths. */
+typedef struct {
+  int64_t cells[3];
+  double lengths[3];
+} lgx_box_info;
+lgx_status lgx_box_axis_quotients(const lgx_box_info *box, double q[3]);
+
 lgx_status lgx_stencil_create_lookup(const int64_t dims[3], const double q[3],
                                      const double coeffs[4], const uint8_t *d_mat,
                                      double sol_start, double sol_end, int zero_to_one,
@@ -231,7 +242,9 @@ lgx_status lgx_matrix_autotune(lgx_matrix *a, int reps, lgx_tune_entry *out, lgx
 /* ------------------------------------------------------------------------
  * Vector reductions and updates (component-wise/sink/accumulator.hpp:151-218,
  * vector-expression.hpp:67-92).  Reductions are deterministic: fixed block
- * partition, fixed-order second stage.  Results land in device memory.
+ * partition, fixed-order second stage.  Results land in device memory; the
+ * reductions synchronise `stream`.  Their partial sums are allocated once per
+ * stream (9.7 KB, kept for the process), so repeated calls do not allocate.
  * ---------------------------------------------------------------------- */
 lgx_status lgx_dot(int64_t n, const double *d_a, const double *d_b, double *d_out,
                    lgx_stream stream);
@@ -240,11 +253,12 @@ lgx_status lgx_norm2sq(int64_t n, const double *d_a, double *d_out, lgx_stream s
 /* lgx_dot without any device allocation.  No reference counterpart: lineal's
  * dot (sink/accumulator.hpp:151-157) is a CPU reduction with no scratch.
  *
- * lgx_dot allocates and frees its partial sums on every call, and cudaFree
- * waits for the whole device.  Callers that must not allocate (code whose
- * device memory is all handed to its own pool, or a loop that keeps several
- * streams busy and cannot afford that device-wide wait) call this instead:
- * the partial sums live in a fixed static device array of the library.
+ * lgx_dot allocates its partial sums with cudaMalloc on the first call on
+ * each stream (and keeps them).  Callers that must not allocate at all (code
+ * whose device memory is all handed to its own pool, or that may run on a
+ * fresh stream inside a region where an allocation would stall or fail) call
+ * this instead: the partial sums live in a fixed static device array of the
+ * library.
  *
  * - Result: the same as lgx_dot (same grid, same summation order), written to
  *   d_out in stream order; the call does not synchronise.
@@ -257,7 +271,9 @@ lgx_status lgx_norm2sq(int64_t n, const double *d_a, double *d_out, lgx_stream s
  *   streams, or two host threads) race on it and give wrong results.  Calls on
  *   one stream are ordered and safe.
  * - The scratch's arrival counter must be zero when a call starts; it is zero
- *   when the library loads and every completed call leaves it at zero. */
+ *   when the library loads and every completed call leaves it at zero.
+ * - cudaDeviceReset ends the context whose scratch address the first call
+ *   looked up; calls after a reset of that device are not supported. */
 lgx_status lgx_dot_static(int64_t n, const double *d_a, const double *d_b, double *d_out,
                           lgx_stream stream);
 lgx_status lgx_max_norm(int64_t n, const double *d_a, double *d_out, lgx_stream stream);
@@ -300,6 +316,14 @@ lgx_status lgx_colouring_create_jp(const lgx_matrix *a, uint64_t seed, lgx_strea
  * to lgx_colouring_create. */
 lgx_status lgx_colour_smallest_last(int64_t n, const int64_t *rowptr, const int32_t *col,
                                     int32_t *colour, int32_t *ncolours);
+/* Red-black colouring of a stencil matrix, colour (p0 + p1 + p2) & 1: the
+ * 7-point stencil's natural two-colouring.  lgx_sor_sweep then runs
+ * matrix-free in natural order, one launch per colour, and equals lineal's
+ * SOR of the assembled matrix in the row order sorted by (colour, index);
+ * SSOR preconditioning of a stencil uses it too.  The permuted-order entry
+ * points refuse it. */
+lgx_status lgx_colouring_create_red_black(const lgx_matrix *a, lgx_stream stream,
+                                          lgx_colouring **out);
 /* User colouring (device array, one colour in [0, ncolours) per row; e.g.
  * the parity colouring of a structured grid).  Validated on the device. */
 lgx_status lgx_colouring_create(const lgx_matrix *a, const int32_t *d_colour, int32_t ncolours,
@@ -550,6 +574,19 @@ typedef struct {
                                    for preconditioners that are not exactly linear (the
                                    float V-cycle of the precision form); no counterpart
                                    in the reference's CG (solver.hpp:105-107) */
+  int refine;                   /* lgx_pcg with an AMG hierarchy built with cycle_f32:
+                                   FP64 iterative refinement (precision form; no
+                                   reference counterpart).  Each outer step forms the
+                                   FP64 residual r = b - A x, solves A d = r / ||r|| by
+                                   PCG with float vectors (float finest-level products
+                                   and float V-cycle; dot products accumulated and CG
+                                   scalars kept in FP64) to inner_rtol, and adds
+                                   ||r|| d to x in FP64; it stops on the FP64 residual.
+                                   *iterations counts the inner iterations (one product
+                                   and one V-cycle each), h_history holds the inner
+                                   residual estimates and, after each outer step, the
+                                   FP64 residual */
+  double inner_rtol;            /* refine: inner relative tolerance (1e-4) */
 } lgx_solve_params;
 
 void lgx_solve_default_params(lgx_solve_params *p);

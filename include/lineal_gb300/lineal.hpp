@@ -220,10 +220,48 @@ class CsrMatrix : public MatrixHandle {
   }
 };
 
+// BoxInfo (discretization/box-equidistant.hpp:57-110): cell counts and axis
+// lengths of an equidistant box and the axis quotients the valuators use
+struct BoxInfo {
+  std::array<int64_t, 3> cell_nums;
+  std::array<double, 3> lengths;
+
+  BoxInfo(std::array<int64_t, 3> cells, std::array<double, 3> axis_lengths)
+      : cell_nums(cells), lengths(axis_lengths) {
+    axis_quotients();  // validates
+  }
+  [[nodiscard]] std::array<double, 3> axis_lengths() const { return lengths; }
+  [[nodiscard]] double axis_length(std::size_t axis) const { return lengths[axis]; }
+  [[nodiscard]] std::array<double, 3> axis_quotients() const {
+    lgx_box_info b{};
+    for (int d = 0; d < 3; ++d) {
+      b.cells[d] = cell_nums[d];
+      b.lengths[d] = lengths[d];
+    }
+    std::array<double, 3> q{};
+    check(lgx_box_axis_quotients(&b, q.data()));
+    return q;
+  }
+  [[nodiscard]] double axis_quotient(std::size_t axis) const { return axis_quotients()[axis]; }
+};
+
 // AdjacentStencilMatrix with a StationaryDiffusionLookupValuator / ValueValuator
 class StencilMatrix : public MatrixHandle {
  public:
   using MatrixHandle::MatrixHandle;
+  // the valuators' BoxInfo constructors (stationary-diffusion-lookup.hpp:28-60)
+  static StencilMatrix lookup(const BoxInfo &box, const double coeffs[4],
+                              const DenseVector<uint8_t> &materials, double sol_start,
+                              double sol_end, bool zero_to_one, const Environment &env) {
+    const auto q = box.axis_quotients();
+    return lookup(box.cell_nums.data(), q.data(), coeffs, materials, sol_start, sol_end,
+                  zero_to_one, env);
+  }
+  static StencilMatrix value(const BoxInfo &box, const DenseVector<double> &k, double sol_start,
+                             double sol_end, bool zero_to_one, const Environment &env) {
+    const auto q = box.axis_quotients();
+    return value(box.cell_nums.data(), q.data(), k, sol_start, sol_end, zero_to_one, env);
+  }
   static StencilMatrix lookup(const int64_t dims[3], const double q[3], const double coeffs[4],
                               const DenseVector<uint8_t> &materials, double sol_start,
                               double sol_end, bool zero_to_one, const Environment &env) {

@@ -117,6 +117,8 @@ class _SolveParams(C.Structure):
         ("rere_period", C.c_int64),
         ("use_graphs", C.c_int),
         ("flexible", C.c_int),
+        ("refine", C.c_int),
+        ("inner_rtol", C.c_double),
     ]
 
 
@@ -378,6 +380,39 @@ class CsrMatrix(_Matrix):
         return rowptr, col, val
 
 
+class _BoxInfo(C.Structure):
+    _fields_ = [("cells", C.c_int64 * 3), ("lengths", C.c_double * 3)]
+
+
+class BoxInfo:
+    """BoxInfo (discretization/box-equidistant.hpp:57-110): cell counts and
+    axis lengths of an equidistant box; axis_quotients() are the stencil
+    valuators' geometric factors q_d = prod_{e != d} h_e / h_d, h = L / N."""
+
+    def __init__(self, cells, lengths):
+        self.cells = tuple(int(c) for c in cells)
+        self.lengths = tuple(float(v) for v in lengths)
+        if len(self.cells) != 3 or len(self.lengths) != 3:
+            raise ValueError("BoxInfo needs three cell counts and three axis lengths")
+
+    def axis_quotients(self) -> np.ndarray:
+        box = _BoxInfo((C.c_int64 * 3)(*self.cells), (C.c_double * 3)(*self.lengths))
+        q = np.zeros(3)
+        _check(lib().lgx_box_axis_quotients(C.byref(box), _ptr(q)))
+        return q
+
+
+def _box_q(dims, q):
+    """(dims, q) from a BoxInfo given as dims (q then must be None), else as given"""
+    if isinstance(dims, BoxInfo):
+        if q is not None:
+            raise ValueError("give either a BoxInfo or dims with q, not both")
+        return dims.cells, dims.axis_quotients()
+    if q is None:
+        raise ValueError("q (axis quotients) is required unless dims is a BoxInfo")
+    return dims, q
+
+
 class StencilMatrix(_Matrix):
     """AdjacentStencilMatrix over a stationary-diffusion valuator (7-point,
     Dirichlet on the faces of axis 0)."""
@@ -385,7 +420,9 @@ class StencilMatrix(_Matrix):
     @classmethod
     def lookup(cls, dims, q, coeffs, materials, sol_start=1.0, sol_end=0.0,
                zero_to_one=True) -> "StencilMatrix":
+        """Lookup valuator; dims may be a BoxInfo (then q=None)."""
         torch = _torch()
+        dims, q = _box_q(dims, q)
         d = np.ascontiguousarray(dims, dtype=np.int64)
         qq = np.ascontiguousarray(q, dtype=np.float64)
         cc = np.ascontiguousarray(coeffs, dtype=np.float64)
@@ -397,6 +434,8 @@ class StencilMatrix(_Matrix):
 
     @classmethod
     def value(cls, dims, q, k, sol_start=1.0, sol_end=0.0, zero_to_one=True) -> "StencilMatrix":
+        """Value valuator; dims may be a BoxInfo (then q=None)."""
+        dims, q = _box_q(dims, q)
         d = np.ascontiguousarray(dims, dtype=np.int64)
         qq = np.ascontiguousarray(q, dtype=np.float64)
         kk = _dvec(k)
@@ -408,8 +447,10 @@ class StencilMatrix(_Matrix):
     @classmethod
     def lookup_henry(cls, dims, q, coeffs, materials, henry, gaseous_mask, sol_start=1.0,
                      sol_end=0.0, zero_to_one=True) -> "StencilMatrix":
-        """Lookup valuator with the Henry-law diffusion factors."""
+        """Lookup valuator with the Henry-law diffusion factors; dims may be a
+        BoxInfo (then q=None)."""
         torch = _torch()
+        dims, q = _box_q(dims, q)
         d = np.ascontiguousarray(dims, dtype=np.int64)
         qq = np.ascontiguousarray(q, dtype=np.float64)
         cc = np.ascontiguousarray(coeffs, dtype=np.float64)
@@ -423,7 +464,9 @@ class StencilMatrix(_Matrix):
     @classmethod
     def values(cls, dims, q, k_axes, sol_start=1.0, sol_end=0.0,
                zero_to_one=True) -> "StencilMatrix":
-        """StationaryDiffusionValuesValuator: one conductivity array per axis."""
+        """StationaryDiffusionValuesValuator: one conductivity array per axis;
+        dims may be a BoxInfo (then q=None)."""
+        dims, q = _box_q(dims, q)
         d = np.ascontiguousarray(dims, dtype=np.int64)
         qq = np.ascontiguousarray(q, dtype=np.float64)
         k0, k1, k2 = (_dvec(v) for v in k_axes)
@@ -563,6 +606,14 @@ class Colouring:
     def jp(cls, a: CsrMatrix, seed: int = 0x5EED) -> "Colouring":
         h = C.c_void_p()
         _check(lib().lgx_colouring_create_jp(a.handle, seed, _stream(), C.byref(h)))
+        return cls(h, a.row_num())
+
+    @classmethod
+    def red_black(cls, a: "StencilMatrix") -> "Colouring":
+        """Red-black colouring of a stencil matrix: its SOR sweeps run
+        matrix-free in natural order."""
+        h = C.c_void_p()
+        _check(lib().lgx_colouring_create_red_black(a.handle, _stream(), C.byref(h)))
         return cls(h, a.row_num())
 
     @classmethod
@@ -964,7 +1015,8 @@ class SolveResult:
 
 def _solve(fn, a: _Matrix, b, x0=None, precon=PRECON_NONE, relax=1.0, ultra=False,
            colouring: Colouring | None = None, amg: Hierarchy | None = None, rtol=1e-8,
-           maxit=1000, rere_period=8, use_graphs=True, flexible=False) -> SolveResult:
+           maxit=1000, rere_period=8, use_graphs=True, flexible=False, refine=False,
+           inner_rtol=1e-4) -> SolveResult:
     b = _dvec(b)
     x = _dvec(x0) if x0 is not None else _empty(b.numel()).zero_()
     if x0 is not None:
@@ -981,6 +1033,8 @@ def _solve(fn, a: _Matrix, b, x0=None, precon=PRECON_NONE, relax=1.0, ultra=Fals
     p.rere_period = rere_period
     p.use_graphs = int(use_graphs)
     p.flexible = int(flexible)
+    p.refine = int(refine)
+    p.inner_rtol = inner_rtol
     it = C.c_int64()
     rel = C.c_double()
     hist = np.zeros(maxit + 1)
@@ -1052,7 +1106,10 @@ def diffusion7_grad(dims, k, lam, x):
 
 def pcg(a: _Matrix, b, **kw) -> SolveResult:
     """Preconditioned CG (ConjugateGradientsSolver); flexible=True selects the
-    flexible-CG beta for the float V-cycle of the precision form."""
+    flexible-CG beta for the float V-cycle of the precision form; refine=True
+    (AMG hierarchy with cycle_f32) runs FP64 iterative refinement over a
+    float-vector PCG with FP64 dots and scalars, each inner solve to
+    inner_rtol."""
     return _solve(lib().lgx_pcg, a, b, **kw)
 
 

@@ -146,18 +146,95 @@ def accurate_gradient(theta, b, dims, x_target, opts: SolveOptions | None = None
     return diffusion7_grad(dims, k, lam, x)
 
 
-def loss_difference_fd(theta, v, h, b, dims, x, x_target, opts: SolveOptions | None = None):
-    """Central difference of L = 0.5 ||x - x_target||^2 along v:
-    (L(theta + h v) - L(theta - h v)) / (2 h).  Both solves start from the
-    solution x at theta and are refined to full FP64 accuracy (compensated
-    residuals), and the loss difference is formed as
-    0.5 sum (x+ - x-)(x+ + x- - 2 x_target), so neither solver error nor the
-    rounding of the two large losses swamps the O(h) difference."""
+def accurate_system(theta, b, dims, opts: SolveOptions | None = None):
+    """(A, hierarchy, x) at theta with x = A^-1 b to full FP64 accuracy."""
     import torch
 
-    xp = accurate_forward(theta + h * v, b, dims, opts, x0=x)
-    xm = accurate_forward(theta - h * v, b, dims, opts, x0=x)
-    num = 0.5 * torch.sum((xp - xm) * (xp + xm - 2.0 * x_target))
+    opts = opts or SolveOptions()
+    dims = tuple(int(d) for d in dims)
+    a, col = _operator(theta, dims)
+    h = HierarchyWright(min_coarsen_size=opts.min_coarsen_size,
+                        partition_size=opts.partition_size).instantiate(a, finest_colouring=col)
+    b = b.detach().to(torch.float64)
+    x = refined_solve(a, b, pcg(a, b, precon=PRECON_AMG, amg=h, rtol=opts.rtol,
+                                maxit=opts.maxit).x, h)
+    return a, h, x
+
+
+def diffusion7_delta_apply(theta, dtheta, x, dims):
+    """(A(theta + dtheta) - A(theta)) x for the operator of gen_7pt with
+    k = exp(theta), without forming either matrix.  A face coefficient is
+    c = 2 / (e^-theta_i + e^-theta_j); its change is
+    -2 du / (u (u + du)) with u = e^-theta_i + e^-theta_j and
+    du = e^-theta_i expm1(-dtheta_i) + e^-theta_j expm1(-dtheta_j), and an
+    axis-0 boundary face changes the diagonal by 2 e^theta expm1(dtheta).
+    Every term is formed from expm1, so the O(|dtheta|) result keeps full
+    FP64 relative accuracy (differencing the two assembled matrices would
+    leave rounding errors of relative size eps / |dtheta|)."""
+    import torch
+
+    n0, n1, n2 = (int(d) for d in dims)
+    th = theta.detach().to(torch.float64).reshape(n0, n1, n2)
+    dt = dtheta.detach().to(torch.float64).reshape(n0, n1, n2)
+    xx = x.detach().to(torch.float64).reshape(n0, n1, n2)
+    em = torch.exp(-th)
+    dm = em * torch.expm1(-dt)
+    y = torch.zeros_like(xx)
+    for ax in range(3):
+        lo = [slice(None)] * 3
+        hi = [slice(None)] * 3
+        lo[ax] = slice(0, -1)
+        hi[ax] = slice(1, None)
+        lo, hi = tuple(lo), tuple(hi)
+        u = em[lo] + em[hi]
+        du = dm[lo] + dm[hi]
+        dc = -2.0 * du / (u * (u + du))
+        f = dc * (xx[lo] - xx[hi])
+        y[lo] += f
+        y[hi] -= f
+    dk = 2.0 * torch.exp(th) * torch.expm1(dt)
+    y[0] += dk[0] * xx[0]
+    y[-1] += dk[-1] * xx[-1]
+    return y.reshape(-1)
+
+
+def perturbed_correction(theta, dtheta, dims, x, a0, h0, steps=4, rtol=1e-10):
+    """d = A(theta + dtheta)^-1 b - x for x = A(theta)^-1 b, solved from
+    A(theta + dtheta) d = -(A(theta + dtheta) - A(theta)) x: a small
+    right-hand side formed accurately (diffusion7_delta_apply), then defect
+    correction with compensated residuals of A(theta + dtheta) and AMG-PCG
+    solves with A(theta) (matrix a0, hierarchy h0) as the approximate inverse.
+    d carries full FP64 relative accuracy although it is O(|dtheta|)."""
+    import torch
+
+    dims = tuple(int(d) for d in dims)
+    a1, _ = _operator(theta + dtheta, dims)
+    rhs = -diffusion7_delta_apply(theta, dtheta, x, dims)
+    d = torch.zeros_like(rhs)
+    rn0 = float(torch.linalg.norm(rhs))
+    for _ in range(steps):
+        r = residual_compensated(a1, rhs, d)
+        if float(torch.linalg.norm(r)) <= 1e-17 * rn0:
+            break
+        d = d + pcg(a0, r, precon=PRECON_AMG, amg=h0, rtol=rtol, maxit=2000).x
+    return d
+
+
+def loss_difference_fd(theta, v, h, dims, x, x_target, a0, h0):
+    """Central difference of L = 0.5 ||x - x_target||^2 along v,
+    (L(theta + h v) - L(theta - h v)) / (2 h), with x(theta +- h v) =
+    x + d+- from perturbed_correction (x, a0, h0: the accurate solution,
+    matrix and hierarchy at theta).  The loss difference is formed as
+    (d+ - d-).(x - x_target) + 0.5 (d+.d+ - d-.d-), so neither the rounding
+    of the two large losses nor that of the assembled perturbed matrices
+    (relative eps / h in A(theta +- h v) - A(theta)) swamps the O(h)
+    difference: what remains is the O(h^2) truncation and FP64 rounding
+    relative to the difference itself."""
+    import torch
+
+    dp = perturbed_correction(theta, h * v, dims, x, a0, h0)
+    dm = perturbed_correction(theta, -h * v, dims, x, a0, h0)
+    num = torch.dot(dp - dm, x - x_target) + 0.5 * (torch.dot(dp, dp) - torch.dot(dm, dm))
     return float(num) / (2.0 * h)
 
 

@@ -8,6 +8,8 @@
 // transport/vector-shared.hpp, hierarchy/wright.hpp, solver.hpp).
 #include <cuda_runtime.h>
 
+#include <cfloat>
+
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -39,6 +41,12 @@ __device__ __forceinline__ int64_t find_col(const int64_t *rowptr, const int32_t
     if (col[mid] < c) lo = mid + 1; else hi = mid;
   }
   return (lo < end && col[lo] == c) ? lo : -1;
+}
+
+__global__ void k_iota(int64_t n, int32_t *out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (int32_t)i;
 }
 
 template <typename VT>
@@ -783,13 +791,24 @@ __global__ void k_dense_from_csr(int64_t n, const int64_t *rowptr, const int32_t
   }
 }
 
-// step k, part 1: pivot row scaled into prow, column factors into pcol
-__global__ void k_gj_pivot(int64_t n, int64_t k, double *a, double *prow, double *pcol,
-                           int *bad, int spd) {
+// step k, part 1: pivot row scaled into prow, column factors into pcol.
+// LuSolver's unpivoted elimination (lu/decomposition.hpp:31-122) needs a
+// usable pivot: non-zero, finite and not below 64 eps times the largest
+// entry of its row (every block forms the row maximum itself).
+__global__ void __launch_bounds__(256)
+  k_gj_pivot(int64_t n, int64_t k, double *a, double *prow, double *pcol, int *bad) {
   const double p = a[k * n + k];
-  // symmetric hierarchies: CholeskySolver's positive pivots; nonsymmetric:
-  // LuSolver's unpivoted elimination, which needs a nonzero finite pivot
-  if (spd ? !(p > 0.0) : !(p != 0.0 && isfinite(p))) {
+  __shared__ double red[256];
+  double m = 0.0;
+  for (int64_t j = threadIdx.x; j < n; j += blockDim.x) m = fmax(m, fabs(a[k * n + j]));
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+    __syncthreads();
+  }
+  const double rowmax = red[0];
+  if (!(p != 0.0 && isfinite(p)) || fabs(p) < 64.0 * DBL_EPSILON * rowmax) {
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(bad, 1);
     return;
   }
@@ -817,6 +836,58 @@ __global__ void k_gj_update(int64_t n, int64_t k, double *a, const double *prow,
   }
 }
 
+// ---- dense FP64 Cholesky of the coarsest matrix (CholeskySolver,
+// cholesky/decomposition.hpp:52-107, on the dense matrix): A = L L^T in the
+// lower triangle, right-looking, one column per step; every pivot must be
+// positive.  The inverse applied per V-cycle is then formed from the factor:
+// Y = L^-1 (forward substitution of the identity, all columns at once) and
+// A^-1 = Y^T Y.
+__global__ void __launch_bounds__(256) k_chol_column(int64_t n, int64_t k, double *a, int *bad) {
+  const double d = a[k * n + k];
+  if (!(d > 0.0) || !isfinite(d)) {
+    if (threadIdx.x == 0) atomicOr(bad, 1);
+    return;
+  }
+  const double lkk = sqrt(d);
+  for (int64_t i = k + 1 + threadIdx.x; i < n; i += blockDim.x) a[i * n + k] = a[i * n + k] / lkk;
+  if (threadIdx.x == 0) a[k * n + k] = lkk;
+}
+
+// trailing update of the lower triangle: a_ij -= l_ik l_jk for k < j <= i
+__global__ void k_chol_update(int64_t n, int64_t k, double *a, const int *bad) {
+  if (*bad) return;
+  const int64_t m = n - k - 1;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < m * m;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = k + 1 + t / m, j = k + 1 + t % m;
+    if (j > i) continue;
+    a[i * n + j] = fma(-a[i * n + k], a[j * n + k], a[i * n + j]);
+  }
+}
+
+// row i of Y = L^-1 (lower triangular): y_ic = (delta_ic - sum_{c<=j<i} l_ij
+// y_jc) / l_ii for every column c <= i
+__global__ void k_chol_inv_row(int64_t n, int64_t i, const double *l, double *y) {
+  const double lii = l[i * n + i];
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c <= i;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    double s = c == i ? 1.0 : 0.0;
+    for (int64_t j = c; j < i; ++j) s = fma(-l[i * n + j], y[j * n + c], s);
+    y[i * n + c] = s / lii;
+  }
+}
+
+// A^-1 = Y^T Y: entry (i, j) = sum_{k >= max(i, j)} y_ki y_kj
+__global__ void k_chol_inv_gram(int64_t n, const double *y, double *inv) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t / n, j = t % n;
+    double s = 0.0;
+    for (int64_t k = i > j ? i : j; k < n; ++k) s = fma(y[k * n + i], y[k * n + j], s);
+    inv[t] = s;
+  }
+}
+
 // x = A^-1 b, one warp per row
 template <typename XT>
 __global__ void k_dense_apply(int64_t n, const double *ainv, const XT *b, XT *x) {
@@ -834,21 +905,56 @@ __global__ void k_dense_apply(int64_t n, const double *ainv, const XT *b, XT *x)
   }
 }
 
-// Explicit inverse of the coarsest matrix by Gauss-Jordan elimination without
-// pivoting: the elimination of CholeskySolver (symmetric matrices: every
-// pivot must be positive) or of LuSolver (nonsymmetric: nonzero pivots;
-// lu/decomposition.hpp:31-122 does not pivot either), applied later as one
-// dense product per V-cycle.
+// The explicit inverse of the coarsest matrix, applied as one dense product
+// per V-cycle (a warp per row: the whole solve is one parallel launch, where
+// two triangular solves would be a chain of n dependent steps).  Symmetric
+// matrices: the dense FP64 Cholesky factor (CholeskySolver; every pivot
+// positive) and the inverse formed from it.  Nonsymmetric: Gauss-Jordan
+// elimination without pivoting, LuSolver's elimination order
+// (lu/decomposition.hpp:31-122 does not pivot either), refusing pivots that
+// are zero, non-finite or tiny against their row.
 lgx_status dense_inverse(const Csr &a, cudaStream_t s, DBuf<double> &inv, int spd) {
   const int64_t n = a.n;
   LGX_CHECK(inv.alloc(n * n));
-  DBuf<double> prow, pcol;
   DBuf<int> bad;
-  LGX_CHECK(prow.alloc(n));
-  LGX_CHECK(pcol.alloc(n));
   LGX_CHECK(bad.alloc(1));
   LGX_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), s));
   if (n == 0) return LGX_OK;
+  if (spd) {
+    DBuf<double> l, y;
+    LGX_CHECK(l.alloc(n * n));
+    LGX_CHECK(y.alloc(n * n));
+    k_dense_from_csr<<<grid_for(n, 128), 128, 0, s>>>(n, a.rowptr.p, a.col.p,
+                                                     a.storage == LGX_F64 ? a.v64.p : nullptr,
+                                                     a.storage == LGX_F32 ? a.v32.p : nullptr,
+                                                     l.p);
+    LGX_LAUNCH_CHECK();
+    for (int64_t k = 0; k < n; ++k) {
+      k_chol_column<<<1, 256, 0, s>>>(n, k, l.p, bad.p);
+      const int64_t m = n - k - 1;
+      if (m > 0)
+        k_chol_update<<<(unsigned)std::min<int64_t>(grid_for(m * m, 256), 4096), 256, 0, s>>>(
+          n, k, l.p, bad.p);
+    }
+    LGX_LAUNCH_CHECK();
+    int h_bad = 0;
+    LGX_CUDA(cudaMemcpyAsync(&h_bad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    LGX_CUDA(cudaStreamSynchronize(s));
+    if (h_bad) return fail(LGX_ERR_NOT_SPD, "matrix has a non-positive pivot");
+    LGX_CUDA(cudaMemsetAsync(y.p, 0, sizeof(double) * (size_t)(n * n), s));
+    for (int64_t i = 0; i < n; ++i)
+      k_chol_inv_row<<<(unsigned)std::min<int64_t>(grid_for(i + 1, 128), 1024), 128, 0, s>>>(
+        n, i, l.p, y.p);
+    LGX_LAUNCH_CHECK();
+    k_chol_inv_gram<<<(unsigned)std::min<int64_t>(grid_for(n * n, 256), 8192), 256, 0, s>>>(
+      n, y.p, inv.p);
+    LGX_LAUNCH_CHECK();
+    LGX_CUDA(cudaStreamSynchronize(s));
+    return LGX_OK;
+  }
+  DBuf<double> prow, pcol;
+  LGX_CHECK(prow.alloc(n));
+  LGX_CHECK(pcol.alloc(n));
   k_dense_from_csr<<<grid_for(n, 128), 128, 0, s>>>(n, a.rowptr.p, a.col.p,
                                                    a.storage == LGX_F64 ? a.v64.p : nullptr,
                                                    a.storage == LGX_F32 ? a.v32.p : nullptr,
@@ -857,7 +963,7 @@ lgx_status dense_inverse(const Csr &a, cudaStream_t s, DBuf<double> &inv, int sp
   const unsigned g1 = (unsigned)std::min<int64_t>(grid_for(n, 256), 1024);
   const unsigned g2 = (unsigned)std::min<int64_t>(grid_for(n * n, 256), 4096);
   for (int64_t k = 0; k < n; ++k) {
-    k_gj_pivot<<<g1, 256, 0, s>>>(n, k, inv.p, prow.p, pcol.p, bad.p, spd);
+    k_gj_pivot<<<g1, 256, 0, s>>>(n, k, inv.p, prow.p, pcol.p, bad.p);
     k_gj_update<<<g2, 256, 0, s>>>(n, k, inv.p, prow.p, pcol.p, bad.p);
   }
   LGX_LAUNCH_CHECK();
@@ -865,8 +971,8 @@ lgx_status dense_inverse(const Csr &a, cudaStream_t s, DBuf<double> &inv, int sp
   LGX_CUDA(cudaMemcpyAsync(&h_bad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   LGX_CUDA(cudaStreamSynchronize(s));
   if (h_bad)
-    return spd ? fail(LGX_ERR_NOT_SPD, "matrix has a non-positive pivot")
-               : fail(LGX_ERR_BREAKDOWN, "matrix has a zero or non-finite pivot");
+    return fail(LGX_ERR_BREAKDOWN,
+                "matrix has a zero, non-finite or tiny pivot (unpivoted elimination)");
   return LGX_OK;
 }
 
@@ -1070,7 +1176,25 @@ static lgx_status amg_build(const lgx_matrix *m, const lgx_amg_params &p,
   h.p = p;
   h.f32 = p.cycle_f32 != 0;
   auto l0 = std::make_unique<lgx_amg_level>();
-  l0->a = &m->csr;
+  // a stencil finest level: its assembled CSR serves the setup (strength,
+  // aggregation, Galerkin product) and is released afterwards
+  std::unique_ptr<lgx_matrix, lgx_status (*)(lgx_matrix *)> assembled(nullptr,
+                                                                       lgx_matrix_destroy);
+  if (m->kind != LGX_MATRIX_CSR) {
+    if (p.cycle_f32)
+      return fail(LGX_ERR_UNSUPPORTED, "a stencil finest level runs the FP64 cycle");
+    lgx_matrix *tmp = nullptr;
+    LGX_CHECK(lgx_stencil_to_csr(m, nullptr, s, &tmp));
+    assembled.reset(tmp);
+    if (tmp->n != m->n)
+      return fail(LGX_ERR_UNSUPPORTED,
+                  "stencil rows with a zero diagonal (ZeroToZero) have no assembled row");
+    l0->a = &tmp->csr;
+    l0->stencil = m;
+    timer.mark(s, "assemble", 0);
+  } else {
+    l0->a = &m->csr;
+  }
   h.lv.push_back(std::move(l0));
   bool aggressive = false;
   for (int64_t level = 0;; ++level) {
@@ -1133,6 +1257,24 @@ static lgx_status amg_build(const lgx_matrix *m, const lgx_amg_params &p,
   // smoother colourings (all but the coarsest level)
   for (int64_t l = 0; l + 1 < L; ++l) {
     lgx_amg_level &lv = *h.lv[l];
+    if (lv.stencil) {
+      // matrix-free red-black sweeps in natural order: the permutation of
+      // the transfers is the identity
+      lgx_colouring *rb = nullptr;
+      LGX_CHECK(lgx_colouring_create_red_black(lv.stencil, s, &rb));
+      lv.col.reset(rb);
+      const int64_t n = lv.a->n;
+      LGX_CHECK(rb->perm.alloc(n));
+      LGX_CHECK(rb->iperm.alloc(n));
+      if (n) {
+        k_iota<<<std::min<int64_t>(grid_for(n, 256), 16384), 256, 0, s>>>(n, rb->perm.p);
+        LGX_LAUNCH_CHECK();
+        k_iota<<<std::min<int64_t>(grid_for(n, 256), 16384), 256, 0, s>>>(n, rb->iperm.p);
+        LGX_LAUNCH_CHECK();
+      }
+      timer.mark(s, "colouring", l);
+      continue;
+    }
     lv.col = std::make_unique<lgx_colouring>();
     if (l == 0 && finest_colouring) {
       LGX_CHECK(colouring_build(*lv.a, finest_colouring->colour.p, finest_colouring->ncolours, s,
@@ -1199,6 +1341,22 @@ static lgx_status amg_build(const lgx_matrix *m, const lgx_amg_params &p,
   timer.mark(s, "transfers", -1);
   LGX_CHECK(dense_inverse(*h.lv[L - 1]->a, s, h.inv));
   timer.mark(s, "coarse_inv", L - 1);
+  if (assembled && L > 1) {
+    // keep the sizes of the assembled finest matrix, release its arrays
+    lgx_amg_level &l0 = *h.lv[0];
+    l0.own.n = assembled->csr.n;
+    l0.own.nnz = assembled->csr.nnz;
+    l0.own.symmetric = assembled->csr.symmetric;
+    l0.a = &l0.own;
+    LGX_CUDA(cudaStreamSynchronize(s));
+    assembled.reset();
+  } else if (assembled) {
+    // a one-level hierarchy keeps the assembled matrix as its (coarsest) level
+    lgx_amg_level &l0 = *h.lv[0];
+    l0.own = std::move(assembled->csr);
+    l0.a = &l0.own;
+    l0.stencil = nullptr;
+  }
   return LGX_OK;
 }
 
@@ -1211,6 +1369,13 @@ static lgx_status level_sor(lgx_amg_level &lv, const lgx_amg &h, int forward, co
   const lgx_colouring &c = *lv.col;
   const double relax = h.p.smoother_relax;
   const int ultra = h.p.smoother_ultra;
+  if (lv.stencil) {
+    if constexpr (sizeof(XT) == 8)
+      return stencil_sor_sweep(lv.stencil, relax, forward, ultra, from_zero ? nullptr : x, x, b,
+                               s);
+    else
+      return fail(LGX_ERR_UNSUPPORTED, "a stencil finest level runs the FP64 cycle");
+  }
   if constexpr (sizeof(XT) == 8) {
     if (c.pcsr.storage == LGX_F64)
       return mc_sor_sweep<double, double>(c, c.pcsr.v64.p, relax, forward, ultra, b, x, s,
@@ -1230,6 +1395,12 @@ template <typename XT>
 static lgx_status level_residual(lgx_amg_level &lv, const lgx_amg &h, const XT *b, const XT *x,
                                  XT *r, cudaStream_t s) {
   const lgx_colouring &c = *lv.col;
+  if (lv.stencil) {
+    if constexpr (sizeof(XT) == 8)
+      return matrix_residual(lv.stencil, b, x, r, nullptr, nullptr, nullptr, s);
+    else
+      return fail(LGX_ERR_UNSUPPORTED, "a stencil finest level runs the FP64 cycle");
+  }
   if constexpr (sizeof(XT) == 8) {
     if (c.pcsr.storage == LGX_F64)
       return csr_residual<double, double>(c.pcsr, c.pcsr.v64.p, b, x, r, nullptr, nullptr,
@@ -1330,6 +1501,19 @@ lgx_status amg_apply_permuted(lgx_amg &h, const double *b, double *x, cudaStream
   return LGX_OK;
 }
 
+// The float V-cycle on float vectors of the finest level's permuted space
+// (the inner solves of the refinement driver); needs a cycle_f32 hierarchy.
+bool amg_cycle_f32(const lgx_amg &h) { return h.f32; }
+lgx_status amg_apply_permuted_f32(lgx_amg &h, const float *b, float *x, cudaStream_t s) {
+  if (!h.f32) return fail(LGX_ERR_UNSUPPORTED, "float V-cycle needs a cycle_f32 hierarchy");
+  return vcycle_impl<float>(h, b, x, s);
+}
+// float values of the finest permuted matrix (the cycle's own copy)
+const float *amg_finest_values_f32(const lgx_amg &h) {
+  const lgx_colouring &c = *h.lv[0]->col;
+  return c.pcsr.storage == LGX_F32 ? c.pcsr.v32.p : c.pv32.p;
+}
+
 }  // namespace lgx
 
 using namespace lgx;
@@ -1364,8 +1548,8 @@ static lgx_status amg_setup(const lgx_matrix *a, const lgx_amg_params *p,
                             const lgx_colouring *finest_colouring, const lgx_agg_map *maps,
                             int64_t nmaps, lgx_stream stream, lgx_amg **out) {
   if (!a || !p || !out) return fail(LGX_ERR_INVALID, "null argument");
-  if (a->kind != LGX_MATRIX_CSR)
-    return fail(LGX_ERR_UNSUPPORTED, "AMG setup needs a CSR matrix (assemble stencils first)");
+  if (a->kind != LGX_MATRIX_CSR && finest_colouring && !finest_colouring->stencil_rb)
+    return fail(LGX_ERR_INVALID, "a stencil finest level takes its red-black colouring");
   if (finest_colouring && finest_colouring->n != a->n)
     return fail(LGX_ERR_INVALID, "finest colouring does not match the matrix");
   if (p->max_aggregate_size > 64 || p->min_aggregate_size < 1 ||
@@ -1425,6 +1609,8 @@ lgx_status lgx_amg_level_download(const lgx_amg *h, int64_t level, int64_t *h_ro
   if (!h || level < 0 || level >= (int64_t)h->lv.size())
     return fail(LGX_ERR_INVALID, "bad level");
   const lgx_amg_level &lv = *h->lv[level];
+  if (lv.stencil)
+    return fail(LGX_ERR_UNSUPPORTED, "the finest level is a matrix-free stencil (no stored CSR)");
   const Csr &c = *lv.a;
   if (h_rowptr)
     LGX_CUDA(cudaMemcpyAsync(h_rowptr, c.rowptr.p, sizeof(int64_t) * (c.n + 1),

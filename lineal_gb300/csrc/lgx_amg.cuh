@@ -30,6 +30,10 @@ struct lgx_amg_level {
   lgx::DBuf<int32_t> rlist;
   lgx::DBuf<double> b64, x64, r64;   // cycle vectors (permuted order)
   lgx::DBuf<float> b32, x32, r32;
+  // level 0 of a hierarchy built on a stencil matrix: the smoother and the
+  // residual run matrix-free on it (red-black, natural order); `own` then
+  // keeps only the sizes of the assembled matrix the setup used
+  const lgx_matrix *stencil = nullptr;
 };
 
 struct lgx_amg {

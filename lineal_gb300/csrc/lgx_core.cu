@@ -3,6 +3,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
+#include <memory>
+#include <map>
 #include <atomic>
 #include <cmath>
 #include <cstdlib>
@@ -286,18 +289,39 @@ lgx_status dot(int64_t n, const double *a, const double *b, double *out, double 
   return LGX_OK;
 }
 
-// Scratch for the public reduction calls: per-call allocation keeps the
-// entry points re-entrant across streams.
+// Scratch of the public reductions (lgx_dot, lgx_norm2sq, lgx_max_norm): one
+// set per stream, allocated on the stream's first call and kept for the life
+// of the process (1216 partial sums and an arrival counter, 9.7 KB), so that
+// later calls neither allocate nor free -- cudaFree waits for the whole
+// device.  Calls on one stream run in order and share its set; the last block
+// of every completed reduction leaves the counter at zero.  Streams are told
+// apart by device and stream id (cudaStreamGetId: ids are not reused while
+// the process runs), so two streams never share a set.
 struct ReduceScratch {
   DBuf<double> partials;
   DBuf<unsigned> counter;
-  lgx_status init(int64_t n, cudaStream_t s) {
-    LGX_CHECK(partials.alloc(reduce_blocks(n)));
-    LGX_CHECK(counter.alloc(1));
-    LGX_CUDA(cudaMemsetAsync(counter.p, 0, sizeof(unsigned), s));
-    return LGX_OK;
-  }
 };
+static std::mutex g_reduce_scratch_mutex;
+static std::map<std::pair<int, unsigned long long>, std::unique_ptr<ReduceScratch>>
+  g_reduce_scratch;
+
+static lgx_status reduce_scratch(cudaStream_t s, ReduceScratch **out) {
+  int dev = 0;
+  LGX_CUDA(cudaGetDevice(&dev));
+  unsigned long long id = 0;
+  LGX_CUDA(cudaStreamGetId(s, &id));
+  std::lock_guard<std::mutex> lock(g_reduce_scratch_mutex);
+  auto &slot = g_reduce_scratch[{dev, id}];
+  if (!slot) {
+    auto rs = std::make_unique<ReduceScratch>();
+    LGX_CHECK(rs->partials.alloc(reduce_blocks(INT64_MAX)));
+    LGX_CHECK(rs->counter.alloc(1));
+    LGX_CUDA(cudaMemsetAsync(rs->counter.p, 0, sizeof(unsigned), s));
+    slot = std::move(rs);
+  }
+  *out = slot.get();
+  return LGX_OK;
+}
 
 // Scratch of lgx_dot_static: one partial sum per block of k_dot and the
 // block-arrival counter, in the module's static device memory (8 KB + 8 B).
@@ -714,9 +738,9 @@ lgx_status lgx_gen_7pt(const int64_t dims[3], const double *d_k, lgx_dtype stora
 lgx_status lgx_dot(int64_t n, const double *d_a, const double *d_b, double *d_out,
                    lgx_stream stream) {
   if (n < 0 || (n > 0 && (!d_a || !d_b)) || !d_out) return fail(LGX_ERR_INVALID, "bad argument");
-  ReduceScratch rs;
-  LGX_CHECK(rs.init(n, stream));
-  LGX_CHECK(dot(n, d_a, d_b, d_out, rs.partials.p, rs.counter.p, stream));
+  ReduceScratch *rs = nullptr;
+  LGX_CHECK(reduce_scratch(stream, &rs));
+  LGX_CHECK(dot(n, d_a, d_b, d_out, rs->partials.p, rs->counter.p, stream));
   LGX_CUDA(cudaStreamSynchronize(stream));
   return LGX_OK;
 }
@@ -751,10 +775,10 @@ lgx_status lgx_norm2sq(int64_t n, const double *d_a, double *d_out, lgx_stream s
 
 lgx_status lgx_max_norm(int64_t n, const double *d_a, double *d_out, lgx_stream stream) {
   if (n < 0 || (n > 0 && !d_a) || !d_out) return fail(LGX_ERR_INVALID, "bad argument");
-  ReduceScratch rs;
-  LGX_CHECK(rs.init(n, stream));
-  k_maxabs<<<reduce_blocks(n), kReduceThreads, 0, stream>>>(n, d_a, d_out, rs.partials.p,
-                                                             rs.counter.p);
+  ReduceScratch *rs = nullptr;
+  LGX_CHECK(reduce_scratch(stream, &rs));
+  k_maxabs<<<reduce_blocks(n), kReduceThreads, 0, stream>>>(n, d_a, d_out, rs->partials.p,
+                                                             rs->counter.p);
   LGX_LAUNCH_CHECK();
   LGX_CUDA(cudaStreamSynchronize(stream));
   return LGX_OK;

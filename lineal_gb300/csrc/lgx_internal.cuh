@@ -197,6 +197,8 @@ struct lgx_colouring {
                                  // the SOR row must divide (permuted order)
   lgx::DBuf<double> pdiag;       // the stored diagonal a_rr, widened (permuted order)
   lgx::DBuf<double> work_b, work_x;  // natural<->permuted staging for the public sweep API
+  bool stencil_rb = false;       // red-black colouring of a stencil matrix: the sweeps run
+                                 // matrix-free in natural order (no permuted copy)
 };
 
 namespace lgx {
@@ -245,6 +247,9 @@ lgx_status stencil_spmv(const StencilDesc &st, const double *x, double *y, cudaS
 lgx_status stencil_residual(const StencilDesc &st, const double *b, const double *x, double *r,
                             double *norm, double *partials, unsigned *counter, cudaStream_t s);
 lgx_status stencil_diagonal(const StencilDesc &st, double *d, cudaStream_t s);
+// red-black SOR sweep of a stencil matrix in natural order (lgx_spmv.cu)
+lgx_status stencil_sor_sweep(const lgx_matrix *a, double relax, int forward, int ultra,
+                             const double *x_in, double *x_out, const double *b, cudaStream_t s);
 lgx_status matrix_diagonal(lgx_matrix *a, cudaStream_t s, const double **out);
 
 // Generic matrix application for the Krylov drivers (CSR or stencil).

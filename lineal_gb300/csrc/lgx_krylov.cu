@@ -21,6 +21,9 @@ namespace lgx {
 lgx_status amg_apply_permuted(lgx_amg &h, const double *b, double *x, cudaStream_t s);
 const Csr &amg_finest_permuted(const lgx_amg &h);
 lgx_colouring *amg_finest_colouring(lgx_amg &h);
+bool amg_cycle_f32(const lgx_amg &h);
+lgx_status amg_apply_permuted_f32(lgx_amg &h, const float *b, float *x, cudaStream_t s);
+const float *amg_finest_values_f32(const lgx_amg &h);
 }  // namespace lgx
 
 namespace lgx {
@@ -261,6 +264,11 @@ struct Solver {
     switch (precon) {
       case LGX_PRECON_JACOBI: return jacobi_diag_zero(n, diag, relax, r, z, s);
       case LGX_PRECON_SSOR: {
+        if (col->stencil_rb) {
+          // SsorBroom: forward from zero into z, backward in place
+          LGX_CHECK(stencil_sor_sweep(m, relax, 1, ultra, nullptr, z, r, s));
+          return stencil_sor_sweep(m, relax, 0, ultra, z, z, r, s);
+        }
         // forward sweep from zero (x need not be cleared), backward in place
         const Csr &p = col->pcsr;
         if (p.storage == LGX_F64) {
@@ -298,8 +306,20 @@ static lgx_status setup_solver(const lgx_matrix *a, const lgx_solve_params *p, c
       LGX_CHECK(matrix_diagonal(const_cast<lgx_matrix *>(a), s, &S.diag));
       break;
     case LGX_PRECON_SSOR: {
-      if (a->kind != LGX_MATRIX_CSR)
-        return fail(LGX_ERR_UNSUPPORTED, "SSOR preconditioning needs a CSR matrix");
+      if (a->kind != LGX_MATRIX_CSR) {
+        // matrix-free red-black SSOR in natural order
+        lgx_colouring *c = const_cast<lgx_colouring *>(p->colouring);
+        if (!c) {
+          lgx_colouring *made = nullptr;
+          LGX_CHECK(lgx_colouring_create_red_black(a, s, &made));
+          own_col.reset(made);
+          c = made;
+        }
+        if (!c->stencil_rb || c->n != a->n)
+          return fail(LGX_ERR_INVALID, "a stencil's SSOR needs its red-black colouring");
+        S.col = c;
+        break;
+      }
       lgx_colouring *c = const_cast<lgx_colouring *>(p->colouring);
       if (!c) {
         own_col = std::make_unique<lgx_colouring>();
@@ -320,8 +340,15 @@ static lgx_status setup_solver(const lgx_matrix *a, const lgx_solve_params *p, c
       lgx_colouring *c = amg_finest_colouring(*p->amg);
       if (c) {
         if (c->n != a->n) return fail(LGX_ERR_INVALID, "hierarchy does not match the matrix");
-        S.pcsr = &c->pcsr;
-        S.perm = c->perm.p;
+        if (c->stencil_rb) {
+          // matrix-free finest level: the iteration runs in natural order on
+          // the stencil itself
+          if (a->kind == LGX_MATRIX_CSR)
+            return fail(LGX_ERR_INVALID, "the hierarchy was built on a stencil matrix");
+        } else {
+          S.pcsr = &c->pcsr;
+          S.perm = c->perm.p;
+        }
       }
       break;
     }
@@ -602,6 +629,247 @@ static lgx_status run_solve(int kind, const lgx_matrix *a, const double *d_b, do
   return st != LGX_OK ? st : st2;
 }
 
+// ---------------------------------------------------------------------------
+// FP64 iterative refinement over a float inner PCG (the precision form; no
+// reference counterpart).  The inner CG runs the recurrence of
+// conjugate-gradients/solver.hpp:75-115 on float vectors: float products of
+// the finest level (grid or row kernels on the cycle's float values) and the
+// float V-cycle, with every dot product accumulated in FP64 and the CG
+// scalars kept in FP64 (KScalars).  The outer loop forms the FP64 residual,
+// hands the inner solve r / ||r|| (so the float vectors stay O(1) however far
+// the residual has fallen), adds ||r|| d to x in FP64 and stops on the FP64
+// residual.
+// ---------------------------------------------------------------------------
+
+// dot(a, b) of float vectors in FP64 with a post operation in the last block
+__global__ void __launch_bounds__(kKT)
+  k_fdot_post(int64_t n, const float *__restrict__ a, const float *__restrict__ b, int post,
+              KScalars *ks, double *partials, unsigned *counter) {
+  double s = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    s = fma((double)a[i], (double)b[i], s);
+  double t;
+  if (grid_reduce<kKT>(s, blockIdx.x, gridDim.x, partials, counter, &t) && threadIdx.x == 0) {
+    if (post == POST_ALPHA) {
+      set_flags(ks, ks->rho, t);
+      ks->den = t;
+      ks->alpha = ks->rho / t;
+    } else if (post == POST_RHO_BETA) {
+      ks->rho_old = ks->rho;
+      ks->rho = t;
+      set_flags(ks, t, ks->rho_old);
+      ks->beta = t / ks->rho_old;
+    } else if (post == POST_RHO) {
+      ks->rho = t;
+      if (!isfinite(t)) ks->flag |= 2;
+    }
+  }
+}
+
+// d += alpha p ; r -= alpha q ; res2 = ||r||^2 (float vectors, FP64 alpha
+// rounded once to float, FP64 sum)
+__global__ void __launch_bounds__(kKT)
+  k_fcg_update(int64_t n, KScalars *ks, const float *__restrict__ p, const float *__restrict__ q,
+               float *__restrict__ d, float *__restrict__ r, double *partials,
+               unsigned *counter) {
+  const float alpha = (float)ks->alpha;
+  double s = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    d[i] = fmaf(p[i], alpha, d[i]);
+    const float rv = fmaf(-alpha, q[i], r[i]);
+    r[i] = rv;
+    s = fma((double)rv, (double)rv, s);
+  }
+  double t;
+  if (grid_reduce<kKT>(s, blockIdx.x, gridDim.x, partials, counter, &t) && threadIdx.x == 0) {
+    ks->res2 = t;
+    if (!isfinite(t)) ks->flag |= 2;
+  }
+}
+
+// p = z + beta p (float)
+__global__ void k_fxpby(int64_t n, const KScalars *ks, const float *__restrict__ z,
+                        float *__restrict__ p) {
+  const float beta = (float)ks->beta;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = fmaf(p[i], beta, z[i]);
+}
+
+// rf = float(r * inv_scale), d = 0
+__global__ void k_refine_start(int64_t n, const double *__restrict__ r, double inv_scale,
+                               float *__restrict__ rf, float *__restrict__ d) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    rf[i] = (float)(r[i] * inv_scale);
+    d[i] = 0.0f;
+  }
+}
+
+// x += scale * d (FP64)
+__global__ void k_refine_add(int64_t n, const float *__restrict__ d, double scale,
+                             double *__restrict__ x) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = fma((double)d[i], scale, x[i]);
+}
+
+struct Refiner {
+  Solver S;
+  std::unique_ptr<lgx_colouring> own_col;
+  DBuf<double> b, x, r;
+  DBuf<float> rf, df, pf, qf, zf;
+  const float *v32 = nullptr;
+  cudaStream_t user_stream = nullptr, capture_stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  uint64_t graph_kernels = 0;
+  ~Refiner() {
+    if (graph) cudaGraphExecDestroy(graph);
+    if (capture_stream) cudaStreamDestroy(capture_stream);
+  }
+
+  // one inner CG iteration on the float vectors
+  lgx_status inner_body() {
+    const int64_t n = S.n;
+    cudaStream_t s = S.s;
+    KScalars *ks = S.ks.p;
+    const unsigned rg = (unsigned)reduce_blocks(n);
+    LGX_CHECK((csr_spmv<float, float>(*S.pcsr, v32, pf.p, qf.p, s)));
+    k_fdot_post<<<rg, kKT, 0, s>>>(n, pf.p, qf.p, POST_ALPHA, ks, S.partials.p, S.counters.p);
+    LGX_LAUNCH_CHECK();
+    k_fcg_update<<<rg, kKT, 0, s>>>(n, ks, pf.p, qf.p, df.p, rf.p, S.partials.p, S.counters.p);
+    LGX_LAUNCH_CHECK();
+    LGX_CHECK(amg_apply_permuted_f32(*S.amg, rf.p, zf.p, s));
+    k_fdot_post<<<rg, kKT, 0, s>>>(n, rf.p, zf.p, POST_RHO_BETA, ks, S.partials.p,
+                                   S.counters.p);
+    LGX_LAUNCH_CHECK();
+    k_fxpby<<<S.vgrid(), 256, 0, s>>>(n, ks, zf.p, pf.p);
+    LGX_LAUNCH_CHECK();
+    return LGX_OK;
+  }
+
+  lgx_status capture() {
+    if (!capture_stream)
+      LGX_CUDA(cudaStreamCreateWithFlags(&capture_stream, cudaStreamNonBlocking));
+    S.s = capture_stream;
+    cudaGraph_t g = nullptr;
+    const uint64_t before = launch_count();
+    cudaError_t e = cudaStreamBeginCapture(capture_stream, cudaStreamCaptureModeThreadLocal);
+    lgx_status st = e == cudaSuccess ? inner_body() : cuda_fail(e, "cudaStreamBeginCapture");
+    graph_kernels = launch_count() - before;
+    count_launches(0 - graph_kernels);
+    cudaError_t e2 = cudaStreamEndCapture(capture_stream, &g);
+    S.s = user_stream;
+    if (st != LGX_OK) {
+      if (g) cudaGraphDestroy(g);
+      return st;
+    }
+    if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    return LGX_OK;
+  }
+
+  lgx_status inner_iterate(bool use_graphs, bool first) {
+    if (use_graphs && !first) {
+      if (!graph) LGX_CHECK(capture());
+      LGX_CUDA(cudaGraphLaunch(graph, user_stream));
+      count_launches(graph_kernels);
+      return LGX_OK;
+    }
+    return inner_body();
+  }
+};
+
+static lgx_status run_refined(const lgx_matrix *a, const double *d_b, double *d_x,
+                              const lgx_solve_params *p, cudaStream_t s, int64_t *iterations,
+                              double *final_rel, double *history) {
+  if (p->precon != LGX_PRECON_AMG || !p->amg)
+    return fail(LGX_ERR_UNSUPPORTED, "refinement needs the AMG preconditioner");
+  if (!amg_cycle_f32(*p->amg))
+    return fail(LGX_ERR_UNSUPPORTED, "refinement needs a float-cycle hierarchy (cycle_f32)");
+  if (!(p->inner_rtol > 0.0 && p->inner_rtol < 1.0))
+    return fail(LGX_ERR_INVALID, "inner_rtol must lie in (0, 1)");
+  Refiner R;
+  R.user_stream = s;
+  LGX_CHECK(setup_solver(a, p, s, R.S, R.own_col));
+  Solver &S = R.S;
+  if (!S.pcsr) return fail(LGX_ERR_UNSUPPORTED, "refinement needs a CSR finest level");
+  const int64_t n = S.n;
+  R.v32 = amg_finest_values_f32(*S.amg);
+  LGX_CHECK(R.b.alloc(n));
+  LGX_CHECK(R.x.alloc(n));
+  LGX_CHECK(R.r.alloc(n));
+  LGX_CHECK(R.rf.alloc(n));
+  LGX_CHECK(R.df.alloc(n));
+  LGX_CHECK(R.pf.alloc(n));
+  LGX_CHECK(R.qf.alloc(n));
+  LGX_CHECK(R.zf.alloc(n));
+  LGX_CHECK(gather<double, double>(n, S.perm, d_b, R.b.p, s));
+  LGX_CHECK(gather<double, double>(n, S.perm, d_x, R.x.p, s));
+  KScalars *ks = S.ks.p;
+  KScalars h{};
+  const unsigned rg = (unsigned)reduce_blocks(n);
+  LGX_CHECK(S.residual(R.b.p, R.x.p, R.r.p, &ks->res2));
+  LGX_CHECK(S.read(h));
+  if (!std::isfinite(h.res2)) return fail(LGX_ERR_NONFINITE, "non-finite initial residual");
+  const double r0 = std::sqrt(h.res2);
+  double res = r0;
+  if (history) history[0] = r0;
+  int64_t it = 0;
+  bool first = true;
+  lgx_status st = LGX_OK;
+  while (st == LGX_OK && it < p->maxit && res > p->rtol * r0 && res > 0.0) {
+    // inner solve of A d = r / ||r|| to the tolerance this step needs
+    const double scale = res;
+    const double tol = std::max(p->inner_rtol, 0.5 * p->rtol * r0 / res);
+    k_refine_start<<<S.vgrid(), 256, 0, s>>>(n, R.r.p, 1.0 / scale, R.rf.p, R.df.p);
+    LGX_LAUNCH_CHECK();
+    LGX_CHECK(amg_apply_permuted_f32(*S.amg, R.rf.p, R.zf.p, s));
+    k_fdot_post<<<rg, kKT, 0, s>>>(n, R.rf.p, R.zf.p, POST_RHO, ks, S.partials.p, S.counters.p);
+    LGX_LAUNCH_CHECK();
+    LGX_CUDA(cudaMemcpyAsync(R.pf.p, R.zf.p, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+    LGX_CHECK(S.read(h));
+    LGX_CHECK(check_flags(h, it));
+    double inner = 1.0;
+    while (it < p->maxit && inner > tol && h.rho != 0.0) {
+      st = R.inner_iterate(p->use_graphs != 0, first);
+      first = false;
+      if (st != LGX_OK) break;
+      ++it;
+      LGX_CHECK(S.read(h));
+      st = check_flags(h, it);
+      inner = std::sqrt(h.res2);
+      if (history) history[it] = scale * inner;
+      if (st != LGX_OK) break;
+    }
+    if (st != LGX_OK) break;
+    k_refine_add<<<S.vgrid(), 256, 0, s>>>(n, R.df.p, scale, R.x.p);
+    LGX_LAUNCH_CHECK();
+    LGX_CHECK(S.residual(R.b.p, R.x.p, R.r.p, &ks->res2));
+    LGX_CHECK(S.read(h));
+    if (!std::isfinite(h.res2)) {
+      st = fail(LGX_ERR_NONFINITE, "non-finite residual after refinement step");
+      break;
+    }
+    const double prev = res;
+    res = std::sqrt(h.res2);
+    if (history) history[it] = res;
+    // an inner solve that no longer reduces the FP64 residual (float
+    // precision reached on an operator the float cycle cannot resolve) ends
+    // the refinement
+    if (res >= prev) break;
+  }
+  LGX_CHECK(scatter<double, double>(n, S.perm, R.x.p, d_x, s));
+  LGX_CUDA(cudaStreamSynchronize(s));
+  if (iterations) *iterations = it;
+  if (final_rel) *final_rel = r0 > 0 ? res / r0 : 0.0;
+  return st;
+}
+
 }  // namespace lgx
 
 using namespace lgx;
@@ -620,12 +888,16 @@ void lgx_solve_default_params(lgx_solve_params *p) {
   p->rere_period = 8;
   p->use_graphs = 1;
   p->flexible = 0;
+  p->refine = 0;
+  p->inner_rtol = 1e-4;
 }
 
 lgx_status lgx_pcg(const lgx_matrix *a, const double *d_b, double *d_x,
                    const lgx_solve_params *p, lgx_stream stream, int64_t *iterations,
                    double *final_rel_residual, double *h_history) {
   if (!a || !p || (a->n > 0 && (!d_b || !d_x))) return fail(LGX_ERR_INVALID, "null argument");
+  if (p->refine)
+    return run_refined(a, d_b, d_x, p, stream, iterations, final_rel_residual, h_history);
   return run_solve(LGX_KRYLOV_CG, a, d_b, d_x, p, stream, iterations, final_rel_residual,
                    h_history);
 }
@@ -634,6 +906,7 @@ lgx_status lgx_pbicgstab(const lgx_matrix *a, const double *d_b, double *d_x,
                          const lgx_solve_params *p, lgx_stream stream, int64_t *iterations,
                          double *final_rel_residual, double *h_history) {
   if (!a || !p || (a->n > 0 && (!d_b || !d_x))) return fail(LGX_ERR_INVALID, "null argument");
+  if (p->refine) return fail(LGX_ERR_UNSUPPORTED, "refinement is a CG option");
   return run_solve(LGX_KRYLOV_BICGSTAB, a, d_b, d_x, p, stream, iterations, final_rel_residual,
                    h_history);
 }
@@ -645,6 +918,7 @@ lgx_status lgx_krylov_create(int kind, const lgx_matrix *a, const double *d_b,
     return fail(LGX_ERR_INVALID, "null argument");
   if (kind != LGX_KRYLOV_CG && kind != LGX_KRYLOV_BICGSTAB)
     return fail(LGX_ERR_INVALID, "unknown Krylov method");
+  if (p->refine) return fail(LGX_ERR_UNSUPPORTED, "refinement runs through lgx_pcg only");
   std::unique_ptr<lgx_krylov> K;
   LGX_CHECK(krylov_create(kind, a, d_b, d_x, p, stream, K));
   *out = K.release();

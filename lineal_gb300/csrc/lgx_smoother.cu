@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <memory>
 #include <cmath>
 #include <vector>
 
@@ -652,6 +653,50 @@ lgx_status lgx_colouring_create_jp(const lgx_matrix *a, uint64_t seed, lgx_strea
 // of the removal order, each vertex takes the smallest colour none of its
 // coloured neighbours has.  O(nnz); every step is fixed, so the colouring is
 // deterministic.
+// The pattern's adjacency as the colouring sees it: the rows themselves when
+// the off-diagonal pattern is structurally symmetric, else every row's sorted
+// union with the matching column of the transpose (the pattern of A + A^T),
+// so that a colouring is proper for both directions of every edge.  Returns
+// false when the rows are used as given.
+static bool symmetrised_pattern(int64_t n, const int64_t *rowptr, const int32_t *col,
+                                std::vector<int64_t> &sptr, std::vector<int32_t> &scol) {
+  std::vector<int64_t> tptr((size_t)n + 1, 0);
+  for (int64_t i = 0; i < n; ++i)
+    for (int64_t e = rowptr[i]; e < rowptr[i + 1]; ++e)
+      if (col[e] != i) ++tptr[(size_t)col[e] + 1];
+  for (int64_t i = 0; i < n; ++i) tptr[(size_t)i + 1] += tptr[(size_t)i];
+  std::vector<int32_t> tcol((size_t)tptr[(size_t)n]);
+  std::vector<int64_t> fill(tptr.begin(), tptr.end() - 1);
+  for (int64_t i = 0; i < n; ++i)
+    for (int64_t e = rowptr[i]; e < rowptr[i + 1]; ++e)
+      if (col[e] != i) tcol[(size_t)fill[(size_t)col[e]]++] = (int32_t)i;
+  bool symmetric = true;
+  std::vector<int32_t> row;
+  for (int64_t i = 0; i < n && symmetric; ++i) {
+    row.clear();
+    for (int64_t e = rowptr[i]; e < rowptr[i + 1]; ++e)
+      if (col[e] != i) row.push_back(col[e]);
+    std::sort(row.begin(), row.end());
+    symmetric = std::equal(row.begin(), row.end(), tcol.begin() + tptr[(size_t)i],
+                           tcol.begin() + tptr[(size_t)i + 1]) &&
+                (int64_t)row.size() == tptr[(size_t)i + 1] - tptr[(size_t)i];
+  }
+  if (symmetric) return false;
+  sptr.assign((size_t)n + 1, 0);
+  scol.clear();
+  for (int64_t i = 0; i < n; ++i) {
+    row.clear();
+    for (int64_t e = rowptr[i]; e < rowptr[i + 1]; ++e)
+      if (col[e] != i) row.push_back(col[e]);
+    row.insert(row.end(), tcol.begin() + tptr[(size_t)i], tcol.begin() + tptr[(size_t)i + 1]);
+    std::sort(row.begin(), row.end());
+    row.erase(std::unique(row.begin(), row.end()), row.end());
+    scol.insert(scol.end(), row.begin(), row.end());
+    sptr[(size_t)i + 1] = (int64_t)scol.size();
+  }
+  return true;
+}
+
 lgx_status lgx_colour_smallest_last(int64_t n, const int64_t *rowptr, const int32_t *col,
                                     int32_t *colour, int32_t *ncolours) {
   if (n < 0 || n > INT32_MAX || (n > 0 && (!rowptr || !col || !colour)) || !ncolours)
@@ -663,6 +708,12 @@ lgx_status lgx_colour_smallest_last(int64_t n, const int64_t *rowptr, const int3
     if (rowptr[i + 1] < rowptr[i]) return fail(LGX_ERR_INVALID, "decreasing row offsets");
   for (int64_t e = 0; e < rowptr[n]; ++e)
     if (col[e] < 0 || col[e] >= n) return fail(LGX_ERR_INVALID, "column index out of range");
+  std::vector<int64_t> sptr;
+  std::vector<int32_t> scol;
+  if (symmetrised_pattern(n, rowptr, col, sptr, scol)) {
+    rowptr = sptr.data();
+    col = scol.data();
+  }
   std::vector<int64_t> deg((size_t)n), next((size_t)n, -1), prev((size_t)n, -1);
   int64_t maxdeg = 0;
   for (int64_t i = 0; i < n; ++i) {
@@ -739,10 +790,53 @@ lgx_status lgx_colouring_create(const lgx_matrix *a, const int32_t *d_colour, in
 lgx_status lgx_colouring_grid27(lgx_colouring *c, const int64_t dims[3], int with_float,
                                 lgx_stream stream, int *attached) {
   if (!c || !dims) return fail(LGX_ERR_INVALID, "null argument");
+  if (c->stencil_rb) {
+    if (attached) *attached = 0;
+    return LGX_OK;
+  }
   if (with_float && c->pcsr.storage == LGX_F64) LGX_CHECK(colouring_make_f32(*c, stream));
   bool att = false;
   LGX_CHECK(grid27_attach(*c, dims, 27, stream, &att));
   if (attached) *attached = att ? 1 : 0;
+  return LGX_OK;
+}
+
+}  // extern "C"
+
+namespace lgx {
+__global__ void k_red_black_colour(int64_t n, int64_t n1, int64_t n2, int32_t *colour) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    colour[i] = (int32_t)(((i / (n1 * n2)) + ((i / n2) % n1) + (i % n2)) & 1);
+}
+}  // namespace lgx
+
+extern "C" {
+
+lgx_status lgx_colouring_create_red_black(const lgx_matrix *a, lgx_stream stream,
+                                          lgx_colouring **out) {
+  if (!a || !out) return fail(LGX_ERR_INVALID, "null argument");
+  if (a->kind == LGX_MATRIX_CSR)
+    return fail(LGX_ERR_UNSUPPORTED,
+                "red-black colouring is for stencil matrices (CSR: lgx_colouring_create)");
+  auto c = std::make_unique<lgx_colouring>();
+  const int64_t n0 = a->st.dims[0], n1 = a->st.dims[1], n2 = a->st.dims[2];
+  c->n = a->n;
+  c->ncolours = 2;
+  c->stencil_rb = true;
+  LGX_CHECK(c->colour.alloc(a->n));
+  if (a->n) {
+    k_red_black_colour<<<std::min<int64_t>(grid_for(a->n, 256), 16384), 256, 0, stream>>>(
+      a->n, n1, n2, c->colour.p);
+    LGX_LAUNCH_CHECK();
+  }
+  // colour 0 holds the cells with even p0 + p1 + p2
+  int64_t even = 0;
+  for (int64_t p0 = 0; p0 < n0; ++p0)
+    for (int64_t p1 = 0; p1 < n1; ++p1) even += (n2 + 1 - ((p0 + p1) & 1)) / 2;
+  c->offsets = {0, even, a->n};
+  LGX_CUDA(cudaStreamSynchronize(stream));
+  *out = c.release();
   return LGX_OK;
 }
 
@@ -767,6 +861,12 @@ lgx_status lgx_sor_sweep(const lgx_matrix *a, const lgx_colouring *c, double rel
                          lgx_stream stream) {
   if (!a || !c || (a->n > 0 && (!d_x_out || !d_b))) return fail(LGX_ERR_INVALID, "null argument");
   if (c->n != a->n) return fail(LGX_ERR_INVALID, "colouring does not match the matrix");
+  if (c->stencil_rb != (a->kind != LGX_MATRIX_CSR))
+    return fail(LGX_ERR_UNSUPPORTED, a->kind == LGX_MATRIX_CSR
+                                       ? "a stencil's red-black colouring on a CSR matrix"
+                                       : "a stencil matrix sweeps with its red-black colouring");
+  if (c->stencil_rb)
+    return stencil_sor_sweep(a, relax, forward, ultra, d_x_in, d_x_out, d_b, stream);
   return colouring_sweep_natural(*const_cast<lgx_colouring *>(c), relax, forward, ultra, d_x_in,
                                  d_x_out, d_b, stream);
 }
@@ -774,18 +874,24 @@ lgx_status lgx_sor_sweep(const lgx_matrix *a, const lgx_colouring *c, double rel
 lgx_status lgx_colouring_permute(const lgx_colouring *c, const double *d_src, double *d_dst,
                                  lgx_stream stream) {
   if (!c || (c->n > 0 && (!d_src || !d_dst))) return fail(LGX_ERR_INVALID, "null argument");
+  if (c->stencil_rb)
+    return fail(LGX_ERR_UNSUPPORTED, "a stencil colouring sweeps in natural order (lgx_sor_sweep)");
   return gather<double, double>(c->n, c->perm.p, d_src, d_dst, stream);
 }
 
 lgx_status lgx_colouring_unpermute(const lgx_colouring *c, const double *d_src, double *d_dst,
                                    lgx_stream stream) {
   if (!c || (c->n > 0 && (!d_src || !d_dst))) return fail(LGX_ERR_INVALID, "null argument");
+  if (c->stencil_rb)
+    return fail(LGX_ERR_UNSUPPORTED, "a stencil colouring sweeps in natural order (lgx_sor_sweep)");
   return scatter<double, double>(c->n, c->perm.p, d_src, d_dst, stream);
 }
 
 lgx_status lgx_sor_sweep_permuted(const lgx_colouring *c, double relax, int forward, int ultra,
                                   double *d_x, const double *d_b, lgx_stream stream) {
   if (!c || (c->n > 0 && (!d_x || !d_b))) return fail(LGX_ERR_INVALID, "null argument");
+  if (c->stencil_rb)
+    return fail(LGX_ERR_UNSUPPORTED, "a stencil colouring sweeps in natural order (lgx_sor_sweep)");
   if (c->pcsr.storage == LGX_F64)
     return mc_sor_sweep<double, double>(*c, c->pcsr.v64.p, relax, forward, ultra, d_b, d_x,
                                         stream);
@@ -795,6 +901,8 @@ lgx_status lgx_sor_sweep_permuted(const lgx_colouring *c, double relax, int forw
 lgx_status lgx_sor_sweep_permuted_f32(lgx_colouring *c, float relax, int forward, int ultra,
                                       float *d_x, const float *d_b, lgx_stream stream) {
   if (!c || (c->n > 0 && (!d_x || !d_b))) return fail(LGX_ERR_INVALID, "null argument");
+  if (c->stencil_rb)
+    return fail(LGX_ERR_UNSUPPORTED, "a stencil colouring sweeps in natural order (lgx_sor_sweep)");
   const float *v = c->pcsr.v32.p;
   if (c->pcsr.storage == LGX_F64) {
     LGX_CHECK(colouring_make_f32(*c, stream));

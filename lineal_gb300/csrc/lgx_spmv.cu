@@ -313,6 +313,52 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// ---- red-black SOR on the matrix-free stencil --------------------------------
+// One colour of a red-black sweep, colour c = (p0 + p1 + p2) & 1, in natural
+// order: thread (m, p1, p0) owns the cell p2 = 2 m + ((p0 + p1 + c) & 1) of
+// its grid line.  Every neighbour has the other colour, so `nb` is where all
+// of them are read: x_out once that colour was visited in this sweep, x_in
+// before (null: zero).  The row is the SorOp row of the assembled matrix
+// (gauss-seidel-variant/sweep.hpp:134-200, csr/create-from.hpp): accum = b_i,
+// then in ascending column order (before axes 0, 1, 2; the diagonal; after
+// axes 2, 1, 0) fma(conn, x_j, accum) for every non-zero connection -- the
+// assembled entry is -conn -- and, in the ultra variant, fma(-a_ii, x_i,
+// accum) at the diagonal; regular: x_i = fma(relax, accum / a_ii,
+// (1 - relax) x_i); ultra: x_i + relax accum / |a_ii|.  The result equals
+// the SOR of the assembled matrix in the row order sorted by (colour, index)
+// bit for bit.
+template <bool LOOKUP>
+__global__ void __launch_bounds__(256)
+  k_st_sor_colour(StencilDev S, int colour, const double *nb, double relax, double m1, int ultra,
+                  const double *x_in, double *x_out, const double *__restrict__ b) {
+  __shared__ double sh_conn[48];
+  const double *conn = stage_conn(S, sh_conn);
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  const int p1 = blockIdx.y * blockDim.y + threadIdx.y;
+  const int p0 = blockIdx.z;
+  const int p2 = 2 * m + ((p0 + p1 + colour) & 1);
+  if (p1 >= S.n1 || p2 >= S.n2) return;
+  const int64_t i = ((int64_t)p0 * S.n1 + p1) * S.n2 + p2;
+  double cv[6];
+  int64_t cj[6];
+  bool has[6];
+  st_row<LOOKUP>(S, conn, p0, p1, p2, i, cv, cj, has);
+  const double xi = x_in ? x_in[i] : 0.0;
+  const double diag = S.diag[i];
+  double accum = b[i];
+#pragma unroll
+  for (int e = 0; e < 6; ++e) {
+    if (e == 3 && ultra) accum = fma(-diag, xi, accum);
+    if (has[e] && cv[e] != 0.0) accum = fma(cv[e], nb ? nb[cj[e]] : 0.0, accum);
+  }
+  if (ultra) {
+    x_out[i] = xi + relax * accum / fabs(diag);
+  } else {
+    const double quot = accum / diag;
+    x_out[i] = fma(relax, quot, m1 * xi);
+  }
+}
+
 __global__ void k_st_rhs(int n0, int n1, int n2, const double *cell_value, double border_q0,
                          double us, double ue, double *b) {
   const int p2 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -740,6 +786,32 @@ static lgx_status stencil_apply(const lgx_matrix *ac, const double *x, const dou
   return LGX_OK;
 }
 
+// One red-black SOR sweep on a stencil matrix: colour 0 then 1 (forward) or
+// 1 then 0 (backward); x_in may equal x_out (in situ) or be null (zero).
+lgx_status stencil_sor_sweep(const lgx_matrix *ac, double relax, int forward, int ultra,
+                             const double *x_in, double *x_out, const double *b,
+                             cudaStream_t s) {
+  lgx_matrix *a = const_cast<lgx_matrix *>(ac);
+  if (a->n == 0) return LGX_OK;
+  LGX_CHECK(stencil_ensure(a, s));
+  StencilDev S = dev_of(a);
+  const dim3 g((unsigned)(((S.n2 + 1) / 2 + 31) / 32), (unsigned)((S.n1 + 7) / 8),
+               (unsigned)S.n0);
+  const double m1 = 1.0 - relax;
+  for (int cc = 0; cc < 2; ++cc) {
+    const int colour = forward ? cc : 1 - cc;
+    const double *nb = cc == 0 ? x_in : x_out;
+    if (a->st.lookup)
+      k_st_sor_colour<true><<<g, kStBlock, 0, s>>>(S, colour, nb, relax, m1, ultra, x_in, x_out,
+                                                   b);
+    else
+      k_st_sor_colour<false><<<g, kStBlock, 0, s>>>(S, colour, nb, relax, m1, ultra, x_in,
+                                                    x_out, b);
+    LGX_LAUNCH_CHECK();
+  }
+  return LGX_OK;
+}
+
 lgx_status matrix_spmv(const lgx_matrix *a, const double *x, double *y, cudaStream_t s) {
   if (a->kind == LGX_MATRIX_CSR) {
     if (a->csr.storage == LGX_F64) return csr_spmv<double, double>(a->csr, a->csr.v64.p, x, y, s);
@@ -926,6 +998,26 @@ static lgx_status stencil_create(const int64_t dims[3], const double q[3], const
   for (int d = 0; d < 3; ++d) nnz += 2 * (dims[d] - 1) * (n / dims[d]);
   m->nnz = nnz;
   *out = m;
+  return LGX_OK;
+}
+
+lgx_status lgx_box_axis_quotients(const lgx_box_info *box, double q[3]) {
+  if (!box || !q) return fail(LGX_ERR_INVALID, "null argument");
+  double h[3];
+  for (int d = 0; d < 3; ++d) {
+    if (box->cells[d] < 1) return fail(LGX_ERR_INVALID, "cell counts must be positive");
+    if (!(box->lengths[d] > 0.0) || !std::isfinite(box->lengths[d]))
+      return fail(LGX_ERR_INVALID, "axis lengths must be positive and finite");
+    h[d] = box->lengths[d] / (double)box->cells[d];
+  }
+  // the axis area (the other axes' spacings multiplied from the lowest axis)
+  // over the axis's own spacing
+  for (int d = 0; d < 3; ++d) {
+    double area = 1.0;
+    for (int e = 0; e < 3; ++e)
+      if (e != d) area = area * h[e];
+    q[d] = area / h[d];
+  }
   return LGX_OK;
 }
 

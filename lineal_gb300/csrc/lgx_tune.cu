@@ -165,7 +165,7 @@ lgx_status confirm_in_cycle(lgx_amg &h, std::vector<lgx_tune_entry> &all, int re
                             cudaStream_t s) {
   const int L = (int)h.lv.size();
   if (L < 2) return LGX_OK;
-  const int64_t n = h.lv[0]->col->pcsr.n;
+  const int64_t n = h.lv[0]->a->n;
   DBuf<double> b, x;
   LGX_CHECK(b.alloc(n));
   LGX_CHECK(x.alloc(n));

@@ -580,9 +580,88 @@ int32_t lo_colour_jp(const lo_csr *a, uint64_t seed, int32_t *colour) {
  * non-empty bucket and move its remaining neighbours (CSR order) to the
  * head of the bucket below; colour in reverse removal order with the
  * smallest colour no coloured neighbour has. */
-int32_t lo_colour_smallest_last(const lo_csr *a, int32_t *colour) {
+static int32_t colour_smallest_last_rows(const lo_csr *a, int32_t *colour);
+
+static int cmp_i32(const void *x, const void *y) {
+  const int32_t a = *(const int32_t *)x, b = *(const int32_t *)y;
+  return (a > b) - (a < b);
+}
+
+/* The adjacency the colouring uses: a's rows when the off-diagonal pattern
+ * is structurally symmetric (returns 0), else in *out the pattern of A + A^T
+ * with sorted rows and no diagonal (returns 1; the caller frees it). */
+static int sl_symmetrised(const lo_csr *a, lo_csr *out) {
   const int64_t n = a->n;
-  if (n == 0) return 0;
+  int64_t *tp = (int64_t *)calloc((size_t)n + 1, sizeof(int64_t));
+  for (int64_t i = 0; i < n; ++i)
+    for (int64_t e = a->rowptr[i]; e < a->rowptr[i + 1]; ++e)
+      if (a->col[e] != i) ++tp[a->col[e] + 1];
+  for (int64_t i = 0; i < n; ++i) tp[i + 1] += tp[i];
+  int32_t *tc = (int32_t *)malloc((size_t)(tp[n] + 1) * sizeof(int32_t));
+  int64_t *fill = (int64_t *)malloc((size_t)(n + 1) * sizeof(int64_t));
+  for (int64_t i = 0; i < n; ++i) fill[i] = tp[i];
+  for (int64_t i = 0; i < n; ++i)
+    for (int64_t e = a->rowptr[i]; e < a->rowptr[i + 1]; ++e)
+      if (a->col[e] != i) tc[fill[a->col[e]]++] = (int32_t)i;
+  int64_t maxrow = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t len = a->rowptr[i + 1] - a->rowptr[i] + tp[i + 1] - tp[i];
+    if (len > maxrow) maxrow = len;
+  }
+  int32_t *row = (int32_t *)malloc((size_t)(maxrow + 1) * sizeof(int32_t));
+  int symmetric = 1;
+  for (int64_t i = 0; i < n && symmetric; ++i) {
+    int64_t m = 0;
+    for (int64_t e = a->rowptr[i]; e < a->rowptr[i + 1]; ++e)
+      if (a->col[e] != i) row[m++] = a->col[e];
+    qsort(row, (size_t)m, sizeof(int32_t), cmp_i32);
+    if (m != tp[i + 1] - tp[i]) symmetric = 0;
+    for (int64_t k = 0; k < m && symmetric; ++k)
+      if (row[k] != tc[tp[i] + k]) symmetric = 0;
+  }
+  if (!symmetric) {
+    int64_t total = 0;
+    int64_t *rp = (int64_t *)malloc((size_t)(n + 1) * sizeof(int64_t));
+    int32_t *cc = (int32_t *)malloc((size_t)(a->rowptr[n] + tp[n] + 1) * sizeof(int32_t));
+    rp[0] = 0;
+    for (int64_t i = 0; i < n; ++i) {
+      int64_t m = 0;
+      for (int64_t e = a->rowptr[i]; e < a->rowptr[i + 1]; ++e)
+        if (a->col[e] != i) row[m++] = a->col[e];
+      for (int64_t k = tp[i]; k < tp[i + 1]; ++k) row[m++] = tc[k];
+      qsort(row, (size_t)m, sizeof(int32_t), cmp_i32);
+      for (int64_t k = 0; k < m; ++k)
+        if (k == 0 || row[k] != row[k - 1]) cc[total++] = row[k];
+      rp[i + 1] = total;
+    }
+    memset(out, 0, sizeof(*out));
+    out->n = n;
+    out->ncols = n;
+    out->rowptr = rp;
+    out->col = cc;
+  }
+  free(tp);
+  free(tc);
+  free(fill);
+  free(row);
+  return !symmetric;
+}
+
+int32_t lo_colour_smallest_last(const lo_csr *a_in, int32_t *colour) {
+  lo_csr sym;
+  const int own = a_in->n > 0 && sl_symmetrised(a_in, &sym);
+  const lo_csr *a = own ? &sym : a_in;
+  const int32_t nc = colour_smallest_last_rows(a, colour);
+  if (own) {
+    free(sym.rowptr);
+    free(sym.col);
+  }
+  return nc;
+}
+
+static int32_t colour_smallest_last_rows(const lo_csr *a, int32_t *colour) {
+  const int64_t n = a->n;
+  if (n <= 0) return 0;
   int64_t *d = (int64_t *)malloc((size_t)n * sizeof(int64_t));
   int64_t *nx = (int64_t *)malloc((size_t)n * sizeof(int64_t));
   int64_t *pv = (int64_t *)malloc((size_t)n * sizeof(int64_t));

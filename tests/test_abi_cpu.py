@@ -109,3 +109,26 @@ def test_ctypes_structs_match_the_header(tmp_path):
         assert got[(cname, "size")] == ctypes.sizeof(py), cname
         for field, _ in py._fields_:
             assert got[(cname, field)] == getattr(py, field).offset, (cname, field)
+
+
+def test_box_info_quotients_match_the_oracle():
+    """BoxInfo's axis quotients (box-equidistant.hpp:67-79) computed by the
+    library's host code equal the oracle's bit for bit; bad boxes are
+    refused.  Host-only call: no GPU needed."""
+    import numpy as np
+
+    import lineal_gb300 as g
+    import oracle as lo
+
+    rng = np.random.default_rng(1)
+    boxes = [((4, 9, 7), (4.0, 9.0, 7.0)), ((64, 64, 64), (64.0, 64.0, 64.0)),
+             ((4, 8, 4), (4.0, 8.0, 4.0)), ((17, 13, 19), (1.3, 0.7, 2.1))]
+    boxes += [(tuple(int(c) for c in rng.integers(1, 300, 3)),
+               tuple(float(v) for v in rng.uniform(0.01, 50.0, 3))) for _ in range(50)]
+    for cells, lengths in boxes:
+        got = g.BoxInfo(cells, lengths).axis_quotients()
+        np.testing.assert_array_equal(got, lo.axis_quotients(cells, lengths))
+    for cells, lengths in (((0, 4, 4), (1.0, 1.0, 1.0)), ((4, 4, 4), (1.0, -1.0, 1.0)),
+                           ((4, 4, 4), (1.0, float("inf"), 1.0))):
+        with pytest.raises(g.LinealError):
+            g.BoxInfo(cells, lengths).axis_quotients()

@@ -78,3 +78,31 @@ def test_oracle_amg_with_smallest_last_coarse_levels():
         its.append(it)
     assert colours[1] < colours[0]
     assert abs(its[1] - its[0]) <= 1
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_structurally_nonsymmetric_pattern_colours_a_plus_at(seed):
+    """A pattern with (i, j) stored but not (j, i): both colourings work on
+    the pattern of A + A^T, agree bit for bit and are proper for every edge
+    in either direction (the multicolour sweep reads both)."""
+    rng = np.random.default_rng(seed)
+    n = 300
+    rows = []
+    for i in range(n):
+        cols = {i}
+        cols.update(int(c) for c in rng.integers(0, n, rng.integers(0, 6)))
+        rows.append(sorted(cols))
+    rowptr = np.zeros(n + 1, np.int64)
+    rowptr[1:] = np.cumsum([len(r) for r in rows])
+    col = np.concatenate([np.asarray(r, np.int32) for r in rows])
+    a = lo.Csr(rowptr, col, np.ones(len(col)), symmetric=False)
+    got, nc = g.colour_smallest_last(rowptr, col)
+    want, wnc = lo.colour_smallest_last(a)
+    np.testing.assert_array_equal(got, want)
+    assert nc == wnc
+    r = np.repeat(np.arange(n), np.diff(rowptr))
+    off = col != r
+    assert not np.any(got[r[off]] == got[col[off]])
+    # the pattern really is nonsymmetric
+    pairs = set(zip(r[off].tolist(), col[off].tolist()))
+    assert any((j, i) not in pairs for i, j in pairs)

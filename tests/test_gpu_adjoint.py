@@ -58,39 +58,71 @@ def _problem(dims, seed=4):
     return theta, theta_t, _bump(dims)
 
 
-@pytest.mark.parametrize("mixed", [False, True])
-def test_adjoint_gradient_matches_finite_differences(cuda, mixed):
+def _fd_check(cuda, dims, mixed, directions, seed=4, partition_size=500):
+    """Largest relative gap between the adjoint gradient along random unit
+    directions and FP64 central differences (h = 1e-6) of the loss."""
     import torch
 
-    from lineal_gb300.autograd import (SolveOptions, accurate_forward, diffusion7_solve,
+    from lineal_gb300.autograd import (SolveOptions, accurate_system, diffusion7_solve,
                                        loss_difference_fd)
 
-    dims = (12, 13, 11)
-    theta0, theta_t, b0 = _problem(dims)
-    opts = SolveOptions(rtol=1e-11, mixed=mixed, min_coarsen_size=100, partition_size=500)
-    fd_opts = SolveOptions(rtol=1e-10, min_coarsen_size=100, partition_size=500)
+    theta0, theta_t, b0 = _problem(dims, seed)
+    opts = SolveOptions(rtol=1e-11, mixed=mixed, min_coarsen_size=100,
+                        partition_size=partition_size)
+    fd_opts = SolveOptions(rtol=1e-10, min_coarsen_size=100, partition_size=partition_size)
     b = torch.as_tensor(b0, device="cuda")
-    x_t = accurate_forward(torch.as_tensor(theta_t, device="cuda"), b, dims, fd_opts)
-
-    def loss(th):
-        x = diffusion7_solve(th, b, dims, opts)
-        return 0.5 * torch.sum((x - x_t) ** 2)
+    _, _, x_t = accurate_system(torch.as_tensor(theta_t, device="cuda"), b, dims, fd_opts)
 
     theta = torch.as_tensor(theta0, device="cuda").requires_grad_(True)
-    loss(theta).backward()
+    x = diffusion7_solve(theta, b, dims, opts)
+    (0.5 * torch.sum((x - x_t) ** 2)).backward()
     g = theta.grad.detach()
     rng = np.random.default_rng(5)
     h = 1e-6
-    worst = 0.0
     th0 = theta.detach()
-    x0 = accurate_forward(th0, b, dims, fd_opts)
-    for _ in range(8):
+    a0, h0, x0 = accurate_system(th0, b, dims, fd_opts)
+    errs = []
+    for _ in range(directions):
         v = rng.standard_normal(theta0.size)
         vt = torch.as_tensor(v / np.linalg.norm(v), device="cuda")
-        fd = loss_difference_fd(th0, vt, h, b, dims, x0, x_t, fd_opts)
+        fd = loss_difference_fd(th0, vt, h, dims, x0, x_t, a0, h0)
         gv = float(torch.dot(g, vt))
-        worst = max(worst, abs(fd - gv) / abs(gv))
-    assert worst <= 1e-6, worst
+        errs.append(abs(fd - gv) / abs(gv))
+    return max(errs)
+
+
+@pytest.mark.parametrize("mixed", [False, True])
+def test_adjoint_gradient_matches_finite_differences(cuda, mixed):
+    assert _fd_check(cuda, (12, 13, 11), mixed, 8) <= 1e-6
+
+
+def test_adjoint_gradient_matches_finite_differences_128(cuda):
+    """The differentiation workload's own size: 128^3, theta ~ N(0, 1), 64
+    random directions, h = 1e-6, mixed-precision forward and adjoint."""
+    assert _fd_check(cuda, (128, 128, 128), True, 64, partition_size=4096) <= 1e-6
+
+
+def test_delta_apply_equals_matrix_difference(cuda):
+    """(A(theta + d) - A(theta)) x without forming the matrices equals the
+    difference of the assembled products where that difference is accurate
+    (a large step), and scales linearly for small steps."""
+    import torch
+
+    from lineal_gb300.autograd import diffusion7_delta_apply
+
+    dims = (9, 10, 11)
+    n = int(np.prod(dims))
+    rng = np.random.default_rng(8)
+    theta = rng.standard_normal(n)
+    d = 1e-2 * rng.standard_normal(n)
+    x = rng.uniform(-1, 1, n)
+    want = (lo.spmv(lo.gen_7pt(dims, np.exp(theta + d)), x)
+            - lo.spmv(lo.gen_7pt(dims, np.exp(theta)), x))
+    t = lambda v: torch.as_tensor(v, device="cuda")  # noqa: E731
+    got = diffusion7_delta_apply(t(theta), t(d), t(x), dims).cpu().numpy()
+    assert np.abs(got - want).max() <= 1e-12 * np.abs(want).max()
+    small = diffusion7_delta_apply(t(theta), t(1e-9 * d), t(x), dims).cpu().numpy()
+    np.testing.assert_allclose(small * 1e9, got, rtol=5e-2, atol=1e-2 * np.abs(got).max())
 
 
 def test_adjoint_gradient_matches_oracle_solves(cuda):

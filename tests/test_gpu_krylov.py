@@ -52,14 +52,17 @@ def test_reference_suite_bounds(cuda, name, fn, kw, iters, bound_x2, bound_rhs):
     assert res.history[-1] <= bound_rhs and np.abs(lo.spmv(a, x) - b).max() <= bound_rhs
 
 
-def test_jacobi_pcg_poisson_matches_oracle(cuda):
-    # small version of the 64^3 Poisson workload: lookup stencil, one material
-    dims = (24, 24, 24)
+@pytest.mark.parametrize("edge", [24, 64])
+def test_jacobi_pcg_poisson_matches_oracle(cuda, edge):
+    # the plain-method workload (64^3 Poisson as a lookup stencil with one
+    # material, unit cells, b ~ U[-1, 1] seed 0, x0 = 0, Jacobi-PCG to 1e-8)
+    # and a smaller copy
+    dims = (edge,) * 3
     n = int(np.prod(dims))
     mat = np.ones(n, dtype=np.uint8)
     coeffs = (0.0, 1.0, 0.0, 0.0)
     b = np.random.default_rng(0).uniform(-1, 1, n)
-    st = cuda.StencilMatrix.lookup(dims, (1, 1, 1), coeffs, mat, 0.0, 0.0)
+    st = cuda.StencilMatrix.lookup(cuda.BoxInfo(dims, dims), None, coeffs, mat, 0.0, 0.0)
     res = cuda.pcg(st, b, precon=cuda.PRECON_JACOBI, rtol=1e-8, maxit=1000)
     ref = lo.Stencil(dims, mat=mat, coeffs=coeffs, sol_start=0, sol_end=0)
     a, _ = ref.to_csr()
@@ -147,6 +150,44 @@ def test_flexible_cg_precision_form(cuda):
     assert flex32.iterations <= plain.iterations + max(2, plain.iterations // 10)
     x64 = plain.x.cpu().numpy()
     assert np.linalg.norm(flex32.x.cpu().numpy() - x64) <= 1e-7 * np.linalg.norm(x64)
+
+
+def test_precision_form_five_levels_matches_oracle(cuda):
+    """The precision-form operator family (7 points, lognormal sigma = 3,
+    seed 2) on a 56^3 grid whose hierarchy has at least five levels, as the
+    256^3 workload's does: level sizes equal the oracle's; the FP64 solve's
+    iterations are the oracle's; flexible CG and the refinement over the
+    float cycle reach 1e-10 verified in FP64 with the oracle's product,
+    within a few iterations of the oracle, close to its solution."""
+    dims = (56, 56, 56)
+    n = int(np.prod(dims))
+    k = np.exp(3.0 * np.random.default_rng(2).standard_normal(n))
+    ref = lo.gen_7pt(dims, k)
+    b = np.random.default_rng(0).uniform(-1, 1, n)
+    m = cuda.gen_7pt(dims, k)
+    i, j, kk = np.meshgrid(*[np.arange(d) for d in dims], indexing="ij")
+    rb = ((i + j + kk) % 2).ravel().astype(np.int32)
+    col = cuda.Colouring.from_array(m, rb, 2)
+    params = dict(min_coarsen_size=200, partition_size=4096)
+    h64 = cuda.HierarchyWright(**params).instantiate(m, finest_colouring=col)
+    h32 = cuda.HierarchyWright(cycle_f32=True, **params).instantiate(m, finest_colouring=col)
+    oh = lo.Amg(ref, finest_colours=rb, ncolours=2, smoother_parts=0, **params)
+    rows, _ = h64.sizes()
+    assert len(rows) >= 5
+    assert rows == [oh.level_size(l) for l in range(oh.nlevels)]
+    xo, it, hist = lo.pcg(ref, b, precon=lo.PRECON_AMG, amg=oh, rtol=1e-10, maxit=600)
+    plain = cuda.pcg(m, b, precon=cuda.PRECON_AMG, amg=h64, rtol=1e-10, maxit=600)
+    assert abs(plain.iterations - it) <= max(1, int(0.05 * it + 0.999))
+    np.testing.assert_allclose(plain.history[:5], hist[:5], rtol=1e-9)
+    for res in (plain,
+                cuda.pcg(m, b, precon=cuda.PRECON_AMG, amg=h32, rtol=1e-10, maxit=600,
+                         flexible=True),
+                cuda.pcg(m, b, precon=cuda.PRECON_AMG, amg=h32, rtol=1e-10, maxit=600,
+                         refine=True)):
+        xr = res.x.cpu().numpy()
+        assert np.linalg.norm(b - lo.spmv(ref, xr)) <= 1.2e-10 * np.linalg.norm(b)
+        assert res.iterations <= it + max(5, (15 * it) // 100)
+        assert np.linalg.norm(xr - xo) <= 1e-6 * np.linalg.norm(xo)
 
 
 @pytest.mark.parametrize("dims,npts", [((20, 20, 20), 27), ((24, 24, 24), 7)])

@@ -78,7 +78,8 @@ def test_stencil_lookup_bitexact(cuda, dims, zero_to_one):
     coeffs = (0.0, 1.0, 2.0, 3.0)
     ref = lo.Stencil(dims, q=q, mat=mat, coeffs=coeffs, sol_start=1.0, sol_end=0.5,
                      zero_to_one=zero_to_one)
-    m = cuda.StencilMatrix.lookup(dims, q, coeffs, mat, 1.0, 0.5, zero_to_one)
+    m = cuda.StencilMatrix.lookup(cuda.BoxInfo(dims, (1.3, 0.7, 2.1)), None, coeffs, mat, 1.0,
+                                  0.5, zero_to_one)
     x = np.random.default_rng(2).uniform(-1, 1, ref.n)
     np.testing.assert_array_equal(cuda.spmv(m, x).cpu().numpy(), ref.spmv(x))
     np.testing.assert_array_equal(m.diagonal().cpu().numpy(), ref.diagonal())
@@ -99,7 +100,7 @@ def test_stencil_value_bitexact(cuda, dims):
     k[::7] = 0.0  # zero conductivities exercise the harmonic-mean guard
     q = lo.axis_quotients(dims, dims)
     ref = lo.Stencil(dims, q=q, k=k, sol_start=1.0, sol_end=0.0)
-    m = cuda.StencilMatrix.value(dims, q, k, 1.0, 0.0)
+    m = cuda.StencilMatrix.value(cuda.BoxInfo(dims, dims), None, k, 1.0, 0.0)
     x = np.random.default_rng(8).uniform(-1, 1, n)
     np.testing.assert_array_equal(cuda.spmv(m, x).cpu().numpy(), ref.spmv(x))
     np.testing.assert_array_equal(m.rhs().cpu().numpy(), ref.rhs())
@@ -195,7 +196,8 @@ def test_effective_diffusion_matches_oracle(cuda, zero_to_one):
     dims, coeffs, lengths = (4, 9, 7), (0.0, 1.0, 2.0, 3.0), (4.0, 9.0, 7.0)
     q = lo.axis_quotients(dims, lengths)
     mat = _diagonal_lines(dims)
-    st = cuda.StencilMatrix.lookup(dims, q, coeffs, mat, 1.0, 0.0, zero_to_one)
+    st = cuda.StencilMatrix.lookup(cuda.BoxInfo(dims, lengths), None, coeffs, mat, 1.0, 0.0,
+                                   zero_to_one)
     ref = lo.Stencil(dims, q=q, mat=mat, coeffs=coeffs, sol_start=1.0, sol_end=0.0,
                      zero_to_one=zero_to_one)
     if zero_to_one:
@@ -224,7 +226,7 @@ def test_stencil_values_bitexact(cuda, stencil_engine):
     ks = [np.exp(rng.standard_normal(n)) for _ in range(3)]
     q = lo.axis_quotients(dims, (1.5, 0.7, 2.0))
     ref = lo.Stencil(dims, q=q, k_axes=ks, sol_start=1.0, sol_end=0.25)
-    m = cuda.StencilMatrix.values(dims, q, ks, 1.0, 0.25)
+    m = cuda.StencilMatrix.values(cuda.BoxInfo(dims, (1.5, 0.7, 2.0)), None, ks, 1.0, 0.25)
     x = rng.uniform(-1, 1, n)
     np.testing.assert_array_equal(cuda.spmv(m, x).cpu().numpy(), ref.spmv(x))
     np.testing.assert_array_equal(m.diagonal().cpu().numpy(), ref.diagonal())
@@ -247,7 +249,8 @@ def test_stencil_henry_bitexact(cuda, stencil_engine):
     q = lo.axis_quotients(dims, lengths)
     ref = lo.Stencil(dims, q=q, mat=mat, coeffs=coeffs, sol_start=1.0, sol_end=0.0, henry=0.3,
                      gaseous_mask=0b0110)
-    m = cuda.StencilMatrix.lookup_henry(dims, q, coeffs, mat, 0.3, 0b0110, 1.0, 0.0)
+    m = cuda.StencilMatrix.lookup_henry(cuda.BoxInfo(dims, lengths), None, coeffs, mat, 0.3,
+                                        0b0110, 1.0, 0.0)
     x = np.random.default_rng(26).uniform(-1, 1, ref.n)
     np.testing.assert_array_equal(cuda.spmv(m, x).cpu().numpy(), ref.spmv(x))
     np.testing.assert_array_equal(m.diagonal().cpu().numpy(), ref.diagonal())
