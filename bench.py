@@ -357,7 +357,8 @@ def precision_form(g, args, stream):
     xs = {}
     for tag, f32, bf16, flexible, refine in (("fp64", False, False, False, False),
                                              ("mixed_fcg", True, False, True, False),
-                                             ("mixed_refined", True, False, False, True),
+                                             ("mixed_refined", True, False, True,
+                                              args.refine),
                                              ("mixed_bf16_fcg", True, True, True, False)):
         t0 = time.perf_counter()
         h = g.HierarchyWright(cycle_f32=f32, cycle_bf16=bf16, **hier_kw).instantiate(
@@ -368,14 +369,14 @@ def precision_form(g, args, stream):
             h.autotune(reps=3)
         for _ in range(args.warmup):
             res = g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=1e-10, maxit=1000,
-                        flexible=flexible, refine=refine)
+                        flexible=flexible, refine=refine, inner_rtol=args.inner_rtol)
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(args.steps):
             res = g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=1e-10, maxit=1000,
-                        flexible=flexible, refine=refine)
+                        flexible=flexible, refine=refine, inner_rtol=args.inner_rtol)
         e1.record(stream)
         e1.synchronize()
         _, rn = g.residual(a, b, res.x)
@@ -497,7 +498,8 @@ def run_gb300(args):
     # hierarchy): float products and V-cycles, FP64 dots, scalars, outer
     # residual and stopping test
     def solve_refined(h):
-        return g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=1e-8, maxit=500, refine=True)
+        return g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=1e-8, maxit=500, refine=args.refine,
+                     inner_rtol=args.inner_rtol, flexible=args.refine_flexible)
 
     for _ in range(args.warmup):
         resr = solve_refined(h32)
@@ -630,6 +632,10 @@ def run_gb300(args):
         h_col_colours = torch.from_numpy(colours).pin_memory()
         del h32
         e2e_ms = []
+        # a one-shot solve: Jones-Plassmann coarse colourings (device-side,
+        # fast setup) whatever the resident solves use
+        e2e_kw = dict(hier_kw, coarse_smallest_last=False)
+        phases = []
         for step in range(args.e2e_steps):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
@@ -638,23 +644,40 @@ def run_gb300(args):
             d_val = h_val.to("cuda", non_blocking=True)
             d_b = h_b.to("cuda", non_blocking=True)
             d_colours = h_col_colours.to("cuda", non_blocking=True)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
             m = g.CsrMatrix.from_device(d_rowptr, d_col, d_val, symmetric=True)
             if args.grid27:
                 m.set_grid27(dims)  # the caller knows its operator is the 27-point grid
             del d_rowptr, d_col, d_val
             c = g.Colouring.from_array(m, d_colours, 8)
-            hh = g.HierarchyWright(cycle_f32=True, **hier_kw).instantiate(
+            torch.cuda.synchronize()
+            t2 = time.perf_counter()
+            hh = g.HierarchyWright(cycle_f32=True, **e2e_kw).instantiate(
                 m, finest_colouring=c)
-            rr = g.pcg(m, d_b, precon=g.PRECON_AMG, amg=hh, rtol=1e-8, maxit=500)
+            torch.cuda.synchronize()
+            t3 = time.perf_counter()
+            rr = g.pcg(m, d_b, precon=g.PRECON_AMG, amg=hh, rtol=1e-8, maxit=500,
+                       refine=args.refine if args.e2e_refine else 0,
+                       inner_rtol=args.inner_rtol)
+            torch.cuda.synchronize()
+            t4 = time.perf_counter()
             xh = rr.x.cpu()
             torch.cuda.synchronize()
-            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+            t5 = time.perf_counter()
+            e2e_ms.append((t5 - t0) * 1e3)
+            phases.append({"h2d": (t1 - t0) * 1e3, "matrix_and_colouring": (t2 - t1) * 1e3,
+                           "hierarchy": (t3 - t2) * 1e3, "solve": (t4 - t3) * 1e3,
+                           "d2h": (t5 - t4) * 1e3, "iterations": rr.iterations})
             del m, c, hh, rr
         h2d = (rowptr.nbytes + colidx.nbytes + val.nbytes + b_host.nbytes + colours.nbytes)
         e2e = {"value": float(np.median(e2e_ms)), "unit": "ms", "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(n * 8),
-               "what": "host CSR + b (pinned) -> device, AMG setup (mixed), PCG, x -> host"}
-        log(f"[gb300] e2e {e2e['value']:.0f} ms")
+               "d2h_bytes_per_step": int(n * 8), "phases_ms": phases[len(phases) // 2],
+               "what": "host CSR + b (pinned) -> device, AMG setup (float cycle, "
+                       "Jones-Plassmann coarse colourings), "
+                       + ("float-vector CG with FP64 residual (refine "
+                          f"{args.refine})" if args.e2e_refine else "CG") + ", x -> host"}
+        log(f"[gb300] e2e {e2e['value']:.0f} ms {e2e['phases_ms']}")
 
     # ---- CPU baseline (bounded sample) -----------------------------------------
     prec = precision_form(g, args, stream) if args.precision_form else None
@@ -700,9 +723,13 @@ def run_gb300(args):
                   "speedup_vs_fp64": ms64 / ms32, "rel_error_vs_fp64_solution": err},
         "mixed_refined": {"ms": msr, "iterations": resr.iterations, "rel_residual_fp64": relr,
                           "speedup_vs_fp64": ms64 / msr, "rel_error_vs_fp64_solution": errr,
-                          "what": "FP64 iterative refinement over a float-vector inner PCG "
-                                  "(float finest products and V-cycle; FP64 dots, CG scalars, "
-                                  "outer residual), inner tolerance 1e-4"},
+                          "what": ("float-vector CG with reliable updates (FP64 solution "
+                                   "and residual replaced every " if args.refine == 2 else
+                                   "FP64 iterative refinement over a float-vector inner PCG, "
+                                   "inner tolerance ") + f"{args.inner_rtol:g}" +
+                                  (" reduction" if args.refine == 2 else "") +
+                                  "; float finest products and V-cycle, FP64 dots and CG "
+                                  "scalars", "refine": args.refine},
         "mixed_speedup_vs_fp64": ms64 / min(ms32, msr),
         "mixed_bf16": {"ms": ms16, "iterations": res16.iterations, "rel_residual_fp64": rel16,
                        "autotune_ms": tune16, "speedup_vs_fp64": ms64 / ms16,
@@ -872,6 +899,32 @@ def run_stencil(args):
                 log(f"[stencil] {name}: {ms:.3f} ms {gbs:.0f} GB/s ({gbs / peak:.0%} of HBM) "
                     f"{tf:.2f} FP64 TFLOP/s ({tf / FP64_PEAK_TFLOPS:.0%} of nominal)")
     g.stencil_engine(0)
+    # matrix-free red-black SOR sweeps (two colour launches, in situ):
+    # algorithmic bytes per cell = valuator data + diagonal + b + x read and
+    # written; 6 FMAs and one division per cell
+    sweep_bytes = {"lookup": 1 + 8 + 8 + 8 + 8, "value": 24 + 8 + 8 + 8 + 8}
+    for kind, m in st.items():
+        col = g.Colouring.red_black(m)
+        xs = x.clone()
+        fn = lambda: g.sor_sweep(m, col, b, x_in=xs, out=xs)  # noqa: E731
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        gbs = sweep_bytes[kind] * n / (ms * 1e-3) / 1e9
+        tf = 2 * (fmas - n) / (ms * 1e-3) / 1e12
+        name = f"{kind}_sor_red_black"
+        out[name] = {"ms": ms, "gbs": gbs, "hbm_frac": gbs / peak, "fp64_tflops": tf,
+                     "fp64_frac": tf / FP64_PEAK_TFLOPS}
+        log(f"[stencil] {name}: {ms:.3f} ms {gbs:.0f} GB/s ({gbs / peak:.0%} of HBM) "
+            f"{tf:.2f} FP64 TFLOP/s of FMAs")
     print(json.dumps({"mode": "stencil", "grid": args.grid, "cells": n, "fp64_fmas": fmas,
                       "hbm_peak_gbs": peak, "hbm_peak_kind": peak_kind,
                       "fp64_peak_tflops": FP64_PEAK_TFLOPS, "fp64_peak_kind": "nominal",
@@ -1196,7 +1249,15 @@ def main():
                     help="skip the 7-point sigma=3 precision-form solves")
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
     ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--no-e2e-refine", dest="e2e_refine", action="store_false",
+                    help="e2e: plain CG over the float cycle instead of --refine")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--refine", type=int, default=2, choices=[1, 2],
+                    help="mixed_refined: 1 iterative refinement, 2 reliable updates")
+    ap.add_argument("--refine-flexible", action="store_true",
+                    help="mixed_refined of the 27-point workload: flexible beta")
+    ap.add_argument("--inner-rtol", type=float, default=1e-4,
+                    help="mixed_refined: inner tolerance / reduction between FP64 residuals")
     ap.add_argument("--no-configs", dest="configs", action="store_false",
                     help="skip the 64^3 Jacobi-PCG, batch, 32-RHS and adjoint keys")
     ap.add_argument("--bench-fd-directions", type=int, default=16,

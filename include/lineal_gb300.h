@@ -316,6 +316,15 @@ lgx_status lgx_colouring_create_jp(const lgx_matrix *a, uint64_t seed, lgx_strea
  * to lgx_colouring_create. */
 lgx_status lgx_colour_smallest_last(int64_t n, const int64_t *rowptr, const int32_t *col,
                                     int32_t *colour, int32_t *ncolours);
+/* Failure-detection self-test (no reference counterpart): launches a kernel
+ * whose bounded wait on a shared-memory barrier can never complete (nothing
+ * arrives), so the wait gives up after about one second of SM clock, records
+ * the time-out in the device error flag and returns; the call then reports
+ * it as LGX_ERR_CUDA ("a device wait ... timed out") and clears the flag,
+ * the same path by which the staged kernels report a copy that never lands.
+ * The context stays usable.  Synchronises `stream`. */
+lgx_status lgx_wait_selftest(lgx_stream stream);
+
 /* Red-black colouring of a stencil matrix, colour (p0 + p1 + p2) & 1: the
  * 7-point stencil's natural two-colouring.  lgx_sor_sweep then runs
  * matrix-free in natural order, one launch per colour, and equals lineal's
@@ -574,19 +583,25 @@ typedef struct {
                                    for preconditioners that are not exactly linear (the
                                    float V-cycle of the precision form); no counterpart
                                    in the reference's CG (solver.hpp:105-107) */
-  int refine;                   /* lgx_pcg with an AMG hierarchy built with cycle_f32:
-                                   FP64 iterative refinement (precision form; no
-                                   reference counterpart).  Each outer step forms the
-                                   FP64 residual r = b - A x, solves A d = r / ||r|| by
-                                   PCG with float vectors (float finest-level products
-                                   and float V-cycle; dot products accumulated and CG
-                                   scalars kept in FP64) to inner_rtol, and adds
-                                   ||r|| d to x in FP64; it stops on the FP64 residual.
-                                   *iterations counts the inner iterations (one product
-                                   and one V-cycle each), h_history holds the inner
-                                   residual estimates and, after each outer step, the
-                                   FP64 residual */
-  double inner_rtol;            /* refine: inner relative tolerance (1e-4) */
+  int refine;                   /* lgx_pcg with an AMG hierarchy built with cycle_f32
+                                   (precision form; no reference counterpart): CG on
+                                   float vectors -- float finest-level products and
+                                   float V-cycle, dot products accumulated and CG
+                                   scalars kept in FP64 -- under an FP64 solution and
+                                   FP64 residual; the solve stops on the FP64 residual.
+                                   1: iterative refinement, each outer step solves
+                                   A d = r / ||r|| from scratch to inner_rtol and adds
+                                   ||r|| d to x.  2: reliable updates, one unbroken
+                                   float recurrence whose accumulated update is folded
+                                   into x, and r replaced by the FP64 residual, each
+                                   time the recursive residual has fallen by inner_rtol
+                                   (with flexible = 1 its beta is the flexible one).
+                                   *iterations counts the float iterations (one product
+                                   and one V-cycle each); h_history holds the float
+                                   residual estimates and, at each FP64 residual, that
+                                   residual */
+  double inner_rtol;            /* refine 1: inner relative tolerance (1e-4); refine 2:
+                                   reduction between FP64 residuals (1e-4) */
 } lgx_solve_params;
 
 void lgx_solve_default_params(lgx_solve_params *p);

@@ -184,6 +184,7 @@ struct AggDev {
   int32_t *eval;        // per front position: 4 ints of evaluation results
   int64_t *pcount;      // aggregates per partition
   int64_t *stats;       // 5 counters (atomic adds)
+  int32_t *conn_flag32; // k_aggregate_block: connected flags by local aggregate id (atomics)
 };
 
 __device__ __forceinline__ int64_t part_begin(int64_t n, int64_t p, int64_t k) {
@@ -515,6 +516,390 @@ struct AggWarp {
 
 constexpr int kAggWarpsPerBlock = 4;
 
+// ---------------------------------------------------------------------------
+// The same aggregation with a whole CTA per partition, for levels with few
+// partitions (the coarse levels: 8 to a few hundred partitions of up to ~1e5
+// vertices), where one warp per partition leaves the GPU almost idle and the
+// front evaluations -- a chain of dependent loads per edge batch -- dominate.
+// Every thread runs the same control flow: each decision is a block-wide
+// reduction whose result every thread reads from shared memory after a
+// barrier, so the loop bounds, branches and barrier counts are uniform across
+// the CTA.  Writes of a single thread (aggregate membership, the front swap)
+// are published by the barrier that follows them.  The front and the
+// connected set take their slots through shared-memory atomics: their order
+// differs from the warp kernel's, but no decision depends on it (selections
+// take the smallest vertex ids, evaluations are recomputed per step), so the
+// aggregates are the warp kernel's -- and the oracle's -- exactly.
+// ---------------------------------------------------------------------------
+constexpr int kAggBlockThreads = 256;
+constexpr int kAggBlockWarps = kAggBlockThreads / 32;
+
+struct AggBlockShared {
+  int32_t front_len, conn_len;
+  int64_t part_i64[kAggBlockWarps];
+  int32_t part_k0[kAggBlockWarps], part_kn[kAggBlockWarps];
+  double part_kc[kAggBlockWarps];
+  int32_t part_have[kAggBlockWarps];
+  int64_t res_i64;
+  int32_t res_k0, res_kn, res_have;
+  double res_kc;
+};
+
+struct AggBlock {
+  const AggDev &D;
+  AggBlockShared &sh;
+  int64_t pb, pe;
+  int tid, lane, warp;
+  // block-uniform state, identical in every thread
+  int64_t counter = 0;
+  int64_t st[5] = {0, 0, 0, 0, 0};
+
+  __device__ AggBlock(const AggDev &d, AggBlockShared &s, int64_t b, int64_t e)
+      : D(d), sh(s), pb(b), pe(e) {
+    tid = threadIdx.x;
+    lane = tid & 31;
+    warp = tid >> 5;
+  }
+  __device__ bool in_range(int64_t v) const { return v >= pb && v < pe; }
+  __device__ int32_t &blen(uint32_t ag) const { return D.block_len[pb + ag]; }
+  __device__ int32_t *block(uint32_t ag) const {
+    return D.blocks + (pb + (int64_t)ag) * D.max_size;
+  }
+
+  // block-wide minimum of an int64 (every thread gets it)
+  __device__ int64_t block_min(int64_t v) {
+    for (int o = 16; o > 0; o >>= 1) {
+      const int64_t other = __shfl_xor_sync(kFull, v, o);
+      v = other < v ? other : v;
+    }
+    if (lane == 0) sh.part_i64[warp] = v;
+    __syncthreads();
+    if (tid == 0) {
+      int64_t m = sh.part_i64[0];
+      for (int w = 1; w < kAggBlockWarps; ++w) m = sh.part_i64[w] < m ? sh.part_i64[w] : m;
+      sh.res_i64 = m;
+    }
+    __syncthreads();
+    return sh.res_i64;
+  }
+
+  __device__ void add_help(int64_t v, uint32_t ag, int64_t &size) {
+    ++size;
+    if (tid == 0) {
+      D.agg[v] = ag;
+      block(ag)[blen(ag)++] = (int32_t)v;
+    }
+    const int64_t eb = D.rowptr[v], ee = D.rowptr[v + 1];
+    for (int64_t e = eb + tid; e < ee; e += kAggBlockThreads) {
+      const int64_t t = D.col[e];
+      if (t == v || !in_range(t)) continue;
+      const uint32_t ta = D.agg[t];
+      if (ta < kIsolated) {
+        if (atomicExch(&D.conn_flag32[pb + ta], 1) == 0) {
+          const int32_t pos = atomicAdd(&sh.conn_len, 1);
+          D.conn[pb + pos] = (int32_t)ta;
+        }
+      } else if (ta == kUnaggregated && D.front_pos[t] < 0) {
+        const int32_t pos = atomicAdd(&sh.front_len, 1);
+        D.front[pb + pos] = (int32_t)t;
+        D.front_pos[t] = pos;
+      }
+    }
+    __syncthreads();
+  }
+
+  __device__ void front_erase(int64_t v) {
+    if (tid == 0) {
+      const int32_t fl = sh.front_len;
+      const int32_t pos = D.front_pos[v];
+      if (pos >= 0) {
+        const int32_t last = D.front[pb + fl - 1];
+        D.front[pb + pos] = last;
+        D.front_pos[last] = pos;
+        D.front_pos[v] = -1;
+      }
+      sh.front_len = fl - 1;
+    }
+    __syncthreads();
+  }
+
+  __device__ void helpers_clear() {
+    const int32_t fl = sh.front_len, cl = sh.conn_len;
+    for (int64_t i = tid; i < fl; i += kAggBlockThreads) D.front_pos[D.front[pb + i]] = -1;
+    for (int64_t i = tid; i < cl; i += kAggBlockThreads) D.conn_flag32[pb + D.conn[pb + i]] = 0;
+    __syncthreads();
+    if (tid == 0) {
+      sh.front_len = 0;
+      sh.conn_len = 0;
+    }
+    __syncthreads();
+  }
+
+  template <class F>
+  __device__ __forceinline__ void edges(int64_t vtx, F &&f) const {
+    const int64_t eb = D.rowptr[vtx], ee = D.rowptr[vtx + 1];
+    for (int64_t e0 = eb; e0 < ee; e0 += 8) {
+      int64_t t[8];
+      bool ok[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int64_t e = e0 + u;
+        t[u] = e < ee ? (int64_t)D.col[e] : vtx;
+        ok[u] = e < ee && t[u] != vtx && in_range(t[u]);
+      }
+      uint32_t ha[8];
+      bool fr[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        ha[u] = ok[u] ? D.agg[t[u]] : kUnaggregated;
+        fr[u] = ok[u] && D.front_pos[t[u]] >= 0;
+      }
+      bool cf[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        cf[u] = ok[u] && ha[u] < kIsolated && D.conn_flag32[pb + ha[u]] != 0;
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (ok[u]) f(e0 + u, t[u], ha[u], fr[u], cf[u]);
+    }
+  }
+
+  // grow_aggregate (base.hpp:532-585), the warp kernel's steps block-wide
+  __device__ void grow(uint32_t ag, int64_t &size) {
+    while (size < D.min_size) {
+      const int32_t fl = sh.front_len;
+      int any2 = 0;
+      for (int64_t i = tid; i < fl; i += kAggBlockThreads) {
+        const int64_t vtx = D.front[pb + i];
+        int32_t *ev = D.eval + 4 * (pb + i);
+        if (D.iso[vtx]) {
+          ev[0] = ev[1] = 0;
+          ev[3] = 0;
+          continue;
+        }
+        int32_t con = 0, nbs = 0, c2 = 0, c1 = 0;
+        edges(vtx, [&](int64_t e, int64_t, uint32_t ha, bool in_front, bool connected) {
+          const bool dep = D.dep[e], inf = D.inf[e];
+          con += connected;
+          nbs += in_front;
+          c2 += (ha == ag) && (inf && dep);
+          c1 += (ha == ag) && (!inf && dep);
+        });
+        ev[0] = c2;
+        ev[1] = c1;
+        ev[2] = con;
+        ev[3] = nbs;
+        any2 |= c2 > 0;
+      }
+      const bool mode2 = __syncthreads_or(any2) != 0;
+      // maximum key among eligible vertices
+      int32_t k0 = 0, kn = 0;
+      double kc = 0.0;
+      bool have = false;
+      for (int64_t i = tid; i < fl; i += kAggBlockThreads) {
+        const int64_t vtx = D.front[pb + i];
+        if (D.iso[vtx]) continue;
+        const int32_t *ev = D.eval + 4 * (pb + i);
+        const int32_t c = mode2 ? ev[0] : ev[1];
+        if (c <= 0) continue;
+        const int64_t adj = (D.rowptr[vtx + 1] - D.rowptr[vtx]) - 1;
+        const double con = (double)ev[2] / (double)adj;
+        if (!have || c > k0 || (c == k0 && (con > kc || (con == kc && ev[3] > kn)))) {
+          k0 = c;
+          kc = con;
+          kn = ev[3];
+          have = true;
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const int32_t o0 = __shfl_xor_sync(kFull, k0, o);
+        const double oc = __shfl_xor_sync(kFull, kc, o);
+        const int32_t on = __shfl_xor_sync(kFull, kn, o);
+        const bool oh = __shfl_xor_sync(kFull, have, o);
+        if (oh && (!have || o0 > k0 || (o0 == k0 && (oc > kc || (oc == kc && on > kn))))) {
+          k0 = o0;
+          kc = oc;
+          kn = on;
+          have = true;
+        }
+      }
+      if (lane == 0) {
+        sh.part_k0[warp] = k0;
+        sh.part_kc[warp] = kc;
+        sh.part_kn[warp] = kn;
+        sh.part_have[warp] = have;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        bool h = false;
+        int32_t b0 = 0, bn = 0;
+        double bc = 0.0;
+        for (int w = 0; w < kAggBlockWarps; ++w) {
+          if (!sh.part_have[w]) continue;
+          const int32_t o0 = sh.part_k0[w], on = sh.part_kn[w];
+          const double oc = sh.part_kc[w];
+          if (!h || o0 > b0 || (o0 == b0 && (oc > bc || (oc == bc && on > bn)))) {
+            b0 = o0;
+            bc = oc;
+            bn = on;
+            h = true;
+          }
+        }
+        sh.res_have = h;
+        sh.res_k0 = b0;
+        sh.res_kc = bc;
+        sh.res_kn = bn;
+      }
+      __syncthreads();
+      if (!sh.res_have) break;  // no candidates (uniform)
+      k0 = sh.res_k0;
+      kc = sh.res_kc;
+      kn = sh.res_kn;
+      // mark the vertices whose key equals the maximum (eval[3] reused as mark)
+      for (int64_t i = tid; i < fl; i += kAggBlockThreads) {
+        const int64_t vtx = D.front[pb + i];
+        int32_t *ev = D.eval + 4 * (pb + i);
+        bool m = false;
+        if (!D.iso[vtx]) {
+          const int32_t c = mode2 ? ev[0] : ev[1];
+          if (c > 0) {
+            const int64_t adj = (D.rowptr[vtx + 1] - D.rowptr[vtx]) - 1;
+            const double con = (double)ev[2] / (double)adj;
+            m = c == k0 && con == kc && ev[3] == kn;
+          }
+        }
+        ev[3] = m;
+      }
+      __syncthreads();
+      // add the smallest `room` candidates in ascending order
+      const int64_t room = D.max_size - size;
+      int64_t floor = -1;
+      int64_t picked[64];
+      int64_t npick = 0;
+      for (int64_t k = 0; k < room; ++k) {
+        int64_t best = INT64_MAX;
+        for (int64_t i = tid; i < fl; i += kAggBlockThreads) {
+          if (!D.eval[4 * (pb + i) + 3]) continue;
+          const int64_t v = D.front[pb + i];
+          if (v > floor && v < best) best = v;
+        }
+        const int64_t v = block_min(best);
+        if (v == INT64_MAX) break;
+        picked[npick++] = v;
+        floor = v;
+      }
+      for (int64_t k = 0; k < npick; ++k) {
+        front_erase(picked[k]);
+        add_help(picked[k], ag, size);
+      }
+    }
+  }
+
+  // round_aggregate (base.hpp:601-636)
+  __device__ void round(uint32_t ag, int64_t &size) {
+    while (size < D.max_size) {
+      const int32_t fl = sh.front_len;
+      int64_t best = INT64_MAX;
+      for (int64_t i = tid; i < fl; i += kAggBlockThreads) {
+        const int64_t vtx = D.front[pb + i];
+        if (D.iso[vtx] || vtx >= best) continue;
+        int32_t cons = 0, unagg = 0, inagg = 0;
+        edges(vtx, [&](int64_t e, int64_t, uint32_t ha, bool, bool) {
+          cons += (ha == ag) && D.dep[e];
+          unagg += ha == kUnaggregated;
+          inagg += ha == ag;
+        });
+        if (cons == 0 || unagg >= inagg) continue;
+        best = vtx;
+      }
+      best = block_min(best);
+      if (best == INT64_MAX) break;
+      front_erase(best);
+      add_help(best, ag, size);
+    }
+  }
+
+  // handle_vertex (base.hpp:638-677)
+  __device__ void handle(int64_t seed) {
+    if (D.agg[seed] != kUnaggregated) return;  // published by the last barrier
+    if (D.iso[seed]) {
+      if (tid == 0) D.agg[seed] = kIsolated;
+      __syncthreads();
+      ++st[4];
+      return;
+    }
+    const uint32_t ag = (uint32_t)counter;
+    int64_t size = 0;
+    add_help(seed, ag, size);
+    grow(ag, size);
+    round(ag, size);
+    if (size == 1 && D.max_size > 1) {
+      // find_merge_aggregate (base.hpp:487-503): the first strong in-range
+      // edge (ascending column) whose head lies in an aggregate with room
+      const int64_t eb = D.rowptr[seed], ee = D.rowptr[seed + 1];
+      int64_t first = INT64_MAX;
+      for (int64_t e = eb + tid; e < ee; e += kAggBlockThreads) {
+        const int64_t t = D.col[e];
+        if (t != seed && in_range(t) && (D.dep[e] || D.inf[e])) {
+          const uint32_t ta = D.agg[t];
+          if (ta < kIsolated && blen(ta) < D.max_size && e < first) first = e;
+        }
+      }
+      first = block_min(first);
+      if (first != INT64_MAX) {
+        const uint32_t target = D.agg[D.col[first]];
+        __syncthreads();  // every thread has read the target before it is written
+        if (tid == 0) {
+          blen(ag) = 0;
+          D.agg[seed] = target;
+          block(target)[blen(target)++] = (int32_t)seed;
+        }
+        __syncthreads();
+        ++st[3];
+        helpers_clear();
+        return;
+      }
+      if (D.aggressive) {
+        __syncthreads();
+        if (tid == 0) {
+          blen(ag) = 0;
+          D.agg[seed] = kIsolated;
+        }
+        __syncthreads();
+        ++st[4];
+        helpers_clear();
+        return;
+      }
+      ++st[2];
+    } else {
+      ++st[1];
+    }
+    ++counter;
+    helpers_clear();
+  }
+};
+
+__global__ void __launch_bounds__(kAggBlockThreads) k_aggregate_block(AggDev D) {
+  __shared__ AggBlockShared sh;
+  const int64_t p = blockIdx.x;
+  if (p >= D.nparts) return;  // the whole block leaves together
+  const int64_t pb = part_begin(D.n, D.nparts, p), pe = part_begin(D.n, D.nparts, p + 1);
+  for (int64_t v = pb + threadIdx.x; v < pe; v += kAggBlockThreads) D.block_len[v] = 0;
+  if (threadIdx.x == 0) {
+    sh.front_len = 0;
+    sh.conn_len = 0;
+  }
+  __syncthreads();
+  AggBlock B(D, sh, pb, pe);
+  for (int64_t v = pb; v < pe; ++v) B.handle(v);
+  if (threadIdx.x == 0) {
+    D.pcount[p] = B.counter;
+    B.st[0] = B.counter;
+    for (int k = 0; k < 5; ++k)
+      if (B.st[k]) atomicAdd((unsigned long long *)&D.stats[k], (unsigned long long)B.st[k]);
+  }
+}
+
 __global__ void __launch_bounds__(32 * kAggWarpsPerBlock) k_aggregate(AggDev D) {
   const int64_t p = (int64_t)blockIdx.x * kAggWarpsPerBlock + (threadIdx.x >> 5);
   if (p >= D.nparts) return;  // whole warps leave together
@@ -579,20 +964,35 @@ __global__ void k_agg_lists(AggDev D, const int64_t *poff, int64_t nc, const int
   }
 }
 
+int sm_count();
+
+// One CTA per partition where the partitions are few (fewer than four per
+// SM), one warp per partition otherwise.  LGX_AGG_BLOCK=0 / 1 forces the
+// warp / block kernel (the tests run both against the oracle).
+static bool agg_block_kernel(int64_t nparts) {
+  const char *e = std::getenv("LGX_AGG_BLOCK");
+  if (e && e[0] == '0') return false;
+  if (e && e[0] == '1') return true;
+  return nparts < 4 * (int64_t)sm_count();
+}
+
 lgx_status aggregate(const Csr &a, const uint8_t *dep, const uint8_t *inf, const uint8_t *iso,
                      int32_t min_size, int32_t max_size, int64_t nparts, int aggressive,
                      cudaStream_t s, AggResult &out, uint32_t *agg_out = nullptr) {
   const int64_t n = a.n;
   if (nparts < 1) nparts = 1;
   if (nparts > n && n > 0) nparts = n;
-  if (max_size < 1 || min_size < 1) return fail(LGX_ERR_INVALID, "invalid aggregate sizes");
+  // the kernels keep up to max_size picks per growth step in a local array
+  if (max_size < 1 || min_size < 1 || max_size > 64 || min_size > max_size)
+    return fail(LGX_ERR_INVALID, "aggregate sizes must satisfy 1 <= min <= max <= 64");
   uint32_t *agg = agg_out;
   if (!agg) {
     LGX_CHECK(out.agg.alloc(n));
     agg = out.agg.p;
   }
-  DBuf<int32_t> front, front_pos, conn, blocks, blen, eval;
+  DBuf<int32_t> front, front_pos, conn, blocks, blen, eval, conn_flag32;
   DBuf<uint8_t> conn_flag;
+  const bool use_block = agg_block_kernel(nparts);
   DBuf<int64_t> pcount, poff, stats, glen;
   LGX_CHECK(front.alloc(n));
   LGX_CHECK(front_pos.alloc(n));
@@ -607,12 +1007,20 @@ lgx_status aggregate(const Csr &a, const uint8_t *dep, const uint8_t *inf, const
   LGX_CUDA(cudaMemsetAsync(agg, 0xFF, sizeof(uint32_t) * std::max<int64_t>(n, 1), s));
   LGX_CUDA(cudaMemsetAsync(front_pos.p, 0xFF, sizeof(int32_t) * std::max<int64_t>(n, 1), s));
   LGX_CUDA(cudaMemsetAsync(conn_flag.p, 0, std::max<int64_t>(n, 1), s));
+  if (use_block) {
+    LGX_CHECK(conn_flag32.alloc(n));
+    LGX_CUDA(cudaMemsetAsync(conn_flag32.p, 0, sizeof(int32_t) * std::max<int64_t>(n, 1), s));
+  }
   LGX_CUDA(cudaMemsetAsync(stats.p, 0, sizeof(int64_t) * 5, s));
   AggDev D{a.rowptr.p, a.col.p,     dep,     inf,         iso,      agg,    n,
            nparts,     min_size,    max_size, aggressive, front.p, front_pos.p, conn.p,
-           conn_flag.p, blocks.p,   blen.p,   eval.p,     pcount.p, stats.p};
+           conn_flag.p, blocks.p,   blen.p,   eval.p,     pcount.p, stats.p,
+           conn_flag32.p};
   if (n > 0) {
-    k_aggregate<<<grid_for(nparts, kAggWarpsPerBlock), 32 * kAggWarpsPerBlock, 0, s>>>(D);
+    if (use_block)
+      k_aggregate_block<<<(unsigned)nparts, kAggBlockThreads, 0, s>>>(D);
+    else
+      k_aggregate<<<grid_for(nparts, kAggWarpsPerBlock), 32 * kAggWarpsPerBlock, 0, s>>>(D);
     LGX_LAUNCH_CHECK();
   }
   LGX_CHECK(inclusive_offsets(nparts, pcount.p, poff.p, s));
@@ -839,9 +1247,9 @@ __global__ void k_gj_update(int64_t n, int64_t k, double *a, const double *prow,
 // ---- dense FP64 Cholesky of the coarsest matrix (CholeskySolver,
 // cholesky/decomposition.hpp:52-107, on the dense matrix): A = L L^T in the
 // lower triangle, right-looking, one column per step; every pivot must be
-// positive.  The inverse applied per V-cycle is then formed from the factor:
-// Y = L^-1 (forward substitution of the identity, all columns at once) and
-// A^-1 = Y^T Y.
+// positive.  The inverse applied per V-cycle is then formed from the factor
+// by two triangular solves with all n columns of the identity at once:
+// Y = L^-1 (forward substitution) and A^-1 = L^-T Y (backward substitution).
 __global__ void __launch_bounds__(256) k_chol_column(int64_t n, int64_t k, double *a, int *bad) {
   const double d = a[k * n + k];
   if (!(d > 0.0) || !isfinite(d)) {
@@ -877,14 +1285,16 @@ __global__ void k_chol_inv_row(int64_t n, int64_t i, const double *l, double *y)
   }
 }
 
-// A^-1 = Y^T Y: entry (i, j) = sum_{k >= max(i, j)} y_ki y_kj
-__global__ void k_chol_inv_gram(int64_t n, const double *y, double *inv) {
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * n;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = t / n, j = t % n;
-    double s = 0.0;
-    for (int64_t k = i > j ? i : j; k < n; ++k) s = fma(y[k * n + i], y[k * n + j], s);
-    inv[t] = s;
+// row i of X = A^-1 = L^-T Y (backward substitution, all columns at once,
+// rows i+1.. already done): x_ic = (y_ic - sum_{j>i} l_ji x_jc) / l_ii
+__global__ void k_chol_inv_back_row(int64_t n, int64_t i, const double *l, const double *y,
+                                    double *x) {
+  const double lii = l[i * n + i];
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    double s = c <= i ? y[i * n + c] : 0.0;
+    for (int64_t j = i + 1; j < n; ++j) s = fma(-l[j * n + i], x[j * n + c], s);
+    x[i * n + c] = s / lii;
   }
 }
 
@@ -946,8 +1356,9 @@ lgx_status dense_inverse(const Csr &a, cudaStream_t s, DBuf<double> &inv, int sp
       k_chol_inv_row<<<(unsigned)std::min<int64_t>(grid_for(i + 1, 128), 1024), 128, 0, s>>>(
         n, i, l.p, y.p);
     LGX_LAUNCH_CHECK();
-    k_chol_inv_gram<<<(unsigned)std::min<int64_t>(grid_for(n * n, 256), 8192), 256, 0, s>>>(
-      n, y.p, inv.p);
+    for (int64_t i = n - 1; i >= 0; --i)
+      k_chol_inv_back_row<<<(unsigned)std::min<int64_t>(grid_for(n, 128), 1024), 128, 0, s>>>(
+        n, i, l.p, y.p, inv.p);
     LGX_LAUNCH_CHECK();
     LGX_CUDA(cudaStreamSynchronize(s));
     return LGX_OK;
@@ -1148,6 +1559,9 @@ static lgx_status upload_map(const lgx_agg_map &m, int64_t level, int64_t n, cud
 
 // a level's smallest-last colouring: its pattern to the host,
 // lgx_colour_smallest_last there, the colours back to the device
+lgx_status colour_smallest_last(int64_t n, const int64_t *rowptr, const int32_t *col,
+                                int32_t *colour, int32_t *ncolours, bool known_symmetric);
+
 static lgx_status colouring_smallest_last(const Csr &a, cudaStream_t s, DBuf<int32_t> &colour,
                                           int32_t &ncolours) {
   const int64_t n = a.n;
@@ -1160,7 +1574,8 @@ static lgx_status colouring_smallest_last(const Csr &a, cudaStream_t s, DBuf<int
     LGX_CUDA(cudaMemcpyAsync(col.data(), a.col.p, sizeof(int32_t) * (size_t)a.nnz,
                              cudaMemcpyDeviceToHost, s));
   LGX_CUDA(cudaStreamSynchronize(s));
-  LGX_CHECK(lgx_colour_smallest_last(n, rowptr.data(), col.data(), h_colour.data(), &ncolours));
+  LGX_CHECK(colour_smallest_last(n, rowptr.data(), col.data(), h_colour.data(), &ncolours,
+                                 a.symmetric != 0));
   LGX_CHECK(colour.alloc(n));
   if (n > 0)
     LGX_CUDA(cudaMemcpyAsync(colour.p, h_colour.data(), sizeof(int32_t) * (size_t)n,

@@ -698,6 +698,45 @@ __global__ void k_fxpby(int64_t n, const KScalars *ks, const float *__restrict__
     p[i] = fmaf(p[i], beta, z[i]);
 }
 
+// flexible CG on float vectors: t1 = r.z, t2 = r.z_old (FP64 sums), then
+// rho_old = rho, rho = t1, beta = (t1 - t2) / rho_old (Notay 2000)
+__global__ void __launch_bounds__(kKT)
+  k_fdot2_fcg(int64_t n, const float *__restrict__ r, const float *__restrict__ z,
+              const float *__restrict__ zold, KScalars *ks, double *partials, double *partials2,
+              unsigned *counter, unsigned *counter2) {
+  double s1 = 0.0, s2 = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double ri = (double)r[i];
+    s1 = fma(ri, (double)z[i], s1);
+    s2 = fma(ri, (double)zold[i], s2);
+  }
+  double t1, t2;
+  const bool l1 = grid_reduce<kKT>(s1, blockIdx.x, gridDim.x, partials, counter, &t1);
+  if (l1 && threadIdx.x == 0) ks->tmp = t1;
+  const bool l2 = grid_reduce<kKT>(s2, blockIdx.x, gridDim.x, partials2, counter2, &t2);
+  if (l2 && threadIdx.x == 0) {
+    __threadfence();
+    const double u1 = ((volatile KScalars *)ks)->tmp;
+    ks->rho_old = ks->rho;
+    ks->rho = u1;
+    set_flags(ks, u1, ks->rho_old);
+    ks->beta = (u1 - t2) / ks->rho_old;
+  }
+}
+
+// p = z + beta p and z_old = z (float, flexible CG)
+__global__ void k_fxpby_save(int64_t n, const KScalars *ks, const float *__restrict__ z,
+                             float *__restrict__ p, float *__restrict__ zold) {
+  const float beta = (float)ks->beta;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float zi = z[i];
+    p[i] = fmaf(p[i], beta, zi);
+    zold[i] = zi;
+  }
+}
+
 // rf = float(r * inv_scale), d = 0
 __global__ void k_refine_start(int64_t n, const double *__restrict__ r, double inv_scale,
                                float *__restrict__ rf, float *__restrict__ d) {
@@ -720,18 +759,23 @@ struct Refiner {
   Solver S;
   std::unique_ptr<lgx_colouring> own_col;
   DBuf<double> b, x, r;
-  DBuf<float> rf, df, pf, qf, zf;
+  DBuf<float> rf, df, pf, qf, zf, zold;
   const float *v32 = nullptr;
+  bool flexible = false;  // flexible beta (Notay 2000) for the float V-cycle
   cudaStream_t user_stream = nullptr, capture_stream = nullptr;
-  cudaGraphExec_t graph = nullptr;
-  uint64_t graph_kernels = 0;
+  // graphs of the two halves of an inner iteration: [0] product and update,
+  // [1] preconditioner and new direction
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  uint64_t graph_kernels[2] = {0, 0};
   ~Refiner() {
-    if (graph) cudaGraphExecDestroy(graph);
+    for (auto &g : graph)
+      if (g) cudaGraphExecDestroy(g);
     if (capture_stream) cudaStreamDestroy(capture_stream);
   }
 
-  // one inner CG iteration on the float vectors
-  lgx_status inner_body() {
+  // first half of a CG iteration on the float vectors: q = A p,
+  // alpha = rho / p.q, d += alpha p, r -= alpha q, ||r||^2
+  lgx_status half_update() {
     const int64_t n = S.n;
     cudaStream_t s = S.s;
     KScalars *ks = S.ks.p;
@@ -741,7 +785,23 @@ struct Refiner {
     LGX_LAUNCH_CHECK();
     k_fcg_update<<<rg, kKT, 0, s>>>(n, ks, pf.p, qf.p, df.p, rf.p, S.partials.p, S.counters.p);
     LGX_LAUNCH_CHECK();
+    return LGX_OK;
+  }
+  // second half: z = M r, rho = r.z, beta, p = z + beta p
+  lgx_status half_direction() {
+    const int64_t n = S.n;
+    cudaStream_t s = S.s;
+    KScalars *ks = S.ks.p;
+    const unsigned rg = (unsigned)reduce_blocks(n);
     LGX_CHECK(amg_apply_permuted_f32(*S.amg, rf.p, zf.p, s));
+    if (flexible) {
+      k_fdot2_fcg<<<rg, kKT, 0, s>>>(n, rf.p, zf.p, zold.p, ks, S.partials.p, S.partials2.p,
+                                     S.counters.p, S.counters.p + 1);
+      LGX_LAUNCH_CHECK();
+      k_fxpby_save<<<S.vgrid(), 256, 0, s>>>(n, ks, zf.p, pf.p, zold.p);
+      LGX_LAUNCH_CHECK();
+      return LGX_OK;
+    }
     k_fdot_post<<<rg, kKT, 0, s>>>(n, rf.p, zf.p, POST_RHO_BETA, ks, S.partials.p,
                                    S.counters.p);
     LGX_LAUNCH_CHECK();
@@ -749,17 +809,18 @@ struct Refiner {
     LGX_LAUNCH_CHECK();
     return LGX_OK;
   }
+  lgx_status half(int which) { return which == 0 ? half_update() : half_direction(); }
 
-  lgx_status capture() {
+  lgx_status capture(int which) {
     if (!capture_stream)
       LGX_CUDA(cudaStreamCreateWithFlags(&capture_stream, cudaStreamNonBlocking));
     S.s = capture_stream;
     cudaGraph_t g = nullptr;
     const uint64_t before = launch_count();
     cudaError_t e = cudaStreamBeginCapture(capture_stream, cudaStreamCaptureModeThreadLocal);
-    lgx_status st = e == cudaSuccess ? inner_body() : cuda_fail(e, "cudaStreamBeginCapture");
-    graph_kernels = launch_count() - before;
-    count_launches(0 - graph_kernels);
+    lgx_status st = e == cudaSuccess ? half(which) : cuda_fail(e, "cudaStreamBeginCapture");
+    graph_kernels[which] = launch_count() - before;
+    count_launches(0 - graph_kernels[which]);
     cudaError_t e2 = cudaStreamEndCapture(capture_stream, &g);
     S.s = user_stream;
     if (st != LGX_OK) {
@@ -767,20 +828,23 @@ struct Refiner {
       return st;
     }
     if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
-    e = cudaGraphInstantiate(&graph, g, 0);
+    e = cudaGraphInstantiate(&graph[which], g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
     return LGX_OK;
   }
 
-  lgx_status inner_iterate(bool use_graphs, bool first) {
+  // one half, eagerly the first time (it also sets per-kernel attributes),
+  // then replayed from its graph
+  lgx_status run_half(int which, bool use_graphs, bool &first) {
     if (use_graphs && !first) {
-      if (!graph) LGX_CHECK(capture());
-      LGX_CUDA(cudaGraphLaunch(graph, user_stream));
-      count_launches(graph_kernels);
+      if (!graph[which]) LGX_CHECK(capture(which));
+      LGX_CUDA(cudaGraphLaunch(graph[which], user_stream));
+      count_launches(graph_kernels[which]);
       return LGX_OK;
     }
-    return inner_body();
+    if (which == 1) first = false;
+    return half(which);
   }
 };
 
@@ -836,8 +900,8 @@ static lgx_status run_refined(const lgx_matrix *a, const double *d_b, double *d_
     LGX_CHECK(check_flags(h, it));
     double inner = 1.0;
     while (it < p->maxit && inner > tol && h.rho != 0.0) {
-      st = R.inner_iterate(p->use_graphs != 0, first);
-      first = false;
+      st = R.run_half(0, p->use_graphs != 0, first);
+      if (st == LGX_OK) st = R.run_half(1, p->use_graphs != 0, first);
       if (st != LGX_OK) break;
       ++it;
       LGX_CHECK(S.read(h));
@@ -862,6 +926,119 @@ static lgx_status run_refined(const lgx_matrix *a, const double *d_b, double *d_
     // precision reached on an operator the float cycle cannot resolve) ends
     // the refinement
     if (res >= prev) break;
+  }
+  LGX_CHECK(scatter<double, double>(n, S.perm, R.x.p, d_x, s));
+  LGX_CUDA(cudaStreamSynchronize(s));
+  if (iterations) *iterations = it;
+  if (final_rel) *final_rel = r0 > 0 ? res / r0 : 0.0;
+  return st;
+}
+
+// Reliable updates (refine == 2; H. A. van der Vorst, Q. Ye, "Residual
+// replacement strategies for Krylov subspace iterative methods for the
+// convergence of true residuals", SIAM J. Sci. Comput. 22 (2000), in the
+// mixed-precision form of M. A. Clark et al., "Solving lattice QCD systems of
+// equations using mixed precision solvers on GPUs", Comput. Phys. Commun. 181
+// (2010)): one CG recurrence on float vectors, never restarted.  The float
+// iterate d accumulates updates to the FP64 solution x; whenever the
+// recursive residual has fallen by reliable_delta since the last FP64
+// residual (and when it reaches the tolerance), x += d, d = 0 and r is
+// replaced by the FP64 residual b - A x before the next preconditioner
+// application.  The search direction is kept, so the iteration count stays
+// the FP64 recurrence's while the products, V-cycles and vector updates run
+// in float; the solve stops on the FP64 residual.
+static lgx_status run_reliable(const lgx_matrix *a, const double *d_b, double *d_x,
+                               const lgx_solve_params *p, cudaStream_t s, int64_t *iterations,
+                               double *final_rel, double *history) {
+  if (p->precon != LGX_PRECON_AMG || !p->amg)
+    return fail(LGX_ERR_UNSUPPORTED, "refinement needs the AMG preconditioner");
+  if (!amg_cycle_f32(*p->amg))
+    return fail(LGX_ERR_UNSUPPORTED, "refinement needs a float-cycle hierarchy (cycle_f32)");
+  if (!(p->inner_rtol > 0.0 && p->inner_rtol < 1.0))
+    return fail(LGX_ERR_INVALID, "inner_rtol must lie in (0, 1)");
+  Refiner R;
+  R.user_stream = s;
+  LGX_CHECK(setup_solver(a, p, s, R.S, R.own_col));
+  Solver &S = R.S;
+  if (!S.pcsr) return fail(LGX_ERR_UNSUPPORTED, "refinement needs a CSR finest level");
+  const int64_t n = S.n;
+  R.v32 = amg_finest_values_f32(*S.amg);
+  LGX_CHECK(R.b.alloc(n));
+  LGX_CHECK(R.x.alloc(n));
+  LGX_CHECK(R.r.alloc(n));
+  LGX_CHECK(R.rf.alloc(n));
+  LGX_CHECK(R.df.alloc(n));
+  LGX_CHECK(R.pf.alloc(n));
+  LGX_CHECK(R.qf.alloc(n));
+  LGX_CHECK(R.zf.alloc(n));
+  R.flexible = p->flexible != 0;
+  if (R.flexible) LGX_CHECK(R.zold.alloc(n));
+  LGX_CHECK(gather<double, double>(n, S.perm, d_b, R.b.p, s));
+  LGX_CHECK(gather<double, double>(n, S.perm, d_x, R.x.p, s));
+  KScalars *ks = S.ks.p;
+  KScalars h{};
+  const unsigned rg = (unsigned)reduce_blocks(n);
+  LGX_CHECK(S.residual(R.b.p, R.x.p, R.r.p, &ks->res2));
+  LGX_CHECK(S.read(h));
+  if (!std::isfinite(h.res2)) return fail(LGX_ERR_NONFINITE, "non-finite initial residual");
+  const double r0 = std::sqrt(h.res2);
+  double res = r0, last = r0;
+  if (history) history[0] = r0;
+  int64_t it = 0;
+  lgx_status st = LGX_OK;
+  if (r0 > 0.0 && p->maxit > 0) {
+    // r = float(b - A x), d = 0, z = M r, rho = r.z, p = z
+    k_refine_start<<<S.vgrid(), 256, 0, s>>>(n, R.r.p, 1.0, R.rf.p, R.df.p);
+    LGX_LAUNCH_CHECK();
+    LGX_CHECK(amg_apply_permuted_f32(*S.amg, R.rf.p, R.zf.p, s));
+    k_fdot_post<<<rg, kKT, 0, s>>>(n, R.rf.p, R.zf.p, POST_RHO, ks, S.partials.p, S.counters.p);
+    LGX_LAUNCH_CHECK();
+    LGX_CUDA(cudaMemcpyAsync(R.pf.p, R.zf.p, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+    if (R.flexible)
+      LGX_CUDA(cudaMemcpyAsync(R.zold.p, R.zf.p, sizeof(float) * n, cudaMemcpyDeviceToDevice,
+                               s));
+    LGX_CHECK(S.read(h));
+    LGX_CHECK(check_flags(h, 0));
+  }
+  bool first = true, pending = false;
+  const bool graphs = p->use_graphs != 0;
+  while (st == LGX_OK && it < p->maxit && res > p->rtol * r0 && h.rho != 0.0) {
+    st = R.run_half(0, graphs, first);
+    if (st != LGX_OK) break;
+    ++it;
+    pending = true;
+    LGX_CHECK(S.read(h));
+    st = check_flags(h, it);
+    if (st != LGX_OK) break;
+    const double est = std::sqrt(h.res2);
+    if (history) history[it] = est;
+    if (est <= p->inner_rtol * last || est <= p->rtol * r0 || it == p->maxit) {
+      // reliable update: fold d into x and replace r by the FP64 residual
+      k_refine_add<<<S.vgrid(), 256, 0, s>>>(n, R.df.p, 1.0, R.x.p);
+      LGX_LAUNCH_CHECK();
+      LGX_CHECK(S.residual(R.b.p, R.x.p, R.r.p, &ks->res2));
+      k_refine_start<<<S.vgrid(), 256, 0, s>>>(n, R.r.p, 1.0, R.rf.p, R.df.p);
+      LGX_LAUNCH_CHECK();
+      LGX_CHECK(S.read(h));
+      if (!std::isfinite(h.res2)) {
+        st = fail(LGX_ERR_NONFINITE, "non-finite residual at a reliable update");
+        break;
+      }
+      res = last = std::sqrt(h.res2);
+      pending = false;
+      if (history) history[it] = res;
+      if (res <= p->rtol * r0 || it == p->maxit) break;
+    }
+    st = R.run_half(1, graphs, first);
+  }
+  if (st == LGX_OK && pending) {
+    // a breakdown (rho = 0) ended the recurrence between updates
+    k_refine_add<<<S.vgrid(), 256, 0, s>>>(n, R.df.p, 1.0, R.x.p);
+    LGX_LAUNCH_CHECK();
+    LGX_CHECK(S.residual(R.b.p, R.x.p, R.r.p, &ks->res2));
+    LGX_CHECK(S.read(h));
+    res = std::sqrt(h.res2);
+    if (history) history[it] = res;
   }
   LGX_CHECK(scatter<double, double>(n, S.perm, R.x.p, d_x, s));
   LGX_CUDA(cudaStreamSynchronize(s));
@@ -896,8 +1073,13 @@ lgx_status lgx_pcg(const lgx_matrix *a, const double *d_b, double *d_x,
                    const lgx_solve_params *p, lgx_stream stream, int64_t *iterations,
                    double *final_rel_residual, double *h_history) {
   if (!a || !p || (a->n > 0 && (!d_b || !d_x))) return fail(LGX_ERR_INVALID, "null argument");
-  if (p->refine)
+  if (p->refine == 2)
+    return run_reliable(a, d_b, d_x, p, stream, iterations, final_rel_residual, h_history);
+  if (p->refine == 1)
     return run_refined(a, d_b, d_x, p, stream, iterations, final_rel_residual, h_history);
+  if (p->refine)
+    return fail(LGX_ERR_INVALID, "refine must be 0, 1 (restarted inner solves) or 2 (reliable "
+                                 "updates)");
   return run_solve(LGX_KRYLOV_CG, a, d_b, d_x, p, stream, iterations, final_rel_residual,
                    h_history);
 }

@@ -697,8 +697,23 @@ static bool symmetrised_pattern(int64_t n, const int64_t *rowptr, const int32_t 
   return true;
 }
 
-lgx_status lgx_colour_smallest_last(int64_t n, const int64_t *rowptr, const int32_t *col,
-                                    int32_t *colour, int32_t *ncolours) {
+}  // extern "C"
+
+namespace lgx {
+lgx_status colour_smallest_last(int64_t n, const int64_t *rowptr, const int32_t *col,
+                                int32_t *colour, int32_t *ncolours, bool known_symmetric);
+}  // namespace lgx
+
+extern "C" lgx_status lgx_colour_smallest_last(int64_t n, const int64_t *rowptr,
+                                               const int32_t *col, int32_t *colour,
+                                               int32_t *ncolours) {
+  return lgx::colour_smallest_last(n, rowptr, col, colour, ncolours, false);
+}
+
+// known_symmetric: the caller's matrix is symmetric (the AMG levels of a
+// symmetric matrix), so its pattern needs no symmetrisation check
+lgx_status lgx::colour_smallest_last(int64_t n, const int64_t *rowptr, const int32_t *col,
+                                     int32_t *colour, int32_t *ncolours, bool known_symmetric) {
   if (n < 0 || n > INT32_MAX || (n > 0 && (!rowptr || !col || !colour)) || !ncolours)
     return fail(LGX_ERR_INVALID, "bad argument");
   *ncolours = 0;
@@ -710,7 +725,7 @@ lgx_status lgx_colour_smallest_last(int64_t n, const int64_t *rowptr, const int3
     if (col[e] < 0 || col[e] >= n) return fail(LGX_ERR_INVALID, "column index out of range");
   std::vector<int64_t> sptr;
   std::vector<int32_t> scol;
-  if (symmetrised_pattern(n, rowptr, col, sptr, scol)) {
+  if (!known_symmetric && symmetrised_pattern(n, rowptr, col, sptr, scol)) {
     rowptr = sptr.data();
     col = scol.data();
   }
@@ -773,6 +788,8 @@ lgx_status lgx_colour_smallest_last(int64_t n, const int64_t *rowptr, const int3
   return LGX_OK;
 }
 
+extern "C" {
+
 lgx_status lgx_colouring_create(const lgx_matrix *a, const int32_t *d_colour, int32_t ncolours,
                                 lgx_stream stream, lgx_colouring **out) {
   if (!a || !out || (a->n > 0 && !d_colour)) return fail(LGX_ERR_INVALID, "null argument");
@@ -804,6 +821,19 @@ lgx_status lgx_colouring_grid27(lgx_colouring *c, const int64_t dims[3], int wit
 }  // extern "C"
 
 namespace lgx {
+// The failure path of the kernels' bounded waits, exercised on purpose: one
+// thread initialises an mbarrier that expects one arrival, issues nothing,
+// and waits on it with the same bounded wait the row engine uses (about
+// one second of SM clock); the wait gives up, the kernel records it in the
+// device error flag and returns.  No copy is ever in flight.
+__global__ void k_wait_selftest(int *err) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x != 0) return;
+  mbar_init(&bar, 1);
+  fence_mbar_init();
+  if (!mbar_wait_bounded(&bar, 0)) atomicOr(err, 1);
+}
+
 __global__ void k_red_black_colour(int64_t n, int64_t n1, int64_t n2, int32_t *colour) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
@@ -812,6 +842,14 @@ __global__ void k_red_black_colour(int64_t n, int64_t n1, int64_t n2, int32_t *c
 }  // namespace lgx
 
 extern "C" {
+
+lgx_status lgx_wait_selftest(lgx_stream stream) {
+  int *err = device_error_flag();
+  if (!err) return fail(LGX_ERR_NOMEM, "device error flag not allocated");
+  k_wait_selftest<<<1, 32, 0, stream>>>(err);
+  LGX_LAUNCH_CHECK();
+  return check_device_error(stream);
+}
 
 lgx_status lgx_colouring_create_red_black(const lgx_matrix *a, lgx_stream stream,
                                           lgx_colouring **out) {

@@ -39,9 +39,16 @@ def test_strength_bitexact(cuda, golden_dir, which):
     np.testing.assert_array_equal(iso.cpu().numpy(), riso)
 
 
+@pytest.fixture(params=["warp", "block"])
+def agg_kernel(request, monkeypatch):
+    """Both aggregation kernels: one warp per partition, one CTA per partition."""
+    monkeypatch.setenv("LGX_AGG_BLOCK", "1" if request.param == "block" else "0")
+    return request.param
+
+
 @pytest.mark.parametrize("nparts", [1, 7, 64])
 @pytest.mark.parametrize("aggressive", [False, True])
-def test_aggregation_bitexact(cuda, nparts, aggressive):
+def test_aggregation_bitexact(cuda, nparts, aggressive, agg_kernel):
     ref = _case()
     m = _dev(cuda, ref)
     dep, inf, iso = cuda.amg_strength(m)
@@ -52,7 +59,25 @@ def test_aggregation_bitexact(cuda, nparts, aggressive):
     np.testing.assert_array_equal(agg, ragg)
 
 
-def test_aggregation_ufz_bitexact(cuda, golden_dir):
+@pytest.mark.parametrize("dims,npts,nparts", [((30, 28, 26), 27, 3), ((40, 36, 30), 7, 5)])
+def test_aggregation_coarse_level_bitexact(cuda, agg_kernel, dims, npts, nparts):
+    """A coarse level (the Galerkin product of the first aggregation: dense,
+    irregular rows) split into few large partitions, the case the CTA
+    kernel serves; plain and aggressive thresholds."""
+    ref = _case(dims, npts=npts)
+    oh = lo.Amg(ref, min_coarsen_size=100, partition_size=4096, smoother_parts=0)
+    c = oh.level_csr(1)
+    m = _dev(cuda, c)
+    for aggressive in (False, True):
+        dep, inf, iso = cuda.amg_strength(m)
+        nc, agg = cuda.amg_aggregate(m, dep, inf, iso, 6, 9, nparts, aggressive)
+        rdep, rinf, riso = lo.amg_strength(c)
+        rnc, ragg, _, _, _ = lo.amg_aggregate(c, rdep, rinf, riso, 6, 9, nparts, aggressive)
+        assert nc == rnc
+        np.testing.assert_array_equal(agg, ragg)
+
+
+def test_aggregation_ufz_bitexact(cuda, golden_dir, agg_kernel):
     ref = _ufz(golden_dir)
     m = _dev(cuda, ref)
     dep, inf, iso = cuda.amg_strength(m)
@@ -67,7 +92,7 @@ PARAMS = dict(min_coarsen_size=64, partition_size=512, max_partitions=1 << 30)
 
 
 @pytest.mark.parametrize("coarse_f32", [False, True])
-def test_hierarchy_bitexact(cuda, coarse_f32):
+def test_hierarchy_bitexact(cuda, coarse_f32, agg_kernel):
     ref = _case()
     m = _dev(cuda, ref)
     h = cuda.HierarchyWright(coarse_f32=coarse_f32, **PARAMS).instantiate(m)

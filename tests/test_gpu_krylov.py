@@ -179,14 +179,17 @@ def test_precision_form_five_levels_matches_oracle(cuda):
     plain = cuda.pcg(m, b, precon=cuda.PRECON_AMG, amg=h64, rtol=1e-10, maxit=600)
     assert abs(plain.iterations - it) <= max(1, int(0.05 * it + 0.999))
     np.testing.assert_allclose(plain.history[:5], hist[:5], rtol=1e-9)
-    for res in (plain,
-                cuda.pcg(m, b, precon=cuda.PRECON_AMG, amg=h32, rtol=1e-10, maxit=600,
-                         flexible=True),
-                cuda.pcg(m, b, precon=cuda.PRECON_AMG, amg=h32, rtol=1e-10, maxit=600,
-                         refine=True)):
+    # (solve, iteration slack): restarted refinement pays for its restarts
+    for res, slack in ((plain, 2),
+                       (cuda.pcg(m, b, precon=cuda.PRECON_AMG, amg=h32, rtol=1e-10, maxit=600,
+                                 flexible=True), max(5, (15 * it) // 100)),
+                       (cuda.pcg(m, b, precon=cuda.PRECON_AMG, amg=h32, rtol=1e-10, maxit=600,
+                                 refine=2), max(5, (15 * it) // 100)),
+                       (cuda.pcg(m, b, precon=cuda.PRECON_AMG, amg=h32, rtol=1e-10, maxit=600,
+                                 refine=1), max(8, (30 * it) // 100))):
         xr = res.x.cpu().numpy()
         assert np.linalg.norm(b - lo.spmv(ref, xr)) <= 1.2e-10 * np.linalg.norm(b)
-        assert res.iterations <= it + max(5, (15 * it) // 100)
+        assert res.iterations <= it + slack
         assert np.linalg.norm(xr - xo) <= 1e-6 * np.linalg.norm(xo)
 
 

@@ -66,7 +66,7 @@ def test_refusals(cuda):
     a = _tridiagonal(8, -1.0, 0.5, -1.0)
     assert np.linalg.norm(1.0 - lo.spmv(a, x)) <= 1e-12 * np.sqrt(8)
     zero_pivot = _dev(cuda, _tridiagonal(6, 1.0, 0.0, 1.0), False)
-    with pytest.raises(cuda.LinealError, match="zero or non-finite pivot"):
+    with pytest.raises(cuda.LinealError, match="zero, non-finite or tiny pivot"):
         cuda.DirectSolver(zero_pivot, lu=True)
     big = cuda.gen_7pt((32, 32, 9), np.ones(32 * 32 * 9))
     with pytest.raises(cuda.LinealError, match="at most"):
