@@ -369,14 +369,16 @@ def precision_form(g, args, stream):
             h.autotune(reps=3)
         for _ in range(args.warmup):
             res = g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=1e-10, maxit=1000,
-                        flexible=flexible, refine=refine, inner_rtol=args.inner_rtol)
+                        flexible=flexible, refine=refine,
+                        inner_rtol=args.precision_inner_rtol)
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(args.steps):
             res = g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=1e-10, maxit=1000,
-                        flexible=flexible, refine=refine, inner_rtol=args.inner_rtol)
+                        flexible=flexible, refine=refine,
+                        inner_rtol=args.precision_inner_rtol)
         e1.record(stream)
         e1.synchronize()
         _, rn = g.residual(a, b, res.x)
@@ -387,6 +389,11 @@ def precision_form(g, args, stream):
         log(f"[precision] {tag}: {out[tag]['ms']:.1f} ms, {res.iterations} it, "
             f"rel {out[tag]['rel_residual_fp64']:.2e}")
         del h
+    out["mixed_refined"]["what"] = (
+        f"float-vector CG (refine {args.refine}, flexible beta) with FP64 residual "
+        f"replacement every {args.precision_inner_rtol:g} reduction; float products and "
+        "V-cycle, FP64 dots and CG scalars")
+    out["mixed_fcg"]["what"] = "flexible CG with FP64 vectors over the float V-cycle"
     for tag in ("mixed_fcg", "mixed_refined", "mixed_bf16_fcg"):
         out[tag]["rel_error_vs_fp64_solution"] = float(
             torch.linalg.norm(xs[tag] - xs["fp64"]).item() / torch.linalg.norm(xs["fp64"]).item())
@@ -1258,12 +1265,17 @@ def main():
                     help="mixed_refined of the 27-point workload: flexible beta")
     ap.add_argument("--inner-rtol", type=float, default=1e-4,
                     help="mixed_refined: inner tolerance / reduction between FP64 residuals")
+    ap.add_argument("--precision-inner-rtol", type=float, default=1e-2,
+                    help="precision form's mixed_refined: reduction between FP64 residuals")
     ap.add_argument("--no-configs", dest="configs", action="store_false",
                     help="skip the 64^3 Jacobi-PCG, batch, 32-RHS and adjoint keys")
     ap.add_argument("--bench-fd-directions", type=int, default=16,
                     help="finite-difference directions of the default line's adjoint key")
-    ap.add_argument("--coarse-smallest-last", action="store_true",
-                    help="colour AMG levels >= 1 by the host smallest-last colouring")
+    ap.add_argument("--no-coarse-smallest-last", dest="coarse_smallest_last",
+                    action="store_false",
+                    help="resident solves: Jones-Plassmann colourings on AMG levels >= 1 "
+                         "instead of the host smallest-last colouring (fewer colours, "
+                         "setup-time host work; the e2e solve always uses Jones-Plassmann)")
     args = ap.parse_args()
     if args.grid is None:
         # the differentiation and multi-right-hand-side configurations are 128^3

@@ -964,16 +964,17 @@ __global__ void k_agg_lists(AggDev D, const int64_t *poff, int64_t nc, const int
   }
 }
 
-int sm_count();
-
-// One CTA per partition where the partitions are few (fewer than four per
-// SM), one warp per partition otherwise.  LGX_AGG_BLOCK=0 / 1 forces the
-// warp / block kernel (the tests run both against the oracle).
+// One CTA per partition where the partitions are few (at most 64), one warp
+// per partition otherwise.  Measured at 256^3 (levels 1-4: 175, 17, 8, 8
+// partitions): warp 154 / 744 / 288 / 45 ms, block 159 / 690 / 272 / 44 ms
+// -- the sequential chain of dependent steps per aggregate, not the front
+// evaluation, bounds both.  LGX_AGG_BLOCK=0 / 1 forces the warp / block
+// kernel (the tests run both against the oracle).
 static bool agg_block_kernel(int64_t nparts) {
   const char *e = std::getenv("LGX_AGG_BLOCK");
   if (e && e[0] == '0') return false;
   if (e && e[0] == '1') return true;
-  return nparts < 4 * (int64_t)sm_count();
+  return nparts <= 64;
 }
 
 lgx_status aggregate(const Csr &a, const uint8_t *dep, const uint8_t *inf, const uint8_t *iso,
@@ -1249,7 +1250,7 @@ __global__ void k_gj_update(int64_t n, int64_t k, double *a, const double *prow,
 // lower triangle, right-looking, one column per step; every pivot must be
 // positive.  The inverse applied per V-cycle is then formed from the factor
 // by two triangular solves with all n columns of the identity at once:
-// Y = L^-1 (forward substitution) and A^-1 = L^-T Y (backward substitution).
+// L^-1 (forward substitution), then A^-1 = L^-T L^-1 (backward).
 __global__ void __launch_bounds__(256) k_chol_column(int64_t n, int64_t k, double *a, int *bad) {
   const double d = a[k * n + k];
   if (!(d > 0.0) || !isfinite(d)) {
@@ -1273,29 +1274,38 @@ __global__ void k_chol_update(int64_t n, int64_t k, double *a, const int *bad) {
   }
 }
 
-// row i of Y = L^-1 (lower triangular): y_ic = (delta_ic - sum_{c<=j<i} l_ij
-// y_jc) / l_ii for every column c <= i
-__global__ void k_chol_inv_row(int64_t n, int64_t i, const double *l, double *y) {
-  const double lii = l[i * n + i];
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c <= i;
-       c += (int64_t)gridDim.x * blockDim.x) {
-    double s = c == i ? 1.0 : 0.0;
-    for (int64_t j = c; j < i; ++j) s = fma(-l[i * n + j], y[j * n + c], s);
-    y[i * n + c] = s / lii;
+// The two triangular solves with all n columns of the identity, column by
+// column of L so that every step is one parallel rank-one update (a row of
+// dependent sums per thread would be a chain of n loads):
+//  forward,  X = L^-1: step k scales row k by 1 / l_kk, then row i > k
+//            subtracts l_ik times row k;
+//  backward, X = L^-T X: step k (from n - 1 down) scales row k by 1 / l_kk,
+//            then row i < k subtracts l_ki times row k.
+// Each scaling is its own launch so the update reads the finished row.
+__global__ void k_tri_scale(int64_t n, int64_t k, const double *l, double *x) {
+  const double d = l[k * n + k];
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x)
+    x[k * n + c] = x[k * n + c] / d;
+}
+
+// rows [r0, r1) of x: x_ic -= f(i) x_kc with f(i) = l_ik (forward) or l_ki
+// (transposed, backward)
+__global__ void k_tri_update(int64_t n, int64_t k, int64_t r0, int64_t r1, int transposed,
+                             const double *l, double *x) {
+  const int64_t rows = r1 - r0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < rows * n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = r0 + t / n, c = t % n;
+    const double f = transposed ? l[k * n + i] : l[i * n + k];
+    x[i * n + c] = fma(-f, x[k * n + c], x[i * n + c]);
   }
 }
 
-// row i of X = A^-1 = L^-T Y (backward substitution, all columns at once,
-// rows i+1.. already done): x_ic = (y_ic - sum_{j>i} l_ji x_jc) / l_ii
-__global__ void k_chol_inv_back_row(int64_t n, int64_t i, const double *l, const double *y,
-                                    double *x) {
-  const double lii = l[i * n + i];
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
-       c += (int64_t)gridDim.x * blockDim.x) {
-    double s = c <= i ? y[i * n + c] : 0.0;
-    for (int64_t j = i + 1; j < n; ++j) s = fma(-l[j * n + i], x[j * n + c], s);
-    x[i * n + c] = s / lii;
-  }
+__global__ void k_set_identity(int64_t n, double *x) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * n;
+       t += (int64_t)gridDim.x * blockDim.x)
+    x[t] = (t / n == t % n) ? 1.0 : 0.0;
 }
 
 // x = A^-1 b, one warp per row
@@ -1331,9 +1341,8 @@ lgx_status dense_inverse(const Csr &a, cudaStream_t s, DBuf<double> &inv, int sp
   LGX_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), s));
   if (n == 0) return LGX_OK;
   if (spd) {
-    DBuf<double> l, y;
+    DBuf<double> l;
     LGX_CHECK(l.alloc(n * n));
-    LGX_CHECK(y.alloc(n * n));
     k_dense_from_csr<<<grid_for(n, 128), 128, 0, s>>>(n, a.rowptr.p, a.col.p,
                                                      a.storage == LGX_F64 ? a.v64.p : nullptr,
                                                      a.storage == LGX_F32 ? a.v32.p : nullptr,
@@ -1351,14 +1360,25 @@ lgx_status dense_inverse(const Csr &a, cudaStream_t s, DBuf<double> &inv, int sp
     LGX_CUDA(cudaMemcpyAsync(&h_bad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     LGX_CUDA(cudaStreamSynchronize(s));
     if (h_bad) return fail(LGX_ERR_NOT_SPD, "matrix has a non-positive pivot");
-    LGX_CUDA(cudaMemsetAsync(y.p, 0, sizeof(double) * (size_t)(n * n), s));
-    for (int64_t i = 0; i < n; ++i)
-      k_chol_inv_row<<<(unsigned)std::min<int64_t>(grid_for(i + 1, 128), 1024), 128, 0, s>>>(
-        n, i, l.p, y.p);
+    // inv = I, then inv = L^-1 inv, then inv = L^-T inv
+    k_set_identity<<<(unsigned)std::min<int64_t>(grid_for(n * n, 256), 8192), 256, 0, s>>>(
+      n, inv.p);
     LGX_LAUNCH_CHECK();
-    for (int64_t i = n - 1; i >= 0; --i)
-      k_chol_inv_back_row<<<(unsigned)std::min<int64_t>(grid_for(n, 128), 1024), 128, 0, s>>>(
-        n, i, l.p, y.p, inv.p);
+    const unsigned gs = (unsigned)std::min<int64_t>(grid_for(n, 256), 64);
+    for (int64_t k = 0; k < n; ++k) {
+      k_tri_scale<<<gs, 256, 0, s>>>(n, k, l.p, inv.p);
+      const int64_t rows = n - k - 1;
+      if (rows > 0)
+        k_tri_update<<<(unsigned)std::min<int64_t>(grid_for(rows * n, 256), 4096), 256, 0, s>>>(
+          n, k, k + 1, n, 0, l.p, inv.p);
+    }
+    LGX_LAUNCH_CHECK();
+    for (int64_t k = n - 1; k >= 0; --k) {
+      k_tri_scale<<<gs, 256, 0, s>>>(n, k, l.p, inv.p);
+      if (k > 0)
+        k_tri_update<<<(unsigned)std::min<int64_t>(grid_for(k * n, 256), 4096), 256, 0, s>>>(
+          n, k, 0, k, 1, l.p, inv.p);
+    }
     LGX_LAUNCH_CHECK();
     LGX_CUDA(cudaStreamSynchronize(s));
     return LGX_OK;

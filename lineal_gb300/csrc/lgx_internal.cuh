@@ -174,6 +174,8 @@ struct lgx_matrix {
   lgx::DBuf<uint8_t> mat;       // stencil lookup materials (owned copy)
   lgx::DBuf<double> k;          // stencil value conductivities (owned copy)
   lgx::DBuf<double> diag;       // cached diagonal (lazily computed)
+  lgx::DBuf<double> rdiag;      // stencil SOR: correctly rounded 1 / diagonal, 0 where the
+                                // sweep divides directly (lazily computed)
   int64_t grid_dims[3] = {0, 0, 0};  // CSR kinds: grid operator on this grid
   int grid_points = 0;                // 27 or 7 points; 0: unknown
 };

@@ -327,10 +327,19 @@ __global__ void __launch_bounds__(256)
 // (1 - relax) x_i); ultra: x_i + relax accum / |a_ii|.  The result equals
 // the SOR of the assembled matrix in the row order sorted by (colour, index)
 // bit for bit.
+// 1 / diagonal, correctly rounded, for the rows whose diagonal lies within
+// [2^-400, 2^400] in magnitude; 0 elsewhere (those rows divide directly)
+__global__ void k_st_rdiag(int64_t n, const double *diag, double *rdiag) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    rdiag[i] = exponent_within_400(diag[i]) ? 1.0 / diag[i] : 0.0;
+}
+
 template <bool LOOKUP>
 __global__ void __launch_bounds__(256)
   k_st_sor_colour(StencilDev S, int colour, const double *nb, double relax, double m1, int ultra,
-                  const double *x_in, double *x_out, const double *__restrict__ b) {
+                  int relax_one, const double *__restrict__ rdiag, const double *x_in,
+                  double *x_out, const double *__restrict__ b) {
   __shared__ double sh_conn[48];
   const double *conn = stage_conn(S, sh_conn);
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
@@ -353,10 +362,18 @@ __global__ void __launch_bounds__(256)
   }
   if (ultra) {
     x_out[i] = xi + relax * accum / fabs(diag);
-  } else {
-    const double quot = accum / diag;
-    x_out[i] = fma(relax, quot, m1 * xi);
+    return;
   }
+  // the quotient through the reciprocal table (the same bits as accum /
+  // diag), and relax = 1's shortcut where it cannot change the result
+  const double y = rdiag[i];
+  const double quot = (nonzero_bits(y) && exponent_within_400(accum))
+                        ? div_by_recip(accum, diag, y) : accum / diag;
+  if (relax_one && nonzero_bits(quot) && exponent_field(xi) != 0x7ff) {
+    x_out[i] = quot;  // fma(1, q, 0 * x_i) == q for nonzero q and finite x_i
+    return;
+  }
+  x_out[i] = fma(relax, quot, m1 * xi);
 }
 
 __global__ void k_st_rhs(int n0, int n1, int n2, const double *cell_value, double border_q0,
@@ -794,19 +811,26 @@ lgx_status stencil_sor_sweep(const lgx_matrix *ac, double relax, int forward, in
   lgx_matrix *a = const_cast<lgx_matrix *>(ac);
   if (a->n == 0) return LGX_OK;
   LGX_CHECK(stencil_ensure(a, s));
+  if (!a->rdiag.p) {
+    LGX_CHECK(a->rdiag.alloc(a->n));
+    k_st_rdiag<<<std::min<int64_t>(grid_for(a->n, 256), 16384), 256, 0, s>>>(a->n, a->diag.p,
+                                                                            a->rdiag.p);
+    LGX_LAUNCH_CHECK();
+  }
   StencilDev S = dev_of(a);
   const dim3 g((unsigned)(((S.n2 + 1) / 2 + 31) / 32), (unsigned)((S.n1 + 7) / 8),
                (unsigned)S.n0);
   const double m1 = 1.0 - relax;
+  const int relax_one = relax == 1.0;
   for (int cc = 0; cc < 2; ++cc) {
     const int colour = forward ? cc : 1 - cc;
     const double *nb = cc == 0 ? x_in : x_out;
     if (a->st.lookup)
-      k_st_sor_colour<true><<<g, kStBlock, 0, s>>>(S, colour, nb, relax, m1, ultra, x_in, x_out,
-                                                   b);
+      k_st_sor_colour<true><<<g, kStBlock, 0, s>>>(S, colour, nb, relax, m1, ultra, relax_one,
+                                                   a->rdiag.p, x_in, x_out, b);
     else
-      k_st_sor_colour<false><<<g, kStBlock, 0, s>>>(S, colour, nb, relax, m1, ultra, x_in,
-                                                    x_out, b);
+      k_st_sor_colour<false><<<g, kStBlock, 0, s>>>(S, colour, nb, relax, m1, ultra, relax_one,
+                                                    a->rdiag.p, x_in, x_out, b);
     LGX_LAUNCH_CHECK();
   }
   return LGX_OK;
