@@ -228,7 +228,7 @@ struct BoxInfo {
 
   BoxInfo(std::array<int64_t, 3> cells, std::array<double, 3> axis_lengths)
       : cell_nums(cells), lengths(axis_lengths) {
-    axis_quotients();  // validates
+    (void)axis_quotients();  // validates
   }
   [[nodiscard]] std::array<double, 3> axis_lengths() const { return lengths; }
   [[nodiscard]] double axis_length(std::size_t axis) const { return lengths[axis]; }
