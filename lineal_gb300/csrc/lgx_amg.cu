@@ -14,6 +14,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdlib>
+#include <cstring>
 #include <memory>
 #include <vector>
 
@@ -184,7 +185,7 @@ struct AggDev {
   int32_t *eval;        // per front position: 4 ints of evaluation results
   int64_t *pcount;      // aggregates per partition
   int64_t *stats;       // 5 counters (atomic adds)
-  int32_t *conn_flag32; // k_aggregate_block: connected flags by local aggregate id (atomics)
+  int32_t cap;          // k_aggregate_cta: front and connected-list capacity
 };
 
 __device__ __forceinline__ int64_t part_begin(int64_t n, int64_t p, int64_t k) {
@@ -516,198 +517,393 @@ struct AggWarp {
 
 constexpr int kAggWarpsPerBlock = 4;
 
-// ---------------------------------------------------------------------------
-// The same aggregation with a whole CTA per partition, for levels with few
-// partitions (the coarse levels: 8 to a few hundred partitions of up to ~1e5
-// vertices), where one warp per partition leaves the GPU almost idle and the
-// front evaluations -- a chain of dependent loads per edge batch -- dominate.
-// Every thread runs the same control flow: each decision is a block-wide
-// reduction whose result every thread reads from shared memory after a
-// barrier, so the loop bounds, branches and barrier counts are uniform across
-// the CTA.  Writes of a single thread (aggregate membership, the front swap)
-// are published by the barrier that follows them.  The front and the
-// connected set take their slots through shared-memory atomics: their order
-// differs from the warp kernel's, but no decision depends on it (selections
-// take the smallest vertex ids, evaluations are recomputed per step), so the
-// aggregates are the warp kernel's -- and the oracle's -- exactly.
-// ---------------------------------------------------------------------------
-constexpr int kAggBlockThreads = 256;
-constexpr int kAggBlockWarps = kAggBlockThreads / 32;
+__global__ void __launch_bounds__(32 * kAggWarpsPerBlock) k_aggregate(AggDev D) {
+  const int64_t p = (int64_t)blockIdx.x * kAggWarpsPerBlock + (threadIdx.x >> 5);
+  if (p >= D.nparts) return;  // whole warps leave together
+  const int64_t pb = part_begin(D.n, D.nparts, p), pe = part_begin(D.n, D.nparts, p + 1);
+  const int lane = threadIdx.x & 31;
+  for (int64_t v = pb + lane; v < pe; v += 32) D.block_len[v] = 0;
+  __syncwarp();
+  AggWarp W(D, pb, pe);
+  for (int64_t v = pb; v < pe; ++v) W.handle(v);
+  if (lane == 0) {
+    D.pcount[p] = W.counter;
+    W.st[0] = W.counter;
+    for (int k = 0; k < 5; ++k)
+      if (W.st[k]) atomicAdd((unsigned long long *)&D.stats[k], (unsigned long long)W.st[k]);
+  }
+}
 
-struct AggBlockShared {
-  int32_t front_len, conn_len;
-  int64_t part_i64[kAggBlockWarps];
-  int32_t part_k0[kAggBlockWarps], part_kn[kAggBlockWarps];
-  double part_kc[kAggBlockWarps];
-  int32_t part_have[kAggBlockWarps];
-  int64_t res_i64;
-  int32_t res_k0, res_kn, res_have;
-  double res_kc;
+// ---------------------------------------------------------------------------
+// The same aggregation with one CTA per partition and the partition's
+// mutable state in shared memory, for levels with few, large partitions (the
+// coarse levels: 8 to a few hundred partitions of 5k-70k vertices and rows
+// of 50-300 entries).  There the front of an aggregate is short (10-20
+// vertices on average) but its rows are long, so evaluating it vertex by
+// vertex leaves most lanes idle behind one long row each.  Here:
+//  - warp 0 runs the sequential steps of the warp kernel (add a vertex,
+//    update the front and connected set, choose, pick) on shared memory:
+//    the aggregate ids (16 bits per vertex), front and connected flags (one
+//    bit per vertex / local aggregate), the front list with each member's
+//    row offset and length, the connected list;
+//  - each evaluation of the front (grow_aggregate's counts, round_
+//    aggregate's test) is spread over the whole CTA as one flat range of
+//    (front vertex, edge) items: prefix sums of the members' row lengths
+//    map item k to its member, the items' strength bytes and columns load
+//    together, and per-member counts form by a segmented warp reduction and
+//    a shared-memory atomic per warp segment.  Warps 1.. wait between
+//    evaluations at a named barrier that warp 0 releases.
+// Decisions are the warp kernel's: counts are order-free sums, selections
+// take the smallest vertex ids, a member's position is found by search, and
+// every aggregate's vertices are added in the same order.  Capacities: local
+// aggregate ids below 0xFFFE, rows below 65536 entries (counts are packed
+// in 16-bit halves), front and connected lists within `cap` entries; a
+// partition that exceeds one sets `overflow` and the host redoes the level
+// with the warp kernel.
+// ---------------------------------------------------------------------------
+constexpr int kAggCtaThreads = 256;
+constexpr int kAggCtaCapMax = 4096;
+constexpr int kAggCtaCapMin = 256;
+constexpr uint16_t kSUnagg = 0xFFFF, kSIso = 0xFFFE;
+constexpr int kCmdGrow = 0, kCmdRound = 1, kCmdDone = 2;
+
+__host__ __device__ inline int64_t agg_align16(int64_t b) { return (b + 15) / 16 * 16; }
+__host__ __device__ inline int64_t agg_bit_words(int64_t P) { return (P + 31) / 32; }
+// shared bytes of a partition of P vertices with list capacity cap (a
+// multiple of 8): aggregate ids, two bit sets, then per list entry the row
+// offset (8), member, row length, two counters (4 each), connected id (2),
+// plus cap + 1 prefix sums
+__host__ __device__ inline int64_t agg_cta_base(int64_t P) {
+  return agg_align16(2 * P) + agg_align16(8 * agg_bit_words(P));
+}
+__host__ __device__ inline int64_t agg_cta_bytes(int64_t P, int64_t cap) {
+  return agg_cta_base(P) + 30 * cap + agg_align16(4 * (cap + 1));
+}
+
+struct AggCtaCtl {
+  int32_t cmd, nfront, total, bad;
+  uint32_t ag;
 };
 
-struct AggBlock {
-  const AggDev &D;
-  AggBlockShared &sh;
-  int64_t pb, pe;
-  int tid, lane, warp;
-  // block-uniform state, identical in every thread
-  int64_t counter = 0;
-  int64_t st[5] = {0, 0, 0, 0, 0};
+__device__ __forceinline__ void agg_cta_sync() {
+  __syncwarp();
+  asm volatile("bar.sync 1, %0;" ::"r"(kAggCtaThreads) : "memory");
+}
 
-  __device__ AggBlock(const AggDev &d, AggBlockShared &s, int64_t b, int64_t e)
-      : D(d), sh(s), pb(b), pe(e) {
-    tid = threadIdx.x;
-    lane = tid & 31;
-    warp = tid >> 5;
+struct AggCta {
+  const AggDev &D;
+  AggCtaCtl *ctl;
+  int64_t pb, pe;
+  int lane;
+  int32_t cap;
+  uint16_t *sagg;   // by local vertex: local aggregate id, kSUnagg, kSIso
+  uint32_t *inF;    // by local vertex: front member
+  uint32_t *cF;     // by local aggregate id: connected
+  int64_t *fbeg;    // per front position: row offset of the member
+  int32_t *front;   // per front position: member (vertex id); unordered
+  int32_t *flen;    // per front position: row length, 0 for isolated members
+  uint32_t *cntA, *cntB;  // per front position: packed 16-bit counts / mark
+  int32_t *psum;    // prefix sums of flen over positions (nfront + 1)
+  uint16_t *conn;   // connected local aggregate ids
+  // warp 0's state (warp-uniform)
+  int64_t front_len = 0, conn_len = 0, counter = 0;
+  int64_t st[5] = {0, 0, 0, 0, 0};
+  bool bad = false;
+
+  __device__ AggCta(const AggDev &d, AggCtaCtl *c, int64_t b, int64_t e, unsigned char *smem)
+      : D(d), ctl(c), pb(b), pe(e) {
+    lane = threadIdx.x & 31;
+    cap = d.cap;
+    const int64_t P = e - b;
+    unsigned char *q = smem;
+    sagg = (uint16_t *)q;
+    q += agg_align16(2 * P);
+    inF = (uint32_t *)q;
+    cF = inF + agg_bit_words(P);
+    q += agg_align16(8 * agg_bit_words(P));
+    fbeg = (int64_t *)q;
+    q += 8 * (int64_t)cap;
+    front = (int32_t *)q;
+    flen = front + cap;
+    cntA = (uint32_t *)(flen + cap);
+    cntB = cntA + cap;
+    psum = (int32_t *)(cntB + cap);
+    q += 16 * (int64_t)cap + agg_align16(4 * (cap + 1));
+    conn = (uint16_t *)q;
   }
   __device__ bool in_range(int64_t v) const { return v >= pb && v < pe; }
   __device__ int32_t &blen(uint32_t ag) const { return D.block_len[pb + ag]; }
   __device__ int32_t *block(uint32_t ag) const {
     return D.blocks + (pb + (int64_t)ag) * D.max_size;
   }
-
-  // block-wide minimum of an int64 (every thread gets it)
-  __device__ int64_t block_min(int64_t v) {
-    for (int o = 16; o > 0; o >>= 1) {
-      const int64_t other = __shfl_xor_sync(kFull, v, o);
-      v = other < v ? other : v;
-    }
-    if (lane == 0) sh.part_i64[warp] = v;
-    __syncthreads();
-    if (tid == 0) {
-      int64_t m = sh.part_i64[0];
-      for (int w = 1; w < kAggBlockWarps; ++w) m = sh.part_i64[w] < m ? sh.part_i64[w] : m;
-      sh.res_i64 = m;
-    }
-    __syncthreads();
-    return sh.res_i64;
+  __device__ uint32_t agg_of(int64_t v) const {
+    const uint16_t a = sagg[v - pb];
+    return a == kSUnagg ? kUnaggregated : a == kSIso ? kIsolated : (uint32_t)a;
+  }
+  __device__ void set_agg(int64_t v, uint32_t a) const {
+    sagg[v - pb] = a == kUnaggregated ? kSUnagg : a == kIsolated ? kSIso : (uint16_t)a;
+  }
+  __device__ bool in_front(int64_t v) const {
+    const int64_t u = v - pb;
+    return (inF[u >> 5] >> (u & 31)) & 1u;
+  }
+  __device__ void front_flag(int64_t v, bool on) const {
+    const int64_t u = v - pb;
+    if (on) atomicOr(&inF[u >> 5], 1u << (u & 31));
+    else atomicAnd(&inF[u >> 5], ~(1u << (u & 31)));
+  }
+  __device__ bool connected(uint32_t ag) const { return (cF[ag >> 5] >> (ag & 31)) & 1u; }
+  __device__ void conn_flag(uint32_t ag, bool on) const {
+    if (on) atomicOr(&cF[ag >> 5], 1u << (ag & 31));
+    else atomicAnd(&cF[ag >> 5], ~(1u << (ag & 31)));
   }
 
-  __device__ void add_help(int64_t v, uint32_t ag, int64_t &size) {
+  // ---- the CTA-wide evaluation (every thread) ----
+  // item k of [0, total) -> front position i with psum[i] <= k < psum[i + 1]
+  __device__ int32_t member_of(int32_t k, int32_t nf) const {
+    int32_t lo = 0, hi = nf;
+    while (lo < hi) {
+      const int32_t mid = (lo + hi) >> 1;
+      if (psum[mid + 1] <= k) lo = mid + 1;
+      else hi = mid;
+    }
+    return lo;
+  }
+
+  __device__ void eval_part() const {
+    const int cmd = ctl->cmd;
+    const int32_t nf = ctl->nfront, total = ctl->total;
+    const uint32_t ag = ctl->ag;
+    constexpr int U = 4;
+    for (int32_t kb = 0; kb < total; kb += U * kAggCtaThreads) {
+      int32_t mi[U];
+      int64_t e[U] = {};
+      int32_t t[U] = {};
+      uint8_t dp[U] = {}, nf_[U] = {};
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int32_t k = kb + u * kAggCtaThreads + (int32_t)threadIdx.x;
+        mi[u] = -1;
+        if (k < total) {
+          mi[u] = member_of(k, nf);
+          e[u] = fbeg[mi[u]] + (k - psum[mi[u]]);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (mi[u] >= 0) {
+          t[u] = D.col[e[u]];
+          dp[u] = D.dep[e[u]];
+          nf_[u] = cmd == kCmdGrow ? D.inf[e[u]] : 0;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        uint32_t a = 0, b = 0;
+        if (mi[u] >= 0 && t[u] != front[mi[u]] && in_range(t[u])) {
+          const uint32_t ha = agg_of(t[u]);
+          if (cmd == kCmdGrow) {
+            // (two-way, one-way) counts into the aggregate | (connected, in front)
+            a = (ha == ag && dp[u] && nf_[u]) | (uint32_t)(ha == ag && dp[u] && !nf_[u]) << 16;
+            b = (ha < kIsolated && connected(ha)) | (uint32_t)in_front(t[u]) << 16;
+          } else {
+            // (dependent edges into the aggregate | edges into it), unaggregated
+            a = (ha == ag && dp[u]) | (uint32_t)(ha == ag) << 16;
+            b = ha == kUnaggregated;
+          }
+        }
+        // lanes hold consecutive items, so equal members form contiguous
+        // segments: sum each onto its first lane
+        const int32_t m = mi[u];
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const uint32_t oa = __shfl_down_sync(kFull, a, d);
+          const uint32_t ob = __shfl_down_sync(kFull, b, d);
+          const int32_t om = __shfl_down_sync(kFull, m, d);
+          if (lane + d < 32 && om == m) {
+            a += oa;
+            b += ob;
+          }
+        }
+        const int32_t prev = __shfl_up_sync(kFull, m, 1);
+        if (m >= 0 && (lane == 0 || prev != m) && (a | b)) {
+          atomicAdd(&cntA[m], a);
+          atomicAdd(&cntB[m], b);
+        }
+      }
+    }
+  }
+
+  // warp 0: counts of every front member into cntA / cntB, the whole CTA
+  // taking part
+  __device__ void eval(int cmd, uint32_t ag) {
+    int32_t run = 0;
+    for (int64_t base = 0; base < front_len; base += 32) {
+      const int64_t i = base + lane;
+      const int32_t len = i < front_len ? flen[i] : 0;
+      int32_t x = len;
+      for (int d = 1; d < 32; d <<= 1) {
+        const int32_t y = __shfl_up_sync(kFull, x, d);
+        if (lane >= d) x += y;
+      }
+      if (i < front_len) {
+        psum[i + 1] = run + x;
+        cntA[i] = 0;
+        cntB[i] = 0;
+      }
+      run += __shfl_sync(kFull, x, 31);
+    }
+    if (lane == 0) {
+      psum[0] = 0;
+      ctl->cmd = cmd;
+      ctl->nfront = (int32_t)front_len;
+      ctl->total = run;
+      ctl->ag = ag;
+    }
+    agg_cta_sync();  // releases the other warps
+    eval_part();
+    agg_cta_sync();  // every count is in
+  }
+
+  // ---- warp 0's sequential steps ----
+  // AggregateManager::add_help: v (row [eb, ee)) joins aggregate ag; its
+  // in-range neighbours update the connected set and the front, new front
+  // members get their row offsets and lengths
+  __device__ void add_help(int64_t v, uint32_t ag, int64_t &size, int64_t eb, int64_t ee) {
     ++size;
-    if (tid == 0) {
-      D.agg[v] = ag;
+    if (lane == 0) {
+      set_agg(v, ag);
       block(ag)[blen(ag)++] = (int32_t)v;
     }
-    const int64_t eb = D.rowptr[v], ee = D.rowptr[v + 1];
-    for (int64_t e = eb + tid; e < ee; e += kAggBlockThreads) {
-      const int64_t t = D.col[e];
-      if (t == v || !in_range(t)) continue;
-      const uint32_t ta = D.agg[t];
-      if (ta < kIsolated) {
-        if (atomicExch(&D.conn_flag32[pb + ta], 1) == 0) {
-          const int32_t pos = atomicAdd(&sh.conn_len, 1);
-          D.conn[pb + pos] = (int32_t)ta;
+    __syncwarp();
+    const int64_t f0 = front_len;
+    for (int64_t base = eb; base < ee; base += 128) {
+      int64_t tt[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int64_t e = base + 32 * j + lane;
+        tt[j] = e < ee ? (int64_t)D.col[e] : -1;
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (base + 32 * j >= ee) break;  // uniform
+        const int64_t t = tt[j];
+        bool want_conn = false, want_front = false;
+        uint32_t ta = kUnaggregated;
+        if (t >= 0 && t != v && in_range(t)) {
+          ta = agg_of(t);
+          want_conn = ta < kIsolated && !connected(ta);
+          want_front = ta == kUnaggregated && !in_front(t);
         }
-      } else if (ta == kUnaggregated && D.front_pos[t] < 0) {
-        const int32_t pos = atomicAdd(&sh.front_len, 1);
-        D.front[pb + pos] = (int32_t)t;
-        D.front_pos[t] = pos;
+        const unsigned cmask = __ballot_sync(kFull, want_conn);
+        bool leader = false;
+        if (want_conn) {
+          const unsigned same = __match_any_sync(cmask, ta);
+          leader = (__ffs(same) - 1) == lane;
+        }
+        const unsigned lmask = __ballot_sync(kFull, leader);
+        const unsigned fmask = __ballot_sync(kFull, want_front);
+        if (conn_len + __popc(lmask) > cap || front_len + __popc(fmask) > cap) {
+          bad = true;  // uniform: the counts come from ballots
+          return;
+        }
+        const unsigned below = (1u << lane) - 1u;
+        if (leader) {
+          conn[conn_len + __popc(lmask & below)] = (uint16_t)ta;
+          conn_flag(ta, true);
+        }
+        conn_len += __popc(lmask);
+        if (want_front) {
+          front[front_len + __popc(fmask & below)] = (int32_t)t;
+          front_flag(t, true);
+        }
+        front_len += __popc(fmask);
+        __syncwarp();
       }
     }
-    __syncthreads();
+    bool long_row = false;
+    for (int64_t q = f0 + lane; q < front_len; q += 32) {
+      const int64_t t = front[q];
+      const int64_t rb = D.rowptr[t], re = D.rowptr[t + 1];
+      fbeg[q] = rb;
+      long_row = long_row || re - rb > 65535;
+      flen[q] = D.iso[t] ? 0 : (int32_t)(re - rb);
+    }
+    if (__any_sync(kFull, long_row)) bad = true;  // counts would not fit 16 bits
+    __syncwarp();
   }
 
-  __device__ void front_erase(int64_t v) {
-    if (tid == 0) {
-      const int32_t fl = sh.front_len;
-      const int32_t pos = D.front_pos[v];
-      if (pos >= 0) {
-        const int32_t last = D.front[pb + fl - 1];
-        D.front[pb + pos] = last;
-        D.front_pos[last] = pos;
-        D.front_pos[v] = -1;
-      }
-      sh.front_len = fl - 1;
+  // removes front member v; returns its row
+  __device__ void front_take(int64_t v, int64_t &eb, int64_t &ee) {
+    int64_t pos = -1;
+    for (int64_t i = lane; i < front_len; i += 32)
+      if (front[i] == (int32_t)v) pos = i;
+    for (int o = 16; o > 0; o >>= 1) {
+      const int64_t other = __shfl_xor_sync(kFull, pos, o);
+      pos = other > pos ? other : pos;
     }
-    __syncthreads();
+    // v was picked from the front, so pos >= 0 (guarded all the same)
+    if (pos < 0) {
+      bad = true;
+      eb = ee = 0;
+      return;
+    }
+    eb = fbeg[pos];
+    ee = eb + flen[pos];
+    __syncwarp();
+    if (lane == 0) {
+      const int64_t last = front_len - 1;
+      front[pos] = front[last];
+      fbeg[pos] = fbeg[last];
+      flen[pos] = flen[last];
+      front_flag(v, false);
+    }
+    __syncwarp();
+    --front_len;
   }
 
   __device__ void helpers_clear() {
-    const int32_t fl = sh.front_len, cl = sh.conn_len;
-    for (int64_t i = tid; i < fl; i += kAggBlockThreads) D.front_pos[D.front[pb + i]] = -1;
-    for (int64_t i = tid; i < cl; i += kAggBlockThreads) D.conn_flag32[pb + D.conn[pb + i]] = 0;
-    __syncthreads();
-    if (tid == 0) {
-      sh.front_len = 0;
-      sh.conn_len = 0;
-    }
-    __syncthreads();
+    for (int64_t i = lane; i < front_len; i += 32) front_flag(front[i], false);
+    for (int64_t i = lane; i < conn_len; i += 32) conn_flag(conn[i], false);
+    front_len = 0;
+    conn_len = 0;
+    __syncwarp();
   }
 
-  template <class F>
-  __device__ __forceinline__ void edges(int64_t vtx, F &&f) const {
-    const int64_t eb = D.rowptr[vtx], ee = D.rowptr[vtx + 1];
-    for (int64_t e0 = eb; e0 < ee; e0 += 8) {
-      int64_t t[8];
-      bool ok[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int64_t e = e0 + u;
-        t[u] = e < ee ? (int64_t)D.col[e] : vtx;
-        ok[u] = e < ee && t[u] != vtx && in_range(t[u]);
-      }
-      uint32_t ha[8];
-      bool fr[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        ha[u] = ok[u] ? D.agg[t[u]] : kUnaggregated;
-        fr[u] = ok[u] && D.front_pos[t[u]] >= 0;
-      }
-      bool cf[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u)
-        cf[u] = ok[u] && ha[u] < kIsolated && D.conn_flag32[pb + ha[u]] != 0;
-#pragma unroll
-      for (int u = 0; u < 8; ++u)
-        if (ok[u]) f(e0 + u, t[u], ha[u], fr[u], cf[u]);
+  // smallest member id > floor among the marked positions (mark in cntA)
+  __device__ int64_t warp_min_marked(int64_t floor) const {
+    int64_t best = INT64_MAX;
+    for (int64_t i = lane; i < front_len; i += 32) {
+      if (!cntA[i]) continue;
+      const int64_t v = front[i];
+      if (v > floor && v < best) best = v;
     }
+    for (int o = 16; o > 0; o >>= 1) {
+      const int64_t other = __shfl_xor_sync(kFull, best, o);
+      best = other < best ? other : best;
+    }
+    return best;
   }
 
-  // grow_aggregate (base.hpp:532-585), the warp kernel's steps block-wide
+  // grow_aggregate (base.hpp:532-585)
   __device__ void grow(uint32_t ag, int64_t &size) {
-    while (size < D.min_size) {
-      const int32_t fl = sh.front_len;
-      int any2 = 0;
-      for (int64_t i = tid; i < fl; i += kAggBlockThreads) {
-        const int64_t vtx = D.front[pb + i];
-        int32_t *ev = D.eval + 4 * (pb + i);
-        if (D.iso[vtx]) {
-          ev[0] = ev[1] = 0;
-          ev[3] = 0;
-          continue;
-        }
-        int32_t con = 0, nbs = 0, c2 = 0, c1 = 0;
-        edges(vtx, [&](int64_t e, int64_t, uint32_t ha, bool in_front, bool connected) {
-          const bool dep = D.dep[e], inf = D.inf[e];
-          con += connected;
-          nbs += in_front;
-          c2 += (ha == ag) && (inf && dep);
-          c1 += (ha == ag) && (!inf && dep);
-        });
-        ev[0] = c2;
-        ev[1] = c1;
-        ev[2] = con;
-        ev[3] = nbs;
-        any2 |= c2 > 0;
-      }
-      const bool mode2 = __syncthreads_or(any2) != 0;
-      // maximum key among eligible vertices
+    while (size < D.min_size && front_len > 0) {
+      eval(kCmdGrow, ag);
+      bool any2 = false;
+      for (int64_t i = lane; i < front_len; i += 32) any2 = any2 || (cntA[i] & 0xFFFFu) != 0;
+      const bool mode2 = __any_sync(kFull, any2);
       int32_t k0 = 0, kn = 0;
       double kc = 0.0;
       bool have = false;
-      for (int64_t i = tid; i < fl; i += kAggBlockThreads) {
-        const int64_t vtx = D.front[pb + i];
-        if (D.iso[vtx]) continue;
-        const int32_t *ev = D.eval + 4 * (pb + i);
-        const int32_t c = mode2 ? ev[0] : ev[1];
+      for (int64_t i = lane; i < front_len; i += 32) {
+        const int32_t c = (int32_t)(mode2 ? cntA[i] & 0xFFFFu : cntA[i] >> 16);
         if (c <= 0) continue;
-        const int64_t adj = (D.rowptr[vtx + 1] - D.rowptr[vtx]) - 1;
-        const double con = (double)ev[2] / (double)adj;
-        if (!have || c > k0 || (c == k0 && (con > kc || (con == kc && ev[3] > kn)))) {
+        const double con = (double)(cntB[i] & 0xFFFFu) / (double)(flen[i] - 1);
+        const int32_t nb = (int32_t)(cntB[i] >> 16);
+        if (!have || c > k0 || (c == k0 && (con > kc || (con == kc && nb > kn)))) {
           k0 = c;
           kc = con;
-          kn = ev[3];
+          kn = nb;
           have = true;
         }
       }
@@ -723,149 +919,118 @@ struct AggBlock {
           have = true;
         }
       }
-      if (lane == 0) {
-        sh.part_k0[warp] = k0;
-        sh.part_kc[warp] = kc;
-        sh.part_kn[warp] = kn;
-        sh.part_have[warp] = have;
-      }
-      __syncthreads();
-      if (tid == 0) {
-        bool h = false;
-        int32_t b0 = 0, bn = 0;
-        double bc = 0.0;
-        for (int w = 0; w < kAggBlockWarps; ++w) {
-          if (!sh.part_have[w]) continue;
-          const int32_t o0 = sh.part_k0[w], on = sh.part_kn[w];
-          const double oc = sh.part_kc[w];
-          if (!h || o0 > b0 || (o0 == b0 && (oc > bc || (oc == bc && on > bn)))) {
-            b0 = o0;
-            bc = oc;
-            bn = on;
-            h = true;
-          }
-        }
-        sh.res_have = h;
-        sh.res_k0 = b0;
-        sh.res_kc = bc;
-        sh.res_kn = bn;
-      }
-      __syncthreads();
-      if (!sh.res_have) break;  // no candidates (uniform)
-      k0 = sh.res_k0;
-      kc = sh.res_kc;
-      kn = sh.res_kn;
-      // mark the vertices whose key equals the maximum (eval[3] reused as mark)
-      for (int64_t i = tid; i < fl; i += kAggBlockThreads) {
-        const int64_t vtx = D.front[pb + i];
-        int32_t *ev = D.eval + 4 * (pb + i);
+      if (!have) break;
+      // mark the members whose key equals the maximum (cntA becomes the mark)
+      for (int64_t i = lane; i < front_len; i += 32) {
+        const int32_t c = (int32_t)(mode2 ? cntA[i] & 0xFFFFu : cntA[i] >> 16);
         bool m = false;
-        if (!D.iso[vtx]) {
-          const int32_t c = mode2 ? ev[0] : ev[1];
-          if (c > 0) {
-            const int64_t adj = (D.rowptr[vtx + 1] - D.rowptr[vtx]) - 1;
-            const double con = (double)ev[2] / (double)adj;
-            m = c == k0 && con == kc && ev[3] == kn;
-          }
+        if (c > 0) {
+          const double con = (double)(cntB[i] & 0xFFFFu) / (double)(flen[i] - 1);
+          m = c == k0 && con == kc && (int32_t)(cntB[i] >> 16) == kn;
         }
-        ev[3] = m;
+        cntA[i] = m;
       }
-      __syncthreads();
-      // add the smallest `room` candidates in ascending order
+      __syncwarp();
       const int64_t room = D.max_size - size;
       int64_t floor = -1;
       int64_t picked[64];
       int64_t npick = 0;
       for (int64_t k = 0; k < room; ++k) {
-        int64_t best = INT64_MAX;
-        for (int64_t i = tid; i < fl; i += kAggBlockThreads) {
-          if (!D.eval[4 * (pb + i) + 3]) continue;
-          const int64_t v = D.front[pb + i];
-          if (v > floor && v < best) best = v;
-        }
-        const int64_t v = block_min(best);
+        const int64_t v = warp_min_marked(floor);
         if (v == INT64_MAX) break;
         picked[npick++] = v;
         floor = v;
       }
       for (int64_t k = 0; k < npick; ++k) {
-        front_erase(picked[k]);
-        add_help(picked[k], ag, size);
+        int64_t eb, ee;
+        front_take(picked[k], eb, ee);
+        if (bad) return;
+        add_help(picked[k], ag, size, eb, ee);
+        if (bad) return;
       }
     }
   }
 
   // round_aggregate (base.hpp:601-636)
   __device__ void round(uint32_t ag, int64_t &size) {
-    while (size < D.max_size) {
-      const int32_t fl = sh.front_len;
+    while (size < D.max_size && front_len > 0) {
+      eval(kCmdRound, ag);
       int64_t best = INT64_MAX;
-      for (int64_t i = tid; i < fl; i += kAggBlockThreads) {
-        const int64_t vtx = D.front[pb + i];
-        if (D.iso[vtx] || vtx >= best) continue;
-        int32_t cons = 0, unagg = 0, inagg = 0;
-        edges(vtx, [&](int64_t e, int64_t, uint32_t ha, bool, bool) {
-          cons += (ha == ag) && D.dep[e];
-          unagg += ha == kUnaggregated;
-          inagg += ha == ag;
-        });
+      for (int64_t i = lane; i < front_len; i += 32) {
+        const uint32_t cons = cntA[i] & 0xFFFFu, inagg = cntA[i] >> 16, unagg = cntB[i];
         if (cons == 0 || unagg >= inagg) continue;
-        best = vtx;
+        best = front[i] < best ? front[i] : best;
       }
-      best = block_min(best);
+      for (int o = 16; o > 0; o >>= 1) {
+        const int64_t other = __shfl_xor_sync(kFull, best, o);
+        best = other < best ? other : best;
+      }
       if (best == INT64_MAX) break;
-      front_erase(best);
-      add_help(best, ag, size);
+      int64_t eb, ee;
+      front_take(best, eb, ee);
+      if (bad) return;
+      add_help(best, ag, size, eb, ee);
+      if (bad) return;
     }
   }
 
   // handle_vertex (base.hpp:638-677)
   __device__ void handle(int64_t seed) {
-    if (D.agg[seed] != kUnaggregated) return;  // published by the last barrier
+    if (agg_of(seed) != kUnaggregated) return;
     if (D.iso[seed]) {
-      if (tid == 0) D.agg[seed] = kIsolated;
-      __syncthreads();
+      if (lane == 0) set_agg(seed, kIsolated);
+      __syncwarp();
       ++st[4];
+      return;
+    }
+    if (counter >= (int64_t)kSIso) {
+      bad = true;  // local aggregate ids must fit 16 bits
       return;
     }
     const uint32_t ag = (uint32_t)counter;
     int64_t size = 0;
-    add_help(seed, ag, size);
+    const int64_t eb = D.rowptr[seed], ee = D.rowptr[seed + 1];
+    add_help(seed, ag, size, eb, ee);
+    if (bad) return;
     grow(ag, size);
+    if (bad) return;
     round(ag, size);
+    if (bad) return;
     if (size == 1 && D.max_size > 1) {
-      // find_merge_aggregate (base.hpp:487-503): the first strong in-range
-      // edge (ascending column) whose head lies in an aggregate with room
-      const int64_t eb = D.rowptr[seed], ee = D.rowptr[seed + 1];
-      int64_t first = INT64_MAX;
-      for (int64_t e = eb + tid; e < ee; e += kAggBlockThreads) {
-        const int64_t t = D.col[e];
-        if (t != seed && in_range(t) && (D.dep[e] || D.inf[e])) {
-          const uint32_t ta = D.agg[t];
-          if (ta < kIsolated && blen(ta) < D.max_size && e < first) first = e;
+      // find_merge_aggregate (base.hpp:487-503): first strong in-range edge
+      // (ascending column) whose head lies in an aggregate with room
+      uint32_t target = kUnaggregated;
+      for (int64_t e0 = eb; e0 < ee && target == kUnaggregated; e0 += 32) {
+        const int64_t e = e0 + lane;
+        bool ok = false;
+        uint32_t ta = kUnaggregated;
+        if (e < ee) {
+          const int64_t t = D.col[e];
+          if (t != seed && in_range(t) && (D.dep[e] || D.inf[e])) {
+            ta = agg_of(t);
+            ok = ta < kIsolated && blen(ta) < D.max_size;
+          }
         }
+        const unsigned m = __ballot_sync(kFull, ok);
+        if (m) target = __shfl_sync(kFull, ta, __ffs(m) - 1);
       }
-      first = block_min(first);
-      if (first != INT64_MAX) {
-        const uint32_t target = D.agg[D.col[first]];
-        __syncthreads();  // every thread has read the target before it is written
-        if (tid == 0) {
+      if (target != kUnaggregated) {
+        if (lane == 0) {
           blen(ag) = 0;
-          D.agg[seed] = target;
+          set_agg(seed, target);
           block(target)[blen(target)++] = (int32_t)seed;
         }
-        __syncthreads();
+        __syncwarp();
         ++st[3];
         helpers_clear();
         return;
       }
       if (D.aggressive) {
-        __syncthreads();
-        if (tid == 0) {
+        if (lane == 0) {
           blen(ag) = 0;
-          D.agg[seed] = kIsolated;
+          set_agg(seed, kIsolated);
         }
-        __syncthreads();
+        __syncwarp();
         ++st[4];
         helpers_clear();
         return;
@@ -879,41 +1044,52 @@ struct AggBlock {
   }
 };
 
-__global__ void __launch_bounds__(kAggBlockThreads) k_aggregate_block(AggDev D) {
-  __shared__ AggBlockShared sh;
+__global__ void __launch_bounds__(kAggCtaThreads) k_aggregate_cta(AggDev D, int *overflow) {
+  extern __shared__ __align__(16) unsigned char agg_smem[];
+  __shared__ AggCtaCtl ctl;
   const int64_t p = blockIdx.x;
   if (p >= D.nparts) return;  // the whole block leaves together
   const int64_t pb = part_begin(D.n, D.nparts, p), pe = part_begin(D.n, D.nparts, p + 1);
-  for (int64_t v = pb + threadIdx.x; v < pe; v += kAggBlockThreads) D.block_len[v] = 0;
+  const int64_t P = pe - pb;
+  AggCta S(D, &ctl, pb, pe, agg_smem);
+  for (int64_t u = threadIdx.x; u < P; u += kAggCtaThreads) {
+    S.sagg[u] = kSUnagg;
+    D.block_len[pb + u] = 0;
+  }
+  for (int64_t w = threadIdx.x; w < 2 * agg_bit_words(P); w += kAggCtaThreads) S.inF[w] = 0u;
   if (threadIdx.x == 0) {
-    sh.front_len = 0;
-    sh.conn_len = 0;
+    ctl.cmd = kCmdGrow;
+    ctl.bad = 0;
   }
   __syncthreads();
-  AggBlock B(D, sh, pb, pe);
-  for (int64_t v = pb; v < pe; ++v) B.handle(v);
-  if (threadIdx.x == 0) {
-    D.pcount[p] = B.counter;
-    B.st[0] = B.counter;
-    for (int k = 0; k < 5; ++k)
-      if (B.st[k]) atomicAdd((unsigned long long *)&D.stats[k], (unsigned long long)B.st[k]);
+  if (threadIdx.x < 32) {
+    for (int64_t v = pb; v < pe && !S.bad; ++v) S.handle(v);
+    if (S.lane == 0) {
+      ctl.cmd = kCmdDone;
+      ctl.bad = S.bad;
+      ctl.ag = (uint32_t)S.counter;
+    }
+    agg_cta_sync();  // releases the other warps for good
+  } else {
+    // one evaluation per round; warp 0 says when the partition is done
+    for (;;) {
+      agg_cta_sync();
+      if (ctl.cmd == kCmdDone) break;
+      S.eval_part();
+      agg_cta_sync();
+    }
   }
-}
-
-__global__ void __launch_bounds__(32 * kAggWarpsPerBlock) k_aggregate(AggDev D) {
-  const int64_t p = (int64_t)blockIdx.x * kAggWarpsPerBlock + (threadIdx.x >> 5);
-  if (p >= D.nparts) return;  // whole warps leave together
-  const int64_t pb = part_begin(D.n, D.nparts, p), pe = part_begin(D.n, D.nparts, p + 1);
-  const int lane = threadIdx.x & 31;
-  for (int64_t v = pb + lane; v < pe; v += 32) D.block_len[v] = 0;
-  __syncwarp();
-  AggWarp W(D, pb, pe);
-  for (int64_t v = pb; v < pe; ++v) W.handle(v);
-  if (lane == 0) {
-    D.pcount[p] = W.counter;
-    W.st[0] = W.counter;
+  __syncthreads();
+  if (ctl.bad) {
+    if (threadIdx.x == 0) atomicExch(overflow, 1);
+    return;
+  }
+  for (int64_t u = threadIdx.x; u < P; u += kAggCtaThreads) D.agg[pb + u] = S.agg_of(pb + u);
+  if (threadIdx.x == 0) {
+    D.pcount[p] = S.counter;
+    S.st[0] = S.counter;
     for (int k = 0; k < 5; ++k)
-      if (W.st[k]) atomicAdd((unsigned long long *)&D.stats[k], (unsigned long long)W.st[k]);
+      if (S.st[k]) atomicAdd((unsigned long long *)&D.stats[k], (unsigned long long)S.st[k]);
   }
 }
 
@@ -964,17 +1140,36 @@ __global__ void k_agg_lists(AggDev D, const int64_t *poff, int64_t nc, const int
   }
 }
 
-// One CTA per partition where the partitions are few (at most 64), one warp
-// per partition otherwise.  Measured at 256^3 (levels 1-4: 175, 17, 8, 8
-// partitions): warp 154 / 744 / 288 / 45 ms, block 159 / 690 / 272 / 44 ms
-// -- the sequential chain of dependent steps per aggregate, not the front
-// evaluation, bounds both.  LGX_AGG_BLOCK=0 / 1 forces the warp / block
-// kernel (the tests run both against the oracle).
-static bool agg_block_kernel(int64_t nparts) {
-  const char *e = std::getenv("LGX_AGG_BLOCK");
-  if (e && e[0] == '0') return false;
-  if (e && e[0] == '1') return true;
-  return nparts <= 64;
+// Kernel choice.  Levels with few partitions (at most four per SM) whose
+// state fits in shared memory with lists of at least kAggCtaCapMin entries
+// take k_aggregate_cta, every partition of the level resident at once;
+// otherwise one warp per partition (the finest level: thousands of small
+// partitions).  Measured at 256^3 (levels 1-4: 175, 17, 8, 8 partitions of
+// 16k, 66k, 27k, 5k vertices, rows of ~50-150 entries) the warp kernel
+// takes 154 / 744 / 288 / 45 ms, three fifths of it evaluating fronts of
+// ~13 members one long row per lane.  LGX_AGG_KERNEL=warp / cta forces a
+// kernel (the tests run both against the oracle; a forced cta choice whose
+// partitions do not fit runs the warp kernel); LGX_AGG_CTA_CAP lowers the
+// list capacity so that tests reach the overflow path on small cases.
+//
+// Capacity of the CTA kernel's lists for a level, 0 where it does not fit:
+// the shared memory of an SM is shared by the partitions it must hold at
+// once (1 KB of it reserved per CTA).
+static int32_t agg_cta_cap(int64_t n, int64_t nparts, int64_t smem_optin, int64_t smem_sm,
+                           int64_t sms, bool forced) {
+  const int64_t pmax = (n + nparts - 1) / nparts;
+  const int64_t per_sm = (nparts + sms - 1) / sms;
+  const int64_t budget =
+    std::min<int64_t>(smem_optin, smem_sm / per_sm - 1024 - (int64_t)sizeof(AggCtaCtl));
+  const int64_t avail = budget - agg_cta_base(pmax) - 16;
+  int64_t cap = std::min<int64_t>(kAggCtaCapMax, avail > 0 ? avail / 34 / 8 * 8 : 0);
+  if (const char *e = std::getenv("LGX_AGG_CTA_CAP")) {
+    const long v = std::strtol(e, nullptr, 10);
+    if (v >= 8) cap = std::min<int64_t>(cap, v / 8 * 8);
+  }
+  if (cap < 8 || agg_cta_bytes(pmax, cap) > budget) return 0;
+  if (!forced && (cap < kAggCtaCapMin || nparts > 4 * sms)) return 0;
+  return (int32_t)cap;
 }
 
 lgx_status aggregate(const Csr &a, const uint8_t *dep, const uint8_t *inf, const uint8_t *iso,
@@ -991,39 +1186,68 @@ lgx_status aggregate(const Csr &a, const uint8_t *dep, const uint8_t *inf, const
     LGX_CHECK(out.agg.alloc(n));
     agg = out.agg.p;
   }
-  DBuf<int32_t> front, front_pos, conn, blocks, blen, eval, conn_flag32;
+  int dev = 0, sms = 1, smem_optin = 0, smem_sm = 0;
+  LGX_CUDA(cudaGetDevice(&dev));
+  LGX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  LGX_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  LGX_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+  const char *force = std::getenv("LGX_AGG_KERNEL");
+  const bool want_warp = force && std::strcmp(force, "warp") == 0;
+  const bool forced_cta = force && std::strcmp(force, "cta") == 0;
+  const int32_t cap =
+    n > 0 && !want_warp ? agg_cta_cap(n, nparts, smem_optin, smem_sm, sms, forced_cta) : 0;
+  DBuf<int32_t> front, front_pos, conn, blocks, blen, eval;
   DBuf<uint8_t> conn_flag;
-  const bool use_block = agg_block_kernel(nparts);
   DBuf<int64_t> pcount, poff, stats, glen;
-  LGX_CHECK(front.alloc(n));
-  LGX_CHECK(front_pos.alloc(n));
-  LGX_CHECK(conn.alloc(n));
-  LGX_CHECK(conn_flag.alloc(n));
   LGX_CHECK(blocks.alloc(n * max_size));
   LGX_CHECK(blen.alloc(n));
-  LGX_CHECK(eval.alloc(4 * n));
   LGX_CHECK(pcount.alloc(nparts));
   LGX_CHECK(poff.alloc(nparts + 1));
   LGX_CHECK(stats.alloc(5));
-  LGX_CUDA(cudaMemsetAsync(agg, 0xFF, sizeof(uint32_t) * std::max<int64_t>(n, 1), s));
-  LGX_CUDA(cudaMemsetAsync(front_pos.p, 0xFF, sizeof(int32_t) * std::max<int64_t>(n, 1), s));
-  LGX_CUDA(cudaMemsetAsync(conn_flag.p, 0, std::max<int64_t>(n, 1), s));
-  if (use_block) {
-    LGX_CHECK(conn_flag32.alloc(n));
-    LGX_CUDA(cudaMemsetAsync(conn_flag32.p, 0, sizeof(int32_t) * std::max<int64_t>(n, 1), s));
-  }
   LGX_CUDA(cudaMemsetAsync(stats.p, 0, sizeof(int64_t) * 5, s));
-  AggDev D{a.rowptr.p, a.col.p,     dep,     inf,         iso,      agg,    n,
-           nparts,     min_size,    max_size, aggressive, front.p, front_pos.p, conn.p,
-           conn_flag.p, blocks.p,   blen.p,   eval.p,     pcount.p, stats.p,
-           conn_flag32.p};
-  if (n > 0) {
-    if (use_block)
-      k_aggregate_block<<<(unsigned)nparts, kAggBlockThreads, 0, s>>>(D);
-    else
-      k_aggregate<<<grid_for(nparts, kAggWarpsPerBlock), 32 * kAggWarpsPerBlock, 0, s>>>(D);
+  LGX_CUDA(cudaMemsetAsync(pcount.p, 0, sizeof(int64_t) * nparts, s));
+  AggDev D{a.rowptr.p, a.col.p,  dep,      inf,        iso,     agg,    n,
+           nparts,     min_size, max_size, aggressive, nullptr, nullptr, nullptr,
+           nullptr,    blocks.p, blen.p,   nullptr,    pcount.p, stats.p, cap};
+  bool done = n == 0;
+  if (cap > 0) {
+    const int bytes = (int)agg_cta_bytes((n + nparts - 1) / nparts, cap);
+    DBuf<int> overflow;
+    LGX_CHECK(overflow.alloc(1));
+    LGX_CUDA(cudaMemsetAsync(overflow.p, 0, sizeof(int), s));
+    LGX_CUDA(cudaFuncSetAttribute(k_aggregate_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  bytes));
+    k_aggregate_cta<<<(unsigned)nparts, kAggCtaThreads, bytes, s>>>(D, overflow.p);
+    LGX_LAUNCH_CHECK();
+    int of = 0;
+    LGX_CUDA(cudaMemcpyAsync(&of, overflow.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    LGX_CUDA(cudaStreamSynchronize(s));
+    done = of == 0;
+    // a partition outgrew a capacity: the warp kernel redoes the level
+    if (!done) LGX_CUDA(cudaMemsetAsync(stats.p, 0, sizeof(int64_t) * 5, s));
+  }
+  if (!done) {
+    LGX_CHECK(front.alloc(n));
+    LGX_CHECK(front_pos.alloc(n));
+    LGX_CHECK(conn.alloc(n));
+    LGX_CHECK(conn_flag.alloc(n));
+    LGX_CHECK(eval.alloc(4 * n));
+    LGX_CUDA(cudaMemsetAsync(agg, 0xFF, sizeof(uint32_t) * n, s));
+    LGX_CUDA(cudaMemsetAsync(front_pos.p, 0xFF, sizeof(int32_t) * n, s));
+    LGX_CUDA(cudaMemsetAsync(conn_flag.p, 0, n, s));
+    D.front = front.p;
+    D.front_pos = front_pos.p;
+    D.conn = conn.p;
+    D.conn_flag = conn_flag.p;
+    D.eval = eval.p;
+    k_aggregate<<<grid_for(nparts, kAggWarpsPerBlock), 32 * kAggWarpsPerBlock, 0, s>>>(D);
     LGX_LAUNCH_CHECK();
   }
+  if (std::getenv("LGX_VERBOSE") && n > 0)
+    std::fprintf(stderr, "[lgx setup] aggregation of %lld rows in %lld partitions: %s\n",
+                 (long long)n, (long long)nparts,
+                 cap > 0 ? (done ? "CTA kernel" : "CTA kernel overflowed, warp kernel")
+                         : "warp kernel");
   LGX_CHECK(inclusive_offsets(nparts, pcount.p, poff.p, s));
   int64_t nc = 0;
   LGX_CUDA(cudaMemcpyAsync(&nc, poff.p + nparts, sizeof(int64_t), cudaMemcpyDeviceToHost, s));

@@ -39,10 +39,11 @@ def test_strength_bitexact(cuda, golden_dir, which):
     np.testing.assert_array_equal(iso.cpu().numpy(), riso)
 
 
-@pytest.fixture(params=["warp", "block"])
+@pytest.fixture(params=["warp", "cta"])
 def agg_kernel(request, monkeypatch):
-    """Both aggregation kernels: one warp per partition, one CTA per partition."""
-    monkeypatch.setenv("LGX_AGG_BLOCK", "1" if request.param == "block" else "0")
+    """Both aggregation kernels: one warp per partition with its state in
+    global memory, one CTA per partition with its state in shared memory."""
+    monkeypatch.setenv("LGX_AGG_KERNEL", request.param)
     return request.param
 
 
@@ -86,6 +87,30 @@ def test_aggregation_ufz_bitexact(cuda, golden_dir, agg_kernel):
     rnc, ragg, _, _, _ = lo.amg_aggregate(ref, rdep, rinf, riso, 6, 9, 4)
     assert nc == rnc
     np.testing.assert_array_equal(agg, ragg)
+
+
+@pytest.mark.parametrize("case", ["front", "ids"])
+def test_aggregation_beyond_shared_capacity(cuda, agg_kernel, monkeypatch, case):
+    """Partitions that outgrow the CTA kernel's capacities -- a front or
+    connected set longer than the list capacity (lowered to 64 entries;
+    27-point rows and aggregates of up to 9 vertices reach ~100),
+    more than 65533 aggregates in one partition (70k vertices, aggregates of
+    one) -- are redone in global memory: the result is the oracle's for
+    every kernel choice."""
+    if case == "front":
+        monkeypatch.setenv("LGX_AGG_CTA_CAP", "64")
+        ref, lo_size, hi_size = _case(), 6, 9
+    else:
+        ref, lo_size, hi_size = _case((40, 42, 42), npts=7), 1, 1
+    m = _dev(cuda, ref)
+    dep, inf, iso = cuda.amg_strength(m)
+    nc, agg = cuda.amg_aggregate(m, dep, inf, iso, lo_size, hi_size, 1)
+    rdep, rinf, riso = lo.amg_strength(ref)
+    rnc, ragg, _, _, _ = lo.amg_aggregate(ref, rdep, rinf, riso, lo_size, hi_size, 1)
+    assert nc == rnc
+    np.testing.assert_array_equal(agg, ragg)
+    if case == "ids":
+        assert nc > 65533
 
 
 PARAMS = dict(min_coarsen_size=64, partition_size=512, max_partitions=1 << 30)
