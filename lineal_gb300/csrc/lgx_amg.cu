@@ -537,29 +537,30 @@ __global__ void __launch_bounds__(32 * kAggWarpsPerBlock) k_aggregate(AggDev D) 
 // ---------------------------------------------------------------------------
 // The same aggregation with one CTA per partition and the partition's
 // mutable state in shared memory, for levels with few, large partitions (the
-// coarse levels: 8 to a few hundred partitions of 5k-70k vertices and rows
-// of 50-300 entries).  There the front of an aggregate is short (10-20
-// vertices on average) but its rows are long, so evaluating it vertex by
-// vertex leaves most lanes idle behind one long row each.  Here:
-//  - warp 0 runs the sequential steps of the warp kernel (add a vertex,
-//    update the front and connected set, choose, pick) on shared memory:
-//    the aggregate ids (16 bits per vertex), front and connected flags (one
-//    bit per vertex / local aggregate), the front list with each member's
-//    row offset and length, the connected list;
+// coarse levels: 8 to a few hundred partitions of 5k-70k vertices, rows of
+// ~20 entries).  The aggregates of a partition form one sequential chain of
+// dependent steps, so the kernel shortens the steps:
+//  - warp 0 runs the warp kernel's sequential steps (add a vertex, update
+//    the front and connected set, choose, pick) on shared memory: the
+//    aggregate ids (16 bits per vertex), front and connected flags (one bit
+//    per vertex / local aggregate), the front list with each member's row
+//    offset and length (loaded once, when it joins), the connected list;
 //  - each evaluation of the front (grow_aggregate's counts, round_
-//    aggregate's test) is spread over the whole CTA as one flat range of
-//    (front vertex, edge) items: prefix sums of the members' row lengths
-//    map item k to its member, the items' strength bytes and columns load
-//    together, and per-member counts form by a segmented warp reduction and
-//    a shared-memory atomic per warp segment.  Warps 1.. wait between
-//    evaluations at a named barrier that warp 0 releases.
-// Decisions are the warp kernel's: counts are order-free sums, selections
-// take the smallest vertex ids, a member's position is found by search, and
-// every aggregate's vertices are added in the same order.  Capacities: local
-// aggregate ids below 0xFFFE, rows below 65536 entries (counts are packed
-// in 16-bit halves), front and connected lists within `cap` entries; a
-// partition that exceeds one sets `overflow` and the host redoes the level
-// with the warp kernel.
+//    aggregate's test) is spread over the CTA, one warp per member, so the
+//    members' rows load at once and each count is one warp reduction;
+//    warps 1.. wait between evaluations at a named barrier that warp 0
+//    releases;
+//  - choices are integer reductions (redux.sync) over 32-bit vertex ids
+//    and a 64-bit key.
+// Measured at 256^3 against the warp kernel: levels 1-3 (174, 17, 8
+// partitions) 153 / 754 / 268 ms before, with 60 % of it evaluating fronts
+// of ~13 members one row per lane.  Decisions are the warp kernel's:
+// counts are order-free sums, selections take the smallest vertex ids, a
+// member's position is found by search, and every aggregate's vertices are
+// added in the same order.  Capacities: local aggregate ids below 0xFFFE,
+// rows below 65536 entries (counts are packed in 16-bit halves), front and
+// connected lists within `cap` entries; a partition that exceeds one sets
+// `overflow` and the host redoes the level with the warp kernel.
 // ---------------------------------------------------------------------------
 constexpr int kAggCtaThreads = 256;
 constexpr int kAggCtaCapMax = 4096;
@@ -571,17 +572,16 @@ __host__ __device__ inline int64_t agg_align16(int64_t b) { return (b + 15) / 16
 __host__ __device__ inline int64_t agg_bit_words(int64_t P) { return (P + 31) / 32; }
 // shared bytes of a partition of P vertices with list capacity cap (a
 // multiple of 8): aggregate ids, two bit sets, then per list entry the row
-// offset (8), member, row length, two counters (4 each), connected id (2),
-// plus cap + 1 prefix sums
+// offset (8), member, row length, two counters (4 each), connected id (2)
 __host__ __device__ inline int64_t agg_cta_base(int64_t P) {
   return agg_align16(2 * P) + agg_align16(8 * agg_bit_words(P));
 }
 __host__ __device__ inline int64_t agg_cta_bytes(int64_t P, int64_t cap) {
-  return agg_cta_base(P) + 30 * cap + agg_align16(4 * (cap + 1));
+  return agg_cta_base(P) + 30 * cap;
 }
 
 struct AggCtaCtl {
-  int32_t cmd, nfront, total, bad;
+  int32_t cmd, nfront, bad;
   uint32_t ag;
 };
 
@@ -603,7 +603,6 @@ struct AggCta {
   int32_t *front;   // per front position: member (vertex id); unordered
   int32_t *flen;    // per front position: row length, 0 for isolated members
   uint32_t *cntA, *cntB;  // per front position: packed 16-bit counts / mark
-  int32_t *psum;    // prefix sums of flen over positions (nfront + 1)
   uint16_t *conn;   // connected local aggregate ids
   // warp 0's state (warp-uniform)
   int64_t front_len = 0, conn_len = 0, counter = 0;
@@ -627,8 +626,7 @@ struct AggCta {
     flen = front + cap;
     cntA = (uint32_t *)(flen + cap);
     cntB = cntA + cap;
-    psum = (int32_t *)(cntB + cap);
-    q += 16 * (int64_t)cap + agg_align16(4 * (cap + 1));
+    q += 16 * (int64_t)cap;
     conn = (uint16_t *)q;
   }
   __device__ bool in_range(int64_t v) const { return v >= pb && v < pe; }
@@ -659,76 +657,62 @@ struct AggCta {
   }
 
   // ---- the CTA-wide evaluation (every thread) ----
-  // item k of [0, total) -> front position i with psum[i] <= k < psum[i + 1]
-  __device__ int32_t member_of(int32_t k, int32_t nf) const {
-    int32_t lo = 0, hi = nf;
-    while (lo < hi) {
-      const int32_t mid = (lo + hi) >> 1;
-      if (psum[mid + 1] <= k) lo = mid + 1;
-      else hi = mid;
-    }
-    return lo;
-  }
-
+  // Warp w counts the members w, w + W, ... (W warps), two at a time with
+  // their loads in flight together; the lanes cover a member's row.
   __device__ void eval_part() const {
+    constexpr int W = kAggCtaThreads / 32;
     const int cmd = ctl->cmd;
-    const int32_t nf = ctl->nfront, total = ctl->total;
+    const int32_t nf = ctl->nfront;
     const uint32_t ag = ctl->ag;
-    constexpr int U = 4;
-    for (int32_t kb = 0; kb < total; kb += U * kAggCtaThreads) {
-      int32_t mi[U];
-      int64_t e[U] = {};
-      int32_t t[U] = {};
-      uint8_t dp[U] = {}, nf_[U] = {};
+    const int32_t warp = (int32_t)(threadIdx.x >> 5);
+    for (int32_t m0 = warp; m0 < nf; m0 += 2 * W) {
+      int32_t mm[2] = {m0, m0 + W};
+      int64_t eb[2];
+      int32_t len[2], self[2];
 #pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int32_t k = kb + u * kAggCtaThreads + (int32_t)threadIdx.x;
-        mi[u] = -1;
-        if (k < total) {
-          mi[u] = member_of(k, nf);
-          e[u] = fbeg[mi[u]] + (k - psum[mi[u]]);
-        }
+      for (int j = 0; j < 2; ++j) {
+        const bool ok = mm[j] < nf;
+        eb[j] = ok ? fbeg[mm[j]] : 0;
+        len[j] = ok ? flen[mm[j]] : 0;
+        self[j] = ok ? front[mm[j]] : -1;
       }
+      const int32_t most = len[0] > len[1] ? len[0] : len[1];
+      uint32_t a[2] = {0, 0}, b[2] = {0, 0};
+      for (int32_t o = lane; o - lane < most; o += 32) {
+        int32_t t[2];
+        uint8_t dp[2], nf_[2];
 #pragma unroll
-      for (int u = 0; u < U; ++u) {
-        if (mi[u] >= 0) {
-          t[u] = D.col[e[u]];
-          dp[u] = D.dep[e[u]];
-          nf_[u] = cmd == kCmdGrow ? D.inf[e[u]] : 0;
+        for (int j = 0; j < 2; ++j) {
+          t[j] = -1;
+          dp[j] = nf_[j] = 0;
+          if (o < len[j]) {
+            const int64_t e = eb[j] + o;
+            t[j] = D.col[e];
+            dp[j] = D.dep[e];
+            nf_[j] = cmd == kCmdGrow ? D.inf[e] : 0;
+          }
         }
-      }
 #pragma unroll
-      for (int u = 0; u < U; ++u) {
-        uint32_t a = 0, b = 0;
-        if (mi[u] >= 0 && t[u] != front[mi[u]] && in_range(t[u])) {
-          const uint32_t ha = agg_of(t[u]);
+        for (int j = 0; j < 2; ++j) {
+          if (t[j] < 0 || t[j] == self[j] || !in_range(t[j])) continue;
+          const uint32_t ha = agg_of(t[j]);
           if (cmd == kCmdGrow) {
             // (two-way, one-way) counts into the aggregate | (connected, in front)
-            a = (ha == ag && dp[u] && nf_[u]) | (uint32_t)(ha == ag && dp[u] && !nf_[u]) << 16;
-            b = (ha < kIsolated && connected(ha)) | (uint32_t)in_front(t[u]) << 16;
+            a[j] += (ha == ag && dp[j] && nf_[j]) | (uint32_t)(ha == ag && dp[j] && !nf_[j]) << 16;
+            b[j] += (ha < kIsolated && connected(ha)) | (uint32_t)in_front(t[j]) << 16;
           } else {
             // (dependent edges into the aggregate | edges into it), unaggregated
-            a = (ha == ag && dp[u]) | (uint32_t)(ha == ag) << 16;
-            b = ha == kUnaggregated;
+            a[j] += (ha == ag && dp[j]) | (uint32_t)(ha == ag) << 16;
+            b[j] += ha == kUnaggregated;
           }
         }
-        // lanes hold consecutive items, so equal members form contiguous
-        // segments: sum each onto its first lane
-        const int32_t m = mi[u];
+      }
 #pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-          const uint32_t oa = __shfl_down_sync(kFull, a, d);
-          const uint32_t ob = __shfl_down_sync(kFull, b, d);
-          const int32_t om = __shfl_down_sync(kFull, m, d);
-          if (lane + d < 32 && om == m) {
-            a += oa;
-            b += ob;
-          }
-        }
-        const int32_t prev = __shfl_up_sync(kFull, m, 1);
-        if (m >= 0 && (lane == 0 || prev != m) && (a | b)) {
-          atomicAdd(&cntA[m], a);
-          atomicAdd(&cntB[m], b);
+      for (int j = 0; j < 2; ++j) {
+        const uint32_t sa = __reduce_add_sync(kFull, a[j]), sb = __reduce_add_sync(kFull, b[j]);
+        if (lane == 0 && mm[j] < nf) {
+          cntA[mm[j]] = sa;
+          cntB[mm[j]] = sb;
         }
       }
     }
@@ -737,27 +721,9 @@ struct AggCta {
   // warp 0: counts of every front member into cntA / cntB, the whole CTA
   // taking part
   __device__ void eval(int cmd, uint32_t ag) {
-    int32_t run = 0;
-    for (int64_t base = 0; base < front_len; base += 32) {
-      const int64_t i = base + lane;
-      const int32_t len = i < front_len ? flen[i] : 0;
-      int32_t x = len;
-      for (int d = 1; d < 32; d <<= 1) {
-        const int32_t y = __shfl_up_sync(kFull, x, d);
-        if (lane >= d) x += y;
-      }
-      if (i < front_len) {
-        psum[i + 1] = run + x;
-        cntA[i] = 0;
-        cntB[i] = 0;
-      }
-      run += __shfl_sync(kFull, x, 31);
-    }
     if (lane == 0) {
-      psum[0] = 0;
       ctl->cmd = cmd;
       ctl->nfront = (int32_t)front_len;
-      ctl->total = run;
       ctl->ag = ag;
     }
     agg_cta_sync();  // releases the other warps
@@ -770,11 +736,13 @@ struct AggCta {
   // in-range neighbours update the connected set and the front, new front
   // members get their row offsets and lengths
   __device__ void add_help(int64_t v, uint32_t ag, int64_t &size, int64_t eb, int64_t ee) {
-    ++size;
+    // the aggregate's list holds its `size` vertices so far
     if (lane == 0) {
       set_agg(v, ag);
-      block(ag)[blen(ag)++] = (int32_t)v;
+      block(ag)[size] = (int32_t)v;
+      blen(ag) = (int32_t)(size + 1);
     }
+    ++size;
     __syncwarp();
     const int64_t f0 = front_len;
     for (int64_t base = eb; base < ee; base += 128) {
@@ -835,19 +803,17 @@ struct AggCta {
 
   // removes front member v; returns its row
   __device__ void front_take(int64_t v, int64_t &eb, int64_t &ee) {
-    int64_t pos = -1;
+    uint32_t pos1 = 0;  // position + 1
     for (int64_t i = lane; i < front_len; i += 32)
-      if (front[i] == (int32_t)v) pos = i;
-    for (int o = 16; o > 0; o >>= 1) {
-      const int64_t other = __shfl_xor_sync(kFull, pos, o);
-      pos = other > pos ? other : pos;
-    }
-    // v was picked from the front, so pos >= 0 (guarded all the same)
-    if (pos < 0) {
+      if (front[i] == (int32_t)v) pos1 = (uint32_t)i + 1;
+    pos1 = __reduce_max_sync(kFull, pos1);
+    // v was picked from the front, so it is there (guarded all the same)
+    if (pos1 == 0) {
       bad = true;
       eb = ee = 0;
       return;
     }
+    const int64_t pos = pos1 - 1;
     eb = fbeg[pos];
     ee = eb + flen[pos];
     __syncwarp();
@@ -870,76 +836,78 @@ struct AggCta {
     __syncwarp();
   }
 
-  // smallest member id > floor among the marked positions (mark in cntA)
-  __device__ int64_t warp_min_marked(int64_t floor) const {
-    int64_t best = INT64_MAX;
+  // smallest member id > floor among the marked positions (mark in cntA);
+  // vertex ids are below 2^31
+  __device__ uint32_t warp_min_marked(uint32_t floor) const {
+    uint32_t best = 0xFFFFFFFFu;
     for (int64_t i = lane; i < front_len; i += 32) {
-      if (!cntA[i]) continue;
-      const int64_t v = front[i];
-      if (v > floor && v < best) best = v;
+      const uint32_t v = (uint32_t)front[i];
+      if (cntA[i] && (floor == 0xFFFFFFFFu || v > floor) && v < best) best = v;
     }
-    for (int o = 16; o > 0; o >>= 1) {
-      const int64_t other = __shfl_xor_sync(kFull, best, o);
-      best = other < best ? other : best;
-    }
-    return best;
+    return __reduce_min_sync(kFull, best);
   }
 
-  // grow_aggregate (base.hpp:532-585)
+  // grow_aggregate (base.hpp:532-585).  A member's key is (count,
+  // connectivity, front neighbours) with connectivity = connected / (row
+  // length - 1) compared as doubles.  Here it is one 64-bit integer:
+  // count << 48 | floor(connected * (2^32 - 1) / (row length - 1)) << 16 |
+  // neighbours.  Distinct fractions with denominators below 2^16 differ by
+  // more than 1 / (2^32 - 1), so the scaled floors order and tie exactly as
+  // the fractions -- and as their correctly rounded quotients, which lie
+  // much closer than that apart only when equal.  Rows without a diagonal
+  // (a connected count above the denominator, or a zero denominator) are
+  // left to the warp kernel.
   __device__ void grow(uint32_t ag, int64_t &size) {
     while (size < D.min_size && front_len > 0) {
       eval(kCmdGrow, ag);
       bool any2 = false;
       for (int64_t i = lane; i < front_len; i += 32) any2 = any2 || (cntA[i] & 0xFFFFu) != 0;
       const bool mode2 = __any_sync(kFull, any2);
-      int32_t k0 = 0, kn = 0;
-      double kc = 0.0;
-      bool have = false;
+      bool odd = false;
+      uint64_t kmax = 0;
       for (int64_t i = lane; i < front_len; i += 32) {
-        const int32_t c = (int32_t)(mode2 ? cntA[i] & 0xFFFFu : cntA[i] >> 16);
-        if (c <= 0) continue;
-        const double con = (double)(cntB[i] & 0xFFFFu) / (double)(flen[i] - 1);
-        const int32_t nb = (int32_t)(cntB[i] >> 16);
-        if (!have || c > k0 || (c == k0 && (con > kc || (con == kc && nb > kn)))) {
-          k0 = c;
-          kc = con;
-          kn = nb;
-          have = true;
-        }
-      }
-      for (int o = 16; o > 0; o >>= 1) {
-        const int32_t o0 = __shfl_xor_sync(kFull, k0, o);
-        const double oc = __shfl_xor_sync(kFull, kc, o);
-        const int32_t on = __shfl_xor_sync(kFull, kn, o);
-        const bool oh = __shfl_xor_sync(kFull, have, o);
-        if (oh && (!have || o0 > k0 || (o0 == k0 && (oc > kc || (oc == kc && on > kn))))) {
-          k0 = o0;
-          kc = oc;
-          kn = on;
-          have = true;
-        }
-      }
-      if (!have) break;
-      // mark the members whose key equals the maximum (cntA becomes the mark)
-      for (int64_t i = lane; i < front_len; i += 32) {
-        const int32_t c = (int32_t)(mode2 ? cntA[i] & 0xFFFFu : cntA[i] >> 16);
-        bool m = false;
+        const uint32_t c = mode2 ? cntA[i] & 0xFFFFu : cntA[i] >> 16;
+        uint64_t key = 0;
         if (c > 0) {
-          const double con = (double)(cntB[i] & 0xFFFFu) / (double)(flen[i] - 1);
-          m = c == k0 && con == kc && (int32_t)(cntB[i] >> 16) == kn;
+          const uint64_t con = cntB[i] & 0xFFFFu, nb = cntB[i] >> 16;
+          const uint64_t den = (uint64_t)(flen[i] - 1);
+          if (den == 0 || con > den) {
+            odd = true;
+          } else {
+            key = (uint64_t)c << 48 | (con * 0xFFFFFFFFull / den) << 16 | nb;
+          }
         }
-        cntA[i] = m;
+        cntA[i] = (uint32_t)(key >> 32);
+        cntB[i] = (uint32_t)key;
+        kmax = key > kmax ? key : kmax;
+      }
+      if (__any_sync(kFull, odd)) {
+        bad = true;
+        return;
+      }
+      const uint32_t khi = __reduce_max_sync(kFull, (uint32_t)(kmax >> 32));
+      const uint32_t klo =
+        __reduce_max_sync(kFull, (uint32_t)(kmax >> 32) == khi ? (uint32_t)kmax : 0u);
+      if (khi == 0 && klo == 0) break;  // no candidates
+      // mark the members whose key equals the maximum (cntA becomes the mark)
+      int64_t nmarked = 0;
+      for (int64_t base = 0; base < front_len; base += 32) {
+        const int64_t i = base + lane;
+        bool m = false;
+        if (i < front_len) {
+          m = cntA[i] == khi && cntB[i] == klo;
+          cntA[i] = m;
+        }
+        nmarked += __popc(__ballot_sync(kFull, m));
       }
       __syncwarp();
       const int64_t room = D.max_size - size;
-      int64_t floor = -1;
-      int64_t picked[64];
-      int64_t npick = 0;
-      for (int64_t k = 0; k < room; ++k) {
-        const int64_t v = warp_min_marked(floor);
-        if (v == INT64_MAX) break;
-        picked[npick++] = v;
-        floor = v;
+      const int64_t npick = nmarked < room ? nmarked : room;
+      uint32_t picked[64];
+      uint32_t floor = 0xFFFFFFFFu;
+      for (int64_t k = 0; k < npick; ++k) {
+        floor = warp_min_marked(floor);
+        picked[k] = floor;
       }
       for (int64_t k = 0; k < npick; ++k) {
         int64_t eb, ee;
@@ -955,17 +923,14 @@ struct AggCta {
   __device__ void round(uint32_t ag, int64_t &size) {
     while (size < D.max_size && front_len > 0) {
       eval(kCmdRound, ag);
-      int64_t best = INT64_MAX;
+      uint32_t best = 0xFFFFFFFFu;
       for (int64_t i = lane; i < front_len; i += 32) {
         const uint32_t cons = cntA[i] & 0xFFFFu, inagg = cntA[i] >> 16, unagg = cntB[i];
         if (cons == 0 || unagg >= inagg) continue;
-        best = front[i] < best ? front[i] : best;
+        best = (uint32_t)front[i] < best ? (uint32_t)front[i] : best;
       }
-      for (int o = 16; o > 0; o >>= 1) {
-        const int64_t other = __shfl_xor_sync(kFull, best, o);
-        best = other < best ? other : best;
-      }
-      if (best == INT64_MAX) break;
+      best = __reduce_min_sync(kFull, best);
+      if (best == 0xFFFFFFFFu) break;
       int64_t eb, ee;
       front_take(best, eb, ee);
       if (bad) return;
@@ -977,7 +942,9 @@ struct AggCta {
   // handle_vertex (base.hpp:638-677)
   __device__ void handle(int64_t seed) {
     if (agg_of(seed) != kUnaggregated) return;
-    if (D.iso[seed]) {
+    const bool iso = D.iso[seed];
+    const int64_t eb = D.rowptr[seed], ee = D.rowptr[seed + 1];
+    if (iso) {
       if (lane == 0) set_agg(seed, kIsolated);
       __syncwarp();
       ++st[4];
@@ -989,7 +956,6 @@ struct AggCta {
     }
     const uint32_t ag = (uint32_t)counter;
     int64_t size = 0;
-    const int64_t eb = D.rowptr[seed], ee = D.rowptr[seed + 1];
     add_help(seed, ag, size, eb, ee);
     if (bad) return;
     grow(ag, size);
@@ -1162,7 +1128,7 @@ static int32_t agg_cta_cap(int64_t n, int64_t nparts, int64_t smem_optin, int64_
   const int64_t budget =
     std::min<int64_t>(smem_optin, smem_sm / per_sm - 1024 - (int64_t)sizeof(AggCtaCtl));
   const int64_t avail = budget - agg_cta_base(pmax) - 16;
-  int64_t cap = std::min<int64_t>(kAggCtaCapMax, avail > 0 ? avail / 34 / 8 * 8 : 0);
+  int64_t cap = std::min<int64_t>(kAggCtaCapMax, avail > 0 ? avail / 30 / 8 * 8 : 0);
   if (const char *e = std::getenv("LGX_AGG_CTA_CAP")) {
     const long v = std::strtol(e, nullptr, 10);
     if (v >= 8) cap = std::min<int64_t>(cap, v / 8 * 8);
