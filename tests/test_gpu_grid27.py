@@ -122,6 +122,36 @@ def test_standalone_colouring_grid_sweeps(cuda, forward):
     assert not cuda.Colouring.from_array(m7, _parity(dims), 8).use_grid27(dims)
 
 
+# Float values and vectors on grids whose colour blocks are whole 256-row
+# tiles run the staged kernel (bulk copies into shared memory, two stages
+# per CTA); these sizes give more tiles than CTAs, so CTAs also compute from
+# their second stage.  Every result equals the CSR kernels' bit for bit.
+@pytest.mark.parametrize("dims", [(48, 48, 48), (32, 64, 40)])
+def test_grid_float_staged_tiles_equal_csr(cuda, dims):
+    m = cuda.gen_27pt(dims, _k(dims, 12))
+    plain = cuda.Colouring.from_array(m, _parity(dims), 8)
+    grid = cuda.Colouring.from_array(m, _parity(dims), 8)
+    assert grid.use_grid27(dims, with_float=True)
+    rng = np.random.default_rng(13)
+    b = cuda.permute(plain, rng.uniform(-1, 1, m.row_num())).float()
+    x0 = cuda.permute(plain, rng.uniform(-1, 1, m.row_num())).float()
+    for forward in (1, 0):
+        xa, xb = x0.clone(), x0.clone()
+        cuda.sor_sweep_permuted(plain, b, xa, forward=forward)
+        cuda.sor_sweep_permuted(grid, b, xb, forward=forward)
+        np.testing.assert_array_equal(xa.cpu().numpy(), xb.cpu().numpy())
+    hg, hc = _pair(cuda, m, dims, cycle_f32=True)
+    assert hg.grid27_active()
+    bb = np.random.default_rng(14).uniform(-1, 1, m.row_num())
+    np.testing.assert_array_equal(hg.vcycle(bb).cpu().numpy(), hc.vcycle(bb).cpu().numpy())
+    for refine in (0, 2):
+        kw = dict(refine=refine) if refine else dict(flexible=True)
+        rg = cuda.pcg(m, bb, precon=cuda.PRECON_AMG, amg=hg, rtol=1e-8, maxit=300, **kw)
+        rc = cuda.pcg(m, bb, precon=cuda.PRECON_AMG, amg=hc, rtol=1e-8, maxit=300, **kw)
+        assert rg.iterations == rc.iterations
+        np.testing.assert_array_equal(rg.x.cpu().numpy(), rc.x.cpu().numpy())
+
+
 def _red_black(dims):
     i, j, k = np.meshgrid(*[np.arange(d) for d in dims], indexing="ij")
     return ((i + j + k) % 2).ravel().astype(np.int32)
