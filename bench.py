@@ -392,7 +392,7 @@ def precision_form(g, args, stream):
     out["mixed_refined"]["what"] = (
         f"float-vector CG (refine {args.refine}, flexible beta) with FP64 residual "
         f"replacement every {args.precision_inner_rtol:g} reduction; float products and "
-        "V-cycle, FP64 dots and CG scalars")
+        "V-cycle, compensated dots and FP64 CG scalars")
     out["mixed_fcg"]["what"] = "flexible CG with FP64 vectors over the float V-cycle"
     for tag in ("mixed_fcg", "mixed_refined", "mixed_bf16_fcg"):
         out[tag]["rel_error_vs_fp64_solution"] = float(
@@ -502,7 +502,7 @@ def run_gb300(args):
     log(f"[gb300] mixed AMG-PCG {ms32:.1f} ms, {res32.iterations} it, rel {rel32:.2e}")
 
     # ---- mixed, FP64 iterative refinement over a float inner PCG (same float
-    # hierarchy): float products and V-cycles, FP64 dots, scalars, outer
+    # hierarchy): float products and V-cycles, compensated dots, FP64 scalars, outer
     # residual and stopping test
     def solve_refined(h):
         return g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=1e-8, maxit=500, refine=args.refine,
@@ -735,7 +735,7 @@ def run_gb300(args):
                                    "FP64 iterative refinement over a float-vector inner PCG, "
                                    "inner tolerance ") + f"{args.inner_rtol:g}" +
                                   (" reduction" if args.refine == 2 else "") +
-                                  "; float finest products and V-cycle, FP64 dots and CG "
+                                  "; float finest products and V-cycle, compensated dots and FP64 CG "
                                   "scalars", "refine": args.refine},
         "mixed_speedup_vs_fp64": ms64 / min(ms32, msr),
         "mixed_bf16": {"ms": ms16, "iterations": res16.iterations, "rel_residual_fp64": rel16,

@@ -1108,8 +1108,8 @@ def pcg(a: _Matrix, b, **kw) -> SolveResult:
     """Preconditioned CG (ConjugateGradientsSolver); flexible=True selects the
     flexible-CG beta for the float V-cycle of the precision form; refine=True
     (AMG hierarchy with cycle_f32) runs FP64 iterative refinement over a
-    float-vector PCG with FP64 dots and scalars, each inner solve to
-    inner_rtol."""
+    float-vector PCG with compensated dots and FP64 scalars, each inner
+    solve to inner_rtol."""
     return _solve(lib().lgx_pcg, a, b, **kw)
 
 

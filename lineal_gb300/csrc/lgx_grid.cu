@@ -429,17 +429,17 @@ __global__ void __launch_bounds__(256)
   for (int q = 0; q < R; ++q) row[q].finish(r0 + q, b, x, y, scale, so);
 }
 
-// ---- 27-point float rows with the values staged by the tensor engine ------
-// Float values and vectors on the 27-point grid: each CTA of kGT rows has
-// its rows' 27 value-plane segments (27 x kGT floats, one 2-D box of the
-// value array viewed as [27][stride]) brought into shared memory by one
+// ---- float grid rows with the values staged by the tensor engine ---------
+// Float values and vectors on the 27- and 7-point grids: each CTA of kGT
+// rows has its rows' value-plane segments (PTS x kGT floats, one 2-D box of
+// the value array viewed as [PTS][stride]) brought into shared memory by one
 // cp.async.bulk.tensor copy, issued before the kernel waits for its
-// predecessor (the values are constant); every thread then issues all its
-// 26 x gathers at once (x is written by other colours' launches and read
-// through the non-coherent path), waits for the copy (bounded) and runs
-// G27Row's arithmetic on the staged values, so results equal k_g27_rows
-// bit for bit.  The row-per-thread kernel has three value loads per round
-// in flight, nine rounds per row, and reaches 0.62 of HBM on a float sweep.
+// predecessor (the values are constant); every thread then issues all its x
+// gathers at once (x is written by other colours' launches and read through
+// the non-coherent path), waits for the copy (bounded) and runs G27Row's
+// arithmetic on the staged values, so results equal k_g27_rows bit for bit.
+// The row-per-thread kernel keeps three value loads per round in flight and
+// reaches 0.62 of HBM on a 27-point float sweep.
 constexpr int kGT = 256;  // rows per CTA
 
 __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int c0, int c1,
@@ -453,13 +453,13 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, i
 
 // FZ: a forward sweep from zero (x of the colours from visit_end on reads
 // as 0), a template argument so that other launches carry no per-entry test.
-// Rows whose 26 neighbours all lie inside the grid (all but the boundary
+// Rows whose neighbours all lie inside the grid (all but the boundary
 // layers) skip the per-entry inside tests.
-template <int MODE, bool FZ>
-__global__ void __launch_bounds__(kGT, 4)
+template <int MODE, bool FZ, int PTS>
+__global__ void __launch_bounds__(kGT, PTS == 27 ? 4 : 6)
   k_g27_vtma(const __grid_constant__ CUtensorMap vmap, G27 g, int64_t rb, int64_t re,
              const float *__restrict__ b, float *x, float *__restrict__ y, G27Sor so, int *err) {
-  __shared__ __align__(128) float sv[27 * kGT];
+  __shared__ __align__(128) float sv[PTS * kGT];
   __shared__ uint64_t bar;
   const int64_t t0 = rb + (int64_t)blockIdx.x * kGT;
   if (threadIdx.x == 0) {
@@ -468,41 +468,40 @@ __global__ void __launch_bounds__(kGT, 4)
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    mbar_expect_tx(&bar, 27 * kGT * 4);
+    mbar_expect_tx(&bar, PTS * kGT * 4);
     tma_load_2d(sv, &vmap, (int)t0, 0, &bar);
   }
   pdl_trigger();
   pdl_wait();
   const int64_t r = t0 + threadIdx.x;
   const bool active = r < re;
-  constexpr int kDiag = 13;
-  G27Row<float, float, MODE, 27> row;
-  float xv[27];
+  constexpr int kDiag = g_diag<PTS>();
+  G27Row<float, float, MODE, PTS> row;
+  float xv[PTS];
   unsigned sides = 0;
   if (active) {
-    const GCell cell = g_cell<27>(g, r);
+    const GCell cell = g_cell<PTS>(g, r);
     sides = g27_sides(g, cell.i, cell.j, cell.k);
     row.init(r, b, x, so);
-    const int32_t *dl = g.delta[cell.c];
     if (sides == 0x3Fu) {
 #pragma unroll
-      for (int e = 0; e < 27; ++e) {
+      for (int e = 0; e < PTS; ++e) {
         if (MODE == 2 && e == kDiag) {
           xv[e] = 0.f;
           continue;
         }
-        const int64_t nb = r + dl[e];
+        const int64_t nb = g_nb<PTS>(g, cell, r, e);
         const float xl = g27_ld(x + nb);
         xv[e] = (FZ && nb >= so.visit_end) ? 0.f : xl;
       }
     } else {
 #pragma unroll
-      for (int e = 0; e < 27; ++e) {
+      for (int e = 0; e < PTS; ++e) {
         if (MODE == 2 && e == kDiag) {
           xv[e] = 0.f;
           continue;
         }
-        const int64_t nb = g_in<27>(sides, e) ? r + dl[e] : r;
+        const int64_t nb = g_in<PTS>(sides, e) ? g_nb<PTS>(g, cell, r, e) : r;
         const float xl = g27_ld(x + nb);
         xv[e] = (FZ && nb >= so.visit_end) ? 0.f : xl;
       }
@@ -521,15 +520,15 @@ __global__ void __launch_bounds__(kGT, 4)
   const float *svt = sv + threadIdx.x;
   if (sides == 0x3Fu) {
 #pragma unroll
-    for (int e = 0; e < 27; ++e) row.step(e, true, svt[e * kGT], xv[e], so);
+    for (int e = 0; e < PTS; ++e) row.step(e, true, svt[e * kGT], xv[e], so);
   } else {
 #pragma unroll
-    for (int e = 0; e < 27; ++e) row.step(e, g_in<27>(sides, e), svt[e * kGT], xv[e], so);
+    for (int e = 0; e < PTS; ++e) row.step(e, g_in<PTS>(sides, e), svt[e * kGT], xv[e], so);
   }
   row.finish(r, b, x, y, nullptr, so);
 }
 
-// the tensor-staged kernel serves float rows with 16-byte-aligned row starts
+// the tensor-staged kernels serve float rows with 16-byte-aligned row starts
 // (LGX_G27_TMA=0 switches it off)
 static bool g27_tma_enabled() {
   static const bool on = [] {
@@ -559,17 +558,17 @@ static G27EncodeFn g27_encode() {
   return fn;
 }
 
-// the float values viewed as [27][stride], boxes of 27 x kGT (cached on the
-// grid, keyed by the value array)
+// the float values viewed as [points][stride], boxes of points x kGT (cached
+// on the grid, keyed by the value array)
 static const CUtensorMap *g27_value_map(const Grid27 &gr, const float *v) {
   static_assert(sizeof(CUtensorMap) <= sizeof(gr.vmap32), "tensor map storage");
   if (gr.vmap32_key == v) return reinterpret_cast<const CUtensorMap *>(gr.vmap32);
   const G27EncodeFn encode = g27_encode();
   if (!encode) return nullptr;
   CUtensorMap *map = reinterpret_cast<CUtensorMap *>(gr.vmap32);
-  const cuuint64_t gdim[2] = {(cuuint64_t)gr.stride, 27};
+  const cuuint64_t gdim[2] = {(cuuint64_t)gr.stride, (cuuint64_t)gr.points};
   const cuuint64_t gstride[1] = {(cuuint64_t)gr.stride * 4};
-  const cuuint32_t box[2] = {(cuuint32_t)kGT, 27};
+  const cuuint32_t box[2] = {(cuuint32_t)kGT, (cuuint32_t)gr.points};
   const cuuint32_t estride[2] = {1, 1};
   if (encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(v), gdim, gstride, box,
              estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -580,17 +579,17 @@ static const CUtensorMap *g27_value_map(const Grid27 &gr, const float *v) {
   return map;
 }
 
-template <int MODE>
+template <int MODE, int PTS>
 static bool g27_tma_launch(const Grid27 &gr, const float *v, int64_t rb, int64_t re,
                            const float *b, float *x, float *y, const G27Sor &so, cudaStream_t s,
                            lgx_status *st) {
-  if (!g27_tma_enabled() || gr.points != 27 || rb % 4 || ((uintptr_t)v & 15u) ||
+  if (!g27_tma_enabled() || gr.points != PTS || rb % 4 || ((uintptr_t)v & 15u) ||
       gr.stride % 4 || gr.stride > (int64_t)INT32_MAX)
     return false;
   const CUtensorMap *map = g27_value_map(gr, v);
   if (!map) return false;
   const int64_t ctas = (re - rb + kGT - 1) / kGT;
-  auto kern = MODE == 2 && so.from_zero ? k_g27_vtma<MODE, true> : k_g27_vtma<MODE, false>;
+  auto kern = MODE == 2 && so.from_zero ? k_g27_vtma<MODE, true, PTS> : k_g27_vtma<MODE, false, PTS>;
   const cudaError_t e = launch_pdl(true, kern, dim3((unsigned)ctas), dim3(kGT), 0, s, *map,
                                    view(gr), rb, re, b, x, y, so, device_error_flag());
   *st = e == cudaSuccess ? LGX_OK : cuda_fail(e, "k_g27_vtma");
@@ -634,9 +633,9 @@ static lgx_status launch_g27_pts(const Grid27 &gr, const VT *v, int64_t rb, int6
       return LGX_OK;
     }
   }
-  if constexpr (std::is_same_v<VT, float> && std::is_same_v<XT, float> && PTS == 27) {
+  if constexpr (std::is_same_v<VT, float> && std::is_same_v<XT, float>) {
     lgx_status st = LGX_OK;
-    if (g27_tma_launch<MODE>(gr, v, rb, re, b, x, y, so, s, &st)) return st;
+    if (g27_tma_launch<MODE, PTS>(gr, v, rb, re, b, x, y, so, s, &st)) return st;
   }
   LGX_CUDA(launch_pdl(pdl, k_g27_rows<VT, XT, MODE, PTS>, dim3((unsigned)((rows + 255) / 256)),
                       dim3(256), 0, s, view(gr), rb, re, v, b, x, y, scale, so));

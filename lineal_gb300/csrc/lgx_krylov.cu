@@ -634,23 +634,48 @@ static lgx_status run_solve(int kind, const lgx_matrix *a, const double *d_b, do
 // reference counterpart).  The inner CG runs the recurrence of
 // conjugate-gradients/solver.hpp:75-115 on float vectors: float products of
 // the finest level (grid or row kernels on the cycle's float values) and the
-// float V-cycle, with every dot product accumulated in FP64 and the CG
+// float V-cycle, with every dot product compensated (Dot2f below) and the CG
 // scalars kept in FP64 (KScalars).  The outer loop forms the FP64 residual,
 // hands the inner solve r / ||r|| (so the float vectors stay O(1) however far
 // the residual has fallen), adds ||r|| d to x in FP64 and stops on the FP64
 // residual.
 // ---------------------------------------------------------------------------
 
-// dot(a, b) of float vectors in FP64 with a post operation in the last block
+// Per-thread dot products of float vectors, compensated in FP32 (Ogita,
+// Rump & Oishi, "Accurate sum and dot product", SIAM J. Sci. Comput. 26,
+// 2005, Algorithm Dot2): each product is split exactly into p + e by an
+// fma (TwoProduct), each running sum exactly into s + q (TwoSum), and the
+// errors e + q are summed in a second float.  The result is as accurate as
+// a sum in twice the working precision; it leaves the thread as s + c in
+// FP64 and the partials meet in FP64.  On GB300 the FP32 pipe has 64 times
+// the FP64 rate, and FP64 accumulation (two float-to-double conversions and
+// a DFMA per element) made these dot kernels FP64-pipe bound.  The
+// operations are the _rn intrinsics, which the compiler does not contract.
+struct Dot2f {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    const float e = __fmaf_rn(a, b, -p);
+    const float t = __fadd_rn(s, p);
+    const float z = __fsub_rn(t, s);
+    const float q = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(q, e));
+  }
+  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
+// dot(a, b) of float vectors (compensated, FP64 partials) with a post operation in the last block
 __global__ void __launch_bounds__(kKT)
   k_fdot_post(int64_t n, const float *__restrict__ a, const float *__restrict__ b, int post,
               KScalars *ks, double *partials, unsigned *counter) {
-  double s = 0.0;
+  Dot2f acc;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
-    s = fma((double)a[i], (double)b[i], s);
+    acc.add(a[i], b[i]);
   double t;
-  if (grid_reduce<kKT>(s, blockIdx.x, gridDim.x, partials, counter, &t) && threadIdx.x == 0) {
+  if (grid_reduce<kKT>(acc.value(), blockIdx.x, gridDim.x, partials, counter, &t) &&
+      threadIdx.x == 0) {
     if (post == POST_ALPHA) {
       set_flags(ks, ks->rho, t);
       ks->den = t;
@@ -668,22 +693,23 @@ __global__ void __launch_bounds__(kKT)
 }
 
 // d += alpha p ; r -= alpha q ; res2 = ||r||^2 (float vectors, FP64 alpha
-// rounded once to float, FP64 sum)
+// rounded once to float, compensated sum)
 __global__ void __launch_bounds__(kKT)
   k_fcg_update(int64_t n, KScalars *ks, const float *__restrict__ p, const float *__restrict__ q,
                float *__restrict__ d, float *__restrict__ r, double *partials,
                unsigned *counter) {
   const float alpha = (float)ks->alpha;
-  double s = 0.0;
+  Dot2f acc;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     d[i] = fmaf(p[i], alpha, d[i]);
     const float rv = fmaf(-alpha, q[i], r[i]);
     r[i] = rv;
-    s = fma((double)rv, (double)rv, s);
+    acc.add(rv, rv);
   }
   double t;
-  if (grid_reduce<kKT>(s, blockIdx.x, gridDim.x, partials, counter, &t) && threadIdx.x == 0) {
+  if (grid_reduce<kKT>(acc.value(), blockIdx.x, gridDim.x, partials, counter, &t) &&
+      threadIdx.x == 0) {
     ks->res2 = t;
     if (!isfinite(t)) ks->flag |= 2;
   }
@@ -698,23 +724,24 @@ __global__ void k_fxpby(int64_t n, const KScalars *ks, const float *__restrict__
     p[i] = fmaf(p[i], beta, z[i]);
 }
 
-// flexible CG on float vectors: t1 = r.z, t2 = r.z_old (FP64 sums), then
+// flexible CG on float vectors: t1 = r.z, t2 = r.z_old (compensated sums), then
 // rho_old = rho, rho = t1, beta = (t1 - t2) / rho_old (Notay 2000)
 __global__ void __launch_bounds__(kKT)
   k_fdot2_fcg(int64_t n, const float *__restrict__ r, const float *__restrict__ z,
               const float *__restrict__ zold, KScalars *ks, double *partials, double *partials2,
               unsigned *counter, unsigned *counter2) {
-  double s1 = 0.0, s2 = 0.0;
+  Dot2f acc1, acc2;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const double ri = (double)r[i];
-    s1 = fma(ri, (double)z[i], s1);
-    s2 = fma(ri, (double)zold[i], s2);
+    const float ri = r[i];
+    acc1.add(ri, z[i]);
+    acc2.add(ri, zold[i]);
   }
   double t1, t2;
-  const bool l1 = grid_reduce<kKT>(s1, blockIdx.x, gridDim.x, partials, counter, &t1);
+  const bool l1 = grid_reduce<kKT>(acc1.value(), blockIdx.x, gridDim.x, partials, counter, &t1);
   if (l1 && threadIdx.x == 0) ks->tmp = t1;
-  const bool l2 = grid_reduce<kKT>(s2, blockIdx.x, gridDim.x, partials2, counter2, &t2);
+  const bool l2 =
+    grid_reduce<kKT>(acc2.value(), blockIdx.x, gridDim.x, partials2, counter2, &t2);
   if (l2 && threadIdx.x == 0) {
     __threadfence();
     const double u1 = ((volatile KScalars *)ks)->tmp;
