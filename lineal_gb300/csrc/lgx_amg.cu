@@ -1266,13 +1266,16 @@ __global__ void k_galerkin_upper(int64_t nc, const int64_t *rowptr, const int64_
   }
 }
 
+// flagged_only: the rows that k_galerkin_warp left (count -1)
 template <typename VT>
 __global__ void k_galerkin_accumulate(int64_t nc, const int64_t *rowptr, const int32_t *col,
                                       const VT *val, const uint32_t *agg, const int64_t *list_ptr,
                                       const int32_t *list, int coarse_f32, const int64_t *soff,
-                                      int32_t *scol, double *sval, int64_t *count) {
+                                      int32_t *scol, double *sval, int64_t *count,
+                                      int flagged_only) {
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nc;
        c += (int64_t)gridDim.x * blockDim.x) {
+    if (flagged_only && count[c] != -1) continue;
     int32_t *cc = scol + soff[c];
     double *vv = sval + soff[c];
     int64_t m = 0;
@@ -1307,6 +1310,139 @@ __global__ void k_galerkin_accumulate(int64_t nc, const int64_t *rowptr, const i
       vv[y + 1] = v0;
     }
     count[c] = m;
+  }
+}
+
+// The same accumulation with one warp per coarse row: the row's fine entries
+// (at most kGalCap, in encounter order: list order, then storage order) are
+// staged in shared memory as (coarse column, value cast to the coarse type);
+// an entry is its column's head when no earlier entry has that column and
+// links to the next entry of its column; each head sums its column's values
+// along the links, in encounter order (the sequential sum of the per-thread
+// kernel), and is written at its rank among the heads by column.  All loads of a row go out in two rounds (the list rows' offsets,
+// then every entry's column, value and aggregate), where the thread-per-row
+// kernel walks its scratch in global memory entry by entry.  Rows with more
+// entries get count -1 and are left to k_galerkin_accumulate (flagged).
+constexpr int kGalCap = 512;
+constexpr int kGalWarps = 4;
+constexpr int kGalMaxList = 64;  // aggregates hold at most 64 rows
+
+template <typename VT>
+__global__ void __launch_bounds__(32 * kGalWarps)
+  k_galerkin_warp(int64_t nc, const int64_t *__restrict__ rowptr, const int32_t *__restrict__ col,
+                  const VT *__restrict__ val, const uint32_t *__restrict__ agg,
+                  const int64_t *__restrict__ list_ptr, const int32_t *__restrict__ list,
+                  int coarse_f32, const int64_t *__restrict__ soff, int32_t *scol, double *sval,
+                  int64_t *count) {
+  __shared__ int32_t sJ[kGalWarps][kGalCap];
+  __shared__ double sV[kGalWarps][kGalCap];
+  __shared__ uint32_t sHead[kGalWarps][kGalCap / 32];
+  __shared__ int16_t sNext[kGalWarps][kGalCap], sHeadList[kGalWarps][kGalCap];
+  __shared__ int64_t sRow[kGalWarps][kGalMaxList];
+  __shared__ int32_t sPfx[kGalWarps][kGalMaxList + 1];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int32_t *J = sJ[w];
+  double *V = sV[w];
+  uint32_t *H = sHead[w];
+  int16_t *NX = sNext[w], *HL = sHeadList[w];
+  int64_t *RB = sRow[w];
+  int32_t *PF = sPfx[w];
+  const int64_t nwarps = (int64_t)gridDim.x * kGalWarps;
+  for (int64_t c = (int64_t)blockIdx.x * kGalWarps + w; c < nc; c += nwarps) {
+    const int64_t n = soff[c + 1] - soff[c];
+    const int64_t l0 = list_ptr[c], nl = list_ptr[c + 1] - l0;
+    if (n > kGalCap || nl > kGalMaxList) {
+      if (lane == 0) count[c] = -1;
+      continue;
+    }
+    // the list rows' offsets and their prefix sums
+    int32_t run = 0;
+    for (int64_t b0 = 0; b0 < nl; b0 += 32) {
+      const int64_t k = b0 + lane;
+      int32_t len = 0;
+      if (k < nl) {
+        const int64_t i = list[l0 + k];
+        const int64_t rb = rowptr[i];
+        RB[k] = rb;
+        len = (int32_t)(rowptr[i + 1] - rb);
+      }
+      int32_t x = len;
+      for (int d = 1; d < 32; d <<= 1) {
+        const int32_t y = __shfl_up_sync(0xffffffffu, x, d);
+        if (lane >= d) x += y;
+      }
+      if (k < nl) PF[k + 1] = run + x;
+      run += __shfl_sync(0xffffffffu, x, 31);
+    }
+    if (lane == 0) PF[0] = 0;
+    __syncwarp();
+    // stage every entry: item p of list row k sits at PF[k] + offset
+    for (int32_t p = lane; p < (int32_t)n; p += 32) {
+      int32_t lo = 0, hi = (int32_t)nl - 1;
+      while (lo < hi) {
+        const int32_t mid = (lo + hi + 1) >> 1;
+        if (PF[mid] <= p) lo = mid;
+        else hi = mid - 1;
+      }
+      const int64_t e = RB[lo] + (p - PF[lo]);
+      const uint32_t jc = agg[col[e]];
+      const VT vr = val[e];
+      J[p] = jc >= kIsolated ? -1 : (int32_t)jc;
+      V[p] = coarse_f32 ? (double)(float)vr : (double)vr;
+    }
+    __syncwarp();
+    // links (integer work only): an entry is its column's head when no
+    // earlier entry has the column; NX[q] = the next entry with q's column
+    // (each scan stops at its first match)
+    for (int32_t q0 = 0; q0 < (int32_t)n; q0 += 32) {
+      const int32_t q = q0 + lane;
+      bool head = false;
+      if (q < (int32_t)n) {
+        const int32_t jq = J[q];
+        int32_t nx = -1;
+        if (jq >= 0) {
+          head = true;
+          for (int32_t t = 0; t < q; ++t)
+            if (J[t] == jq) {
+              head = false;
+              break;
+            }
+          for (int32_t t = q + 1; t < (int32_t)n; ++t)
+            if (J[t] == jq) {
+              nx = t;
+              break;
+            }
+        }
+        NX[q] = nx;
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, head);
+      if (lane == 0) H[q0 >> 5] = m;
+    }
+    __syncwarp();
+    // the heads in entry order
+    int32_t nh = 0;
+    for (int32_t wd = 0; wd < ((int32_t)n + 31) / 32; ++wd) {
+      const unsigned m = H[wd];
+      if ((m >> lane) & 1u) HL[nh + __popc(m & ((1u << lane) - 1u))] = (int16_t)(wd * 32 + lane);
+      nh += __popc(m);
+    }
+    __syncwarp();
+    // one head per lane: its rank among the heads by column, and its
+    // column's sum in encounter order along the links (the FP64 adds run
+    // only along the chains: a warp-wide FP64 instruction costs the pipe the
+    // same however few lanes it has)
+    for (int32_t k = lane; k < nh; k += 32) {
+      const int32_t q = HL[k], jq = J[q];
+      int32_t rank = 0;
+      for (int32_t u = 0; u < nh; ++u) rank += J[HL[u]] < jq;
+      double sum = V[q];
+      for (int32_t t = NX[q]; t >= 0; t = NX[t]) sum = __dadd_rn(sum, V[t]);
+      scol[soff[c] + rank] = jq;
+      sval[soff[c] + rank] = sum;
+    }
+    const int32_t heads = nh;
+    if (lane == 0) count[c] = heads;
+    __syncwarp();
   }
 }
 
@@ -1345,14 +1481,30 @@ lgx_status galerkin(const Csr &a, const AggResult &ag, int coarse_f32, cudaStrea
   LGX_CHECK(scol.alloc(total));
   LGX_CHECK(sval.alloc(total));
   if (nc > 0) {
-    if (a.storage == LGX_F64)
+    // warp per coarse row, then the thread-per-row kernel for the rows too
+    // long for its shared memory (LGX_GALERKIN_WARP=0: thread per row only)
+    static const bool warp_on = [] {
+      const char *e = std::getenv("LGX_GALERKIN_WARP");
+      return !(e && e[0] == '0');
+    }();
+    const unsigned gw = (unsigned)std::min<int64_t>(grid_for(nc, kGalWarps), 16 * 152);
+    if (a.storage == LGX_F64) {
+      if (warp_on)
+        k_galerkin_warp<double><<<gw, 32 * kGalWarps, 0, s>>>(
+          nc, a.rowptr.p, a.col.p, a.v64.p, ag.agg.p, ag.list_ptr.p, ag.list.p, coarse_f32,
+          soff.p, scol.p, sval.p, count.p);
       k_galerkin_accumulate<double><<<g, 128, 0, s>>>(nc, a.rowptr.p, a.col.p, a.v64.p, ag.agg.p,
                                                       ag.list_ptr.p, ag.list.p, coarse_f32, soff.p,
-                                                      scol.p, sval.p, count.p);
-    else
+                                                      scol.p, sval.p, count.p, warp_on);
+    } else {
+      if (warp_on)
+        k_galerkin_warp<float><<<gw, 32 * kGalWarps, 0, s>>>(
+          nc, a.rowptr.p, a.col.p, a.v32.p, ag.agg.p, ag.list_ptr.p, ag.list.p, coarse_f32,
+          soff.p, scol.p, sval.p, count.p);
       k_galerkin_accumulate<float><<<g, 128, 0, s>>>(nc, a.rowptr.p, a.col.p, a.v32.p, ag.agg.p,
                                                      ag.list_ptr.p, ag.list.p, coarse_f32, soff.p,
-                                                     scol.p, sval.p, count.p);
+                                                     scol.p, sval.p, count.p, warp_on);
+    }
     LGX_LAUNCH_CHECK();
   }
   LGX_CHECK(inclusive_offsets(nc, count.p, rowptr_c.p, s));
@@ -1498,6 +1650,228 @@ __global__ void k_set_identity(int64_t n, double *x) {
     x[t] = (t / n == t % n) ? 1.0 : 0.0;
 }
 
+// ---- blocked form (panels of kCb columns): the same factor and inverse in
+// about 5 n / kCb launches instead of 6 n.  Per panel K = [k0, k1):
+//  k_bchol_panel  every CTA factors the diagonal block A_KK (kCb x kCb) in
+//                 shared memory (the same arithmetic in every CTA, every
+//                 pivot checked) and solves its rows below the panel,
+//                 L_iK = A_iK L_KK^-T (CTA 0 writes L_KK);
+//  k_bchol_trail  A_IJ -= L_IK L_JK^T on the lower tiles of the trailing
+//                 matrix (32 x 32 tiles, the panel in shared memory).
+// Then X = L^-1 by blocked forward substitution (k_btri_diag: X_KC =
+// L_KK^-1 X_KC for the columns C < k1; k_btri_update: X_IC -= L_IK X_KC for
+// the rows below) and A^-1 = X^T X over the lower tiles, mirrored
+// (k_bgram).  FP64 throughout; the sums differ from the column-sweep form
+// only in their order.
+constexpr int kCb = 32;
+
+// factor the kCb x kCb (or smaller, last panel) block in shared memory with
+// one warp; returns false on a non-positive or non-finite pivot
+__device__ bool bchol_diag(double (*D)[kCb + 1], int nb) {
+  const int lane = threadIdx.x & 31;
+  bool ok = true;
+  for (int j = 0; j < nb; ++j) {
+    const double d = D[j][j];
+    if (!(d > 0.0) || !isfinite(d)) ok = false;
+    const double ljj = sqrt(d);
+    __syncwarp();
+    if (lane == j) D[j][j] = ljj;
+    if (lane > j && lane < nb) D[lane][j] = D[lane][j] / ljj;
+    __syncwarp();
+    if (lane > j && lane < nb)
+      for (int m = j + 1; m <= lane; ++m) D[lane][m] = fma(-D[lane][j], D[m][j], D[lane][m]);
+    __syncwarp();
+  }
+  return ok;
+}
+
+__global__ void __launch_bounds__(256) k_bchol_panel(int64_t n, int64_t k0, double *a, int *bad) {
+  __shared__ double D[kCb][kCb + 1];
+  if (*bad) return;
+  const int nb = (int)(n - k0 < kCb ? n - k0 : kCb);
+  const int64_t k1 = k0 + nb;
+  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
+    const int r = t / nb, c = t % nb;
+    D[r][c] = c <= r ? a[(k0 + r) * n + k0 + c] : 0.0;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const bool ok = bchol_diag(D, nb);
+    if (!ok && threadIdx.x == 0) atomicOr(bad, 1);
+  }
+  __syncthreads();
+  if (blockIdx.x == 0)
+    for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
+      const int r = t / nb, c = t % nb;
+      if (c <= r) a[(k0 + r) * n + k0 + c] = D[r][c];
+    }
+  // rows below the panel: x_j = (a_j - sum_{m<j} x_m l_jm) / l_jj
+  const int64_t i = k1 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double x[kCb];
+  double *row = a + i * n + k0;
+#pragma unroll
+  for (int j = 0; j < kCb; ++j) x[j] = j < nb ? row[j] : 0.0;
+#pragma unroll
+  for (int j = 0; j < kCb; ++j) {
+    if (j >= nb) break;
+    double s = x[j];
+#pragma unroll
+    for (int m = 0; m < j; ++m) s = fma(-x[m], D[j][m], s);
+    x[j] = s / D[j][j];
+  }
+#pragma unroll
+  for (int j = 0; j < kCb; ++j)
+    if (j < nb) row[j] = x[j];
+}
+
+// lower tiles (I >= J) of the trailing matrix rows/columns >= k1
+__global__ void __launch_bounds__(256) k_bchol_trail(int64_t n, int64_t k0, double *a,
+                                                     const int *bad) {
+  __shared__ double LI[32][kCb + 1], LJ[32][kCb + 1];
+  if (*bad) return;
+  const int nb = (int)(n - k0 < kCb ? n - k0 : kCb);
+  const int64_t k1 = k0 + nb;
+  // tile t -> (I, J) with J <= I, row-major over the lower triangle
+  const int64_t t = blockIdx.x;
+  int64_t I = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+  while (I * (I + 1) / 2 > t) --I;
+  while ((I + 1) * (I + 2) / 2 <= t) ++I;
+  const int64_t J = t - I * (I + 1) / 2;
+  const int64_t i0 = k1 + I * 32, j0 = k1 + J * 32;
+  for (int q = threadIdx.x; q < 32 * kCb; q += blockDim.x) {
+    const int r = q / kCb, m = q % kCb;
+    LI[r][m] = (i0 + r < n && m < nb) ? a[(i0 + r) * n + k0 + m] : 0.0;
+    LJ[r][m] = (j0 + r < n && m < nb) ? a[(j0 + r) * n + k0 + m] : 0.0;
+  }
+  __syncthreads();
+  const int ri = (threadIdx.x >> 4) * 2, cj = (threadIdx.x & 15) * 2;
+  double s00 = 0.0, s01 = 0.0, s10 = 0.0, s11 = 0.0;
+#pragma unroll
+  for (int m = 0; m < kCb; ++m) {
+    const double x0 = LI[ri][m], x1 = LI[ri + 1][m], y0 = LJ[cj][m], y1 = LJ[cj + 1][m];
+    s00 = fma(x0, y0, s00);
+    s01 = fma(x0, y1, s01);
+    s10 = fma(x1, y0, s10);
+    s11 = fma(x1, y1, s11);
+  }
+  const double sv[2][2] = {{s00, s01}, {s10, s11}};
+#pragma unroll
+  for (int u = 0; u < 2; ++u)
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+      const int64_t i = i0 + ri + u, j = j0 + cj + v;
+      if (i < n && j <= i) a[i * n + j] -= sv[u][v];
+    }
+}
+
+// X_KC = L_KK^-1 X_KC for the columns c < k1, one column per thread
+__global__ void __launch_bounds__(256) k_btri_diag(int64_t n, int64_t k0, const double *l,
+                                                   double *x) {
+  __shared__ double D[kCb][kCb + 1];
+  const int nb = (int)(n - k0 < kCb ? n - k0 : kCb);
+  const int64_t k1 = k0 + nb;
+  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
+    const int r = t / nb, c = t % nb;
+    D[r][c] = c <= r ? l[(k0 + r) * n + k0 + c] : 0.0;
+  }
+  __syncthreads();
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= k1) return;
+  double y[kCb];
+#pragma unroll
+  for (int j = 0; j < kCb; ++j) y[j] = j < nb ? x[(k0 + j) * n + c] : 0.0;
+#pragma unroll
+  for (int j = 0; j < kCb; ++j) {
+    if (j >= nb) break;
+    double s = y[j];
+#pragma unroll
+    for (int m = 0; m < j; ++m) s = fma(-D[j][m], y[m], s);
+    y[j] = s / D[j][j];
+  }
+#pragma unroll
+  for (int j = 0; j < kCb; ++j)
+    if (j < nb) x[(k0 + j) * n + c] = y[j];
+}
+
+// X_IC -= L_IK X_KC for the rows i >= k1 and the columns c < k1 (32 x 32
+// tiles; blockIdx.x over the row tiles, blockIdx.y over the column tiles)
+__global__ void __launch_bounds__(256) k_btri_update(int64_t n, int64_t k0, const double *l,
+                                                     double *x) {
+  __shared__ double LI[32][kCb + 1], XK[kCb][32 + 1];
+  const int nb = (int)(n - k0 < kCb ? n - k0 : kCb);
+  const int64_t k1 = k0 + nb;
+  const int64_t i0 = k1 + (int64_t)blockIdx.x * 32, c0 = (int64_t)blockIdx.y * 32;
+  for (int q = threadIdx.x; q < 32 * kCb; q += blockDim.x) {
+    const int r = q / kCb, m = q % kCb;
+    LI[r][m] = (i0 + r < n && m < nb) ? l[(i0 + r) * n + k0 + m] : 0.0;
+    const int mm = q / 32, cc = q % 32;
+    XK[mm][cc] = (mm < nb && c0 + cc < k1) ? x[(k0 + mm) * n + c0 + cc] : 0.0;
+  }
+  __syncthreads();
+  const int ri = (threadIdx.x >> 4) * 2, cj = (threadIdx.x & 15) * 2;
+  double s00 = 0.0, s01 = 0.0, s10 = 0.0, s11 = 0.0;
+#pragma unroll
+  for (int m = 0; m < kCb; ++m) {
+    const double x0 = LI[ri][m], x1 = LI[ri + 1][m], y0 = XK[m][cj], y1 = XK[m][cj + 1];
+    s00 = fma(x0, y0, s00);
+    s01 = fma(x0, y1, s01);
+    s10 = fma(x1, y0, s10);
+    s11 = fma(x1, y1, s11);
+  }
+  const double sv[2][2] = {{s00, s01}, {s10, s11}};
+#pragma unroll
+  for (int u = 0; u < 2; ++u)
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+      const int64_t i = i0 + ri + u, c = c0 + cj + v;
+      if (i < n && c < k1) x[i * n + c] -= sv[u][v];
+    }
+}
+
+// inv_ij = sum_k X_ki X_kj (X lower triangular: k >= max(i, j)) on the lower
+// tiles, written to both halves
+__global__ void __launch_bounds__(256) k_bgram(int64_t n, const double *x, double *inv) {
+  __shared__ double XI[32][32 + 1], XJ[32][32 + 1];
+  const int64_t t = blockIdx.x;
+  int64_t I = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+  while (I * (I + 1) / 2 > t) --I;
+  while ((I + 1) * (I + 2) / 2 <= t) ++I;
+  const int64_t J = t - I * (I + 1) / 2;
+  const int64_t i0 = I * 32, j0 = J * 32;
+  const int ri = (threadIdx.x >> 4) * 2, cj = (threadIdx.x & 15) * 2;
+  double s00 = 0.0, s01 = 0.0, s10 = 0.0, s11 = 0.0;
+  for (int64_t kb = i0; kb < n; kb += 32) {
+    __syncthreads();
+    for (int q = threadIdx.x; q < 32 * 32; q += blockDim.x) {
+      const int m = q / 32, cc = q % 32;
+      const bool in = kb + m < n;
+      XI[m][cc] = (in && i0 + cc < n) ? x[(kb + m) * n + i0 + cc] : 0.0;
+      XJ[m][cc] = (in && j0 + cc < n) ? x[(kb + m) * n + j0 + cc] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int m = 0; m < 32; ++m) {
+      const double x0 = XI[m][ri], x1 = XI[m][ri + 1], y0 = XJ[m][cj], y1 = XJ[m][cj + 1];
+      s00 = fma(x0, y0, s00);
+      s01 = fma(x0, y1, s01);
+      s10 = fma(x1, y0, s10);
+      s11 = fma(x1, y1, s11);
+    }
+  }
+  const double sv[2][2] = {{s00, s01}, {s10, s11}};
+#pragma unroll
+  for (int u = 0; u < 2; ++u)
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+      const int64_t i = i0 + ri + u, j = j0 + cj + v;
+      if (i < n && j < n && j <= i) {
+        inv[i * n + j] = sv[u][v];
+        inv[j * n + i] = sv[u][v];
+      }
+    }
+}
+
 // x = A^-1 b, one warp per row
 template <typename XT>
 __global__ void k_dense_apply(int64_t n, const double *ainv, const XT *b, XT *x) {
@@ -1538,6 +1912,44 @@ lgx_status dense_inverse(const Csr &a, cudaStream_t s, DBuf<double> &inv, int sp
                                                      a.storage == LGX_F32 ? a.v32.p : nullptr,
                                                      l.p);
     LGX_LAUNCH_CHECK();
+    // the blocked form (LGX_BLOCKED_CHOL=0: the column sweeps below)
+    static const bool blocked = [] {
+      const char *e = std::getenv("LGX_BLOCKED_CHOL");
+      return !(e && e[0] == '0');
+    }();
+    if (blocked) {
+      const int64_t npan = (n + kCb - 1) / kCb;
+      for (int64_t K = 0; K < npan; ++K) {
+        const int64_t k0 = K * kCb, k1 = std::min<int64_t>(k0 + kCb, n), below = n - k1;
+        k_bchol_panel<<<(unsigned)std::max<int64_t>(1, (below + 255) / 256), 256, 0, s>>>(
+          n, k0, l.p, bad.p);
+        if (below > 0) {
+          const int64_t T = (below + 31) / 32;
+          k_bchol_trail<<<(unsigned)(T * (T + 1) / 2), 256, 0, s>>>(n, k0, l.p, bad.p);
+        }
+      }
+      LGX_LAUNCH_CHECK();
+      int h_bad = 0;
+      LGX_CUDA(cudaMemcpyAsync(&h_bad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+      LGX_CUDA(cudaStreamSynchronize(s));
+      if (h_bad) return fail(LGX_ERR_NOT_SPD, "matrix has a non-positive pivot");
+      DBuf<double> xl;
+      LGX_CHECK(xl.alloc(n * n));
+      k_set_identity<<<(unsigned)std::min<int64_t>(grid_for(n * n, 256), 8192), 256, 0, s>>>(
+        n, xl.p);
+      for (int64_t K = 0; K < npan; ++K) {
+        const int64_t k0 = K * kCb, k1 = std::min<int64_t>(k0 + kCb, n), below = n - k1;
+        k_btri_diag<<<(unsigned)((k1 + 255) / 256), 256, 0, s>>>(n, k0, l.p, xl.p);
+        if (below > 0)
+          k_btri_update<<<dim3((unsigned)((below + 31) / 32), (unsigned)((k1 + 31) / 32)), 256, 0,
+                          s>>>(n, k0, l.p, xl.p);
+      }
+      const int64_t T = (n + 31) / 32;
+      k_bgram<<<(unsigned)(T * (T + 1) / 2), 256, 0, s>>>(n, xl.p, inv.p);
+      LGX_LAUNCH_CHECK();
+      LGX_CUDA(cudaStreamSynchronize(s));
+      return LGX_OK;
+    }
     for (int64_t k = 0; k < n; ++k) {
       k_chol_column<<<1, 256, 0, s>>>(n, k, l.p, bad.p);
       const int64_t m = n - k - 1;

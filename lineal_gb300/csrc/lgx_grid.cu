@@ -429,9 +429,9 @@ __global__ void __launch_bounds__(256)
   for (int q = 0; q < R; ++q) row[q].finish(r0 + q, b, x, y, scale, so);
 }
 
-// ---- float grid rows with the values staged by the tensor engine ---------
-// Float values and vectors on the 27- and 7-point grids: each CTA of kGT
-// rows has its rows' value-plane segments (PTS x kGT floats, one 2-D box of
+// ---- grid rows with the values staged by the tensor engine ---------------
+// Float or FP64 values and vectors on the 27- and 7-point grids: each CTA of
+// RT rows has its rows' value-plane segments (PTS x RT values, one 2-D box of
 // the value array viewed as [PTS][stride]) brought into shared memory by one
 // cp.async.bulk.tensor copy, issued before the kernel waits for its
 // predecessor (the values are constant); every thread then issues all its x
@@ -440,8 +440,6 @@ __global__ void __launch_bounds__(256)
 // arithmetic on the staged values, so results equal k_g27_rows bit for bit.
 // The row-per-thread kernel keeps three value loads per round in flight and
 // reaches 0.62 of HBM on a 27-point float sweep.
-constexpr int kGT = 256;  // rows per CTA
-
 __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int c0, int c1,
                                             uint64_t *bar) {
   asm volatile(
@@ -454,21 +452,33 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, i
 // FZ: a forward sweep from zero (x of the colours from visit_end on reads
 // as 0), a template argument so that other launches carry no per-entry test.
 // Rows whose neighbours all lie inside the grid (all but the boundary
-// layers) skip the per-entry inside tests.
-template <int MODE, bool FZ, int PTS>
-__global__ void __launch_bounds__(kGT, PTS == 27 ? 4 : 6)
+// layers) skip the per-entry inside tests.  T = float: 256 rows per CTA
+// (T = double would take 128: the 27 gathered x of a row take 54
+// registers); every row's sum in offset order as in k_g27_rows.
+template <typename T>
+constexpr int g_rows_per_cta() {
+  return sizeof(T) == 8 ? 128 : 256;
+}
+template <typename T, int PTS>
+constexpr int g_ctas_per_sm() {
+  return sizeof(T) == 8 ? (PTS == 27 ? 5 : 8) : (PTS == 27 ? 4 : 6);
+}
+
+template <typename T, int MODE, bool FZ, int PTS>
+__global__ void __launch_bounds__(g_rows_per_cta<T>(), g_ctas_per_sm<T, PTS>())
   k_g27_vtma(const __grid_constant__ CUtensorMap vmap, G27 g, int64_t rb, int64_t re,
-             const float *__restrict__ b, float *x, float *__restrict__ y, G27Sor so, int *err) {
-  __shared__ __align__(128) float sv[PTS * kGT];
+             const T *__restrict__ b, T *x, T *__restrict__ y, G27Sor so, int *err) {
+  constexpr int RT = g_rows_per_cta<T>();
+  __shared__ __align__(128) T sv[PTS * RT];
   __shared__ uint64_t bar;
-  const int64_t t0 = rb + (int64_t)blockIdx.x * kGT;
+  const int64_t t0 = rb + (int64_t)blockIdx.x * RT;
   if (threadIdx.x == 0) {
     mbar_init(&bar, 1);
     fence_mbar_init();
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    mbar_expect_tx(&bar, PTS * kGT * 4);
+    mbar_expect_tx(&bar, PTS * RT * (unsigned)sizeof(T));
     tma_load_2d(sv, &vmap, (int)t0, 0, &bar);
   }
   pdl_trigger();
@@ -476,8 +486,8 @@ __global__ void __launch_bounds__(kGT, PTS == 27 ? 4 : 6)
   const int64_t r = t0 + threadIdx.x;
   const bool active = r < re;
   constexpr int kDiag = g_diag<PTS>();
-  G27Row<float, float, MODE, PTS> row;
-  float xv[PTS];
+  G27Row<T, T, MODE, PTS> row;
+  T xv[PTS];
   unsigned sides = 0;
   if (active) {
     const GCell cell = g_cell<PTS>(g, r);
@@ -487,23 +497,23 @@ __global__ void __launch_bounds__(kGT, PTS == 27 ? 4 : 6)
 #pragma unroll
       for (int e = 0; e < PTS; ++e) {
         if (MODE == 2 && e == kDiag) {
-          xv[e] = 0.f;
+          xv[e] = T(0);
           continue;
         }
         const int64_t nb = g_nb<PTS>(g, cell, r, e);
-        const float xl = g27_ld(x + nb);
-        xv[e] = (FZ && nb >= so.visit_end) ? 0.f : xl;
+        const T xl = g27_ld(x + nb);
+        xv[e] = (FZ && nb >= so.visit_end) ? T(0) : xl;
       }
     } else {
 #pragma unroll
       for (int e = 0; e < PTS; ++e) {
         if (MODE == 2 && e == kDiag) {
-          xv[e] = 0.f;
+          xv[e] = T(0);
           continue;
         }
         const int64_t nb = g_in<PTS>(sides, e) ? g_nb<PTS>(g, cell, r, e) : r;
-        const float xl = g27_ld(x + nb);
-        xv[e] = (FZ && nb >= so.visit_end) ? 0.f : xl;
+        const T xl = g27_ld(x + nb);
+        xv[e] = (FZ && nb >= so.visit_end) ? T(0) : xl;
       }
     }
   }
@@ -517,13 +527,13 @@ __global__ void __launch_bounds__(kGT, PTS == 27 ? 4 : 6)
     return;
   }
   if (!active) return;
-  const float *svt = sv + threadIdx.x;
+  const T *svt = sv + threadIdx.x;
   if (sides == 0x3Fu) {
 #pragma unroll
-    for (int e = 0; e < PTS; ++e) row.step(e, true, svt[e * kGT], xv[e], so);
+    for (int e = 0; e < PTS; ++e) row.step(e, true, svt[e * RT], xv[e], so);
   } else {
 #pragma unroll
-    for (int e = 0; e < PTS; ++e) row.step(e, g_in<PTS>(sides, e), svt[e * kGT], xv[e], so);
+    for (int e = 0; e < PTS; ++e) row.step(e, g_in<PTS>(sides, e), svt[e * RT], xv[e], so);
   }
   row.finish(r, b, x, y, nullptr, so);
 }
@@ -558,39 +568,44 @@ static G27EncodeFn g27_encode() {
   return fn;
 }
 
-// the float values viewed as [points][stride], boxes of points x kGT (cached
-// on the grid, keyed by the value array)
-static const CUtensorMap *g27_value_map(const Grid27 &gr, const float *v) {
+// the values viewed as [points][stride], boxes of points x rows-per-CTA
+// (cached on the grid, keyed by the value array)
+template <typename T>
+static const CUtensorMap *g27_value_map(const Grid27 &gr, const T *v) {
+  unsigned char *store = sizeof(T) == 8 ? gr.vmap64 : gr.vmap32;
+  const void *&key = sizeof(T) == 8 ? gr.vmap64_key : gr.vmap32_key;
   static_assert(sizeof(CUtensorMap) <= sizeof(gr.vmap32), "tensor map storage");
-  if (gr.vmap32_key == v) return reinterpret_cast<const CUtensorMap *>(gr.vmap32);
+  if (key == v) return reinterpret_cast<const CUtensorMap *>(store);
   const G27EncodeFn encode = g27_encode();
   if (!encode) return nullptr;
-  CUtensorMap *map = reinterpret_cast<CUtensorMap *>(gr.vmap32);
+  CUtensorMap *map = reinterpret_cast<CUtensorMap *>(store);
   const cuuint64_t gdim[2] = {(cuuint64_t)gr.stride, (cuuint64_t)gr.points};
-  const cuuint64_t gstride[1] = {(cuuint64_t)gr.stride * 4};
-  const cuuint32_t box[2] = {(cuuint32_t)kGT, (cuuint32_t)gr.points};
+  const cuuint64_t gstride[1] = {(cuuint64_t)gr.stride * sizeof(T)};
+  const cuuint32_t box[2] = {(cuuint32_t)g_rows_per_cta<T>(), (cuuint32_t)gr.points};
   const cuuint32_t estride[2] = {1, 1};
-  if (encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(v), gdim, gstride, box,
-             estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-             CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+  if (encode(map, sizeof(T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+             2, const_cast<T *>(v), gdim, gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
     return nullptr;
-  gr.vmap32_key = v;
+  key = v;
   return map;
 }
 
-template <int MODE, int PTS>
-static bool g27_tma_launch(const Grid27 &gr, const float *v, int64_t rb, int64_t re,
-                           const float *b, float *x, float *y, const G27Sor &so, cudaStream_t s,
-                           lgx_status *st) {
-  if (!g27_tma_enabled() || gr.points != PTS || rb % 4 || ((uintptr_t)v & 15u) ||
-      gr.stride % 4 || gr.stride > (int64_t)INT32_MAX)
+template <typename T, int MODE, int PTS>
+static bool g27_tma_launch(const Grid27 &gr, const T *v, int64_t rb, int64_t re, const T *b, T *x,
+                           T *y, const G27Sor &so, bool pdl, cudaStream_t s, lgx_status *st) {
+  if (!g27_tma_enabled() || gr.points != PTS || rb % (16 / (int64_t)sizeof(T)) ||
+      ((uintptr_t)v & 15u) || (gr.stride * (int64_t)sizeof(T)) % 16 ||
+      gr.stride > (int64_t)INT32_MAX)
     return false;
-  const CUtensorMap *map = g27_value_map(gr, v);
+  const CUtensorMap *map = g27_value_map<T>(gr, v);
   if (!map) return false;
-  const int64_t ctas = (re - rb + kGT - 1) / kGT;
-  auto kern = MODE == 2 && so.from_zero ? k_g27_vtma<MODE, true, PTS> : k_g27_vtma<MODE, false, PTS>;
-  const cudaError_t e = launch_pdl(true, kern, dim3((unsigned)ctas), dim3(kGT), 0, s, *map,
+  constexpr int RT = g_rows_per_cta<T>();
+  const int64_t ctas = (re - rb + RT - 1) / RT;
+  auto kern =
+    MODE == 2 && so.from_zero ? k_g27_vtma<T, MODE, true, PTS> : k_g27_vtma<T, MODE, false, PTS>;
+  const cudaError_t e = launch_pdl(pdl, kern, dim3((unsigned)ctas), dim3(RT), 0, s, *map,
                                    view(gr), rb, re, b, x, y, so, device_error_flag());
   *st = e == cudaSuccess ? LGX_OK : cuda_fail(e, "k_g27_vtma");
   count_launch();
@@ -633,9 +648,13 @@ static lgx_status launch_g27_pts(const Grid27 &gr, const VT *v, int64_t rb, int6
       return LGX_OK;
     }
   }
+  // float rows take the value-staged kernel; FP64 rows stay on k_g27_rows:
+  // they are FP64-pipe bound, and staging their 216 bytes of values per row
+  // leaves too few warps per SM to cover the FMA chains (measured at 256^3:
+  // FP64 SOR sweep 1.198 -> 1.328 ms, FP64 AMG-PCG 420 -> 480 ms)
   if constexpr (std::is_same_v<VT, float> && std::is_same_v<XT, float>) {
     lgx_status st = LGX_OK;
-    if (g27_tma_launch<MODE, PTS>(gr, v, rb, re, b, x, y, so, s, &st)) return st;
+    if (g27_tma_launch<VT, MODE, PTS>(gr, v, rb, re, b, x, y, so, pdl, s, &st)) return st;
   }
   LGX_CUDA(launch_pdl(pdl, k_g27_rows<VT, XT, MODE, PTS>, dim3((unsigned)((rows + 255) / 256)),
                       dim3(256), 0, s, view(gr), rb, re, v, b, x, y, scale, so));

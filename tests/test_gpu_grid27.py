@@ -122,12 +122,12 @@ def test_standalone_colouring_grid_sweeps(cuda, forward):
     assert not cuda.Colouring.from_array(m7, _parity(dims), 8).use_grid27(dims)
 
 
-# Float values and vectors on grids whose colour blocks are whole 256-row
-# tiles run the staged kernel (bulk copies into shared memory, two stages
-# per CTA); these sizes give more tiles than CTAs, so CTAs also compute from
-# their second stage.  Every result equals the CSR kernels' bit for bit.
+# Grids of more than a hundred thousand rows: the value-staged kernels (one
+# tensor copy of a CTA's value planes, FP64 and float, sweeps from zero and
+# from a given x) against the CSR kernels, bit for bit, in sweeps, V-cycles
+# and solves.
 @pytest.mark.parametrize("dims", [(48, 48, 48), (32, 64, 40)])
-def test_grid_float_staged_tiles_equal_csr(cuda, dims):
+def test_grid_staged_values_equal_csr(cuda, dims):
     m = cuda.gen_27pt(dims, _k(dims, 12))
     plain = cuda.Colouring.from_array(m, _parity(dims), 8)
     grid = cuda.Colouring.from_array(m, _parity(dims), 8)
@@ -136,13 +136,16 @@ def test_grid_float_staged_tiles_equal_csr(cuda, dims):
     b = cuda.permute(plain, rng.uniform(-1, 1, m.row_num())).float()
     x0 = cuda.permute(plain, rng.uniform(-1, 1, m.row_num())).float()
     for forward in (1, 0):
-        xa, xb = x0.clone(), x0.clone()
-        cuda.sor_sweep_permuted(plain, b, xa, forward=forward)
-        cuda.sor_sweep_permuted(grid, b, xb, forward=forward)
-        np.testing.assert_array_equal(xa.cpu().numpy(), xb.cpu().numpy())
+        for dt in (b.dtype, b.double().dtype):
+            xa, xb = x0.to(dt), x0.to(dt)
+            cuda.sor_sweep_permuted(plain, b.to(dt), xa, forward=forward)
+            cuda.sor_sweep_permuted(grid, b.to(dt), xb, forward=forward)
+            np.testing.assert_array_equal(xa.cpu().numpy(), xb.cpu().numpy())
+    bb = np.random.default_rng(14).uniform(-1, 1, m.row_num())
+    h64g, h64c = _pair(cuda, m, dims)
+    np.testing.assert_array_equal(h64g.vcycle(bb).cpu().numpy(), h64c.vcycle(bb).cpu().numpy())
     hg, hc = _pair(cuda, m, dims, cycle_f32=True)
     assert hg.grid27_active()
-    bb = np.random.default_rng(14).uniform(-1, 1, m.row_num())
     np.testing.assert_array_equal(hg.vcycle(bb).cpu().numpy(), hc.vcycle(bb).cpu().numpy())
     for refine in (0, 2):
         kw = dict(refine=refine) if refine else dict(flexible=True)
