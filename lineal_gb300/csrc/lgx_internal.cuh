@@ -140,9 +140,11 @@ struct Grid27 {
   DBuf<float> v32;
   DBuf<bf16> v16;
   const void *src64 = nullptr, *src32 = nullptr, *src16 = nullptr;
-  // tensor map of the float values (a CUtensorMap, encoded on first use)
+  // tensor maps of the float and FP64 values (CUtensorMaps, encoded on
+  // first use)
   alignas(64) mutable unsigned char vmap32[128] = {};
-  mutable const void *vmap32_key = nullptr;
+  alignas(64) mutable unsigned char vmap64[128] = {};
+  mutable const void *vmap32_key = nullptr, *vmap64_key = nullptr;
 };
 
 // Csr::tuned index of a value type
