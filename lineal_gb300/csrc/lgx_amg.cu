@@ -50,13 +50,18 @@ __global__ void k_iota(int64_t n, int32_t *out) {
     out[i] = (int32_t)i;
 }
 
+// the diagonal of every row; rd (FP64 values): 1 / d correctly rounded, or
+// 0 where |d| lies outside [2^-400, 2^400] (or is not finite) and the
+// quotients divide
 template <typename VT>
 __global__ void k_row_diag(int64_t n, const int64_t *rowptr, const int32_t *col, const VT *val,
-                           VT *diag) {
+                           VT *diag, double *rd) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t k = find_col(rowptr, col, i, (int32_t)i);
-    diag[i] = k >= 0 ? val[k] : VT(0);
+    const VT d = k >= 0 ? val[k] : VT(0);
+    diag[i] = d;
+    if (rd) rd[i] = exponent_within_400((double)d) ? 1.0 / (double)d : 0.0;
   }
 }
 
@@ -78,35 +83,88 @@ __device__ __forceinline__ VT edge_strength(int64_t i, int64_t e, const int64_t 
   return nn * opp / diag[j];
 }
 
+// the same quotient through the reciprocal table rd (FP64: the correctly
+// rounded quotient in five FP64 operations where rd marks d and the
+// numerator lies in range; otherwise the division)
 template <typename VT>
-__global__ void k_strength(int64_t n, const int64_t *rowptr, const int32_t *col, const VT *val,
-                           const VT *diag, int symmetric, VT theta, uint8_t *dep, uint8_t *inf,
-                           uint8_t *iso) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
+__device__ __forceinline__ VT edge_strength_rd(int64_t i, int64_t e, const int64_t *rowptr,
+                                               const int32_t *col, const VT *val, const VT *diag,
+                                               const double *rd, int symmetric) {
+  if constexpr (sizeof(VT) != 8) {
+    return edge_strength(i, e, rowptr, col, val, diag, symmetric);
+  } else {
+    const int32_t j = col[e];
+    const VT w = -val[e];
+    const VT nn = w > VT(0) ? w : VT(0);
+    VT opp;
+    if (symmetric) {
+      opp = nn;
+    } else {
+      const int64_t r = find_col(rowptr, col, j, (int32_t)i);
+      const VT wr = r >= 0 ? -val[r] : VT(0);
+      opp = r >= 0 ? (wr > VT(0) ? wr : VT(0)) : VT(0);
+    }
+    const double num = nn * opp, y = rd[j];
+    return (nonzero_bits(y) && exponent_within_400(num)) ? div_by_recip(num, diag[j], y)
+                                                         : num / diag[j];
+  }
+}
+
+// Strength flags of every row, one warp per row and a lane per entry: the
+// row's largest off-diagonal strength, then per edge dep = s > theta * max,
+// the reverse entry's inf flag (found by binary search in the head's row),
+// and iso when no edge is strong.  The entries' searches run side by side
+// (a thread per row walked 27 searches one after another: 19.6 ms at 256^3);
+// a warp walks a contiguous run of rows;
+// the row maximum is reduced with the sequential comparison (s > m), so it
+// is the sequential maximum.
+template <typename VT>
+__global__ void k_strength_warp(int64_t n, const int64_t *rowptr, const int32_t *col,
+                                const VT *val, const VT *diag, const double *rd, int symmetric,
+                                VT theta, uint8_t *dep, uint8_t *inf, uint8_t *iso) {
+  const int lane = threadIdx.x & 31;
+  // each warp a contiguous run of rows: consecutive rows search mostly the
+  // same neighbour rows, which then come from L1
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t per = (n + nw - 1) / nw;
+  const int64_t i0 = w * per, i1 = i0 + per < n ? i0 + per : n;
+  for (int64_t i = i0; i < i1; ++i) {
     const int64_t b = rowptr[i], e = rowptr[i + 1];
     VT maxs = VT(0);
-    for (int64_t k = b; k < e; ++k) {
+    // a lane's first two strengths stay in registers for the second pass (the
+    // FP64 division in each is what bounds this kernel on GB300)
+    VT keep0 = VT(0), keep1 = VT(0);
+    for (int64_t k = b + lane, m = 0; k < e; k += 32, ++m) {
       if (col[k] == i) continue;
-      const VT s = edge_strength(i, k, rowptr, col, val, diag, symmetric);
-      if (s > maxs) maxs = s;
+      const VT sk = edge_strength_rd(i, k, rowptr, col, val, diag, rd, symmetric);
+      if (m == 0) keep0 = sk;
+      else if (m == 1) keep1 = sk;
+      if (sk > maxs) maxs = sk;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const VT other = __shfl_xor_sync(0xffffffffu, maxs, o);
+      if (other > maxs) maxs = other;
     }
     const VT lb = theta * maxs;
     bool any = false;
-    for (int64_t k = b; k < e; ++k) {
+    for (int64_t k = b + lane, m = 0; k < e; k += 32, ++m) {
       const int32_t j = col[k];
       if (j == i) {
         dep[k] = 0;
         continue;
       }
-      const VT s = edge_strength(i, k, rowptr, col, val, diag, symmetric);
-      const bool cond = s > lb;
+      const VT sk = m == 0   ? keep0
+                    : m == 1 ? keep1
+                             : edge_strength_rd(i, k, rowptr, col, val, diag, rd, symmetric);
+      const bool cond = sk > lb;
       any = any || cond;
       dep[k] = cond;
       const int64_t r = find_col(rowptr, col, j, (int32_t)i);
       if (r >= 0) inf[r] = cond;
     }
-    iso[i] = !any;
+    any = __any_sync(0xffffffffu, any);
+    if (lane == 0) iso[i] = !any;
   }
 }
 
@@ -121,25 +179,27 @@ lgx_status strength(const Csr &a, double theta, uint8_t *dep, uint8_t *inf, uint
   const int64_t n = a.n;
   if (n == 0) return LGX_OK;
   const unsigned g = (unsigned)std::min<int64_t>(grid_for(n, 128), 65535);
+  const unsigned gw = (unsigned)std::min<int64_t>(grid_for(n, 8), 16384);  // warp per row
   // diagonal entries of the diagonal itself carry no influence flag
   k_fill_u8<<<std::min<int64_t>(grid_for(a.nnz, 256), 16384), 256, 0, s>>>(a.nnz, inf, 0);
   LGX_LAUNCH_CHECK();
   if (a.storage == LGX_F64) {
-    DBuf<double> d;
+    DBuf<double> d, rd;
     LGX_CHECK(d.alloc(n));
-    k_row_diag<double><<<g, 128, 0, s>>>(n, a.rowptr.p, a.col.p, a.v64.p, d.p);
+    LGX_CHECK(rd.alloc(n));
+    k_row_diag<double><<<g, 128, 0, s>>>(n, a.rowptr.p, a.col.p, a.v64.p, d.p, rd.p);
     LGX_LAUNCH_CHECK();
-    k_strength<double><<<g, 128, 0, s>>>(n, a.rowptr.p, a.col.p, a.v64.p, d.p, a.symmetric, theta,
-                                         dep, inf, iso);
+    k_strength_warp<double><<<gw, 256, 0, s>>>(n, a.rowptr.p, a.col.p, a.v64.p, d.p, rd.p,
+                                               a.symmetric, theta, dep, inf, iso);
     LGX_LAUNCH_CHECK();
     LGX_CUDA(cudaStreamSynchronize(s));
   } else {
     DBuf<float> d;
     LGX_CHECK(d.alloc(n));
-    k_row_diag<float><<<g, 128, 0, s>>>(n, a.rowptr.p, a.col.p, a.v32.p, d.p);
+    k_row_diag<float><<<g, 128, 0, s>>>(n, a.rowptr.p, a.col.p, a.v32.p, d.p, nullptr);
     LGX_LAUNCH_CHECK();
-    k_strength<float><<<g, 128, 0, s>>>(n, a.rowptr.p, a.col.p, a.v32.p, d.p, a.symmetric,
-                                        (float)theta, dep, inf, iso);
+    k_strength_warp<float><<<gw, 256, 0, s>>>(n, a.rowptr.p, a.col.p, a.v32.p, d.p, nullptr,
+                                              a.symmetric, (float)theta, dep, inf, iso);
     LGX_LAUNCH_CHECK();
     LGX_CUDA(cudaStreamSynchronize(s));
   }

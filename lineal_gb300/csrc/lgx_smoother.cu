@@ -201,17 +201,20 @@ __global__ void k_perm_rowlen(int64_t n, const int64_t *rowptr, const int32_t *p
   }
 }
 
+// one warp per permuted row: the row's entries copy coalesced (a thread
+// per row walked 32 scattered rows per warp instruction: 216 GB/s at 256^3)
 template <typename VT>
 __global__ void k_perm_fill(int64_t n, const int64_t *rowptr, const int32_t *col, const VT *val,
                             const int32_t *perm, const int32_t *iperm, const int64_t *prowptr,
                             int32_t *pcol, VT *pval) {
-  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n;
-       r += (int64_t)gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; r < n; r += nw) {
     const int64_t i = perm[r];
-    int64_t o = prowptr[r];
-    for (int64_t k = rowptr[i]; k < rowptr[i + 1]; ++k, ++o) {
-      pcol[o] = iperm[col[k]];
-      pval[o] = val[k];
+    const int64_t b = rowptr[i], len = rowptr[i + 1] - b, o = prowptr[r];
+    for (int64_t k = lane; k < len; k += 32) {
+      pcol[o + k] = iperm[col[b + k]];
+      pval[o + k] = val[b + k];
     }
   }
 }
