@@ -1062,10 +1062,11 @@ def run_batch(args):
 
 def run_profile(args):
     """Profiler target: one untimed AMG-PCG solve of the --grid^3 27-point
-    workload (FP64, or the float cycle with --mixed, with bfloat16 level values
-    with --bf16; row engine autotuned unless --no-autotune), then one more
-    inside the NVTX range "solve" (ncu --nvtx --nvtx-include solve/ selects
-    its kernels)."""
+    workload (FP64, or the float cycle with --mixed -- the float-vector CG with
+    reliable updates with --profile-refined -- with bfloat16 level values with
+    --bf16; the bench's hierarchy options; row engine autotuned unless
+    --no-autotune), then one more inside the NVTX range "solve" (ncu --nvtx
+    --nvtx-include solve/ selects its kernels)."""
     import torch
 
     import lineal_gb300 as g
@@ -1078,18 +1079,23 @@ def run_profile(args):
     h = g.HierarchyWright(min_coarsen_size=2000, cycle_f32=mixed, cycle_bf16=args.bf16,
                           partition_size=args.partition_size,
                           partition_growth=args.partition_growth,
-                          min_partitions=args.min_partitions,
-                          grid27=args.grid27).instantiate(a, finest_colouring=col)
+                          min_partitions=args.min_partitions, grid27=args.grid27,
+                          coarse_smallest_last=args.coarse_smallest_last).instantiate(
+        a, finest_colouring=col)
     if args.autotune:
         h.autotune(reps=3)
     b = torch.as_tensor(b_host, device="cuda")
-    res = g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=1e-8, maxit=500)
+    # --mixed --profile-refined: the float-vector CG with reliable updates
+    kw = (dict(refine=args.refine, inner_rtol=args.inner_rtol, flexible=args.refine_flexible)
+          if mixed and args.profile_refined else {})
+    res = g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=1e-8, maxit=500, **kw)
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_push("solve")
-    res = g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=1e-8, maxit=500)
+    res = g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=1e-8, maxit=500, **kw)
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
-    form = "bf16" if args.bf16 else "mixed" if args.mixed else "fp64"
+    form = ("bf16" if args.bf16 else "mixed refined" if kw else "mixed" if args.mixed
+            else "fp64")
     log(f"[profile] {form} solve: {res.iterations} it")
 
 
@@ -1235,6 +1241,8 @@ def main():
                     choices=["solve", "kernels", "stencil", "adjoint", "batch", "multi",
                              "profile"])
     ap.add_argument("--mixed", action="store_true", help="--mode profile: the float cycle")
+    ap.add_argument("--profile-refined", action="store_true",
+                    help="--mode profile --mixed: the float-vector CG (--refine)")
     ap.add_argument("--bf16", action="store_true",
                     help="--mode profile: the float cycle with bfloat16 level values")
     ap.add_argument("--batch-systems", type=int, default=1024)
