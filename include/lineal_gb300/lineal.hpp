@@ -133,6 +133,41 @@ class DenseVector : public SharedVectorBase {
   [[nodiscard]] Value *data() { return p_; }
   [[nodiscard]] const Value *data() const { return p_; }
 
+  // Host element access (dense/vector/shared.hpp:268-310): the vector lives
+  // in device memory, so every access is one synchronous copy of one
+  // element -- for inspection and set-up, not for loops over the vector.
+  // compute / store run on the environment's stream (after the work queued
+  // there); operator[] uses a blocking copy, ordered after the legacy
+  // default stream and every blocking stream.
+  class ElementRef {
+   public:
+    ElementRef(DenseVector &v, Size i) : v_(v), i_(i) {}
+    operator Value() const { return v_.read(i_); }  // NOLINT: a value proxy
+    ElementRef &operator=(Value x) {
+      v_.write(i_, x);
+      return *this;
+    }
+    ElementRef &operator=(const ElementRef &o) { return *this = (Value)o; }
+
+   private:
+    DenseVector &v_;
+    Size i_;
+  };
+  [[nodiscard]] Value operator[](Size i) const { return read(i); }
+  [[nodiscard]] ElementRef operator[](Size i) { return ElementRef(*this, i); }
+  [[nodiscard]] Value compute(Size i, const Environment &env) const {
+    bounds(i);
+    Value h{};
+    check_cuda(cudaMemcpyAsync(&h, p_ + i, sizeof(Value), cudaMemcpyDeviceToHost, env.stream()));
+    check_cuda(cudaStreamSynchronize(env.stream()));
+    return h;
+  }
+  void store(Size i, Value v, const Environment &env) {
+    bounds(i);
+    check_cuda(cudaMemcpyAsync(p_ + i, &v, sizeof(Value), cudaMemcpyHostToDevice, env.stream()));
+    check_cuda(cudaStreamSynchronize(env.stream()));
+  }
+
   void upload(const std::vector<Value> &h, const Environment &env) {
     check_cuda(cudaMemcpyAsync(p_, h.data(), n_ * sizeof(Value), cudaMemcpyHostToDevice,
                                env.stream()));
@@ -149,6 +184,19 @@ class DenseVector : public SharedVectorBase {
  private:
   void alloc() {
     if (n_) check_cuda(cudaMalloc(&p_, n_ * sizeof(Value)));
+  }
+  void bounds(Size i) const {
+    if (i >= n_) throw std::out_of_range("DenseVector element index out of range");
+  }
+  [[nodiscard]] Value read(Size i) const {
+    bounds(i);
+    Value h{};
+    check_cuda(cudaMemcpy(&h, p_ + i, sizeof(Value), cudaMemcpyDeviceToHost));
+    return h;
+  }
+  void write(Size i, Value v) {
+    bounds(i);
+    check_cuda(cudaMemcpy(p_ + i, &v, sizeof(Value), cudaMemcpyHostToDevice));
   }
   Size n_ = 0;
   Value *p_ = nullptr;
@@ -218,6 +266,106 @@ class CsrMatrix : public MatrixHandle {
     check(lgx_gen_27pt(dims, k.data(), storage, env.stream(), &h));
     return CsrMatrix(h);
   }
+};
+
+// Host row access to a CSR matrix (csr/shared.hpp:120-333, 926-1036): one
+// download of the whole matrix (rows, sorted columns, values), then rows with
+// lineal's ConstRow interface -- size, index, column indices, find /
+// contains, value by column, iterate over all entries or split around the
+// diagonal.  The matrix stays in device memory; the snapshot does not follow
+// later changes.  An iterate operation that returns a std::optional ends the
+// walk at the first engaged value and returns it (lineal's valued returns).
+class HostCsr {
+ public:
+  using Size = std::size_t;
+  using Value = double;
+  using ColumnIdx = int32_t;
+
+  class ConstRow {
+   public:
+    ConstRow(const int32_t *col, const double *val, Size row, Size nnz)
+        : col_(col), val_(val), row_(row), nnz_(nnz) {}
+    [[nodiscard]] Size index() const { return row_; }
+    [[nodiscard]] Size size() const { return nnz_; }
+    [[nodiscard]] Size offdiagonal_num() const { return contains((ColumnIdx)row_) ? nnz_ - 1 : nnz_; }
+    [[nodiscard]] std::vector<ColumnIdx> column_indices() const {
+      return std::vector<ColumnIdx>(col_, col_ + nnz_);
+    }
+    // position of column c among the row's entries, or none
+    [[nodiscard]] std::optional<Size> find(ColumnIdx c) const {
+      const int32_t *it = std::lower_bound(col_, col_ + nnz_, c);
+      if (it == col_ + nnz_ || *it != c) return std::nullopt;
+      return (Size)(it - col_);
+    }
+    [[nodiscard]] bool contains(ColumnIdx c) const { return find(c).has_value(); }
+    // the entry in column c (an absent column is an error: lineal asserts)
+    [[nodiscard]] Value operator[](ColumnIdx c) const {
+      const auto k = find(c);
+      if (!k) throw std::out_of_range("HostCsr row has no entry in this column");
+      return val_[*k];
+    }
+    [[nodiscard]] Value back() const { return val_[nnz_ - 1]; }
+    [[nodiscard]] ColumnIdx back_column() const { return col_[nnz_ - 1]; }
+    // op(column, value) for every entry in column order
+    template <typename Op>
+    auto iterate(Op op) const {
+      using Ret = decltype(op(ColumnIdx{}, Value{}));
+      for (Size k = 0; k < nnz_; ++k) {
+        if constexpr (is_optional<Ret>) {
+          if (auto r = op(col_[k], val_[k])) return r;
+        } else {
+          op(col_[k], val_[k]);
+        }
+      }
+      if constexpr (is_optional<Ret>) return Ret{};
+    }
+    // before(column, value) for the columns left of the diagonal,
+    // diagonal(column, value) for the diagonal, after(...) for the rest
+    template <typename B, typename D, typename A>
+    void iterate(B before, D diagonal, A after) const {
+      for (Size k = 0; k < nnz_; ++k) {
+        const ColumnIdx c = col_[k];
+        if ((Size)c < row_) before(c, val_[k]);
+        else if ((Size)c == row_) diagonal(c, val_[k]);
+        else after(c, val_[k]);
+      }
+    }
+
+   private:
+    template <typename T>
+    struct optional_check : std::false_type {};
+    template <typename T>
+    struct optional_check<std::optional<T>> : std::true_type {};
+    template <typename T>
+    static constexpr bool is_optional = optional_check<T>::value;
+
+    const int32_t *col_;
+    const double *val_;
+    Size row_, nnz_;
+  };
+
+  static HostCsr download(const CsrMatrix &m, const Environment &env) {
+    HostCsr h;
+    const Size n = m.row_num(), nnz = m.non_zero_num();
+    h.rowptr_.resize(n + 1);
+    h.col_.resize(nnz);
+    h.val_.resize(nnz);
+    check(lgx_csr_download(m.handle(), h.rowptr_.data(), h.col_.data(), h.val_.data(),
+                           env.stream()));
+    return h;
+  }
+  [[nodiscard]] Size row_num() const { return rowptr_.empty() ? 0 : rowptr_.size() - 1; }
+  [[nodiscard]] Size non_zero_num() const { return col_.size(); }
+  [[nodiscard]] ConstRow operator[](Size row) const {
+    if (row >= row_num()) throw std::out_of_range("HostCsr row index out of range");
+    const int64_t b = rowptr_[row];
+    return ConstRow(col_.data() + b, val_.data() + b, row, (Size)(rowptr_[row + 1] - b));
+  }
+
+ private:
+  std::vector<int64_t> rowptr_;
+  std::vector<int32_t> col_;
+  std::vector<double> val_;
 };
 
 // BoxInfo (discretization/box-equidistant.hpp:57-110): cell counts and axis

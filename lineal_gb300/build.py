@@ -83,8 +83,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
 
 def build_cpp_demo(verbose: bool = False, name: str = "concepts_demo") -> str:
     """Compiles a C++ concept-layer program of tests/cpp (concepts_demo,
-    direct_demo, vector_demo, aggs_io_demo, aggs_solver_demo) that drives the library through
-    include/lineal_gb300/lineal.hpp."""
+    direct_demo, vector_demo, aggs_io_demo, aggs_solver_demo, access_demo)
+    that drives the library through include/lineal_gb300/lineal.hpp."""
     lib = build(verbose=verbose)
     src = os.path.join(ROOT, "tests", "cpp", name + ".cpp")
     out = os.path.join(OUT_DIR, name)

@@ -76,7 +76,7 @@ def test_concept_layer_compiles_and_links(library):
     from lineal_gb300 import build
 
     for name in ("concepts_demo", "direct_demo", "vector_demo", "aggs_io_demo",
-                 "aggs_solver_demo"):
+                 "aggs_solver_demo", "access_demo"):
         exe = build.build_cpp_demo(name=name)
         assert os.path.isfile(exe) and os.access(exe, os.X_OK)
 
