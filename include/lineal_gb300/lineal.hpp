@@ -304,6 +304,14 @@ class HostCsr {
       if (!k) throw std::out_of_range("HostCsr row has no entry in this column");
       return val_[*k];
     }
+    // the diagonal entry (lineal's rows always store it)
+    [[nodiscard]] Value diagonal() const { return (*this)[(ColumnIdx)row_]; }
+    // position of column c among the row's off-diagonal entries
+    [[nodiscard]] Size offdiagonal_index_within(ColumnIdx c) const {
+      const auto k = find(c);
+      if (!k || (Size)c == row_) throw std::out_of_range("no off-diagonal entry in this column");
+      return *k - ((Size)c > row_ && contains((ColumnIdx)row_) ? 1 : 0);
+    }
     [[nodiscard]] Value back() const { return val_[nnz_ - 1]; }
     [[nodiscard]] ColumnIdx back_column() const { return col_[nnz_ - 1]; }
     // op(column, value) for every entry in column order
@@ -355,7 +363,15 @@ class HostCsr {
     return h;
   }
   [[nodiscard]] Size row_num() const { return rowptr_.empty() ? 0 : rowptr_.size() - 1; }
+  [[nodiscard]] Size column_num() const { return row_num(); }
   [[nodiscard]] Size non_zero_num() const { return col_.size(); }
+  [[nodiscard]] Value diagonal_at(Size row) const { return (*this)[row].diagonal(); }
+  [[nodiscard]] Value entry_at(Size row, ColumnIdx c) const { return (*this)[row][c]; }
+  // the CSR arrays themselves (csr/shared.hpp row_offsets / column_indices /
+  // entries)
+  [[nodiscard]] const std::vector<int64_t> &row_offsets() const { return rowptr_; }
+  [[nodiscard]] const std::vector<int32_t> &column_indices() const { return col_; }
+  [[nodiscard]] const std::vector<double> &entries() const { return val_; }
   [[nodiscard]] ConstRow operator[](Size row) const {
     if (row >= row_num()) throw std::out_of_range("HostCsr row index out of range");
     const int64_t b = rowptr_[row];

@@ -45,6 +45,8 @@ int main() {
     const auto m = lg::CsrMatrix::from_host(rowptr, col, val, lg::IsSymmetric{false});
     const auto h = lg::HostCsr::download(m, env);
     if (h.row_num() != (std::size_t)n || h.non_zero_num() != col.size()) return fail("sizes");
+    if (h.row_offsets() != rowptr || h.column_indices() != col || h.entries() != val)
+      return fail("arrays");
     for (int64_t i = 0; i < n; ++i) {
       const auto row = h[(std::size_t)i];
       const auto len = (std::size_t)(rowptr[i + 1] - rowptr[i]);
@@ -58,6 +60,16 @@ int main() {
         if (!row.find(c) || *row.find(c) != k) return fail("find");
       }
       if (row.contains((int32_t)(i + 5)) || row.find((int32_t)(i + 5))) return fail("absent");
+      if (row.diagonal() != h.diagonal_at((std::size_t)i) ||
+          h.entry_at((std::size_t)i, (int32_t)i) != row[(int32_t)i])
+        return fail("diagonal");
+      // off-diagonal positions skip the diagonal
+      std::size_t off = 0;
+      for (std::size_t q = 0; q < len; ++q) {
+        const int32_t c = col[(std::size_t)rowptr[i] + q];
+        if (c == i) continue;
+        if (row.offdiagonal_index_within(c) != off++) return fail("offdiagonal_index_within");
+      }
       // the full walk in column order
       std::size_t k = 0;
       bool ordered = true;

@@ -134,6 +134,33 @@ def test_hierarchy_bitexact(cuda, coarse_f32, agg_kernel):
             np.testing.assert_array_equal(agg, oh.level_agg(l))
 
 
+def test_hierarchy_bitexact_large_aggregates(cuda):
+    """Aggregates of 24 to 48 rows: coarse rows gather up to 48 * 27 fine
+    entries, beyond the 512 the warp-per-row Galerkin product stages, so
+    those rows take the thread-per-row product while the smaller ones stay
+    on the warp kernel; every level equals the oracle's bit for bit."""
+    ref = _case((18, 20, 22))
+    m = _dev(cuda, ref)
+    params = dict(PARAMS, min_aggregate_size=24, max_aggregate_size=48)
+    h = cuda.HierarchyWright(**params).instantiate(m)
+    oh = lo.Amg(ref, smoother_parts=0, **params)
+    rows, _ = h.sizes()
+    assert len(rows) == oh.nlevels >= 2
+    for l in range(oh.nlevels):
+        rowptr, col, val, agg = h.level(l)
+        rl = oh.level_csr(l)
+        np.testing.assert_array_equal(rowptr, rl.rowptr)
+        np.testing.assert_array_equal(col, rl.col)
+        np.testing.assert_array_equal(val, rl.val)
+    # the first coarse level holds rows gathered from more than 512 entries
+    rowptr0 = oh.level_csr(0).rowptr
+    agg0 = oh.level_agg(0)
+    lens = np.diff(rowptr0)
+    sizes = np.zeros(rows[1], dtype=np.int64)
+    np.add.at(sizes, agg0[agg0 < rows[1]], lens[agg0 < rows[1]])
+    assert sizes.max() > 512 and sizes.min() <= 512
+
+
 @pytest.mark.parametrize("coarse_f32", [False, True])
 def test_vcycle_matches_oracle(cuda, coarse_f32):
     ref = _case()
