@@ -503,12 +503,17 @@ lgx_status lgx_amg_level_lists(const lgx_amg *h, int64_t level, int64_t *h_list_
 /* CholeskySolver (direct/cholesky/solver.hpp:22-67, kind
  * LGX_DIRECT_CHOLESKY) or LuSolver (direct/lu/solver.hpp:21-66, kind
  * LGX_DIRECT_LU) as the dense FP64 solve the AMG uses on its coarsest level:
- * lgx_direct_create inverts the CSR matrix once by Gauss-Jordan elimination
- * without pivoting (Cholesky: every pivot positive, else LGX_ERR_NOT_SPD;
- * LU: every pivot nonzero and finite, else LGX_ERR_BREAKDOWN — lineal's LU
- * does not pivot either) and synchronises `stream`; lgx_direct_solve
+ * lgx_direct_create forms the inverse once -- Cholesky: the dense Cholesky
+ * factor (every pivot positive, else LGX_ERR_NOT_SPD) and the inverse from
+ * it; LU: Gauss-Jordan elimination without pivoting (every pivot nonzero,
+ * finite and not tiny against its row, else LGX_ERR_BREAKDOWN — lineal's LU
+ * does not pivot either) -- and synchronises `stream`; lgx_direct_solve
  * computes x = A^-1 b with one dense product (b and x distinct device
- * vectors of n doubles).  Dense storage: n <= LGX_DIRECT_MAX_ROWS. */
+ * vectors of n doubles).  Dense storage: n <= LGX_DIRECT_MAX_ROWS.  Beyond
+ * that, Cholesky factors in a band (lineal's factor, cholesky/decomposition
+ * .hpp:52-107, fills the lower envelope of the natural order: the band of
+ * width max_i (i - first column of row i)), at most 2^31 band values, and
+ * each solve is a forward and a backward substitution; LU refuses. */
 #define LGX_DIRECT_MAX_ROWS 8192
 enum { LGX_DIRECT_CHOLESKY = 0, LGX_DIRECT_LU = 1 };
 typedef struct lgx_direct lgx_direct;

@@ -942,11 +942,13 @@ class Hierarchy:
 
 
 class DirectSolver:
-    """Dense FP64 direct solver: lineal's CholeskySolver (positive pivots) or
+    """FP64 direct solver: lineal's CholeskySolver (positive pivots) or
     LuSolver (nonzero pivots, no pivoting), direct/cholesky/solver.hpp:22-67,
     direct/lu/solver.hpp:21-66.  ``lu=None`` picks Cholesky for a matrix
-    created symmetric.  The inverse is formed once, each solve is one dense
-    product.  At most DIRECT_MAX_ROWS rows."""
+    created symmetric.  Up to DIRECT_MAX_ROWS rows the inverse is formed
+    once and each solve is one dense product; beyond, Cholesky factors in
+    the band of the matrix's lower envelope and solves by substitution (LU
+    refuses)."""
 
     def __init__(self, a: CsrMatrix, lu: bool | None = None):
         if lu is None:

@@ -1932,6 +1932,206 @@ __global__ void __launch_bounds__(256) k_bgram(int64_t n, const double *x, doubl
     }
 }
 
+// ===========================================================================
+// Banded Cholesky for the standalone solver beyond the dense limit.
+// lineal's CholeskySolver (cholesky/decomposition.hpp:52-107) factors row by
+// row in the natural order (Cholesky-Banachiewicz, no reordering): row i of
+// L fills every column from its first nonzero up to i, so the factor is the
+// matrix's lower envelope -- a band of width bw = max_i (i - first column of
+// row i).  Here the band is stored by rows, (bw + 1) values per row (column
+// j of row i at j - i + bw), and factored with the dense form's 32-column
+// panels restricted to the band window: k_band_panel factors the panel's
+// diagonal block (in every CTA) and solves the rows below it that reach the
+// panel; k_band_trail updates the window below and right of the panel.
+// Entries outside the band are exact zeros of the factor and never stored.
+// Each solve is a forward and a backward substitution by 32-row blocks in
+// one CTA (k_band_fwd, k_band_bwd): a block's products with the band run
+// over 32 warps, its triangle in one warp.  FP64 throughout; the sums run in
+// another order than lineal's, so results agree to rounding.
+// ===========================================================================
+struct Band {
+  int64_t n, bw, ld;
+  double *b;
+  __device__ __forceinline__ double get(int64_t i, int64_t j) const {
+    return (i - j <= bw && j <= i) ? b[i * ld + (j - i + bw)] : 0.0;
+  }
+  __device__ __forceinline__ double *at(int64_t i, int64_t j) const {
+    return b + i * ld + (j - i + bw);
+  }
+};
+
+__global__ void k_band_width(int64_t n, const int64_t *rowptr, const int32_t *col,
+                             unsigned long long *bw) {
+  __shared__ unsigned long long part[8];
+  unsigned long long m = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    if (rowptr[i + 1] > rowptr[i]) {
+      const int64_t j = col[rowptr[i]];
+      if (j < i && (unsigned long long)(i - j) > m) m = (unsigned long long)(i - j);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long q = __shfl_xor_sync(0xffffffffu, m, o);
+    m = q > m ? q : m;
+  }
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = part[w] > m ? part[w] : m;
+    atomicMax(bw, m);
+  }
+}
+
+// the lower triangle of the CSR matrix into the band (zeros elsewhere)
+__global__ void k_band_fill(Band B, const int64_t *rowptr, const int32_t *col, const double *v64,
+                            const float *v32) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < B.n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    for (int64_t e = rowptr[i]; e < rowptr[i + 1]; ++e) {
+      const int64_t j = col[e];
+      if (j <= i) *B.at(i, j) = v64 ? v64[e] : (double)v32[e];
+    }
+}
+
+// panel [k0, k0 + nb): rows [k1, min(n, k1 + bw)) reach it
+__global__ void __launch_bounds__(256) k_band_panel(Band B, int64_t k0, int *bad) {
+  __shared__ double D[kCb][kCb + 1];
+  if (*bad) return;
+  const int64_t n = B.n;
+  const int nb = (int)(n - k0 < kCb ? n - k0 : kCb);
+  const int64_t k1 = k0 + nb, rend = k1 + B.bw < n ? k1 + B.bw : n;
+  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
+    const int r = t / nb, c = t % nb;
+    D[r][c] = c <= r ? B.get(k0 + r, k0 + c) : 0.0;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const bool ok = bchol_diag(D, nb);
+    if (!ok && threadIdx.x == 0) atomicOr(bad, 1);
+  }
+  __syncthreads();
+  if (blockIdx.x == 0)
+    for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
+      const int r = t / nb, c = t % nb;
+      if (c <= r && r - c <= B.bw) *B.at(k0 + r, k0 + c) = D[r][c];
+    }
+  const int64_t i = k1 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= rend) return;
+  double x[kCb];
+#pragma unroll
+  for (int j = 0; j < kCb; ++j) x[j] = j < nb ? B.get(i, k0 + j) : 0.0;
+#pragma unroll
+  for (int j = 0; j < kCb; ++j) {
+    if (j >= nb) break;
+    double s = x[j];
+#pragma unroll
+    for (int m = 0; m < j; ++m) s = fma(-x[m], D[j][m], s);
+    x[j] = s / D[j][j];
+  }
+#pragma unroll
+  for (int j = 0; j < kCb; ++j)
+    if (j < nb && i - (k0 + j) <= B.bw) *B.at(i, k0 + j) = x[j];
+}
+
+// the window [k1, rend)^2 (lower tiles): A_ij -= L_iK L_jK^T
+__global__ void __launch_bounds__(256) k_band_trail(Band B, int64_t k0, const int *bad) {
+  __shared__ double LI[32][kCb + 1], LJ[32][kCb + 1];
+  if (*bad) return;
+  const int64_t n = B.n;
+  const int nb = (int)(n - k0 < kCb ? n - k0 : kCb);
+  const int64_t k1 = k0 + nb, rend = k1 + B.bw < n ? k1 + B.bw : n;
+  const int64_t t = blockIdx.x;
+  int64_t I = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+  while (I * (I + 1) / 2 > t) --I;
+  while ((I + 1) * (I + 2) / 2 <= t) ++I;
+  const int64_t J = t - I * (I + 1) / 2;
+  const int64_t i0 = k1 + I * 32, j0 = k1 + J * 32;
+  for (int q = threadIdx.x; q < 32 * kCb; q += blockDim.x) {
+    const int r = q / kCb, m = q % kCb;
+    LI[r][m] = (i0 + r < rend && m < nb) ? B.get(i0 + r, k0 + m) : 0.0;
+    LJ[r][m] = (j0 + r < rend && m < nb) ? B.get(j0 + r, k0 + m) : 0.0;
+  }
+  __syncthreads();
+  const int ri = (threadIdx.x >> 4) * 2, cj = (threadIdx.x & 15) * 2;
+  double s00 = 0.0, s01 = 0.0, s10 = 0.0, s11 = 0.0;
+#pragma unroll
+  for (int m = 0; m < kCb; ++m) {
+    const double x0 = LI[ri][m], x1 = LI[ri + 1][m], y0 = LJ[cj][m], y1 = LJ[cj + 1][m];
+    s00 = fma(x0, y0, s00);
+    s01 = fma(x0, y1, s01);
+    s10 = fma(x1, y0, s10);
+    s11 = fma(x1, y1, s11);
+  }
+  const double sv[2][2] = {{s00, s01}, {s10, s11}};
+#pragma unroll
+  for (int u = 0; u < 2; ++u)
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+      const int64_t i = i0 + ri + u, j = j0 + cj + v;
+      if (i < rend && j <= i) *B.at(i, j) -= sv[u][v];
+    }
+}
+
+// L y = b by 32-row blocks, one CTA of 1024 threads: warp r sums row
+// k0 + r's products with the earlier y, warp 0 then solves the block
+__global__ void __launch_bounds__(1024) k_band_fwd(Band B, const double *b, double *y) {
+  __shared__ double part[kCb];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int64_t k0 = 0; k0 < B.n; k0 += kCb) {
+    const int nb = (int)(B.n - k0 < kCb ? B.n - k0 : kCb);
+    if (w < nb) {
+      const int64_t i = k0 + w, j0 = i - B.bw > 0 ? i - B.bw : 0;
+      double s = 0.0;
+      for (int64_t j = j0 + lane; j < k0; j += 32) s = fma(B.get(i, j), y[j], s);
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) part[w] = s;
+    }
+    __syncthreads();
+    if (w == 0) {
+      double rhs = lane < nb ? b[k0 + lane] - part[lane] : 0.0, yv = 0.0;
+      for (int m = 0; m < nb; ++m) {
+        const double ym = __shfl_sync(0xffffffffu, rhs / B.get(k0 + m, k0 + m), m);
+        if (lane == m) yv = ym;
+        if (lane > m && lane < nb) rhs = fma(-B.get(k0 + lane, k0 + m), ym, rhs);
+      }
+      if (lane < nb) y[k0 + lane] = yv;
+    }
+    __syncthreads();
+  }
+}
+
+// L^T x = y by 32-row blocks from the end: warp r sums column k0 + r's
+// products with the later x, warp 0 solves the block's transposed triangle
+__global__ void __launch_bounds__(1024) k_band_bwd(Band B, const double *y, double *x) {
+  __shared__ double part[kCb];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t nblk = (B.n + kCb - 1) / kCb;
+  for (int64_t K = nblk - 1; K >= 0; --K) {
+    const int64_t k0 = K * kCb;
+    const int nb = (int)(B.n - k0 < kCb ? B.n - k0 : kCb);
+    const int64_t k1 = k0 + nb;
+    if (w < nb) {
+      const int64_t j = k0 + w, iend = j + B.bw + 1 < B.n ? j + B.bw + 1 : B.n;
+      double s = 0.0;
+      for (int64_t i = k1 + lane; i < iend; i += 32) s = fma(B.get(i, j), x[i], s);
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) part[w] = s;
+    }
+    __syncthreads();
+    if (w == 0) {
+      double rhs = lane < nb ? y[k0 + lane] - part[lane] : 0.0, xv = 0.0;
+      for (int m = nb - 1; m >= 0; --m) {
+        const double xm = __shfl_sync(0xffffffffu, rhs / B.get(k0 + m, k0 + m), m);
+        if (lane == m) xv = xm;
+        if (lane < m) rhs = fma(-B.get(k0 + m, k0 + lane), xm, rhs);
+      }
+      if (lane < nb) x[k0 + lane] = xv;
+    }
+    __syncthreads();
+  }
+}
+
 // x = A^-1 b, one warp per row
 template <typename XT>
 __global__ void k_dense_apply(int64_t n, const double *ainv, const XT *b, XT *x) {
@@ -2797,7 +2997,62 @@ lgx_status lgx_amg_level_lists(const lgx_amg *h, int64_t level, int64_t *h_list_
 struct lgx_direct {
   int64_t n = 0;
   lgx::DBuf<double> inv;
+  // banded Cholesky beyond the dense limit: bw >= 0, the band and a work
+  // vector for the forward substitution
+  int64_t bw = -1, ld = 0;
+  lgx::DBuf<double> band, y;
 };
+
+namespace lgx {
+// the band may take at most this many values (16 GiB)
+constexpr int64_t kBandMaxEntries = (int64_t)1 << 31;
+
+static lgx_status band_create(const Csr &a, cudaStream_t s, lgx_direct &d) {
+  const int64_t n = a.n;
+  DBuf<unsigned long long> bwd;
+  LGX_CHECK(bwd.alloc(1));
+  LGX_CUDA(cudaMemsetAsync(bwd.p, 0, sizeof(unsigned long long), s));
+  k_band_width<<<(unsigned)std::min<int64_t>(grid_for(n, 256), 4096), 256, 0, s>>>(
+    n, a.rowptr.p, a.col.p, bwd.p);
+  LGX_LAUNCH_CHECK();
+  unsigned long long hbw = 0;
+  LGX_CUDA(cudaMemcpyAsync(&hbw, bwd.p, sizeof(hbw), cudaMemcpyDeviceToHost, s));
+  LGX_CUDA(cudaStreamSynchronize(s));
+  const int64_t bw = (int64_t)hbw, ld = bw + 1;
+  if (ld > kBandMaxEntries / n)
+    return fail(LGX_ERR_INVALID, "the banded Cholesky takes at most 2^31 band values (n = " +
+                                     std::to_string(n) + ", bandwidth " + std::to_string(bw) +
+                                     ")");
+  d.bw = bw;
+  d.ld = ld;
+  LGX_CHECK(d.band.alloc(n * ld));
+  LGX_CHECK(d.y.alloc(n));
+  LGX_CUDA(cudaMemsetAsync(d.band.p, 0, sizeof(double) * n * ld, s));
+  const Band B{n, bw, ld, d.band.p};
+  k_band_fill<<<(unsigned)std::min<int64_t>(grid_for(n, 256), 16384), 256, 0, s>>>(
+    B, a.rowptr.p, a.col.p, a.storage == LGX_F64 ? a.v64.p : nullptr,
+    a.storage == LGX_F32 ? a.v32.p : nullptr);
+  LGX_LAUNCH_CHECK();
+  DBuf<int> bad;
+  LGX_CHECK(bad.alloc(1));
+  LGX_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), s));
+  for (int64_t k0 = 0; k0 < n; k0 += kCb) {
+    const int64_t k1 = std::min<int64_t>(k0 + kCb, n), rend = std::min<int64_t>(k1 + bw, n);
+    k_band_panel<<<(unsigned)std::max<int64_t>(1, (rend - k1 + 255) / 256), 256, 0, s>>>(
+      B, k0, bad.p);
+    if (rend > k1) {
+      const int64_t T = (rend - k1 + 31) / 32;
+      k_band_trail<<<(unsigned)(T * (T + 1) / 2), 256, 0, s>>>(B, k0, bad.p);
+    }
+  }
+  LGX_LAUNCH_CHECK();
+  int h_bad = 0;
+  LGX_CUDA(cudaMemcpyAsync(&h_bad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  LGX_CUDA(cudaStreamSynchronize(s));
+  if (h_bad) return fail(LGX_ERR_NOT_SPD, "matrix has a non-positive pivot");
+  return LGX_OK;
+}
+}  // namespace lgx
 
 lgx_status lgx_direct_create(const lgx_matrix *a, int kind, lgx_stream stream,
                              lgx_direct **out) {
@@ -2806,11 +3061,18 @@ lgx_status lgx_direct_create(const lgx_matrix *a, int kind, lgx_stream stream,
     return fail(LGX_ERR_INVALID, "kind must be LGX_DIRECT_CHOLESKY or LGX_DIRECT_LU");
   if (a->kind != LGX_MATRIX_CSR)
     return fail(LGX_ERR_UNSUPPORTED, "the direct solver needs a CSR matrix");
-  if (a->csr.n > LGX_DIRECT_MAX_ROWS)
-    return fail(LGX_ERR_INVALID, "the dense direct solver takes at most " +
-                                     std::to_string(LGX_DIRECT_MAX_ROWS) + " rows");
   auto d = std::make_unique<lgx_direct>();
   d->n = a->csr.n;
+  if (a->csr.n > LGX_DIRECT_MAX_ROWS) {
+    // beyond the dense limit: the banded Cholesky (lineal's factor is the
+    // envelope of the natural order); the unpivoted LU stays dense
+    if (kind != LGX_DIRECT_CHOLESKY)
+      return fail(LGX_ERR_INVALID, "the dense LU solver takes at most " +
+                                       std::to_string(LGX_DIRECT_MAX_ROWS) + " rows");
+    LGX_CHECK(band_create(a->csr, (cudaStream_t)stream, *d));
+    *out = d.release();
+    return LGX_OK;
+  }
   LGX_CHECK(dense_inverse(a->csr, (cudaStream_t)stream, d->inv, kind == LGX_DIRECT_CHOLESKY));
   *out = d.release();
   return LGX_OK;
@@ -2823,6 +3085,16 @@ lgx_status lgx_direct_solve(const lgx_direct *d, const double *d_b, double *d_x,
   if (!d_b || !d_x) return fail(LGX_ERR_INVALID, "null vector");
   if (d_b == d_x) return fail(LGX_ERR_INVALID, "b and x must not be the same vector");
   const cudaStream_t s = (cudaStream_t)stream;
+  if (d->bw >= 0) {
+    const Band B{d->n, d->bw, d->ld, const_cast<double *>(d->band.p)};
+    double *y = const_cast<double *>(d->y.p);
+    k_band_fwd<<<1, 1024, 0, s>>>(B, d_b, y);
+    k_band_bwd<<<1, 1024, 0, s>>>(B, y, d_x);
+    LGX_LAUNCH_CHECK();
+    count_launch();
+    count_launch();
+    return LGX_OK;
+  }
   LGX_CUDA(launch_pdl(false, k_dense_apply<double>,
                       dim3((unsigned)std::min<int64_t>(grid_for(d->n * 32, 256), 4096)), dim3(256),
                       0, s, d->n, (const double *)d->inv.p, d_b, d_x));

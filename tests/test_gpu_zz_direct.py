@@ -1,7 +1,8 @@
-"""The standalone dense direct solver (lgx_direct_*: CholeskySolver and
-LuSolver, direct/cholesky/solver.hpp:22-67, direct/lu/solver.hpp:21-66)
-against the reference's Cholesky golden solve and the UFZ_CT_02 system, its
-refusals, and the C++ concept layer's CholeskySolver/LuSolver program."""
+"""The standalone direct solver (lgx_direct_*: CholeskySolver and LuSolver,
+direct/cholesky/solver.hpp:22-67, direct/lu/solver.hpp:21-66) against the
+reference's Cholesky golden solve and the UFZ_CT_02 system, the banded
+Cholesky beyond the dense limit, its refusals, and the C++ concept layer's
+CholeskySolver/LuSolver program."""
 
 import os
 import subprocess
@@ -70,7 +71,7 @@ def test_refusals(cuda):
         cuda.DirectSolver(zero_pivot, lu=True)
     big = cuda.gen_7pt((32, 32, 9), np.ones(32 * 32 * 9))
     with pytest.raises(cuda.LinealError, match="at most"):
-        cuda.DirectSolver(big)
+        cuda.DirectSolver(big, lu=True)
     d = cuda.DirectSolver(_dev(cuda, _tridiagonal(4, -1.0, 2.0, -1.0), True))
     with pytest.raises(ValueError):
         d.solve(np.ones(5))
@@ -83,3 +84,40 @@ def test_cpp_direct_solvers(cuda):
     out = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert out.returncode == 0, out.stdout + out.stderr
     assert "direct_demo ok" in out.stdout
+
+
+@pytest.mark.parametrize("dims,npts", [((30, 30, 12), 7), ((24, 24, 16), 27), ((96, 10, 10), 7)])
+def test_banded_cholesky_beyond_dense_limit(cuda, dims, npts):
+    """More rows than the dense limit: the Cholesky factor in the band of the
+    lower envelope (natural order; bandwidth n1 n2 for 7 points, n1 n2 +
+    n2 + 1 for 27), then a forward and a backward substitution.  Solutions
+    of A x = A x_true agree with x_true to the conditioning's reach and the
+    FP64 residual is small; the factor is reused across solves."""
+    n = int(np.prod(dims))
+    assert n > cuda.DIRECT_MAX_ROWS
+    k = np.exp(np.random.default_rng(8).standard_normal(n))
+    ref = (lo.gen_27pt if npts == 27 else lo.gen_7pt)(dims, k)
+    m = (cuda.gen_27pt if npts == 27 else cuda.gen_7pt)(dims, k)
+    d = cuda.DirectSolver(m)
+    rng = np.random.default_rng(9)
+    for _ in range(2):
+        xt = rng.uniform(-1, 1, n)
+        b = lo.spmv(ref, xt)
+        x = d.solve(b).cpu().numpy()
+        assert np.linalg.norm(b - lo.spmv(ref, x)) <= 1e-12 * np.linalg.norm(b)
+        assert np.linalg.norm(x - xt) <= 1e-9 * np.linalg.norm(xt)
+
+
+def test_banded_cholesky_refuses_indefinite(cuda):
+    dims = (30, 30, 12)
+    n = int(np.prod(dims))
+    ref = lo.gen_7pt(dims, np.ones(n))
+    val = ref.val.copy()
+    # one negative diagonal entry deep inside the matrix
+    row = n // 2
+    for e in range(ref.rowptr[row], ref.rowptr[row + 1]):
+        if ref.col[e] == row:
+            val[e] = -1.0
+    m = cuda.CsrMatrix.from_host(ref.rowptr, ref.col, val, symmetric=True)
+    with pytest.raises(cuda.LinealError, match="non-positive pivot"):
+        cuda.DirectSolver(m)
