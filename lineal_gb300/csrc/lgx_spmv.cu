@@ -358,7 +358,7 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
   for (int e = 0; e < 6; ++e) {
     if (e == 3 && ultra) accum = fma(-diag, xi, accum);
-    if (has[e] && cv[e] != 0.0) accum = fma(cv[e], nb ? nb[cj[e]] : 0.0, accum);
+    if (has[e] && nonzero_bits(cv[e])) accum = fma(cv[e], nb ? nb[cj[e]] : 0.0, accum);
   }
   if (ultra) {
     x_out[i] = xi + relax * accum / fabs(diag);
