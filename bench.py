@@ -1062,7 +1062,8 @@ def run_batch(args):
 
 def run_profile(args):
     """Profiler target: one untimed AMG-PCG solve of the --grid^3 27-point
-    workload (FP64, or the float cycle with --mixed -- the float-vector CG with
+    workload (or the precision form's 7-point workload with
+    --profile-precision) (FP64, or the float cycle with --mixed -- the float-vector CG with
     reliable updates with --profile-refined -- with bfloat16 level values with
     --bf16; the bench's hierarchy options; row engine autotuned unless
     --no-autotune), then one more inside the NVTX range "solve" (ncu --nvtx
@@ -1072,9 +1073,16 @@ def run_profile(args):
     import lineal_gb300 as g
 
     g.build.build()
-    dims, k, b_host = make_problem(args.grid)
-    a = g.gen_27pt(dims, k)
-    col = g.Colouring.from_array(a, parity_colours(dims), 8)
+    if args.profile_precision:
+        # the precision form's workload: 7-point lognormal(sigma=3), red-black
+        dims, k, b_host = make_problem(args.grid, seed_k=2, seed_b=0, sigma=3.0)
+        a = g.gen_7pt(dims, k)
+        col = g.Colouring.from_array(a, red_black_colours(dims), 2)
+    else:
+        dims, k, b_host = make_problem(args.grid)
+        a = g.gen_27pt(dims, k)
+        col = g.Colouring.from_array(a, parity_colours(dims), 8)
+    rtol = 1e-10 if args.profile_precision else 1e-8
     mixed = args.mixed or args.bf16
     h = g.HierarchyWright(min_coarsen_size=2000, cycle_f32=mixed, cycle_bf16=args.bf16,
                           partition_size=args.partition_size,
@@ -1086,16 +1094,22 @@ def run_profile(args):
         h.autotune(reps=3)
     b = torch.as_tensor(b_host, device="cuda")
     # --mixed --profile-refined: the float-vector CG with reliable updates
-    kw = (dict(refine=args.refine, inner_rtol=args.inner_rtol, flexible=args.refine_flexible)
-          if mixed and args.profile_refined else {})
-    res = g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=1e-8, maxit=500, **kw)
+    # (with --profile-precision, as the precision form runs them: flexible CG
+    # over the float cycle, the float-vector CG with its inner reduction)
+    if args.profile_precision:
+        kw = (dict(refine=args.refine, inner_rtol=args.precision_inner_rtol, flexible=True)
+              if mixed and args.profile_refined else dict(flexible=mixed))
+    else:
+        kw = (dict(refine=args.refine, inner_rtol=args.inner_rtol,
+                   flexible=args.refine_flexible) if mixed and args.profile_refined else {})
+    res = g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=rtol, maxit=1000, **kw)
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_push("solve")
-    res = g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=1e-8, maxit=500, **kw)
+    res = g.pcg(a, b, precon=g.PRECON_AMG, amg=h, rtol=rtol, maxit=1000, **kw)
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
-    form = ("bf16" if args.bf16 else "mixed refined" if kw else "mixed" if args.mixed
-            else "fp64")
+    form = ("bf16" if args.bf16 else "mixed refined" if mixed and args.profile_refined
+            else "mixed" if args.mixed else "fp64")
     log(f"[profile] {form} solve: {res.iterations} it")
 
 
@@ -1245,6 +1259,9 @@ def main():
                     help="--mode profile --mixed: the float-vector CG (--refine)")
     ap.add_argument("--bf16", action="store_true",
                     help="--mode profile: the float cycle with bfloat16 level values")
+    ap.add_argument("--profile-precision", action="store_true",
+                    help="--mode profile: the precision form's 7-point sigma=3 workload "
+                         "solved to 1e-10")
     ap.add_argument("--batch-systems", type=int, default=1024)
     ap.add_argument("--batch-cpu-sample", type=int, default=16)
     ap.add_argument("--fd-directions", type=int, default=64)
