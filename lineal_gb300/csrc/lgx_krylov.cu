@@ -692,17 +692,16 @@ __global__ void __launch_bounds__(kKT)
   }
 }
 
-// d += alpha p ; r -= alpha q ; res2 = ||r||^2 (float vectors, FP64 alpha
-// rounded once to float, compensated sum)
+// r -= alpha q ; res2 = ||r||^2 (float vectors, FP64 alpha rounded once to
+// float, compensated sum).  The iterate's d += alpha p waits for the
+// direction kernel (k_fxpby_d), which reads p anyway.
 __global__ void __launch_bounds__(kKT)
-  k_fcg_update(int64_t n, KScalars *ks, const float *__restrict__ p, const float *__restrict__ q,
-               float *__restrict__ d, float *__restrict__ r, double *partials,
-               unsigned *counter) {
+  k_fcg_update(int64_t n, KScalars *ks, const float *__restrict__ q, float *__restrict__ r,
+               double *partials, unsigned *counter) {
   const float alpha = (float)ks->alpha;
   Dot2f acc;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    d[i] = fmaf(p[i], alpha, d[i]);
     const float rv = fmaf(-alpha, q[i], r[i]);
     r[i] = rv;
     acc.add(rv, rv);
@@ -715,13 +714,26 @@ __global__ void __launch_bounds__(kKT)
   }
 }
 
-// p = z + beta p (float)
-__global__ void k_fxpby(int64_t n, const KScalars *ks, const float *__restrict__ z,
-                        float *__restrict__ p) {
-  const float beta = (float)ks->beta;
+// d += alpha p (the deferred iterate update, before an FP64 residual)
+__global__ void k_faxpy_alpha(int64_t n, const KScalars *ks, const float *__restrict__ p,
+                              float *__restrict__ d) {
+  const float alpha = (float)ks->alpha;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = fmaf(p[i], beta, z[i]);
+    d[i] = fmaf(p[i], alpha, d[i]);
+}
+
+// d += alpha p (this iteration's alpha), then p = z + beta p (float)
+__global__ void k_fxpby_d(int64_t n, const KScalars *ks, const float *__restrict__ z,
+                          float *__restrict__ p, float *__restrict__ d) {
+  const float alpha = (float)ks->alpha;
+  const float beta = (float)ks->beta;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float pi = p[i];
+    d[i] = fmaf(pi, alpha, d[i]);
+    p[i] = fmaf(pi, beta, z[i]);
+  }
 }
 
 // flexible CG on float vectors: t1 = r.z, t2 = r.z_old (compensated sums), then
@@ -752,18 +764,6 @@ __global__ void __launch_bounds__(kKT)
   }
 }
 
-// p = z + beta p and z_old = z (float, flexible CG)
-__global__ void k_fxpby_save(int64_t n, const KScalars *ks, const float *__restrict__ z,
-                             float *__restrict__ p, float *__restrict__ zold) {
-  const float beta = (float)ks->beta;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const float zi = z[i];
-    p[i] = fmaf(p[i], beta, zi);
-    zold[i] = zi;
-  }
-}
-
 // rf = float(r * inv_scale), d = 0
 __global__ void k_refine_start(int64_t n, const double *__restrict__ r, double inv_scale,
                                float *__restrict__ rf, float *__restrict__ d) {
@@ -786,14 +786,19 @@ struct Refiner {
   Solver S;
   std::unique_ptr<lgx_colouring> own_col;
   DBuf<double> b, x, r;
-  DBuf<float> rf, df, pf, qf, zf, zold;
+  DBuf<float> rf, df, pf, qf, zf, zf2;
   const float *v32 = nullptr;
   bool flexible = false;  // flexible beta (Notay 2000) for the float V-cycle
+  // flexible CG needs the previous preconditioned residual: the V-cycle
+  // writes z into zbuf(par) while zbuf(par ^ 1) still holds the previous z
+  // (the buffers alternate instead of z being copied every iteration)
+  int par = 0;
+  float *zbuf(int k) { return k ? zf2.p : zf.p; }
   cudaStream_t user_stream = nullptr, capture_stream = nullptr;
   // graphs of the two halves of an inner iteration: [0] product and update,
-  // [1] preconditioner and new direction
-  cudaGraphExec_t graph[2] = {nullptr, nullptr};
-  uint64_t graph_kernels[2] = {0, 0};
+  // [1 + par] preconditioner and new direction
+  cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
+  uint64_t graph_kernels[3] = {0, 0, 0};
   ~Refiner() {
     for (auto &g : graph)
       if (g) cudaGraphExecDestroy(g);
@@ -801,7 +806,8 @@ struct Refiner {
   }
 
   // first half of a CG iteration on the float vectors: q = A p,
-  // alpha = rho / p.q, d += alpha p, r -= alpha q, ||r||^2
+  // alpha = rho / p.q, r -= alpha q, ||r||^2 (d += alpha p follows in the
+  // second half, or in fold_alpha before an FP64 residual)
   lgx_status half_update() {
     const int64_t n = S.n;
     cudaStream_t s = S.s;
@@ -810,35 +816,53 @@ struct Refiner {
     LGX_CHECK((csr_spmv<float, float>(*S.pcsr, v32, pf.p, qf.p, s)));
     k_fdot_post<<<rg, kKT, 0, s>>>(n, pf.p, qf.p, POST_ALPHA, ks, S.partials.p, S.counters.p);
     LGX_LAUNCH_CHECK();
-    k_fcg_update<<<rg, kKT, 0, s>>>(n, ks, pf.p, qf.p, df.p, rf.p, S.partials.p, S.counters.p);
+    k_fcg_update<<<rg, kKT, 0, s>>>(n, ks, qf.p, rf.p, S.partials.p, S.counters.p);
     LGX_LAUNCH_CHECK();
     return LGX_OK;
   }
-  // second half: z = M r, rho = r.z, beta, p = z + beta p
+  // second half: z = M r, rho = r.z, beta, d += alpha p, p = z + beta p
   lgx_status half_direction() {
     const int64_t n = S.n;
     cudaStream_t s = S.s;
     KScalars *ks = S.ks.p;
     const unsigned rg = (unsigned)reduce_blocks(n);
-    LGX_CHECK(amg_apply_permuted_f32(*S.amg, rf.p, zf.p, s));
+    float *z = flexible ? zbuf(par) : zf.p;
+    LGX_CHECK(amg_apply_permuted_f32(*S.amg, rf.p, z, s));
     if (flexible) {
-      k_fdot2_fcg<<<rg, kKT, 0, s>>>(n, rf.p, zf.p, zold.p, ks, S.partials.p, S.partials2.p,
-                                     S.counters.p, S.counters.p + 1);
-      LGX_LAUNCH_CHECK();
-      k_fxpby_save<<<S.vgrid(), 256, 0, s>>>(n, ks, zf.p, pf.p, zold.p);
-      LGX_LAUNCH_CHECK();
-      return LGX_OK;
+      k_fdot2_fcg<<<rg, kKT, 0, s>>>(n, rf.p, z, zbuf(par ^ 1), ks, S.partials.p,
+                                     S.partials2.p, S.counters.p, S.counters.p + 1);
+    } else {
+      k_fdot_post<<<rg, kKT, 0, s>>>(n, rf.p, z, POST_RHO_BETA, ks, S.partials.p,
+                                     S.counters.p);
     }
-    k_fdot_post<<<rg, kKT, 0, s>>>(n, rf.p, zf.p, POST_RHO_BETA, ks, S.partials.p,
-                                   S.counters.p);
     LGX_LAUNCH_CHECK();
-    k_fxpby<<<S.vgrid(), 256, 0, s>>>(n, ks, zf.p, pf.p);
+    k_fxpby_d<<<S.vgrid(), 256, 0, s>>>(n, ks, z, pf.p, df.p);
     LGX_LAUNCH_CHECK();
     return LGX_OK;
   }
   lgx_status half(int which) { return which == 0 ? half_update() : half_direction(); }
 
-  lgx_status capture(int which) {
+  // the float vectors of a solve of n rows
+  lgx_status alloc(int64_t n) {
+    LGX_CHECK(rf.alloc(n));
+    LGX_CHECK(df.alloc(n));
+    LGX_CHECK(pf.alloc(n));
+    LGX_CHECK(qf.alloc(n));
+    LGX_CHECK(zf.alloc(n));
+    if (flexible) LGX_CHECK(zf2.alloc(n));
+    return LGX_OK;
+  }
+
+  // d += alpha p now (the last update's alpha), and alpha = 0 so that the
+  // direction kernel that follows adds nothing more
+  lgx_status fold_alpha() {
+    k_faxpy_alpha<<<S.vgrid(), 256, 0, S.s>>>(S.n, S.ks.p, pf.p, df.p);
+    LGX_LAUNCH_CHECK();
+    LGX_CUDA(cudaMemsetAsync(&S.ks.p->alpha, 0, sizeof(double), S.s));
+    return LGX_OK;
+  }
+
+  lgx_status capture(int slot, int which) {
     if (!capture_stream)
       LGX_CUDA(cudaStreamCreateWithFlags(&capture_stream, cudaStreamNonBlocking));
     S.s = capture_stream;
@@ -846,8 +870,8 @@ struct Refiner {
     const uint64_t before = launch_count();
     cudaError_t e = cudaStreamBeginCapture(capture_stream, cudaStreamCaptureModeThreadLocal);
     lgx_status st = e == cudaSuccess ? half(which) : cuda_fail(e, "cudaStreamBeginCapture");
-    graph_kernels[which] = launch_count() - before;
-    count_launches(0 - graph_kernels[which]);
+    graph_kernels[slot] = launch_count() - before;
+    count_launches(0 - graph_kernels[slot]);
     cudaError_t e2 = cudaStreamEndCapture(capture_stream, &g);
     S.s = user_stream;
     if (st != LGX_OK) {
@@ -855,7 +879,7 @@ struct Refiner {
       return st;
     }
     if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
-    e = cudaGraphInstantiate(&graph[which], g, 0);
+    e = cudaGraphInstantiate(&graph[slot], g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
     return LGX_OK;
@@ -864,14 +888,17 @@ struct Refiner {
   // one half, eagerly the first time (it also sets per-kernel attributes),
   // then replayed from its graph
   lgx_status run_half(int which, bool use_graphs, bool &first) {
+    const int slot = which == 0 ? 0 : 1 + (flexible ? par : 0);
     if (use_graphs && !first) {
-      if (!graph[which]) LGX_CHECK(capture(which));
-      LGX_CUDA(cudaGraphLaunch(graph[which], user_stream));
-      count_launches(graph_kernels[which]);
-      return LGX_OK;
+      if (!graph[slot]) LGX_CHECK(capture(slot, which));
+      LGX_CUDA(cudaGraphLaunch(graph[slot], user_stream));
+      count_launches(graph_kernels[slot]);
+    } else {
+      if (which == 1) first = false;
+      LGX_CHECK(half(which));
     }
-    if (which == 1) first = false;
-    return half(which);
+    if (which == 1 && flexible) par ^= 1;
+    return LGX_OK;
   }
 };
 
@@ -894,11 +921,7 @@ static lgx_status run_refined(const lgx_matrix *a, const double *d_b, double *d_
   LGX_CHECK(R.b.alloc(n));
   LGX_CHECK(R.x.alloc(n));
   LGX_CHECK(R.r.alloc(n));
-  LGX_CHECK(R.rf.alloc(n));
-  LGX_CHECK(R.df.alloc(n));
-  LGX_CHECK(R.pf.alloc(n));
-  LGX_CHECK(R.qf.alloc(n));
-  LGX_CHECK(R.zf.alloc(n));
+  LGX_CHECK(R.alloc(n));
   LGX_CHECK(gather<double, double>(n, S.perm, d_b, R.b.p, s));
   LGX_CHECK(gather<double, double>(n, S.perm, d_x, R.x.p, s));
   KScalars *ks = S.ks.p;
@@ -923,6 +946,7 @@ static lgx_status run_refined(const lgx_matrix *a, const double *d_b, double *d_
     k_fdot_post<<<rg, kKT, 0, s>>>(n, R.rf.p, R.zf.p, POST_RHO, ks, S.partials.p, S.counters.p);
     LGX_LAUNCH_CHECK();
     LGX_CUDA(cudaMemcpyAsync(R.pf.p, R.zf.p, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+    R.par = R.flexible ? 1 : 0;  // this solve's first z is the previous z of its first step
     LGX_CHECK(S.read(h));
     LGX_CHECK(check_flags(h, it));
     double inner = 1.0;
@@ -993,13 +1017,8 @@ static lgx_status run_reliable(const lgx_matrix *a, const double *d_b, double *d
   LGX_CHECK(R.b.alloc(n));
   LGX_CHECK(R.x.alloc(n));
   LGX_CHECK(R.r.alloc(n));
-  LGX_CHECK(R.rf.alloc(n));
-  LGX_CHECK(R.df.alloc(n));
-  LGX_CHECK(R.pf.alloc(n));
-  LGX_CHECK(R.qf.alloc(n));
-  LGX_CHECK(R.zf.alloc(n));
   R.flexible = p->flexible != 0;
-  if (R.flexible) LGX_CHECK(R.zold.alloc(n));
+  LGX_CHECK(R.alloc(n));
   LGX_CHECK(gather<double, double>(n, S.perm, d_b, R.b.p, s));
   LGX_CHECK(gather<double, double>(n, S.perm, d_x, R.x.p, s));
   KScalars *ks = S.ks.p;
@@ -1021,9 +1040,7 @@ static lgx_status run_reliable(const lgx_matrix *a, const double *d_b, double *d
     k_fdot_post<<<rg, kKT, 0, s>>>(n, R.rf.p, R.zf.p, POST_RHO, ks, S.partials.p, S.counters.p);
     LGX_LAUNCH_CHECK();
     LGX_CUDA(cudaMemcpyAsync(R.pf.p, R.zf.p, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
-    if (R.flexible)
-      LGX_CUDA(cudaMemcpyAsync(R.zold.p, R.zf.p, sizeof(float) * n, cudaMemcpyDeviceToDevice,
-                               s));
+    R.par = R.flexible ? 1 : 0;  // z is the previous z of the first step
     LGX_CHECK(S.read(h));
     LGX_CHECK(check_flags(h, 0));
   }
@@ -1041,6 +1058,7 @@ static lgx_status run_reliable(const lgx_matrix *a, const double *d_b, double *d
     if (history) history[it] = est;
     if (est <= p->inner_rtol * last || est <= p->rtol * r0 || it == p->maxit) {
       // reliable update: fold d into x and replace r by the FP64 residual
+      LGX_CHECK(R.fold_alpha());
       k_refine_add<<<S.vgrid(), 256, 0, s>>>(n, R.df.p, 1.0, R.x.p);
       LGX_LAUNCH_CHECK();
       LGX_CHECK(S.residual(R.b.p, R.x.p, R.r.p, &ks->res2));
