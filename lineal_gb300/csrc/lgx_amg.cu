@@ -2662,7 +2662,9 @@ static lgx_status amg_build(const lgx_matrix *m, const lgx_amg_params &p,
 // float values (the stored floats or the float copy of a double level).
 template <typename XT>
 static lgx_status level_sor(lgx_amg_level &lv, const lgx_amg &h, int forward, const XT *b, XT *x,
-                            cudaStream_t s, int from_zero = 0) {
+                            cudaStream_t s, int from_zero = 0, XT *r_last = nullptr,
+                            int64_t *res_from = nullptr) {
+  if (res_from) *res_from = lv.a->n;
   const lgx_colouring &c = *lv.col;
   const double relax = h.p.smoother_relax;
   const int ultra = h.p.smoother_ultra;
@@ -2676,17 +2678,25 @@ static lgx_status level_sor(lgx_amg_level &lv, const lgx_amg &h, int forward, co
   if constexpr (sizeof(XT) == 8) {
     if (c.pcsr.storage == LGX_F64)
       return mc_sor_sweep<double, double>(c, c.pcsr.v64.p, relax, forward, ultra, b, x, s,
-                                          from_zero);
+                                          from_zero, nullptr, r_last, res_from);
     return mc_sor_sweep<float, double>(c, c.pcsr.v32.p, relax, forward, ultra, b, x, s,
-                                       from_zero);
+                                       from_zero, nullptr, r_last, res_from);
   } else {
     if (h.p.cycle_bf16)
       return mc_sor_sweep<bf16, float>(c, c.pv16.p, relax, forward, ultra, b, x, s, from_zero,
                                        c.pscale.p);
     const float *v = c.pcsr.storage == LGX_F32 ? c.pcsr.v32.p : c.pv32.p;
-    return mc_sor_sweep<float, float>(c, v, relax, forward, ultra, b, x, s, from_zero);
+    return mc_sor_sweep<float, float>(c, v, relax, forward, ultra, b, x, s, from_zero, nullptr,
+                                      r_last, res_from);
   }
 }
+
+// The residual of rows [0, rend) of a level whose sweep left the residuals
+// of its last colour (rows rend on) already; the whole residual when rend
+// is the level's size.
+template <typename XT>
+static lgx_status level_residual_part(lgx_amg_level &lv, const lgx_amg &h, const XT *b,
+                                      const XT *x, XT *r, int64_t rend, cudaStream_t s);
 
 template <typename XT>
 static lgx_status level_residual(lgx_amg_level &lv, const lgx_amg &h, const XT *b, const XT *x,
@@ -2714,12 +2724,44 @@ static lgx_status level_residual(lgx_amg_level &lv, const lgx_amg &h, const XT *
 }
 
 template <typename XT>
+static lgx_status level_residual_part(lgx_amg_level &lv, const lgx_amg &h, const XT *b,
+                                      const XT *x, XT *r, int64_t rend, cudaStream_t s) {
+  if (rend >= lv.a->n) return level_residual<XT>(lv, h, b, x, r, s);
+  const lgx_colouring &c = *lv.col;
+  bool done = false;
+  if constexpr (sizeof(XT) == 8) {
+    if (c.pcsr.storage == LGX_F64)
+      LGX_CHECK((grid_residual_rows<double, double>(c.pcsr, c.pcsr.v64.p, b, x, r, 0, rend, s,
+                                                    &done)));
+    else
+      LGX_CHECK((grid_residual_rows<float, double>(c.pcsr, c.pcsr.v32.p, b, x, r, 0, rend, s,
+                                                   &done)));
+  } else {
+    const float *v = c.pcsr.storage == LGX_F32 ? c.pcsr.v32.p : c.pv32.p;
+    LGX_CHECK((grid_residual_rows<float, float>(c.pcsr, v, b, x, r, 0, rend, s, &done)));
+  }
+  // the sweep wrote residuals only through the grid rows this residual uses
+  if (!done) return fail(LGX_ERR_INVALID, "partial residual without grid rows");
+  return LGX_OK;
+}
+
+template <typename XT>
 static XT *level_vec(lgx_amg_level &lv, int which) {
   if constexpr (sizeof(XT) == 8) {
     return which == 0 ? (XT *)lv.b64.p : which == 1 ? (XT *)lv.x64.p : (XT *)lv.r64.p;
   } else {
     return which == 0 ? (XT *)lv.b32.p : which == 1 ? (XT *)lv.x32.p : (XT *)lv.r32.p;
   }
+}
+
+// the residuals of a forward sweep's last colour from its own kernel
+// (LGX_FUSED_RESIDUAL=0: a separate residual pass over every row)
+static bool fused_residual_enabled() {
+  static const bool on = [] {
+    const char *e = std::getenv("LGX_FUSED_RESIDUAL");
+    return !(e && e[0] == '0');
+  }();
+  return on;
 }
 
 // V-cycle in permuted space (multigrid/solver.hpp:56-176, REGULAR cycle with
@@ -2735,8 +2777,14 @@ static lgx_status vcycle_impl(lgx_amg &h, const XT *b0, XT *x0, cudaStream_t s) 
     XT *x = l == 0 ? x0 : level_vec<XT>(lv, 1);
     const int64_t n = lv.a->n;
     if (n == 0) continue;
-    LGX_CHECK(level_sor<XT>(lv, h, 1, b, x, s, 1));  // forward sweep from x = 0
-    LGX_CHECK(level_residual<XT>(lv, h, b, x, level_vec<XT>(lv, 2), s));
+    // forward sweep from x = 0; its last colour, on float 7-point grid rows,
+    // also leaves its rows' residuals, so the residual pass covers the rows
+    // before it
+    XT *r = level_vec<XT>(lv, 2);
+    int64_t res_from = n;
+    LGX_CHECK(level_sor<XT>(lv, h, 1, b, x, s, 1, fused_residual_enabled() ? r : nullptr,
+                            &res_from));
+    LGX_CHECK(level_residual_part<XT>(lv, h, b, x, r, res_from, s));
     lgx_amg_level &cv = *h.lv[l + 1];
     const int64_t nc = cv.a->n;
     if (nc) {

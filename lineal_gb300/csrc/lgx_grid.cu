@@ -201,7 +201,10 @@ __global__ void k_g27_fill(G27 g, const int64_t *__restrict__ rowptr,
 
 // ---- row operations ---------------------------------------------------------
 // MODE 0: y = A x; 1: r = b - A x (bf16: A x scaled by the row factor);
-// 2: SOR row in place (the arithmetic of SorOp, lgx_smoother.cu)
+// 2: SOR row in place (the arithmetic of SorOp, lgx_smoother.cu); 4: the
+// SOR row of MODE 2, then the row's residual b - A x with its new x written
+// to y (the last colour of a forward sweep: every neighbour already holds
+// its final value, and the residual is MODE 1's sum in the same order)
 struct G27Sor {
   double relax, m1;
   int ultra, relax_one, from_zero;
@@ -239,14 +242,20 @@ __device__ __forceinline__ bf16 g27_ld(const bf16 *p) {
 // than deeper rounds in fewer warps.
 constexpr int kG27Batch = 3;
 
+template <int MODE>
+constexpr bool g_sor_mode() {
+  return MODE == 2 || MODE == 4;
+}
+
 // One row's state through its entries, in the arithmetic of SpmvOp
-// (MODE 0), ResidualOp (MODE 1) and SorOp (MODE 2, lgx_smoother.cu).
+// (MODE 0), ResidualOp (MODE 1) and SorOp (MODE 2 and 4, lgx_smoother.cu).
 template <typename VT, typename XT, int MODE, int PTS>
 struct G27Row {
   static constexpr int kDiag = g_diag<PTS>();
   XT acc = XT(0), diag = XT(0), xi = XT(0);  // sum | SOR accum (bf16: t), diagonal (bf16: v_ii)
+  XT xnew = XT(0);                           // SOR: the row's new x
   __device__ __forceinline__ void init(int64_t r, const XT *b, const XT *x, const G27Sor &so) {
-    if constexpr (MODE == 2) {
+    if constexpr (g_sor_mode<MODE>()) {
       xi = so.from_zero ? XT(0) : x[r];
       if constexpr (!kIsBf16<VT>) acc = b[r];
     }
@@ -254,7 +263,7 @@ struct G27Row {
   // entry e with value a and neighbour value xv (in: inside the grid)
   __device__ __forceinline__ void step(int e, bool in, XT a, XT xv, const G27Sor &so) {
     if (!in) return;
-    if constexpr (MODE != 2) {
+    if constexpr (!g_sor_mode<MODE>()) {
       acc = fma(a, xv, acc);
     } else if constexpr (kIsBf16<VT>) {
       if (e == kDiag) diag = a;
@@ -284,13 +293,15 @@ struct G27Row {
         XT accum = fma(-si, acc, b[r]);
         if (so.ultra) {
           accum = fma(-dg, xi, accum);
-          x[r] = xi + relax * accum / fabs(dg);
+          xnew = xi + relax * accum / fabs(dg);
         } else {
-          x[r] = fma(relax, accum / dg, m1 * xi);
+          xnew = fma(relax, accum / dg, m1 * xi);
         }
+        x[r] = xnew;
       } else {
         if (so.ultra) {
-          x[r] = xi + relax * acc / fabs(diag);
+          xnew = xi + relax * acc / fabs(diag);
+          x[r] = xnew;
           return;
         }
         XT quot;
@@ -299,13 +310,15 @@ struct G27Row {
           quot = (nonzero_bits(yr) && exponent_within_400(acc)) ? div_by_recip(acc, diag, yr)
                                                                 : acc / diag;
           if (so.relax_one && nonzero_bits(quot) && exponent_field(xi) != 0x7ff) {
-            x[r] = quot;
+            xnew = quot;  // fma(1, q, 0 * x_i) == q for nonzero q and finite x_i
+            x[r] = xnew;
             return;
           }
         } else {
           quot = acc / diag;
         }
-        x[r] = fma(relax, quot, m1 * xi);
+        xnew = fma(relax, quot, m1 * xi);
+        x[r] = xnew;
       }
     }
   }
@@ -315,9 +328,9 @@ struct G27Row {
 // forward sweep from zero; the diagonal's x is not read here)
 template <typename XT, int MODE, int PTS>
 __device__ __forceinline__ XT g27_x(const XT *x, int64_t c, int e, const G27Sor &so) {
-  if (MODE == 2 && e == g_diag<PTS>()) return XT(0);
+  if (g_sor_mode<MODE>() && e == g_diag<PTS>()) return XT(0);
   const XT xl = g27_ld(x + c);
-  return (MODE == 2 && so.from_zero && c >= so.visit_end) ? XT(0) : xl;
+  return (g_sor_mode<MODE>() && so.from_zero && c >= so.visit_end) ? XT(0) : xl;
 }
 
 // one row per thread
@@ -354,6 +367,31 @@ __global__ void __launch_bounds__(256)
     }
   }
   row.finish(r, b, x, y, scale, so);
+  if constexpr (MODE == 4) {
+    // the residual with the new x: the values and neighbours again (L1),
+    // the row's own x from the register
+    XT sum = XT(0);
+#pragma unroll
+    for (int e0 = 0; e0 < PTS; e0 += B) {
+      XT xv[B], av[B];
+#pragma unroll
+      for (int u = 0; u < B; ++u) {
+        const int e = e0 + u;
+        if (e >= PTS) break;
+        av[u] = cvt<XT>(g27_ld(v + (int64_t)e * g.stride + r));
+        xv[u] = (e == g_diag<PTS>() || !g_in<PTS>(sides, e))
+                  ? row.xnew
+                  : g27_ld(x + g_nb<PTS>(g, cell, r, e));
+      }
+#pragma unroll
+      for (int u = 0; u < B; ++u) {
+        const int e = e0 + u;
+        if (e >= PTS) break;
+        if (g_in<PTS>(sides, e)) sum = fma(av[u], xv[u], sum);
+      }
+    }
+    y[r] = b[r] - sum;
+  }
 }
 
 // four consecutive rows of a colour per thread (float vectors): the value
@@ -496,7 +534,7 @@ __global__ void __launch_bounds__(g_rows_per_cta<T>(), g_ctas_per_sm<T, PTS>())
     if (sides == 0x3Fu) {
 #pragma unroll
       for (int e = 0; e < PTS; ++e) {
-        if (MODE == 2 && e == kDiag) {
+        if (g_sor_mode<MODE>() && e == kDiag) {
           xv[e] = T(0);
           continue;
         }
@@ -507,7 +545,7 @@ __global__ void __launch_bounds__(g_rows_per_cta<T>(), g_ctas_per_sm<T, PTS>())
     } else {
 #pragma unroll
       for (int e = 0; e < PTS; ++e) {
-        if (MODE == 2 && e == kDiag) {
+        if (g_sor_mode<MODE>() && e == kDiag) {
           xv[e] = T(0);
           continue;
         }
@@ -536,6 +574,15 @@ __global__ void __launch_bounds__(g_rows_per_cta<T>(), g_ctas_per_sm<T, PTS>())
     for (int e = 0; e < PTS; ++e) row.step(e, g_in<PTS>(sides, e), svt[e * RT], xv[e], so);
   }
   row.finish(r, b, x, y, nullptr, so);
+  if constexpr (MODE == 4) {
+    // the residual with the new x (staged values, gathered neighbours)
+    T sum = T(0);
+#pragma unroll
+    for (int e = 0; e < PTS; ++e)
+      if (sides == 0x3Fu || g_in<PTS>(sides, e))
+        sum = fma(svt[e * RT], e == kDiag ? row.xnew : xv[e], sum);
+    y[r] = b[r] - sum;
+  }
 }
 
 // the tensor-staged kernels serve float rows with 16-byte-aligned row starts
@@ -603,8 +650,9 @@ static bool g27_tma_launch(const Grid27 &gr, const T *v, int64_t rb, int64_t re,
   if (!map) return false;
   constexpr int RT = g_rows_per_cta<T>();
   const int64_t ctas = (re - rb + RT - 1) / RT;
-  auto kern =
-    MODE == 2 && so.from_zero ? k_g27_vtma<T, MODE, true, PTS> : k_g27_vtma<T, MODE, false, PTS>;
+  auto kern = k_g27_vtma<T, MODE, false, PTS>;
+  if constexpr (g_sor_mode<MODE>())
+    if (so.from_zero) kern = k_g27_vtma<T, MODE, true, PTS>;
   const cudaError_t e = launch_pdl(pdl, kern, dim3((unsigned)ctas), dim3(RT), 0, s, *map,
                                    view(gr), rb, re, b, x, y, so, device_error_flag());
   *st = e == cudaSuccess ? LGX_OK : cuda_fail(e, "k_g27_vtma");
@@ -667,9 +715,15 @@ static lgx_status launch_g27(const Grid27 &gr, const VT *v, int64_t rb, int64_t 
                              XT *x, XT *y, const float *scale, const G27Sor &so,
                              cudaStream_t s) {
   if (re <= rb) return LGX_OK;
-  if (gr.points == 7)
+  if constexpr (MODE == 4) {
+    // the sweep with residuals serves the 7-point grid only (grid_sweep_residual)
+    if (gr.points != 7) return fail(LGX_ERR_UNSUPPORTED, "sweep with residual: 27-point grid");
     return launch_g27_pts<VT, XT, MODE, 7>(gr, v, rb, re, b, x, y, scale, so, s);
-  return launch_g27_pts<VT, XT, MODE, 27>(gr, v, rb, re, b, x, y, scale, so, s);
+  } else {
+    if (gr.points == 7)
+      return launch_g27_pts<VT, XT, MODE, 7>(gr, v, rb, re, b, x, y, scale, so, s);
+    return launch_g27_pts<VT, XT, MODE, 27>(gr, v, rb, re, b, x, y, scale, so, s);
+  }
 }
 
 template <typename VT, typename XT>
@@ -702,7 +756,7 @@ template <typename VT, typename XT>
 lgx_status grid_sor_rows(const Csr &a, const VT *val, int64_t rb, int64_t re, const XT *b, XT *x,
                          double relax, int ultra, const double *rdiag, int relax_one,
                          int from_zero, int64_t visit_end, const float *scale, cudaStream_t s,
-                         bool *done) {
+                         bool *done, XT *r_out) {
   *done = false;
   if (!a.grid) return LGX_OK;
   const VT *v = grid_values(*a.grid, val);
@@ -710,7 +764,38 @@ lgx_status grid_sor_rows(const Csr &a, const VT *val, int64_t rb, int64_t re, co
   G27Sor so{relax, 1.0 - relax, ultra, relax_one, from_zero, visit_end, rdiag};
   // the float SOR of SorOp forms XT(1) - XT(relax): the same in XT
   so.m1 = (double)((XT)1 - (XT)relax);
+  if constexpr (!kIsBf16<VT> && sizeof(XT) == 4) {
+    if (r_out) {
+      LGX_CHECK((launch_g27<VT, XT, 4>(*a.grid, v, rb, re, b, x, r_out, scale, so, s)));
+      *done = true;
+      return LGX_OK;
+    }
+  }
+  if (r_out) return fail(LGX_ERR_UNSUPPORTED, "sweep with residual: FP64 or bfloat16 rows");
   LGX_CHECK((launch_g27<VT, XT, 2>(*a.grid, v, rb, re, b, x, nullptr, scale, so, s)));
+  *done = true;
+  return LGX_OK;
+}
+
+// A red-black sweep's second colour leaves half the residual for free: its
+// rows hold every value the residual needs.  Float rows only: measured at
+// 256^3 (7-point, sigma = 3, to 1e-10) the float-vector CG went 318.7 ->
+// 308.6 ms, while the FP64 solve went 531.6 -> 562.7 ms (the FP64 row with
+// its residual holds 48 instead of 40 registers on an FP64-pipe-bound
+// launch).  On the 27-point grid the last of eight colours would save an
+// eighth of the residual pass at the price of a longer row, so it keeps the
+// pass.
+bool grid_sweep_residual(const Csr &a) { return a.grid && a.grid->points == 7; }
+
+template <typename VT, typename XT>
+lgx_status grid_residual_rows(const Csr &a, const VT *val, const XT *b, const XT *x, XT *r,
+                              int64_t rb, int64_t re, cudaStream_t s, bool *done) {
+  *done = false;
+  if (!a.grid) return LGX_OK;
+  const VT *v = grid_values(*a.grid, val);
+  if (!v) return LGX_OK;
+  LGX_CHECK((launch_g27<VT, XT, 1>(*a.grid, v, rb, re, b, const_cast<XT *>(x), r, nullptr,
+                                   G27Sor{}, s)));
   *done = true;
   return LGX_OK;
 }
@@ -736,19 +821,28 @@ template lgx_status grid_residual<bf16, float>(const Csr &, const bf16 *, const 
 template lgx_status grid_sor_rows<double, double>(const Csr &, const double *, int64_t, int64_t,
                                                   const double *, double *, double, int,
                                                   const double *, int, int, int64_t,
-                                                  const float *, cudaStream_t, bool *);
+                                                  const float *, cudaStream_t, bool *, double *);
 template lgx_status grid_sor_rows<float, double>(const Csr &, const float *, int64_t, int64_t,
                                                  const double *, double *, double, int,
                                                  const double *, int, int, int64_t,
-                                                 const float *, cudaStream_t, bool *);
+                                                 const float *, cudaStream_t, bool *, double *);
 template lgx_status grid_sor_rows<float, float>(const Csr &, const float *, int64_t, int64_t,
                                                 const float *, float *, double, int,
                                                 const double *, int, int, int64_t, const float *,
-                                                cudaStream_t, bool *);
+                                                cudaStream_t, bool *, float *);
 template lgx_status grid_sor_rows<bf16, float>(const Csr &, const bf16 *, int64_t, int64_t,
                                                const float *, float *, double, int,
                                                const double *, int, int, int64_t, const float *,
-                                               cudaStream_t, bool *);
+                                               cudaStream_t, bool *, float *);
+template lgx_status grid_residual_rows<double, double>(const Csr &, const double *,
+                                                       const double *, const double *, double *,
+                                                       int64_t, int64_t, cudaStream_t, bool *);
+template lgx_status grid_residual_rows<float, double>(const Csr &, const float *, const double *,
+                                                      const double *, double *, int64_t, int64_t,
+                                                      cudaStream_t, bool *);
+template lgx_status grid_residual_rows<float, float>(const Csr &, const float *, const float *,
+                                                     const float *, float *, int64_t, int64_t,
+                                                     cudaStream_t, bool *);
 
 // ---- attach -------------------------------------------------------------------
 template <typename VT>

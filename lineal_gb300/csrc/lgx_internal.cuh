@@ -244,11 +244,19 @@ lgx_status grid_spmv(const Csr &a, const VT *val, const XT *x, XT *y, cudaStream
 template <typename VT, typename XT>
 lgx_status grid_residual(const Csr &a, const VT *val, const XT *b, const XT *x, XT *r,
                          const float *scale, cudaStream_t s, bool *done);
+// r_out: the rows' residuals b - A x with their new x are written there as
+// well (the last colour of a forward sweep; float values and vectors only)
 template <typename VT, typename XT>
 lgx_status grid_sor_rows(const Csr &a, const VT *val, int64_t rb, int64_t re, const XT *b, XT *x,
                          double relax, int ultra, const double *rdiag, int relax_one,
                          int from_zero, int64_t visit_end, const float *scale, cudaStream_t s,
-                         bool *done);
+                         bool *done, XT *r_out = nullptr);
+// whether grid_sor_rows takes r_out on this matrix (7-point grid rows, float)
+bool grid_sweep_residual(const Csr &a);
+// the residual of rows [rb, re) only
+template <typename VT, typename XT>
+lgx_status grid_residual_rows(const Csr &a, const VT *val, const XT *b, const XT *x, XT *r,
+                              int64_t rb, int64_t re, cudaStream_t s, bool *done);
 
 lgx_status stencil_spmv(const StencilDesc &st, const double *x, double *y, cudaStream_t s);
 lgx_status stencil_residual(const StencilDesc &st, const double *b, const double *x, double *r,
@@ -275,11 +283,16 @@ lgx_status colouring_jp(const Csr &a, uint64_t seed, cudaStream_t s, DBuf<int32_
 // One multicolour sweep on the permuted matrix (vectors in permuted order,
 // in place).  VT value type, XT vector/arithmetic type.
 // from_zero: the sweep starts from x = 0 (x need not be cleared); scale: the
-// per-row factor of bfloat16 values.
+// per-row factor of bfloat16 values.  r_last / res_from (forward sweeps):
+// when the last colour runs on float 7-point grid rows, its rows' residuals
+// b - A x are written to r_last as well and *res_from is that colour's
+// first row (else c.n): the caller's residual then needs rows
+// [0, *res_from) only.
 template <typename VT, typename XT>
 lgx_status mc_sor_sweep(const lgx_colouring &c, const VT *val, double relax, int forward,
                         int ultra, const XT *b, XT *x, cudaStream_t s, int from_zero = 0,
-                        const float *scale = nullptr);
+                        const float *scale = nullptr, XT *r_last = nullptr,
+                        int64_t *res_from = nullptr);
 lgx_status colouring_make_bf16(lgx_colouring &c, cudaStream_t s);
 // gives c.pcsr a Grid27 when it is the parity-coloured 27-point (points 27)
 // or red-black 7-point (points 7) operator on `dims` (checked on the device;

@@ -522,7 +522,8 @@ __global__ void k_sor_first_colour(int64_t rb, int64_t re, const double *__restr
 template <typename VT, typename XT>
 lgx_status mc_sor_sweep(const lgx_colouring &c, const VT *val, double relax, int forward,
                         int ultra, const XT *b, XT *x, cudaStream_t s, int from_zero,
-                        const float *scale) {
+                        const float *scale, XT *r_last, int64_t *res_from) {
+  if (res_from) *res_from = c.n;
   const Csr &p = c.pcsr;
   SorOp<VT, XT> op{b, x, (XT)relax, XT(1) - (XT)relax, ultra};
   op.scale = scale;
@@ -549,10 +550,18 @@ lgx_status mc_sor_sweep(const lgx_colouring &c, const VT *val, double relax, int
       continue;
     }
     op.visit_end = rb;  // forward: exactly the rows before this colour are visited
+    // the last colour of a forward sweep on grid rows can also leave its
+    // rows' residuals in r_last
+    const bool with_res = r_last && res_from && forward && k == c.ncolours - 1 && re > rb &&
+                          !kIsBf16<VT> && sizeof(XT) == 4 && grid_sweep_residual(p);
     bool done = false;
     LGX_CHECK((grid_sor_rows<VT, XT>(p, val, rb, re, b, x, relax, ultra, op.rdiag, op.relax_one,
-                                     op.from_zero, op.visit_end, scale, s, &done)));
-    if (done) continue;
+                                     op.from_zero, op.visit_end, scale, s, &done,
+                                     with_res ? r_last : nullptr)));
+    if (done) {
+      if (with_res) *res_from = rb;
+      continue;
+    }
     LGX_CHECK(launch_rows<VT>(rb, re, p, val, op, s));
   }
   return LGX_OK;
@@ -560,16 +569,17 @@ lgx_status mc_sor_sweep(const lgx_colouring &c, const VT *val, double relax, int
 
 template lgx_status mc_sor_sweep<double, double>(const lgx_colouring &, const double *, double,
                                                  int, int, const double *, double *,
-                                                 cudaStream_t, int, const float *);
+                                                 cudaStream_t, int, const float *, double *,
+                                                 int64_t *);
 template lgx_status mc_sor_sweep<float, double>(const lgx_colouring &, const float *, double, int,
                                                 int, const double *, double *, cudaStream_t, int,
-                                                const float *);
+                                                const float *, double *, int64_t *);
 template lgx_status mc_sor_sweep<float, float>(const lgx_colouring &, const float *, double, int,
                                                int, const float *, float *, cudaStream_t, int,
-                                               const float *);
+                                               const float *, float *, int64_t *);
 template lgx_status mc_sor_sweep<bf16, float>(const lgx_colouring &, const bf16 *, double, int,
                                               int, const float *, float *, cudaStream_t, int,
-                                              const float *);
+                                              const float *, float *, int64_t *);
 
 lgx_status jacobi_csr(const Csr &a, double relax, const double *x_in, double *x_out,
                       const double *b, cudaStream_t s) {

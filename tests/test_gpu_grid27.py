@@ -193,6 +193,33 @@ def test_grid7_pcg_equals_csr(cuda, form):
     np.testing.assert_array_equal(rg.x.cpu().numpy(), rc.x.cpu().numpy())
 
 
+# A red-black sweep's second colour also writes its rows' residuals (the
+# V-cycle's residual pass then covers the first colour only): at sizes with
+# the value-staged float kernels and every cycle form, against the CSR path
+# (one residual pass over all rows), bit for bit.
+@pytest.mark.parametrize("dims", [(48, 48, 48), (33, 40, 26)])
+def test_grid7_sweep_residual_equals_csr(cuda, dims):
+    m = cuda.gen_7pt(dims, np.exp(3.0 * np.random.default_rng(21).standard_normal(
+        int(np.prod(dims)))))
+    col = cuda.Colouring.from_array(m, _red_black(dims), 2)
+    bb = np.random.default_rng(22).uniform(-1, 1, m.row_num())
+    for form in ("fp64", "f32", "f32_coarse"):
+        kw = FORMS[form]
+        hg = cuda.HierarchyWright(grid27=True, **PARAMS, **kw).instantiate(
+            m, finest_colouring=col)
+        hc = cuda.HierarchyWright(grid27=False, **PARAMS, **kw).instantiate(
+            m, finest_colouring=col)
+        assert hg.grid27_active() and not hc.grid27_active()
+        np.testing.assert_array_equal(hg.vcycle(bb).cpu().numpy(), hc.vcycle(bb).cpu().numpy())
+        solves = [dict()] if form == "fp64" else [dict(flexible=True), dict(refine=2),
+                                                   dict(refine=2, flexible=True)]
+        for skw in solves:
+            rg = cuda.pcg(m, bb, precon=cuda.PRECON_AMG, amg=hg, rtol=1e-10, maxit=500, **skw)
+            rc = cuda.pcg(m, bb, precon=cuda.PRECON_AMG, amg=hc, rtol=1e-10, maxit=500, **skw)
+            assert rg.iterations == rc.iterations
+            np.testing.assert_array_equal(rg.x.cpu().numpy(), rc.x.cpu().numpy())
+
+
 def test_grid7_stays_off_without_the_structure(cuda):
     dims = (6, 8, 10)
     # odd n2, a 27-point matrix declared as 7-point, a parity (8-colour)
