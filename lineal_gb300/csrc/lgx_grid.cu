@@ -210,7 +210,30 @@ struct G27Sor {
   int ultra, relax_one, from_zero;
   int64_t visit_end;
   const double *rdiag;
+  // sweep from zero: bit e set when the neighbour at offset e lies in a
+  // colour the sweep has not visited yet (it reads as 0 and is not loaded);
+  // the same for every row of a colour launch (g27_unvisited)
+  uint32_t fz_mask = 0;
 };
+
+// The offsets whose neighbours lie in colours after colour c: the parity
+// colouring c = 4 (i & 1) + 2 (j & 1) + (k & 1) gives the neighbour at
+// (dz, dy, dx) the colour c ^ (4 [dz != 0] + 2 [dy != 0] + [dx != 0]); the
+// red-black colouring gives every neighbour the other colour.  Colours
+// occupy consecutive row blocks, so "a later colour" is "a row at or past
+// the launch's first row", the test a forward sweep from zero makes.
+template <int PTS>
+static uint32_t g27_unvisited(int c) {
+  uint32_t m = 0;
+  for (int e = 0; e < PTS; ++e) {
+    if (e == g_diag<PTS>()) continue;
+    const int nc = PTS == 27 ? c ^ (4 * (g_dz<PTS>(e) != 0) + 2 * (g_dy<PTS>(e) != 0) +
+                                    (g_dx<PTS>(e) != 0))
+                             : 1 - c;
+    if (nc > c) m |= 1u << e;
+  }
+  return m;
+}
 
 // Loads through the non-coherent path as volatile asm, which the compiler
 // does not sink into the branches that use them: every load of a round is
@@ -329,8 +352,9 @@ struct G27Row {
 template <typename XT, int MODE, int PTS>
 __device__ __forceinline__ XT g27_x(const XT *x, int64_t c, int e, const G27Sor &so) {
   if (g_sor_mode<MODE>() && e == g_diag<PTS>()) return XT(0);
+  // the load stays unconditional (a round's loads go out together)
   const XT xl = g27_ld(x + c);
-  return (g_sor_mode<MODE>() && so.from_zero && c >= so.visit_end) ? XT(0) : xl;
+  return (g_sor_mode<MODE>() && ((so.fz_mask >> e) & 1u)) ? XT(0) : xl;
 }
 
 // one row per thread
@@ -534,24 +558,20 @@ __global__ void __launch_bounds__(g_rows_per_cta<T>(), g_ctas_per_sm<T, PTS>())
     if (sides == 0x3Fu) {
 #pragma unroll
       for (int e = 0; e < PTS; ++e) {
-        if (g_sor_mode<MODE>() && e == kDiag) {
+        if ((g_sor_mode<MODE>() && e == kDiag) || (FZ && ((so.fz_mask >> e) & 1u))) {
           xv[e] = T(0);
           continue;
         }
-        const int64_t nb = g_nb<PTS>(g, cell, r, e);
-        const T xl = g27_ld(x + nb);
-        xv[e] = (FZ && nb >= so.visit_end) ? T(0) : xl;
+        xv[e] = g27_ld(x + g_nb<PTS>(g, cell, r, e));
       }
     } else {
 #pragma unroll
       for (int e = 0; e < PTS; ++e) {
-        if (g_sor_mode<MODE>() && e == kDiag) {
+        if ((g_sor_mode<MODE>() && e == kDiag) || (FZ && ((so.fz_mask >> e) & 1u))) {
           xv[e] = T(0);
           continue;
         }
-        const int64_t nb = g_in<PTS>(sides, e) ? g_nb<PTS>(g, cell, r, e) : r;
-        const T xl = g27_ld(x + nb);
-        xv[e] = (FZ && nb >= so.visit_end) ? T(0) : xl;
+        xv[e] = g27_ld(x + (g_in<PTS>(sides, e) ? g_nb<PTS>(g, cell, r, e) : r));
       }
     }
   }
@@ -764,6 +784,15 @@ lgx_status grid_sor_rows(const Csr &a, const VT *val, int64_t rb, int64_t re, co
   G27Sor so{relax, 1.0 - relax, ultra, relax_one, from_zero, visit_end, rdiag};
   // the float SOR of SorOp forms XT(1) - XT(relax): the same in XT
   so.m1 = (double)((XT)1 - (XT)relax);
+  // a forward sweep from zero visits the colours in order: the rows before
+  // rb (= visit_end, a colour's first row) are visited, the others read 0
+  if (from_zero) {
+    const Grid27 &gr = *a.grid;
+    if (rb != visit_end || rb % gr.block || re - rb > gr.block)
+      return fail(LGX_ERR_INVALID, "grid sweep from zero: rows are not one colour's block");
+    const int c = (int)(rb / gr.block);
+    so.fz_mask = gr.points == 27 ? g27_unvisited<27>(c) : g27_unvisited<7>(c);
+  }
   if constexpr (!kIsBf16<VT> && sizeof(XT) == 4) {
     if (r_out) {
       LGX_CHECK((launch_g27<VT, XT, 4>(*a.grid, v, rb, re, b, x, r_out, scale, so, s)));
