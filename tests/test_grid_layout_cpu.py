@@ -79,3 +79,60 @@ def test_red_black_7pt_neighbours(dims):
         for cc in cols:
             off = (int(i[cc] - i[r]), int(j[cc] - j[r]), int(k[cc] - k[r]))
             assert new[cc] == want[off]
+
+
+def _unvisited27(c):
+    """g27_unvisited<27>: offsets whose neighbours lie in colours after c"""
+    m = 0
+    for e in range(27):
+        if e == 13:
+            continue
+        dz, dy, dx = e // 9 - 1, (e // 3) % 3 - 1, e % 3 - 1
+        if c ^ (4 * (dz != 0) + 2 * (dy != 0) + (dx != 0)) > c:
+            m |= 1 << e
+    return m
+
+
+def _unvisited7(c):
+    """g27_unvisited<7>: every off-diagonal offset for colour 0, none for 1"""
+    return sum(1 << e for e in range(7) if e != 3 and 1 - c > c)
+
+
+@pytest.mark.parametrize("dims", [(2, 2, 2), (4, 6, 8), (6, 4, 10)])
+def test_unvisited_masks_match_row_order_27pt(dims):
+    """A forward sweep from zero reads a neighbour as 0 when its row sits at
+    or past the first row of the launch's colour; the grid kernels test the
+    per-colour offset mask instead.  Both agree on every in-grid entry."""
+    n = int(np.prod(dims))
+    a = lo.gen_27pt(dims, np.ones(n))
+    i, j, k = np.unravel_index(np.arange(n), dims)
+    colour = 4 * (i & 1) + 2 * (j & 1) + (k & 1)
+    new = _colour_order(colour)
+    block = n // 8
+    for r in range(n):
+        c = int(colour[r])
+        m = _unvisited27(c)
+        for cc in a.col[a.rowptr[r]:a.rowptr[r + 1]]:
+            if cc == r:
+                continue
+            e = (i[cc] - i[r] + 1) * 9 + (j[cc] - j[r] + 1) * 3 + (k[cc] - k[r] + 1)
+            assert bool((m >> e) & 1) == (new[cc] >= c * block)
+
+
+@pytest.mark.parametrize("dims", [(3, 5, 4), (4, 3, 6), (2, 2, 2)])
+def test_unvisited_masks_match_row_order_7pt(dims):
+    n = int(np.prod(dims))
+    a = lo.gen_7pt(dims, np.ones(n))
+    i, j, k = np.unravel_index(np.arange(n), dims)
+    colour = (i + j + k) & 1
+    new = _colour_order(colour)
+    block = n // 2
+    offsets = [(-1, 0, 0), (0, -1, 0), (0, 0, -1), (0, 0, 0), (0, 0, 1), (0, 1, 0), (1, 0, 0)]
+    for r in range(n):
+        c = int(colour[r])
+        m = _unvisited7(c)
+        for cc in a.col[a.rowptr[r]:a.rowptr[r + 1]]:
+            if cc == r:
+                continue
+            e = offsets.index((int(i[cc] - i[r]), int(j[cc] - j[r]), int(k[cc] - k[r])))
+            assert bool((m >> e) & 1) == (new[cc] >= c * block)
